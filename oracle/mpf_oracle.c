@@ -1,0 +1,756 @@
+/* CPU oracle: plain-C restatement of the reference photon-propagation path.
+ * TEST INFRASTRUCTURE ONLY (see mpf_oracle.h).  Build with -ffp-contract=off.
+ *
+ * Sources restated (reference paths):
+ *   keys             src/magrathea/simplehyperoctreeindex.h:572-575 (level),
+ *                    :679-694 (parent/child), :888-893 (center),
+ *                    :950-955 (extent), :997-1001 (containing),
+ *                    :1165-1189 (compute/cipher)
+ *   locate           src/magrathea/simplehyperoctree.h:874-899
+ *   cic              src/magrathea/simplehyperoctree.h:1410-1469
+ *   tsc (cached)     src/magrathea/simplehyperoctree.h:1552-1644
+ *   mac              src/magrathea/simplehyperoctree.h:1905-1910
+ *   interpolate      src/utility.h:441-449
+ *   launch (6 args)  src/integrator.h:283-309
+ *   dphotondl        src/integrator.h:409-445
+ *   integrate (stop) src/integrator.h:648-824
+ *   Jacobian         src/lensing.h:399-472
+ *   plane crossings  src/hmaps.h:612-676 (per-surface interpolation)
+ */
+#include "mpf_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef unsigned __int128 u128;
+
+#define OCT_EXTENT 4
+#define LEVEL_SHIFT 2  /* log2(EXTENT) */
+
+static const double C_LIGHT = 299792458.0;
+
+static inline u128 mk(uint64_t hi, uint64_t lo) { return ((u128)hi << 64) | lo; }
+static inline u128 markers(void) { return mk(0x8888888888888888ULL, 0x8888888888888888ULL); }
+static inline u128 invalid_key(void) { return (((u128)1) << 127) - 1; }
+
+static inline unsigned ctz128(u128 m)
+{
+    const uint64_t lo = (uint64_t)m;
+    if (lo) return (unsigned)__builtin_ctzll(lo);
+    const uint64_t hi = (uint64_t)(m >> 64);
+    return hi ? 64u + (unsigned)__builtin_ctzll(hi) : 128u;
+}
+
+static inline unsigned key_level(u128 k)
+{
+    const u128 m = k & markers();
+    const unsigned tz = m ? ctz128(m) : 128u;
+    return (128u - tz) / 4u + (k != 0);
+}
+
+static inline int key_containing(u128 a, u128 b)
+{
+    const u128 x = a ^ b;
+    return ((~markers() & x) <= (markers() & x)) && (a <= b);
+}
+
+static inline u128 key_parent(u128 k)
+{
+    const unsigned loc = 132u - key_level(k) * 4u;
+    const u128 mask = (loc < 128u) ? (~(u128)0) << loc : (u128)0;
+    return k & mask;
+}
+
+static inline u128 key_child(u128 k, unsigned site)
+{
+    const unsigned l = key_level(k);
+    if (l >= 32u) return k;
+    return k | ((u128)((site & 7u) | 8u) << (128u - (l + 1u) * 4u));
+}
+
+static inline uint64_t axis_coord(unsigned level, double x)
+{
+    const double scale = (1.0 / (double)OCT_EXTENT) * (double)(((u128)1) << level);
+    const double v = scale * (x - (-(double)OCT_EXTENT / 2.0));
+    uint64_t c;
+    if (!(v > 0.0)) c = 0;                         /* reference: undefined for v < 0 */
+    else if (v >= 18446744073709551616.0) c = ~0ULL;
+    else c = (uint64_t)v;
+    return (level >= 64) ? c : (c & ((1ULL << level) - 1ULL));
+}
+
+static inline u128 key_compute(unsigned level, double x, double y, double z)
+{
+    if (level == 0) return 0;
+    const uint64_t cx = axis_coord(level, x), cy = axis_coord(level, y), cz = axis_coord(level, z);
+    u128 k = 0;
+    for (unsigned i = 1; i <= level; ++i) {
+        const unsigned b = level - i;
+        const unsigned nib = 8u | (unsigned)(((cz >> b) & 1u) << 2) | (unsigned)(((cy >> b) & 1u) << 1) | (unsigned)((cx >> b) & 1u);
+        k |= (u128)nib << (128u - 4u * i);
+    }
+    return k;
+}
+
+static inline double key_center(u128 k, unsigned dim)
+{
+    const unsigned l = key_level(k);
+    uint64_t c = 0;
+    for (unsigned i = 0; i < 32u; ++i) c |= (uint64_t)((k >> (128u - 4u * (i + 1u) + dim)) & 1u) << (31u - i);
+    c >>= (32u - l);
+    return (-(double)OCT_EXTENT / 2.0) +
+           ((double)OCT_EXTENT * ((double)(2 * (u128)c + 1) / (double)(((u128)1) << (l + 1u))));
+}
+
+/* extent() with the default unit extent: 1 / 2^level */
+static inline double key_extent1(u128 k) { return 1.0 / (1.0 * (double)(((u128)1) << key_level(k))); }
+/* extent<double, ratio<0>, ratio<EXTENT>>(): EXTENT / 2^level */
+static inline double key_extent4(u128 k) { return (double)OCT_EXTENT / (1.0 * (double)(((u128)1) << key_level(k))); }
+
+static inline u128 tkey(const mpfo_tree* T, int64_t i) { return mk(T->keys[2 * i], T->keys[2 * i + 1]); }
+
+/* Number of keys <= K (std::upper_bound position). */
+static inline int64_t upper(const mpfo_tree* T, u128 K)
+{
+    int64_t first = 0, count = T->n;
+    while (count > 0) {
+        const int64_t step = count / 2, it = first + step;
+        if (!(K < tkey(T, it))) { first = it + 1; count -= step + 1; }
+        else count = step;
+    }
+    return first;
+}
+
+/* The reference's lookup: the last key <= K if it contains K, else -1. */
+static inline int64_t find(const mpfo_tree* T, u128 K)
+{
+    if (T->n <= 0) return -1;
+    const int64_t m = upper(T, K);
+    return (m > 0 && key_containing(tkey(T, m - 1), K)) ? m - 1 : -1;
+}
+
+int64_t mpfo_locate(const mpfo_tree* T, double x, double y, double z)
+{
+    return find(T, key_compute(32, x, y, z));
+}
+
+void mpfo_key_compute(unsigned level, double x, double y, double z, uint64_t* out)
+{
+    const u128 k = key_compute(level, x, y, z);
+    out[0] = (uint64_t)(k >> 64);
+    out[1] = (uint64_t)k;
+}
+
+unsigned mpfo_key_level(uint64_t hi, uint64_t lo) { return key_level(mk(hi, lo)); }
+
+static inline void mac7(float* acc, const float* f, double w)
+{
+    for (int k = 0; k < 7; ++k) acc[k] = (float)((double)acc[k] + (double)f[k] * w);
+}
+
+static inline void zero7(float* a) { for (int k = 0; k < 7; ++k) a[k] = 0.0f; }
+
+static inline int empty7(const float* a)
+{
+    for (int k = 0; k < 7; ++k) if (a[k] != 0.0f) return 0;
+    return 1;
+}
+
+void mpfo_cic(const mpfo_tree* T, double x, double y, double z, float* res)
+{
+    const double pt[3] = {x, y, z};
+    u128 ekey = key_compute(32, x, y, z);
+    const int64_t f0 = find(T, ekey);
+    u128 idx = (f0 >= 0) ? tkey(T, f0) : invalid_key();
+    unsigned ilvl = key_level(idx), lvl = ilvl;
+    double half = (double)OCT_EXTENT / 1.0 * key_extent1(idx) / 2.0;
+    unsigned site = 0;
+    zero7(res);
+    do {
+        ilvl = lvl;
+        if (idx != invalid_key()) {
+            double dist[3];
+            for (int d = 0; d < 3; ++d) dist[d] = fabs((key_center(idx, d) - pt[d]) / (half + half));
+            for (unsigned s = 0; s < 8u; ++s)
+                if (key_containing(key_child(idx, s), ekey)) { site = s; break; }
+            for (unsigned v = 0; v < 8u; ++v) {
+                double w = 1.0, vert[3];
+                const unsigned diff = site ^ v;
+                for (int d = 0; d < 3; ++d) {
+                    const int b = (v >> d) & 1u, db = (diff >> d) & 1u;
+                    vert[d] = pt[d] + ((double)b * half) - ((double)(!b) * half);
+                    w *= ((double)db * (1.0 - dist[d])) + ((double)(!db) * dist[d]);
+                }
+                ekey = key_compute(ilvl, vert[0], vert[1], vert[2]);
+                const int64_t fi = find(T, ekey);
+                if (fi >= 0) {
+                    const unsigned fl = key_level(tkey(T, fi));
+                    if (fl < lvl) lvl = fl;
+                    mac7(res, T->fields + 7 * fi, w);
+                } else {
+                    zero7(res);
+                    break;
+                }
+            }
+        }
+        if (lvl < ilvl) {
+            ekey = key_compute(lvl + 1, x, y, z);
+            idx = key_parent(ekey);
+            zero7(res);
+            half = (double)OCT_EXTENT / 1.0 * key_extent1(idx) / 2.0;
+        }
+    } while (lvl < ilvl);
+}
+
+typedef struct {
+    u128 key[27];
+    float f[27][7];
+} tsc_cache;
+
+static inline void cache_init(tsc_cache* c) { memset(c, 0, sizeof(*c)); }
+
+static inline double tsc_w(int a, double d)
+{
+    return (double)a * 0.5 * (1.5 - d) * (1.5 - d) + (double)(1 - a) * (0.75 - d * d);
+}
+
+static void tsc_cached(const mpfo_tree* T, tsc_cache* cache, double x, double y, double z, float* res)
+{
+    const double pt[3] = {x, y, z};
+    u128 ekey = key_compute(32, x, y, z);
+    const int64_t f0 = find(T, ekey);
+    u128 idx = (f0 >= 0) ? tkey(T, f0) : invalid_key();
+    unsigned ilvl = key_level(idx), lvl = ilvl;
+    double half = (double)OCT_EXTENT / 1.0 * key_extent1(idx) / 2.0;
+    zero7(res);
+    if (x == 0.0 && y == 0.0 && z == 0.0) {
+        mpfo_cic(T, 0., 0., 0., res);
+        return;
+    }
+    tsc_cache tmp;
+    do {
+        ilvl = lvl;
+        const double tw = 2.0 * half;
+        if (cache->key[13] == idx) {
+            int ic = 0;
+            for (int ix = -1; ix <= 1; ++ix)
+                for (int iy = -1; iy <= 1; ++iy)
+                    for (int iz = -1; iz <= 1; ++iz) {
+                        double dist[3];
+                        for (int d = 0; d < 3; ++d) dist[d] = fabs((key_center(cache->key[ic], d) - pt[d]) / tw);
+                        const double w = tsc_w(abs(ix), dist[0]) * tsc_w(abs(iy), dist[1]) * tsc_w(abs(iz), dist[2]);
+                        mac7(res, cache->f[ic], w);
+                        ++ic;
+                    }
+            return;
+        } else if (idx != invalid_key()) {
+            int ic = 0, stop = 0;
+            for (int ix = -1; ix <= 1 && !stop; ++ix)
+                for (int iy = -1; iy <= 1 && !stop; ++iy)
+                    for (int iz = -1; iz <= 1 && !stop; ++iz) {
+                        ekey = key_compute(ilvl, pt[0] + ix * tw, pt[1] + iy * tw, pt[2] + iz * tw);
+                        const int64_t fi = find(T, ekey);
+                        if (fi >= 0) {
+                            tmp.key[ic] = tkey(T, fi);
+                            memcpy(tmp.f[ic], T->fields + 7 * fi, sizeof(tmp.f[ic]));
+                            double dist[3];
+                            for (int d = 0; d < 3; ++d) dist[d] = fabs((key_center(ekey, d) - pt[d]) / tw);
+                            const double w = tsc_w(abs(ix), dist[0]) * tsc_w(abs(iy), dist[1]) * tsc_w(abs(iz), dist[2]);
+                            const unsigned fl = key_level(tmp.key[ic]);
+                            if (fl < lvl) lvl = fl;
+                            if (lvl < ilvl) { zero7(res); stop = 1; }
+                            else { mac7(res, tmp.f[ic], w); ++ic; }
+                        } else {
+                            zero7(res);
+                            stop = 1;
+                        }
+                    }
+            if (ic == 27) *cache = tmp;
+        }
+        if (lvl < ilvl) {
+            ekey = key_compute(lvl + 1, x, y, z);
+            idx = key_parent(ekey);
+            zero7(res);
+            half = (double)OCT_EXTENT / 1.0 * key_extent1(idx) / 2.0;
+        }
+    } while (lvl < ilvl);
+}
+
+void mpfo_tsc(const mpfo_tree* T, double x, double y, double z, float* out)
+{
+    tsc_cache c;
+    cache_init(&c);
+    tsc_cached(T, &c, x, y, z, out);
+}
+
+double mpfo_interpolate(double x0, const double* x, const double* y, int64_t n)
+{
+    int64_t first = 0, count = n;
+    while (count > 0) {
+        const int64_t step = count / 2, it = first + step;
+        if (!(x0 < x[it])) { first = it + 1; count -= step + 1; }
+        else count = step;
+    }
+    int64_t i = first;
+    i += (n > 1) * ((i <= 0) - (i >= n));
+    return (n > 1) ? (y[i - 1] + ((y[i] - y[i - 1]) * (x0 - x[i - 1]) / (x[i] - x[i - 1]))) : ((n > 0) ? y[0] : 0.0);
+}
+
+/* ---------------------------------------------------------------------- */
+/* integrator                                                              */
+/* ---------------------------------------------------------------------- */
+enum { PA = 0, PT, PX, PY, PZ, PK0, PK1, PK2, PK3, PLEVEL, PAH, PRHO, PPHI, PDX, PDY, PDZ, PDT, PDL, PLAP, PZRED,
+       PDS2, PERR, PISW, PISWOLD, PCHI, PLAMBDA, PS, PINDEX };
+
+typedef struct {
+    const mpfo_tree* T;
+    const mpfo_cosmo* C;
+    int order;
+    double length;
+    tsc_cache cache;
+} ctx_t;
+
+static inline void gather(ctx_t* c, double x, double y, double z, float* d)
+{
+    if (c->order == 1) mpfo_cic(c->T, x, y, z, d);
+    else tsc_cached(c->T, &c->cache, x, y, z, d);
+}
+
+/* field indices in the 7-float record */
+enum { FRHO = 0, FPHI, FDX, FDY, FDZ, FA, FDT };
+
+static void dphotondl(ctx_t* c, double* out, const double* in)
+{
+    const double two = 2.0;
+    const double c2 = C_LIGHT * C_LIGHT;
+    float d[7];
+    gather(c, in[PX], in[PY], in[PZ], d);
+    const double dphidl = (double)d[FDT] * in[PK0] + ((double)d[FDX] * in[PK1] + (double)d[FDY] * in[PK2] + (double)d[FDZ] * in[PK3]);
+    const double dadt = mpfo_interpolate(in[PT], c->C->t, c->C->dadt, c->C->n);
+    const double scale = c->length;
+    out[PA] = in[PK0] * dadt;
+    out[PT] = in[PK0];
+    out[PX] = in[PK1] / scale;
+    out[PY] = in[PK2] / scale;
+    out[PZ] = in[PK3] / scale;
+    out[PK0] = -(two * dadt / in[PA] * in[PK0] * in[PK0]) - (two / c2 * in[PK0]) * (dphidl - (double)d[FDT] * in[PK0]);
+    out[PK1] = -(two * dadt / in[PA] * in[PK0] * in[PK1]) + (two / c2 * dphidl * in[PK1]) - (two * (double)d[FDX] * in[PK0] * in[PK0]);
+    out[PK2] = -(two * dadt / in[PA] * in[PK0] * in[PK2]) + (two / c2 * dphidl * in[PK2]) - (two * (double)d[FDY] * in[PK0] * in[PK0]);
+    out[PK3] = -(two * dadt / in[PA] * in[PK0] * in[PK3]) + (two / c2 * dphidl * in[PK3]) - (two * (double)d[FDZ] * in[PK0] * in[PK0]);
+}
+
+typedef struct {
+    double* p;
+    int64_t n, cap;
+} traj_t;
+
+static double* traj_push(traj_t* t)
+{
+    if (t->n == t->cap) {
+        t->cap = t->cap ? 2 * t->cap : 256;
+        t->p = (double*)realloc(t->p, (size_t)t->cap * MPFO_PHOTON * sizeof(double));
+    }
+    return t->p + MPFO_PHOTON * (t->n++);
+}
+
+static int stop_reached(int kind, double ref, const double* back, const double* photon, const double* ki)
+{
+    switch (kind) {
+    case MPFO_STOP_R: return back[PCHI] > ref;
+    case MPFO_STOP_LAMBDA: return back[PLAMBDA] > ref;
+    case MPFO_STOP_REDSHIFT: return back[PZRED] > ref;
+    case MPFO_STOP_T: return back[PT] > ref;
+    case MPFO_STOP_A: return back[PA] < ref;
+    case MPFO_STOP_PLANE: return (photon[PX] * ki[0] + photon[PY] * ki[1] + photon[PZ] * ki[2]) > ref;
+    case MPFO_STOP_S: return back[PS] > ref;
+    default: return 1;
+    }
+}
+
+/* integrate() with a stop criterion; the trajectory grows in *tr. */
+static void integrate(ctx_t* c, traj_t* tr, unsigned nsteps, int stop_kind, double stop_ref, const double* ki)
+{
+    const double zero = 0.0, one = 1.0, two = 2.0, six = 6.0;
+    const double cl = C_LIGHT, c2 = C_LIGHT * C_LIGHT;
+    const double mn = 0.0 - (double)OCT_EXTENT / two, mx = 0.0 + (double)OCT_EXTENT / two;
+    const double scale = c->length;
+    float data[7];
+    double* b = tr->p + MPFO_PHOTON * (tr->n - 1);
+    gather(c, b[PX], b[PY], b[PZ], data);
+    const double norm = sqrt((c2 * (one + two * ((double)data[FPHI] / c2)) * b[PK0] * b[PK0]) /
+                             ((one - two * ((double)data[FPHI] / c2)) * (b[PK1] * b[PK1] + b[PK2] * b[PK2] + b[PK3] * b[PK3])));
+    b[PK1] *= norm;
+    b[PK2] *= norm;
+    b[PK3] *= norm;
+    b[PA] = mpfo_interpolate(b[PT], c->C->t, c->C->a, c->C->n);
+    int64_t loc = mpfo_locate(c->T, b[PX], b[PY], b[PZ]);
+    b[PLEVEL] = (loc >= 0) ? (double)key_level(tkey(c->T, loc)) : 0.0;
+    b[PAH] = zero;
+    b[PRHO] = data[FRHO];
+    b[PPHI] = data[FPHI];
+    b[PDX] = data[FDX];
+    b[PDY] = data[FDY];
+    b[PDZ] = data[FDZ];
+    b[PDT] = data[FDT];
+    b[PDL] = zero;
+    b[PLAP] = zero;
+    b[PZRED] = zero;
+    b[PDS2] = (b[PA] * b[PA]) * (-(c2 * (one + two * (b[PPHI] / c2)) * b[PK0] * b[PK0]) +
+                                 ((one - two * (b[PPHI] / c2)) * (b[PK1] * b[PK1] + b[PK2] * b[PK2] + b[PK3] * b[PK3])));
+    b[PERR] = one - ((one - two * (b[PPHI] / c2)) * (b[PK1] * b[PK1] + b[PK2] * b[PK2] + b[PK3] * b[PK3])) /
+                        (c2 * (one + two * (b[PPHI] / c2)) * b[PK0] * b[PK0]);
+    b[PISW] = zero;
+    b[PCHI] = zero;
+    b[PISWOLD] = zero;
+    b[PLAMBDA] = zero;
+    b[PS] = zero;
+    double ratio = b[PA] * b[PA] * (scale / cl) / nsteps;
+    double dl = (loc >= 0 ? key_extent4(tkey(c->T, loc)) : 0.0) * ratio;
+    const double a0 = b[PA];
+    const double phi0c2 = b[PPHI] / c2;
+    double photon[MPFO_PHOTON];
+    memset(photon, 0, sizeof(photon));
+    double dcore[4][9];
+    while (!empty7(data)) {
+        b = tr->p + MPFO_PHOTON * (tr->n - 1);
+        photon[PINDEX] = b[PINDEX] + one;
+        dphotondl(c, dcore[0], b);
+        for (int i = 0; i < 9; ++i) photon[i] = b[i] + dl / two * dcore[0][i];
+        dphotondl(c, dcore[1], photon);
+        for (int i = 0; i < 9; ++i) photon[i] = b[i] + dl / two * dcore[1][i];
+        dphotondl(c, dcore[2], photon);
+        for (int i = 0; i < 9; ++i) photon[i] = b[i] + dl * dcore[2][i];
+        dphotondl(c, dcore[3], photon);
+        for (int i = 0; i < 9; ++i)
+            photon[i] = b[i] + (dl / six) * (dcore[0][i] + two * dcore[1][i] + two * dcore[2][i] + dcore[3][i]);
+        gather(c, photon[PX], photon[PY], photon[PZ], data);
+        if (!(!(photon[PA] < zero) && ((photon[PX] > mn) && (photon[PX] < mx) && (photon[PY] > mn) &&
+                                       (photon[PY] < mx) && (photon[PZ] > mn) && (photon[PZ] < mx))))
+            zero7(data);
+        loc = mpfo_locate(c->T, photon[PX], photon[PY], photon[PZ]);
+        photon[PLEVEL] = (loc >= 0) ? (double)key_level(tkey(c->T, loc)) : 0.0;
+        photon[PAH] = data[FA];
+        photon[PRHO] = data[FRHO];
+        photon[PPHI] = data[FPHI];
+        photon[PDX] = data[FDX];
+        photon[PDY] = data[FDY];
+        photon[PDZ] = data[FDZ];
+        photon[PDT] = -(double)data[FDT];
+        photon[PDL] = (double)data[FDT] * photon[PK0] + (photon[PDX] * photon[PK1] + photon[PDY] * photon[PK2] + photon[PDZ] * photon[PK3]);
+        photon[PLAP] = ((double)data[FPHI] - b[PPHI]) / dl;
+        photon[PDS2] = (photon[PA] * photon[PA]) * ((-c2 * (one + two * (photon[PPHI] / c2)) * photon[PK0] * photon[PK0]) +
+                                                    ((one - two * (photon[PPHI] / c2)) * (photon[PK1] * photon[PK1] + photon[PK2] * photon[PK2] + photon[PK3] * photon[PK3])));
+        photon[PERR] = one - ((one - two * (photon[PPHI] / c2)) * (photon[PK1] * photon[PK1] + photon[PK2] * photon[PK2] + photon[PK3] * photon[PK3])) /
+                                 (c2 * (one + two * (photon[PPHI] / c2)) * photon[PK0] * photon[PK0]);
+        photon[PISW] += (b[PDT] + photon[PDT]) * (photon[PT] - b[PT]) / c2;
+        photon[PISWOLD] -= 2 * (photon[PPHI] - b[PPHI]) / c2 -
+                           ((b[PDX] + photon[PDX]) * (photon[PX] - b[PX]) * scale + (b[PDY] + photon[PDY]) * (photon[PY] - b[PY]) * scale +
+                            (b[PDZ] + photon[PDZ]) * (photon[PZ] - b[PZ]) * scale) / c2;
+        photon[PCHI] = sqrt(photon[PX] * photon[PX] + photon[PY] * photon[PY] + photon[PZ] * photon[PZ]);
+        photon[PLAMBDA] += dl;
+        photon[PS] += sqrt((photon[PX] - b[PX]) * (photon[PX] - b[PX]) + (photon[PY] - b[PY]) * (photon[PY] - b[PY]) +
+                           (photon[PZ] - b[PZ]) * (photon[PZ] - b[PZ]));
+        photon[PZRED] = a0 / photon[PA] * (one + phi0c2 - photon[PPHI] / c2) - one;
+        if (!empty7(data)) {
+            ratio = photon[PA] * photon[PA] * (scale / cl) / nsteps;
+            dl = (loc >= 0 ? key_extent4(tkey(c->T, loc)) : 0.0) * ratio;
+            double* dst = traj_push(tr);
+            memcpy(dst, photon, sizeof(photon));
+        }
+        b = tr->p + MPFO_PHOTON * (tr->n - 1);
+        if (stop_reached(stop_kind, stop_ref, b, photon, ki)) break;
+    }
+    if (tr->n > 0) {
+        b = tr->p + MPFO_PHOTON * (tr->n - 1);
+        if (signbit(b[PZRED]) || signbit(b[PA])) tr->n--;
+    }
+}
+
+static void launch6(const double* L, double* p)
+{
+    memset(p, 0, MPFO_PHOTON * sizeof(double));
+    const double norm = sqrt((L[3] - L[0]) * (L[3] - L[0]) + (L[4] - L[1]) * (L[4] - L[1]) + (L[5] - L[2]) * (L[5] - L[2]));
+    p[PA] = 1.0;
+    p[PT] = 0.0;
+    p[PX] = L[0];
+    p[PY] = L[1];
+    p[PZ] = L[2];
+    p[PK0] = 1.0;
+    p[PK1] = (L[3] - L[0]) / norm;
+    p[PK2] = (L[4] - L[1]) / norm;
+    p[PK3] = (L[5] - L[2]) / norm;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Jacobian and planes                                                     */
+/* ---------------------------------------------------------------------- */
+static int64_t upper_by(const traj_t* tr, int q, double v, int descending)
+{
+    int64_t first = 0, count = tr->n;
+    while (count > 0) {
+        const int64_t step = count / 2, it = first + step;
+        const double e = tr->p[MPFO_PHOTON * it + q];
+        const int less = descending ? (v > e) : (v < e);
+        if (!less) { first = it + 1; count -= step + 1; }
+        else count = step;
+    }
+    return first;
+}
+
+static void jacobian(ctx_t* c, const traj_t* tr, int nd, const double* dist, double* A /* nd x 3 */)
+{
+    const double c2 = C_LIGHT * C_LIGHT;
+    double* a11 = (double*)calloc((size_t)nd * (size_t)tr->n, sizeof(double));
+    double* a12 = (double*)calloc((size_t)nd * (size_t)tr->n, sizeof(double));
+    double* a22 = (double*)calloc((size_t)nd * (size_t)tr->n, sizeof(double));
+    tsc_cache cache;
+    cache_init(&cache);
+    for (int64_t i = 1; i < tr->n; ++i) {
+        const double* P = tr->p + MPFO_PHOTON * i;
+        const double* Q = tr->p + MPFO_PHOTON * (i - 1);
+        const double x = P[PX], y = P[PY], z = P[PZ], r = P[PCHI];
+        const double phi = atan2(y, x);
+        const double theta = acos(z / r);
+        const double cp = cos(phi), sp = sin(phi), ct = cos(theta), st = sin(theta);
+        const double s2p = sin(2 * phi), s2t = sin(2 * theta);
+        const double dl = pow(2, -(P[PLEVEL] - 1 - LEVEL_SHIFT));
+        float xm[7], xp[7], ym[7], yp[7], zm[7], zp[7];
+        tsc_cached(c->T, &cache, x - 0.5 * dl, y, z, xm);
+        tsc_cached(c->T, &cache, x + 0.5 * dl, y, z, xp);
+        tsc_cached(c->T, &cache, x, y - 0.5 * dl, z, ym);
+        tsc_cached(c->T, &cache, x, y + 0.5 * dl, z, yp);
+        tsc_cached(c->T, &cache, x, y, z - 0.5 * dl, zm);
+        tsc_cached(c->T, &cache, x, y, z + 0.5 * dl, zp);
+        const double dxxp = (xp[FDX] - xm[FDX]) / dl;
+        const double dxyp = (yp[FDX] - ym[FDX]) / dl;
+        const double dxzp = (zp[FDX] - zm[FDX]) / dl;
+        const double dyyp = (yp[FDY] - ym[FDY]) / dl;
+        const double dyzp = (zp[FDY] - zm[FDY]) / dl;
+        const double dzzp = (zp[FDZ] - zm[FDZ]) / dl;
+        const double d1d1p = sp * sp * dxxp + cp * cp * dyyp - s2p * dxyp;
+        const double d2d2p = cp * cp * ct * ct * dxxp + sp * sp * ct * ct * dyyp + st * st * dzzp + s2p * ct * ct * dxyp - sp * s2t * dyzp - cp * s2t * dxzp;
+        const double d1d2p = ct * cp * sp * (dyyp - dxxp) + (cp * cp - sp * sp) * ct * dxyp + sp * st * dxzp - cp * st * dyzp;
+        const double dr = P[PCHI] - Q[PCHI];
+        for (int j = 0; j < nd; ++j) {
+            const double gxsx = (dist[j] - P[PCHI]) * P[PCHI] / dist[j];
+            const int64_t o = (int64_t)j * tr->n;
+            a11[o + i] = a11[o + i - 1] + gxsx * d1d1p * dr;
+            a12[o + i] = a12[o + i - 1] + gxsx * d1d2p * dr;
+            a22[o + i] = a22[o + i - 1] + gxsx * d2d2p * dr;
+        }
+    }
+    for (int j = 0; j < nd; ++j) {
+        const int64_t marked = upper_by(tr, PCHI, dist[j], 0);
+        const int64_t fid = marked - (marked > 0);
+        const int64_t o = (int64_t)j * tr->n;
+        A[3 * j + 0] = 1 - 2 * a11[o + fid] / c2 * c->length;
+        A[3 * j + 1] = -2 * a12[o + fid] / c2 * c->length;
+        A[3 * j + 2] = 1 - 2 * a22[o + fid] / c2 * c->length;
+    }
+    free(a11);
+    free(a12);
+    free(a22);
+}
+
+static int stop_quantity(int kind)
+{
+    switch (kind) {
+    case MPFO_STOP_R: return PCHI;
+    case MPFO_STOP_LAMBDA: return PLAMBDA;
+    case MPFO_STOP_T: return PT;
+    case MPFO_STOP_A: return PA;
+    case MPFO_STOP_S: return PS;
+    case MPFO_STOP_REDSHIFT: return PZRED;
+    default: return -1;
+    }
+}
+
+static void planes_of(ctx_t* c, const traj_t* tr, int stop_kind, int np, const double* planes, int jac, double* out)
+{
+    const int q = stop_quantity(stop_kind);
+    double* dist = (double*)malloc(sizeof(double) * (size_t)(np > 0 ? np : 1));
+    for (int i = 0; i < np; ++i) {
+        double* o = out + MPFO_PLANE * i;
+        memset(o, 0, MPFO_PLANE * sizeof(double));
+        int64_t marked;
+        if (q < 0 || tr->n == 0) { marked = tr->n; }
+        else if (stop_kind == MPFO_STOP_REDSHIFT) {
+            marked = tr->n;
+            for (int64_t k = 0; k < tr->n; ++k)
+                if (tr->p[MPFO_PHOTON * k + PZRED] > planes[i]) { marked = k; break; }
+        } else marked = upper_by(tr, q, planes[i], stop_kind == MPFO_STOP_A);
+        const int64_t fid = marked - (marked > 0);
+        o[0] = (double)fid;
+        o[19] = (tr->n > 0 && q >= 0 && fid + 1 < tr->n && !(fid == tr->n - 1 || fid == 0)) ? 1.0 : 0.0;
+        dist[i] = 0.0;
+        if (!(tr->n > 0 && q >= 0 && fid + 1 < tr->n)) continue;
+        const double* P0 = tr->p + MPFO_PHOTON * fid;
+        const double* P1 = tr->p + MPFO_PHOTON * (fid + 1);
+        const double f = (P1[q] - planes[i]) / (P1[q] - P0[q]);
+        o[1] = f;
+        o[2] = P0[PX] * f + P1[PX] * (1 - f);
+        o[3] = P0[PY] * f + P1[PY] * (1 - f);
+        o[4] = P0[PZ] * f + P1[PZ] * (1 - f);
+        o[5] = sqrt(o[2] * o[2] + o[3] * o[3] + o[4] * o[4]);
+        dist[i] = o[5];
+        const int qs[9] = {PT, PA, PZRED, PCHI, PLAMBDA, PS, PISW, PRHO, PPHI};
+        for (int k = 0; k < 9; ++k) o[9 + k] = P0[qs[k]] * f + P1[qs[k]] * (1 - f);
+        double mx = 0.0;
+        int have = 0;
+        for (int64_t k = 0; k < fid; ++k) {
+            const double r = tr->p[MPFO_PHOTON * k + PRHO];
+            if (!have || mx < r) { mx = r; have = 1; }
+        }
+        o[18] = mx;
+    }
+    if (jac && np > 0 && tr->n > 0) {
+        double* A = (double*)malloc(sizeof(double) * 3 * (size_t)np);
+        jacobian(c, tr, np, dist, A);
+        for (int i = 0; i < np; ++i) {
+            double* o = out + MPFO_PLANE * i;
+            o[6] = A[3 * i];
+            o[7] = A[3 * i + 1];
+            o[8] = A[3 * i + 2];
+        }
+        free(A);
+    }
+    free(dist);
+}
+
+/* ---------------------------------------------------------------------- */
+/* batch drivers                                                           */
+/* ---------------------------------------------------------------------- */
+typedef struct {
+    const mpfo_tree* T;
+    const mpfo_cosmo* C;
+    int order, stop_kind, nplanes, jac;
+    double length, stop_ref;
+    unsigned nsteps;
+    const double* ki;
+    const double* launch;
+    const double* planes;
+    int64_t* steps;
+    double* final_out;
+    double* plane_out;
+    int64_t n;
+    int64_t next;
+    pthread_mutex_t mu;
+} job_t;
+
+static int64_t take(job_t* J)
+{
+    pthread_mutex_lock(&J->mu);
+    const int64_t i = J->next++;
+    pthread_mutex_unlock(&J->mu);
+    return i;
+}
+
+static void* worker(void* arg)
+{
+    job_t* J = (job_t*)arg;
+    ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+    traj_t tr = {0, 0, 0};
+    for (int64_t i; (i = take(J)) < J->n;) {
+        c->T = J->T;
+        c->C = J->C;
+        c->order = J->order;
+        c->length = J->length;
+        cache_init(&c->cache);
+        tr.n = 0;
+        launch6(J->launch + 6 * i, traj_push(&tr));
+        const double ref = (J->nplanes > 0) ? J->planes[J->nplanes - 1] : J->stop_ref;
+        integrate(c, &tr, J->nsteps, J->stop_kind, ref, J->ki);
+        J->steps[i] = tr.n;
+        if (J->final_out) {
+            if (tr.n > 0) memcpy(J->final_out + MPFO_PHOTON * i, tr.p + MPFO_PHOTON * (tr.n - 1), MPFO_PHOTON * sizeof(double));
+            else memset(J->final_out + MPFO_PHOTON * i, 0, MPFO_PHOTON * sizeof(double));
+        }
+        if (J->nplanes > 0 && J->plane_out)
+            planes_of(c, &tr, J->stop_kind, J->nplanes, J->planes, J->jac, J->plane_out + (int64_t)MPFO_PLANE * J->nplanes * i);
+    }
+    free(tr.p);
+    free(c);
+    return 0;
+}
+
+int mpfo_propagate(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
+                   int stop_kind, double stop_ref, const double* ki_target,
+                   int64_t n, const double* launch, int nplanes, const double* planes, int jacobian_on,
+                   int64_t* steps, double* final_out, double* plane_out, int nthreads)
+{
+    if (!T || !C || (order != 1 && order != 2) || nsteps == 0 || n < 0) return -1;
+    static const double zero3[3] = {0, 0, 0};
+    job_t J;
+    J.T = T; J.C = C; J.order = order; J.stop_kind = stop_kind; J.nplanes = nplanes; J.jac = jacobian_on;
+    J.length = length; J.stop_ref = stop_ref; J.nsteps = nsteps; J.ki = ki_target ? ki_target : zero3;
+    J.launch = launch; J.planes = planes; J.steps = steps; J.final_out = final_out; J.plane_out = plane_out;
+    J.n = n; J.next = 0;
+    pthread_mutex_init(&J.mu, 0);
+    if (nthreads <= 1) worker(&J);
+    else {
+        pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+        for (int t = 0; t < nthreads; ++t) pthread_create(&th[t], 0, worker, &J);
+        for (int t = 0; t < nthreads; ++t) pthread_join(th[t], 0);
+        free(th);
+    }
+    pthread_mutex_destroy(&J.mu);
+    return 0;
+}
+
+int64_t mpfo_trajectory(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
+                        int stop_kind, double stop_ref, const double* launch, double* out, int64_t cap)
+{
+    static const double zero3[3] = {0, 0, 0};
+    ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+    c->T = T; c->C = C; c->order = order; c->length = length;
+    cache_init(&c->cache);
+    traj_t tr = {0, 0, 0};
+    launch6(launch, traj_push(&tr));
+    integrate(c, &tr, nsteps, stop_kind, stop_ref, zero3);
+    const int64_t m = tr.n;
+    for (int64_t k = 0; k < m && k < cap; ++k) memcpy(out + MPFO_PHOTON * k, tr.p + MPFO_PHOTON * k, MPFO_PHOTON * sizeof(double));
+    free(tr.p);
+    free(c);
+    return m;
+}
+
+typedef struct {
+    const mpfo_tree* T;
+    int64_t n;
+    const double* xyz;
+    void* out;
+    int kind;
+    int nthreads, tid;
+} gjob_t;
+
+static void* gworker(void* arg)
+{
+    gjob_t* g = (gjob_t*)arg;
+    for (int64_t i = g->tid; i < g->n; i += g->nthreads) {
+        const double* p = g->xyz + 3 * i;
+        if (g->kind == 0) ((int64_t*)g->out)[i] = mpfo_locate(g->T, p[0], p[1], p[2]);
+        else if (g->kind == 1) mpfo_cic(g->T, p[0], p[1], p[2], (float*)g->out + 7 * i);
+        else mpfo_tsc(g->T, p[0], p[1], p[2], (float*)g->out + 7 * i);
+    }
+    return 0;
+}
+
+static void gbatch(const mpfo_tree* T, int64_t n, const double* xyz, void* out, int kind, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    gjob_t* g = (gjob_t*)malloc(sizeof(gjob_t) * (size_t)nthreads);
+    for (int t = 0; t < nthreads; ++t) {
+        g[t].T = T; g[t].n = n; g[t].xyz = xyz; g[t].out = out; g[t].kind = kind; g[t].nthreads = nthreads; g[t].tid = t;
+        pthread_create(&th[t], 0, gworker, &g[t]);
+    }
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], 0);
+    free(th);
+    free(g);
+}
+
+void mpfo_batch_locate(const mpfo_tree* T, int64_t n, const double* xyz, int64_t* out, int nthreads) { gbatch(T, n, xyz, out, 0, nthreads); }
+void mpfo_batch_cic(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads) { gbatch(T, n, xyz, out, 1, nthreads); }
+void mpfo_batch_tsc(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads) { gbatch(T, n, xyz, out, 2, nthreads); }

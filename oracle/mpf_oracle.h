@@ -1,0 +1,77 @@
+/* CPU oracle for the photon-propagation path: a plain-C restatement of the
+ * reference's octree gather, RK4 geodesic integrator, infinitesimal lensing
+ * Jacobian and per-pixel map reduction.
+ *
+ * TEST INFRASTRUCTURE ONLY.  It is the checker the CUDA path is compared
+ * against (tests/, __graft_entry__.smoke) and the timed CPU baseline of
+ * bench.py; the product never links or calls it.  It is itself pinned
+ * bit-for-bit to the reference's own code (oracle/ref_harness.cpp) by
+ * tests/test_oracle_vs_reference.py and the committed golden fixtures.
+ *
+ * Every floating-point expression keeps the reference's operation order and
+ * must be compiled without FMA contraction (-ffp-contract=off), as the
+ * reference's x86-64 build is. */
+#ifndef MPF_ORACLE_H
+#define MPF_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Sorted octree: n keys (128-bit, as hi/lo pairs) and 7 float fields per cell
+ * in the order rho, phi, dphidx, dphidy, dphidz, a, dphidt. */
+typedef struct {
+    int64_t n;
+    const uint64_t* keys;   /* n x 2: hi, lo */
+    const float* fields;    /* n x 7 */
+} mpfo_tree;
+
+typedef struct {
+    int64_t n;
+    const double* t;
+    const double* a;
+    const double* dadt;
+} mpfo_cosmo;
+
+enum { MPFO_STOP_REDSHIFT = 0, MPFO_STOP_R = 1, MPFO_STOP_LAMBDA = 2, MPFO_STOP_T = 3,
+       MPFO_STOP_A = 4, MPFO_STOP_PLANE = 5, MPFO_STOP_S = 6 };
+
+/* Photon record (28 doubles): a t x y z dtdl dxdl dydl dzdl level ah rho phi
+ * dphidx dphidy dphidz dphidt dphidl laplacian redshift dsdl2 error isw iswold
+ * chi lambda s index.
+ * Plane record (20 doubles): firstid f x y z distance A11 A12 A22 t a redshift
+ * chi lambda s isw rho phi rho_max valid. */
+#define MPFO_PHOTON 28
+#define MPFO_PLANE 20
+
+void mpfo_key_compute(unsigned level, double x, double y, double z, uint64_t* out);
+unsigned mpfo_key_level(uint64_t hi, uint64_t lo);
+int64_t mpfo_locate(const mpfo_tree* T, double x, double y, double z);
+void mpfo_cic(const mpfo_tree* T, double x, double y, double z, float* out7);
+void mpfo_tsc(const mpfo_tree* T, double x, double y, double z, float* out7);
+double mpfo_interpolate(double x0, const double* x, const double* y, int64_t n);
+
+/* Batch of rays.  launch: n x 6 (start xyz, end xyz, the 6-argument
+ * Integrator::launch).  planes: values of the stop quantity at which map
+ * planes are read (the last one is also the stop value); nplanes may be 0,
+ * then stop_ref is used.  jacobian != 0 computes the infinitesimal Jacobian
+ * at each plane's distance.  Outputs: steps[n], final[n x 28],
+ * plane_out[n x nplanes x 20].  Returns 0, or a negative error. */
+int mpfo_propagate(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
+                   int stop_kind, double stop_ref, const double* ki_target,
+                   int64_t n, const double* launch, int nplanes, const double* planes, int jacobian,
+                   int64_t* steps, double* final_out, double* plane_out, int nthreads);
+
+/* Whole trajectory of one ray; returns the number of records (may exceed cap). */
+int64_t mpfo_trajectory(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
+                        int stop_kind, double stop_ref, const double* launch, double* out, int64_t cap);
+
+void mpfo_batch_locate(const mpfo_tree* T, int64_t n, const double* xyz, int64_t* out, int nthreads);
+void mpfo_batch_cic(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads);
+void mpfo_batch_tsc(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,135 @@
+"""ctypes wrapper of the C oracle (oracle/mpf_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: the checker for the CUDA path in tests/ and
+__graft_entry__.smoke(), and the timed CPU baseline of bench.py.  Nothing in
+the product imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmpf_oracle.so")
+
+STOP = {"redshift": 0, "r": 1, "radius": 1, "lambda": 2, "t": 3, "eta": 3, "a": 4, "plane": 5, "s": 6}
+PHOTON_FIELDS = ("a t x y z dtdl dxdl dydl dzdl level ah rho phi dphidx dphidy dphidz dphidt dphidl "
+                 "laplacian redshift dsdl2 error isw iswold chi lambda s index").split()
+PLANE_FIELDS = ("firstid f x y z distance A11 A12 A22 t a redshift chi lambda s isw rho phi rho_max "
+                "valid").split()
+
+_lib = None
+_p = C.c_void_p
+_i64 = C.c_int64
+_d = C.c_double
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle into oracle/_build/ (no FMA contraction)."""
+    src = os.path.join(HERE, "mpf_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+        subprocess.check_call(["gcc", "-O3", "-std=gnu11", "-ffp-contract=off", "-fPIC", "-shared",
+                               "-o", LIB_PATH, src, "-lm", "-lpthread"])
+    return LIB_PATH
+
+
+class _Tree(C.Structure):
+    _fields_ = [("n", _i64), ("keys", _p), ("fields", _p)]
+
+
+class _Cosmo(C.Structure):
+    _fields_ = [("n", _i64), ("t", _p), ("a", _p), ("dadt", _p)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        L.mpfo_locate.restype = _i64
+        L.mpfo_locate.argtypes = [_p, _d, _d, _d]
+        L.mpfo_cic.argtypes = [_p, _d, _d, _d, _p]
+        L.mpfo_tsc.argtypes = [_p, _d, _d, _d, _p]
+        L.mpfo_interpolate.restype = _d
+        L.mpfo_interpolate.argtypes = [_d, _p, _p, _i64]
+        L.mpfo_key_compute.argtypes = [C.c_uint, _d, _d, _d, _p]
+        L.mpfo_propagate.restype = C.c_int
+        L.mpfo_propagate.argtypes = [_p, _p, C.c_int, _d, C.c_uint, C.c_int, _d, _p, _i64, _p, C.c_int, _p,
+                                     C.c_int, _p, _p, _p, C.c_int]
+        L.mpfo_trajectory.restype = _i64
+        L.mpfo_trajectory.argtypes = [_p, _p, C.c_int, _d, C.c_uint, C.c_int, _d, _p, _p, _i64]
+        for f in ("mpfo_batch_locate", "mpfo_batch_cic", "mpfo_batch_tsc"):
+            getattr(L, f).argtypes = [_p, _i64, _p, _p, C.c_int]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_p)
+
+
+def fields7(records: np.ndarray) -> np.ndarray:
+    """7-float rows (rho phi dphidx dphidy dphidz a dphidt) of 48-B records."""
+    return np.stack([records[k] for k in ("rho", "phi", "dphidx", "dphidy", "dphidz", "a", "dphidt")],
+                    axis=1).astype(np.float32)
+
+
+class Oracle:
+    def __init__(self, records: np.ndarray, cosmo: dict, length: float, nthreads: int = 0):
+        self.keys = np.ascontiguousarray(np.stack([records["hi"], records["lo"]], axis=1).astype(np.uint64))
+        self.fields = np.ascontiguousarray(fields7(records))
+        self.tree = _Tree(records.shape[0], _ptr(self.keys), _ptr(self.fields))
+        self.t = np.ascontiguousarray(cosmo["t"], dtype=np.float64)
+        self.a = np.ascontiguousarray(cosmo["a"], dtype=np.float64)
+        self.dadt = np.ascontiguousarray(cosmo["dadt"], dtype=np.float64)
+        self.cosmo = _Cosmo(self.t.shape[0], _ptr(self.t), _ptr(self.a), _ptr(self.dadt))
+        self.length = float(length)
+        self.nthreads = nthreads or (os.cpu_count() or 1)
+        self.L = lib()
+
+    def locate(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        out = np.zeros(xyz.shape[0], dtype=np.int64)
+        self.L.mpfo_batch_locate(C.byref(self.tree), xyz.shape[0], _ptr(xyz), _ptr(out), self.nthreads)
+        return out
+
+    def cic(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        out = np.zeros((xyz.shape[0], 7), dtype=np.float32)
+        self.L.mpfo_batch_cic(C.byref(self.tree), xyz.shape[0], _ptr(xyz), _ptr(out), self.nthreads)
+        return out
+
+    def tsc(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        out = np.zeros((xyz.shape[0], 7), dtype=np.float32)
+        self.L.mpfo_batch_tsc(C.byref(self.tree), xyz.shape[0], _ptr(xyz), _ptr(out), self.nthreads)
+        return out
+
+    def propagate(self, launch, order=2, nsteps=10, stop="redshift", stop_ref=0.5, planes=None, jacobian=True,
+                  ki_target=None, nthreads=None):
+        launch = np.ascontiguousarray(launch, dtype=np.float64)
+        n = launch.shape[0]
+        pl = np.ascontiguousarray(planes if planes is not None else np.zeros(0), dtype=np.float64)
+        npl = pl.shape[0]
+        steps = np.zeros(n, dtype=np.int64)
+        final = np.zeros((n, 28))
+        pout = np.zeros((n, max(npl, 1), 20))
+        ki = np.ascontiguousarray(ki_target if ki_target is not None else np.zeros(3), dtype=np.float64)
+        rc = self.L.mpfo_propagate(C.byref(self.tree), C.byref(self.cosmo), order, self.length, nsteps,
+                                   STOP[stop], stop_ref, _ptr(ki), n, _ptr(launch), npl,
+                                   _ptr(pl) if npl else None, int(bool(jacobian)), _ptr(steps), _ptr(final),
+                                   _ptr(pout), int(nthreads or self.nthreads))
+        if rc != 0:
+            raise ValueError("oracle propagate failed: %d" % rc)
+        return steps, final, pout[:, :npl]
+
+    def trajectory(self, launch, order=2, nsteps=10, stop="redshift", stop_ref=0.5, cap=200000):
+        L = np.ascontiguousarray(launch, dtype=np.float64)
+        out = np.zeros((cap, 28))
+        m = self.L.mpfo_trajectory(C.byref(self.tree), C.byref(self.cosmo), order, self.length, nsteps,
+                                   STOP[stop], stop_ref, _ptr(L), _ptr(out), cap)
+        return out[:min(m, cap)]

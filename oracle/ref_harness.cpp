@@ -1,0 +1,391 @@
+// Reference harness: a thin extern "C" shell around the reference's OWN
+// templates (Integrator::integrate, Lensing::dbetadtheta_infinitesimal,
+// Hmaps::FillMap, SimpleHyperOctree::{locate,cic,tsc}, SimpleHyperOctreeIndex
+// ::{compute,cipher}, Input::{acquire,correct,load}).  It is TEST
+// INFRASTRUCTURE: built by oracle/build_ref.sh into oracle/_ref/ from the
+// sources under the reference tree, loaded by tests/golden/make_golden.py and
+// by CPU tests through ctypes, and never linked into the product.
+//
+// The hmaps driver needs HEALPix only for pix2vec_ring (hmaps.h:599); the
+// harness supplies its own RING-scheme implementation (Gorski et al. 2005,
+// ApJ 622, 759, eqs. 4-10), the same formulas the CUDA map kernel uses, so
+// pixel->direction is consistent on both sides but not pinned to libhealpix.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <array>
+#include <map>
+#include <atomic>
+#include <thread>
+#include <mpi.h>
+
+// pix2vec_ring, RING scheme, written from the published formulas.
+static inline void harness_pix2vec_ring(long nside, long ipix, double* vec)
+{
+    const double ns = (double)nside;
+    const long ncap = 2 * nside * (nside - 1);
+    const long npix = 12 * nside * nside;
+    double z, phi;
+    if (ipix < ncap) {                       // north polar cap
+        const long iring = (long)((1 + (long)std::sqrt((double)(1 + 2 * ipix))) / 2);
+        long ir = iring;
+        // guard the integer square root against rounding
+        while (2 * ir * (ir - 1) > ipix) --ir;
+        while (2 * (ir + 1) * ir <= ipix) ++ir;
+        const long iphi = ipix - 2 * ir * (ir - 1) + 1;
+        z = 1.0 - (double)(ir * ir) / (3.0 * ns * ns);
+        phi = ((double)iphi - 0.5) * (M_PI / (2.0 * (double)ir));
+    } else if (ipix < npix - ncap) {         // equatorial belt
+        const long ip = ipix - ncap;
+        const long iring = ip / (4 * nside) + nside;
+        const long iphi = ip % (4 * nside) + 1;
+        const double fodd = ((iring + nside) & 1) ? 1.0 : 0.5;
+        z = (2.0 * ns - (double)iring) * 2.0 / (3.0 * ns);
+        phi = ((double)iphi - fodd) * (M_PI / (2.0 * ns));
+    } else {                                 // south polar cap
+        const long ip = npix - ipix;
+        long ir = (long)((1 + (long)std::sqrt((double)(2 * ip - 1))) / 2);
+        while (2 * ir * (ir - 1) >= ip) --ir;
+        while (2 * (ir + 1) * ir < ip) ++ir;
+        const long iphi = 4 * ir + 1 - (ip - 2 * ir * (ir - 1));
+        z = -1.0 + (double)(ir * ir) / (3.0 * ns * ns);
+        phi = ((double)iphi - 0.5) * (M_PI / (2.0 * (double)ir));
+    }
+    const double st = std::sqrt((1.0 - z) * (1.0 + z));
+    vec[0] = st * std::cos(phi);
+    vec[1] = st * std::sin(phi);
+    vec[2] = z;
+}
+static inline void pix2vec_ring(long nside, long ipix, double* vec) { harness_pix2vec_ring(nside, ipix, vec); }
+static inline long nside2npix(long nside) { return 12 * nside * nside; }
+
+using uint = unsigned int;
+using real = double;
+using point = std::array<real, 3>;
+
+#include "magrathea/simplehyperoctree.h"
+#include "magrathea/simplehyperoctreeindex.h"
+#include "magrathea/evolution.h"
+#include "magrathea/filelist.h"
+#include "cone.h"
+#include "utility.h"
+#include "input.h"
+#include "integrator.h"
+#include "lensing.h"
+#include "gravity.h"
+#include "miscellaneous.h"
+#include "hmaps.h"
+
+using namespace magrathea;
+using Index = SimpleHyperOctreeIndex<__uint128_t, 3>;
+using Oct = SimpleHyperOctree<double, Index, Gravity<float, 3>, 3, std::ratio<0>, std::ratio<EXTENT>>;
+using Traj = Evolution<Photon<double, 3>>;
+using Cosmo = std::array<std::vector<double>, 4>;
+
+static Oct g_octree;
+static Cosmo g_cosmo;
+static double g_length = 0.0;
+
+struct CosmoParams { std::string celldir, paramfile, evolfile; double mpc = 3.08568E22; };
+
+static void split(__uint128_t k, uint64_t* out)
+{
+    out[0] = (uint64_t)(k >> 64);
+    out[1] = (uint64_t)k;
+}
+
+static void data7(const Gravity<float, 3>& d, float* out)
+{
+    out[0] = d.rho(); out[1] = d.phi(); out[2] = d.dphidx(); out[3] = d.dphidy();
+    out[4] = d.dphidz(); out[5] = d.a(); out[6] = d.dphidt();
+}
+
+// Photon record, in this order: a t x y z dtdl dxdl dydl dzdl level ah rho phi
+// dphidx dphidy dphidz dphidt dphidl laplacian redshift dsdl2 error isw iswold
+// chi lambda s index   (28 doubles)
+static void photon28(const Photon<double, 3>& p, double* o)
+{
+    o[0] = p.a(); o[1] = p.t(); o[2] = p.x(); o[3] = p.y(); o[4] = p.z();
+    o[5] = p.dtdl(); o[6] = p.dxdl(); o[7] = p.dydl(); o[8] = p.dzdl();
+    o[9] = p.level(); o[10] = p.ah(); o[11] = p.rho(); o[12] = p.phi();
+    o[13] = p.dphidx(); o[14] = p.dphidy(); o[15] = p.dphidz(); o[16] = p.dphidt();
+    o[17] = p.dphidl(); o[18] = p.laplacian(); o[19] = p.redshift(); o[20] = p.dsdl2();
+    o[21] = p.error(); o[22] = p.isw(); o[23] = p.iswold(); o[24] = p.chi();
+    o[25] = p.lambda(); o[26] = p.s(); o[27] = (double)p.index();
+}
+
+template <class F> static void run_threads(int64_t n, int nthreads, F f)
+{
+    if (nthreads <= 1) { for (int64_t i = 0; i < n; ++i) f(i); return; }
+    std::atomic<int64_t> next(0);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t)
+        pool.emplace_back([&]() { for (int64_t i; (i = next.fetch_add(1)) < n;) f(i); });
+    for (auto& th : pool) th.join();
+}
+
+extern "C" {
+
+int ref_extent() { return EXTENT; }
+int ref_order() { return ORDER; }
+
+int64_t ref_load(const char* path)
+{
+    g_octree.fullclear();
+    if (!Input::load(g_octree, std::string(path))) return -1;
+    return (int64_t)g_octree.size();
+}
+
+int64_t ref_size() { return (int64_t)g_octree.size(); }
+
+void ref_keys(uint64_t* out)
+{
+    for (size_t i = 0; i < g_octree.size(); ++i) split(std::get<0>(g_octree[i])(), out + 2 * i);
+}
+
+void ref_compute(unsigned lvl, double x, double y, double z, uint64_t* out)
+{
+    split(Index::compute<double, std::ratio<0>, std::ratio<EXTENT>>(lvl, x, y, z)(), out);
+}
+
+void ref_cipher(double x, double y, double z, uint64_t* out)
+{
+    split(Index::cipher<double, std::ratio<0>, std::ratio<EXTENT>>(x, y, z)(), out);
+}
+
+unsigned ref_key_level(uint64_t hi, uint64_t lo)
+{
+    return Index((((__uint128_t)hi) << 64) | lo).level();
+}
+
+double ref_key_center(uint64_t hi, uint64_t lo, unsigned dim)
+{
+    return Index((((__uint128_t)hi) << 64) | lo).center<double, std::ratio<0>, std::ratio<EXTENT>>(dim);
+}
+
+int ref_key_containing(uint64_t ahi, uint64_t alo, uint64_t bhi, uint64_t blo)
+{
+    return Index((((__uint128_t)ahi) << 64) | alo).containing(Index((((__uint128_t)bhi) << 64) | blo));
+}
+
+// Index of the located element, or -1 when locate() returns end().
+int64_t ref_locate(double x, double y, double z)
+{
+    auto it = g_octree.locate(x, y, z);
+    return (it == g_octree.end()) ? -1 : (int64_t)(it - g_octree.begin());
+}
+
+void ref_batch_locate(int64_t n, const double* xyz, int64_t* out, int nthreads)
+{
+    run_threads(n, nthreads, [&](int64_t i) { out[i] = ref_locate(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]); });
+}
+
+void ref_batch_cic(int64_t n, const double* xyz, float* out, int nthreads)
+{
+    run_threads(n, nthreads, [&](int64_t i) { data7(g_octree.cic(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]), out + 7 * i); });
+}
+
+void ref_batch_tsc(int64_t n, const double* xyz, float* out, int nthreads)
+{
+    run_threads(n, nthreads, [&](int64_t i) {
+        std::vector<std::pair<Index, Gravity<float, 3>>> cache(27);
+        data7(g_octree.tsc(cache, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]), out + 7 * i);
+    });
+}
+
+// Sequential cached TSC over a list of points sharing one 27-cell cache, as the
+// integrator does along a ray (simplehyperoctree.h:1552-1644).
+void ref_seq_tsc(int64_t n, const double* xyz, float* out)
+{
+    std::vector<std::pair<Index, Gravity<float, 3>>> cache(27);
+    for (int64_t i = 0; i < n; ++i) data7(g_octree.tsc(cache, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]), out + 7 * i);
+}
+
+// Cosmology table as hmaps/catalogues/rays build it: Input::acquire, an FLRW
+// ray through a homogeneous level-5 octree (integrate<-1>), Input::correct
+// (hmaps.cpp:157-173).  Returns the table size, or -1.
+int64_t ref_cosmology(const char* celldir, const char* paramfile, const char* evolfile, double* hol)
+{
+    CosmoParams p;
+    p.celldir = celldir; p.paramfile = paramfile; p.evolfile = evolfile;
+    double h = 0, om = 0, lbox = 0;
+    Cosmo cosmology = Input::acquire(p, h, om, lbox);
+    if (std::get<0>(cosmology).empty()) return -1;
+    const double length = lbox * p.mpc / h;
+    Oct octree;
+    Traj reference;
+    const std::array<double, 3> v0{0, 0, 0};
+    Input::homogenize(octree.assign(5, 0));
+    reference.append(Integrator::launch(0., 0., 0., 0. + EXTENT / 2., 0., 0.));
+    Integrator::integrate<-1>(reference, cosmology, octree, v0, length,
+        EXTENT * std::pow(2., (uint)(std::log2(std::get<0>(cosmology).size() / std::pow(2., 5) + 1) + 1) + 1));
+    g_cosmo = Input::correct(cosmology, reference);
+    g_length = length;
+    hol[0] = h; hol[1] = om; hol[2] = lbox; hol[3] = length;
+    return (int64_t)std::get<0>(g_cosmo).size();
+}
+
+void ref_cosmology_get(double* t, double* a, double* dadt, double* d2adt2)
+{
+    const size_t n = std::get<0>(g_cosmo).size();
+    for (size_t i = 0; i < n; ++i) {
+        t[i] = g_cosmo[0][i]; a[i] = g_cosmo[1][i]; dadt[i] = g_cosmo[2][i]; d2adt2[i] = g_cosmo[3][i];
+    }
+}
+
+void ref_cosmology_set(int64_t n, const double* t, const double* a, const double* dadt, const double* d2adt2, double length)
+{
+    for (int k = 0; k < 4; ++k) g_cosmo[k].assign((size_t)n, 0.0);
+    for (int64_t i = 0; i < n; ++i) {
+        g_cosmo[0][i] = t[i]; g_cosmo[1][i] = a[i]; g_cosmo[2][i] = dadt[i]; g_cosmo[3][i] = d2adt2[i];
+    }
+    g_length = length;
+}
+
+double ref_interpolate(double x0, int col)
+{
+    return Utility::interpolate(x0, g_cosmo[0], g_cosmo[col]);
+}
+
+// One ray per launch record (x0 y0 z0 x1 y1 z1, the 6-argument
+// Integrator::launch), integrated with the stop criterion, then the
+// infinitesimal Jacobian at each distance in dists (lensing.h:399-472).
+// final28: photon record of trajectory.back(); jac: per distance a11 a12 a21 a22.
+void ref_integrate(int64_t n, const double* launch, const char* stop, double stop_ref, unsigned nsteps,
+                   int ndist, const double* dists, int64_t* steps, double* final28, double* jac, int nthreads)
+{
+    const std::string stop_s(stop);
+    const std::array<double, 3> v0{0, 0, 0};
+    run_threads(n, nthreads, [&](int64_t i) {
+        const double* L = launch + 6 * i;
+        Traj traj;
+        traj.append(Integrator::launch(L[0], L[1], L[2], L[3], L[4], L[5]));
+        Integrator::integrate(traj, stop_s, stop_ref, g_cosmo, g_octree, v0, g_length, nsteps);
+        steps[i] = (int64_t)traj.size();
+        if (!traj.empty()) photon28(traj.back(), final28 + 28 * i);
+        if (ndist > 0 && traj.size() > 0) {
+            std::vector<double> d(dists, dists + ndist);
+            auto J = Lensing::dbetadtheta_infinitesimal(d, traj, g_octree, g_length);
+            for (int j = 0; j < ndist; ++j) {
+                double* o = jac + 4 * (i * ndist + j);
+                o[0] = J[j][0][0]; o[1] = J[j][0][1]; o[2] = J[j][1][0]; o[3] = J[j][1][1];
+            }
+        }
+    });
+}
+
+// Whole trajectory of one ray (28 doubles per step); returns its size.
+int64_t ref_trajectory(const double* L, const char* stop, double stop_ref, unsigned nsteps, double* out, int64_t cap)
+{
+    const std::array<double, 3> v0{0, 0, 0};
+    Traj traj;
+    traj.append(Integrator::launch(L[0], L[1], L[2], L[3], L[4], L[5]));
+    Integrator::integrate(traj, std::string(stop), stop_ref, g_cosmo, g_octree, v0, g_length, nsteps);
+    const int64_t m = (int64_t)traj.size();
+    for (int64_t k = 0; k < m && k < cap; ++k) photon28(traj[k], out + 28 * k);
+    return m;
+}
+
+// Homogeneous (FLRW) quantities at each redshift, as hmaps.cpp:302-333 derives
+// them from the reference ray: out[5*i..] = t, chi, lambda, a, z.
+int ref_homogeneous(int nz, const double* zs, double* out)
+{
+    Oct octree;
+    Traj reference;
+    const std::array<double, 3> v0{0, 0, 0};
+    Input::homogenize(octree.assign(5, 0));
+    reference.append(Integrator::launch(0., 0., 0., 0. + EXTENT / 2., 0., 0.));
+    Integrator::integrate<-1>(reference, g_cosmo, octree, v0, g_length,
+        EXTENT * std::pow(2., (uint)(std::log2(std::get<0>(g_cosmo).size() / std::pow(2., 5) + 1) + 1) + 1));
+    Photon<double, 3> photon;
+    for (int i = 0; i < nz; ++i) {
+        photon.redshift() = zs[i];
+        const unsigned long marked = std::distance(std::begin(reference), std::upper_bound(std::begin(reference), std::end(reference), photon,
+            [](const Photon<double, 3>& a, const Photon<double, 3>& b) { return a.redshift() < b.redshift(); }));
+        const unsigned long firstid = marked - (marked > 0);
+        if (firstid + 1 >= reference.size()) return -1;
+        const double f = (reference[firstid + 1].redshift() - zs[i]) / (reference[firstid + 1].redshift() - reference[firstid].redshift());
+        out[5 * i + 0] = reference[firstid].t() * f + reference[firstid + 1].t() * (1 - f);
+        out[5 * i + 1] = reference[firstid].chi() * f + reference[firstid + 1].chi() * (1 - f);
+        out[5 * i + 2] = reference[firstid].lambda() * f + reference[firstid + 1].lambda() * (1 - f);
+        out[5 * i + 3] = 1. / (1. + zs[i]);
+        out[5 * i + 4] = zs[i];
+    }
+    return 0;
+}
+
+// Hmaps::FillMap (hmaps.h:579-836) itself, with map_components = "lensing"
+// (infinitesimal Jacobian) plus the per-pixel extras requested in comps
+// (a comma list among dr dl dt da dz ds isw dens dens_max steps phi
+// deflection), one ray per pixel of `pixels`.  maps: nmaps*nz rows of npix
+// floats, row-major, the layout of the reference's map vector.
+int ref_fillmap(long nside, int nz, const double* zvals, const char* stop_ray, const char* comps, unsigned nsteps,
+                int64_t npixels, const long* pixels, float* maps, int* nmaps_out)
+{
+    parameters.nside = nside;
+    parameters.nb_z_maps = nz;
+    parameters.nsteps = nsteps;
+    parameters.stop_ray = stop_ray;
+    parameters.jacobiantype = "infinitesimal";
+    parameters.plane = "normal";
+    parameters.stop_bundle = "redshift";
+    parameters.map_components = comps;
+    std::vector<std::string> map_components;
+    {
+        std::string cur;
+        for (const char c : parameters.map_components) {
+            if (c == ',' || c == ' ') { if (!cur.empty()) map_components.push_back(cur); cur.clear(); }
+            else cur.push_back(c);
+        }
+        if (!cur.empty()) map_components.push_back(cur);
+    }
+    std::vector<uint> index_components(map_components.size());
+    static const std::map<std::string, uint> ids = {
+        {"lensing", 0}, {"lensing_born", 1}, {"dr", 2}, {"dl", 3}, {"dt", 4}, {"da", 5}, {"dz", 6}, {"ds", 7},
+        {"isw", 8}, {"dens", 9}, {"dens_max", 10}, {"steps", 11}, {"phi", 12}, {"deflection", 13}};
+    uint nmaps = 0;
+    for (size_t i = 0; i < map_components.size(); ++i) {
+        auto it = ids.find(map_components[i]);
+        if (it == ids.end() || it->second == 1) return -1;
+        index_components[i] = it->second;
+        nmaps += (it->second == 0) ? 4 : (it->second == 13 ? 2 : 1);
+    }
+    *nmaps_out = (int)nmaps;
+    std::vector<double> hom(5 * (size_t)nz);
+    std::vector<double> zs(zvals, zvals + nz);
+    if (ref_homogeneous(nz, zvals, hom.data()) != 0) return -2;
+    std::vector<double> thomo(nz), rhomo(nz), lambdahomo(nz), ahomo(nz), redshifthomo(nz);
+    for (int i = 0; i < nz; ++i) {
+        thomo[i] = hom[5 * i]; rhomo[i] = hom[5 * i + 1]; lambdahomo[i] = hom[5 * i + 2];
+        ahomo[i] = hom[5 * i + 3]; redshifthomo[i] = hom[5 * i + 4];
+    }
+    std::vector<double> interpRefvec;
+    const std::string s(stop_ray);
+    if (s == "t") interpRefvec = thomo;
+    else if (s == "r" || s == "s") interpRefvec = rhomo;
+    else if (s == "lambda") interpRefvec = lambdahomo;
+    else if (s == "a") interpRefvec = ahomo;
+    else if (s == "redshift") interpRefvec = zs;
+    else return -3;
+    // pixel ids are used as map offsets: remap them to 0..npixels-1 rows
+    std::vector<long> pix(pixels, pixels + npixels);
+    long maxpix = 0;
+    for (long p : pix) maxpix = std::max(maxpix, p);
+    std::vector<std::vector<float>> map((size_t)nmaps * nz, std::vector<float>((size_t)maxpix + 1, 0.f));
+    const std::array<double, 3> v0{0, 0, 0};
+    const point observer{{0., 0., 0.}};
+    Hmaps::FillMap(parameters, map_components, index_components, (unsigned)npixels, 0u, g_octree, v0, map, nmaps, pix,
+                   g_cosmo, observer, g_length, interpRefvec, rhomo, thomo, lambdahomo, redshifthomo, ahomo);
+    for (size_t r = 0; r < map.size(); ++r)
+        for (int64_t k = 0; k < npixels; ++k) maps[r * npixels + k] = map[r][pix[k]];
+    return 0;
+}
+
+void ref_pix2vec_ring(long nside, int64_t n, const long* pix, double* vec)
+{
+    for (int64_t i = 0; i < n; ++i) harness_pix2vec_ring(nside, pix[i], vec + 3 * i);
+}
+
+}  // extern "C"

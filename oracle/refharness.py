@@ -1,0 +1,172 @@
+"""ctypes wrapper of the reference harness (oracle/_ref/libref_o{1,2}.so).
+
+Test infrastructure only: used to generate golden fixtures and to pin the
+C restatement (oracle/mpf_oracle.c) to the reference in this container.  The
+library exists only where the reference sources were available at build time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIBS = {}
+
+_d = C.c_double
+_i64 = C.c_int64
+_p = C.c_void_p
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_p)
+
+
+def available(order: int = 2) -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", "libref_o%d.so" % order))
+
+
+def lib(order: int = 2):
+    if order not in _LIBS:
+        path = os.path.join(HERE, "_ref", "libref_o%d.so" % order)
+        L = C.CDLL(path, mode=C.RTLD_LOCAL)
+        L.ref_load.restype = _i64
+        L.ref_load.argtypes = [C.c_char_p]
+        L.ref_size.restype = _i64
+        L.ref_keys.argtypes = [_p]
+        L.ref_compute.argtypes = [C.c_uint, _d, _d, _d, _p]
+        L.ref_cipher.argtypes = [_d, _d, _d, _p]
+        L.ref_key_level.restype = C.c_uint
+        L.ref_key_level.argtypes = [C.c_uint64, C.c_uint64]
+        L.ref_key_center.restype = _d
+        L.ref_key_center.argtypes = [C.c_uint64, C.c_uint64, C.c_uint]
+        L.ref_key_containing.restype = C.c_int
+        L.ref_key_containing.argtypes = [C.c_uint64] * 4
+        L.ref_locate.restype = _i64
+        L.ref_locate.argtypes = [_d, _d, _d]
+        for f in ("ref_batch_locate", "ref_batch_cic", "ref_batch_tsc"):
+            getattr(L, f).argtypes = [_i64, _p, _p, C.c_int]
+        L.ref_seq_tsc.argtypes = [_i64, _p, _p]
+        L.ref_cosmology.restype = _i64
+        L.ref_cosmology.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, _p]
+        L.ref_cosmology_get.argtypes = [_p, _p, _p, _p]
+        L.ref_cosmology_set.argtypes = [_i64, _p, _p, _p, _p, _d]
+        L.ref_interpolate.restype = _d
+        L.ref_interpolate.argtypes = [_d, C.c_int]
+        L.ref_integrate.argtypes = [_i64, _p, C.c_char_p, _d, C.c_uint, C.c_int, _p, _p, _p, _p, C.c_int]
+        L.ref_trajectory.restype = _i64
+        L.ref_trajectory.argtypes = [_p, C.c_char_p, _d, C.c_uint, _p, _i64]
+        L.ref_homogeneous.restype = C.c_int
+        L.ref_homogeneous.argtypes = [C.c_int, _p, _p]
+        L.ref_fillmap.restype = C.c_int
+        L.ref_fillmap.argtypes = [C.c_long, C.c_int, _p, C.c_char_p, C.c_char_p, C.c_uint, _i64, _p, _p, _p]
+        L.ref_pix2vec_ring.argtypes = [C.c_long, _i64, _p, _p]
+        _LIBS[order] = L
+    return _LIBS[order]
+
+
+class Reference:
+    """The reference's own octree / integrator / map driver, one per ORDER."""
+
+    def __init__(self, order: int = 2, nthreads: int = 0):
+        self.L = lib(order)
+        self.order = order
+        self.nthreads = nthreads or (os.cpu_count() or 1)
+
+    def load(self, path: str) -> int:
+        n = self.L.ref_load(path.encode())
+        if n < 0:
+            raise IOError("reference could not load %s" % path)
+        return n
+
+    def keys(self):
+        n = self.L.ref_size()
+        out = np.zeros((n, 2), dtype=np.uint64)
+        self.L.ref_keys(_ptr(out))
+        return out
+
+    def compute(self, level, x, y, z):
+        out = np.zeros(2, dtype=np.uint64)
+        self.L.ref_compute(level, x, y, z, _ptr(out))
+        return int(out[0]), int(out[1])
+
+    def cipher(self, x, y, z):
+        out = np.zeros(2, dtype=np.uint64)
+        self.L.ref_cipher(x, y, z, _ptr(out))
+        return int(out[0]), int(out[1])
+
+    def locate(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        out = np.zeros(xyz.shape[0], dtype=np.int64)
+        self.L.ref_batch_locate(xyz.shape[0], _ptr(xyz), _ptr(out), self.nthreads)
+        return out
+
+    def cic(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        out = np.zeros((xyz.shape[0], 7), dtype=np.float32)
+        self.L.ref_batch_cic(xyz.shape[0], _ptr(xyz), _ptr(out), self.nthreads)
+        return out
+
+    def tsc(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        out = np.zeros((xyz.shape[0], 7), dtype=np.float32)
+        self.L.ref_batch_tsc(xyz.shape[0], _ptr(xyz), _ptr(out), self.nthreads)
+        return out
+
+    def cosmology(self, celldir, paramfile, evolfile):
+        hol = np.zeros(4)
+        n = self.L.ref_cosmology(celldir.encode(), paramfile.encode(), evolfile.encode(), _ptr(hol))
+        if n < 0:
+            raise RuntimeError("reference cosmology failed")
+        t, a, dadt, d2 = (np.zeros(n) for _ in range(4))
+        self.L.ref_cosmology_get(_ptr(t), _ptr(a), _ptr(dadt), _ptr(d2))
+        return dict(t=t, a=a, dadt=dadt, d2adt2=d2, h=hol[0], omega_m=hol[1], lbox=hol[2], length=hol[3])
+
+    def set_cosmology(self, t, a, dadt, d2adt2, length):
+        arrs = [np.ascontiguousarray(v, dtype=np.float64) for v in (t, a, dadt, d2adt2)]
+        self.L.ref_cosmology_set(arrs[0].shape[0], *[_ptr(v) for v in arrs], float(length))
+        self._keep = arrs
+
+    def integrate(self, launch, stop="redshift", stop_ref=0.5, nsteps=10, dists=None):
+        launch = np.ascontiguousarray(launch, dtype=np.float64)
+        n = launch.shape[0]
+        d = np.ascontiguousarray(dists if dists is not None else np.zeros(0), dtype=np.float64)
+        nd = d.shape[0]
+        steps = np.zeros(n, dtype=np.int64)
+        final = np.zeros((n, 28))
+        jac = np.zeros((n, max(nd, 1), 4))
+        self.L.ref_integrate(n, _ptr(launch), stop.encode(), stop_ref, nsteps, nd, _ptr(d) if nd else None,
+                             _ptr(steps), _ptr(final), _ptr(jac), self.nthreads)
+        return steps, final, jac[:, :nd]
+
+    def trajectory(self, launch, stop="redshift", stop_ref=0.5, nsteps=10, cap=200000):
+        L = np.ascontiguousarray(launch, dtype=np.float64)
+        out = np.zeros((cap, 28))
+        m = self.L.ref_trajectory(_ptr(L), stop.encode(), stop_ref, nsteps, _ptr(out), cap)
+        return out[:min(m, cap)]
+
+    def homogeneous(self, zs):
+        zs = np.ascontiguousarray(zs, dtype=np.float64)
+        out = np.zeros((zs.shape[0], 5))
+        if self.L.ref_homogeneous(zs.shape[0], _ptr(zs), _ptr(out)) != 0:
+            raise RuntimeError("homogeneous quantities failed")
+        return out
+
+    def fillmap(self, nside, zs, pixels, stop_ray="redshift", comps="lensing", nsteps=10):
+        zs = np.ascontiguousarray(zs, dtype=np.float64)
+        pix = np.ascontiguousarray(pixels, dtype=np.int64)
+        nmaps_guess = 32
+        maps = np.zeros(nmaps_guess * zs.shape[0] * pix.shape[0], dtype=np.float32)
+        nm = C.c_int(0)
+        rc = self.L.ref_fillmap(nside, zs.shape[0], _ptr(zs), stop_ray.encode(), comps.encode(), nsteps,
+                                pix.shape[0], _ptr(pix), _ptr(maps), C.byref(nm))
+        if rc != 0:
+            raise RuntimeError("ref_fillmap failed: %d" % rc)
+        return maps[: nm.value * zs.shape[0] * pix.shape[0]].reshape(zs.shape[0], nm.value, pix.shape[0])
+
+    def pix2vec(self, nside, pixels):
+        pix = np.ascontiguousarray(pixels, dtype=np.int64)
+        out = np.zeros((pix.shape[0], 3))
+        self.L.ref_pix2vec_ring(nside, pix.shape[0], _ptr(pix), _ptr(out))
+        return out
