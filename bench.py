@@ -1,0 +1,342 @@
+"""Benchmark of the photon-propagation path on one GB300 (or N replicas).
+
+Workload (the plain-octree AMR configuration): a 256^3 periodic base field
+(octree level 10, file level 8) refined to octree level 14 inside 2000 seeded
+NFW haloes; 1000 x 1000 rays on a regular grid filling a 10 x 10 degree cone,
+integrated to z = 2 with TSC interpolation, 8 steps per cell and the
+infinitesimal lensing Jacobian at z = 2.  Inputs are seeded synthetic data
+with those shapes (no simulation data are available).
+
+One step = one batch of rays (whole 8 x 4 sky tiles drawn at random from the
+grid, so every batch samples the whole cone).  The octree (GBs) is larger
+than L2, so no flush is needed between steps.
+
+Metric: RK4 photon-steps per second (one accepted RK4 step of one ray =
+one photon-step, src/integrator.h:776).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import hashlib
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+PKG = "magrathea-pathfinder_gb300"
+
+METRIC = "RK4 photon-steps/s on 1 GB300, surrogate vs plain octree, at <=1e-3 rel deflection"
+UNIT = "photon-steps/s"
+# payload bytes requested per photon-step, TSC + Jacobian: 4 RK stages x 27 cells x 16 B
+# + post-step 27 x 28 B + Jacobian 6 x 27 x 12 B
+BYTES_PER_PHOTON_STEP = 4 * 27 * 16 + 27 * 28 + 6 * 27 * 12
+# DRAM bytes per photon-step of the propagate kernel measured with ncu on the AMR
+# workload (profiles/propagate_tsc_amr.md); None until measured
+DRAM_BYTES_PER_PHOTON_STEP = None
+
+
+def workload_spec(synth, small: bool):
+    cosmo = synth.Cosmology()
+    chi2 = float(cosmo.chi_of_z(2.0)[0])
+    if small:
+        return synth.OctreeSpec(base_level=8, box_cells=64, lbox=2048.0, half_y=5.0, half_z=5.0, chi_max=chi2 * 1.02,
+                                halos=50, max_level=11, refine_cells=2.5, seed=42)
+    return synth.OctreeSpec(base_level=10, box_cells=256, lbox=2048.0, half_y=5.0, half_z=5.0, chi_max=chi2 * 1.02,
+                            halos=2000, max_level=14, mass_min=1e12, mass_max=1e15, refine_cells=4.5, seed=42)
+
+
+def octree_records(synth, spec):
+    key = hashlib.sha1(repr(spec).encode()).hexdigest()[:16]
+    path = os.path.join(os.environ.get("TMPDIR", "/tmp"), "mpf_bench_%s.bin" % key)
+    if os.path.exists(path):
+        return synth.read_bin(path)
+    rec = synth.make_octree(spec)
+    tmp = path + ".%d" % os.getpid()
+    synth.write_bin(tmp, rec)
+    os.replace(tmp, path)
+    return rec
+
+
+def ray_grid(n_side=1000, half_deg=5.0, tile=(8, 4), seed=0):
+    """Launch records of the n_side^2 grid, reordered by shuffled 8x4 tiles."""
+    t = (np.arange(n_side) + 0.5) / n_side * 2.0 - 1.0
+    ph = np.radians(half_deg) * t
+    th = np.pi / 2 + np.radians(half_deg) * t
+    ty, tz = tile
+    ny, nz = n_side // ty, n_side // tz
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(ny * nz)
+    iy = (order // nz)[:, None] * ty + (np.arange(ty * tz) % ty)[None, :]
+    iz = (order % nz)[:, None] * tz + (np.arange(ty * tz) // ty)[None, :]
+    P, T = ph[iy.ravel()], th[iz.ravel()]
+    out = np.zeros((P.shape[0], 6))
+    out[:, 3] = np.sin(T) * np.cos(P)
+    out[:, 4] = np.sin(T) * np.sin(P)
+    out[:, 5] = np.cos(T)
+    return out
+
+
+def cosmology_table(synth):
+    return synth.Cosmology().conformal_table(n=4000, amin=0.05)
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(os.environ.get("TMPDIR", "/tmp"), "mpf_clocks_%d.csv" % os.getpid())
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(oracle_mod, records, cos, length, launch, planes, per_thread=4, seed=1):
+    """The C oracle (restated reference algorithm, binary search over sorted
+    keys, trajectory then Jacobian post-pass) on a bounded random sample."""
+    nthreads = os.cpu_count() or 1
+    O = oracle_mod.Oracle(records, {"t": cos[0], "a": cos[1], "dadt": cos[2]}, length, nthreads=nthreads)
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(launch.shape[0], size=per_thread * nthreads, replace=False)
+    t0 = time.perf_counter()
+    steps, _, _ = O.propagate(launch[idx], order=2, nsteps=8, stop="redshift", planes=planes, jacobian=True)
+    dt = time.perf_counter() - t0
+    total = int(steps.sum())
+    return {"value": total / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": "%d rays drawn from the grid, %d photon-steps, %.1f s, %d threads (C oracle, Jacobian post-pass)"
+                      % (idx.shape[0], total, dt, nthreads)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("MPF_BENCH_GLOO") is None else "gloo")
+    return world, rank, local, dist
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=65536)
+    ap.add_argument("--small", action="store_true", help="small octree (debug only)")
+    ap.add_argument("--exact", action="store_true", help="reference float64 gather order")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, dist = dist_setup()
+    synth = importlib.import_module(PKG + ".synth")
+    spec = workload_spec(synth, args.small)
+    config = {"workload": "AMR cone octree, 256^3 base (level 10) refined to level 14 in 2000 NFW haloes; "
+                          "1000x1000 rays over 10x10 deg to z=2; TSC, 8 steps/cell, infinitesimal Jacobian at z=2"
+                          if not args.small else "small debug octree",
+              "rays": 1000 * 1000, "batch_rays": args.batch, "order": "TSC", "nsteps": 8, "z_stop": 2.0,
+              "gather_arithmetic": "float64 reference order" if args.exact else "fp32 gather, fp64 state",
+              "l2": "octree larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single GPU"}
+    cos = cosmology_table(synth)
+    length = spec.lbox * synth.MPC / spec.cosmo.h
+    planes = np.array([2.0])
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import oracle as oracle_mod
+        oracle_mod.build()
+        rec = octree_records(synth, spec)
+        launch = ray_grid()
+        nthreads = os.cpu_count() or 1
+        O = oracle_mod.Oracle(rec, {"t": cos[0], "a": cos[1], "dadt": cos[2]}, length, nthreads=nthreads)
+        rng = np.random.default_rng(3)
+        per_step = 2 * nthreads
+        times, counts = [], []
+        for s in range(args.warmup + args.steps):
+            idx = rng.choice(launch.shape[0], size=per_step, replace=False)
+            t0 = time.perf_counter()
+            st, _, _ = O.propagate(launch[idx], order=2, nsteps=8, stop="redshift", planes=planes, jacobian=True)
+            dt = time.perf_counter() - t0
+            if s >= args.warmup:
+                times.append(dt)
+                counts.append(int(st.sum()))
+        value = sum(counts) / sum(times)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "impl": "reference",
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                                 "sample": "%d random rays per step of the grid, C oracle restating the reference "
+                                           "(the reference's x86 build does not run on this Arm host)" % per_step},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    pkg = importlib.import_module(PKG)
+    importlib.import_module(PKG + ".build").build()
+    lib = pkg.library()
+    capi = importlib.import_module(PKG + ".capi")
+    rec = octree_records(synth, spec)
+    tree = pkg.Octree.from_records(rec)
+    info = tree.info
+    config.update({"cells": int(info["cells"]), "levels": [info["level_min"], info["level_max"]],
+                   "octree_device_bytes": int(info["device_bytes"])})
+    cosmo = pkg.Cosmology(*cos)
+    launch = ray_grid()
+    B = min(args.batch, launch.shape[0])
+    nb = launch.shape[0] // B
+    dev = torch.device("cuda", local)
+    d_launch = torch.from_numpy(launch).to(dev)
+    d_steps = torch.zeros((args.warmup + args.steps, B), dtype=torch.int64, device=dev)
+    d_planes = torch.zeros(B * 1 * capi.MPF_PLANE_FIELDS, dtype=torch.float64, device=dev)
+    d_status = torch.zeros(1, dtype=torch.int32, device=dev)
+    p, keep = capi.make_params(length, nsteps=8, order=2, stop="redshift", planes=planes, jacobian=True,
+                               exact=args.exact)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(k):
+        off = (k % nb) * B
+        rc = lib.mpf_propagate_device(tree._h, cosmo._h, C.byref(p), B, C.c_void_p(d_launch.data_ptr() + off * 48),
+                                      C.c_void_p(d_steps[k].data_ptr()), None, C.c_void_p(d_planes.data_ptr()),
+                                      C.c_void_p(d_status.data_ptr()), C.c_void_p(stream.cuda_stream))
+        capi.check(rc)
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launch_ms = []
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for k in range(args.steps):
+            e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e_a.record(stream)
+            step(args.warmup + k)
+            e_b.record(stream)
+            launch_ms.append((e_a, e_b))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    per_launch = [a.elapsed_time(b) for a, b in launch_ms]
+    photon_steps = int(d_steps[args.warmup:].sum().item())
+    status = int(d_status.item())
+    t_max = elapsed_ms
+    total_steps = photon_steps
+    if dist is not None:
+        t = torch.tensor([elapsed_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+        c = torch.tensor([photon_steps], dtype=torch.float64, device=dev)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        total_steps = int(c.item())
+    value = total_steps / (t_max / 1000.0)
+
+    # end to end through the public API: host launch records in, host steps and
+    # surface records out, every step
+    h_launch = np.ascontiguousarray(launch[:B])
+    e2e_t = []
+    e2e_steps = 0
+    for k in range(max(2, min(args.steps, 3))):
+        off = ((k + 1) % nb) * B
+        h = np.ascontiguousarray(launch[off:off + B])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st, _, pl, _ = pkg.propagate(tree, cosmo, h, length, nsteps=8, order=2, stop="redshift", planes=planes,
+                                     jacobian=True, exact=args.exact, want_final=False)
+        e2e_t.append(time.perf_counter() - t0)
+        e2e_steps += int(st.sum())
+    e2e_value = e2e_steps / sum(e2e_t)
+    del h_launch
+
+    peak, peak_kind = measured_peak_hbm()
+    avg_launch_s = (sum(per_launch) / len(per_launch)) / 1000.0
+    bytes_per_launch = (photon_steps / args.steps) * BYTES_PER_PHOTON_STEP
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": (DRAM_BYTES_PER_PHOTON_STEP * photon_steps / args.steps) if DRAM_BYTES_PER_PHOTON_STEP else None,
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "bytes_per_photon_step": BYTES_PER_PHOTON_STEP}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+            "form": "plain octree (surrogate not built)",
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": B * 6 * 8,
+                    "d2h_bytes_per_step": B * 8 + B * capi.MPF_PLANE_FIELDS * 8},
+            "gpu_launches": args.steps, "roofline": roofline, "status_bits": status,
+            "clocks": clk.summary()}
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle as oracle_mod
+        oracle_mod.build()
+        line["cpu_baseline"] = cpu_baseline(oracle_mod, rec, cos, length, launch, planes)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,134 @@
+/* mpf_gb300: GB300 (sm_103a) photon-propagation path of Magrathea-Pathfinder.
+ *
+ * C ABI: plain pointers and sizes, no C++ or CUDA types.  Every entry point
+ * returns an mpf_status (0 = success, < 0 = error, > 0 = completed with a
+ * warning); mpf_last_error() gives a message for the calling thread.
+ *
+ * Handles (mpf_octree, mpf_cosmology) own device memory on the device that
+ * was current when they were created; they are not re-entrant: one host
+ * thread at a time per handle.  Buffers passed to the mpf_* calls below are
+ * HOST memory unless the name ends in _device.
+ *
+ * Each entry point names the reference interface it stands in for
+ * (paths within the reference source tree).
+ */
+#ifndef MPF_GB300_H
+#define MPF_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MPF_OK = 0,
+    MPF_WARN_MAX_STEPS = 1,      /* at least one ray hit params.max_steps */
+    MPF_BAD_INPUT = -1,
+    MPF_OUT_OF_MEMORY = -2,
+    MPF_CUDA_ERROR = -3,
+    MPF_NOT_SORTED = -4,         /* cone records must be sorted by key */
+    MPF_NO_DEVICE = -5,
+    MPF_IO_ERROR = -6
+} mpf_status;
+
+typedef enum {                    /* stop_ray / stop criterion, src/integrator.h:779-811 */
+    MPF_STOP_REDSHIFT = 0,
+    MPF_STOP_RADIUS = 1,          /* "r" / "radius": comoving distance in octree units */
+    MPF_STOP_LAMBDA = 2,
+    MPF_STOP_T = 3,               /* "t" / "eta": conformal time */
+    MPF_STOP_A = 4,
+    MPF_STOP_PLANE = 5,           /* x . plane_normal > stop_value */
+    MPF_STOP_S = 6
+} mpf_stop;
+
+typedef struct mpf_octree mpf_octree;
+typedef struct mpf_cosmology mpf_cosmology;
+
+typedef struct {
+    int64_t cells;
+    int64_t nodes;
+    int level_min, level_max;
+    int top_level;
+    int grid[3];
+    int64_t device_bytes;
+} mpf_octree_info;
+
+/* Ray-tracing parameters (the parameter-file keys of the rays / hmaps /
+ * catalogues executables, src/hmaps.h:148-199). */
+typedef struct {
+    double length;             /* lbox * mpc / h in metres (hmaps.cpp:165) */
+    double stop_value;         /* interpRef; ignored when nplanes > 0 (last plane is used) */
+    double plane_normal[3];    /* kiTarget for MPF_STOP_PLANE */
+    const double* planes;      /* surfaces (values of the stop quantity), ascending; host memory */
+    int nplanes;               /* <= MPF_MAX_PLANES */
+    unsigned nsteps;           /* steps per cell */
+    int order;                 /* 1 = CIC, 2 = TSC (the reference's ORDER) */
+    int stop;                  /* mpf_stop */
+    int jacobian;              /* infinitesimal Jacobian at each surface */
+    int exact;                 /* 1: the reference's float64 gather arithmetic, bit-exact
+                                  trajectories; 0: FP32 gather arithmetic (faster) */
+    int64_t max_steps;         /* per ray; <= 0 means 1e8 */
+} mpf_params;
+
+#define MPF_MAX_PLANES 16
+#define MPF_PHOTON_FIELDS 28
+#define MPF_PLANE_FIELDS 20
+
+/* Photon record (28 doubles), the reference's Photon<double,3>:
+ *   a t x y z dtdl dxdl dydl dzdl level ah rho phi dphidx dphidy dphidz dphidt
+ *   dphidl laplacian redshift dsdl2 error isw iswold chi lambda s index
+ * Surface record (20 doubles), what FillMap reads at each surface
+ * (src/hmaps.h:612-676):
+ *   firstid f x y z distance A11 A12 A22 t a redshift chi lambda s isw rho phi
+ *   rho_max valid
+ * A = the infinitesimal Jacobian (src/lensing.h:459-469), A21 = A12. */
+
+int mpf_version(void);
+const char* mpf_last_error(void);
+int mpf_device_count(void);
+
+/* Octree upload from cone records (48 bytes each, sorted by key): the
+ * in-memory image the reference reads with Input::load (src/input.h:1297-1313)
+ * and searches with SimpleHyperOctree::locate/cic/tsc
+ * (src/magrathea/simplehyperoctree.h:874-899, 1410-1644). */
+int mpf_octree_upload(const void* records, int64_t n, mpf_octree** out);
+/* Same, reading a cone .bin file (Miscellaneous::loadOctree, src/miscellaneous.h:422-449). */
+int mpf_octree_load(const char* path, mpf_octree** out);
+int mpf_octree_get_info(const mpf_octree* o, mpf_octree_info* info);
+void mpf_octree_destroy(mpf_octree* o);
+
+/* Cosmology table: conformal time, a, da/dt, d2a/dt2 rows as returned by
+ * Input::acquire + Input::correct (src/input.h:1090-1224, 1329-1360). */
+int mpf_cosmology_upload(const double* t, const double* a, const double* dadt, const double* d2adt2, int64_t n,
+                         mpf_cosmology** out);
+void mpf_cosmology_destroy(mpf_cosmology* c);
+
+/* SimpleHyperOctree::locate: index of the cell (position in the sorted
+ * records) or -1, for n positions xyz[3n]. */
+int mpf_locate(const mpf_octree* o, int64_t n, const double* xyz, int64_t* cell);
+
+/* SimpleHyperOctree::cic (order 1) / tsc (order 2): 7 floats per position in
+ * the order rho phi dphidx dphidy dphidz a dphidt. */
+int mpf_interpolate(const mpf_octree* o, int order, int exact, int64_t n, const double* xyz, float* out7);
+
+/* Integrator::launch (6-argument form) + Integrator::integrate with a stop
+ * criterion (src/integrator.h:648-824) + Lensing::dbetadtheta_infinitesimal
+ * (src/lensing.h:399-472) at each surface, for n rays; the per-pixel body of
+ * Hmaps::FillMap (src/hmaps.h:583-700) and of the catalogue Newton step.
+ * launch[6n]: start x y z, end x y z (direction = end - start).
+ * Outputs (host, each may be NULL): steps[n] = trajectory size,
+ * final_rec[28n] = last trajectory point, plane_rec[20 * nplanes * n]. */
+int mpf_propagate(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t n, const double* launch,
+                  int64_t* steps, double* final_rec, double* plane_rec);
+
+/* Same with device buffers, asynchronous on `stream` (a cudaStream_t, or NULL
+ * for the legacy default stream).  status_device: one uint32 in device memory
+ * that receives warning bits (bit 0: max_steps reached). */
+int mpf_propagate_device(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t n,
+                         const double* launch_device, int64_t* steps_device, double* final_device,
+                         double* plane_device, uint32_t* status_device, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,148 @@
+"""GB300 photon-propagation path of Magrathea-Pathfinder (host-side mirror).
+
+The compute runs in libmpf_gb300.so (CUDA, sm_103a) through its C ABI
+(include/mpf_gb300.h); this module mirrors the reference's interface for the
+path:
+
+==========================  ==================================================
+reference                   here
+==========================  ==================================================
+Input::load / loadOctree    ``Octree.load(path)`` / ``Octree.from_records``
+SimpleHyperOctree::locate   ``Octree.locate(xyz)``
+SimpleHyperOctree::cic/tsc  ``Octree.cic(xyz)`` / ``Octree.tsc(xyz)``
+Input::acquire+correct      ``Cosmology(t, a, dadt, d2adt2)`` (the table)
+Integrator::integrate       ``propagate(...)`` (batched over rays), with
+ + Lensing::dbetadtheta_     the infinitesimal Jacobian and FillMap's
+   infinitesimal            per-surface values at each surface
+==========================  ==================================================
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import MPF_PHOTON_FIELDS, MPF_PLANE_FIELDS, MpfError
+
+PHOTON_FIELDS = ("a t x y z dtdl dxdl dydl dzdl level ah rho phi dphidx dphidy dphidz dphidt dphidl "
+                 "laplacian redshift dsdl2 error isw iswold chi lambda s index").split()
+PLANE_FIELDS = ("firstid f x y z distance A11 A12 A22 t a redshift chi lambda s isw rho phi rho_max "
+                "valid").split()
+
+__all__ = ["Octree", "Cosmology", "propagate", "MpfError", "PHOTON_FIELDS", "PLANE_FIELDS", "library"]
+
+
+def library():
+    """The loaded native library (raises ImportError if it is not built)."""
+    return capi.load()
+
+
+class Octree:
+    """Device octree (cone records sorted by 128-bit key)."""
+
+    def __init__(self, handle):
+        self._h = handle
+        self._lib = capi.load()
+
+    @classmethod
+    def from_records(cls, records: np.ndarray) -> "Octree":
+        L = capi.load()
+        rec = np.ascontiguousarray(records)
+        if rec.dtype.itemsize != 48:
+            raise ValueError("records must be 48-byte cone records")
+        h = C.c_void_p()
+        capi.check(L.mpf_octree_upload(capi.ptr(rec), rec.shape[0], C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def load(cls, path: str) -> "Octree":
+        L = capi.load()
+        h = C.c_void_p()
+        capi.check(L.mpf_octree_load(path.encode(), C.byref(h)))
+        return cls(h)
+
+    @property
+    def info(self) -> dict:
+        i = capi.OctreeInfo()
+        capi.check(self._lib.mpf_octree_get_info(self._h, C.byref(i)))
+        return dict(cells=i.cells, nodes=i.nodes, level_min=i.level_min, level_max=i.level_max,
+                    top_level=i.top_level, grid=tuple(i.grid), device_bytes=i.device_bytes)
+
+    def locate(self, xyz) -> np.ndarray:
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(xyz.shape[0], dtype=np.int64)
+        capi.check(self._lib.mpf_locate(self._h, xyz.shape[0], capi.ptr(xyz), capi.ptr(out)))
+        return out
+
+    def _interp(self, order, xyz, exact):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((xyz.shape[0], 7), dtype=np.float32)
+        capi.check(self._lib.mpf_interpolate(self._h, order, int(bool(exact)), xyz.shape[0], capi.ptr(xyz),
+                                             capi.ptr(out)))
+        return out
+
+    def cic(self, xyz, exact: bool = True) -> np.ndarray:
+        """rho phi dphidx dphidy dphidz a dphidt at each position."""
+        return self._interp(1, xyz, exact)
+
+    def tsc(self, xyz, exact: bool = True) -> np.ndarray:
+        return self._interp(2, xyz, exact)
+
+    def close(self):
+        if self._h:
+            self._lib.mpf_octree_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Cosmology:
+    """Conformal time / scale factor table on the device."""
+
+    def __init__(self, t, a, dadt, d2adt2=None):
+        L = capi.load()
+        self._arr = [np.ascontiguousarray(v, dtype=np.float64) for v in
+                     (t, a, dadt, d2adt2 if d2adt2 is not None else np.zeros(len(t)))]
+        h = C.c_void_p()
+        capi.check(L.mpf_cosmology_upload(*[capi.ptr(v) for v in self._arr], self._arr[0].shape[0], C.byref(h)))
+        self._h = h
+        self._lib = L
+
+    def close(self):
+        if self._h:
+            self._lib.mpf_cosmology_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def propagate(octree: Octree, cosmology: Cosmology, launch, length: float, nsteps: int = 10, order: int = 2,
+              stop: str = "redshift", stop_value: float = 0.0, planes=None, jacobian: bool = True,
+              exact: bool = False, max_steps: int = 0, plane_normal=(0.0, 0.0, 0.0), want_final: bool = True):
+    """Integrate rays launched from launch[:, 0:3] toward launch[:, 3:6].
+
+    Returns (steps[n], final[n, 28] or None, planes[n, nplanes, 20] or None, status).
+    """
+    L = capi.load()
+    launch = np.ascontiguousarray(launch, dtype=np.float64).reshape(-1, 6)
+    n = launch.shape[0]
+    p, keep = capi.make_params(length, nsteps, order, stop, stop_value, planes, jacobian, exact, max_steps,
+                               plane_normal)
+    steps = np.zeros(n, dtype=np.int64)
+    final = np.zeros((n, MPF_PHOTON_FIELDS)) if want_final else None
+    np_ = p.nplanes
+    pout = np.zeros((n, np_, MPF_PLANE_FIELDS)) if np_ > 0 else None
+    rc = L.mpf_propagate(octree._h, cosmology._h, C.byref(p), n, capi.ptr(launch), capi.ptr(steps),
+                         capi.ptr(final), capi.ptr(pout))
+    capi.check(rc)
+    del keep
+    return steps, final, pout, rc

@@ -1,0 +1,118 @@
+"""ctypes binding of libmpf_gb300.so (declarations: include/mpf_gb300.h).
+
+The binding loads the in-tree library and fails loudly when it is missing:
+there is no CPU fallback on this path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmpf_gb300.so")
+
+MPF_PHOTON_FIELDS = 28
+MPF_PLANE_FIELDS = 20
+MPF_MAX_PLANES = 16
+
+STATUS = {0: "MPF_OK", 1: "MPF_WARN_MAX_STEPS", -1: "MPF_BAD_INPUT", -2: "MPF_OUT_OF_MEMORY", -3: "MPF_CUDA_ERROR",
+          -4: "MPF_NOT_SORTED", -5: "MPF_NO_DEVICE", -6: "MPF_IO_ERROR"}
+
+STOP = {"redshift": 0, "r": 1, "radius": 1, "lambda": 2, "t": 3, "eta": 3, "a": 4, "plane": 5, "s": 6}
+
+# every symbol include/mpf_gb300.h declares
+EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_upload", "mpf_octree_load",
+           "mpf_octree_get_info", "mpf_octree_destroy", "mpf_cosmology_upload", "mpf_cosmology_destroy", "mpf_locate",
+           "mpf_interpolate", "mpf_propagate", "mpf_propagate_device")
+
+
+class MpfError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (%d): %s" % (STATUS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class OctreeInfo(C.Structure):
+    _fields_ = [("cells", C.c_int64), ("nodes", C.c_int64), ("level_min", C.c_int), ("level_max", C.c_int),
+                ("top_level", C.c_int), ("grid", C.c_int * 3), ("device_bytes", C.c_int64)]
+
+
+class Params(C.Structure):
+    _fields_ = [("length", C.c_double), ("stop_value", C.c_double), ("plane_normal", C.c_double * 3),
+                ("planes", C.c_void_p), ("nplanes", C.c_int), ("nsteps", C.c_uint), ("order", C.c_int),
+                ("stop", C.c_int), ("jacobian", C.c_int), ("exact", C.c_int), ("max_steps", C.c_int64)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("libmpf_gb300.so not built: run __graft_entry__.build() (or python %s)"
+                          % os.path.join(HERE, "build.py"))
+    L = C.CDLL(path)
+    vp, i64, d = C.c_void_p, C.c_int64, C.c_double
+    L.mpf_version.restype = C.c_int
+    L.mpf_last_error.restype = C.c_char_p
+    L.mpf_device_count.restype = C.c_int
+    L.mpf_octree_upload.argtypes = [vp, i64, C.POINTER(vp)]
+    L.mpf_octree_load.argtypes = [C.c_char_p, C.POINTER(vp)]
+    L.mpf_octree_get_info.argtypes = [vp, C.POINTER(OctreeInfo)]
+    L.mpf_octree_destroy.argtypes = [vp]
+    L.mpf_octree_destroy.restype = None
+    L.mpf_cosmology_upload.argtypes = [vp, vp, vp, vp, i64, C.POINTER(vp)]
+    L.mpf_cosmology_destroy.argtypes = [vp]
+    L.mpf_cosmology_destroy.restype = None
+    L.mpf_locate.argtypes = [vp, i64, vp, vp]
+    L.mpf_interpolate.argtypes = [vp, C.c_int, C.c_int, i64, vp, vp]
+    L.mpf_propagate.argtypes = [vp, vp, C.POINTER(Params), i64, vp, vp, vp, vp]
+    L.mpf_propagate_device.argtypes = [vp, vp, C.POINTER(Params), i64, vp, vp, vp, vp, vp, vp]
+    for name in EXPORTS:
+        if name not in ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_destroy",
+                        "mpf_cosmology_destroy"):
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(code: int, allow_warning: bool = True) -> int:
+    if code < 0 or (code > 0 and not allow_warning):
+        msg = _lib.mpf_last_error().decode(errors="replace") if _lib is not None else ""
+        raise MpfError(code, msg)
+    return code
+
+
+def ptr(a) -> C.c_void_p:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return C.c_void_p(a.ctypes.data)
+    return C.c_void_p(int(a))
+
+
+def make_params(length, nsteps=10, order=2, stop="redshift", stop_value=0.0, planes=None, jacobian=True, exact=False,
+                max_steps=0, plane_normal=(0.0, 0.0, 0.0)):
+    """Params struct plus the array that must outlive the call."""
+    pl = np.ascontiguousarray(planes if planes is not None else np.zeros(0), dtype=np.float64)
+    if pl.shape[0] > MPF_MAX_PLANES:
+        raise ValueError("at most %d surfaces" % MPF_MAX_PLANES)
+    p = Params()
+    p.length = float(length)
+    p.stop_value = float(stop_value)
+    for k in range(3):
+        p.plane_normal[k] = float(plane_normal[k])
+    p.planes = pl.ctypes.data if pl.shape[0] else None
+    p.nplanes = int(pl.shape[0])
+    p.nsteps = int(nsteps)
+    p.order = int(order)
+    p.stop = STOP[stop] if isinstance(stop, str) else int(stop)
+    p.jacobian = int(bool(jacobian))
+    p.exact = int(bool(exact))
+    p.max_steps = int(max_steps)
+    return p, pl

@@ -1,0 +1,259 @@
+// C ABI of the photon-propagation path (declarations: include/mpf_gb300.h).
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mpf_gb300.h"
+#include "mpf_internal.h"
+
+extern "C" int mpf_internal_octree_build(const void* records, int64_t n, int on_device, cudaStream_t stream,
+                                         mpf_octree** out, char* err, int errlen);
+
+namespace mpf {
+cudaError_t launch_gather_exact(const DevTree& T, int kind, const double* d_xyz, long long n, void* d_out, cudaStream_t s);
+cudaError_t launch_gather_fast(const DevTree& T, int kind, const double* d_xyz, long long n, void* d_out, cudaStream_t s);
+}  // namespace mpf
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+int cuda_err(cudaError_t e, const char* where)
+{
+    return set_err(e == cudaErrorMemoryAllocation ? MPF_OUT_OF_MEMORY : MPF_CUDA_ERROR,
+                   std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+bool has_device()
+{
+    int n = 0;
+    return cudaGetDeviceCount(&n) == cudaSuccess && n > 0;
+}
+
+// RAII device buffer
+struct DBuf {
+    void* p = nullptr;
+    cudaError_t alloc(size_t bytes)
+    {
+        if (bytes == 0) return cudaSuccess;
+        return cudaMalloc(&p, bytes);
+    }
+    ~DBuf()
+    {
+        if (p) cudaFree(p);
+    }
+};
+
+bool fill_params(const mpf_params* p, mpf::PropParams& P)
+{
+    if (!p || p->nsteps == 0 || (p->order != 1 && p->order != 2) || p->stop < 0 || p->stop > 6 || p->nplanes < 0 ||
+        p->nplanes > MPF_MAX_PLANES || !(p->length > 0.0))
+        return false;
+    if (p->nplanes > 0 && !p->planes) return false;
+    if (p->nplanes > 0 && p->stop == MPF_STOP_PLANE) return false;
+    std::memset(&P, 0, sizeof(P));
+    P.length = p->length;
+    P.stop_ref = (p->nplanes > 0) ? p->planes[p->nplanes - 1] : p->stop_value;
+    for (int k = 0; k < 3; ++k) P.ki[k] = p->plane_normal[k];
+    for (int k = 0; k < p->nplanes; ++k) P.planes[k] = p->planes[k];
+    P.max_steps = (p->max_steps > 0) ? p->max_steps : 100000000ll;
+    P.nsteps = p->nsteps;
+    P.order = p->order;
+    P.stop_kind = p->stop;
+    P.nplanes = p->nplanes;
+    P.jacobian = p->jacobian ? 1 : 0;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpf_version(void) { return 1; }
+
+const char* mpf_last_error(void) { return g_err.c_str(); }
+
+int mpf_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+int mpf_octree_upload(const void* records, int64_t n, mpf_octree** out)
+{
+    if (!records || n <= 0 || !out) return set_err(MPF_BAD_INPUT, "mpf_octree_upload: null buffer or empty octree");
+    if (!has_device()) return set_err(MPF_NO_DEVICE, "mpf_octree_upload: no CUDA device");
+    char err[256] = {0};
+    const int rc = mpf_internal_octree_build(records, n, 0, 0, out, err, sizeof(err));
+    if (rc == 0) return MPF_OK;
+    const int code = (rc == -2) ? MPF_OUT_OF_MEMORY : (rc == -3) ? MPF_CUDA_ERROR : (rc == -4) ? MPF_NOT_SORTED : MPF_BAD_INPUT;
+    return set_err(code, std::string("mpf_octree_upload: ") + err);
+}
+
+int mpf_octree_load(const char* path, mpf_octree** out)
+{
+    if (!path || !out) return set_err(MPF_BAD_INPUT, "mpf_octree_load: null argument");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return set_err(MPF_IO_ERROR, std::string("mpf_octree_load: cannot open ") + path);
+    std::fseek(f, 0, SEEK_END);
+    const long long size = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    if (size <= 0 || size % 48 != 0) {
+        std::fclose(f);
+        return set_err(MPF_IO_ERROR, std::string("mpf_octree_load: size is not a multiple of 48 bytes: ") + path);
+    }
+    std::vector<unsigned char> buf((size_t)size);
+    const size_t got = std::fread(buf.data(), 1, (size_t)size, f);
+    std::fclose(f);
+    if (got != (size_t)size) return set_err(MPF_IO_ERROR, std::string("mpf_octree_load: short read: ") + path);
+    return mpf_octree_upload(buf.data(), size / 48, out);
+}
+
+int mpf_octree_get_info(const mpf_octree* o, mpf_octree_info* info)
+{
+    if (!o || !info) return set_err(MPF_BAD_INPUT, "mpf_octree_get_info: null argument");
+    info->cells = o->n;
+    info->nodes = o->nnodes;
+    info->level_min = o->level_min;
+    info->level_max = o->level_max;
+    info->top_level = o->tree.Lt;
+    info->grid[0] = o->tree.gnx;
+    info->grid[1] = o->tree.gny;
+    info->grid[2] = o->tree.gnz;
+    info->device_bytes = o->n * (int64_t)(sizeof(ulonglong2) + 2 * sizeof(float4)) + o->nnodes * (int64_t)sizeof(int2) +
+                         (int64_t)o->tree.gnx * o->tree.gny * o->tree.gnz * (int64_t)sizeof(int);
+    return MPF_OK;
+}
+
+void mpf_octree_destroy(mpf_octree* o)
+{
+    if (!o) return;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(o->device);
+    cudaFree(o->keys);
+    cudaFree(o->grad);
+    cudaFree(o->scal);
+    cudaFree(o->node);
+    cudaFree(o->grid);
+    cudaSetDevice(cur);
+    delete o;
+}
+
+int mpf_cosmology_upload(const double* t, const double* a, const double* dadt, const double* d2adt2, int64_t n,
+                         mpf_cosmology** out)
+{
+    if (!t || !a || !dadt || n <= 0 || n > (1 << 30) || !out) return set_err(MPF_BAD_INPUT, "mpf_cosmology_upload: bad table");
+    if (!has_device()) return set_err(MPF_NO_DEVICE, "mpf_cosmology_upload: no CUDA device");
+    mpf_cosmology* c = new mpf_cosmology();
+    cudaGetDevice(&c->device);
+    c->n = (int)n;
+    const size_t bytes = (size_t)n * sizeof(double);
+    cudaError_t e = cudaMalloc(&c->t, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->a, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->dadt, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d2adt2, bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(c->t, t, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->a, a, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->dadt, dadt, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = d2adt2 ? cudaMemcpy(c->d2adt2, d2adt2, bytes, cudaMemcpyHostToDevice) : cudaMemset(c->d2adt2, 0, bytes);
+    if (e != cudaSuccess) {
+        mpf_cosmology_destroy(c);
+        return cuda_err(e, "mpf_cosmology_upload");
+    }
+    *out = c;
+    return MPF_OK;
+}
+
+void mpf_cosmology_destroy(mpf_cosmology* c)
+{
+    if (!c) return;
+    cudaFree(c->t);
+    cudaFree(c->a);
+    cudaFree(c->dadt);
+    cudaFree(c->d2adt2);
+    delete c;
+}
+
+static int gather_host(const mpf_octree* o, int kind, int exact, int64_t n, const double* xyz, void* out, size_t out_elem)
+{
+    if (!o || n < 0 || (n > 0 && (!xyz || !out))) return set_err(MPF_BAD_INPUT, "gather: bad argument");
+    if (n == 0) return MPF_OK;
+    DBuf dx, dout;
+    cudaError_t e = dx.alloc((size_t)n * 3 * sizeof(double));
+    if (e == cudaSuccess) e = dout.alloc((size_t)n * out_elem);
+    if (e == cudaSuccess) e = cudaMemcpy(dx.p, xyz, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = exact ? mpf::launch_gather_exact(o->tree, kind, (const double*)dx.p, n, dout.p, 0)
+                  : mpf::launch_gather_fast(o->tree, kind, (const double*)dx.p, n, dout.p, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout.p, (size_t)n * out_elem, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(e, "gather");
+    return MPF_OK;
+}
+
+int mpf_locate(const mpf_octree* o, int64_t n, const double* xyz, int64_t* cell)
+{
+    return gather_host(o, 0, 1, n, xyz, cell, sizeof(int64_t));
+}
+
+int mpf_interpolate(const mpf_octree* o, int order, int exact, int64_t n, const double* xyz, float* out7)
+{
+    if (order != 1 && order != 2) return set_err(MPF_BAD_INPUT, "mpf_interpolate: order must be 1 (CIC) or 2 (TSC)");
+    return gather_host(o, order, exact, n, xyz, out7, 7 * sizeof(float));
+}
+
+int mpf_propagate_device(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t n,
+                         const double* launch_device, int64_t* steps_device, double* final_device, double* plane_device,
+                         uint32_t* status_device, void* stream)
+{
+    mpf::PropParams P;
+    if (!o || !c || !fill_params(p, P) || n < 0 || (n > 0 && (!launch_device || !steps_device || !status_device)))
+        return set_err(MPF_BAD_INPUT, "mpf_propagate_device: bad argument");
+    mpf::DevCosmo C{c->t, c->a, c->dadt, c->n};
+    mpf::PropOut O{(long long*)steps_device, final_device, plane_device, (unsigned*)status_device};
+    const cudaError_t e = p->exact ? mpf::launch_propagate<true>(o->tree, C, P, launch_device, n, O, (cudaStream_t)stream)
+                                   : mpf::launch_propagate<false>(o->tree, C, P, launch_device, n, O, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_err(e, "mpf_propagate_device");
+    return MPF_OK;
+}
+
+int mpf_propagate(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t n, const double* launch,
+                  int64_t* steps, double* final_rec, double* plane_rec)
+{
+    mpf::PropParams P;
+    if (!o || !c || !fill_params(p, P) || n < 0 || (n > 0 && !launch))
+        return set_err(MPF_BAD_INPUT, "mpf_propagate: bad argument");
+    if (n == 0) return MPF_OK;
+    const int np = p->nplanes;
+    DBuf dl, ds, df, dp, dst;
+    cudaError_t e = dl.alloc((size_t)n * 6 * sizeof(double));
+    if (e == cudaSuccess) e = ds.alloc((size_t)n * sizeof(int64_t));
+    if (e == cudaSuccess && final_rec) e = df.alloc((size_t)n * MPF_PHOTON_FIELDS * sizeof(double));
+    if (e == cudaSuccess && plane_rec && np > 0) e = dp.alloc((size_t)n * np * MPF_PLANE_FIELDS * sizeof(double));
+    if (e == cudaSuccess) e = dst.alloc(sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(dst.p, 0, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpy(dl.p, launch, (size_t)n * 6 * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_err(e, "mpf_propagate");
+    int rc = mpf_propagate_device(o, c, p, n, (const double*)dl.p, (int64_t*)ds.p, (double*)df.p, (double*)dp.p,
+                                  (uint32_t*)dst.p, nullptr);
+    if (rc != MPF_OK) return rc;
+    uint32_t status = 0;
+    e = cudaMemcpy(&status, dst.p, sizeof(status), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && steps) e = cudaMemcpy(steps, ds.p, (size_t)n * sizeof(int64_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && final_rec) e = cudaMemcpy(final_rec, df.p, (size_t)n * MPF_PHOTON_FIELDS * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && plane_rec && np > 0)
+        e = cudaMemcpy(plane_rec, dp.p, (size_t)n * np * MPF_PLANE_FIELDS * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(e, "mpf_propagate");
+    if (status & 1u) return set_err(MPF_WARN_MAX_STEPS, "mpf_propagate: a ray reached max_steps");
+    return MPF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,43 @@
+// Internal host-side structures shared by the CUDA translation units.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mpf_device.cuh"
+#include "mpf_propagate.cuh"
+
+struct mpf_octree {
+    int device;
+    int64_t n;
+    int64_t nnodes;
+    int level_min, level_max;
+    mpf::DevTree tree;       // device pointers inside
+    ulonglong2* keys;
+    float4* grad;
+    float4* scal;
+    int2* node;
+    int* grid;
+};
+
+struct mpf_cosmology {
+    int device;
+    int n;
+    double* t;
+    double* a;
+    double* dadt;
+    double* d2adt2;
+};
+
+namespace mpf {
+
+// exclusive scan of n int32 values in place on `stream`; returns the total
+int64_t exclusive_scan(int* d, int64_t n, cudaStream_t stream);
+
+template <bool EXACT>
+cudaError_t launch_propagate(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* d_launch, long long n,
+                             const PropOut& O, cudaStream_t stream);
+
+cudaError_t launch_gather(const DevTree& T, int kind, bool exact, const double* d_xyz, long long n, void* d_out,
+                          cudaStream_t stream);
+
+}  // namespace mpf

@@ -39,4 +39,6 @@ done
 pids+=($!)
 rc=0
 for p in "${pids[@]}"; do wait "$p" || rc=1; done
+# keep only the built binaries in oracle/_ref/
+rm -rf "$OUT/patched"
 exit $rc

@@ -1,0 +1,40 @@
+"""CPU tests of the C ABI library: it builds, loads, exports every declared
+symbol, and reports errors as status codes (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from conftest import ROOT, PKG
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "mpf_gb300.h")).read()
+    decl = r"^\s*(?:int|void|const\s+char\s*\*|int64_t|uint32_t)\s*\**\s*(mpf_[a-z_0-9]+)\s*\("
+    return sorted(set(re.findall(decl, src, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol(pkg):
+    import importlib
+    importlib.import_module(PKG + ".build").build()
+    L = pkg.library()
+    names = declared_symbols()
+    assert len(names) >= 10
+    for name in names:
+        assert hasattr(L, name), name
+    from importlib import import_module
+    capi = import_module(PKG + ".capi")
+    assert set(capi.EXPORTS) == set(names)
+
+
+def test_bad_input_is_a_status_not_a_crash(pkg):
+    L = pkg.library()
+    h = ctypes.c_void_p()
+    assert L.mpf_octree_upload(None, 0, ctypes.byref(h)) == -1
+    assert b"null" in L.mpf_last_error() or b"empty" in L.mpf_last_error()
+    rc = L.mpf_octree_load(b"/nonexistent/cone.bin", ctypes.byref(h))
+    assert rc == -6
+    if L.mpf_device_count() == 0:
+        rec = np.zeros(2, dtype=np.dtype([("b", "u1", 48)]))
+        assert L.mpf_octree_upload(ctypes.c_void_p(rec.ctypes.data), 2, ctypes.byref(h)) == -5

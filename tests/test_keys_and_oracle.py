@@ -1,0 +1,61 @@
+"""CPU tests: the key arithmetic and the C oracle against the reference's own
+outputs recorded in tests/golden (bit-exact)."""
+import numpy as np
+import pytest
+
+
+def test_keys_match_reference(golden, synth):
+    for lvl, pos, ref in zip(golden["key_level"], golden["key_pos"], golden["key_ref"]):
+        hi, lo = synth.compute_key(int(lvl), pos[None])
+        assert (int(hi[0]), int(lo[0])) == (int(ref[0]), int(ref[1])), (lvl, pos)
+    hi, lo = golden["records"]["hi"], golden["records"]["lo"]
+    lev = synth.key_level(hi, lo)
+    assert lev.min() >= 0 and lev.max() <= 32
+    # records strictly increasing by key (the reference's sorted container)
+    assert np.all((hi[1:] > hi[:-1]) | ((hi[1:] == hi[:-1]) & (lo[1:] > lo[:-1])))
+
+
+def _oracle(golden, oracle_mod):
+    cos = {k: golden["cosmo_" + k] for k in ("t", "a", "dadt")}
+    return oracle_mod.Oracle(golden["records"], cos, float(golden["cosmo_length"]))
+
+
+def test_oracle_gathers_bit_exact(golden, oracle_mod):
+    O = _oracle(golden, oracle_mod)
+    pts = golden["pts"]
+    np.testing.assert_array_equal(O.locate(pts), golden["ref_locate"])
+    np.testing.assert_array_equal(O.cic(pts).view(np.uint32), golden["ref_cic"].view(np.uint32))
+    np.testing.assert_array_equal(O.tsc(pts).view(np.uint32), golden["ref_tsc"].view(np.uint32))
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_oracle_integrate_bit_exact(golden, oracle_mod, order):
+    O = _oracle(golden, oracle_mod)
+    steps, final, _ = O.propagate(golden["launch"], order=order, nsteps=int(golden["nsteps"]), stop="redshift",
+                                  stop_ref=float(golden["zs"][-1]))
+    np.testing.assert_array_equal(steps, golden["ref_steps_o%d" % order])
+    np.testing.assert_array_equal(final.view(np.uint64), golden["ref_final_o%d" % order].view(np.uint64))
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_oracle_maps_bit_exact(golden, oracle_mod, maps_mod, order):
+    O = _oracle(golden, oracle_mod)
+    dirs = golden["pixel_dirs"]
+    launch = np.zeros((dirs.shape[0], 6))
+    launch[:, 3:] = dirs
+    _, _, planes = O.propagate(launch, order=order, nsteps=int(golden["nsteps"]), stop="redshift",
+                               planes=golden["zs"], jacobian=True)
+    comps = str(golden["components"]).split(",")
+    maps = maps_mod.assemble(planes, dirs, golden["homogeneous"], comps)
+    ref = golden["ref_maps_o%d" % order]
+    assert maps.shape == ref.shape
+    np.testing.assert_array_equal(maps.view(np.uint32), ref.view(np.uint32))
+
+
+def test_amr_fixture_exercises_levels(synth):
+    from conftest import load_golden
+    g = load_golden("amr")
+    lev = synth.key_level(g["records"]["hi"], g["records"]["lo"])
+    assert lev.max() - lev.min() >= 3
+    # some reference rays end in refined cells and some are longer than uniform ones
+    assert len(np.unique(g["ref_final_o2"][:, 9])) >= 2
