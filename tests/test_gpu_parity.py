@@ -102,8 +102,11 @@ def test_maps_against_reference_fillmap(dev, golden, pkg, maps_mod, order, exact
     got = maps_mod.assemble(planes, dirs, golden["homogeneous"], comps)
     ref = golden["ref_maps_o%d" % order]
     assert got.shape == ref.shape
-    valid_ref = ref[:, 5] != 0            # dz row is nonzero exactly where the surface was valid
-    valid_got = got[:, 5] != 0
+    # the steps row (firstid) is >= 1 exactly where the surface was valid, 0 elsewhere
+    assert comps[0] == "lensing"
+    srow = 4 + comps.index("steps") - 1          # lensing fills rows 0-3, one row per component after it
+    valid_ref = ref[:, srow] != 0
+    valid_got = got[:, srow] != 0
     np.testing.assert_array_equal(valid_got, valid_ref)
     # lensing rows: kappa gamma1 gamma2 (small) and 1/mu (~1)
     for row, tol in ((0, 1e-9), (1, 1e-9), (2, 1e-9), (3, 1e-9)):
