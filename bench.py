@@ -183,6 +183,8 @@ def main():
     ap.add_argument("--small", action="store_true", help="small octree (debug only)")
     ap.add_argument("--exact", action="store_true", help="reference float64 gather order")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--zstop", type=float, default=2.0, help="stop redshift (profiling captures use a short path)")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     synth = importlib.import_module(PKG + ".synth")
@@ -190,12 +192,12 @@ def main():
     config = {"workload": "AMR cone octree, 256^3 base (level 10) refined to level 14 in 2000 NFW haloes; "
                           "1000x1000 rays over 10x10 deg to z=2; TSC, 8 steps/cell, infinitesimal Jacobian at z=2"
                           if not args.small else "small debug octree",
-              "rays": 1000 * 1000, "batch_rays": args.batch, "order": "TSC", "nsteps": 8, "z_stop": 2.0,
+              "rays": 1000 * 1000, "batch_rays": args.batch, "order": "TSC", "nsteps": 8, "z_stop": args.zstop,
               "gather_arithmetic": "float64 reference order" if args.exact else "fp32 gather, fp64 state",
               "l2": "octree larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single GPU"}
     cos = cosmology_table(synth)
     length = spec.lbox * synth.MPC / spec.cosmo.h
-    planes = np.array([2.0])
+    planes = np.array([args.zstop])
 
     if args.impl == "reference":
         if rank != 0:
@@ -297,10 +299,9 @@ def main():
 
     # end to end through the public API: host launch records in, host steps and
     # surface records out, every step
-    h_launch = np.ascontiguousarray(launch[:B])
     e2e_t = []
     e2e_steps = 0
-    for k in range(max(2, min(args.steps, 3))):
+    for k in range(0 if args.no_e2e else max(2, min(args.steps, 3))):
         off = ((k + 1) % nb) * B
         h = np.ascontiguousarray(launch[off:off + B])
         torch.cuda.synchronize()
@@ -309,8 +310,7 @@ def main():
                                      jacobian=True, exact=args.exact, want_final=False)
         e2e_t.append(time.perf_counter() - t0)
         e2e_steps += int(st.sum())
-    e2e_value = e2e_steps / sum(e2e_t)
-    del h_launch
+    e2e_value = e2e_steps / sum(e2e_t) if e2e_t else None
 
     peak, peak_kind = measured_peak_hbm()
     avg_launch_s = (sum(per_launch) / len(per_launch)) / 1000.0

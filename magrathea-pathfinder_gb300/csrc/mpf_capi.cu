@@ -1,5 +1,6 @@
 // C ABI of the photon-propagation path (declarations: include/mpf_gb300.h).
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -151,20 +152,46 @@ void mpf_octree_destroy(mpf_octree* o)
 int mpf_cosmology_upload(const double* t, const double* a, const double* dadt, const double* d2adt2, int64_t n,
                          mpf_cosmology** out)
 {
-    if (!t || !a || !dadt || n <= 0 || n > (1 << 30) || !out) return set_err(MPF_BAD_INPUT, "mpf_cosmology_upload: bad table");
+    if (!t || !a || !dadt || n <= 0 || n > (1 << 28) || !out) return set_err(MPF_BAD_INPUT, "mpf_cosmology_upload: bad table");
+    for (int64_t i = 1; i < n; ++i)
+        if (!(t[i] > t[i - 1])) return set_err(MPF_BAD_INPUT, "mpf_cosmology_upload: conformal time must increase");
     if (!has_device()) return set_err(MPF_NO_DEVICE, "mpf_cosmology_upload: no CUDA device");
     mpf_cosmology* c = new mpf_cosmology();
     cudaGetDevice(&c->device);
     c->n = (int)n;
+    // search accelerator and slopes for the FP32-gather mode
+    c->nlut = (int)std::min<int64_t>(4 * n, 1 << 20);
+    c->t0 = t[0];
+    c->lut_scale = (n > 1) ? (double)c->nlut / (t[n - 1] - t[0]) : 0.0;
+    std::vector<int> lut((size_t)c->nlut + 1);
+    {
+        int64_t i = 0;
+        for (int k = 0; k <= c->nlut; ++k) {
+            const double x = c->t0 + (double)k / (c->lut_scale > 0 ? c->lut_scale : 1.0);
+            while (i < n && !(x < t[i])) ++i;
+            lut[(size_t)k] = (int)i;
+        }
+    }
+    std::vector<double> sa((size_t)n, 0.0), sd((size_t)n, 0.0);
+    for (int64_t i = 0; i + 1 < n; ++i) {
+        sa[(size_t)i] = (a[i + 1] - a[i]) / (t[i + 1] - t[i]);
+        sd[(size_t)i] = (dadt[i + 1] - dadt[i]) / (t[i + 1] - t[i]);
+    }
     const size_t bytes = (size_t)n * sizeof(double);
     cudaError_t e = cudaMalloc(&c->t, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&c->a, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&c->dadt, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&c->d2adt2, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->slope_a, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->slope_dadt, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->lut, lut.size() * sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpy(c->t, t, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(c->a, a, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(c->dadt, dadt, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = d2adt2 ? cudaMemcpy(c->d2adt2, d2adt2, bytes, cudaMemcpyHostToDevice) : cudaMemset(c->d2adt2, 0, bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(c->slope_a, sa.data(), bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->slope_dadt, sd.data(), bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->lut, lut.data(), lut.size() * sizeof(int), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         mpf_cosmology_destroy(c);
         return cuda_err(e, "mpf_cosmology_upload");
@@ -180,6 +207,9 @@ void mpf_cosmology_destroy(mpf_cosmology* c)
     cudaFree(c->a);
     cudaFree(c->dadt);
     cudaFree(c->d2adt2);
+    cudaFree(c->slope_a);
+    cudaFree(c->slope_dadt);
+    cudaFree(c->lut);
     delete c;
 }
 
@@ -217,7 +247,7 @@ int mpf_propagate_device(const mpf_octree* o, const mpf_cosmology* c, const mpf_
     mpf::PropParams P;
     if (!o || !c || !fill_params(p, P) || n < 0 || (n > 0 && (!launch_device || !steps_device || !status_device)))
         return set_err(MPF_BAD_INPUT, "mpf_propagate_device: bad argument");
-    mpf::DevCosmo C{c->t, c->a, c->dadt, c->n};
+    mpf::DevCosmo C{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
     mpf::PropOut O{(long long*)steps_device, final_device, plane_device, (unsigned*)status_device};
     const cudaError_t e = p->exact ? mpf::launch_propagate<true>(o->tree, C, P, launch_device, n, O, (cudaStream_t)stream)
                                    : mpf::launch_propagate<false>(o->tree, C, P, launch_device, n, O, (cudaStream_t)stream);

@@ -26,6 +26,11 @@ struct mpf_cosmology {
     double* a;
     double* dadt;
     double* d2adt2;
+    int* lut;
+    int nlut;
+    double t0, lut_scale;
+    double* slope_a;
+    double* slope_dadt;
 };
 
 namespace mpf {

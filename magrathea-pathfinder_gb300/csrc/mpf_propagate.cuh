@@ -29,6 +29,13 @@ struct DevCosmo {
     const double* a;
     const double* dadt;
     int n;
+    // fast-mode search accelerator: lut[k] = upper_bound(t, t0 + k / lut_scale),
+    // and per-interval slopes of a and da/dt
+    const int* lut;
+    int nlut;
+    double t0, lut_scale;
+    const double* slope_a;
+    const double* slope_dadt;
 };
 
 struct PropParams {

@@ -118,8 +118,9 @@ def test_maps_against_reference_fillmap(dev, golden, pkg, maps_mod, order, exact
         if exact and row < ref.shape[1] - 2:
             np.testing.assert_array_equal(got[:, row].view(np.uint32), ref[:, row].view(np.uint32), err_msg=str(row))
         else:
+            # dz is ~1e-16 by construction (the surface is a redshift): absolute floor
             scale = np.abs(ref[:, row]).max() + 1e-30
-            assert np.abs(got[:, row] - ref[:, row]).max() <= 2e-6 * scale, row
+            assert np.abs(got[:, row] - ref[:, row]).max() <= 2e-6 * scale + 1e-12, row
 
 
 def test_against_oracle_larger_batch(gpu_lib, pkg, oracle_mod, synth):
