@@ -129,7 +129,7 @@ int mpf_octree_get_info(const mpf_octree* o, mpf_octree_info* info)
     info->grid[0] = o->tree.gnx;
     info->grid[1] = o->tree.gny;
     info->grid[2] = o->tree.gnz;
-    info->device_bytes = o->n * (int64_t)(sizeof(ulonglong2) + 2 * sizeof(float4)) + o->nnodes * (int64_t)sizeof(int2) +
+    info->device_bytes = o->n * (int64_t)(sizeof(ulonglong2) + 2 * sizeof(float4) + 8 * sizeof(int4)) + o->nnodes * (int64_t)sizeof(int2) +
                          (int64_t)o->tree.gnx * o->tree.gny * o->tree.gnz * (int64_t)sizeof(int);
     return MPF_OK;
 }
@@ -145,6 +145,7 @@ void mpf_octree_destroy(mpf_octree* o)
     cudaFree(o->scal);
     cudaFree(o->node);
     cudaFree(o->grid);
+    cudaFree(o->stencil);
     cudaSetDevice(cur);
     delete o;
 }
@@ -248,7 +249,7 @@ int mpf_propagate_device(const mpf_octree* o, const mpf_cosmology* c, const mpf_
     if (!o || !c || !fill_params(p, P) || n < 0 || (n > 0 && (!launch_device || !steps_device || !status_device)))
         return set_err(MPF_BAD_INPUT, "mpf_propagate_device: bad argument");
     mpf::DevCosmo C{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
-    mpf::PropOut O{(long long*)steps_device, final_device, plane_device, (unsigned*)status_device};
+    mpf::PropOut O{(long long*)steps_device, final_device, plane_device, (unsigned*)status_device, nullptr};
     const cudaError_t e = p->exact ? mpf::launch_propagate<true>(o->tree, C, P, launch_device, n, O, (cudaStream_t)stream)
                                    : mpf::launch_propagate<false>(o->tree, C, P, launch_device, n, O, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_err(e, "mpf_propagate_device");

@@ -30,6 +30,14 @@ struct DevTree {
     const float4* scal;
     const int2* node;
     const int* grid;
+    // per-cell stencil records, 8 x int4 (128 B) per cell:
+    //   ints 0..26  the 27 cells of the cell's level around it, x-major
+    //               (ix outer, iz inner), each the reference lookup result
+    //               (deepest existing cell <= that level, or -1)
+    //   int 27      level | has_children << 8
+    //   int 28      bit j set: entry j is at exactly the cell's level
+    //   int 29      node index of the cell
+    const int4* stencil;
     int64_t n;
     int Lt;                // level of the top grid
     int gx0, gy0, gz0;     // grid origin (integer coords at Lt)

@@ -4,21 +4,17 @@
 // fused src/lensing.h:399-472 Jacobian), reorganised for the GB300's
 // arithmetic balance:
 //
-//  * Cell window.  Each ray keeps, in shared memory, the cell indices of the
-//    5x5x5 block of cells of its current level around the cell it is in,
-//    each tagged "has children".  A TSC stencil whose 27 cells are all in the
-//    window at that level, around a leaf centre, is gathered straight from the
-//    window; anything else (refinement boundaries, missing or coarser
-//    neighbours, the origin) falls back to the full lookup, which keeps the
-//    reference's restart semantics.  The window is rebuilt when the ray
-//    enters another cell (every ~8-30 steps), so the steady state does no
-//    octree walks at all.
-//  * The six Jacobian gathers at +-1 cell are the finite differences of TSC
-//    sums over the 5x3x3 boxes of the window; they are evaluated as one sum
-//    with the weight differences, which is the same quantity without the
-//    cancellation of subtracting two TSC values.
-//  * FP64 is kept for the RK4 state, the RHS, affine parameter, redshift and
-//    distances.  Cell coordinates use exact power-of-two scalings (no
+//  * Stencil records.  Every cell carries, in HBM, its 27 same-level
+//    neighbours resolved with the reference's lookup semantics, a mask of the
+//    ones at exactly its level and its level / children flags (built on the
+//    GPU at upload, mpf_octree.cu).  A TSC or CIC gather is then one 128-byte
+//    record load plus the payload loads; a restart at a coarser neighbour
+//    (simplehyperoctree.h:1532-1537) re-centres on the coarser cell's record.
+//    The deepest cell of a point near a known cell is read from that cell's
+//    record, so the RK stages, the post-step gather and the six Jacobian
+//    gathers of a step do no octree walks in the common case.
+//  * FP64 is kept for the RK4 state, the RHS, the affine parameter, redshift
+//    and distances.  Cell coordinates use exact power-of-two scalings (no
 //    divisions), TSC weights and field accumulation are FP32, the cosmology
 //    search uses a uniform index table.
 #pragma once
@@ -26,12 +22,7 @@
 
 namespace mpf {
 
-constexpr int kWin = 5;
-constexpr int kWin3 = kWin * kWin * kWin;
-constexpr int kHasChildren = 1 << 30;
-constexpr int kCellMask = kHasChildren - 1;
-
-__device__ __forceinline__ int widx(int ox, int oy, int oz) { return ((oz + 2) * kWin + (oy + 2)) * kWin + (ox + 2); }
+constexpr unsigned kFullMask = (1u << 27) - 1u;
 
 // Utility::interpolate with the uniform index table (same bracketing interval
 // as the reference's upper_bound; slope precomputed per interval).
@@ -42,8 +33,8 @@ __device__ __forceinline__ double interp_fast(const DevCosmo& C, double x0, cons
     if (x0 < C.t0) {
         i = 0;
     } else {
-        double kk = (x0 - C.t0) * C.lut_scale;
-        int k = (kk < (double)C.nlut) ? (int)kk : C.nlut;
+        const double kk = (x0 - C.t0) * C.lut_scale;
+        const int k = (kk < (double)C.nlut) ? (int)kk : C.nlut;
         i = __ldg(C.lut + k);
         while (i < C.n && !(x0 < __ldg(C.t + i))) ++i;
     }
@@ -53,77 +44,12 @@ __device__ __forceinline__ double interp_fast(const DevCosmo& C, double x0, cons
     return __ldg(y + i - 1) + __ldg(slope + i - 1) * (x0 - __ldg(C.t + i - 1));
 }
 
-struct Win {
-    uint32_t cx, cy, cz;
-    int level;        // -1: no window
-    bool core_ok;     // the 27 cells around the centre exist at `level` and the centre is a leaf
-    bool jac_ok;      // core_ok, the 81-cell cross exists, and the 6 face neighbours are leaves
-};
-
-// The 125 lookups advance together, one tree level per round, so each round
-// is 125 independent loads instead of 125 dependent chains.  The shared-memory
-// slots hold the running node index between rounds.
-__device__ void win_build(const DevTree& T, int L, uint32_t cx, uint32_t cy, uint32_t cz, int* ws, int stride, Win& w)
+__device__ __forceinline__ void tsc_w3(float f, float* w)
 {
-    const uint64_t mask = (L >= 32) ? 0xffffffffull : ((1ull << L) - 1ull);
-    const int sh = L - T.Lt;
-    // round 0: top-grid entries
-    for (int k = 0; k < kWin3; ++k) {
-        const int ox = k % kWin - 2, oy = (k / kWin) % kWin - 2, oz = k / (kWin * kWin) - 2;
-        const uint64_t qx = ((uint64_t)cx + (uint64_t)(int64_t)ox) & mask, qy = ((uint64_t)cy + (uint64_t)(int64_t)oy) & mask,
-                       qz = ((uint64_t)cz + (uint64_t)(int64_t)oz) & mask;
-        int nd = -1;
-        if (sh >= 0) {
-            const long gx = (long)(qx >> sh) - T.gx0, gy = (long)(qy >> sh) - T.gy0, gz = (long)(qz >> sh) - T.gz0;
-            if (gx >= 0 && gy >= 0 && gz >= 0 && gx < T.gnx && gy < T.gny && gz < T.gnz)
-                nd = __ldg(T.grid + ((gz * T.gny + gy) * (long)T.gnx + gx));
-        }
-        ws[k * stride] = nd;
-    }
-    // rounds 1..L-Lt: descend one level; a slot that cannot descend becomes -1
-    for (int l = T.Lt + 1; l <= L; ++l) {
-        const int b = L - l;
-#pragma unroll 5
-        for (int k = 0; k < kWin3; ++k) {
-            int nd = ws[k * stride];
-            if (nd >= 0) {
-                const int child = __ldg(&T.node[nd].x);
-                if (child < 0) nd = -1;
-                else {
-                    const int ox = k % kWin - 2, oy = (k / kWin) % kWin - 2, oz = k / (kWin * kWin) - 2;
-                    const uint64_t qx = ((uint64_t)cx + (uint64_t)(int64_t)ox) & mask, qy = ((uint64_t)cy + (uint64_t)(int64_t)oy) & mask,
-                                   qz = ((uint64_t)cz + (uint64_t)(int64_t)oz) & mask;
-                    nd = child + ((int)((qx >> b) & 1ull) | ((int)((qy >> b) & 1ull) << 1) | ((int)((qz >> b) & 1ull) << 2));
-                }
-                ws[k * stride] = nd;
-            }
-        }
-    }
-    // last round: node -> tagged cell, and the window flags
-    bool core = true, jac = true;
-#pragma unroll 5
-    for (int k = 0; k < kWin3; ++k) {
-        const int nd = ws[k * stride];
-        int e = -1;
-        if (nd >= 0) {
-            const int2 v = __ldg(T.node + nd);
-            if (v.y >= 0) e = v.y | ((v.x >= 0) ? kHasChildren : 0);
-        }
-        ws[k * stride] = e;
-        const int ox = k % kWin - 2, oy = (k / kWin) % kWin - 2, oz = k / (kWin * kWin) - 2;
-        const int ax = abs(ox), ay = abs(oy), az = abs(oz);
-        const bool inner = ax <= 1 && ay <= 1 && az <= 1;
-        const bool cross = (ax <= 2 && ay <= 1 && az <= 1) || (ax <= 1 && ay <= 2 && az <= 1) || (ax <= 1 && ay <= 1 && az <= 2);
-        if (inner && e < 0) core = false;
-        if (cross && e < 0) jac = false;
-        if ((ax + ay + az) <= 1 && (e < 0 || (e & kHasChildren))) {
-            jac = false;
-            if (ax + ay + az == 0) core = false;
-        }
-    }
-    w.cx = cx; w.cy = cy; w.cz = cz; w.level = L;
-    w.core_ok = core;
-    w.jac_ok = core && jac;
+    const float m = 0.5f - f, p = 0.5f + f;
+    w[0] = 0.5f * m * m;
+    w[1] = 0.75f - f * f;
+    w[2] = 0.5f * p * p;
 }
 
 // integer coordinates at level L and the offset of the point from its cell
@@ -140,213 +66,193 @@ __device__ __forceinline__ void point_cell(int L, double x, double y, double z, 
     }
 }
 
-__device__ __forceinline__ void tsc_w3(float f, float* w)
+__device__ __forceinline__ int rec_flags(const DevTree& T, int cell) { return __ldg(&T.stencil[8 * (size_t)cell + 6].w); }
+__device__ __forceinline__ int rec_entry(const DevTree& T, int cell, int j)
 {
-    const float m = 0.5f - f, p = 0.5f + f;
-    w[0] = 0.5f * m * m;
-    w[1] = 0.75f - f * f;
-    w[2] = 0.5f * p * p;
+    return __ldg(reinterpret_cast<const int*>(T.stencil + 8 * (size_t)cell) + j);
 }
 
-// TSC through the window; returns false (and leaves `res` untouched) when the
-// stencil is not fully inside the window at the window's level.
-__device__ __forceinline__ bool tsc_win(const DevTree& T, const Win& w, const int* ws, int stride, double x, double y, double z,
-                                        bool need_all, Field7& res)
+// stats slots
+enum { ST_RK_REC = 0, ST_RK_SLOW, ST_POST_REC, ST_POST_SLOW, ST_JAC_REC, ST_JAC_SLOW, ST_CELL_CHANGE, ST_STEPS, ST_N };
+
+__device__ __forceinline__ void stat(unsigned long long* st, int k)
 {
-    if (w.level < 0) return false;
-    if (x == 0.0 && y == 0.0 && z == 0.0) return false;
+    if (st) atomicAdd(st + k, 1ull);
+}
+
+// Out-of-line slow paths (reference semantics with full walks), single copies
+// so that the hot loop stays small in the instruction cache.
+__device__ __noinline__ Field7 tsc_slow(const DevTree& T, double x, double y, double z, int need_all)
+{
+    return tsc<false>(T, x, y, z, need_all != 0);
+}
+__device__ __noinline__ Field7 cic_slow(const DevTree& T, double x, double y, double z, int need_all)
+{
+    return cic<false>(T, x, y, z, need_all != 0);
+}
+__device__ __noinline__ Found locate_slow(const DevTree& T, double x, double y, double z) { return locate(T, x, y, z); }
+
+// A located point: its deepest cell, that cell's level and the point's
+// integer coordinates at that level.
+struct Loc {
+    int cell;
+    int level;
     uint32_t c[3];
-    float fd[3];
-    point_cell(w.level, x, y, z, c, fd);
-    const int ox = (int)(c[0] - w.cx), oy = (int)(c[1] - w.cy), oz = (int)(c[2] - w.cz);
-    if (abs(ox) > 1 || abs(oy) > 1 || abs(oz) > 1) return false;
-    const int ec = ws[widx(ox, oy, oz) * stride];
-    if (ec < 0 || (ec & kHasChildren)) return false;
-    if (!(w.core_ok && ox == 0 && oy == 0 && oz == 0)) {
-        for (int dz = -1; dz <= 1; ++dz)
-            for (int dy = -1; dy <= 1; ++dy)
-                for (int dx = -1; dx <= 1; ++dx)
-                    if (ws[widx(ox + dx, oy + dy, oz + dz) * stride] < 0) return false;
-    }
-    float wx[3], wy[3], wz[3];
-    tsc_w3(fd[0], wx);
-    tsc_w3(fd[1], wy);
-    tsc_w3(fd[2], wz);
-    float gx = 0.f, gy = 0.f, gz = 0.f, gt = 0.f, rho = 0.f, phi = 0.f, a = 0.f;
-    // x-major order as the reference (ix outermost)
-#pragma unroll
-    for (int ix = 0; ix < 3; ++ix) {
-#pragma unroll
-        for (int iy = 0; iy < 3; ++iy) {
-            const float wxy = wx[ix] * wy[iy];
-#pragma unroll
-            for (int iz = 0; iz < 3; ++iz) {
-                const float wt = wxy * wz[iz];
-                const int cell = ws[widx(ox + ix - 1, oy + iy - 1, oz + iz - 1) * stride] & kCellMask;
-                const float4 g = __ldg(T.grad + cell);
-                gx = fmaf(g.x, wt, gx);
-                gy = fmaf(g.y, wt, gy);
-                gz = fmaf(g.z, wt, gz);
-                gt = fmaf(g.w, wt, gt);
-                if (need_all) {
-                    const float4 s = __ldg(T.scal + cell);
-                    rho = fmaf(s.x, wt, rho);
-                    phi = fmaf(s.y, wt, phi);
-                    a = fmaf(s.z, wt, a);
+};
+
+// Deepest cell of point (x, y, z) given a nearby located cell `h`: read from
+// h's record when the point lies in h or one of its 26 neighbours and that
+// neighbour is a leaf of h's level; otherwise a full walk.
+__device__ __forceinline__ Loc locate_near(const DevTree& T, const Loc& h, double x, double y, double z)
+{
+    Loc r;
+    if (h.cell >= 0) {
+        float fd[3];
+        point_cell(h.level, x, y, z, r.c, fd);
+        const int ox = (int)(r.c[0] - h.c[0]), oy = (int)(r.c[1] - h.c[1]), oz = (int)(r.c[2] - h.c[2]);
+        if (ox == 0 && oy == 0 && oz == 0) {
+            r.cell = h.cell;
+            r.level = h.level;
+            return r;
+        }
+        if (abs(ox) <= 1 && abs(oy) <= 1 && abs(oz) <= 1) {
+            const int e = rec_entry(T, h.cell, (ox + 1) * 9 + (oy + 1) * 3 + (oz + 1));
+            if (e >= 0) {
+                const int fl = rec_flags(T, e);
+                if (!(fl & 256) && (fl & 255) == h.level) {
+                    r.cell = e;
+                    r.level = h.level;
+                    return r;
                 }
             }
         }
     }
-    res = Field7{rho, phi, gx, gy, gz, a, gt};
-    return true;
+    const Found f = locate_slow(T, x, y, z);
+    r.cell = f.cell;
+    r.level = f.level;
+    if (f.cell >= 0) {
+        float fd[3];
+        point_cell(f.level, x, y, z, r.c, fd);
+    }
+    return r;
 }
 
-// Hessian terms of the infinitesimal Jacobian (lensing.h:430-443) from the
-// window: d_ij = [TSC(x + h e_j).dphidi - TSC(x - h e_j).dphidi] / (2h), h = one cell.
-__device__ __forceinline__ void hessian_win(const DevTree& T, const int* ws, int stride, const float* fd, float inv_dl, float* H)
+// TSC at a point whose deepest cell is `cell` (simplehyperoctree.h:1479-1541
+// through the stencil records).  Returns false when a restart centre is not
+// itself a cell (left to the slow path).
+__device__ __forceinline__ bool tsc_rec(const DevTree& T, int cell, int L, double x, double y, double z, bool need_all,
+                                        Field7& res)
 {
-    float wx[3], wy[3], wz[3];
-    tsc_w3(fd[0], wx);
-    tsc_w3(fd[1], wy);
-    tsc_w3(fd[2], wz);
-    // weight differences over 5 cells: (+h stencil) - (-h stencil)
-    const float dx5[5] = {-wx[0], -wx[1], wx[0] - wx[2], wx[1], wx[2]};
-    const float dy5[5] = {-wy[0], -wy[1], wy[0] - wy[2], wy[1], wy[2]};
-    const float dz5[5] = {-wz[0], -wz[1], wz[0] - wz[2], wz[1], wz[2]};
-    float dxx = 0.f, dxy = 0.f, dyy = 0.f, dxz = 0.f, dyz = 0.f, dzz = 0.f;
-    // x box: 5 x 3 x 3
-    for (int i = 0; i < 5; ++i)
-        for (int j = 0; j < 3; ++j)
-            for (int k = 0; k < 3; ++k) {
-                const float4 g = __ldg(T.grad + (ws[widx(i - 2, j - 1, k - 1) * stride] & kCellMask));
-                dxx = fmaf(g.x, dx5[i] * wy[j] * wz[k], dxx);
+    for (int guard = 0; guard <= kMaxLevel; ++guard) {
+        const int4* rp = T.stencil + 8 * (size_t)cell;
+        const int4 r7 = __ldg(rp + 7);
+        const unsigned exact = (unsigned)r7.x;
+        if (exact == kFullMask) {
+            int e[28];
+#pragma unroll
+            for (int q = 0; q < 7; ++q) {
+                const int4 v = __ldg(rp + q);
+                e[4 * q] = v.x; e[4 * q + 1] = v.y; e[4 * q + 2] = v.z; e[4 * q + 3] = v.w;
             }
-    // y box
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 5; ++j)
-            for (int k = 0; k < 3; ++k) {
-                const float4 g = __ldg(T.grad + (ws[widx(i - 1, j - 2, k - 1) * stride] & kCellMask));
-                const float wt = wx[i] * dy5[j] * wz[k];
-                dxy = fmaf(g.x, wt, dxy);
-                dyy = fmaf(g.y, wt, dyy);
+            uint32_t c[3];
+            float fd[3];
+            point_cell(L, x, y, z, c, fd);
+            float wx[3], wy[3], wz[3];
+            tsc_w3(fd[0], wx);
+            tsc_w3(fd[1], wy);
+            tsc_w3(fd[2], wz);
+            float gx = 0.f, gy = 0.f, gz = 0.f, gt = 0.f, rho = 0.f, phi = 0.f, a = 0.f;
+#pragma unroll
+            for (int j = 0; j < 27; ++j) {
+                const float wt = wx[j / 9] * wy[(j / 3) % 3] * wz[j % 3];
+                const float4 g = __ldg(T.grad + e[j]);
+                gx = fmaf(g.x, wt, gx); gy = fmaf(g.y, wt, gy); gz = fmaf(g.z, wt, gz); gt = fmaf(g.w, wt, gt);
+                if (need_all) {
+                    const float4 s = __ldg(T.scal + e[j]);
+                    rho = fmaf(s.x, wt, rho); phi = fmaf(s.y, wt, phi); a = fmaf(s.z, wt, a);
+                }
             }
-    // z box
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j)
-            for (int k = 0; k < 5; ++k) {
-                const float4 g = __ldg(T.grad + (ws[widx(i - 1, j - 1, k - 2) * stride] & kCellMask));
-                const float wt = wx[i] * wy[j] * dz5[k];
-                dxz = fmaf(g.x, wt, dxz);
-                dyz = fmaf(g.y, wt, dyz);
-                dzz = fmaf(g.z, wt, dzz);
-            }
-    H[0] = dxx * inv_dl; H[1] = dxy * inv_dl; H[2] = dxz * inv_dl;
-    H[3] = dyy * inv_dl; H[4] = dyz * inv_dl; H[5] = dzz * inv_dl;
+            res = Field7{rho, phi, gx, gy, gz, a, gt};
+            return true;
+        }
+        // first entry (x-major) not at this level: missing -> empty, coarser -> restart there
+        const int j = __ffs(~exact & kFullMask) - 1;
+        const int e = __ldg(reinterpret_cast<const int*>(rp) + j);
+        if (e < 0) {
+            clear(res);
+            return true;
+        }
+        const int lc = rec_flags(T, e) & 255;
+        const Found f = find_cell(T, lc, axis_coord(lc, x), axis_coord(lc, y), axis_coord(lc, z));
+        if (f.cell < 0 || f.level != lc) return false;
+        cell = f.cell;
+        L = lc;
+    }
+    return false;
 }
 
-// Jacobian contribution (d1d1, d1d2, d2d2 of lensing.h:444-447) at point p
-// whose deepest cell is the window centre (or a fallback to six full TSC).
-__device__ __forceinline__ void jac_fast(const DevTree& T, const Win& w, const int* ws, int stride, double x, double y,
-                                         double z, int level, float* out3)
+// CIC at a point whose deepest cell is `cell` (simplehyperoctree.h:1410-1469).
+__device__ __forceinline__ bool cic_rec(const DevTree& T, int cell, int L, double x, double y, double z, bool need_all,
+                                        Field7& res)
 {
-    float H[6];
-    const double dl = ldexp(1.0, kLevelShift + 1 - level);
-    bool done = false;
-    if (w.jac_ok && w.level == level) {
+    for (int guard = 0; guard <= kMaxLevel; ++guard) {
         uint32_t c[3];
         float fd[3];
-        point_cell(level, x, y, z, c, fd);
-        if (c[0] == w.cx && c[1] == w.cy && c[2] == w.cz) {
-            hessian_win(T, ws, stride, fd, (float)(1.0 / dl), H);
-            done = true;
+        point_cell(L, x, y, z, c, fd);
+        const int sx = (fd[0] >= 0.f) ? 1 : -1, sy = (fd[1] >= 0.f) ? 1 : -1, sz = (fd[2] >= 0.f) ? 1 : -1;
+        const float ax = fabsf(fd[0]), ay = fabsf(fd[1]), az = fabsf(fd[2]);
+        int lvl = L;
+        bool missing = false;
+        float gx = 0.f, gy = 0.f, gz = 0.f, gt = 0.f, rho = 0.f, phi = 0.f, a = 0.f;
+        for (int v = 0; v < 8; ++v) {
+            const int ox = (v & 1) ? ((sx > 0) ? 1 : 0) : ((sx > 0) ? 0 : -1);
+            const int oy = (v & 2) ? ((sy > 0) ? 1 : 0) : ((sy > 0) ? 0 : -1);
+            const int oz = (v & 4) ? ((sz > 0) ? 1 : 0) : ((sz > 0) ? 0 : -1);
+            const int e = rec_entry(T, cell, (ox + 1) * 9 + (oy + 1) * 3 + (oz + 1));
+            if (e < 0) { missing = true; break; }
+            const int le = rec_flags(T, e) & 255;
+            lvl = min(lvl, le);
+            // the neighbour cell gets |fd|, the centre cell 1 - |fd| (per axis)
+            const float wt = (ox ? ax : 1.f - ax) * (oy ? ay : 1.f - ay) * (oz ? az : 1.f - az);
+            const float4 g = __ldg(T.grad + e);
+            gx = fmaf(g.x, wt, gx); gy = fmaf(g.y, wt, gy); gz = fmaf(g.z, wt, gz); gt = fmaf(g.w, wt, gt);
+            if (need_all) {
+                const float4 s = __ldg(T.scal + e);
+                rho = fmaf(s.x, wt, rho); phi = fmaf(s.y, wt, phi); a = fmaf(s.z, wt, a);
+            }
         }
+        if (lvl == L) {
+            if (missing) clear(res);
+            else res = Field7{rho, phi, gx, gy, gz, a, gt};
+            return true;
+        }
+        const Found f = find_cell(T, lvl, axis_coord(lvl, x), axis_coord(lvl, y), axis_coord(lvl, z));
+        if (f.cell < 0 || f.level != lvl) return false;
+        cell = f.cell;
+        L = lvl;
     }
-    if (!done) {
-        const double h = 0.5 * dl;
-        const Field7 xm = tsc<false>(T, x - h, y, z, false), xp = tsc<false>(T, x + h, y, z, false);
-        const Field7 ym = tsc<false>(T, x, y - h, z, false), yp = tsc<false>(T, x, y + h, z, false);
-        const Field7 zm = tsc<false>(T, x, y, z - h, false), zp = tsc<false>(T, x, y, z + h, false);
-        const float idl = (float)(1.0 / dl);
-        H[0] = (xp.dx - xm.dx) * idl; H[1] = (yp.dx - ym.dx) * idl; H[2] = (zp.dx - zm.dx) * idl;
-        H[3] = (yp.dy - ym.dy) * idl; H[4] = (zp.dy - zm.dy) * idl; H[5] = (zp.dz - zm.dz) * idl;
-    }
-    const float fx = (float)x, fy = (float)y, fz = (float)z;
-    const float rho = sqrtf(fx * fx + fy * fy);
-    const float r = sqrtf(fx * fx + fy * fy + fz * fz);
-    const float cp = (rho > 0.f) ? fx / rho : 1.f, sp = (rho > 0.f) ? fy / rho : 0.f;
-    const float ct = fz / r, st = rho / r;
-    const float s2p = 2.f * sp * cp, s2t = 2.f * st * ct;
-    const float dxx = H[0], dxy = H[1], dxz = H[2], dyy = H[3], dyz = H[4], dzz = H[5];
-    out3[0] = sp * sp * dxx + cp * cp * dyy - s2p * dxy;
-    out3[1] = ct * cp * sp * (dyy - dxx) + (cp * cp - sp * sp) * ct * dxy + sp * st * dxz - cp * st * dyz;
-    out3[2] = cp * cp * ct * ct * dxx + sp * sp * ct * ct * dyy + st * st * dzz + s2p * ct * ct * dxy - sp * s2t * dyz - cp * s2t * dxz;
+    return false;
 }
 
-// deepest cell of a point: through the window when possible
-__device__ __forceinline__ Found locate_fast(const DevTree& T, const Win& w, const int* ws, int stride, double x, double y,
-                                             double z)
-{
-    if (w.level >= 0) {
-        uint32_t c[3];
-        float fd[3];
-        point_cell(w.level, x, y, z, c, fd);
-        const int ox = (int)(c[0] - w.cx), oy = (int)(c[1] - w.cy), oz = (int)(c[2] - w.cz);
-        if (abs(ox) <= 2 && abs(oy) <= 2 && abs(oz) <= 2) {
-            const int e = ws[widx(ox, oy, oz) * stride];
-            if (e >= 0 && !(e & kHasChildren)) return Found{e & kCellMask, w.level};
-        }
-    }
-    return locate(T, x, y, z);
-}
-
-// CIC through the window: the 8 cells of the centre's level around the point
-// (simplehyperoctree.h:1410-1469 without a restart).
-__device__ __forceinline__ bool cic_win(const DevTree& T, const Win& w, const int* ws, int stride, double x, double y, double z,
-                                        bool need_all, Field7& res)
-{
-    if (w.level < 0) return false;
-    uint32_t c[3];
-    float fd[3];
-    point_cell(w.level, x, y, z, c, fd);
-    const int ox = (int)(c[0] - w.cx), oy = (int)(c[1] - w.cy), oz = (int)(c[2] - w.cz);
-    if (abs(ox) > 1 || abs(oy) > 1 || abs(oz) > 1) return false;
-    const int ec = ws[widx(ox, oy, oz) * stride];
-    if (ec < 0 || (ec & kHasChildren)) return false;
-    // neighbour on the point's side along each axis, weights (1-|fd|, |fd|)
-    const int sx = (fd[0] >= 0.f) ? 1 : -1, sy = (fd[1] >= 0.f) ? 1 : -1, sz = (fd[2] >= 0.f) ? 1 : -1;
-    const float ax = fabsf(fd[0]), ay = fabsf(fd[1]), az = fabsf(fd[2]);
-    int cell[8];
-#pragma unroll
-    for (int v = 0; v < 8; ++v) {
-        const int e = ws[widx(ox + ((v & 1) ? sx : 0), oy + ((v & 2) ? sy : 0), oz + ((v & 4) ? sz : 0)) * stride];
-        if (e < 0) return false;
-        cell[v] = e & kCellMask;
-    }
-    float gx = 0.f, gy = 0.f, gz = 0.f, gt = 0.f, rho = 0.f, phi = 0.f, a = 0.f;
-#pragma unroll
-    for (int v = 0; v < 8; ++v) {
-        const float wt = ((v & 1) ? ax : 1.f - ax) * ((v & 2) ? ay : 1.f - ay) * ((v & 4) ? az : 1.f - az);
-        const float4 g = __ldg(T.grad + cell[v]);
-        gx = fmaf(g.x, wt, gx); gy = fmaf(g.y, wt, gy); gz = fmaf(g.z, wt, gz); gt = fmaf(g.w, wt, gt);
-        if (need_all) {
-            const float4 s = __ldg(T.scal + cell[v]);
-            rho = fmaf(s.x, wt, rho); phi = fmaf(s.y, wt, phi); a = fmaf(s.z, wt, a);
-        }
-    }
-    res = Field7{rho, phi, gx, gy, gz, a, gt};
-    return true;
-}
-
-__device__ __forceinline__ Field7 gather_fast(const DevTree& T, const Win& w, const int* ws, int stride, int order, double x,
-                                              double y, double z, bool need_all)
+__device__ __forceinline__ Field7 gather_at(const DevTree& T, int order, const Loc& d, double x, double y, double z, bool need_all,
+                                            unsigned long long* st, int slot)
 {
     Field7 r;
-    if (order == 1) {
-        if (cic_win(T, w, ws, stride, x, y, z, need_all, r)) return r;
-        return cic<false>(T, x, y, z, need_all);
+    if (d.cell < 0) {
+        clear(r);
+        stat(st, slot);
+        return r;
     }
-    if (tsc_win(T, w, ws, stride, x, y, z, need_all, r)) return r;
-    return tsc<false>(T, x, y, z, need_all);
+    if (!(x == 0.0 && y == 0.0 && z == 0.0)) {
+        const bool ok = (order == 1) ? cic_rec(T, d.cell, d.level, x, y, z, need_all, r)
+                                     : tsc_rec(T, d.cell, d.level, x, y, z, need_all, r);
+        if (ok) {
+            stat(st, slot);
+            return r;
+        }
+    }
+    stat(st, slot + 1);
+    return (order == 1) ? cic_slow(T, x, y, z, need_all) : tsc_slow(T, x, y, z, need_all);
 }
 
 struct FastRec {
@@ -356,12 +262,13 @@ struct FastRec {
     int level;
 };
 
-__device__ __forceinline__ void rhs_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const Win& w, const int* ws,
-                                         int stride, double inv_scale, const double* in, double* out)
+__device__ __forceinline__ void rhs_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const Loc& here,
+                                         double inv_scale, const double* in, double* out, unsigned long long* st)
 {
     const double c2 = kC * kC;
-    const Field7 d = gather_fast(T, w, ws, stride, P.order, in[2], in[3], in[4], false);
-    const double dphidl = (double)d.dt * in[5] + ((double)d.dx * in[6] + (double)d.dy * in[7] + (double)d.dz * in[8]);
+    const Loc d = locate_near(T, here, in[2], in[3], in[4]);
+    const Field7 g = gather_at(T, P.order, d, in[2], in[3], in[4], false, st, ST_RK_REC);
+    const double dphidl = (double)g.dt * in[5] + ((double)g.dx * in[6] + (double)g.dy * in[7] + (double)g.dz * in[8]);
     const double dadt = interp_fast(C, in[1], C.dadt, C.slope_dadt);
     out[0] = in[5] * dadt;
     out[1] = in[5];
@@ -369,50 +276,77 @@ __device__ __forceinline__ void rhs_fast(const DevTree& T, const DevCosmo& C, co
     out[3] = in[7] * inv_scale;
     out[4] = in[8] * inv_scale;
     const double hub = 2.0 * dadt / in[0] * in[5];
-    const double g = (2.0 / c2) * dphidl;
+    const double gg = (2.0 / c2) * dphidl;
     const double k02 = 2.0 * in[5] * in[5];
-    out[5] = -(hub * in[5]) - ((2.0 / c2) * in[5]) * (dphidl - (double)d.dt * in[5]);
-    out[6] = -(hub * in[6]) + (g * in[6]) - ((double)d.dx * k02);
-    out[7] = -(hub * in[7]) + (g * in[7]) - ((double)d.dy * k02);
-    out[8] = -(hub * in[8]) + (g * in[8]) - ((double)d.dz * k02);
+    out[5] = -(hub * in[5]) - ((2.0 / c2) * in[5]) * (dphidl - (double)g.dt * in[5]);
+    out[6] = -(hub * in[6]) + (gg * in[6]) - ((double)g.dx * k02);
+    out[7] = -(hub * in[7]) + (gg * in[7]) - ((double)g.dy * k02);
+    out[8] = -(hub * in[8]) + (gg * in[8]) - ((double)g.dz * k02);
+}
+
+// Jacobian terms (d1d1, d1d2, d2d2 of lensing.h:430-447) at a trajectory
+// point located at `here`: six TSC gathers at +-1 cell.
+__device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, double x, double y, double z, float* out3,
+                                         unsigned long long* st)
+{
+    const double dl = ldexp(1.0, kLevelShift + 1 - here.level);
+    const double h = 0.5 * dl;
+    float g[6][3];
+#pragma unroll 1
+    for (int a = 0; a < 6; ++a) {
+        const int ax = a >> 1;
+        const double sg = (a & 1) ? h : -h;
+        const double qx = x + (ax == 0 ? sg : 0.0), qy = y + (ax == 1 ? sg : 0.0), qz = z + (ax == 2 ? sg : 0.0);
+        const Loc d = locate_near(T, here, qx, qy, qz);
+        const Field7 f = gather_at(T, 2, d, qx, qy, qz, false, st, ST_JAC_REC);
+        g[a][0] = f.dx; g[a][1] = f.dy; g[a][2] = f.dz;
+    }
+    const float idl = (float)(1.0 / dl);
+    const float dxx = (g[1][0] - g[0][0]) * idl, dxy = (g[3][0] - g[2][0]) * idl, dxz = (g[5][0] - g[4][0]) * idl;
+    const float dyy = (g[3][1] - g[2][1]) * idl, dyz = (g[5][1] - g[4][1]) * idl, dzz = (g[5][2] - g[4][2]) * idl;
+    const float fx = (float)x, fy = (float)y, fz = (float)z;
+    const float rho = sqrtf(fx * fx + fy * fy);
+    const float r = sqrtf(fx * fx + fy * fy + fz * fz);
+    const float cp = (rho > 0.f) ? fx / rho : 1.f, sp = (rho > 0.f) ? fy / rho : 0.f;
+    const float ct = fz / r, snt = rho / r;
+    const float s2p = 2.f * sp * cp, s2t = 2.f * snt * ct;
+    out3[0] = sp * sp * dxx + cp * cp * dyy - s2p * dxy;
+    out3[1] = ct * cp * sp * (dyy - dxx) + (cp * cp - sp * sp) * ct * dxy + sp * snt * dxz - cp * snt * dyz;
+    out3[2] = cp * cp * ct * ct * dxx + sp * sp * ct * ct * dyy + snt * snt * dzz + s2p * ct * ct * dxy - sp * s2t * dyz -
+              cp * s2t * dxz;
 }
 
 __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* L, long long i,
-                               const PropOut& O, int* ws, int stride)
+                               const PropOut& O)
 {
     const double c2 = kC * kC;
     const double mn = -(double)kExtent / 2.0, mx = (double)kExtent / 2.0;
     const double scale = P.length;
     const double inv_scale = 1.0 / scale;
     const int np = P.nplanes;
-    Win w;
-    w.level = -1;
+    unsigned long long* const st = O.stats;
     FastRec b;
     {
         const double norm = sqrt((L[3] - L[0]) * (L[3] - L[0]) + (L[4] - L[1]) * (L[4] - L[1]) + (L[5] - L[2]) * (L[5] - L[2]));
         b.a = 1.0; b.t = 0.0; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = 1.0;
         b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
     }
-    Field7 data = gather<false>(T, P.order, b.x, b.y, b.z, true);
+    Loc here;
+    here.cell = -1;
+    here = locate_near(T, here, b.x, b.y, b.z);
+    Field7 data = gather_at(T, P.order, here, b.x, b.y, b.z, true, st, ST_POST_REC);
     {
         const double ph = (double)data.phi / c2;
         const double norm = sqrt((c2 * (1.0 + 2.0 * ph) * b.k0 * b.k0) / ((1.0 - 2.0 * ph) * (b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3)));
         b.k1 *= norm; b.k2 *= norm; b.k3 *= norm;
     }
     b.a = interp_fast(C, b.t, C.a, C.slope_a);
-    Found loc = locate(T, b.x, b.y, b.z);
-    b.level = (loc.cell >= 0) ? loc.level : 0;
-    if (loc.cell >= 0) {
-        uint32_t c[3];
-        float fd[3];
-        point_cell(loc.level, b.x, b.y, b.z, c, fd);
-        win_build(T, loc.level, c[0], c[1], c[2], ws, stride, w);
-    }
+    b.level = (here.cell >= 0) ? here.level : 0;
     b.ah = 0.f;
     b.rho = data.rho; b.phi = data.phi; b.dx = data.dx; b.dy = data.dy; b.dz = data.dz; b.dt = data.dt;
     b.red = 0.0; b.isw = 0.0; b.chi = 0.0; b.iswold = 0.0; b.lambda = 0.0; b.s = 0.0;
     double ratio = b.a * b.a * (scale / kC) / P.nsteps;
-    double dl = (loc.cell >= 0 ? cell_extent(loc.level) : 0.0) * ratio;
+    double dl = (here.cell >= 0 ? cell_extent(here.level) : 0.0) * ratio;
     const double a0 = b.a;
     const double phi0c2 = b.phi / c2;
     float last_data_dt = data.dt;
@@ -441,27 +375,29 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     while (!is_empty(data)) {
         if (k >= P.max_steps) { status |= 1u; break; }
         const double bc[9] = {b.a, b.t, b.x, b.y, b.z, b.k0, b.k1, b.k2, b.k3};
-        const double hdl = 0.5 * dl;
-        // stage derivatives folded into acc = d0 + 2 d1 + 2 d2 + d3 in that order
-        rhs_fast(T, C, P, w, ws, stride, inv_scale, bc, dc);
+        // stages: core = b + c_s dl * d_{s-1};  acc = d0 + 2 d1 + 2 d2 + d3 (in that order)
+#pragma unroll 1
+        for (int sg = 0; sg < 4; ++sg) {
+            rhs_fast(T, C, P, here, inv_scale, (sg == 0) ? bc : core, dc, st);
+            const double cs = (sg < 2) ? 0.5 * dl : dl;
+            const double wa = (sg == 0) ? 0.0 : 2.0;
+            if (sg < 3) {
 #pragma unroll
-        for (int q = 0; q < 9; ++q) { acc[q] = dc[q]; core[q] = bc[q] + hdl * dc[q]; }
-        rhs_fast(T, C, P, w, ws, stride, inv_scale, core, dc);
-#pragma unroll
-        for (int q = 0; q < 9; ++q) { acc[q] += 2.0 * dc[q]; core[q] = bc[q] + hdl * dc[q]; }
-        rhs_fast(T, C, P, w, ws, stride, inv_scale, core, dc);
-#pragma unroll
-        for (int q = 0; q < 9; ++q) { acc[q] += 2.0 * dc[q]; core[q] = bc[q] + dl * dc[q]; }
-        rhs_fast(T, C, P, w, ws, stride, inv_scale, core, dc);
+                for (int q = 0; q < 9; ++q) {
+                    acc[q] = (sg == 0) ? dc[q] : acc[q] + wa * dc[q];
+                    core[q] = bc[q] + cs * dc[q];
+                }
+            }
+        }
         const double dl6 = dl * (1.0 / 6.0);
 #pragma unroll
         for (int q = 0; q < 9; ++q) core[q] = bc[q] + dl6 * (acc[q] + dc[q]);
         p.a = core[0]; p.t = core[1]; p.x = core[2]; p.y = core[3]; p.z = core[4];
         p.k0 = core[5]; p.k1 = core[6]; p.k2 = core[7]; p.k3 = core[8];
-        data = gather_fast(T, w, ws, stride, P.order, p.x, p.y, p.z, true);
+        const Loc ploc = locate_near(T, here, p.x, p.y, p.z);
+        data = gather_at(T, P.order, ploc, p.x, p.y, p.z, true, st, ST_POST_REC);
         if (!(!(p.a < 0.0) && ((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx)))) clear(data);
-        loc = locate_fast(T, w, ws, stride, p.x, p.y, p.z);
-        p.level = (loc.cell >= 0) ? loc.level : 0;
+        p.level = (ploc.cell >= 0) ? ploc.level : 0;
         p.ah = data.a;
         p.rho = data.rho; p.phi = data.phi; p.dx = data.dx; p.dy = data.dy; p.dz = data.dz;
         p.dt = -data.dt;
@@ -477,21 +413,16 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         p.isw = isw; p.iswold = iswold; p.lambda = lambda; p.s = sacc;
         if (!is_empty(data)) {
             ratio = p.a * p.a * (scale / kC) / P.nsteps;
-            dl = (loc.cell >= 0 ? cell_extent(loc.level) : 0.0) * ratio;
+            dl = (ploc.cell >= 0 ? cell_extent(ploc.level) : 0.0) * ratio;
             last_data_dt = data.dt;
             last_lap = lap;
-            // keep the window centred on the new point's cell
-            if (loc.cell >= 0) {
-                uint32_t c[3];
-                float fd[3];
-                point_cell(loc.level, p.x, p.y, p.z, c, fd);
-                if (w.level != loc.level || c[0] != w.cx || c[1] != w.cy || c[2] != w.cz)
-                    win_build(T, loc.level, c[0], c[1], c[2], ws, stride, w);
-            }
+            if (ploc.cell != here.cell) stat(st, ST_CELL_CHANGE);
+            here = ploc;
             ++k;
+            stat(st, ST_STEPS);
             if (P.jacobian) {
                 float h3[3];
-                jac_fast(T, w, ws, stride, p.x, p.y, p.z, p.level, h3);
+                jac_fast(T, here, p.x, p.y, p.z, h3, st);
                 const double dr = p.chi - b.chi;
                 chim2 = chim1; chim1 = b.chi;
 #pragma unroll
@@ -621,11 +552,10 @@ constexpr int kFastThreads = 128;
 // Persistent launch: each warp takes the next 32 rays from a global counter
 // until the batch is exhausted, so uneven path lengths do not leave tail
 // waves.  `queue` is zeroed before the launch.
-__global__ void __launch_bounds__(kFastThreads) k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
-                                                                 const double* __restrict__ launch, long long n, PropOut O,
-                                                                 unsigned long long* queue)
+__global__ void __launch_bounds__(kFastThreads, 3) k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
+                                                                    const double* __restrict__ launch, long long n, PropOut O,
+                                                                    unsigned long long* queue)
 {
-    extern __shared__ int smem_win[];
     const int lane = threadIdx.x & 31;
     for (;;) {
         unsigned long long base = 0;
@@ -633,9 +563,27 @@ __global__ void __launch_bounds__(kFastThreads) k_propagate_fast(DevTree T, DevC
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= (unsigned long long)n) break;
         const long long i = (long long)base + lane;
-        if (i < n) propagate_fast(T, C, P, launch + 6 * i, i, O, smem_win + threadIdx.x, blockDim.x);
+        if (i < n) propagate_fast(T, C, P, launch + 6 * i, i, O);
         __syncwarp();
     }
+}
+
+// Fast-mode gathers through the stencil records (tests / mpf_interpolate).
+__global__ void k_gather_rec(DevTree T, int kind, const double* __restrict__ xyz, long long n, void* out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+    Loc none;
+    none.cell = -1;
+    const Loc d = locate_near(T, none, x, y, z);
+    if (kind == 0) {
+        ((long long*)out)[i] = d.cell;
+        return;
+    }
+    const Field7 f = gather_at(T, kind, d, x, y, z, true, nullptr, 0);
+    float* o = (float*)out + 7 * i;
+    o[0] = f.rho; o[1] = f.phi; o[2] = f.dx; o[3] = f.dy; o[4] = f.dz; o[5] = f.a; o[6] = f.dt;
 }
 
 }  // namespace mpf

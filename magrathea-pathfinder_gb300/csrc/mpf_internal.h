@@ -17,6 +17,7 @@ struct mpf_octree {
     float4* scal;
     int2* node;
     int* grid;
+    int4* stencil;
 };
 
 struct mpf_cosmology {

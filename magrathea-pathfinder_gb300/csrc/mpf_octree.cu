@@ -13,7 +13,10 @@
 //      contiguous child slots (exclusive scan), each key's level-(l+1) node is
 //      its parent's base + its site, and a key of exactly level l+1 names its
 //      node's cell;
-//   4. scatter the level-Lt nodes into the dense top grid.
+//   4. scatter the level-Lt nodes into the dense top grid;
+//   5. per cell, its stencil record: the 27 same-level lookups around it with
+//      the reference's lookup semantics, resolved once here so that a TSC
+//      gather during propagation is one record load plus the payload loads.
 #include <cstdio>
 #include <vector>
 
@@ -133,11 +136,14 @@ __global__ void k_top_ids(const ulonglong2* keys, const float4* scal, int64_t n,
     }
 }
 
-__global__ void k_top_cells(const float4* scal, int64_t n, int Lt, const int* nodeid, int2* node)
+__global__ void k_top_cells(const float4* scal, int64_t n, int Lt, const int* nodeid, int2* node, int* cell_node)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (__float_as_int(scal[i].w) == Lt) node[nodeid[i]].y = (int)i;
+    if (__float_as_int(scal[i].w) == Lt) {
+        node[nodeid[i]].y = (int)i;
+        cell_node[i] = nodeid[i];
+    }
 }
 
 // mark level-l nodes that own a deeper key
@@ -164,7 +170,7 @@ __global__ void k_children(int64_t cnt_l, int64_t off_l, int64_t off_next, const
 // (ids are global; `cur` holds level l from global id off_l, `next` level l+1
 // from global id off_next)
 __global__ void k_descend(const ulonglong2* keys, const float4* scal, int64_t n, int l, const int* nodeid, int* nodeid_next,
-                          const int2* cur, int64_t off_l, int2* next, int64_t off_next)
+                          const int2* cur, int64_t off_l, int2* next, int64_t off_next, int* cell_node)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -173,7 +179,40 @@ __global__ void k_descend(const ulonglong2* keys, const float4* scal, int64_t n,
     const Key k{keys[i].x, keys[i].y};
     const int id = cur[nodeid[i] - off_l].x + key_site(k, l + 1);
     nodeid_next[i] = id;
-    if (L == l + 1) next[id - off_next].y = (int)i;
+    if (L == l + 1) {
+        next[id - off_next].y = (int)i;
+        cell_node[i] = id;
+    }
+}
+
+// Stencil record of each cell (layout in mpf_device.cuh).
+__global__ void k_stencil(DevTree T, const int* cell_node, int4* out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= T.n) return;
+    const Key k{T.keys[i].x, T.keys[i].y};
+    const int L = __float_as_int(T.scal[i].w);
+    const uint64_t cx = key_axis(k, L, 0), cy = key_axis(k, L, 1), cz = key_axis(k, L, 2);
+    const uint64_t mask = (L >= 32) ? 0xffffffffull : ((1ull << L) - 1ull);
+    int e[32];
+    unsigned exact = 0;
+    int j = 0;
+    for (int ix = -1; ix <= 1; ++ix)
+        for (int iy = -1; iy <= 1; ++iy)
+            for (int iz = -1; iz <= 1; ++iz, ++j) {
+                const Found f = find_cell(T, L, (cx + (uint64_t)(int64_t)ix) & mask, (cy + (uint64_t)(int64_t)iy) & mask,
+                                          (cz + (uint64_t)(int64_t)iz) & mask);
+                e[j] = f.cell;
+                if (f.cell >= 0 && f.level == L) exact |= 1u << j;
+            }
+    const int nd = cell_node[i];
+    e[27] = L | ((T.node[nd].x >= 0) ? 256 : 0);
+    e[28] = (int)exact;
+    e[29] = nd;
+    e[30] = 0;
+    e[31] = 0;
+    int4* o = out + 8 * i;
+    for (int q = 0; q < 8; ++q) o[q] = make_int4(e[4 * q], e[4 * q + 1], e[4 * q + 2], e[4 * q + 3]);
 }
 
 inline unsigned blocks(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -225,6 +264,7 @@ extern "C" int mpf_internal_octree_build(const void* records, int64_t n, int on_
         temps.clear();
         if (all) {
             cudaFree(o->keys); cudaFree(o->grad); cudaFree(o->scal); cudaFree(o->node); cudaFree(o->grid);
+            cudaFree(o->stencil);
             delete o;
         }
     };
@@ -272,8 +312,9 @@ extern "C" int mpf_internal_octree_build(const void* records, int64_t n, int on_
     }
     const int gnx = bb[3] - bb[0] + 1, gny = bb[4] - bb[1] + 1, gnz = bb[5] - bb[2] + 1;
     const int64_t gsz = (int64_t)gnx * gny * gnz;
-    int *flag = nullptr, *fscan = nullptr, *nid = nullptr, *nid2 = nullptr;
+    int *flag = nullptr, *fscan = nullptr, *nid = nullptr, *nid2 = nullptr, *cell_node = nullptr;
     if (!dalloc((void**)&o->grid, (size_t)gsz * sizeof(int), false) || !dalloc((void**)&flag, (size_t)n * sizeof(int), true) ||
+        !dalloc((void**)&cell_node, (size_t)n * sizeof(int), true) ||
         !dalloc((void**)&fscan, (size_t)n * sizeof(int), true) || !dalloc((void**)&nid, (size_t)n * sizeof(int), true) ||
         !dalloc((void**)&nid2, (size_t)n * sizeof(int), true)) {
         release(true);
@@ -291,7 +332,7 @@ extern "C" int mpf_internal_octree_build(const void* records, int64_t n, int on_
     if (!dalloc((void**)&top, (size_t)cnt_top * sizeof(int2), true)) { release(true); return fail("out of device memory", -2); }
     k_top_ids<<<blocks(n, 256), 256, 0, stream>>>(o->keys, o->scal, n, Lt, fscan, flag, nid, top, o->grid, bb[0], bb[1], bb[2],
                                                   gnx, gny);
-    k_top_cells<<<blocks(n, 256), 256, 0, stream>>>(o->scal, n, Lt, nid, top);
+    k_top_cells<<<blocks(n, 256), 256, 0, stream>>>(o->scal, n, Lt, nid, top, cell_node);
     chunks.push_back(top);
     counts.push_back(cnt_top);
     offsets.push_back(0);
@@ -314,7 +355,8 @@ extern "C" int mpf_internal_octree_build(const void* records, int64_t n, int on_
         int2* next = nullptr;
         if (!dalloc((void**)&next, (size_t)cnt_next * sizeof(int2), true)) { release(true); return fail("out of device memory", -2); }
         k_children<<<blocks(cnt, 256), 256, 0, stream>>>(cnt, 0, off_next, has, scan, chunks.back(), next);
-        k_descend<<<blocks(n, 256), 256, 0, stream>>>(o->keys, o->scal, n, l, nid, nid2, chunks.back(), off, next, off_next);
+        k_descend<<<blocks(n, 256), 256, 0, stream>>>(o->keys, o->scal, n, l, nid, nid2, chunks.back(), off, next, off_next,
+                                                      cell_node);
         std::swap(nid, nid2);
         chunks.push_back(next);
         counts.push_back(cnt_next);
@@ -324,10 +366,6 @@ extern "C" int mpf_internal_octree_build(const void* records, int64_t n, int on_
     if (!dalloc((void**)&o->node, (size_t)total * sizeof(int2), false)) { release(true); return fail("out of device memory", -2); }
     for (size_t c = 0; c < chunks.size(); ++c)
         cudaMemcpyAsync(o->node + offsets[c], chunks[c], (size_t)counts[c] * sizeof(int2), cudaMemcpyDeviceToDevice, stream);
-    ce = cudaStreamSynchronize(stream);
-    if (ce == cudaSuccess) ce = cudaGetLastError();
-    release(false);
-    if (ce != cudaSuccess) { release(true); return fail(cudaGetErrorString(ce), -3); }
     o->nnodes = total;
     o->tree.keys = o->keys;
     o->tree.grad = o->grad;
@@ -338,6 +376,13 @@ extern "C" int mpf_internal_octree_build(const void* records, int64_t n, int on_
     o->tree.Lt = Lt;
     o->tree.gx0 = bb[0]; o->tree.gy0 = bb[1]; o->tree.gz0 = bb[2];
     o->tree.gnx = gnx; o->tree.gny = gny; o->tree.gnz = gnz;
+    if (!dalloc((void**)&o->stencil, (size_t)n * 8 * sizeof(int4), false)) { release(true); return fail("out of device memory", -2); }
+    o->tree.stencil = o->stencil;
+    k_stencil<<<blocks(n, 128), 128, 0, stream>>>(o->tree, cell_node, o->stencil);
+    ce = cudaStreamSynchronize(stream);
+    if (ce == cudaSuccess) ce = cudaGetLastError();
+    release(false);
+    if (ce != cudaSuccess) { release(true); return fail(cudaGetErrorString(ce), -3); }
     *out = o;
     return 0;
 }

@@ -1,9 +1,11 @@
-// Throughput mode: FP32 gather arithmetic through the per-ray cell window,
-// FP64 RK4 state (with FMA).
+// Throughput mode: FP32 gather arithmetic through the per-cell stencil
+// records, FP64 RK4 state (with FMA).
 #include "mpf_fast.cuh"
 #include "mpf_prop_impl.cuh"
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 
 namespace mpf {
 template <>
@@ -12,12 +14,10 @@ cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const P
 {
     if (n <= 0) return cudaSuccess;
     const int tpb = kFastThreads;
-    const size_t smem = (size_t)kWin3 * tpb * sizeof(int);
     static int blocks_per_sm = 0, sms = 0;
     static unsigned long long* queue = nullptr;   // one work counter per process (calls on a stream are ordered)
     if (blocks_per_sm == 0) {
-        cudaError_t e = cudaFuncSetAttribute(k_propagate_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_propagate_fast, tpb, smem);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_propagate_fast, tpb, 0);
         int dev = 0;
         if (e == cudaSuccess) e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -29,11 +29,30 @@ cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const P
     if (e != cudaSuccess) return e;
     const long long need = (n + tpb - 1) / tpb;
     const long long grid = std::min<long long>(need, (long long)blocks_per_sm * sms);
-    k_propagate_fast<<<(unsigned)grid, tpb, smem, stream>>>(T, C, P, d_launch, n, O, queue);
-    return cudaGetLastError();
+    // MPF_STATS=1: count record-path gathers and slow-path fallbacks (diagnostics; serialises the call)
+    static const bool want_stats = getenv("MPF_STATS") != nullptr;
+    PropOut o2 = O;
+    unsigned long long* dstats = nullptr;
+    if (want_stats && cudaMalloc(&dstats, ST_N * sizeof(unsigned long long)) == cudaSuccess) {
+        cudaMemsetAsync(dstats, 0, ST_N * sizeof(unsigned long long), stream);
+        o2.stats = dstats;
+    }
+    k_propagate_fast<<<(unsigned)grid, tpb, 0, stream>>>(T, C, P, d_launch, n, o2, queue);
+    e = cudaGetLastError();
+    if (dstats) {
+        unsigned long long h[ST_N];
+        cudaMemcpyAsync(h, dstats, sizeof(h), cudaMemcpyDeviceToHost, stream);
+        cudaStreamSynchronize(stream);
+        fprintf(stderr, "mpf_stats rk_rec %llu rk_slow %llu post_rec %llu post_slow %llu jac_rec %llu jac_slow %llu cell_changes %llu steps %llu\n",
+                h[0], h[1], h[2], h[3], h[4], h[5], h[6], h[7]);
+        cudaFree(dstats);
+    }
+    return e;
 }
 cudaError_t launch_gather_fast(const DevTree& T, int kind, const double* d_xyz, long long n, void* d_out, cudaStream_t stream)
 {
-    return launch_gather_impl<false>(T, kind, d_xyz, n, d_out, stream);
+    if (n <= 0) return cudaSuccess;
+    k_gather_rec<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(T, kind, d_xyz, n, d_out);
+    return cudaGetLastError();
 }
 }  // namespace mpf

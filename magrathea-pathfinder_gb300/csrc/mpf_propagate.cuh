@@ -56,6 +56,7 @@ struct PropOut {
     double* final_rec;     // n x 28, or null
     double* plane_rec;     // n x nplanes x 20, or null
     unsigned* status;      // bit 0: a ray hit max_steps
+    unsigned long long* stats;   // optional path counters (fast mode), or null
 };
 
 // Utility::interpolate (src/utility.h:441-449)
