@@ -128,6 +128,23 @@ int mpf_propagate_device(const mpf_octree* o, const mpf_cosmology* c, const mpf_
                          const double* launch_device, int64_t* steps_device, double* final_device,
                          double* plane_device, uint32_t* status_device, void* stream);
 
+/* mpf_propagate with HOST buffers but without any device allocation: for
+ * callers that cannot call cudaMalloc/cudaFree while they run (a pooling
+ * allocator owns the GPU's memory, a hard per-process memory cap, or a loop
+ * that cannot afford the device synchronisation of an allocation).  It has no
+ * counterpart in the reference (which has no device code).  Launch records,
+ * outputs, the work-queue counter and the status word are staged through one
+ * static device array of MPF_NOALLOC_SCRATCH_BYTES per GPU, kept until the
+ * process exits; a batch that does not fit is rejected with MPF_BAD_INPUT.
+ * All calls share that array: calls that overlap on the GPU race, so
+ * serialise them.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress): make it before any stream capture.  Message of a
+ * failed call: mpf_noalloc_last_error(). */
+#define MPF_NOALLOC_SCRATCH_BYTES (16u << 20)
+int mpf_propagate_noalloc(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t n, const double* launch,
+                          int64_t* steps, double* final_rec, double* plane_rec);
+const char* mpf_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

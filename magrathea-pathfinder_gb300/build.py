@@ -24,6 +24,7 @@ UNITS = [
     ("mpf_prop_fast.cu", []),
     ("mpf_octree.cu", []),
     ("mpf_capi.cu", []),
+    ("mpf_noalloc.cu", []),
 ]
 
 

@@ -25,7 +25,8 @@ STOP = {"redshift": 0, "r": 1, "radius": 1, "lambda": 2, "t": 3, "eta": 3, "a": 
 # every symbol include/mpf_gb300.h declares
 EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_upload", "mpf_octree_load",
            "mpf_octree_get_info", "mpf_octree_destroy", "mpf_cosmology_upload", "mpf_cosmology_destroy", "mpf_locate",
-           "mpf_interpolate", "mpf_propagate", "mpf_propagate_device")
+           "mpf_interpolate", "mpf_propagate", "mpf_propagate_device", "mpf_propagate_noalloc",
+           "mpf_noalloc_last_error")
 
 
 class MpfError(RuntimeError):
@@ -73,9 +74,11 @@ def load(path: str = LIB_PATH):
     L.mpf_interpolate.argtypes = [vp, C.c_int, C.c_int, i64, vp, vp]
     L.mpf_propagate.argtypes = [vp, vp, C.POINTER(Params), i64, vp, vp, vp, vp]
     L.mpf_propagate_device.argtypes = [vp, vp, C.POINTER(Params), i64, vp, vp, vp, vp, vp, vp]
+    L.mpf_propagate_noalloc.argtypes = [vp, vp, C.POINTER(Params), i64, vp, vp, vp, vp]
+    L.mpf_noalloc_last_error.restype = C.c_char_p
     for name in EXPORTS:
         if name not in ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_destroy",
-                        "mpf_cosmology_destroy"):
+                        "mpf_cosmology_destroy", "mpf_noalloc_last_error"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L

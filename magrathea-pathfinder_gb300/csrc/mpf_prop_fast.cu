@@ -56,3 +56,24 @@ cudaError_t launch_gather_fast(const DevTree& T, int kind, const double* d_xyz, 
     return cudaGetLastError();
 }
 }  // namespace mpf
+
+namespace mpf {
+// Same launch as launch_propagate<false>, with the work-queue counter supplied
+// by the caller (no allocation here).  The counter must be zero on entry.
+cudaError_t launch_propagate_fast_with_queue(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* d_launch,
+                                             long long n, const PropOut& O, unsigned long long* queue, cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    const int tpb = kFastThreads;
+    int blocks_per_sm = 0, sms = 0, dev = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_propagate_fast, tpb, 0);
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    if (blocks_per_sm < 1) blocks_per_sm = 1;
+    const long long need = (n + tpb - 1) / tpb;
+    const long long grid = std::min<long long>(need, (long long)blocks_per_sm * sms);
+    k_propagate_fast<<<(unsigned)grid, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
+    return cudaGetLastError();
+}
+}  // namespace mpf
