@@ -45,12 +45,15 @@ BYTES_PER_PHOTON_STEP = 4 * 27 * 16 + 27 * 28 + 6 * 27 * 12
 DRAM_BYTES_PER_PHOTON_STEP = None
 
 
-def workload_spec(synth, small: bool):
+def workload_spec(synth, workload: str):
     cosmo = synth.Cosmology()
     chi2 = float(cosmo.chi_of_z(2.0)[0])
-    if small:
+    if workload == "small":
         return synth.OctreeSpec(base_level=8, box_cells=64, lbox=2048.0, half_y=5.0, half_z=5.0, chi_max=chi2 * 1.02,
                                 halos=50, max_level=11, refine_cells=2.5, seed=42)
+    if workload == "medium":   # the same construction one level coarser: larger than L2, ~1 GB on the device
+        return synth.OctreeSpec(base_level=9, box_cells=128, lbox=2048.0, half_y=5.0, half_z=5.0, chi_max=chi2 * 1.02,
+                                halos=500, max_level=13, mass_min=1e12, mass_max=1e15, refine_cells=4.5, seed=42)
     return synth.OctreeSpec(base_level=10, box_cells=256, lbox=2048.0, half_y=5.0, half_z=5.0, chi_max=chi2 * 1.02,
                             halos=2000, max_level=14, mass_min=1e12, mass_max=1e15, refine_cells=4.5, seed=42)
 
@@ -146,7 +149,7 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(oracle_mod, records, cos, length, launch, planes, per_thread=4, seed=1):
+def cpu_baseline(oracle_mod, records, cos, length, launch, planes, per_thread=24, seed=1):
     """The C oracle (restated reference algorithm, binary search over sorted
     keys, trajectory then Jacobian post-pass) on a bounded random sample."""
     nthreads = os.cpu_count() or 1
@@ -179,8 +182,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=65536)
-    ap.add_argument("--small", action="store_true", help="small octree (debug only)")
+    ap.add_argument("--batch", type=int, default=131072)
+    ap.add_argument("--workload", default="amr", choices=["amr", "medium", "small"],
+                    help="amr = the benchmark configuration; medium / small for profiling and debugging")
     ap.add_argument("--exact", action="store_true", help="reference float64 gather order")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--zstop", type=float, default=2.0, help="stop redshift (profiling captures use a short path)")
@@ -188,10 +192,10 @@ def main():
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     synth = importlib.import_module(PKG + ".synth")
-    spec = workload_spec(synth, args.small)
+    spec = workload_spec(synth, args.workload)
     config = {"workload": "AMR cone octree, 256^3 base (level 10) refined to level 14 in 2000 NFW haloes; "
                           "1000x1000 rays over 10x10 deg to z=2; TSC, 8 steps/cell, infinitesimal Jacobian at z=2"
-                          if not args.small else "small debug octree",
+                          if args.workload == "amr" else "%s octree (profiling / debugging)" % args.workload,
               "rays": 1000 * 1000, "batch_rays": args.batch, "order": "TSC", "nsteps": 8, "z_stop": args.zstop,
               "gather_arithmetic": "float64 reference order" if args.exact else "fp32 gather, fp64 state",
               "l2": "octree larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single GPU"}
