@@ -92,27 +92,45 @@ __device__ __noinline__ Field7 cic_slow(const DevTree& T, double x, double y, do
 }
 __device__ __noinline__ Found locate_slow(const DevTree& T, double x, double y, double z) { return locate(T, x, y, z); }
 
-// A located point: its deepest cell, that cell's level and the point's
-// integer coordinates at that level.
+// A located point: its deepest cell, that cell's level, integer coordinates
+// and centre, and the point's offset from the centre in cell units.
 struct Loc {
     int cell;
     int level;
     uint32_t c[3];
+    double cen[3];
+    float fd[3];
 };
 
-// Deepest cell of point (x, y, z) given a nearby located cell `h`: read from
-// h's record when the point lies in h or one of its 26 neighbours and that
-// neighbour is a leaf of h's level; otherwise a full walk.
-__device__ __forceinline__ Loc locate_near(const DevTree& T, const Loc& h, double x, double y, double z)
+__device__ __forceinline__ float cells_per_unit(int L) { return (float)(1ull << L) * (1.0f / (float)kExtent); }
+
+// full location by a walk from the top grid (float64 coordinates)
+__device__ __noinline__ Loc locate_full(const DevTree& T, double x, double y, double z)
 {
     Loc r;
+    const Found f = locate(T, x, y, z);
+    r.cell = f.cell;
+    r.level = f.level;
+    if (f.cell >= 0) {
+        point_cell(f.level, x, y, z, r.c, r.fd);
+        for (int d = 0; d < 3; ++d) r.cen[d] = coord_center(f.level, r.c[d]);
+    }
+    return r;
+}
+
+// Deepest cell of point (x, y, z) given a nearby located cell `h`: the offset
+// from h's centre is formed in float64 (one subtraction per axis) and the rest
+// in FP32; the cell is h or one of its 26 neighbours read from h's record when
+// that neighbour is a leaf of h's level; otherwise a full walk.
+__device__ __forceinline__ Loc locate_near(const DevTree& T, const Loc& h, double x, double y, double z)
+{
     if (h.cell >= 0) {
-        float fd[3];
-        point_cell(h.level, x, y, z, r.c, fd);
-        const int ox = (int)(r.c[0] - h.c[0]), oy = (int)(r.c[1] - h.c[1]), oz = (int)(r.c[2] - h.c[2]);
+        const float sc = cells_per_unit(h.level);
+        const float rx = (float)(x - h.cen[0]) * sc, ry = (float)(y - h.cen[1]) * sc, rz = (float)(z - h.cen[2]) * sc;
+        const int ox = (int)floorf(rx + 0.5f), oy = (int)floorf(ry + 0.5f), oz = (int)floorf(rz + 0.5f);
         if (ox == 0 && oy == 0 && oz == 0) {
-            r.cell = h.cell;
-            r.level = h.level;
+            Loc r = h;
+            r.fd[0] = rx; r.fd[1] = ry; r.fd[2] = rz;
             return r;
         }
         if (abs(ox) <= 1 && abs(oy) <= 1 && abs(oz) <= 1) {
@@ -120,29 +138,49 @@ __device__ __forceinline__ Loc locate_near(const DevTree& T, const Loc& h, doubl
             if (e >= 0) {
                 const int fl = rec_flags(T, e);
                 if (!(fl & 256) && (fl & 255) == h.level) {
+                    Loc r;
                     r.cell = e;
                     r.level = h.level;
+                    const double w = cell_extent(h.level);
+                    r.c[0] = h.c[0] + ox; r.c[1] = h.c[1] + oy; r.c[2] = h.c[2] + oz;
+                    r.cen[0] = h.cen[0] + ox * w; r.cen[1] = h.cen[1] + oy * w; r.cen[2] = h.cen[2] + oz * w;
+                    r.fd[0] = rx - (float)ox; r.fd[1] = ry - (float)oy; r.fd[2] = rz - (float)oz;
                     return r;
                 }
             }
         }
     }
-    const Found f = locate_slow(T, x, y, z);
-    r.cell = f.cell;
-    r.level = f.level;
-    if (f.cell >= 0) {
-        float fd[3];
-        point_cell(f.level, x, y, z, r.c, fd);
+    return locate_full(T, x, y, z);
+}
+
+// The point one cell away from a located point along an axis: same in-cell
+// offset, neighbouring cell from the record (the six Jacobian points).
+__device__ __forceinline__ Loc step_cell(const DevTree& T, const Loc& h, int axis, int sgn, double x, double y, double z)
+{
+    const int ox = axis == 0 ? sgn : 0, oy = axis == 1 ? sgn : 0, oz = axis == 2 ? sgn : 0;
+    const int e = rec_entry(T, h.cell, (ox + 1) * 9 + (oy + 1) * 3 + (oz + 1));
+    if (e >= 0) {
+        const int fl = rec_flags(T, e);
+        if (!(fl & 256) && (fl & 255) == h.level) {
+            Loc r = h;
+            r.cell = e;
+            const double w = cell_extent(h.level);
+            r.c[0] += ox; r.c[1] += oy; r.c[2] += oz;
+            r.cen[0] += ox * w; r.cen[1] += oy * w; r.cen[2] += oz * w;
+            return r;
+        }
     }
-    return r;
+    return locate_full(T, x, y, z);
 }
 
 // TSC at a point whose deepest cell is `cell` (simplehyperoctree.h:1479-1541
 // through the stencil records).  Returns false when a restart centre is not
 // itself a cell (left to the slow path).
-__device__ __forceinline__ bool tsc_rec(const DevTree& T, int cell, int L, double x, double y, double z, bool need_all,
+__device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, double x, double y, double z, bool need_all,
                                         Field7& res)
 {
+    int cell = d.cell, L = d.level;
+    float fd[3] = {d.fd[0], d.fd[1], d.fd[2]};
     for (int guard = 0; guard <= kMaxLevel; ++guard) {
         const int4* rp = T.stencil + 8 * (size_t)cell;
         const int4 r7 = __ldg(rp + 7);
@@ -154,9 +192,6 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, int cell, int L, doubl
                 const int4 v = __ldg(rp + q);
                 e[4 * q] = v.x; e[4 * q + 1] = v.y; e[4 * q + 2] = v.z; e[4 * q + 3] = v.w;
             }
-            uint32_t c[3];
-            float fd[3];
-            point_cell(L, x, y, z, c, fd);
             float wx[3], wy[3], wz[3];
             tsc_w3(fd[0], wx);
             tsc_w3(fd[1], wy);
@@ -187,18 +222,19 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, int cell, int L, doubl
         if (f.cell < 0 || f.level != lc) return false;
         cell = f.cell;
         L = lc;
+        uint32_t c[3];
+        point_cell(L, x, y, z, c, fd);
     }
     return false;
 }
 
 // CIC at a point whose deepest cell is `cell` (simplehyperoctree.h:1410-1469).
-__device__ __forceinline__ bool cic_rec(const DevTree& T, int cell, int L, double x, double y, double z, bool need_all,
+__device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, double x, double y, double z, bool need_all,
                                         Field7& res)
 {
+    int cell = d.cell, L = d.level;
+    float fd[3] = {d.fd[0], d.fd[1], d.fd[2]};
     for (int guard = 0; guard <= kMaxLevel; ++guard) {
-        uint32_t c[3];
-        float fd[3];
-        point_cell(L, x, y, z, c, fd);
         const int sx = (fd[0] >= 0.f) ? 1 : -1, sy = (fd[1] >= 0.f) ? 1 : -1, sz = (fd[2] >= 0.f) ? 1 : -1;
         const float ax = fabsf(fd[0]), ay = fabsf(fd[1]), az = fabsf(fd[2]);
         int lvl = L;
@@ -230,12 +266,16 @@ __device__ __forceinline__ bool cic_rec(const DevTree& T, int cell, int L, doubl
         if (f.cell < 0 || f.level != lvl) return false;
         cell = f.cell;
         L = lvl;
+        uint32_t c[3];
+        point_cell(L, x, y, z, c, fd);
     }
     return false;
 }
 
+// maybe_origin: the point can be the exact origin (first step of a ray),
+// where the reference's TSC falls back to CIC (simplehyperoctree.h:1570-1571)
 __device__ __forceinline__ Field7 gather_at(const DevTree& T, int order, const Loc& d, double x, double y, double z, bool need_all,
-                                            unsigned long long* st, int slot)
+                                            unsigned long long* st, int slot, bool maybe_origin)
 {
     Field7 r;
     if (d.cell < 0) {
@@ -243,9 +283,8 @@ __device__ __forceinline__ Field7 gather_at(const DevTree& T, int order, const L
         stat(st, slot);
         return r;
     }
-    if (!(x == 0.0 && y == 0.0 && z == 0.0)) {
-        const bool ok = (order == 1) ? cic_rec(T, d.cell, d.level, x, y, z, need_all, r)
-                                     : tsc_rec(T, d.cell, d.level, x, y, z, need_all, r);
+    if (!(maybe_origin && x == 0.0 && y == 0.0 && z == 0.0)) {
+        const bool ok = (order == 1) ? cic_rec(T, d, x, y, z, need_all, r) : tsc_rec(T, d, x, y, z, need_all, r);
         if (ok) {
             stat(st, slot);
             return r;
@@ -262,12 +301,21 @@ struct FastRec {
     int level;
 };
 
+// 1/a: FP32 seed refined by two Newton steps (full float64 accuracy)
+__device__ __forceinline__ double recip(double a)
+{
+    double r = (double)(1.0f / (float)a);
+    r = fma(r, fma(-a, r, 1.0), r);
+    r = fma(r, fma(-a, r, 1.0), r);
+    return r;
+}
+
 __device__ __forceinline__ void rhs_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const Loc& here,
-                                         double inv_scale, const double* in, double* out, unsigned long long* st)
+                                         double inv_scale, const double* in, double* out, unsigned long long* st, bool maybe_origin)
 {
     const double c2 = kC * kC;
     const Loc d = locate_near(T, here, in[2], in[3], in[4]);
-    const Field7 g = gather_at(T, P.order, d, in[2], in[3], in[4], false, st, ST_RK_REC);
+    const Field7 g = gather_at(T, P.order, d, in[2], in[3], in[4], false, st, ST_RK_REC, maybe_origin);
     const double dphidl = (double)g.dt * in[5] + ((double)g.dx * in[6] + (double)g.dy * in[7] + (double)g.dz * in[8]);
     const double dadt = interp_fast(C, in[1], C.dadt, C.slope_dadt);
     out[0] = in[5] * dadt;
@@ -275,7 +323,7 @@ __device__ __forceinline__ void rhs_fast(const DevTree& T, const DevCosmo& C, co
     out[2] = in[6] * inv_scale;
     out[3] = in[7] * inv_scale;
     out[4] = in[8] * inv_scale;
-    const double hub = 2.0 * dadt / in[0] * in[5];
+    const double hub = 2.0 * dadt * recip(in[0]) * in[5];
     const double gg = (2.0 / c2) * dphidl;
     const double k02 = 2.0 * in[5] * in[5];
     out[5] = -(hub * in[5]) - ((2.0 / c2) * in[5]) * (dphidl - (double)g.dt * in[5]);
@@ -290,15 +338,15 @@ __device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, doub
                                          unsigned long long* st)
 {
     const double dl = ldexp(1.0, kLevelShift + 1 - here.level);
-    const double h = 0.5 * dl;
+    const double h = 0.5 * dl;   // one cell of the point's level
     float g[6][3];
 #pragma unroll 1
     for (int a = 0; a < 6; ++a) {
         const int ax = a >> 1;
-        const double sg = (a & 1) ? h : -h;
-        const double qx = x + (ax == 0 ? sg : 0.0), qy = y + (ax == 1 ? sg : 0.0), qz = z + (ax == 2 ? sg : 0.0);
-        const Loc d = locate_near(T, here, qx, qy, qz);
-        const Field7 f = gather_at(T, 2, d, qx, qy, qz, false, st, ST_JAC_REC);
+        const int sgn = (a & 1) ? 1 : -1;
+        const double qx = x + (ax == 0 ? sgn * h : 0.0), qy = y + (ax == 1 ? sgn * h : 0.0), qz = z + (ax == 2 ? sgn * h : 0.0);
+        const Loc d = step_cell(T, here, ax, sgn, qx, qy, qz);
+        const Field7 f = gather_at(T, 2, d, qx, qy, qz, false, st, ST_JAC_REC, false);
         g[a][0] = f.dx; g[a][1] = f.dy; g[a][2] = f.dz;
     }
     const float idl = (float)(1.0 / dl);
@@ -331,10 +379,8 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         b.a = 1.0; b.t = 0.0; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = 1.0;
         b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
     }
-    Loc here;
-    here.cell = -1;
-    here = locate_near(T, here, b.x, b.y, b.z);
-    Field7 data = gather_at(T, P.order, here, b.x, b.y, b.z, true, st, ST_POST_REC);
+    Loc here = locate_full(T, b.x, b.y, b.z);
+    Field7 data = gather_at(T, P.order, here, b.x, b.y, b.z, true, st, ST_POST_REC, true);
     {
         const double ph = (double)data.phi / c2;
         const double norm = sqrt((c2 * (1.0 + 2.0 * ph) * b.k0 * b.k0) / ((1.0 - 2.0 * ph) * (b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3)));
@@ -345,12 +391,14 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     b.ah = 0.f;
     b.rho = data.rho; b.phi = data.phi; b.dx = data.dx; b.dy = data.dy; b.dz = data.dz; b.dt = data.dt;
     b.red = 0.0; b.isw = 0.0; b.chi = 0.0; b.iswold = 0.0; b.lambda = 0.0; b.s = 0.0;
-    double ratio = b.a * b.a * (scale / kC) / P.nsteps;
+    const double ratio_k = (scale / kC) / P.nsteps;
+    double ratio = b.a * b.a * ratio_k;
     double dl = (here.cell >= 0 ? cell_extent(here.level) : 0.0) * ratio;
     const double a0 = b.a;
     const double phi0c2 = b.phi / c2;
     float last_data_dt = data.dt;
-    double last_lap = 0.0;
+    float last_dphi = 0.f;
+    double last_dl = 1.0;
 
     int next_plane = 0;
     long long cross_k[kMaxPlanes];
@@ -378,7 +426,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         // stages: core = b + c_s dl * d_{s-1};  acc = d0 + 2 d1 + 2 d2 + d3 (in that order)
 #pragma unroll 1
         for (int sg = 0; sg < 4; ++sg) {
-            rhs_fast(T, C, P, here, inv_scale, (sg == 0) ? bc : core, dc, st);
+            rhs_fast(T, C, P, here, inv_scale, (sg == 0) ? bc : core, dc, st, k == 0);
             const double cs = (sg < 2) ? 0.5 * dl : dl;
             const double wa = (sg == 0) ? 0.0 : 2.0;
             if (sg < 3) {
@@ -395,27 +443,29 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         p.a = core[0]; p.t = core[1]; p.x = core[2]; p.y = core[3]; p.z = core[4];
         p.k0 = core[5]; p.k1 = core[6]; p.k2 = core[7]; p.k3 = core[8];
         const Loc ploc = locate_near(T, here, p.x, p.y, p.z);
-        data = gather_at(T, P.order, ploc, p.x, p.y, p.z, true, st, ST_POST_REC);
+        data = gather_at(T, P.order, ploc, p.x, p.y, p.z, true, st, ST_POST_REC, false);
         if (!(!(p.a < 0.0) && ((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx)))) clear(data);
         p.level = (ploc.cell >= 0) ? ploc.level : 0;
         p.ah = data.a;
         p.rho = data.rho; p.phi = data.phi; p.dx = data.dx; p.dy = data.dy; p.dz = data.dz;
         p.dt = -data.dt;
-        const double lap = ((double)data.phi - b.phi) / dl;
+        const float dphi_last = data.phi - (float)b.phi;   // laplacian of the final record, divided at the end
+        const double dl_last = dl;
         isw += ((double)b.dt + (double)p.dt) * (p.t - b.t) * (1.0 / c2);
         iswold -= 2.0 * (p.phi - b.phi) * (1.0 / c2) -
                   (((double)b.dx + (double)p.dx) * (p.x - b.x) * scale + ((double)b.dy + (double)p.dy) * (p.y - b.y) * scale +
                    ((double)b.dz + (double)p.dz) * (p.z - b.z) * scale) * (1.0 / c2);
         p.chi = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
         lambda += dl;
-        sacc += sqrt((p.x - b.x) * (p.x - b.x) + (p.y - b.y) * (p.y - b.y) + (p.z - b.z) * (p.z - b.z));
+        sacc += (double)sqrtf((float)((p.x - b.x) * (p.x - b.x) + (p.y - b.y) * (p.y - b.y) + (p.z - b.z) * (p.z - b.z)));
         p.red = a0 / p.a * (1.0 + phi0c2 - p.phi / c2) - 1.0;
         p.isw = isw; p.iswold = iswold; p.lambda = lambda; p.s = sacc;
         if (!is_empty(data)) {
-            ratio = p.a * p.a * (scale / kC) / P.nsteps;
+            ratio = p.a * p.a * ratio_k;
             dl = (ploc.cell >= 0 ? cell_extent(ploc.level) : 0.0) * ratio;
             last_data_dt = data.dt;
-            last_lap = lap;
+            last_dphi = dphi_last;
+            last_dl = dl_last;
             if (ploc.cell != here.cell) stat(st, ST_CELL_CHANGE);
             here = ploc;
             ++k;
@@ -519,7 +569,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             r.level = b.level; r.ah = b.ah; r.rho = b.rho; r.phi = b.phi;
             r.dx = b.dx; r.dy = b.dy; r.dz = b.dz; r.dt = b.dt;
             r.dphidl = (k > 0) ? ((double)last_data_dt * b.k0 + ((double)b.dx * b.k1 + (double)b.dy * b.k2 + (double)b.dz * b.k3)) : 0.0;
-            r.lap = (k > 0) ? last_lap : 0.0;
+            r.lap = (k > 0) ? (double)last_dphi / last_dl : 0.0;
             const double kk = b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3;
             r.ds2 = (b.a * b.a) * (-(c2 * (1.0 + 2.0 * (b.phi / c2)) * b.k0 * b.k0) + ((1.0 - 2.0 * (b.phi / c2)) * kk));
             r.err = 1.0 - ((1.0 - 2.0 * (b.phi / c2)) * kk) / (c2 * (1.0 + 2.0 * (b.phi / c2)) * b.k0 * b.k0);
@@ -574,14 +624,12 @@ __global__ void k_gather_rec(DevTree T, int kind, const double* __restrict__ xyz
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
-    Loc none;
-    none.cell = -1;
-    const Loc d = locate_near(T, none, x, y, z);
+    const Loc d = locate_full(T, x, y, z);
     if (kind == 0) {
         ((long long*)out)[i] = d.cell;
         return;
     }
-    const Field7 f = gather_at(T, kind, d, x, y, z, true, nullptr, 0);
+    const Field7 f = gather_at(T, kind, d, x, y, z, true, nullptr, 0, true);
     float* o = (float*)out + 7 * i;
     o[0] = f.rho; o[1] = f.phi; o[2] = f.dx; o[3] = f.dy; o[4] = f.dz; o[5] = f.a; o[6] = f.dt;
 }
