@@ -42,7 +42,7 @@ UNIT = "photon-steps/s"
 BYTES_PER_PHOTON_STEP = 4 * 27 * 16 + 27 * 28 + 6 * 27 * 12
 # DRAM bytes per photon-step of the propagate kernel measured with ncu on the AMR
 # workload (profiles/propagate_tsc_amr.md); None until measured
-DRAM_BYTES_PER_PHOTON_STEP = None
+DRAM_BYTES_PER_PHOTON_STEP = 6.8   # measured: (43.6 + 427.5) MB over 6.95e7 photon-steps, medium octree
 
 
 def workload_spec(synth, workload: str):

@@ -274,9 +274,11 @@ __device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, double x
 
 // maybe_origin: the point can be the exact origin (first step of a ray),
 // where the reference's TSC falls back to CIC (simplehyperoctree.h:1570-1571)
-__device__ __forceinline__ Field7 gather_at(const DevTree& T, int order, const Loc& d, double x, double y, double z, bool need_all,
+template <int ORDER>
+__device__ __forceinline__ Field7 gather_at(const DevTree& T, const Loc& d, double x, double y, double z, bool need_all,
                                             unsigned long long* st, int slot, bool maybe_origin)
 {
+    constexpr int order = ORDER;
     Field7 r;
     if (d.cell < 0) {
         clear(r);
@@ -310,12 +312,11 @@ __device__ __forceinline__ double recip(double a)
     return r;
 }
 
-__device__ __forceinline__ void rhs_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const Loc& here,
-                                         double inv_scale, const double* in, double* out, unsigned long long* st, bool maybe_origin)
+
+// geodesic RHS (integrator.h:409-445) from the field at the point
+__device__ __forceinline__ void rhs_math(const DevCosmo& C, const Field7& g, double inv_scale, const double* in, double* out)
 {
     const double c2 = kC * kC;
-    const Loc d = locate_near(T, here, in[2], in[3], in[4]);
-    const Field7 g = gather_at(T, P.order, d, in[2], in[3], in[4], false, st, ST_RK_REC, maybe_origin);
     const double dphidl = (double)g.dt * in[5] + ((double)g.dx * in[6] + (double)g.dy * in[7] + (double)g.dz * in[8]);
     const double dadt = interp_fast(C, in[1], C.dadt, C.slope_dadt);
     out[0] = in[5] * dadt;
@@ -346,7 +347,7 @@ __device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, doub
         const int sgn = (a & 1) ? 1 : -1;
         const double qx = x + (ax == 0 ? sgn * h : 0.0), qy = y + (ax == 1 ? sgn * h : 0.0), qz = z + (ax == 2 ? sgn * h : 0.0);
         const Loc d = step_cell(T, here, ax, sgn, qx, qy, qz);
-        const Field7 f = gather_at(T, 2, d, qx, qy, qz, false, st, ST_JAC_REC, false);
+        const Field7 f = gather_at<2>(T, d, qx, qy, qz, false, st, ST_JAC_REC, false);
         g[a][0] = f.dx; g[a][1] = f.dy; g[a][2] = f.dz;
     }
     const float idl = (float)(1.0 / dl);
@@ -364,6 +365,7 @@ __device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, doub
               cp * s2t * dxz;
 }
 
+template <int ORDER>
 __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* L, long long i,
                                const PropOut& O)
 {
@@ -380,7 +382,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
     }
     Loc here = locate_full(T, b.x, b.y, b.z);
-    Field7 data = gather_at(T, P.order, here, b.x, b.y, b.z, true, st, ST_POST_REC, true);
+    Field7 data = gather_at<ORDER>(T, here, b.x, b.y, b.z, true, st, ST_POST_REC, true);
     {
         const double ph = (double)data.phi / c2;
         const double norm = sqrt((c2 * (1.0 + 2.0 * ph) * b.k0 * b.k0) / ((1.0 - 2.0 * ph) * (b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3)));
@@ -424,9 +426,17 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         if (k >= P.max_steps) { status |= 1u; break; }
         const double bc[9] = {b.a, b.t, b.x, b.y, b.z, b.k0, b.k1, b.k2, b.k3};
         // stages: core = b + c_s dl * d_{s-1};  acc = d0 + 2 d1 + 2 d2 + d3 (in that order)
+        // stage 1 is at b, where the previous step's post-step gather already
+        // read the field (data); stages 2-4 gather at their own points
 #pragma unroll 1
         for (int sg = 0; sg < 4; ++sg) {
-            rhs_fast(T, C, P, here, inv_scale, (sg == 0) ? bc : core, dc, st, k == 0);
+            if (sg == 0) {
+                rhs_math(C, data, inv_scale, bc, dc);
+            } else {
+                const Loc d = locate_near(T, here, core[2], core[3], core[4]);
+                const Field7 g = gather_at<ORDER>(T, d, core[2], core[3], core[4], false, st, ST_RK_REC, false);
+                rhs_math(C, g, inv_scale, core, dc);
+            }
             const double cs = (sg < 2) ? 0.5 * dl : dl;
             const double wa = (sg == 0) ? 0.0 : 2.0;
             if (sg < 3) {
@@ -443,7 +453,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         p.a = core[0]; p.t = core[1]; p.x = core[2]; p.y = core[3]; p.z = core[4];
         p.k0 = core[5]; p.k1 = core[6]; p.k2 = core[7]; p.k3 = core[8];
         const Loc ploc = locate_near(T, here, p.x, p.y, p.z);
-        data = gather_at(T, P.order, ploc, p.x, p.y, p.z, true, st, ST_POST_REC, false);
+        data = gather_at<ORDER>(T, ploc, p.x, p.y, p.z, true, st, ST_POST_REC, false);
         if (!(!(p.a < 0.0) && ((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx)))) clear(data);
         p.level = (ploc.cell >= 0) ? ploc.level : 0;
         p.ah = data.a;
@@ -602,6 +612,7 @@ constexpr int kFastThreads = 128;
 // Persistent launch: each warp takes the next 32 rays from a global counter
 // until the batch is exhausted, so uneven path lengths do not leave tail
 // waves.  `queue` is zeroed before the launch.
+template <int ORDER>
 __global__ void __launch_bounds__(kFastThreads, 3) k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
                                                                     const double* __restrict__ launch, long long n, PropOut O,
                                                                     unsigned long long* queue)
@@ -613,7 +624,7 @@ __global__ void __launch_bounds__(kFastThreads, 3) k_propagate_fast(DevTree T, D
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= (unsigned long long)n) break;
         const long long i = (long long)base + lane;
-        if (i < n) propagate_fast(T, C, P, launch + 6 * i, i, O);
+        if (i < n) propagate_fast<ORDER>(T, C, P, launch + 6 * i, i, O);
         __syncwarp();
     }
 }
@@ -629,7 +640,8 @@ __global__ void k_gather_rec(DevTree T, int kind, const double* __restrict__ xyz
         ((long long*)out)[i] = d.cell;
         return;
     }
-    const Field7 f = gather_at(T, kind, d, x, y, z, true, nullptr, 0, true);
+    const Field7 f = (kind == 1) ? gather_at<1>(T, d, x, y, z, true, nullptr, 0, true)
+                                 : gather_at<2>(T, d, x, y, z, true, nullptr, 0, true);
     float* o = (float*)out + 7 * i;
     o[0] = f.rho; o[1] = f.phi; o[2] = f.dx; o[3] = f.dy; o[4] = f.dz; o[5] = f.a; o[6] = f.dt;
 }
