@@ -716,6 +716,222 @@ int64_t mpfo_trajectory(const mpfo_tree* T, const mpfo_cosmo* C, int order, doub
     return m;
 }
 
+/* ---------------------------------------------------------------------- */
+/* catalogue root-finder                                                   */
+/* ---------------------------------------------------------------------- */
+/* Integrator::launch, (phi, theta) form (integrator.h:305-329). */
+static void launch5(double phi, double theta, double* p)
+{
+    memset(p, 0, MPFO_PHOTON * sizeof(double));
+    p[PA] = 1.0;
+    p[PK0] = 1.0;
+    p[PK1] = cos(phi) * sin(theta);
+    p[PK2] = sin(phi) * sin(theta);
+    p[PK3] = cos(theta);
+}
+
+typedef struct {
+    const mpfo_tree* T;
+    const mpfo_cosmo* C;
+    int order, max_iterations;
+    double length, accuracy, h, mpc;
+    unsigned nsteps;
+    const double* src;
+    const double* rot;
+    const double* vobs;
+    double* out;
+    int64_t n, next;
+    pthread_mutex_t mu;
+} cjob_t;
+
+/* One Catalogues::newtonMethod2d call (catalogues.h:410-727) with
+ * jacobiantype = infinitesimal and use_previous_catalogues = 0: res =
+ * {{phi', theta'}, {miss, firstid}}; jac and z are updated in place as the
+ * reference updates its jacobian and redshifts arguments. */
+static void newton2d(ctx_t* c, traj_t* tr, const cjob_t* J, const double* target, const double* vel, double dist,
+                     double phi, double theta, unsigned iteration, double res[2][2], double jac[2][2], double* z)
+{
+    static const double cl = C_LIGHT, c2 = C_LIGHT * C_LIGHT;
+    tr->n = 0;
+    launch5(phi, theta, traj_push(tr));
+    integrate(c, tr, J->nsteps, MPFO_STOP_R, dist, (const double[3]){0, 0, 0});
+    const int64_t marked = tr->n - 1;
+    const int64_t firstid = marked - (marked > 0);
+    const double* P0 = tr->p + MPFO_PHOTON * firstid;
+    if (marked == 0 || tr->p[MPFO_PHOTON * marked + PCHI] < dist) {
+        res[0][0] = 42; res[0][1] = 42; res[1][0] = 0; res[1][1] = (double)firstid;
+        return;
+    }
+    const double* P1 = P0 + MPFO_PHOTON;
+    const double previous = P0[PCHI], next = P1[PCHI];
+    const double f = (next - dist) / (next - previous);
+    z[1] = P0[PZRED] * f + P1[PZRED] * (1 - f);
+    const double scale_factor = P0[PA] * f + P1[PA] * (1 - f);
+    double fp[3];
+    fp[0] = P0[PX] * f + P1[PX] * (1 - f);
+    fp[1] = P0[PY] * f + P1[PY] * (1 - f);
+    fp[2] = P0[PZ] * f + P1[PZ] * (1 - f);
+    const double dist_sep = sqrt(pow(target[0] - fp[0], 2) + pow(target[1] - fp[1], 2) + pow(target[2] - fp[2], 2));
+    res[1][0] = dist_sep / dist;
+    if (res[1][0] > J->accuracy) {
+        double ji[2][2] = {{1, 0}, {0, 1}};
+        if (iteration >= 3) {
+            double A[3];
+            jacobian(c, tr, 1, &dist, A);
+            jac[0][0] = A[0]; jac[0][1] = A[1]; jac[1][0] = A[1]; jac[1][1] = A[2];
+            /* Utility::invMatrix2d (utility.h:686-696) */
+            const double invdet = 1. / (jac[0][0] * jac[1][1] - jac[0][1] * jac[1][0]);
+            ji[0][0] = jac[1][1] * invdet;
+            ji[0][1] = -jac[0][1] * invdet;
+            ji[1][0] = -jac[1][0] * invdet;
+            ji[1][1] = jac[0][0] * invdet;
+        }
+        /* Newton step in the screen basis (catalogues.h:625-655) */
+        const double cp = cos(phi), sp = sin(phi), ct = cos(theta), st = sin(theta);
+        double e1[3], e2[3], sep[3], pos[3], targeted[3];
+        e1[0] = -sp; e1[1] = cp; e1[2] = 0;
+        e2[0] = -cp * ct; e2[1] = -sp * ct; e2[2] = st;
+        targeted[0] = dist * cp * st;
+        targeted[1] = dist * sp * st;
+        targeted[2] = dist * ct;
+        for (int k = 0; k < 3; ++k) {
+            sep[k] = fp[k] - target[k];
+            pos[k] = targeted[k] - target[k];
+        }
+        const double sepx = sep[0] * e1[0] + sep[1] * e1[1];
+        const double sepy = sep[0] * e2[0] + sep[1] * e2[1] + sep[2] * e2[2];
+        const double posx = pos[0] * e1[0] + pos[1] * e1[1];
+        const double posy = pos[0] * e2[0] + pos[1] * e2[1] + pos[2] * e2[2];
+        const double sepxnew = ji[0][0] * sepx + ji[0][1] * sepy;
+        const double sepynew = ji[1][0] * sepx + ji[1][1] * sepy;
+        const double posxnew = posx - sepxnew;
+        const double posynew = posy - sepynew;
+        const double xnew = target[0] + (posxnew * e1[0] + posynew * e2[0]);
+        const double ynew = target[1] + (posxnew * e1[1] + posynew * e2[1]);
+        const double znew = target[2] + posynew * e2[2];
+        res[0][0] = atan2(ynew, xnew);
+        res[0][1] = acos(znew / sqrt(xnew * xnew + ynew * ynew + znew * znew));
+        return;
+    }
+    /* converged: Jacobian and redshift decomposition (catalogues.h:660-723) */
+    {
+        double A[3];
+        jacobian(c, tr, 1, &dist, A);
+        jac[0][0] = A[0]; jac[0][1] = A[1]; jac[1][0] = A[1]; jac[1][1] = A[2];
+    }
+    const double* T0 = tr->p;
+    const double* vo = J->vobs;
+    const double potential = P0[PPHI] * f + P1[PPHI] * (1 - f);
+    const double isw = P0[PISW] * f + P1[PISW] * (1 - f);
+    z[0] = -1 + 1. / (scale_factor);
+    const double unit_t = scale_factor * scale_factor * J->mpc / (J->h * 100.0 * 1000.0);
+    const double unit_l = scale_factor * c->length * 100;
+    const double velocityx = vel[0] * unit_l * 1e-2 / (unit_t * cl);
+    const double velocityy = vel[1] * unit_l * 1e-2 / (unit_t * cl);
+    const double velocityz = vel[2] * unit_l * 1e-2 / (unit_t * cl);
+    const double gref = -T0[PA] * cl * T0[PK0] * (1. + T0[PPHI] / c2 + (vo[0] * T0[PK1] + vo[1] * T0[PK2] + vo[2] * T0[PK3]) / (cl * T0[PK0]) +
+                                                   0.5 * (vo[0] * vo[0] + vo[1] * vo[1] + vo[2] * vo[2]));
+    const double dtdl = P0[PK0] * f + P1[PK0] * (1 - f);
+    const double dxdl = P0[PK1] * f + P1[PK1] * (1 - f);
+    const double dydl = P0[PK2] * f + P1[PK2] * (1 - f);
+    const double dzdl = P0[PK3] * f + P1[PK3] * (1 - f);
+    const double gK = -scale_factor * cl * dtdl * (1. + potential / c2 + (velocityx * dxdl + velocityy * dydl + velocityz * dzdl) / (cl * dtdl) +
+                                                    0.5 * (velocityx * velocityx + velocityy * velocityy + velocityz * velocityz));
+    z[2] = z[1] + (velocityx * dxdl + velocityy * dydl + velocityz * dzdl) / (scale_factor * cl * dtdl) -
+           (vo[0] * T0[PK1] + vo[1] * T0[PK2] + vo[2] * T0[PK3]) / (scale_factor * cl * T0[PK0]);
+    z[3] = z[2] + 0.5 * (velocityx * velocityx + velocityy * velocityy + velocityz * velocityz - vo[0] * vo[0] - vo[1] * vo[1] - vo[2] * vo[2]) / scale_factor;
+    z[4] = z[3] + isw / scale_factor;
+    z[5] = gK / gref - 1;
+    res[0][0] = phi;
+    res[0][1] = theta;
+}
+
+/* Catalogues::iterateNewtonMethod (catalogues.h:757-783) behind relCat's
+ * per-source setup and row (catalogues.h:811-856). */
+static void catalogue_one(ctx_t* c, traj_t* tr, const cjob_t* J, int64_t i)
+{
+    const double* s = J->src + 6 * i;
+    double target[3], vel[3];
+    for (int j = 0; j < 3; ++j) {
+        if (!J->rot) {
+            target[j] = s[j];
+            vel[j] = s[j + 3];
+        } else {
+            target[j] = s[0] * J->rot[3 * j + 0] + s[1] * J->rot[3 * j + 1] + s[2] * J->rot[3 * j + 2];
+            vel[j] = s[3] * J->rot[3 * j + 0] + s[4] * J->rot[3 * j + 1] + s[5] * J->rot[3 * j + 2];
+        }
+    }
+    const double dist = sqrt(target[0] * target[0] + target[1] * target[1] + target[2] * target[2]);
+    const double theta = acos(target[2] / dist);
+    const double phi = atan2(target[1], target[0]);
+    double res[2][2] = {{phi, theta}, {0, 0}};
+    double jac[2][2] = {{0, 0}, {0, 0}};
+    double z[6] = {0, 0, 0, 0, 0, 0};
+    unsigned iteration = 0;
+    for (;;) {
+        const double p0 = res[0][0], t0 = res[0][1];
+        newton2d(c, tr, J, target, vel, dist, p0, t0, iteration, res, jac, z);
+        iteration++;
+        if (res[0][0] == 42 && res[0][1] == 42) break;
+        if (iteration > (unsigned)J->max_iterations && res[1][0] > J->accuracy) {
+            res[1][1] = 42;
+            break;
+        }
+        if (!(res[1][0] > J->accuracy)) {
+            res[1][1] = iteration;
+            break;
+        }
+    }
+    double* o = J->out + 16 * i;
+    o[0] = phi; o[1] = theta;
+    o[2] = res[0][0]; o[3] = res[0][1]; o[4] = res[1][0]; o[5] = res[1][1];
+    for (int k = 0; k < 6; ++k) o[6 + k] = z[k];
+    o[12] = jac[0][0]; o[13] = jac[0][1]; o[14] = jac[1][0]; o[15] = jac[1][1];
+}
+
+static void* cworker(void* arg)
+{
+    cjob_t* J = (cjob_t*)arg;
+    ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+    traj_t tr = {0, 0, 0};
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        const int64_t i = J->next++;
+        pthread_mutex_unlock(&J->mu);
+        if (i >= J->n) break;
+        c->T = J->T;
+        c->C = J->C;
+        c->order = J->order;
+        c->length = J->length;
+        cache_init(&c->cache);
+        catalogue_one(c, &tr, J, i);
+    }
+    free(tr.p);
+    free(c);
+    return 0;
+}
+
+int mpfo_catalogue(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
+                   int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
+                   double h, double mpc, int max_iterations, double* out, int nthreads)
+{
+    if (!T || !C || (order != 1 && order != 2) || nsteps == 0 || n < 0 || !vobs) return -1;
+    cjob_t J;
+    J.T = T; J.C = C; J.order = order; J.max_iterations = max_iterations; J.length = length;
+    J.accuracy = cat_accuracy; J.h = h; J.mpc = mpc; J.nsteps = nsteps; J.src = src; J.rot = rotm1;
+    J.vobs = vobs; J.out = out; J.n = n; J.next = 0;
+    pthread_mutex_init(&J.mu, 0);
+    if (nthreads <= 1) cworker(&J);
+    else {
+        pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+        for (int t = 0; t < nthreads; ++t) pthread_create(&th[t], 0, cworker, &J);
+        for (int t = 0; t < nthreads; ++t) pthread_join(th[t], 0);
+        free(th);
+    }
+    pthread_mutex_destroy(&J.mu);
+    return 0;
+}
+
 typedef struct {
     const mpfo_tree* T;
     int64_t n;

@@ -67,6 +67,17 @@ int mpfo_propagate(const mpfo_tree* T, const mpfo_cosmo* C, int order, double le
 int64_t mpfo_trajectory(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
                         int stop_kind, double stop_ref, const double* launch, double* out, int64_t cap);
 
+/* Catalogue root-finder (Catalogues::iterateNewtonMethod, infinitesimal
+ * Jacobian, at most max_iterations + 1 rays per source).  src: n x 6 (x y z
+ * vx vy vz in octree units and RAMSES velocity units), rotm1: 3x3 row-major
+ * rotation to the octree frame or NULL (full sky), vobs: observer velocity.
+ * out: n x 16 catalog rows: comoving phi theta, observed phi theta, miss,
+ * iterations (42: rejected; with phi = theta = 42: failed, then firstid),
+ * z_flrw z_pot z_dopp z_tdopp z_isw z_gr, a11 a12 a21 a22. */
+int mpfo_catalogue(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
+                   int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
+                   double h, double mpc, int max_iterations, double* out, int nthreads);
+
 void mpfo_batch_locate(const mpfo_tree* T, int64_t n, const double* xyz, int64_t* out, int nthreads);
 void mpfo_batch_cic(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads);
 void mpfo_batch_tsc(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads);

@@ -62,6 +62,9 @@ def lib():
                                      C.c_int, _p, _p, _p, C.c_int]
         L.mpfo_trajectory.restype = _i64
         L.mpfo_trajectory.argtypes = [_p, _p, C.c_int, _d, C.c_uint, C.c_int, _d, _p, _p, _i64]
+        L.mpfo_catalogue.restype = C.c_int
+        L.mpfo_catalogue.argtypes = [_p, _p, C.c_int, _d, C.c_uint, _i64, _p, _p, _p, _d, _d, _d, C.c_int, _p,
+                                     C.c_int]
         for f in ("mpfo_batch_locate", "mpfo_batch_cic", "mpfo_batch_tsc"):
             getattr(L, f).argtypes = [_p, _i64, _p, _p, C.c_int]
         _lib = L
@@ -133,3 +136,18 @@ class Oracle:
         m = self.L.mpfo_trajectory(C.byref(self.tree), C.byref(self.cosmo), order, self.length, nsteps,
                                    STOP[stop], stop_ref, _ptr(L), _ptr(out), cap)
         return out[:min(m, cap)]
+
+    def catalogue(self, sources, order=2, nsteps=10, cat_accuracy=1e-8, h=0.68, mpc=3.08568e22,
+                  vobs=(0.0, 0.0, 0.0), rotm1=None, max_iterations=10, nthreads=None):
+        """relCat rows (n x 16) for sources (n x 6: x y z vx vy vz)."""
+        src = np.ascontiguousarray(np.asarray(sources)[:, :6], dtype=np.float64)
+        vo = np.ascontiguousarray(vobs, dtype=np.float64)
+        rot = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64).reshape(9)
+        out = np.zeros((src.shape[0], 16))
+        rc = self.L.mpfo_catalogue(C.byref(self.tree), C.byref(self.cosmo), order, self.length, nsteps,
+                                   src.shape[0], _ptr(src), _ptr(rot) if rot is not None else None, _ptr(vo),
+                                   float(cat_accuracy), float(h), float(mpc), int(max_iterations), _ptr(out),
+                                   int(nthreads or self.nthreads))
+        if rc != 0:
+            raise ValueError("oracle catalogue failed: %d" % rc)
+        return out

@@ -77,6 +77,14 @@ using point = std::array<real, 3>;
 #include "gravity.h"
 #include "miscellaneous.h"
 #include "hmaps.h"
+// catalogues.h defines a parameters_t struct and a global `parameters` of
+// its own, as hmaps.h does; its dependencies are all in already, so it is
+// read with both names renamed.
+#define parameters_t catalogues_parameters_t
+#define parameters catalogues_parameters
+#include "catalogues.h"
+#undef parameters
+#undef parameters_t
 
 using namespace magrathea;
 using Index = SimpleHyperOctreeIndex<__uint128_t, 3>;
@@ -386,6 +394,60 @@ int ref_fillmap(long nside, int nz, const double* zvals, const char* stop_ray, c
 void ref_pix2vec_ring(long nside, int64_t n, const long* pix, double* vec)
 {
     for (int64_t i = 0; i < n; ++i) harness_pix2vec_ring(nside, pix[i], vec + 3 * i);
+}
+
+// Catalogues::relCat's per-source work (catalogues.h:811-856): the source
+// position and velocity (rotated by rotm1 unless it is null, the full-sky
+// case), the comoving first guess, Catalogues::iterateNewtonMethod with the
+// infinitesimal Jacobian, and the 16-double catalog row.
+// src: n x 6 (x y z vx vy vz); rotm1: 3x3 row-major or null; vobs: 3;
+// out: n x 16.
+void ref_catalogue(int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
+                   unsigned nsteps, double h, double mpc, double* out, int nthreads)
+{
+    catalogues_parameters_t P;
+    P.isfullsky = rotm1 ? 0 : 1;
+    P.mpc = mpc;
+    P.cat_accuracy = cat_accuracy;
+    P.jacobiantype = "infinitesimal";
+    P.plane = "normal";
+    P.stop_bundle = "r";
+    P.nsteps = nsteps;
+    P.use_previous_catalogues = 0;
+    P.openingmin = 0;
+    const point vo{{vobs[0], vobs[1], vobs[2]}};
+    const point observer{{0., 0., 0.}};
+    std::array<std::array<double, 3>, 3> rot{};
+    if (rotm1)
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k) rot[j][k] = rotm1[3 * j + k];
+    run_threads(n, nthreads, [&](int64_t i) {
+        const double* s = src + 6 * i;
+        point trueTarget, velocityTarget;
+        for (unsigned j = 0; j < 3; j++) {
+            if (P.isfullsky == 1) {
+                trueTarget[j] = s[j];
+                velocityTarget[j] = s[j + 3];
+            } else {
+                trueTarget[j] = s[0] * rot[j][0] + s[1] * rot[j][1] + s[2] * rot[j][2];
+                velocityTarget[j] = s[3] * rot[j][0] + s[4] * rot[j][1] + s[5] * rot[j][2];
+            }
+        }
+        std::array<std::array<double, 2>, 2> jacobian;
+        double interpRef = 0;
+        std::vector<double> redshifts(6);
+        const double distTarget = std::sqrt(trueTarget[0] * trueTarget[0] + trueTarget[1] * trueTarget[1] +
+                                            trueTarget[2] * trueTarget[2]);
+        const double theta = std::acos(trueTarget[2] / distTarget);
+        const double phi = std::atan2(trueTarget[1], trueTarget[0]);
+        auto result = Catalogues::iterateNewtonMethod(vo, observer, phi, theta, trueTarget, velocityTarget, jacobian, P,
+                                                      g_cosmo, g_octree, g_length, h, redshifts, interpRef);
+        double* o = out + 16 * i;
+        o[0] = phi; o[1] = theta;
+        o[2] = result[0][0]; o[3] = result[0][1]; o[4] = result[1][0]; o[5] = result[1][1];
+        for (int k = 0; k < 6; ++k) o[6 + k] = redshifts[k];
+        o[12] = jacobian[0][0]; o[13] = jacobian[0][1]; o[14] = jacobian[1][0]; o[15] = jacobian[1][1];
+    });
 }
 
 }  // extern "C"

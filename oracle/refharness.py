@@ -62,6 +62,7 @@ def lib(order: int = 2):
         L.ref_fillmap.restype = C.c_int
         L.ref_fillmap.argtypes = [C.c_long, C.c_int, _p, C.c_char_p, C.c_char_p, C.c_uint, _i64, _p, _p, _p]
         L.ref_pix2vec_ring.argtypes = [C.c_long, _i64, _p, _p]
+        L.ref_catalogue.argtypes = [_i64, _p, _p, _p, _d, C.c_uint, _d, _d, _p, C.c_int]
         _LIBS[order] = L
     return _LIBS[order]
 
@@ -169,4 +170,14 @@ class Reference:
         pix = np.ascontiguousarray(pixels, dtype=np.int64)
         out = np.zeros((pix.shape[0], 3))
         self.L.ref_pix2vec_ring(nside, pix.shape[0], _ptr(pix), _ptr(out))
+        return out
+
+    def catalogue(self, sources, cat_accuracy=1e-8, nsteps=10, h=0.68, mpc=3.08568e22, vobs=(0.0, 0.0, 0.0), rotm1=None):
+        """relCat rows (n x 16) for sources (n x 6: x y z vx vy vz)."""
+        src = np.ascontiguousarray(sources[:, :6], dtype=np.float64)
+        vo = np.ascontiguousarray(vobs, dtype=np.float64)
+        rot = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64).reshape(9)
+        out = np.zeros((src.shape[0], 16))
+        self.L.ref_catalogue(src.shape[0], _ptr(src), _ptr(rot) if rot is not None else None, _ptr(vo),
+                             float(cat_accuracy), int(nsteps), float(h), float(mpc), _ptr(out), self.nthreads)
         return out

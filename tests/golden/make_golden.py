@@ -9,7 +9,9 @@ Each fixture holds the octree records it was computed on (so the GPU machine,
 which has no reference, reads exactly the same bytes), the cosmology table
 the reference derived from its evolution file (Input::acquire + correct), and
 the reference's outputs: locate / cic / tsc at random points, per-ray step
-counts and final photon records (Integrator::integrate), and FillMap maps.
+counts and final photon records (Integrator::integrate), FillMap maps, and
+catalogue rows (Catalogues::iterateNewtonMethod through relCat's per-source
+setup) for seeded sources at three accuracies, with and without a rotation.
 """
 from __future__ import annotations
 
@@ -48,6 +50,32 @@ def cone_pixels(R, nside, half_deg):
     th = np.arccos(v[:, 2])
     sel = (np.abs(phi) < np.radians(half_deg)) & (np.abs(th - np.pi / 2) < np.radians(half_deg))
     return allp[sel]
+
+
+CAT_ACCURACIES = (1e-8, 1e-13, 0.0)   # job default; deep enough for the Jacobian steps; never met (rejects)
+CAT_VOBS = (1e-4, -2e-4, 5e-5)
+
+
+def catalogue_sources(rng, n, chi_max_box):
+    """Sources in the octree frame: most inside the data, the last 4 beyond it (failures)."""
+    d = rng.uniform(0.05, 0.95 * chi_max_box, n)
+    d[-4:] = rng.uniform(1.15 * chi_max_box, 1.4 * chi_max_box, 4)
+    ph = np.radians(rng.uniform(-2.0, 2.0, n))
+    th = np.pi / 2 + np.radians(rng.uniform(-2.0, 2.0, n))
+    src = np.zeros((n, 6))
+    src[:, 0] = d * np.cos(ph) * np.sin(th)
+    src[:, 1] = d * np.sin(ph) * np.sin(th)
+    src[:, 2] = d * np.cos(th)
+    src[:, 3:] = rng.normal(0.0, 1e-3, (n, 3))
+    return src
+
+
+def rotation(ax, ay, az):
+    cx, sx, cy, sy, cz, sz = np.cos(ax), np.sin(ax), np.cos(ay), np.sin(ay), np.cos(az), np.sin(az)
+    Rx = np.array([[1, 0, 0], [0, cx, -sx], [0, sx, cx]])
+    Ry = np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
+    Rz = np.array([[cz, -sz, 0], [sz, cz, 0], [0, 0, 1]])
+    return Rz @ Ry @ Rx
 
 
 def make(name, cfg):
@@ -97,6 +125,23 @@ def make(name, cfg):
         out["pixels"] = pix
         out["pixel_dirs"] = R.pix2vec(cfg["nside"], pix)
         out["ref_maps_o%d" % order] = R.fillmap(cfg["nside"], out["zs"], pix, "redshift", COMPONENTS, cfg["nsteps"])
+        if order == 1:
+            crng = np.random.default_rng(23)
+            src = catalogue_sources(crng, 40, spec.chi_max / spec.lbox)
+            rot = rotation(0.3, -0.2, 0.7)
+            out["cat_src"] = src
+            # the same sources given in a rotated frame, with the rotation to the octree frame
+            out["cat_src_rotated"] = np.concatenate([src[:, :3] @ rot, src[:, 3:] @ rot], axis=1)
+            out["cat_rotm1"] = rot
+            out["cat_vobs"] = np.array(CAT_VOBS)
+            out["cat_accuracy"] = np.array(CAT_ACCURACIES)
+            out["cosmo_h"] = cos["h"]
+            out["cosmo_mpc"] = 3.08568e22
+        for ia, acc in enumerate(CAT_ACCURACIES):
+            out["ref_cat_o%d_a%d" % (order, ia)] = R.catalogue(out["cat_src"], acc, cfg["nsteps"], out["cosmo_h"],
+                                                               out["cosmo_mpc"], CAT_VOBS)
+        out["ref_cat_rot_o%d" % order] = R.catalogue(out["cat_src_rotated"], CAT_ACCURACIES[0], cfg["nsteps"],
+                                                     out["cosmo_h"], out["cosmo_mpc"], CAT_VOBS, out["cat_rotm1"])
     path = os.path.join(HERE, "%s.npz" % name)
     np.savez_compressed(path, **out)
     print("%s: %d cells (levels %d-%d), %d rays, %d pixels -> %s (%d KB)" % (

@@ -52,6 +52,36 @@ def test_oracle_maps_bit_exact(golden, oracle_mod, maps_mod, order):
     np.testing.assert_array_equal(maps.view(np.uint32), ref.view(np.uint32))
 
 
+@pytest.mark.parametrize("order", [1, 2])
+def test_oracle_catalogue_bit_exact(golden, oracle_mod, order):
+    """Catalogue rows (Newton root-finder) of the C oracle == the reference's
+    iterateNewtonMethod at three accuracies, and through a frame rotation."""
+    O = _oracle(golden, oracle_mod)
+    kw = dict(order=order, nsteps=int(golden["nsteps"]), h=float(golden["cosmo_h"]), mpc=float(golden["cosmo_mpc"]),
+              vobs=golden["cat_vobs"])
+    for ia, acc in enumerate(golden["cat_accuracy"]):
+        rows = O.catalogue(golden["cat_src"], cat_accuracy=float(acc), **kw)
+        np.testing.assert_array_equal(rows.view(np.uint64), golden["ref_cat_o%d_a%d" % (order, ia)].view(np.uint64))
+    rows = O.catalogue(golden["cat_src_rotated"], cat_accuracy=float(golden["cat_accuracy"][0]),
+                       rotm1=golden["cat_rotm1"], **kw)
+    np.testing.assert_array_equal(rows.view(np.uint64), golden["ref_cat_rot_o%d" % order].view(np.uint64))
+
+
+def test_catalogue_fixture_covers_every_outcome(golden):
+    """The fixture holds converged (2-4 rays, so the infinitesimal-Jacobian
+    steps run), rejected (42 after 11 rays) and failed (phi = theta = 42) sources."""
+    r8 = golden["ref_cat_o2_a0"]
+    r13 = golden["ref_cat_o2_a1"]
+    r0 = golden["ref_cat_o2_a2"]
+    failed = r8[:, 2] == 42
+    assert 1 <= failed.sum() < r8.shape[0] // 2
+    assert np.all(r8[~failed, 5] >= 2) and np.all(r8[~failed, 5] <= 3)
+    assert np.any(r13[~failed, 5] == 4)
+    assert np.all(r0[~failed, 5] == 42)
+    # converged rows carry a Jacobian near the identity and six redshifts
+    assert np.all(np.abs(r8[~failed, 12] - 1) < 1e-2) and np.all(r8[~failed, 6] > 0)
+
+
 def test_amr_fixture_exercises_levels(synth):
     from conftest import load_golden
     g = load_golden("amr")
