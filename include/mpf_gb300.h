@@ -145,6 +145,48 @@ int mpf_propagate_noalloc(const mpf_octree* o, const mpf_cosmology* c, const mpf
                           int64_t* steps, double* final_rec, double* plane_rec);
 const char* mpf_noalloc_last_error(void);
 
+/* ------------------------------------------------------------------------ */
+/* Catalogue root-finder                                                     */
+/* ------------------------------------------------------------------------ */
+/* Parameters of the catalogues executable that the root-finder reads
+ * (src/catalogues.h:61-97; the observer is at the origin, catalogues.cpp:196-199). */
+typedef struct {
+    double length;             /* lbox * mpc / h in metres (catalogues.cpp:163) */
+    double h;                  /* dimensionless Hubble parameter (Input::acquire) */
+    double mpc;                /* metres per Mpc: parameters.mpc */
+    double cat_accuracy;       /* stop when |x_s - x_ray| / |x_s| <= cat_accuracy */
+    double vobs[3];            /* observer velocity: parameters.v0x, v0y, v0z */
+    const double* rotm1;       /* 3x3 row-major rotation into the octree frame (narrow cones,
+                                  relCat catalogues.h:818-826), or NULL (isfullsky) */
+    unsigned nsteps;           /* RK4 steps per cell */
+    int order;                 /* 1 = CIC, 2 = TSC */
+    int exact;                 /* 1: reference float64 order; 0: FP32 gathers */
+    int max_iterations;        /* 10 in the reference (use_previous_catalogues = 0) */
+} mpf_catalogue_params;
+
+#define MPF_CATALOGUE_FIELDS 16
+
+typedef struct {
+    int64_t rays;              /* rays integrated, Jacobian re-traces included */
+    int64_t photon_steps;      /* accepted RK4 steps over all of them */
+    int iterations;            /* Newton rounds run (at most max_iterations + 1) */
+} mpf_catalogue_stats;
+
+/* Replaces Catalogues::relCat's per-source loop body (src/catalogues.h:811-856)
+ * with Catalogues::iterateNewtonMethod / newtonMethod2d (catalogues.h:410-783)
+ * and jacobiantype = "infinitesimal": for each source, rays launched at
+ * (phi, theta) are integrated to the source radius, the miss is measured in
+ * the screen basis and a Newton step updates (phi, theta), up to
+ * max_iterations + 1 rays.  sources: n rows of `stride` doubles (>= 6: x y z
+ * in octree units, vx vy vz in RAMSES units, then anything, e.g. id and npart
+ * as in the reference's 8-column rows).  rows: n x 16, relCat's catalog row:
+ * comoving phi theta, observed phi theta, miss, rays used (42 = rejected),
+ * z_FLRW z_pot z_Doppler z_transverse z_ISW z_GR, a11 a12 a21 a22.  A source
+ * the rays cannot reach has observed phi = theta = 42, miss 0 and the
+ * reference's firstid in column 5 (catalogues.h:436-442).  stats may be NULL. */
+int mpf_catalogue_newton(const mpf_octree* o, const mpf_cosmology* c, const mpf_catalogue_params* p, int64_t n,
+                         const double* sources, int64_t stride, double* rows, mpf_catalogue_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,6 +14,8 @@ Input::acquire+correct      ``Cosmology(t, a, dadt, d2adt2)`` (the table)
 Integrator::integrate       ``propagate(...)`` (batched over rays), with
  + Lensing::dbetadtheta_     the infinitesimal Jacobian and FillMap's
    infinitesimal            per-surface values at each surface
+Catalogues::relCat /        ``catalogue(...)``: the Newton root-finder for a
+  iterateNewtonMethod       batch of sources, relCat's 16-column rows
 ==========================  ==================================================
 """
 from __future__ import annotations
@@ -30,7 +32,11 @@ PHOTON_FIELDS = ("a t x y z dtdl dxdl dydl dzdl level ah rho phi dphidx dphidy d
 PLANE_FIELDS = ("firstid f x y z distance A11 A12 A22 t a redshift chi lambda s isw rho phi rho_max "
                 "valid").split()
 
-__all__ = ["Octree", "Cosmology", "propagate", "MpfError", "PHOTON_FIELDS", "PLANE_FIELDS", "library"]
+CATALOGUE_FIELDS = ("phi theta phi_obs theta_obs miss iterations z_flrw z_pot z_dopp z_tdopp z_isw z_gr "
+                    "a11 a12 a21 a22").split()
+
+__all__ = ["Octree", "Cosmology", "propagate", "catalogue", "MpfError", "PHOTON_FIELDS", "PLANE_FIELDS",
+           "CATALOGUE_FIELDS", "library"]
 
 
 def library():
@@ -146,3 +152,31 @@ def propagate(octree: Octree, cosmology: Cosmology, launch, length: float, nstep
     capi.check(rc)
     del keep
     return steps, final, pout, rc
+
+
+def catalogue(octree: Octree, cosmology: Cosmology, sources, length: float, h: float, mpc: float = 3.08568e22,
+              cat_accuracy: float = 1e-8, nsteps: int = 10, order: int = 2, vobs=(0.0, 0.0, 0.0), rotm1=None,
+              exact: bool = False, max_iterations: int = 10):
+    """Catalogues::relCat for a batch of sources (rows of >= 6 doubles: x y z vx vy vz ...).
+
+    Returns (rows[n, 16] in relCat's column order, stats dict, status).
+    """
+    L = capi.load()
+    src = np.ascontiguousarray(sources, dtype=np.float64)
+    if src.ndim != 2 or src.shape[1] < 6:
+        raise ValueError("sources must be n x (>= 6)")
+    n, stride = src.shape
+    p = capi.CatalogueParams()
+    p.length, p.h, p.mpc, p.cat_accuracy = float(length), float(h), float(mpc), float(cat_accuracy)
+    for k in range(3):
+        p.vobs[k] = float(vobs[k])
+    rot = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64).reshape(9)
+    p.rotm1 = rot.ctypes.data if rot is not None else None
+    p.nsteps, p.order, p.exact, p.max_iterations = int(nsteps), int(order), int(bool(exact)), int(max_iterations)
+    rows = np.zeros((n, capi.MPF_CATALOGUE_FIELDS))
+    st = capi.CatalogueStats()
+    rc = L.mpf_catalogue_newton(octree._h, cosmology._h, C.byref(p), n, capi.ptr(src), stride, capi.ptr(rows),
+                                C.byref(st))
+    capi.check(rc)
+    del rot
+    return rows, dict(rays=st.rays, photon_steps=st.photon_steps, iterations=st.iterations), rc

@@ -1,9 +1,9 @@
 """Build recipe of the native library (libmpf_gb300.so) for sm_103a.
 
 Compiles each CUDA translation unit with nvcc in parallel and links a shared
-library next to this file.  The reference-order translation unit is built
-with -fmad=false so its float64 arithmetic rounds exactly as the
-reference's; the others keep FMA contraction.
+library next to this file.  The reference-order translation unit and the
+catalogue root-finder are built with -fmad=false so their float64 arithmetic
+keeps the reference's rounding; the others keep FMA contraction.
 """
 from __future__ import annotations
 
@@ -25,6 +25,7 @@ UNITS = [
     ("mpf_octree.cu", []),
     ("mpf_capi.cu", []),
     ("mpf_noalloc.cu", []),
+    ("mpf_catalogue.cu", ["-fmad=false"]),
 ]
 
 

@@ -26,7 +26,9 @@ STOP = {"redshift": 0, "r": 1, "radius": 1, "lambda": 2, "t": 3, "eta": 3, "a": 
 EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_upload", "mpf_octree_load",
            "mpf_octree_get_info", "mpf_octree_destroy", "mpf_cosmology_upload", "mpf_cosmology_destroy", "mpf_locate",
            "mpf_interpolate", "mpf_propagate", "mpf_propagate_device", "mpf_propagate_noalloc",
-           "mpf_noalloc_last_error")
+           "mpf_noalloc_last_error", "mpf_catalogue_newton")
+
+MPF_CATALOGUE_FIELDS = 16
 
 
 class MpfError(RuntimeError):
@@ -44,6 +46,16 @@ class Params(C.Structure):
     _fields_ = [("length", C.c_double), ("stop_value", C.c_double), ("plane_normal", C.c_double * 3),
                 ("planes", C.c_void_p), ("nplanes", C.c_int), ("nsteps", C.c_uint), ("order", C.c_int),
                 ("stop", C.c_int), ("jacobian", C.c_int), ("exact", C.c_int), ("max_steps", C.c_int64)]
+
+
+class CatalogueParams(C.Structure):
+    _fields_ = [("length", C.c_double), ("h", C.c_double), ("mpc", C.c_double), ("cat_accuracy", C.c_double),
+                ("vobs", C.c_double * 3), ("rotm1", C.c_void_p), ("nsteps", C.c_uint), ("order", C.c_int),
+                ("exact", C.c_int), ("max_iterations", C.c_int)]
+
+
+class CatalogueStats(C.Structure):
+    _fields_ = [("rays", C.c_int64), ("photon_steps", C.c_int64), ("iterations", C.c_int)]
 
 
 _lib = None
@@ -76,6 +88,8 @@ def load(path: str = LIB_PATH):
     L.mpf_propagate_device.argtypes = [vp, vp, C.POINTER(Params), i64, vp, vp, vp, vp, vp, vp]
     L.mpf_propagate_noalloc.argtypes = [vp, vp, C.POINTER(Params), i64, vp, vp, vp, vp]
     L.mpf_noalloc_last_error.restype = C.c_char_p
+    L.mpf_catalogue_newton.argtypes = [vp, vp, C.POINTER(CatalogueParams), i64, vp, i64, vp,
+                                       C.POINTER(CatalogueStats)]
     for name in EXPORTS:
         if name not in ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_destroy",
                         "mpf_cosmology_destroy", "mpf_noalloc_last_error"):

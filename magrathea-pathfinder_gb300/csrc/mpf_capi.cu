@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "../../include/mpf_gb300.h"
+#include "mpf_catalogue.h"
 #include "mpf_internal.h"
 
 extern "C" int mpf_internal_octree_build(const void* records, int64_t n, int on_device, cudaStream_t stream,
@@ -284,6 +285,47 @@ int mpf_propagate(const mpf_octree* o, const mpf_cosmology* c, const mpf_params*
         e = cudaMemcpy(plane_rec, dp.p, (size_t)n * np * MPF_PLANE_FIELDS * sizeof(double), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_err(e, "mpf_propagate");
     if (status & 1u) return set_err(MPF_WARN_MAX_STEPS, "mpf_propagate: a ray reached max_steps");
+    return MPF_OK;
+}
+
+int mpf_catalogue_newton(const mpf_octree* o, const mpf_cosmology* c, const mpf_catalogue_params* p, int64_t n,
+                         const double* sources, int64_t stride, double* rows, mpf_catalogue_stats* stats)
+{
+    if (!o || !c || !p || n < 0 || (n > 0 && (!sources || !rows)) || stride < 6 || stride > 1024)
+        return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: null argument or stride < 6");
+    if (p->nsteps == 0 || (p->order != 1 && p->order != 2) || !(p->length > 0.0) || !(p->h > 0.0) || !(p->mpc > 0.0) ||
+        p->max_iterations < 0 || p->max_iterations > 1000 || !(p->cat_accuracy >= 0.0))
+        return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: bad parameters");
+    if (n > 0x7fffffffll) return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: at most 2^31 - 1 sources per call");
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (n == 0) return MPF_OK;
+    mpf::CatConst K;
+    K.length = p->length; K.h = p->h; K.mpc = p->mpc; K.accuracy = p->cat_accuracy;
+    for (int k = 0; k < 3; ++k) K.vobs[k] = p->vobs[k];
+    K.max_iterations = p->max_iterations;
+    mpf::CatRotation R;
+    if (p->rotm1)
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k) R.m[j][k] = p->rotm1[3 * j + k];
+    mpf::DevCosmo C{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
+    DBuf dsrc, drows;
+    cudaError_t e = dsrc.alloc((size_t)n * (size_t)stride * sizeof(double));
+    if (e == cudaSuccess) e = drows.alloc((size_t)n * MPF_CATALOGUE_FIELDS * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(dsrc.p, sources, (size_t)n * (size_t)stride * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_err(e, "mpf_catalogue_newton");
+    mpf::CatRunStats st;
+    unsigned status = 0;
+    e = mpf::catalogue_newton(o->tree, C, K, p->rotm1 ? &R : nullptr, p->exact != 0, p->order, p->nsteps, n,
+                              (const double*)dsrc.p, (int)stride, (double*)drows.p, &st, &status, nullptr);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(rows, drows.p, (size_t)n * MPF_CATALOGUE_FIELDS * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(e, "mpf_catalogue_newton");
+    if (stats) {
+        stats->rays = st.rays;
+        stats->photon_steps = st.photon_steps;
+        stats->iterations = st.iterations;
+    }
+    if (status & 1u) return set_err(MPF_WARN_MAX_STEPS, "mpf_catalogue_newton: a ray reached max_steps");
     return MPF_OK;
 }
 

@@ -1,0 +1,35 @@
+// Catalogue root-finder driver (mpf_catalogue.cu), called by the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "mpf_device.cuh"
+#include "mpf_propagate.cuh"
+
+namespace mpf {
+
+constexpr int kCatalogueFields = 16;
+
+struct CatConst {
+    double length, h, mpc, accuracy;
+    double vobs[3];
+    int max_iterations;
+};
+
+struct CatRotation {
+    double m[3][3];
+};
+
+struct CatRunStats {
+    long long rays;
+    long long photon_steps;
+    int iterations;
+};
+
+// d_src: n rows of `stride` doubles on the device; d_rows: n x 16 on the
+// device.  Synchronises `stream` once per Newton round (the size of the next
+// round decides its launch).  h_status: the propagate status bits.
+cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& C, const CatConst& K, const CatRotation* rot, bool exact,
+                             int order, unsigned nsteps, long long n, const double* d_src, int stride, double* d_rows,
+                             CatRunStats* stats, unsigned* h_status, cudaStream_t stream);
+
+}  // namespace mpf

@@ -365,7 +365,7 @@ __device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, doub
               cp * s2t * dxz;
 }
 
-template <int ORDER>
+template <int ORDER, bool SRC>
 __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* L, long long i,
                                const PropOut& O)
 {
@@ -373,10 +373,17 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     const double mn = -(double)kExtent / 2.0, mx = (double)kExtent / 2.0;
     const double scale = P.length;
     const double inv_scale = 1.0 / scale;
-    const int np = P.nplanes;
+    const int np = SRC ? 1 : P.nplanes;
+    const int skind = SRC ? (int)STOP_R : P.stop_kind;
+    const double stop_ref = SRC ? P.ray_stop[i] : P.stop_ref;
+    const int rec_fields = SRC ? kSourceFields : kPlaneFields;
     unsigned long long* const st = O.stats;
     FastRec b;
-    {
+    if (SRC) {
+        // (phi, theta) launch form: the direction is given
+        b.a = 1.0; b.t = 0.0; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = 1.0;
+        b.k1 = L[3]; b.k2 = L[4]; b.k3 = L[5];
+    } else {
         const double norm = sqrt((L[3] - L[0]) * (L[3] - L[0]) + (L[4] - L[1]) * (L[4] - L[1]) + (L[5] - L[2]) * (L[5] - L[2]));
         b.a = 1.0; b.t = 0.0; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = 1.0;
         b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
@@ -405,11 +412,15 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     int next_plane = 0;
     long long cross_k[kMaxPlanes];
     for (int j = 0; j < np; ++j) cross_k[j] = -1;
-    double* prow = O.plane_rec ? O.plane_rec + (long long)i * np * kPlaneFields : nullptr;
-    while (next_plane < np && ((P.stop_kind == STOP_A) ? (b.a < P.planes[next_plane])
-                                                        : (((P.stop_kind == STOP_R) ? b.chi : (P.stop_kind == STOP_LAMBDA) ? b.lambda
-                                                            : (P.stop_kind == STOP_T) ? b.t : (P.stop_kind == STOP_S) ? b.s : b.red) >
-                                                           P.planes[next_plane]))) {
+    double* prow = O.plane_rec ? O.plane_rec + (long long)i * np * rec_fields : nullptr;
+    if (SRC && prow) {
+        prow[24] = b.a; prow[25] = b.phi; prow[26] = b.k1; prow[27] = b.k2; prow[28] = b.k3;
+        prow[29] = prow[30] = prow[31] = 0.0;
+    }
+    while (next_plane < np && ((skind == STOP_A) ? (b.a < (SRC ? stop_ref : P.planes[next_plane]))
+                                                  : (((skind == STOP_R) ? b.chi : (skind == STOP_LAMBDA) ? b.lambda
+                                                      : (skind == STOP_T) ? b.t : (skind == STOP_S) ? b.s : b.red) >
+                                                     (SRC ? stop_ref : P.planes[next_plane])))) {
         cross_k[next_plane] = 0;
         ++next_plane;
     }
@@ -496,15 +507,15 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                 }
             }
             while (next_plane < np) {
-                const int kind = P.stop_kind;
+                const int kind = skind;
                 const double q1 = (kind == STOP_R) ? p.chi : (kind == STOP_LAMBDA) ? p.lambda : (kind == STOP_T) ? p.t
                                 : (kind == STOP_A) ? p.a : (kind == STOP_S) ? p.s : p.red;
-                const double ref = P.planes[next_plane];
+                const double ref = SRC ? stop_ref : P.planes[next_plane];
                 if (!((kind == STOP_A) ? (q1 < ref) : (q1 > ref))) break;
                 const int j = next_plane++;
                 cross_k[j] = k;
                 if (prow) {
-                    double* o = prow + j * kPlaneFields;
+                    double* o = prow + j * rec_fields;
                     const double q0 = (kind == STOP_R) ? b.chi : (kind == STOP_LAMBDA) ? b.lambda : (kind == STOP_T) ? b.t
                                     : (kind == STOP_A) ? b.a : (kind == STOP_S) ? b.s : b.red;
                     const double f = (q1 - ref) / (q1 - q0);
@@ -522,14 +533,22 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                     o[17] = b.phi * f + p.phi * (1 - f);
                     o[18] = have_rmax ? rmax : 0.0;
                     o[19] = 1.0;
+                    if (SRC) {
+                        o[20] = b.k0 * f + p.k0 * (1 - f);
+                        o[21] = b.k1 * f + p.k1 * (1 - f);
+                        o[22] = b.k2 * f + p.k2 * (1 - f);
+                        o[23] = b.k3 * f + p.k3 * (1 - f);
+                    }
                     if (P.jacobian) {
+                        // at the surface's distance, or at the source radius in source mode
+                        const double jd = SRC ? ref : dist;
                         double s1[3], s2[3];
                         bool ok = true;
-                        if (p.chi <= dist) {
+                        if (p.chi <= jd) {
                             for (int q = 0; q < 3; ++q) { s1[q] = S[q]; s2[q] = S[3 + q]; }
-                        } else if (chim1 <= dist) {
+                        } else if (chim1 <= jd) {
                             for (int q = 0; q < 3; ++q) { s1[q] = S[q] - c_k[q]; s2[q] = S[3 + q] - c_k[3 + q]; }
-                        } else if (k >= 2 && chim2 <= dist) {
+                        } else if (k >= 2 && chim2 <= jd) {
                             for (int q = 0; q < 3; ++q) {
                                 s1[q] = S[q] - c_k[q] - c_km1[q];
                                 s2[q] = S[3 + q] - c_k[3 + q] - c_km1[3 + q];
@@ -539,7 +558,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                             status |= 2u;
                         }
                         if (ok) {
-                            const double idist = 1.0 / dist;
+                            const double idist = 1.0 / jd;
                             o[6] = 1.0 - 2.0 * (s1[0] - s2[0] * idist) / c2 * P.length;
                             o[7] = -2.0 * (s1[1] - s2[1] * idist) / c2 * P.length;
                             o[8] = 1.0 - 2.0 * (s1[2] - s2[2] * idist) / c2 * P.length;
@@ -556,14 +575,14 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             b = p;
         }
         bool stop;
-        switch (P.stop_kind) {
-        case STOP_R: stop = b.chi > P.stop_ref; break;
-        case STOP_LAMBDA: stop = b.lambda > P.stop_ref; break;
-        case STOP_REDSHIFT: stop = b.red > P.stop_ref; break;
-        case STOP_T: stop = b.t > P.stop_ref; break;
-        case STOP_A: stop = b.a < P.stop_ref; break;
-        case STOP_PLANE: stop = (p.x * P.ki[0] + p.y * P.ki[1] + p.z * P.ki[2]) > P.stop_ref; break;
-        case STOP_S: stop = b.s > P.stop_ref; break;
+        switch (skind) {
+        case STOP_R: stop = b.chi > stop_ref; break;
+        case STOP_LAMBDA: stop = b.lambda > stop_ref; break;
+        case STOP_REDSHIFT: stop = b.red > stop_ref; break;
+        case STOP_T: stop = b.t > stop_ref; break;
+        case STOP_A: stop = b.a < stop_ref; break;
+        case STOP_PLANE: stop = (p.x * P.ki[0] + p.y * P.ki[1] + p.z * P.ki[2]) > stop_ref; break;
+        case STOP_S: stop = b.s > stop_ref; break;
         default: stop = true;
         }
         if (stop) break;
@@ -591,7 +610,16 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             status |= 4u;
         }
     }
-    if (prow) {
+    if (SRC && prow) {
+        const long long ck = cross_k[0];
+        const bool ok = (ck >= 1) && (ck < size);
+        if (!ok) {
+            for (int q = 0; q < 24; ++q) prow[q] = 0.0;
+            const long long marked = size - 1;
+            prow[0] = (double)(marked - (marked > 0));
+        }
+        prow[19] = ok ? 1.0 : 0.0;
+    } else if (prow) {
         for (int j = 0; j < np; ++j) {
             double* o = prow + j * kPlaneFields;
             const long long ck = cross_k[j];
@@ -612,7 +640,7 @@ constexpr int kFastThreads = 128;
 // Persistent launch: each warp takes the next 32 rays from a global counter
 // until the batch is exhausted, so uneven path lengths do not leave tail
 // waves.  `queue` is zeroed before the launch.
-template <int ORDER>
+template <int ORDER, bool SRC>
 __global__ void __launch_bounds__(kFastThreads, 3) k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
                                                                     const double* __restrict__ launch, long long n, PropOut O,
                                                                     unsigned long long* queue)
@@ -624,7 +652,7 @@ __global__ void __launch_bounds__(kFastThreads, 3) k_propagate_fast(DevTree T, D
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= (unsigned long long)n) break;
         const long long i = (long long)base + lane;
-        if (i < n) propagate_fast<ORDER>(T, C, P, launch + 6 * i, i, O);
+        if (i < n) propagate_fast<ORDER, SRC>(T, C, P, launch + 6 * i, i, O);
         __syncwarp();
     }
 }

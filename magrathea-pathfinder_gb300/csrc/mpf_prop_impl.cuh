@@ -28,7 +28,9 @@ cudaError_t launch_propagate_impl(const DevTree& T, const DevCosmo& C, const Pro
 {
     if (n <= 0) return cudaSuccess;
     const int tpb = 128;
-    k_propagate<EXACT><<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, stream>>>(T, C, P, d_launch, n, O);
+    const unsigned grid = (unsigned)((n + tpb - 1) / tpb);
+    if (P.ray_stop) k_propagate<EXACT, true><<<grid, tpb, 0, stream>>>(T, C, P, d_launch, n, O);
+    else k_propagate<EXACT, false><<<grid, tpb, 0, stream>>>(T, C, P, d_launch, n, O);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,10 @@ namespace mpf {
 constexpr int kMaxPlanes = 16;
 constexpr int kPhotonFields = 28;
 constexpr int kPlaneFields = 20;
+// Source mode (catalogue root-finder): one record per ray at its own stop
+// radius: the 20 surface fields, then dtdl dxdl dydl dzdl interpolated at the
+// radius (20-23) and the launch point's a, phi, dxdl, dydl, dzdl (24-28).
+constexpr int kSourceFields = 32;
 
 enum StopKind { STOP_REDSHIFT = 0, STOP_R = 1, STOP_LAMBDA = 2, STOP_T = 3, STOP_A = 4, STOP_PLANE = 5, STOP_S = 6 };
 
@@ -49,6 +53,9 @@ struct PropParams {
     int stop_kind;
     int nplanes;
     int jacobian;
+    // source mode: per-ray stop radius; the launch record is the start point
+    // and a unit direction (Integrator::launch, (phi, theta) form)
+    const double* ray_stop;
 };
 
 struct PropOut {
@@ -181,7 +188,7 @@ __device__ void jac_point(const DevTree& T, const Rec& p, double dr, double* H)
     (void)r;
 }
 
-template <bool EXACT>
+template <bool EXACT, bool SRC>
 __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* L, long long i,
                               const PropOut& O)
 {
@@ -189,10 +196,18 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
     const double c2 = kC * kC;
     const double mn = 0.0 - (double)kExtent / two, mx = 0.0 + (double)kExtent / two;
     const double scale = P.length;
-    const int np = P.nplanes;
+    const int np = SRC ? 1 : P.nplanes;
+    const int kind = SRC ? (int)STOP_R : P.stop_kind;
+    const double stop_ref = SRC ? P.ray_stop[i] : P.stop_ref;
+    const int rec_fields = SRC ? kSourceFields : kPlaneFields;
     Rec b;
-    // launch (src/integrator.h:283-309, 6-argument form)
-    {
+    if (SRC) {
+        // launch, (phi, theta) form (src/integrator.h:305-329): direction given
+        b.a = one; b.t = zero; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = one;
+        b.k1 = L[3]; b.k2 = L[4]; b.k3 = L[5];
+        b.index = 0.0;
+    } else {
+        // launch (src/integrator.h:283-309, 6-argument form)
         const double norm = sqrt((L[3] - L[0]) * (L[3] - L[0]) + (L[4] - L[1]) * (L[4] - L[1]) + (L[5] - L[2]) * (L[5] - L[2]));
         b.a = one; b.t = zero; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = one;
         b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
@@ -225,9 +240,14 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
     int next_plane = 0;
     long long cross_k[kMaxPlanes];
     for (int j = 0; j < np; ++j) cross_k[j] = -1;
-    double* prow = O.plane_rec ? O.plane_rec + (long long)i * np * kPlaneFields : nullptr;
+    double* prow = O.plane_rec ? O.plane_rec + (long long)i * np * rec_fields : nullptr;
+    if (SRC && prow) {
+        // trajectory[0] as the redshift decomposition reads it (catalogues.h:691-693)
+        prow[24] = b.a; prow[25] = b.phi; prow[26] = b.k1; prow[27] = b.k2; prow[28] = b.k3;
+        prow[29] = prow[30] = prow[31] = 0.0;
+    }
     // a surface crossed by the first point lies at firstid 0: invalid in the map driver
-    while (next_plane < np && plane_crossed(P.stop_kind, b, P.planes[next_plane])) {
+    while (next_plane < np && plane_crossed(kind, b, SRC ? stop_ref : P.planes[next_plane])) {
         cross_k[next_plane] = 0;
         ++next_plane;
     }
@@ -301,13 +321,13 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
                     S.s2[q] += p.chi * p.chi * H[q];
                 }
             }
-            while (next_plane < np && plane_crossed(P.stop_kind, p, P.planes[next_plane])) {
+            while (next_plane < np && plane_crossed(kind, p, SRC ? stop_ref : P.planes[next_plane])) {
                 const int j = next_plane++;
                 cross_k[j] = k;
                 if (prow) {
-                    double* o = prow + j * kPlaneFields;
-                    const double ref = P.planes[j];
-                    const double q1 = plane_q(P.stop_kind, p), q0 = plane_q(P.stop_kind, b);
+                    double* o = prow + j * rec_fields;
+                    const double ref = SRC ? stop_ref : P.planes[j];
+                    const double q1 = plane_q(kind, p), q0 = plane_q(kind, b);
                     const double f = (q1 - ref) / (q1 - q0);
                     const double px = b.x * f + p.x * (1 - f), py = b.y * f + p.y * (1 - f), pz = b.z * f + p.z * (1 - f);
                     const double dist = sqrt(px * px + py * py + pz * pz);
@@ -324,17 +344,26 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
                     // max rho over points [0, firstid) = [0, k-1): all points before b
                     o[18] = have_rmax ? rmax_before_b : 0.0;
                     o[19] = 1.0;
+                    if (SRC) {
+                        o[20] = b.k0 * f + p.k0 * (1 - f);
+                        o[21] = b.k1 * f + p.k1 * (1 - f);
+                        o[22] = b.k2 * f + p.k2 * (1 - f);
+                        o[23] = b.k3 * f + p.k3 * (1 - f);
+                    }
                     if (P.jacobian) {
-                        // last point with chi <= dist among k, k-1, k-2
+                        // the Jacobian at the surface's distance (hmaps.h:653-656),
+                        // or at the source radius itself (catalogues.h:517)
+                        const double jd = SRC ? ref : dist;
+                        // last point with chi <= jd among k, k-1, k-2
                         const JSum* J = nullptr;
-                        if (p.chi <= dist) J = &S;
-                        else if (chim1 <= dist) J = &Sm1;
-                        else if (k >= 2 && chim2 <= dist) J = &Sm2;
+                        if (p.chi <= jd) J = &S;
+                        else if (chim1 <= jd) J = &Sm1;
+                        else if (k >= 2 && chim2 <= jd) J = &Sm2;
                         double A[3] = {1.0, 0.0, 1.0};
                         if (J) {
-                            const double a11 = J->s1[0] - J->s2[0] / dist;
-                            const double a12 = J->s1[1] - J->s2[1] / dist;
-                            const double a22 = J->s1[2] - J->s2[2] / dist;
+                            const double a11 = J->s1[0] - J->s2[0] / jd;
+                            const double a12 = J->s1[1] - J->s2[1] / jd;
+                            const double a22 = J->s1[2] - J->s2[2] / jd;
                             A[0] = 1 - 2 * a11 / c2 * P.length;
                             A[1] = -2 * a12 / c2 * P.length;
                             A[2] = 1 - 2 * a22 / c2 * P.length;
@@ -354,14 +383,14 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
         }
         // stop test on trajectory.back()
         bool stop = false;
-        switch (P.stop_kind) {
-        case STOP_R: stop = b.chi > P.stop_ref; break;
-        case STOP_LAMBDA: stop = b.lambda > P.stop_ref; break;
-        case STOP_REDSHIFT: stop = b.red > P.stop_ref; break;
-        case STOP_T: stop = b.t > P.stop_ref; break;
-        case STOP_A: stop = b.a < P.stop_ref; break;
-        case STOP_PLANE: stop = (p.x * P.ki[0] + p.y * P.ki[1] + p.z * P.ki[2]) > P.stop_ref; break;
-        case STOP_S: stop = b.s > P.stop_ref; break;
+        switch (kind) {
+        case STOP_R: stop = b.chi > stop_ref; break;
+        case STOP_LAMBDA: stop = b.lambda > stop_ref; break;
+        case STOP_REDSHIFT: stop = b.red > stop_ref; break;
+        case STOP_T: stop = b.t > stop_ref; break;
+        case STOP_A: stop = b.a < stop_ref; break;
+        case STOP_PLANE: stop = (p.x * P.ki[0] + p.y * P.ki[1] + p.z * P.ki[2]) > stop_ref; break;
+        case STOP_S: stop = b.s > stop_ref; break;
         default: stop = true;
         }
         if (stop) break;
@@ -380,7 +409,18 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
             status |= 4u;
         }
     }
-    if (prow) {
+    if (SRC && prow) {
+        // the source is reached when the last kept point is the crossing
+        // (catalogues.h:433-442: marked > 0 and chi(marked) >= radius)
+        const long long ck = cross_k[0];
+        const bool ok = (ck >= 1) && (ck < size);
+        if (!ok) {
+            for (int q = 0; q < 24; ++q) prow[q] = 0.0;
+            const long long marked = size - 1;
+            prow[0] = (double)(marked - (marked > 0));
+        }
+        prow[19] = ok ? 1.0 : 0.0;
+    } else if (prow) {
         for (int j = 0; j < np; ++j) {
             double* o = prow + j * kPlaneFields;
             const long long ck = cross_k[j];
@@ -397,13 +437,13 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
     if (status) atomicOr(O.status, status);
 }
 
-template <bool EXACT>
+template <bool EXACT, bool SRC>
 __global__ void __launch_bounds__(128) k_propagate(DevTree T, DevCosmo C, PropParams P, const double* __restrict__ launch,
                                                    long long n, PropOut O)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    propagate_one<EXACT>(T, C, P, launch + 6 * i, i, O);
+    propagate_one<EXACT, SRC>(T, C, P, launch + 6 * i, i, O);
 }
 
 }  // namespace mpf

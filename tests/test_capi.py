@@ -35,6 +35,13 @@ def test_bad_input_is_a_status_not_a_crash(pkg):
     assert b"null" in L.mpf_last_error() or b"empty" in L.mpf_last_error()
     rc = L.mpf_octree_load(b"/nonexistent/cone.bin", ctypes.byref(h))
     assert rc == -6
+    from importlib import import_module
+    capi = import_module(PKG + ".capi")
+    cp = capi.CatalogueParams()
+    rows = np.zeros((1, 16))
+    src = np.zeros((1, 6))
+    assert L.mpf_catalogue_newton(None, None, ctypes.byref(cp), 1, capi.ptr(src), 6, capi.ptr(rows), None) == -1
+    assert b"mpf_catalogue_newton" in L.mpf_last_error()
     if L.mpf_device_count() == 0:
         rec = np.zeros(2, dtype=np.dtype([("b", "u1", 48)]))
         assert L.mpf_octree_upload(ctypes.c_void_p(rec.ctypes.data), 2, ctypes.byref(h)) == -5
