@@ -13,6 +13,12 @@ than L2, so no flush is needed between steps.
 
 Metric: RK4 photon-steps per second (one accepted RK4 step of one ray =
 one photon-step, src/integrator.h:776).
+
+--mode catalogue measures the catalogue root-finder instead (a second JSON
+line, not the headline): one step = one batch of sources on the same octree,
+uniform in comoving volume inside the cone out to z = 2, solved to
+cat_accuracy = 1e-8 (Catalogues::iterateNewtonMethod, at most 11 rays per
+source); metric sources/s, with the photon-steps/s over all rounds beside it.
 """
 from __future__ import annotations
 
@@ -165,6 +171,30 @@ def cpu_baseline(oracle_mod, records, cos, length, launch, planes, per_thread=24
                       % (idx.shape[0], total, dt, nthreads)}
 
 
+CAT_METRIC = "catalogue sources/s (Newton root-finder to cat_accuracy 1e-8, TSC, <=11 rays per source)"
+CAT_UNIT = "sources/s"
+# payload bytes per photon-step without the lensing Jacobian (rounds 0-2 of the root-finder)
+BYTES_PER_PHOTON_STEP_NOJAC = 4 * 27 * 16 + 27 * 28
+
+
+def catalogue_sources(synth, n, seed, zmax=2.0, half_deg=4.5):
+    """Sources uniform in comoving volume inside the cone (octree units), RAMSES-unit velocities."""
+    cosmo = synth.Cosmology()
+    chi_max = float(cosmo.chi_of_z(zmax)[0]) / 2048.0
+    rng = np.random.default_rng(seed)
+    d = chi_max * rng.uniform(0.02, 1.0, n) ** (1.0 / 3.0)
+    ph = np.radians(rng.uniform(-half_deg, half_deg, n))
+    th = np.pi / 2 + np.radians(rng.uniform(-half_deg, half_deg, n))
+    src = np.zeros((n, 8))
+    src[:, 0] = d * np.cos(ph) * np.sin(th)
+    src[:, 1] = d * np.sin(ph) * np.sin(th)
+    src[:, 2] = d * np.cos(th)
+    src[:, 3:6] = rng.normal(0.0, 1e-3, (n, 3))
+    src[:, 6] = np.arange(n)          # id
+    src[:, 7] = 1.0                   # npart
+    return src
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -189,6 +219,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--zstop", type=float, default=2.0, help="stop redshift (profiling captures use a short path)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--mode", default="propagate", choices=["propagate", "catalogue"],
+                    help="propagate = the headline ray-tracing benchmark; catalogue = the Newton root-finder")
+    ap.add_argument("--sources", type=int, default=65536, help="catalogue sources per step")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     synth = importlib.import_module(PKG + ".synth")
@@ -202,6 +235,8 @@ def main():
     cos = cosmology_table(synth)
     length = spec.lbox * synth.MPC / spec.cosmo.h
     planes = np.array([args.zstop])
+    if args.mode == "catalogue":
+        return run_catalogue(args, synth, spec, cos, length, world, rank, local, dist)
 
     if args.impl == "reference":
         if rank != 0:
@@ -259,8 +294,10 @@ def main():
                                exact=args.exact)
     stream = torch.cuda.current_stream(dev)
 
+    replicas = importlib.import_module(PKG + ".replicas")
+
     def step(k):
-        off = (k % nb) * B
+        off = replicas.batch_ids(k, rank, world, nb) * B
         rc = lib.mpf_propagate_device(tree._h, cosmo._h, C.byref(p), B, C.c_void_p(d_launch.data_ptr() + off * 48),
                                       C.c_void_p(d_steps[k].data_ptr()), None, C.c_void_p(d_planes.data_ptr()),
                                       C.c_void_p(d_status.data_ptr()), C.c_void_p(stream.cuda_stream))
@@ -290,15 +327,7 @@ def main():
     per_launch = [a.elapsed_time(b) for a, b in launch_ms]
     photon_steps = int(d_steps[args.warmup:].sum().item())
     status = int(d_status.item())
-    t_max = elapsed_ms
-    total_steps = photon_steps
-    if dist is not None:
-        t = torch.tensor([elapsed_ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-        c = torch.tensor([photon_steps], dtype=torch.float64, device=dev)
-        dist.all_reduce(c, op=dist.ReduceOp.SUM)
-        total_steps = int(c.item())
+    t_max, total_steps = replicas.reduce_counters(dist, elapsed_ms, photon_steps, dev)
     value = total_steps / (t_max / 1000.0)
 
     # end to end through the public API: host launch records in, host steps and
@@ -336,6 +365,150 @@ def main():
         import oracle as oracle_mod
         oracle_mod.build()
         line["cpu_baseline"] = cpu_baseline(oracle_mod, rec, cos, length, launch, planes)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_catalogue(args, synth, spec, cos, length, world, rank, local, dist):
+    h = spec.cosmo.h
+    config = {"workload": "catalogue on the AMR cone octree (256^3 base refined to level 14 in 2000 NFW haloes): "
+                          "%d sources per step uniform in comoving volume to z=2 inside 9x9 deg, cat_accuracy 1e-8, "
+                          "TSC, 8 steps/cell" % args.sources if args.workload == "amr"
+              else "catalogue on the %s octree (profiling / debugging)" % args.workload,
+              "sources_per_step": args.sources, "order": "TSC", "nsteps": 8, "cat_accuracy": 1e-8,
+              "max_rays_per_source": 11,
+              "gather_arithmetic": "float64 reference order" if args.exact else "fp32 gather, fp64 state",
+              "l2": "octree larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single GPU"}
+    kw = dict(cat_accuracy=1e-8, nsteps=8, order=2, vobs=(0.0, 0.0, 0.0), max_iterations=10)
+    nsrc = args.sources
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import oracle as oracle_mod
+        oracle_mod.build()
+        rec = octree_records(synth, spec)
+        nthreads = os.cpu_count() or 1
+        O = oracle_mod.Oracle(rec, {"t": cos[0], "a": cos[1], "dadt": cos[2]}, length, nthreads=nthreads)
+        per_step = nthreads
+        times, counts = [], 0
+        for s in range(args.warmup + args.steps):
+            src = catalogue_sources(synth, per_step, 1000 + s)
+            t0 = time.perf_counter()
+            O.catalogue(src, h=h, **kw)
+            dt = time.perf_counter() - t0
+            if s >= args.warmup:
+                times.append(dt)
+                counts += per_step
+        value = counts / sum(times)
+        line = {"metric": CAT_METRIC, "value": value, "unit": CAT_UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "impl": "reference",
+                "cpu_baseline": {"value": value, "unit": CAT_UNIT, "cores": nthreads, "kind": "port",
+                                 "sample": "%d sources per step, C oracle restating iterateNewtonMethod" % per_step},
+                "e2e": {"value": value, "unit": CAT_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    pkg = importlib.import_module(PKG)
+    importlib.import_module(PKG + ".build").build()
+    lib = pkg.library()
+    capi = importlib.import_module(PKG + ".capi")
+    rec = octree_records(synth, spec)
+    tree = pkg.Octree.from_records(rec)
+    info = tree.info
+    config.update({"cells": int(info["cells"]), "levels": [info["level_min"], info["level_max"]]})
+    cosmo = pkg.Cosmology(*cos)
+    dev = torch.device("cuda", local)
+    nstep = args.warmup + args.steps
+    pool = catalogue_sources(synth, nsrc * nstep, 7 + rank)
+    d_src = torch.from_numpy(pool).to(dev)
+    d_rows = torch.zeros((nsrc, capi.MPF_CATALOGUE_FIELDS), dtype=torch.float64, device=dev)
+    p, keep = pkg.catalogue_params(length, h, exact=args.exact, **kw)
+    stream = torch.cuda.current_stream(dev)
+    stats = []
+
+    def step(k):
+        st = capi.CatalogueStats()
+        rc = lib.mpf_catalogue_newton_device(tree._h, cosmo._h, C.byref(p), nsrc,
+                                             C.c_void_p(d_src.data_ptr() + k * nsrc * 8 * 8), 8,
+                                             C.c_void_p(d_rows.data_ptr()), C.byref(st), C.c_void_p(stream.cuda_stream))
+        capi.check(rc)
+        return pkg.catalogue_stats(st)
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    per_call = []
+    with Clocks(local) as clk:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for k in range(args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            stats.append(step(args.warmup + k))
+            b.record(stream)
+            per_call.append((a, b))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    replicas = importlib.import_module(PKG + ".replicas")
+    t_max, total_src = replicas.reduce_counters(dist, elapsed_ms, nsrc * args.steps, dev)
+    value = total_src / (t_max / 1000.0)
+    psteps = sum(s["photon_steps"] for s in stats)
+    psteps_jac = sum(s["photon_steps_jacobian"] for s in stats)
+    rays = sum(s["rays"] for s in stats)
+    rows = d_rows.cpu().numpy()
+    converged = float(np.mean((rows[:, 2] != 42) & (rows[:, 5] != 42)))
+
+    e2e_t, e2e_n = [], 0
+    for k in range(0 if args.no_e2e else 2):
+        hsrc = np.ascontiguousarray(pool[k * nsrc:(k + 1) * nsrc])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pkg.catalogue(tree, cosmo, hsrc, length, h, exact=args.exact, **kw)
+        e2e_t.append(time.perf_counter() - t0)
+        e2e_n += nsrc
+    e2e_value = e2e_n / sum(e2e_t) if e2e_t else None
+
+    peak, peak_kind = measured_peak_hbm()
+    avg_s = sum(a.elapsed_time(b) for a, b in per_call) / len(per_call) / 1000.0
+    alg_bytes = (BYTES_PER_PHOTON_STEP_NOJAC * (psteps - psteps_jac) + BYTES_PER_PHOTON_STEP * psteps_jac) / args.steps
+    achieved = alg_bytes / avg_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": (DRAM_BYTES_PER_PHOTON_STEP * psteps / args.steps) if DRAM_BYTES_PER_PHOTON_STEP else None,
+                "peak_source": peak_kind, "scope": "whole mpf_catalogue_newton_device call (all rounds, host syncs)",
+                "bytes_per_photon_step": {"with_jacobian": BYTES_PER_PHOTON_STEP,
+                                          "without_jacobian": BYTES_PER_PHOTON_STEP_NOJAC}}
+    line = {"metric": CAT_METRIC, "value": value, "unit": CAT_UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+            "photon_steps_per_s": psteps * world / (t_max / 1000.0), "rays_per_source": rays / (nsrc * args.steps),
+            "converged_fraction": converged,
+            "e2e": {"value": e2e_value, "unit": CAT_UNIT, "h2d_bytes_per_step": nsrc * 8 * 8,
+                    "d2h_bytes_per_step": nsrc * capi.MPF_CATALOGUE_FIELDS * 8},
+            "gpu_launches": sum(s["kernel_launches"] for s in stats), "roofline": roofline, "clocks": clk.summary()}
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle as oracle_mod
+        oracle_mod.build()
+        nthreads = os.cpu_count() or 1
+        O = oracle_mod.Oracle(rec, {"t": cos[0], "a": cos[1], "dadt": cos[2]}, length, nthreads=nthreads)
+        src = catalogue_sources(synth, 2 * nthreads, 99)
+        t0 = time.perf_counter()
+        O.catalogue(src, h=h, **kw)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": src.shape[0] / dt, "unit": CAT_UNIT, "cores": nthreads, "kind": "port",
+                                "sample": "%d sources, %.1f s, %d threads (C oracle restating iterateNewtonMethod)"
+                                          % (src.shape[0], dt, nthreads)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

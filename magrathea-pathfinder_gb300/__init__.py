@@ -166,6 +166,19 @@ def catalogue(octree: Octree, cosmology: Cosmology, sources, length: float, h: f
     if src.ndim != 2 or src.shape[1] < 6:
         raise ValueError("sources must be n x (>= 6)")
     n, stride = src.shape
+    p, rot = catalogue_params(length, h, mpc, cat_accuracy, nsteps, order, vobs, rotm1, exact, max_iterations)
+    rows = np.zeros((n, capi.MPF_CATALOGUE_FIELDS))
+    st = capi.CatalogueStats()
+    rc = L.mpf_catalogue_newton(octree._h, cosmology._h, C.byref(p), n, capi.ptr(src), stride, capi.ptr(rows),
+                                C.byref(st))
+    capi.check(rc)
+    del rot
+    return rows, catalogue_stats(st), rc
+
+
+def catalogue_params(length, h, mpc=3.08568e22, cat_accuracy=1e-8, nsteps=10, order=2, vobs=(0.0, 0.0, 0.0),
+                     rotm1=None, exact=False, max_iterations=10):
+    """mpf_catalogue_params plus the rotation array that must outlive the call."""
     p = capi.CatalogueParams()
     p.length, p.h, p.mpc, p.cat_accuracy = float(length), float(h), float(mpc), float(cat_accuracy)
     for k in range(3):
@@ -173,10 +186,9 @@ def catalogue(octree: Octree, cosmology: Cosmology, sources, length: float, h: f
     rot = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64).reshape(9)
     p.rotm1 = rot.ctypes.data if rot is not None else None
     p.nsteps, p.order, p.exact, p.max_iterations = int(nsteps), int(order), int(bool(exact)), int(max_iterations)
-    rows = np.zeros((n, capi.MPF_CATALOGUE_FIELDS))
-    st = capi.CatalogueStats()
-    rc = L.mpf_catalogue_newton(octree._h, cosmology._h, C.byref(p), n, capi.ptr(src), stride, capi.ptr(rows),
-                                C.byref(st))
-    capi.check(rc)
-    del rot
-    return rows, dict(rays=st.rays, photon_steps=st.photon_steps, iterations=st.iterations), rc
+    return p, rot
+
+
+def catalogue_stats(st) -> dict:
+    return dict(rays=st.rays, photon_steps=st.photon_steps, photon_steps_jacobian=st.photon_steps_jacobian,
+                iterations=st.iterations, kernel_launches=st.kernel_launches)

@@ -44,13 +44,24 @@ def _sources_mtime() -> float:
     return m
 
 
+STAMP = os.path.join(OUT, "flags.txt")
+
+
+def _extra_flags():
+    """Extra nvcc flags from MPF_NVCC_EXTRA (tuning sweeps, e.g. -DMPF_FAST_MINB=2)."""
+    return os.environ.get("MPF_NVCC_EXTRA", "").split()
+
+
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime():
+    extra = _extra_flags()
+    stamp = " ".join(extra)
+    same_flags = os.path.exists(STAMP) and open(STAMP).read() == stamp
+    if not force and same_flags and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime():
         return LIB
     os.makedirs(OUT, exist_ok=True)
     cc = nvcc()
     common = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC,
-                     "-I", os.path.join(HERE, "..", "include")]
+                     "-I", os.path.join(HERE, "..", "include")] + extra
     if ptxas_info:
         common += ["-Xptxas", "-v"]
 
@@ -75,6 +86,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s" % r.stderr)
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(stamp)
     return LIB
 
 

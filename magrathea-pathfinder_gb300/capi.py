@@ -26,7 +26,8 @@ STOP = {"redshift": 0, "r": 1, "radius": 1, "lambda": 2, "t": 3, "eta": 3, "a": 
 EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_upload", "mpf_octree_load",
            "mpf_octree_get_info", "mpf_octree_destroy", "mpf_cosmology_upload", "mpf_cosmology_destroy", "mpf_locate",
            "mpf_interpolate", "mpf_propagate", "mpf_propagate_device", "mpf_propagate_noalloc",
-           "mpf_noalloc_last_error", "mpf_catalogue_newton")
+           "mpf_noalloc_last_error", "mpf_catalogue_newton",
+           "mpf_catalogue_newton_device")
 
 MPF_CATALOGUE_FIELDS = 16
 
@@ -55,7 +56,8 @@ class CatalogueParams(C.Structure):
 
 
 class CatalogueStats(C.Structure):
-    _fields_ = [("rays", C.c_int64), ("photon_steps", C.c_int64), ("iterations", C.c_int)]
+    _fields_ = [("rays", C.c_int64), ("photon_steps", C.c_int64), ("photon_steps_jacobian", C.c_int64),
+                ("iterations", C.c_int), ("kernel_launches", C.c_int)]
 
 
 _lib = None
@@ -90,6 +92,8 @@ def load(path: str = LIB_PATH):
     L.mpf_noalloc_last_error.restype = C.c_char_p
     L.mpf_catalogue_newton.argtypes = [vp, vp, C.POINTER(CatalogueParams), i64, vp, i64, vp,
                                        C.POINTER(CatalogueStats)]
+    L.mpf_catalogue_newton_device.argtypes = [vp, vp, C.POINTER(CatalogueParams), i64, vp, i64, vp,
+                                              C.POINTER(CatalogueStats), vp]
     for name in EXPORTS:
         if name not in ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_destroy",
                         "mpf_cosmology_destroy", "mpf_noalloc_last_error"):

@@ -288,45 +288,72 @@ int mpf_propagate(const mpf_octree* o, const mpf_cosmology* c, const mpf_params*
     return MPF_OK;
 }
 
-int mpf_catalogue_newton(const mpf_octree* o, const mpf_cosmology* c, const mpf_catalogue_params* p, int64_t n,
-                         const double* sources, int64_t stride, double* rows, mpf_catalogue_stats* stats)
+namespace {
+bool catalogue_consts(const mpf_catalogue_params* p, mpf::CatConst& K, mpf::CatRotation& R)
 {
-    if (!o || !c || !p || n < 0 || (n > 0 && (!sources || !rows)) || stride < 6 || stride > 1024)
-        return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: null argument or stride < 6");
-    if (p->nsteps == 0 || (p->order != 1 && p->order != 2) || !(p->length > 0.0) || !(p->h > 0.0) || !(p->mpc > 0.0) ||
-        p->max_iterations < 0 || p->max_iterations > 1000 || !(p->cat_accuracy >= 0.0))
-        return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: bad parameters");
-    if (n > 0x7fffffffll) return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: at most 2^31 - 1 sources per call");
-    if (stats) std::memset(stats, 0, sizeof(*stats));
-    if (n == 0) return MPF_OK;
-    mpf::CatConst K;
+    if (!p || p->nsteps == 0 || (p->order != 1 && p->order != 2) || !(p->length > 0.0) || !(p->h > 0.0) ||
+        !(p->mpc > 0.0) || p->max_iterations < 0 || p->max_iterations > 1000 || !(p->cat_accuracy >= 0.0))
+        return false;
     K.length = p->length; K.h = p->h; K.mpc = p->mpc; K.accuracy = p->cat_accuracy;
     for (int k = 0; k < 3; ++k) K.vobs[k] = p->vobs[k];
     K.max_iterations = p->max_iterations;
-    mpf::CatRotation R;
     if (p->rotm1)
         for (int j = 0; j < 3; ++j)
             for (int k = 0; k < 3; ++k) R.m[j][k] = p->rotm1[3 * j + k];
+    return true;
+}
+}  // namespace
+
+int mpf_catalogue_newton_device(const mpf_octree* o, const mpf_cosmology* c, const mpf_catalogue_params* p, int64_t n,
+                                const double* sources_device, int64_t stride, double* rows_device,
+                                mpf_catalogue_stats* stats, void* stream)
+{
+    mpf::CatConst K;
+    mpf::CatRotation R;
+    if (!o || !c || n < 0 || (n > 0 && (!sources_device || !rows_device)) || stride < 6 || stride > 1024)
+        return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: null argument or stride < 6");
+    if (!catalogue_consts(p, K, R)) return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: bad parameters");
+    if (n > 0x7fffffffll) return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: at most 2^31 - 1 sources per call");
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (n == 0) return MPF_OK;
     mpf::DevCosmo C{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
+    mpf::CatRunStats st;
+    unsigned status = 0;
+    const cudaError_t e = mpf::catalogue_newton(o->tree, C, K, p->rotm1 ? &R : nullptr, p->exact != 0, p->order, p->nsteps,
+                                                n, sources_device, (int)stride, rows_device, &st, &status,
+                                                (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_err(e, "mpf_catalogue_newton");
+    if (stats) {
+        stats->rays = st.rays;
+        stats->photon_steps = st.photon_steps;
+        stats->photon_steps_jacobian = st.photon_steps_jacobian;
+        stats->iterations = st.iterations;
+        stats->kernel_launches = st.launches;
+    }
+    if (status & 1u) return set_err(MPF_WARN_MAX_STEPS, "mpf_catalogue_newton: a ray reached max_steps");
+    return MPF_OK;
+}
+
+int mpf_catalogue_newton(const mpf_octree* o, const mpf_cosmology* c, const mpf_catalogue_params* p, int64_t n,
+                         const double* sources, int64_t stride, double* rows, mpf_catalogue_stats* stats)
+{
+    mpf::CatConst K;
+    mpf::CatRotation R;
+    if (!o || !c || n < 0 || (n > 0 && (!sources || !rows)) || stride < 6 || stride > 1024)
+        return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: null argument or stride < 6");
+    if (!catalogue_consts(p, K, R)) return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: bad parameters");
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (n == 0) return MPF_OK;
     DBuf dsrc, drows;
     cudaError_t e = dsrc.alloc((size_t)n * (size_t)stride * sizeof(double));
     if (e == cudaSuccess) e = drows.alloc((size_t)n * MPF_CATALOGUE_FIELDS * sizeof(double));
     if (e == cudaSuccess) e = cudaMemcpy(dsrc.p, sources, (size_t)n * (size_t)stride * sizeof(double), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_err(e, "mpf_catalogue_newton");
-    mpf::CatRunStats st;
-    unsigned status = 0;
-    e = mpf::catalogue_newton(o->tree, C, K, p->rotm1 ? &R : nullptr, p->exact != 0, p->order, p->nsteps, n,
-                              (const double*)dsrc.p, (int)stride, (double*)drows.p, &st, &status, nullptr);
-    if (e == cudaSuccess)
-        e = cudaMemcpy(rows, drows.p, (size_t)n * MPF_CATALOGUE_FIELDS * sizeof(double), cudaMemcpyDeviceToHost);
+    const int rc = mpf_catalogue_newton_device(o, c, p, n, (const double*)dsrc.p, stride, (double*)drows.p, stats, nullptr);
+    if (rc < 0) return rc;
+    e = cudaMemcpy(rows, drows.p, (size_t)n * MPF_CATALOGUE_FIELDS * sizeof(double), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_err(e, "mpf_catalogue_newton");
-    if (stats) {
-        stats->rays = st.rays;
-        stats->photon_steps = st.photon_steps;
-        stats->iterations = st.iterations;
-    }
-    if (status & 1u) return set_err(MPF_WARN_MAX_STEPS, "mpf_catalogue_newton: a ray reached max_steps");
-    return MPF_OK;
+    return rc;
 }
 
 }  // extern "C"

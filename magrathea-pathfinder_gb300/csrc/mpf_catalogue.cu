@@ -107,7 +107,10 @@ __global__ void k_cat_update(long long m, int iteration, int traced_jacobian, Ca
     CatState S = state[s];
     double* row = rows + (long long)kCatalogueFields * s;
     const double* o = rec + (long long)kSourceFields * j;
-    atomicAdd(photon_steps, (unsigned long long)(steps[j] > 0 ? steps[j] - 1 : 0));
+    // photon_steps[0]: all accepted steps; [1]: those traced with the Jacobian
+    const unsigned long long ns = (unsigned long long)(steps[j] > 0 ? steps[j] - 1 : 0);
+    atomicAdd(photon_steps, ns);
+    if (traced_jacobian) atomicAdd(photon_steps + 1, ns);
     const unsigned count = (unsigned)iteration + 1u;
     if (o[19] == 0.0) {
         // the ray did not reach the source radius (catalogues.h:436-442)
@@ -204,7 +207,9 @@ __global__ void k_cat_jacobian(long long m, const int* __restrict__ list, const 
 {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m) return;
-    atomicAdd(photon_steps, (unsigned long long)(steps[j] > 0 ? steps[j] - 1 : 0));
+    const unsigned long long ns = (unsigned long long)(steps[j] > 0 ? steps[j] - 1 : 0);
+    atomicAdd(photon_steps, ns);
+    atomicAdd(photon_steps + 1, ns);
     const double* o = rec + (long long)kSourceFields * j;
     double* row = rows + (long long)kCatalogueFields * list[j];
     if (o[19] == 0.0) return;
@@ -231,7 +236,9 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     *h_status = 0;
     stats->rays = 0;
     stats->photon_steps = 0;
+    stats->photon_steps_jacobian = 0;
     stats->iterations = 0;
+    stats->launches = 0;
     if (n <= 0) return cudaSuccess;
     const int tpb = 128;
     CatBuffers B;
@@ -252,19 +259,20 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     act1 = (int*)alloc(2, (size_t)n * sizeof(int));
     retr = (int*)alloc(3, (size_t)n * sizeof(int));
     counters = (unsigned*)alloc(4, 8 * sizeof(unsigned));
-    psteps = (unsigned long long*)alloc(5, sizeof(unsigned long long));
+    psteps = (unsigned long long*)alloc(5, 2 * sizeof(unsigned long long));
     launch = (double*)alloc(6, (size_t)n * 6 * sizeof(double));
     radius = (double*)alloc(7, (size_t)n * sizeof(double));
     rec = (double*)alloc(8, (size_t)n * kSourceFields * sizeof(double));
     steps = (long long*)alloc(9, (size_t)n * sizeof(long long));
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(counters, 0, 8 * sizeof(unsigned), stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(psteps, 0, sizeof(unsigned long long), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(psteps, 0, 2 * sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     CatRotation R{};
     if (rot) R = *rot;
     k_cat_init<<<blocks(n, tpb), tpb, 0, stream>>>(n, d_src, stride, R, rot ? 1 : 0, state, d_rows, act0, counters);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    stats->launches = 1;
     unsigned m = 0;
     if ((e = cudaMemcpyAsync(&m, counters, sizeof(unsigned), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
@@ -294,6 +302,7 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         stats->rays += m;
         stats->iterations = it + 1;
+        stats->launches += 3;
         if ((e = cudaMemcpyAsync(&m, counters + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
         if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
         std::swap(cur, nxt);
@@ -311,12 +320,14 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
         k_cat_jacobian<<<blocks(r, tpb), tpb, 0, stream>>>(r, retr, rec, steps, d_rows, psteps);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         stats->rays += r;
+        stats->launches += 3;
     }
-    unsigned long long ps = 0;
-    if ((e = cudaMemcpyAsync(&ps, psteps, sizeof(ps), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
+    unsigned long long ps[2] = {0, 0};
+    if ((e = cudaMemcpyAsync(ps, psteps, sizeof(ps), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(h_status, counters + 3, sizeof(unsigned), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
-    stats->photon_steps = (long long)ps;
+    stats->photon_steps = (long long)ps[0];
+    stats->photon_steps_jacobian = (long long)ps[1];
     return cudaSuccess;
 }
 

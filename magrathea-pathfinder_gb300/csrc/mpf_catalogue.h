@@ -22,7 +22,9 @@ struct CatRotation {
 struct CatRunStats {
     long long rays;
     long long photon_steps;
+    long long photon_steps_jacobian;
     int iterations;
+    int launches;
 };
 
 // d_src: n rows of `stride` doubles on the device; d_rows: n x 16 on the

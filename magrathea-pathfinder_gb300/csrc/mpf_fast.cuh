@@ -635,13 +635,22 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     if (status) atomicOr(O.status, status);
 }
 
-constexpr int kFastThreads = 128;
+// Launch shape of the persistent kernel: threads per block and the minimum
+// resident blocks per SM promised to the register allocator (168 registers
+// per thread at 128 x 3).  Overridable at build time for tuning sweeps.
+#ifndef MPF_FAST_THREADS
+#define MPF_FAST_THREADS 128
+#endif
+#ifndef MPF_FAST_MINB
+#define MPF_FAST_MINB 3
+#endif
+constexpr int kFastThreads = MPF_FAST_THREADS;
 
 // Persistent launch: each warp takes the next 32 rays from a global counter
 // until the batch is exhausted, so uneven path lengths do not leave tail
 // waves.  `queue` is zeroed before the launch.
 template <int ORDER, bool SRC>
-__global__ void __launch_bounds__(kFastThreads, 3) k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
+__global__ void __launch_bounds__(kFastThreads, MPF_FAST_MINB) k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
                                                                     const double* __restrict__ launch, long long n, PropOut O,
                                                                     unsigned long long* queue)
 {
