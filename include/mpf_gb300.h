@@ -169,7 +169,9 @@ typedef struct {
 typedef struct {
     int64_t rays;              /* rays integrated, Jacobian re-traces included */
     int64_t photon_steps;      /* accepted RK4 steps over all of them */
+    int64_t photon_steps_jacobian;  /* the part traced with the lensing Jacobian */
     int iterations;            /* Newton rounds run (at most max_iterations + 1) */
+    int kernel_launches;       /* kernels this call launched */
 } mpf_catalogue_stats;
 
 /* Replaces Catalogues::relCat's per-source loop body (src/catalogues.h:811-856)
@@ -186,6 +188,45 @@ typedef struct {
  * reference's firstid in column 5 (catalogues.h:436-442).  stats may be NULL. */
 int mpf_catalogue_newton(const mpf_octree* o, const mpf_cosmology* c, const mpf_catalogue_params* p, int64_t n,
                          const double* sources, int64_t stride, double* rows, mpf_catalogue_stats* stats);
+/* Same, with sources and rows in device memory, on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream).  The call synchronises the stream once
+ * per Newton round (the size of each round decides the next launch) and
+ * returns when the rows are complete. */
+int mpf_catalogue_newton_device(const mpf_octree* o, const mpf_cosmology* c, const mpf_catalogue_params* p, int64_t n,
+                                const double* sources_device, int64_t stride, double* rows_device,
+                                mpf_catalogue_stats* stats, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* HEALPix maps                                                              */
+/* ------------------------------------------------------------------------ */
+/* Map components, the reference's index_components (src/hmaps.cpp:196-269,
+ * hmaps.h:716-829): rows per surface in the order given; lensing gives 4
+ * rows (kappa, gamma1, gamma2, 1/mu), deflection 2 (phi - beta1,
+ * theta - beta2), the others 1. */
+typedef enum {
+    MPF_MAP_LENSING = 0,
+    MPF_MAP_DR = 2, MPF_MAP_DL = 3, MPF_MAP_DT = 4, MPF_MAP_DA = 5, MPF_MAP_DZ = 6, MPF_MAP_DS = 7,
+    MPF_MAP_ISW = 8, MPF_MAP_DENS = 9, MPF_MAP_DENS_MAX = 10, MPF_MAP_STEPS = 11, MPF_MAP_PHI = 12,
+    MPF_MAP_DEFLECTION = 13
+} mpf_map_component;
+#define MPF_MAX_MAP_COMPONENTS 16
+
+/* Replaces Hmaps::FillMap (src/hmaps.h:583-832, jacobiantype = "infinitesimal")
+ * for npix RING pixels of an nside map: pixel centre (pix2vec_ring), one ray
+ * per pixel from the origin integrated to the last surface (p->planes, the
+ * stop quantity p->stop: interpRefvec), the Jacobian and per-surface values,
+ * and the float map rows.  homogeneous: nplanes x 5 (t, chi, lambda, a, z of
+ * the FLRW reference ray at each surface, hmaps.cpp:302-333; the dr / dl /
+ * dt / da / dz / ds rows are relative to them).  maps: nmaps * nplanes rows of
+ * npix floats, row nmaps * iz + r for surface iz (the reference's map vector
+ * order, columns in the order of `pixels`).  A pixel whose surface crossing
+ * is unusable has 0 in every row of that surface, as in the reference. */
+int mpf_hmaps_fill(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t nside, int64_t npix,
+                   const int64_t* pixels, int ncomp, const int* components, const double* homogeneous, float* maps);
+
+/* RING pixel centres computed on the device (the directions mpf_hmaps_fill
+ * launches): vec[3n]. */
+int mpf_pix2vec_ring(int64_t nside, int64_t n, const int64_t* pixels, double* vec);
 
 #ifdef __cplusplus
 }

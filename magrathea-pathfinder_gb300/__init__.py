@@ -16,6 +16,8 @@ Integrator::integrate       ``propagate(...)`` (batched over rays), with
    infinitesimal            per-surface values at each surface
 Catalogues::relCat /        ``catalogue(...)``: the Newton root-finder for a
   iterateNewtonMethod       batch of sources, relCat's 16-column rows
+Hmaps::FillMap              ``hmaps_fill(...)``: pixels in, float map rows out
+pix2vec_ring                ``pix2vec_ring(nside, pixels)`` (device)
 ==========================  ==================================================
 """
 from __future__ import annotations
@@ -35,7 +37,7 @@ PLANE_FIELDS = ("firstid f x y z distance A11 A12 A22 t a redshift chi lambda s 
 CATALOGUE_FIELDS = ("phi theta phi_obs theta_obs miss iterations z_flrw z_pot z_dopp z_tdopp z_isw z_gr "
                     "a11 a12 a21 a22").split()
 
-__all__ = ["Octree", "Cosmology", "propagate", "catalogue", "MpfError", "PHOTON_FIELDS", "PLANE_FIELDS",
+__all__ = ["Octree", "Cosmology", "propagate", "catalogue", "hmaps_fill", "pix2vec_ring", "MpfError", "PHOTON_FIELDS", "PLANE_FIELDS",
            "CATALOGUE_FIELDS", "library"]
 
 
@@ -192,3 +194,37 @@ def catalogue_params(length, h, mpc=3.08568e22, cat_accuracy=1e-8, nsteps=10, or
 def catalogue_stats(st) -> dict:
     return dict(rays=st.rays, photon_steps=st.photon_steps, photon_steps_jacobian=st.photon_steps_jacobian,
                 iterations=st.iterations, kernel_launches=st.kernel_launches)
+
+
+def hmaps_fill(octree: Octree, cosmology: Cosmology, nside: int, pixels, surfaces, homogeneous, components,
+               length: float, nsteps: int = 10, order: int = 2, stop: str = "redshift", exact: bool = False,
+               max_steps: int = 0):
+    """Hmaps::FillMap for the given RING pixels: float maps [nsurfaces, nmaps, npix].
+
+    surfaces: the stop-quantity values of the map surfaces (interpRefvec);
+    homogeneous: [nsurfaces, 5] = t, chi, lambda, a, z of the FLRW ray there;
+    components: the reference's map component names, in order.
+    """
+    L = capi.load()
+    pix = np.ascontiguousarray(pixels, dtype=np.int64)
+    comps = [capi.MAP_COMPONENTS[c] for c in components]
+    nm = sum(4 if c == 0 else 2 if c == 13 else 1 for c in comps)
+    p, keep = capi.make_params(length, nsteps, order, stop, 0.0, surfaces, True, exact, max_steps)
+    hom = np.ascontiguousarray(homogeneous, dtype=np.float64).reshape(-1, 5)
+    cc = np.ascontiguousarray(comps, dtype=np.int32)
+    nz = p.nplanes
+    maps = np.zeros((nz, nm, pix.shape[0]), dtype=np.float32)
+    rc = L.mpf_hmaps_fill(octree._h, cosmology._h, C.byref(p), int(nside), pix.shape[0], capi.ptr(pix), len(comps),
+                          capi.ptr(cc), capi.ptr(hom), capi.ptr(maps))
+    capi.check(rc)
+    del keep
+    return maps
+
+
+def pix2vec_ring(nside: int, pixels) -> np.ndarray:
+    """RING pixel centres computed on the device: [n, 3]."""
+    L = capi.load()
+    pix = np.ascontiguousarray(pixels, dtype=np.int64)
+    out = np.zeros((pix.shape[0], 3))
+    capi.check(L.mpf_pix2vec_ring(int(nside), pix.shape[0], capi.ptr(pix), capi.ptr(out)))
+    return out

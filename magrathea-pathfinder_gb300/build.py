@@ -26,6 +26,7 @@ UNITS = [
     ("mpf_capi.cu", []),
     ("mpf_noalloc.cu", []),
     ("mpf_catalogue.cu", ["-fmad=false"]),
+    ("mpf_maps.cu", ["-fmad=false"]),
 ]
 
 

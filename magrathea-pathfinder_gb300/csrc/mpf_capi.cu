@@ -8,6 +8,7 @@
 #include "../../include/mpf_gb300.h"
 #include "mpf_catalogue.h"
 #include "mpf_internal.h"
+#include "mpf_maps.h"
 
 extern "C" int mpf_internal_octree_build(const void* records, int64_t n, int on_device, cudaStream_t stream,
                                          mpf_octree** out, char* err, int errlen);
@@ -354,6 +355,72 @@ int mpf_catalogue_newton(const mpf_octree* o, const mpf_cosmology* c, const mpf_
     e = cudaMemcpy(rows, drows.p, (size_t)n * MPF_CATALOGUE_FIELDS * sizeof(double), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_err(e, "mpf_catalogue_newton");
     return rc;
+}
+
+int mpf_hmaps_fill(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t nside, int64_t npix,
+                   const int64_t* pixels, int ncomp, const int* components, const double* homogeneous, float* maps)
+{
+    mpf::PropParams P;
+    if (!o || !c || !fill_params(p, P) || npix < 0 || (npix > 0 && (!pixels || !maps)) || nside < 1 ||
+        nside > (1ll << 29) || ncomp < 1 || ncomp > MPF_MAX_MAP_COMPONENTS || !components || !homogeneous)
+        return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill: bad argument");
+    if (p->nplanes < 1) return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill: at least one surface (p->planes) is needed");
+    if (p->stop == MPF_STOP_PLANE) return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill: stop_ray 'plane' has no map surfaces");
+    mpf::MapSpec M;
+    std::memset(&M, 0, sizeof(M));
+    M.ncomp = ncomp;
+    for (int q = 0; q < ncomp; ++q) {
+        const int k = components[q];
+        if (k < 0 || k > 13 || k == 1)
+            return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill: unknown map component (lensing_born is not built)");
+        M.comp[q] = k;
+        M.nmaps += (k == MPF_MAP_LENSING) ? 4 : (k == MPF_MAP_DEFLECTION) ? 2 : 1;
+    }
+    for (int iz = 0; iz < p->nplanes; ++iz)
+        for (int k = 0; k < 5; ++k) M.homogeneous[iz][k] = homogeneous[5 * iz + k];
+    const long long npixall = 12ll * nside * nside;
+    for (int64_t i = 0; i < npix; ++i)
+        if (pixels[i] < 0 || pixels[i] >= npixall) return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill: pixel id out of range");
+    P.jacobian = 1;
+    if (npix == 0) return MPF_OK;
+    mpf::DevCosmo C{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
+    const size_t map_bytes = (size_t)M.nmaps * (size_t)p->nplanes * (size_t)npix * sizeof(float);
+    DBuf dpix, dmaps;
+    cudaError_t e = dpix.alloc((size_t)npix * sizeof(int64_t));
+    if (e == cudaSuccess) e = dmaps.alloc(map_bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(dpix.p, pixels, (size_t)npix * sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_err(e, "mpf_hmaps_fill");
+    unsigned status = 0;
+    e = mpf::hmaps_fill(o->tree, C, P, p->exact != 0, nside, npix, (const long long*)dpix.p, M, (float*)dmaps.p,
+                        1ll << 22, &status, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(maps, dmaps.p, map_bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(e, "mpf_hmaps_fill");
+    if (status & 1u) return set_err(MPF_WARN_MAX_STEPS, "mpf_hmaps_fill: a ray reached max_steps");
+    return MPF_OK;
+}
+
+int mpf_pix2vec_ring(int64_t nside, int64_t n, const int64_t* pixels, double* vec)
+{
+    if (nside < 1 || nside > (1ll << 29) || n < 0 || (n > 0 && (!pixels || !vec)))
+        return set_err(MPF_BAD_INPUT, "mpf_pix2vec_ring: bad argument");
+    for (int64_t i = 0; i < n; ++i)
+        if (pixels[i] < 0 || pixels[i] >= 12ll * nside * nside) return set_err(MPF_BAD_INPUT, "mpf_pix2vec_ring: pixel id out of range");
+    if (n == 0) return MPF_OK;
+    if (!has_device()) return set_err(MPF_NO_DEVICE, "mpf_pix2vec_ring: no CUDA device");
+    DBuf dpix, dl;
+    cudaError_t e = dpix.alloc((size_t)n * sizeof(int64_t));
+    if (e == cudaSuccess) e = dl.alloc((size_t)n * 6 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(dpix.p, pixels, (size_t)n * sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = mpf::pix2vec_device(nside, n, (const long long*)dpix.p, (double*)dl.p, nullptr);
+    std::vector<double> L;
+    if (e == cudaSuccess) {
+        L.resize((size_t)n * 6);
+        e = cudaMemcpy(L.data(), dl.p, (size_t)n * 6 * sizeof(double), cudaMemcpyDeviceToHost);
+    }
+    if (e != cudaSuccess) return cuda_err(e, "mpf_pix2vec_ring");
+    for (int64_t i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) vec[3 * i + k] = L[6 * i + 3 + k];
+    return MPF_OK;
 }
 
 }  // extern "C"

@@ -56,7 +56,7 @@ __device__ __forceinline__ void tsc_w3(float f, float* w)
 // centre in cell units (exact scaling by 2^L / EXTENT)
 __device__ __forceinline__ void point_cell(int L, double x, double y, double z, uint32_t* c, float* fd)
 {
-    const double s = (double)(1ull << L) * (1.0 / (double)kExtent);
+    const double s = pow2(L - kLevelShift);   // 2^L / EXTENT, exact
     const double u[3] = {(x + 2.0) * s, (y + 2.0) * s, (z + 2.0) * s};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -102,7 +102,7 @@ struct Loc {
     float fd[3];
 };
 
-__device__ __forceinline__ float cells_per_unit(int L) { return (float)(1ull << L) * (1.0f / (float)kExtent); }
+__device__ __forceinline__ float cells_per_unit(int L) { return __int_as_float((127 + L - kLevelShift) << 23); }
 
 // full location by a walk from the top grid (float64 coordinates)
 __device__ __noinline__ Loc locate_full(const DevTree& T, double x, double y, double z)
@@ -143,7 +143,10 @@ __device__ __forceinline__ Loc locate_near(const DevTree& T, const Loc& h, doubl
                     r.level = h.level;
                     const double w = cell_extent(h.level);
                     r.c[0] = h.c[0] + ox; r.c[1] = h.c[1] + oy; r.c[2] = h.c[2] + oz;
-                    r.cen[0] = h.cen[0] + ox * w; r.cen[1] = h.cen[1] + oy * w; r.cen[2] = h.cen[2] + oz * w;
+                    // +-w or 0 per axis (selects, no int-to-double conversion)
+                    r.cen[0] = h.cen[0] + (ox > 0 ? w : (ox < 0 ? -w : 0.0));
+                    r.cen[1] = h.cen[1] + (oy > 0 ? w : (oy < 0 ? -w : 0.0));
+                    r.cen[2] = h.cen[2] + (oz > 0 ? w : (oz < 0 ? -w : 0.0));
                     r.fd[0] = rx - (float)ox; r.fd[1] = ry - (float)oy; r.fd[2] = rz - (float)oz;
                     return r;
                 }
@@ -164,9 +167,12 @@ __device__ __forceinline__ Loc step_cell(const DevTree& T, const Loc& h, int axi
         if (!(fl & 256) && (fl & 255) == h.level) {
             Loc r = h;
             r.cell = e;
-            const double w = cell_extent(h.level);
+            const double sw = (sgn > 0) ? cell_extent(h.level) : -cell_extent(h.level);
             r.c[0] += ox; r.c[1] += oy; r.c[2] += oz;
-            r.cen[0] += ox * w; r.cen[1] += oy * w; r.cen[2] += oz * w;
+            const double moved = ((axis == 0) ? h.cen[0] : (axis == 1) ? h.cen[1] : h.cen[2]) + sw;
+            if (axis == 0) r.cen[0] = moved;
+            else if (axis == 1) r.cen[1] = moved;
+            else r.cen[2] = moved;
             return r;
         }
     }
@@ -313,24 +319,37 @@ __device__ __forceinline__ double recip(double a)
 }
 
 
-// geodesic RHS (integrator.h:409-445) from the field at the point
-__device__ __forceinline__ void rhs_math(const DevCosmo& C, const Field7& g, double inv_scale, const double* in, double* out)
+// geodesic RHS (integrator.h:409-445) from the field at the point.
+// in = (a, t, x, y, z, k0, k1, k2, k3).  The FP64 pipe of this GPU retires 2
+// operations per cycle per SM (1/64 of FP32), so the RHS keeps in FP64 only
+// what the trajectory's accuracy needs:
+//  * dphi/dlambda and the terms built from it are FP32: they only enter as
+//    (2/c^2) dphi/dlambda, a rate that multiplies k (its error changes |k| by
+//    a relative 1e-7 of that term's increment, not the direction);
+//  * the lensing source 2 dphi/dx^i k0^2 is an FP32 product (the field is FP32);
+//  * the Hubble drag and the k^i multiplications stay FP64, so the direction
+//    of k and the positions keep float64 accuracy;
+//  * dx/dlambda is returned as k itself: the caller folds 1/scale into the
+//    RK coefficient (one multiplication per stage instead of three).
+__device__ __forceinline__ void rhs_math(const DevCosmo& C, const Field7& g, const double* in, double* out)
 {
     const double c2 = kC * kC;
-    const double dphidl = (double)g.dt * in[5] + ((double)g.dx * in[6] + (double)g.dy * in[7] + (double)g.dz * in[8]);
+    const float k0f = (float)in[5], k1f = (float)in[6], k2f = (float)in[7], k3f = (float)in[8];
+    const float dphidl = g.dt * k0f + (g.dx * k1f + g.dy * k2f + g.dz * k3f);
     const double dadt = interp_fast(C, in[1], C.dadt, C.slope_dadt);
     out[0] = in[5] * dadt;
     out[1] = in[5];
-    out[2] = in[6] * inv_scale;
-    out[3] = in[7] * inv_scale;
-    out[4] = in[8] * inv_scale;
-    const double hub = 2.0 * dadt * recip(in[0]) * in[5];
-    const double gg = (2.0 / c2) * dphidl;
-    const double k02 = 2.0 * in[5] * in[5];
-    out[5] = -(hub * in[5]) - ((2.0 / c2) * in[5]) * (dphidl - (double)g.dt * in[5]);
-    out[6] = -(hub * in[6]) + (gg * in[6]) - ((double)g.dx * k02);
-    out[7] = -(hub * in[7]) + (gg * in[7]) - ((double)g.dy * k02);
-    out[8] = -(hub * in[8]) + (gg * in[8]) - ((double)g.dz * k02);
+    out[2] = in[6];
+    out[3] = in[7];
+    out[4] = in[8];
+    const double hub = 2.0 * out[0] * recip(in[0]);
+    const float two_c2 = (float)(2.0 / c2);
+    const float k02 = 2.0f * k0f * k0f;
+    out[5] = -(hub * in[5]) - (double)((two_c2 * k0f) * (dphidl - g.dt * k0f));
+    const double coef = (double)(two_c2 * dphidl) - hub;
+    out[6] = fma(coef, in[6], -(double)(g.dx * k02));
+    out[7] = fma(coef, in[7], -(double)(g.dy * k02));
+    out[8] = fma(coef, in[8], -(double)(g.dz * k02));
 }
 
 // Jacobian terms (d1d1, d1d2, d2d2 of lensing.h:430-447) at a trajectory
@@ -338,19 +357,20 @@ __device__ __forceinline__ void rhs_math(const DevCosmo& C, const Field7& g, dou
 __device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, double x, double y, double z, float* out3,
                                          unsigned long long* st)
 {
-    const double dl = ldexp(1.0, kLevelShift + 1 - here.level);
-    const double h = 0.5 * dl;   // one cell of the point's level
+    // dl = 2^-(level - 1 - log2 EXTENT) (lensing.h:430); h = dl / 2 = one cell of the point's level
+    const double h = pow2(kLevelShift - here.level);
     float g[6][3];
 #pragma unroll 1
     for (int a = 0; a < 6; ++a) {
         const int ax = a >> 1;
         const int sgn = (a & 1) ? 1 : -1;
-        const double qx = x + (ax == 0 ? sgn * h : 0.0), qy = y + (ax == 1 ? sgn * h : 0.0), qz = z + (ax == 2 ? sgn * h : 0.0);
+        const double moved = ((ax == 0) ? x : (ax == 1) ? y : z) + ((a & 1) ? h : -h);
+        const double qx = (ax == 0) ? moved : x, qy = (ax == 1) ? moved : y, qz = (ax == 2) ? moved : z;
         const Loc d = step_cell(T, here, ax, sgn, qx, qy, qz);
         const Field7 f = gather_at<2>(T, d, qx, qy, qz, false, st, ST_JAC_REC, false);
         g[a][0] = f.dx; g[a][1] = f.dy; g[a][2] = f.dz;
     }
-    const float idl = (float)(1.0 / dl);
+    const float idl = __int_as_float((127 + here.level - kLevelShift - 1) << 23);   // 1 / dl, exact
     const float dxx = (g[1][0] - g[0][0]) * idl, dxy = (g[3][0] - g[2][0]) * idl, dxz = (g[5][0] - g[4][0]) * idl;
     const float dyy = (g[3][1] - g[2][1]) * idl, dyz = (g[5][1] - g[4][1]) * idl, dzz = (g[5][2] - g[4][2]) * idl;
     const float fx = (float)x, fy = (float)y, fz = (float)z;
@@ -442,25 +462,27 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
 #pragma unroll 1
         for (int sg = 0; sg < 4; ++sg) {
             if (sg == 0) {
-                rhs_math(C, data, inv_scale, bc, dc);
+                rhs_math(C, data, bc, dc);
             } else {
                 const Loc d = locate_near(T, here, core[2], core[3], core[4]);
                 const Field7 g = gather_at<ORDER>(T, d, core[2], core[3], core[4], false, st, ST_RK_REC, false);
-                rhs_math(C, g, inv_scale, core, dc);
+                rhs_math(C, g, core, dc);
             }
             const double cs = (sg < 2) ? 0.5 * dl : dl;
+            const double csp = cs * inv_scale;   // positions: dx/dl = k / scale
             const double wa = (sg == 0) ? 0.0 : 2.0;
             if (sg < 3) {
 #pragma unroll
                 for (int q = 0; q < 9; ++q) {
                     acc[q] = (sg == 0) ? dc[q] : acc[q] + wa * dc[q];
-                    core[q] = bc[q] + cs * dc[q];
+                    core[q] = bc[q] + ((q >= 2 && q <= 4) ? csp : cs) * dc[q];
                 }
             }
         }
         const double dl6 = dl * (1.0 / 6.0);
+        const double dl6p = dl6 * inv_scale;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) core[q] = bc[q] + dl6 * (acc[q] + dc[q]);
+        for (int q = 0; q < 9; ++q) core[q] = bc[q] + ((q >= 2 && q <= 4) ? dl6p : dl6) * (acc[q] + dc[q]);
         p.a = core[0]; p.t = core[1]; p.x = core[2]; p.y = core[3]; p.z = core[4];
         p.k0 = core[5]; p.k1 = core[6]; p.k2 = core[7]; p.k3 = core[8];
         const Loc ploc = locate_near(T, here, p.x, p.y, p.z);
@@ -472,14 +494,16 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         p.dt = -data.dt;
         const float dphi_last = data.phi - (float)b.phi;   // laplacian of the final record, divided at the end
         const double dl_last = dl;
-        isw += ((double)b.dt + (double)p.dt) * (p.t - b.t) * (1.0 / c2);
-        iswold -= 2.0 * (p.phi - b.phi) * (1.0 / c2) -
-                  (((double)b.dx + (double)p.dx) * (p.x - b.x) * scale + ((double)b.dy + (double)p.dy) * (p.y - b.y) * scale +
-                   ((double)b.dz + (double)p.dz) * (p.z - b.z) * scale) * (1.0 / c2);
+        isw += (double)(b.dt + p.dt) * (p.t - b.t) * (1.0 / c2);
+        if (O.final_rec) {   // only the final photon record reports it
+            iswold -= 2.0 * (p.phi - b.phi) * (1.0 / c2) -
+                      (((double)b.dx + (double)p.dx) * (p.x - b.x) * scale + ((double)b.dy + (double)p.dy) * (p.y - b.y) * scale +
+                       ((double)b.dz + (double)p.dz) * (p.z - b.z) * scale) * (1.0 / c2);
+        }
         p.chi = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
         lambda += dl;
         sacc += (double)sqrtf((float)((p.x - b.x) * (p.x - b.x) + (p.y - b.y) * (p.y - b.y) + (p.z - b.z) * (p.z - b.z)));
-        p.red = a0 / p.a * (1.0 + phi0c2 - p.phi / c2) - 1.0;
+        p.red = a0 * recip(p.a) * (1.0 + phi0c2 - p.phi * (1.0 / c2)) - 1.0;
         p.isw = isw; p.iswold = iswold; p.lambda = lambda; p.s = sacc;
         if (!is_empty(data)) {
             ratio = p.a * p.a * ratio_k;

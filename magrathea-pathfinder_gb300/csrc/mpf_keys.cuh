@@ -12,6 +12,7 @@
 // reference is evaluated in IEEE float64 without contraction; the CUDA
 // sources that include this header are compiled with -fmad=false.
 #pragma once
+#include <cmath>
 #include <cstdint>
 
 #if defined(__CUDACC__)
@@ -30,6 +31,18 @@ struct Key {
     uint64_t hi, lo;
 };
 
+// 2^e as a double, built from its exponent bits (|e| <= 1022): the cell
+// sizes and scales below are powers of two, so they need neither an
+// int-to-double conversion nor a division, and are exact.
+MPF_HD double pow2(int e)
+{
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)(1023 + e) << 52);
+#else
+    return std::ldexp(1.0, e);
+#endif
+}
+
 MPF_HD bool key_less(Key a, Key b) { return (a.hi < b.hi) || (a.hi == b.hi && a.lo < b.lo); }
 MPF_HD bool key_le(Key a, Key b) { return !key_less(b, a); }
 MPF_HD bool key_eq(Key a, Key b) { return a.hi == b.hi && a.lo == b.lo; }
@@ -38,7 +51,7 @@ MPF_HD bool key_eq(Key a, Key b) { return a.hi == b.hi && a.lo == b.lo; }
 // (the reference's conversion is undefined there; valid rays never get there).
 MPF_HD uint64_t axis_coord(int level, double x)
 {
-    const double scale = (1.0 / (double)kExtent) * (double)(1ull << level);
+    const double scale = pow2(level - kLevelShift);   // (1 / EXTENT) * 2^level, exact
     const double v = scale * (x - (-(double)kExtent / 2.0));
     uint64_t c = (v > 0.0) ? (uint64_t)v : 0ull;
     return (level >= 64) ? c : (c & ((1ull << level) - 1ull));
@@ -79,17 +92,18 @@ MPF_HD int key_level(Key k)
 // (exact in float64 for level <= 32).
 MPF_HD double coord_center(int level, uint64_t c)
 {
-    return (-(double)kExtent / 2.0) + ((double)kExtent * ((double)(2ull * c + 1ull) / (double)(1ull << (level + 1))));
+    // EXTENT * ((2c + 1) / 2^(L+1)) == (2c + 1) * 2^(2-L-1) exactly (powers of two)
+    return (-(double)kExtent / 2.0) + (double)(2ull * c + 1ull) * pow2(kLevelShift - level - 1);
 }
 
 // Half of the cell size at `level`, in octree units, as the reference
 // computes it: EXTENT/1 * (1/(1*2^L)) / 2.
 MPF_HD double half_cell(int level)
 {
-    return (double)kExtent / 1.0 * (1.0 / (1.0 * (double)(1ull << level))) / 2.0;
+    return pow2(kLevelShift - level - 1);   // EXTENT/1 * (1/2^L) / 2, exact
 }
 
 // extent<double, ratio<0>, ratio<EXTENT>>(): EXTENT / (1 * 2^L).
-MPF_HD double cell_extent(int level) { return (double)kExtent / (1.0 * (double)(1ull << level)); }
+MPF_HD double cell_extent(int level) { return pow2(kLevelShift - level); }
 
 }  // namespace mpf

@@ -42,6 +42,16 @@ def test_bad_input_is_a_status_not_a_crash(pkg):
     src = np.zeros((1, 6))
     assert L.mpf_catalogue_newton(None, None, ctypes.byref(cp), 1, capi.ptr(src), 6, capi.ptr(rows), None) == -1
     assert b"mpf_catalogue_newton" in L.mpf_last_error()
+    p, keep = capi.make_params(1.0, planes=[0.1])
+    comps = np.zeros(1, dtype=np.int32)
+    maps = np.zeros(4, dtype=np.float32)
+    pix = np.zeros(1, dtype=np.int64)
+    assert L.mpf_hmaps_fill(None, None, ctypes.byref(p), 4, 1, capi.ptr(pix), 1, capi.ptr(comps), capi.ptr(rows),
+                            capi.ptr(maps)) == -1
+    assert L.mpf_pix2vec_ring(0, 1, capi.ptr(pix), capi.ptr(rows)) == -1
+    pix[0] = 12 * 4 * 4      # out of range for nside 4
+    assert L.mpf_pix2vec_ring(4, 1, capi.ptr(pix), capi.ptr(rows)) == -1
+    del keep
     if L.mpf_device_count() == 0:
         rec = np.zeros(2, dtype=np.dtype([("b", "u1", 48)]))
         assert L.mpf_octree_upload(ctypes.c_void_p(rec.ctypes.data), 2, ctypes.byref(h)) == -5

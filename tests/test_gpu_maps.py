@@ -1,0 +1,44 @@
+"""Map filling on the GPU (mpf_hmaps_fill: pixels in, float map rows out)
+against the reference's own Hmaps::FillMap maps in tests/golden.
+
+The device computes the RING pixel centres itself; they agree with the
+harness's pix2vec_ring (the same published formulas with glibc's cos / sin)
+to 4e-16, so exact-mode rays start a few ulps apart from the reference's and
+the maps are compared with the fast-mode tolerances: the validity pattern
+exactly, lensing rows within 1e-6 of their scale, the other rows within
+2e-6 of their scale plus 1e-12."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_pix2vec_matches_harness(gpu_lib, pkg, golden):
+    v = pkg.pix2vec_ring(int(golden["nside"]), golden["pixels"])
+    assert np.abs(v - golden["pixel_dirs"]).max() <= 4e-16
+    # pixels over the whole sphere: unit vectors, and the ring latitudes of the scheme
+    nside = 8
+    allv = pkg.pix2vec_ring(nside, np.arange(12 * nside * nside))
+    assert np.allclose(np.linalg.norm(allv, axis=1), 1.0, atol=1e-15)
+    assert np.unique(np.round(allv[:, 2], 12)).shape[0] == 4 * nside - 1
+    assert abs(allv[:, 2].mean()) < 1e-12     # equal-area pixels: zero mean z
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("exact", [True, False])
+def test_hmaps_fill_matches_reference_fillmap(gpu_lib, pkg, golden, order, exact):
+    tree = pkg.Octree.from_records(golden["records"])
+    cos = pkg.Cosmology(golden["cosmo_t"], golden["cosmo_a"], golden["cosmo_dadt"], golden["cosmo_d2adt2"])
+    comps = str(golden["components"]).split(",")
+    got = pkg.hmaps_fill(tree, cos, int(golden["nside"]), golden["pixels"], golden["zs"], golden["homogeneous"], comps,
+                         float(golden["cosmo_length"]), nsteps=int(golden["nsteps"]), order=order, exact=exact)
+    ref = golden["ref_maps_o%d" % order]
+    assert got.shape == ref.shape
+    srow = 4 + comps.index("steps") - 1
+    np.testing.assert_array_equal(got[:, srow] != 0, ref[:, srow] != 0)
+    for row in range(4):
+        scale = max(np.abs(ref[:, row]).max(), 1e-6)
+        assert np.abs(got[:, row] - ref[:, row]).max() <= 1e-6 * scale + 2e-7 * (row == 3), row
+    for row in range(4, ref.shape[1]):
+        scale = np.abs(ref[:, row]).max() + 1e-30
+        assert np.abs(got[:, row] - ref[:, row]).max() <= 2e-6 * scale + 1e-12, row
