@@ -660,13 +660,15 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
 }
 
 // Launch shape of the persistent kernel: threads per block and the minimum
-// resident blocks per SM promised to the register allocator (168 registers
-// per thread at 128 x 3).  Overridable at build time for tuning sweeps.
+// resident blocks per SM promised to the register allocator.  128 x 2 (up to
+// 255 registers, 8 warps per SM) measured fastest on the AMR and medium
+// octrees, ahead of 128 x 3 (168 registers, spills) and 128 x 4.
+// Overridable at build time for tuning sweeps.
 #ifndef MPF_FAST_THREADS
 #define MPF_FAST_THREADS 128
 #endif
 #ifndef MPF_FAST_MINB
-#define MPF_FAST_MINB 3
+#define MPF_FAST_MINB 2
 #endif
 constexpr int kFastThreads = MPF_FAST_THREADS;
 
