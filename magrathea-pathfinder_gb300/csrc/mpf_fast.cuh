@@ -44,6 +44,33 @@ __device__ __forceinline__ double interp_fast(const DevCosmo& C, double x0, cons
     return __ldg(y + i - 1) + __ldg(slope + i - 1) * (x0 - __ldg(C.t + i - 1));
 }
 
+// Upper-bound position of x0 in the cosmology table (the bracket
+// Utility::interpolate uses), from the uniform index table.
+__device__ __forceinline__ int bracket_lut(const DevCosmo& C, double x0)
+{
+    if (x0 < C.t0) return 0;
+    const double kk = (x0 - C.t0) * C.lut_scale;
+    const int k = (kk < (double)C.nlut) ? (int)kk : C.nlut;
+    int i = __ldg(C.lut + k);
+    while (i < C.n && !(x0 < __ldg(C.t + i))) ++i;
+    return i;
+}
+
+// Utility::interpolate with the bracket carried from the previous call: a
+// ray's conformal time moves by much less than a table interval between two
+// calls, so `first` (the upper bound of x0) is re-checked, not searched.
+__device__ __forceinline__ double interp_cached(const DevCosmo& C, double x0, const double* __restrict__ y,
+                                                const double* __restrict__ slope, int& first)
+{
+    const int n = C.n;
+    while (first < n && !(x0 < __ldg(C.t + first))) ++first;
+    while (first > 0 && x0 < __ldg(C.t + first - 1)) --first;
+    int i = first;
+    i += (n > 1) * ((i <= 0) - (i >= n));
+    if (n <= 1) return (n > 0) ? __ldg(y) : 0.0;
+    return __ldg(y + i - 1) + __ldg(slope + i - 1) * (x0 - __ldg(C.t + i - 1));
+}
+
 __device__ __forceinline__ void tsc_w3(float f, float* w)
 {
     const float m = 0.5f - f, p = 0.5f + f;
@@ -92,6 +119,24 @@ __device__ __noinline__ Field7 cic_slow(const DevTree& T, double x, double y, do
 }
 __device__ __noinline__ Found locate_slow(const DevTree& T, double x, double y, double z) { return locate(T, x, y, z); }
 
+// A point given by its float64 coordinates.
+struct PosAt {
+    double x, y, z;
+    __device__ __forceinline__ double px() const { return x; }
+    __device__ __forceinline__ double py() const { return y; }
+    __device__ __forceinline__ double pz() const { return z; }
+};
+
+// An RK stage point, b + c k: its float64 coordinates are formed only where a
+// rare path (a full walk, a restart at a coarser cell) needs them; the common
+// path works on the FP32 offset from the step's start cell.
+struct PosStage {
+    double bx, by, bz, c, kx, ky, kz;
+    __device__ __forceinline__ double px() const { return fma(c, kx, bx); }
+    __device__ __forceinline__ double py() const { return fma(c, ky, by); }
+    __device__ __forceinline__ double pz() const { return fma(c, kz, bz); }
+};
+
 // A located point: its deepest cell, that cell's level, integer coordinates
 // and centre, and the point's offset from the centre in cell units.
 struct Loc {
@@ -122,11 +167,10 @@ __device__ __noinline__ Loc locate_full(const DevTree& T, double x, double y, do
 // from h's centre is formed in float64 (one subtraction per axis) and the rest
 // in FP32; the cell is h or one of its 26 neighbours read from h's record when
 // that neighbour is a leaf of h's level; otherwise a full walk.
-__device__ __forceinline__ Loc locate_near(const DevTree& T, const Loc& h, double x, double y, double z)
+template <class P>
+__device__ __forceinline__ Loc locate_rel(const DevTree& T, const Loc& h, float rx, float ry, float rz, const P& pos)
 {
     if (h.cell >= 0) {
-        const float sc = cells_per_unit(h.level);
-        const float rx = (float)(x - h.cen[0]) * sc, ry = (float)(y - h.cen[1]) * sc, rz = (float)(z - h.cen[2]) * sc;
         const int ox = (int)floorf(rx + 0.5f), oy = (int)floorf(ry + 0.5f), oz = (int)floorf(rz + 0.5f);
         if (ox == 0 && oy == 0 && oz == 0) {
             Loc r = h;
@@ -153,7 +197,20 @@ __device__ __forceinline__ Loc locate_near(const DevTree& T, const Loc& h, doubl
             }
         }
     }
-    return locate_full(T, x, y, z);
+    return locate_full(T, pos.px(), pos.py(), pos.pz());
+}
+
+// Deepest cell of a point given by float64 coordinates near a located cell:
+// the offset from the cell's centre is formed in float64 (one subtraction per
+// axis) and rounded to FP32 cell units.
+__device__ __forceinline__ Loc locate_near(const DevTree& T, const Loc& h, double x, double y, double z)
+{
+    float rx = 0.f, ry = 0.f, rz = 0.f;
+    if (h.cell >= 0) {
+        const float sc = cells_per_unit(h.level);
+        rx = (float)(x - h.cen[0]) * sc; ry = (float)(y - h.cen[1]) * sc; rz = (float)(z - h.cen[2]) * sc;
+    }
+    return locate_rel(T, h, rx, ry, rz, PosAt{x, y, z});
 }
 
 // The point one cell away from a located point along an axis: same in-cell
@@ -182,8 +239,8 @@ __device__ __forceinline__ Loc step_cell(const DevTree& T, const Loc& h, int axi
 // TSC at a point whose deepest cell is `cell` (simplehyperoctree.h:1479-1541
 // through the stencil records).  Returns false when a restart centre is not
 // itself a cell (left to the slow path).
-__device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, double x, double y, double z, bool need_all,
-                                        Field7& res)
+template <class P>
+__device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P& pos, bool need_all, Field7& res)
 {
     int cell = d.cell, L = d.level;
     float fd[3] = {d.fd[0], d.fd[1], d.fd[2]};
@@ -224,6 +281,7 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, double x
             return true;
         }
         const int lc = rec_flags(T, e) & 255;
+        const double x = pos.px(), y = pos.py(), z = pos.pz();
         const Found f = find_cell(T, lc, axis_coord(lc, x), axis_coord(lc, y), axis_coord(lc, z));
         if (f.cell < 0 || f.level != lc) return false;
         cell = f.cell;
@@ -235,8 +293,8 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, double x
 }
 
 // CIC at a point whose deepest cell is `cell` (simplehyperoctree.h:1410-1469).
-__device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, double x, double y, double z, bool need_all,
-                                        Field7& res)
+template <class P>
+__device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, const P& pos, bool need_all, Field7& res)
 {
     int cell = d.cell, L = d.level;
     float fd[3] = {d.fd[0], d.fd[1], d.fd[2]};
@@ -268,6 +326,7 @@ __device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, double x
             else res = Field7{rho, phi, gx, gy, gz, a, gt};
             return true;
         }
+        const double x = pos.px(), y = pos.py(), z = pos.pz();
         const Found f = find_cell(T, lvl, axis_coord(lvl, x), axis_coord(lvl, y), axis_coord(lvl, z));
         if (f.cell < 0 || f.level != lvl) return false;
         cell = f.cell;
@@ -280,8 +339,8 @@ __device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, double x
 
 // maybe_origin: the point can be the exact origin (first step of a ray),
 // where the reference's TSC falls back to CIC (simplehyperoctree.h:1570-1571)
-template <int ORDER>
-__device__ __forceinline__ Field7 gather_at(const DevTree& T, const Loc& d, double x, double y, double z, bool need_all,
+template <int ORDER, class P>
+__device__ __forceinline__ Field7 gather_at(const DevTree& T, const Loc& d, const P& pos, bool need_all,
                                             unsigned long long* st, int slot, bool maybe_origin)
 {
     constexpr int order = ORDER;
@@ -291,15 +350,16 @@ __device__ __forceinline__ Field7 gather_at(const DevTree& T, const Loc& d, doub
         stat(st, slot);
         return r;
     }
-    if (!(maybe_origin && x == 0.0 && y == 0.0 && z == 0.0)) {
-        const bool ok = (order == 1) ? cic_rec(T, d, x, y, z, need_all, r) : tsc_rec(T, d, x, y, z, need_all, r);
+    if (!(maybe_origin && pos.px() == 0.0 && pos.py() == 0.0 && pos.pz() == 0.0)) {
+        const bool ok = (order == 1) ? cic_rec(T, d, pos, need_all, r) : tsc_rec(T, d, pos, need_all, r);
         if (ok) {
             stat(st, slot);
             return r;
         }
     }
     stat(st, slot + 1);
-    return (order == 1) ? cic_slow(T, x, y, z, need_all) : tsc_slow(T, x, y, z, need_all);
+    return (order == 1) ? cic_slow(T, pos.px(), pos.py(), pos.pz(), need_all)
+                        : tsc_slow(T, pos.px(), pos.py(), pos.pz(), need_all);
 }
 
 struct FastRec {
@@ -331,18 +391,22 @@ __device__ __forceinline__ double recip(double a)
 //    of k and the positions keep float64 accuracy;
 //  * dx/dlambda is returned as k itself: the caller folds 1/scale into the
 //    RK coefficient (one multiplication per stage instead of three).
-__device__ __forceinline__ void rhs_math(const DevCosmo& C, const Field7& g, const double* in, double* out)
+// inv_a = 1 / in[0]; tb = the cosmology bracket carried along the ray.
+// kf: k^1..k^3 rounded to FP32 (the next stage's point offset in cell units).
+__device__ __forceinline__ void rhs_math(const DevCosmo& C, const Field7& g, const double* in, double inv_a, int& tb,
+                                         double* out, float* kf)
 {
     const double c2 = kC * kC;
     const float k0f = (float)in[5], k1f = (float)in[6], k2f = (float)in[7], k3f = (float)in[8];
+    kf[0] = k1f; kf[1] = k2f; kf[2] = k3f;
     const float dphidl = g.dt * k0f + (g.dx * k1f + g.dy * k2f + g.dz * k3f);
-    const double dadt = interp_fast(C, in[1], C.dadt, C.slope_dadt);
+    const double dadt = interp_cached(C, in[1], C.dadt, C.slope_dadt, tb);
     out[0] = in[5] * dadt;
     out[1] = in[5];
     out[2] = in[6];
     out[3] = in[7];
     out[4] = in[8];
-    const double hub = 2.0 * out[0] * recip(in[0]);
+    const double hub = 2.0 * out[0] * inv_a;
     const float two_c2 = (float)(2.0 / c2);
     const float k02 = 2.0f * k0f * k0f;
     out[5] = -(hub * in[5]) - (double)((two_c2 * k0f) * (dphidl - g.dt * k0f));
@@ -367,7 +431,7 @@ __device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, doub
         const double moved = ((ax == 0) ? x : (ax == 1) ? y : z) + ((a & 1) ? h : -h);
         const double qx = (ax == 0) ? moved : x, qy = (ax == 1) ? moved : y, qz = (ax == 2) ? moved : z;
         const Loc d = step_cell(T, here, ax, sgn, qx, qy, qz);
-        const Field7 f = gather_at<2>(T, d, qx, qy, qz, false, st, ST_JAC_REC, false);
+        const Field7 f = gather_at<2>(T, d, PosAt{qx, qy, qz}, false, st, ST_JAC_REC, false);
         g[a][0] = f.dx; g[a][1] = f.dy; g[a][2] = f.dz;
     }
     const float idl = __int_as_float((127 + here.level - kLevelShift - 1) << 23);   // 1 / dl, exact
@@ -409,7 +473,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
     }
     Loc here = locate_full(T, b.x, b.y, b.z);
-    Field7 data = gather_at<ORDER>(T, here, b.x, b.y, b.z, true, st, ST_POST_REC, true);
+    Field7 data = gather_at<ORDER>(T, here, PosAt{b.x, b.y, b.z}, true, st, ST_POST_REC, true);
     {
         const double ph = (double)data.phi / c2;
         const double norm = sqrt((c2 * (1.0 + 2.0 * ph) * b.k0 * b.k0) / ((1.0 - 2.0 * ph) * (b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3)));
@@ -424,6 +488,8 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     double ratio = b.a * b.a * ratio_k;
     double dl = (here.cell >= 0 ? cell_extent(here.level) : 0.0) * ratio;
     const double a0 = b.a;
+    double inv_a = recip(b.a);          // 1 / a at b (stage 1 of the next step)
+    int tb = bracket_lut(C, b.t);       // cosmology-table bracket of the ray's conformal time
     const double phi0c2 = b.phi / c2;
     float last_data_dt = data.dt;
     float last_dphi = 0.f;
@@ -459,24 +525,33 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         // stages: core = b + c_s dl * d_{s-1};  acc = d0 + 2 d1 + 2 d2 + d3 (in that order)
         // stage 1 is at b, where the previous step's post-step gather already
         // read the field (data); stages 2-4 gather at their own points
+        // The stage points b + pc k are located and gathered from their FP32
+        // offset to b's cell (pc k is a fraction of a cell); their float64
+        // coordinates are formed only on the rare full-walk / restart paths.
+        float kfs[3];
+        double pk[3] = {0.0, 0.0, 0.0}, pc = 0.0;
 #pragma unroll 1
         for (int sg = 0; sg < 4; ++sg) {
             if (sg == 0) {
-                rhs_math(C, data, bc, dc);
+                rhs_math(C, data, bc, inv_a, tb, dc, kfs);
             } else {
-                const Loc d = locate_near(T, here, core[2], core[3], core[4]);
-                const Field7 g = gather_at<ORDER>(T, d, core[2], core[3], core[4], false, st, ST_RK_REC, false);
-                rhs_math(C, g, core, dc);
+                const float cc = (float)pc * cells_per_unit(here.level);
+                const PosStage ps{bc[2], bc[3], bc[4], pc, pk[0], pk[1], pk[2]};
+                const Loc d = locate_rel(T, here, fmaf(cc, kfs[0], here.fd[0]), fmaf(cc, kfs[1], here.fd[1]),
+                                         fmaf(cc, kfs[2], here.fd[2]), ps);
+                const Field7 g = gather_at<ORDER>(T, d, ps, false, st, ST_RK_REC, false);
+                rhs_math(C, g, core, recip(core[0]), tb, dc, kfs);
             }
             const double cs = (sg < 2) ? 0.5 * dl : dl;
-            const double csp = cs * inv_scale;   // positions: dx/dl = k / scale
             const double wa = (sg == 0) ? 0.0 : 2.0;
             if (sg < 3) {
 #pragma unroll
                 for (int q = 0; q < 9; ++q) {
                     acc[q] = (sg == 0) ? dc[q] : acc[q] + wa * dc[q];
-                    core[q] = bc[q] + ((q >= 2 && q <= 4) ? csp : cs) * dc[q];
+                    if (q < 2 || q > 4) core[q] = bc[q] + cs * dc[q];
                 }
+                pc = cs * inv_scale;   // positions: dx/dl = k / scale
+                pk[0] = dc[2]; pk[1] = dc[3]; pk[2] = dc[4];
             }
         }
         const double dl6 = dl * (1.0 / 6.0);
@@ -486,8 +561,17 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         p.a = core[0]; p.t = core[1]; p.x = core[2]; p.y = core[3]; p.z = core[4];
         p.k0 = core[5]; p.k1 = core[6]; p.k2 = core[7]; p.k3 = core[8];
         const Loc ploc = locate_near(T, here, p.x, p.y, p.z);
-        data = gather_at<ORDER>(T, ploc, p.x, p.y, p.z, true, st, ST_POST_REC, false);
-        if (!(!(p.a < 0.0) && ((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx)))) clear(data);
+        data = gather_at<ORDER>(T, ploc, PosAt{p.x, p.y, p.z}, true, st, ST_POST_REC, false);
+        {
+            // the extent test (integrator.h:757): a point in a located cell away from
+            // the domain faces is inside; only cells on a face (or wrapped keys)
+            // need the float64 comparison
+            const uint32_t last = (ploc.cell >= 0) ? (uint32_t)((1ull << ploc.level) - 1ull) : 0u;
+            const bool face = (ploc.cell < 0) || ploc.c[0] == 0u || ploc.c[1] == 0u || ploc.c[2] == 0u ||
+                              ploc.c[0] >= last || ploc.c[1] >= last || ploc.c[2] >= last;
+            if (p.a < 0.0 || (face && !((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx))))
+                clear(data);
+        }
         p.level = (ploc.cell >= 0) ? ploc.level : 0;
         p.ah = data.a;
         p.rho = data.rho; p.phi = data.phi; p.dx = data.dx; p.dy = data.dy; p.dz = data.dz;
@@ -503,7 +587,8 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         p.chi = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
         lambda += dl;
         sacc += (double)sqrtf((float)((p.x - b.x) * (p.x - b.x) + (p.y - b.y) * (p.y - b.y) + (p.z - b.z) * (p.z - b.z)));
-        p.red = a0 * recip(p.a) * (1.0 + phi0c2 - p.phi * (1.0 / c2)) - 1.0;
+        const double inv_pa = recip(p.a);
+        p.red = a0 * inv_pa * (1.0 + phi0c2 - p.phi * (1.0 / c2)) - 1.0;
         p.isw = isw; p.iswold = iswold; p.lambda = lambda; p.s = sacc;
         if (!is_empty(data)) {
             ratio = p.a * p.a * ratio_k;
@@ -597,6 +682,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             if (!have_rmax || rmax < (double)b.rho) rmax = b.rho;
             have_rmax = true;
             b = p;
+            inv_a = inv_pa;
         }
         bool stop;
         switch (skind) {
@@ -703,8 +789,8 @@ __global__ void k_gather_rec(DevTree T, int kind, const double* __restrict__ xyz
         ((long long*)out)[i] = d.cell;
         return;
     }
-    const Field7 f = (kind == 1) ? gather_at<1>(T, d, x, y, z, true, nullptr, 0, true)
-                                 : gather_at<2>(T, d, x, y, z, true, nullptr, 0, true);
+    const Field7 f = (kind == 1) ? gather_at<1>(T, d, PosAt{x, y, z}, true, nullptr, 0, true)
+                                 : gather_at<2>(T, d, PosAt{x, y, z}, true, nullptr, 0, true);
     float* o = (float*)out + 7 * i;
     o[0] = f.rho; o[1] = f.phi; o[2] = f.dx; o[3] = f.dy; o[4] = f.dz; o[5] = f.a; o[6] = f.dt;
 }
