@@ -24,6 +24,19 @@ namespace mpf {
 
 constexpr unsigned kFullMask = (1u << 27) - 1u;
 
+// Launch shape of the persistent kernel: threads per block and the minimum
+// resident blocks per SM promised to the register allocator.  128 x 2 (up to
+// 255 registers, 8 warps per SM) measured fastest on the AMR and medium
+// octrees, ahead of 128 x 3 (168 registers, spills) and 128 x 4.
+// Overridable at build time for tuning sweeps.
+#ifndef MPF_FAST_THREADS
+#define MPF_FAST_THREADS 128
+#endif
+#ifndef MPF_FAST_MINB
+#define MPF_FAST_MINB 2
+#endif
+constexpr int kFastThreads = MPF_FAST_THREADS;
+
 // Utility::interpolate with the uniform index table (same bracketing interval
 // as the reference's upper_bound; slope precomputed per interval).
 __device__ __forceinline__ double interp_fast(const DevCosmo& C, double x0, const double* __restrict__ y,
@@ -449,9 +462,20 @@ __device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, doub
               cp * s2t * dxz;
 }
 
+// Per-thread Jacobian running sums kept in shared memory (touched once per
+// step, so they need not occupy 36 registers through the gathers): S (6), the
+// last point's contribution c_k (6) and the one before it c_km1 (6), strided
+// by the block size.
+struct JacSums {
+    double* base;   // this thread's slot 0
+    __device__ __forceinline__ double& S(int q) const { return base[q * kFastThreads]; }
+    __device__ __forceinline__ double& ck(int q) const { return base[(6 + q) * kFastThreads]; }
+    __device__ __forceinline__ double& ckm1(int q) const { return base[(12 + q) * kFastThreads]; }
+};
+
 template <int ORDER, bool SRC>
 __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* L, long long i,
-                               const PropOut& O)
+                               const PropOut& O, JacSums J)
 {
     const double c2 = kC * kC;
     const double mn = -(double)kExtent / 2.0, mx = (double)kExtent / 2.0;
@@ -512,7 +536,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     }
     double rmax = 0.0;
     bool have_rmax = false;
-    double S[6] = {0, 0, 0, 0, 0, 0}, c_k[6] = {0, 0, 0, 0, 0, 0}, c_km1[6] = {0, 0, 0, 0, 0, 0};
+    for (int q = 0; q < 6; ++q) { J.S(q) = 0.0; J.ck(q) = 0.0; J.ckm1(q) = 0.0; }
     double chim1 = 0.0, chim2 = 0.0;
     long long k = 0;
     unsigned status = 0;
@@ -607,12 +631,13 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                 chim2 = chim1; chim1 = b.chi;
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
-                    c_km1[q] = c_k[q]; c_km1[3 + q] = c_k[3 + q];
+                    J.ckm1(q) = J.ck(q); J.ckm1(3 + q) = J.ck(3 + q);
                     const double hd = (double)h3[q] * dr;
-                    c_k[q] = p.chi * hd;
-                    c_k[3 + q] = p.chi * p.chi * hd;
-                    S[q] += c_k[q];
-                    S[3 + q] += c_k[3 + q];
+                    const double c1 = p.chi * hd, c2v = p.chi * p.chi * hd;
+                    J.ck(q) = c1;
+                    J.ck(3 + q) = c2v;
+                    J.S(q) += c1;
+                    J.S(3 + q) += c2v;
                 }
             }
             while (next_plane < np) {
@@ -654,13 +679,13 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                         double s1[3], s2[3];
                         bool ok = true;
                         if (p.chi <= jd) {
-                            for (int q = 0; q < 3; ++q) { s1[q] = S[q]; s2[q] = S[3 + q]; }
+                            for (int q = 0; q < 3; ++q) { s1[q] = J.S(q); s2[q] = J.S(3 + q); }
                         } else if (chim1 <= jd) {
-                            for (int q = 0; q < 3; ++q) { s1[q] = S[q] - c_k[q]; s2[q] = S[3 + q] - c_k[3 + q]; }
+                            for (int q = 0; q < 3; ++q) { s1[q] = J.S(q) - J.ck(q); s2[q] = J.S(3 + q) - J.ck(3 + q); }
                         } else if (k >= 2 && chim2 <= jd) {
                             for (int q = 0; q < 3; ++q) {
-                                s1[q] = S[q] - c_k[q] - c_km1[q];
-                                s2[q] = S[3 + q] - c_k[3 + q] - c_km1[3 + q];
+                                s1[q] = J.S(q) - J.ck(q) - J.ckm1(q);
+                                s2[q] = J.S(3 + q) - J.ck(3 + q) - J.ckm1(3 + q);
                             }
                         } else {
                             ok = false;
@@ -745,18 +770,6 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     if (status) atomicOr(O.status, status);
 }
 
-// Launch shape of the persistent kernel: threads per block and the minimum
-// resident blocks per SM promised to the register allocator.  128 x 2 (up to
-// 255 registers, 8 warps per SM) measured fastest on the AMR and medium
-// octrees, ahead of 128 x 3 (168 registers, spills) and 128 x 4.
-// Overridable at build time for tuning sweeps.
-#ifndef MPF_FAST_THREADS
-#define MPF_FAST_THREADS 128
-#endif
-#ifndef MPF_FAST_MINB
-#define MPF_FAST_MINB 2
-#endif
-constexpr int kFastThreads = MPF_FAST_THREADS;
 
 // Persistent launch: each warp takes the next 32 rays from a global counter
 // until the batch is exhausted, so uneven path lengths do not leave tail
@@ -766,6 +779,8 @@ __global__ void __launch_bounds__(kFastThreads, MPF_FAST_MINB) k_propagate_fast(
                                                                     const double* __restrict__ launch, long long n, PropOut O,
                                                                     unsigned long long* queue)
 {
+    __shared__ double jac_sh[18 * kFastThreads];
+    const JacSums J{jac_sh + threadIdx.x};
     const int lane = threadIdx.x & 31;
     for (;;) {
         unsigned long long base = 0;
@@ -773,7 +788,7 @@ __global__ void __launch_bounds__(kFastThreads, MPF_FAST_MINB) k_propagate_fast(
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= (unsigned long long)n) break;
         const long long i = (long long)base + lane;
-        if (i < n) propagate_fast<ORDER, SRC>(T, C, P, launch + 6 * i, i, O);
+        if (i < n) propagate_fast<ORDER, SRC>(T, C, P, launch + 6 * i, i, O, J);
         __syncwarp();
     }
 }
