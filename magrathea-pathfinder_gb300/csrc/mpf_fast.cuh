@@ -35,6 +35,11 @@ constexpr unsigned kFullMask = (1u << 27) - 1u;
 #ifndef MPF_FAST_MINB
 #define MPF_FAST_MINB 2
 #endif
+// 1: the TSC gather runs as a loop over three x-slabs (smaller code, fewer
+// registers); 0: fully unrolled over the 27 cells.
+#ifndef MPF_TSC_SLABS
+#define MPF_TSC_SLABS 0
+#endif
 constexpr int kFastThreads = MPF_FAST_THREADS;
 
 // Utility::interpolate with the uniform index table (same bracketing interval
@@ -262,17 +267,37 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
         const int4 r7 = __ldg(rp + 7);
         const unsigned exact = (unsigned)r7.x;
         if (exact == kFullMask) {
+            float wx[3], wy[3], wz[3];
+            tsc_w3(fd[0], wx);
+            tsc_w3(fd[1], wy);
+            tsc_w3(fd[2], wz);
+            float gx = 0.f, gy = 0.f, gz = 0.f, gt = 0.f, rho = 0.f, phi = 0.f, a = 0.f;
+#if MPF_TSC_SLABS
+            // three x-slabs of 9 cells, one loop body: a third of the code and
+            // of the loads in flight (the accumulation order is unchanged)
+            const int* re = reinterpret_cast<const int*>(rp);
+#pragma unroll 1
+            for (int sx = 0; sx < 3; ++sx) {
+                const float wxs = (sx == 0) ? wx[0] : (sx == 1) ? wx[1] : wx[2];
+#pragma unroll
+                for (int jj = 0; jj < 9; ++jj) {
+                    const int ej = __ldg(re + 9 * sx + jj);
+                    const float wt = wxs * wy[jj / 3] * wz[jj % 3];
+                    const float4 g = __ldg(T.grad + ej);
+                    gx = fmaf(g.x, wt, gx); gy = fmaf(g.y, wt, gy); gz = fmaf(g.z, wt, gz); gt = fmaf(g.w, wt, gt);
+                    if (need_all) {
+                        const float4 s = __ldg(T.scal + ej);
+                        rho = fmaf(s.x, wt, rho); phi = fmaf(s.y, wt, phi); a = fmaf(s.z, wt, a);
+                    }
+                }
+            }
+#else
             int e[28];
 #pragma unroll
             for (int q = 0; q < 7; ++q) {
                 const int4 v = __ldg(rp + q);
                 e[4 * q] = v.x; e[4 * q + 1] = v.y; e[4 * q + 2] = v.z; e[4 * q + 3] = v.w;
             }
-            float wx[3], wy[3], wz[3];
-            tsc_w3(fd[0], wx);
-            tsc_w3(fd[1], wy);
-            tsc_w3(fd[2], wz);
-            float gx = 0.f, gy = 0.f, gz = 0.f, gt = 0.f, rho = 0.f, phi = 0.f, a = 0.f;
 #pragma unroll
             for (int j = 0; j < 27; ++j) {
                 const float wt = wx[j / 9] * wy[(j / 3) % 3] * wz[j % 3];
@@ -283,6 +308,7 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
                     rho = fmaf(s.x, wt, rho); phi = fmaf(s.y, wt, phi); a = fmaf(s.z, wt, a);
                 }
             }
+#endif
             res = Field7{rho, phi, gx, gy, gz, a, gt};
             return true;
         }
