@@ -499,13 +499,6 @@ struct JacSums {
     __device__ __forceinline__ double& ckm1(int q) const { return base[(12 + q) * kFastThreads]; }
 };
 
-// Per-thread step index at which the ray crossed each surface, in shared
-// memory (dynamically indexed, so it would otherwise live in local memory).
-struct CrossK {
-    int* base;   // this thread's slot 0
-    __device__ __forceinline__ int& operator[](int j) const { return base[j * kFastThreads]; }
-};
-
 // Constants of a launch (formed once per thread: a float64 division is a
 // long FP64-pipe sequence on this GPU).
 struct FastK {
@@ -530,10 +523,10 @@ struct FastRay {
     int tb, next_plane;
     unsigned status;
     bool have_rmax;
-    CrossK cross_k;
+    long long cross_k[kMaxPlanes];
 
     __device__ __forceinline__ void start(const DevTree& T, const DevCosmo& C, const PropParams& P, const FastK& K,
-                                          const double* L, long long ray, const PropOut& O, JacSums J, CrossK X)
+                                          const double* L, long long ray, const PropOut& O, JacSums J)
     {
         const double c2 = kC * kC;
         const double mn = -(double)kExtent / 2.0, mx = (double)kExtent / 2.0;
@@ -544,7 +537,6 @@ struct FastRay {
         unsigned long long* const st = O.stats;
         (void)mn; (void)mx; (void)scale; (void)rec_fields; (void)st; (void)np; (void)skind;
         i = ray;
-        cross_k = X;
         stop_ref = SRC ? P.ray_stop[i] : P.stop_ref;
         if (SRC) {
             // (phi, theta) launch form: the direction is given
@@ -719,7 +711,7 @@ struct FastRay {
                     const double ref = SRC ? stop_ref : P.planes[next_plane];
                     if (!((kind == STOP_A) ? (q1 < ref) : (q1 > ref))) break;
                     const int j = next_plane++;
-                    cross_k[j] = (int)k;
+                    cross_k[j] = k;
                     if (prow) {
                         double* o = prow + j * rec_fields;
                         const double q0 = (kind == STOP_R) ? b.chi : (kind == STOP_LAMBDA) ? b.lambda : (kind == STOP_T) ? b.t
@@ -823,7 +815,7 @@ struct FastRay {
             }
         }
         if (SRC && prow) {
-            const long long ck = (long long)cross_k[0];
+            const long long ck = cross_k[0];
             const bool ok = (ck >= 1) && (ck < size);
             if (!ok) {
                 for (int q = 0; q < 24; ++q) prow[q] = 0.0;
@@ -834,7 +826,7 @@ struct FastRay {
         } else if (prow) {
             for (int j = 0; j < np; ++j) {
                 double* o = prow + j * kPlaneFields;
-                const long long ck = (long long)cross_k[j];
+                const long long ck = cross_k[j];
                 const bool found = (ck >= 1) && (ck < size);
                 const bool valid = found && !((ck - 1) == size - 1 || (ck - 1) == 0);
                 if (ck < 0 || ck == 0 || ck >= size) {
@@ -862,9 +854,7 @@ __global__ void __launch_bounds__(kFastThreads, MPF_FAST_MINB) k_propagate_fast(
                                                                     unsigned long long* queue)
 {
     __shared__ double jac_sh[18 * kFastThreads];
-    __shared__ int cross_sh[kMaxPlanes * kFastThreads];
     const JacSums J{jac_sh + threadIdx.x};
-    const CrossK X{cross_sh + threadIdx.x};
     const FastK K{1.0 / P.length, (P.length / kC) / P.nsteps};
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -880,7 +870,7 @@ __global__ void __launch_bounds__(kFastThreads, MPF_FAST_MINB) k_propagate_fast(
             if (!active && !exhausted) {
                 const long long i = (long long)base + __popc(need & ((1u << lane) - 1u));
                 if (i < n) {
-                    r.start(T, C, P, K, launch + 6 * i, i, O, J, X);
+                    r.start(T, C, P, K, launch + 6 * i, i, O, J);
                     active = true;
                 } else {
                     exhausted = true;
