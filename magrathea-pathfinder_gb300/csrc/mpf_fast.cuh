@@ -499,355 +499,307 @@ struct JacSums {
     __device__ __forceinline__ double& ckm1(int q) const { return base[(12 + q) * kFastThreads]; }
 };
 
-// Constants of a launch (formed once per thread: a float64 division is a
-// long FP64-pipe sequence on this GPU).
-struct FastK {
-    double inv_scale;   // 1 / length
-    double ratio_k;     // (length / c) / nsteps
-};
-
-// One ray of the fast kernel as a resumable state machine: start() launches
-// it, advance() takes one RK4 step (false when the ray has ended) and
-// finish() writes its records.  The persistent kernel calls advance() once
-// per loop iteration for every lane, so a lane whose ray ends takes a new ray
-// at once instead of idling until the longest ray of its warp is done.
 template <int ORDER, bool SRC>
-struct FastRay {
+__device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* L, long long i,
+                               const PropOut& O, JacSums J)
+{
+    const double c2 = kC * kC;
+    const double mn = -(double)kExtent / 2.0, mx = (double)kExtent / 2.0;
+    const double scale = P.length;
+    const double inv_scale = 1.0 / scale;
+    const int np = SRC ? 1 : P.nplanes;
+    const int skind = SRC ? (int)STOP_R : P.stop_kind;
+    const double stop_ref = SRC ? P.ray_stop[i] : P.stop_ref;
+    const int rec_fields = SRC ? kSourceFields : kPlaneFields;
+    unsigned long long* const st = O.stats;
     FastRec b;
-    Loc here;
-    Field7 data;
-    double dl, ratio, a0, phi0c2, inv_a, stop_ref, rmax, chim1, chim2, isw, iswold, lambda, sacc, last_dl;
-    double* prow;
-    long long i, k;
-    float last_data_dt, last_dphi;
-    int tb, next_plane;
-    unsigned status;
-    bool have_rmax;
-    long long cross_k[kMaxPlanes];
-
-    __device__ __forceinline__ void start(const DevTree& T, const DevCosmo& C, const PropParams& P, const FastK& K,
-                                          const double* L, long long ray, const PropOut& O, JacSums J)
-    {
-        const double c2 = kC * kC;
-        const double mn = -(double)kExtent / 2.0, mx = (double)kExtent / 2.0;
-        const double scale = P.length;
-        const int np = SRC ? 1 : P.nplanes;
-        const int skind = SRC ? (int)STOP_R : P.stop_kind;
-        const int rec_fields = SRC ? kSourceFields : kPlaneFields;
-        unsigned long long* const st = O.stats;
-        (void)mn; (void)mx; (void)scale; (void)rec_fields; (void)st; (void)np; (void)skind;
-        i = ray;
-        stop_ref = SRC ? P.ray_stop[i] : P.stop_ref;
-        if (SRC) {
-            // (phi, theta) launch form: the direction is given
-            b.a = 1.0; b.t = 0.0; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = 1.0;
-            b.k1 = L[3]; b.k2 = L[4]; b.k3 = L[5];
-        } else {
-            const double norm = sqrt((L[3] - L[0]) * (L[3] - L[0]) + (L[4] - L[1]) * (L[4] - L[1]) + (L[5] - L[2]) * (L[5] - L[2]));
-            b.a = 1.0; b.t = 0.0; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = 1.0;
-            b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
-        }
-        here = locate_full(T, b.x, b.y, b.z);
-        data = gather_at<ORDER>(T, here, PosAt{b.x, b.y, b.z}, true, st, ST_POST_REC, true);
-        {
-            const double ph = (double)data.phi / c2;
-            const double norm = sqrt((c2 * (1.0 + 2.0 * ph) * b.k0 * b.k0) / ((1.0 - 2.0 * ph) * (b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3)));
-            b.k1 *= norm; b.k2 *= norm; b.k3 *= norm;
-        }
-        b.a = interp_fast(C, b.t, C.a, C.slope_a);
-        b.level = (here.cell >= 0) ? here.level : 0;
-        b.ah = 0.f;
-        b.rho = data.rho; b.phi = data.phi; b.dx = data.dx; b.dy = data.dy; b.dz = data.dz; b.dt = data.dt;
-        b.red = 0.0; b.isw = 0.0; b.chi = 0.0; b.iswold = 0.0; b.lambda = 0.0; b.s = 0.0;
-        ratio = b.a * b.a * K.ratio_k;
-        dl = (here.cell >= 0 ? cell_extent(here.level) : 0.0) * ratio;
-        a0 = b.a;
-        inv_a = recip(b.a);          // 1 / a at b (stage 1 of the next step)
-        tb = bracket_lut(C, b.t);       // cosmology-table bracket of the ray's conformal time
-        phi0c2 = b.phi / c2;
-        last_data_dt = data.dt;
-        last_dphi = 0.f;
-        last_dl = 1.0;
-
-        next_plane = 0;
-        for (int j = 0; j < np; ++j) cross_k[j] = -1;
-        prow = O.plane_rec ? O.plane_rec + (long long)i * np * rec_fields : nullptr;
-        if (SRC && prow) {
-            prow[24] = b.a; prow[25] = b.phi; prow[26] = b.k1; prow[27] = b.k2; prow[28] = b.k3;
-            prow[29] = prow[30] = prow[31] = 0.0;
-        }
-        while (next_plane < np && ((skind == STOP_A) ? (b.a < (SRC ? stop_ref : P.planes[next_plane]))
-                                                      : (((skind == STOP_R) ? b.chi : (skind == STOP_LAMBDA) ? b.lambda
-                                                          : (skind == STOP_T) ? b.t : (skind == STOP_S) ? b.s : b.red) >
-                                                         (SRC ? stop_ref : P.planes[next_plane])))) {
-            cross_k[next_plane] = 0;
-            ++next_plane;
-        }
-        rmax = 0.0;
-        have_rmax = false;
-        for (int q = 0; q < 6; ++q) { J.S(q) = 0.0; J.ck(q) = 0.0; J.ckm1(q) = 0.0; }
-        chim1 = 0.0; chim2 = 0.0;
-        k = 0;
-        status = 0;
-        isw = 0.0; iswold = 0.0; lambda = 0.0; sacc = 0.0;
+    if (SRC) {
+        // (phi, theta) launch form: the direction is given
+        b.a = 1.0; b.t = 0.0; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = 1.0;
+        b.k1 = L[3]; b.k2 = L[4]; b.k3 = L[5];
+    } else {
+        const double norm = sqrt((L[3] - L[0]) * (L[3] - L[0]) + (L[4] - L[1]) * (L[4] - L[1]) + (L[5] - L[2]) * (L[5] - L[2]));
+        b.a = 1.0; b.t = 0.0; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = 1.0;
+        b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
     }
-
-    // One RK4 step of the ray (the loop body of integrator.h:713-812);
-    // false when the ray has ended.
-    __device__ __forceinline__ bool advance(const DevTree& T, const DevCosmo& C, const PropParams& P, const FastK& K,
-                                            const PropOut& O, JacSums J)
+    Loc here = locate_full(T, b.x, b.y, b.z);
+    Field7 data = gather_at<ORDER>(T, here, PosAt{b.x, b.y, b.z}, true, st, ST_POST_REC, true);
     {
-        const double c2 = kC * kC;
-        const double mn = -(double)kExtent / 2.0, mx = (double)kExtent / 2.0;
-        const double scale = P.length;
-        const int np = SRC ? 1 : P.nplanes;
-        const int skind = SRC ? (int)STOP_R : P.stop_kind;
-        const int rec_fields = SRC ? kSourceFields : kPlaneFields;
-        unsigned long long* const st = O.stats;
-        (void)mn; (void)mx; (void)scale; (void)rec_fields; (void)st; (void)np; (void)skind;
-        if (is_empty(data)) return false;
-        if (k >= P.max_steps) { status |= 1u; return false; }
-        double core[9], dc[9], acc[9];
-        FastRec p;
-            const double bc[9] = {b.a, b.t, b.x, b.y, b.z, b.k0, b.k1, b.k2, b.k3};
-            // stages: core = b + c_s dl * d_{s-1};  acc = d0 + 2 d1 + 2 d2 + d3 (in that order)
-            // stage 1 is at b, where the previous step's post-step gather already
-            // read the field (data); stages 2-4 gather at their own points
-            // The stage points b + pc k are located and gathered from their FP32
-            // offset to b's cell (pc k is a fraction of a cell); their float64
-            // coordinates are formed only on the rare full-walk / restart paths.
-            float kfs[3];
-            double pk[3] = {0.0, 0.0, 0.0}, pc = 0.0;
-    #pragma unroll 1
-            for (int sg = 0; sg < 4; ++sg) {
-                if (sg == 0) {
-                    rhs_math(C, data, bc, inv_a, tb, dc, kfs);
-                } else {
-                    const float cc = (float)pc * cells_per_unit(here.level);
-                    const PosStage ps{bc[2], bc[3], bc[4], pc, pk[0], pk[1], pk[2]};
-                    const Loc d = locate_rel(T, here, fmaf(cc, kfs[0], here.fd[0]), fmaf(cc, kfs[1], here.fd[1]),
-                                             fmaf(cc, kfs[2], here.fd[2]), ps);
-                    const Field7 g = gather_at<ORDER>(T, d, ps, false, st, ST_RK_REC, false);
-                    rhs_math(C, g, core, recip(core[0]), tb, dc, kfs);
+        const double ph = (double)data.phi / c2;
+        const double norm = sqrt((c2 * (1.0 + 2.0 * ph) * b.k0 * b.k0) / ((1.0 - 2.0 * ph) * (b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3)));
+        b.k1 *= norm; b.k2 *= norm; b.k3 *= norm;
+    }
+    b.a = interp_fast(C, b.t, C.a, C.slope_a);
+    b.level = (here.cell >= 0) ? here.level : 0;
+    b.ah = 0.f;
+    b.rho = data.rho; b.phi = data.phi; b.dx = data.dx; b.dy = data.dy; b.dz = data.dz; b.dt = data.dt;
+    b.red = 0.0; b.isw = 0.0; b.chi = 0.0; b.iswold = 0.0; b.lambda = 0.0; b.s = 0.0;
+    const double ratio_k = (scale / kC) / P.nsteps;
+    double ratio = b.a * b.a * ratio_k;
+    double dl = (here.cell >= 0 ? cell_extent(here.level) : 0.0) * ratio;
+    const double a0 = b.a;
+    double inv_a = recip(b.a);          // 1 / a at b (stage 1 of the next step)
+    int tb = bracket_lut(C, b.t);       // cosmology-table bracket of the ray's conformal time
+    const double phi0c2 = b.phi / c2;
+    float last_data_dt = data.dt;
+    float last_dphi = 0.f;
+    double last_dl = 1.0;
+
+    int next_plane = 0;
+    long long cross_k[kMaxPlanes];
+    for (int j = 0; j < np; ++j) cross_k[j] = -1;
+    double* prow = O.plane_rec ? O.plane_rec + (long long)i * np * rec_fields : nullptr;
+    if (SRC && prow) {
+        prow[24] = b.a; prow[25] = b.phi; prow[26] = b.k1; prow[27] = b.k2; prow[28] = b.k3;
+        prow[29] = prow[30] = prow[31] = 0.0;
+    }
+    while (next_plane < np && ((skind == STOP_A) ? (b.a < (SRC ? stop_ref : P.planes[next_plane]))
+                                                  : (((skind == STOP_R) ? b.chi : (skind == STOP_LAMBDA) ? b.lambda
+                                                      : (skind == STOP_T) ? b.t : (skind == STOP_S) ? b.s : b.red) >
+                                                     (SRC ? stop_ref : P.planes[next_plane])))) {
+        cross_k[next_plane] = 0;
+        ++next_plane;
+    }
+    double rmax = 0.0;
+    bool have_rmax = false;
+    for (int q = 0; q < 6; ++q) { J.S(q) = 0.0; J.ck(q) = 0.0; J.ckm1(q) = 0.0; }
+    double chim1 = 0.0, chim2 = 0.0;
+    long long k = 0;
+    unsigned status = 0;
+    double isw = 0.0, iswold = 0.0, lambda = 0.0, sacc = 0.0;
+    double core[9], dc[9], acc[9];
+    FastRec p;
+    while (!is_empty(data)) {
+        if (k >= P.max_steps) { status |= 1u; break; }
+        const double bc[9] = {b.a, b.t, b.x, b.y, b.z, b.k0, b.k1, b.k2, b.k3};
+        // stages: core = b + c_s dl * d_{s-1};  acc = d0 + 2 d1 + 2 d2 + d3 (in that order)
+        // stage 1 is at b, where the previous step's post-step gather already
+        // read the field (data); stages 2-4 gather at their own points
+        // The stage points b + pc k are located and gathered from their FP32
+        // offset to b's cell (pc k is a fraction of a cell); their float64
+        // coordinates are formed only on the rare full-walk / restart paths.
+        float kfs[3];
+        double pk[3] = {0.0, 0.0, 0.0}, pc = 0.0;
+#pragma unroll 1
+        for (int sg = 0; sg < 4; ++sg) {
+            if (sg == 0) {
+                rhs_math(C, data, bc, inv_a, tb, dc, kfs);
+            } else {
+                const float cc = (float)pc * cells_per_unit(here.level);
+                const PosStage ps{bc[2], bc[3], bc[4], pc, pk[0], pk[1], pk[2]};
+                const Loc d = locate_rel(T, here, fmaf(cc, kfs[0], here.fd[0]), fmaf(cc, kfs[1], here.fd[1]),
+                                         fmaf(cc, kfs[2], here.fd[2]), ps);
+                const Field7 g = gather_at<ORDER>(T, d, ps, false, st, ST_RK_REC, false);
+                rhs_math(C, g, core, recip(core[0]), tb, dc, kfs);
+            }
+            const double cs = (sg < 2) ? 0.5 * dl : dl;
+            const double wa = (sg == 0) ? 0.0 : 2.0;
+            if (sg < 3) {
+#pragma unroll
+                for (int q = 0; q < 9; ++q) {
+                    acc[q] = (sg == 0) ? dc[q] : acc[q] + wa * dc[q];
+                    if (q < 2 || q > 4) core[q] = bc[q] + cs * dc[q];
                 }
-                const double cs = (sg < 2) ? 0.5 * dl : dl;
-                const double wa = (sg == 0) ? 0.0 : 2.0;
-                if (sg < 3) {
-    #pragma unroll
-                    for (int q = 0; q < 9; ++q) {
-                        acc[q] = (sg == 0) ? dc[q] : acc[q] + wa * dc[q];
-                        if (q < 2 || q > 4) core[q] = bc[q] + cs * dc[q];
+                pc = cs * inv_scale;   // positions: dx/dl = k / scale
+                pk[0] = dc[2]; pk[1] = dc[3]; pk[2] = dc[4];
+            }
+        }
+        const double dl6 = dl * (1.0 / 6.0);
+        const double dl6p = dl6 * inv_scale;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) core[q] = bc[q] + ((q >= 2 && q <= 4) ? dl6p : dl6) * (acc[q] + dc[q]);
+        p.a = core[0]; p.t = core[1]; p.x = core[2]; p.y = core[3]; p.z = core[4];
+        p.k0 = core[5]; p.k1 = core[6]; p.k2 = core[7]; p.k3 = core[8];
+        const Loc ploc = locate_near(T, here, p.x, p.y, p.z);
+        data = gather_at<ORDER>(T, ploc, PosAt{p.x, p.y, p.z}, true, st, ST_POST_REC, false);
+        {
+            // the extent test (integrator.h:757): a point in a located cell away from
+            // the domain faces is inside; only cells on a face (or wrapped keys)
+            // need the float64 comparison
+            const uint32_t last = (ploc.cell >= 0) ? (uint32_t)((1ull << ploc.level) - 1ull) : 0u;
+            const bool face = (ploc.cell < 0) || ploc.c[0] == 0u || ploc.c[1] == 0u || ploc.c[2] == 0u ||
+                              ploc.c[0] >= last || ploc.c[1] >= last || ploc.c[2] >= last;
+            if (p.a < 0.0 || (face && !((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx))))
+                clear(data);
+        }
+        p.level = (ploc.cell >= 0) ? ploc.level : 0;
+        p.ah = data.a;
+        p.rho = data.rho; p.phi = data.phi; p.dx = data.dx; p.dy = data.dy; p.dz = data.dz;
+        p.dt = -data.dt;
+        const float dphi_last = data.phi - (float)b.phi;   // laplacian of the final record, divided at the end
+        const double dl_last = dl;
+        isw += (double)(b.dt + p.dt) * (p.t - b.t) * (1.0 / c2);
+        if (O.final_rec) {   // only the final photon record reports it
+            iswold -= 2.0 * (p.phi - b.phi) * (1.0 / c2) -
+                      (((double)b.dx + (double)p.dx) * (p.x - b.x) * scale + ((double)b.dy + (double)p.dy) * (p.y - b.y) * scale +
+                       ((double)b.dz + (double)p.dz) * (p.z - b.z) * scale) * (1.0 / c2);
+        }
+        p.chi = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
+        lambda += dl;
+        sacc += (double)sqrtf((float)((p.x - b.x) * (p.x - b.x) + (p.y - b.y) * (p.y - b.y) + (p.z - b.z) * (p.z - b.z)));
+        const double inv_pa = recip(p.a);
+        p.red = a0 * inv_pa * (1.0 + phi0c2 - p.phi * (1.0 / c2)) - 1.0;
+        p.isw = isw; p.iswold = iswold; p.lambda = lambda; p.s = sacc;
+        if (!is_empty(data)) {
+            ratio = p.a * p.a * ratio_k;
+            dl = (ploc.cell >= 0 ? cell_extent(ploc.level) : 0.0) * ratio;
+            last_data_dt = data.dt;
+            last_dphi = dphi_last;
+            last_dl = dl_last;
+            if (ploc.cell != here.cell) stat(st, ST_CELL_CHANGE);
+            here = ploc;
+            ++k;
+            stat(st, ST_STEPS);
+            if (P.jacobian) {
+                float h3[3];
+                jac_fast(T, here, p.x, p.y, p.z, h3, st);
+                const double dr = p.chi - b.chi;
+                chim2 = chim1; chim1 = b.chi;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    J.ckm1(q) = J.ck(q); J.ckm1(3 + q) = J.ck(3 + q);
+                    const double hd = (double)h3[q] * dr;
+                    const double c1 = p.chi * hd, c2v = p.chi * p.chi * hd;
+                    J.ck(q) = c1;
+                    J.ck(3 + q) = c2v;
+                    J.S(q) += c1;
+                    J.S(3 + q) += c2v;
+                }
+            }
+            while (next_plane < np) {
+                const int kind = skind;
+                const double q1 = (kind == STOP_R) ? p.chi : (kind == STOP_LAMBDA) ? p.lambda : (kind == STOP_T) ? p.t
+                                : (kind == STOP_A) ? p.a : (kind == STOP_S) ? p.s : p.red;
+                const double ref = SRC ? stop_ref : P.planes[next_plane];
+                if (!((kind == STOP_A) ? (q1 < ref) : (q1 > ref))) break;
+                const int j = next_plane++;
+                cross_k[j] = k;
+                if (prow) {
+                    double* o = prow + j * rec_fields;
+                    const double q0 = (kind == STOP_R) ? b.chi : (kind == STOP_LAMBDA) ? b.lambda : (kind == STOP_T) ? b.t
+                                    : (kind == STOP_A) ? b.a : (kind == STOP_S) ? b.s : b.red;
+                    const double f = (q1 - ref) / (q1 - q0);
+                    const double px = b.x * f + p.x * (1 - f), py = b.y * f + p.y * (1 - f), pz = b.z * f + p.z * (1 - f);
+                    const double dist = sqrt(px * px + py * py + pz * pz);
+                    o[0] = (double)(k - 1); o[1] = f; o[2] = px; o[3] = py; o[4] = pz; o[5] = dist;
+                    o[9] = b.t * f + p.t * (1 - f);
+                    o[10] = b.a * f + p.a * (1 - f);
+                    o[11] = b.red * f + p.red * (1 - f);
+                    o[12] = b.chi * f + p.chi * (1 - f);
+                    o[13] = b.lambda * f + p.lambda * (1 - f);
+                    o[14] = b.s * f + p.s * (1 - f);
+                    o[15] = b.isw * f + p.isw * (1 - f);
+                    o[16] = (double)b.rho * f + (double)p.rho * (1 - f);
+                    o[17] = b.phi * f + p.phi * (1 - f);
+                    o[18] = have_rmax ? rmax : 0.0;
+                    o[19] = 1.0;
+                    if (SRC) {
+                        o[20] = b.k0 * f + p.k0 * (1 - f);
+                        o[21] = b.k1 * f + p.k1 * (1 - f);
+                        o[22] = b.k2 * f + p.k2 * (1 - f);
+                        o[23] = b.k3 * f + p.k3 * (1 - f);
                     }
-                    pc = cs * K.inv_scale;   // positions: dx/dl = k / scale
-                    pk[0] = dc[2]; pk[1] = dc[3]; pk[2] = dc[4];
-                }
-            }
-            const double dl6 = dl * (1.0 / 6.0);
-            const double dl6p = dl6 * K.inv_scale;
-    #pragma unroll
-            for (int q = 0; q < 9; ++q) core[q] = bc[q] + ((q >= 2 && q <= 4) ? dl6p : dl6) * (acc[q] + dc[q]);
-            p.a = core[0]; p.t = core[1]; p.x = core[2]; p.y = core[3]; p.z = core[4];
-            p.k0 = core[5]; p.k1 = core[6]; p.k2 = core[7]; p.k3 = core[8];
-            const Loc ploc = locate_near(T, here, p.x, p.y, p.z);
-            data = gather_at<ORDER>(T, ploc, PosAt{p.x, p.y, p.z}, true, st, ST_POST_REC, false);
-            {
-                // the extent test (integrator.h:757): a point in a located cell away from
-                // the domain faces is inside; only cells on a face (or wrapped keys)
-                // need the float64 comparison
-                const uint32_t last = (ploc.cell >= 0) ? (uint32_t)((1ull << ploc.level) - 1ull) : 0u;
-                const bool face = (ploc.cell < 0) || ploc.c[0] == 0u || ploc.c[1] == 0u || ploc.c[2] == 0u ||
-                                  ploc.c[0] >= last || ploc.c[1] >= last || ploc.c[2] >= last;
-                if (p.a < 0.0 || (face && !((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx))))
-                    clear(data);
-            }
-            p.level = (ploc.cell >= 0) ? ploc.level : 0;
-            p.ah = data.a;
-            p.rho = data.rho; p.phi = data.phi; p.dx = data.dx; p.dy = data.dy; p.dz = data.dz;
-            p.dt = -data.dt;
-            const float dphi_last = data.phi - (float)b.phi;   // laplacian of the final record, divided at the end
-            const double dl_last = dl;
-            isw += (double)(b.dt + p.dt) * (p.t - b.t) * (1.0 / c2);
-            if (O.final_rec) {   // only the final photon record reports it
-                iswold -= 2.0 * (p.phi - b.phi) * (1.0 / c2) -
-                          (((double)b.dx + (double)p.dx) * (p.x - b.x) * scale + ((double)b.dy + (double)p.dy) * (p.y - b.y) * scale +
-                           ((double)b.dz + (double)p.dz) * (p.z - b.z) * scale) * (1.0 / c2);
-            }
-            p.chi = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
-            lambda += dl;
-            sacc += (double)sqrtf((float)((p.x - b.x) * (p.x - b.x) + (p.y - b.y) * (p.y - b.y) + (p.z - b.z) * (p.z - b.z)));
-            const double inv_pa = recip(p.a);
-            p.red = a0 * inv_pa * (1.0 + phi0c2 - p.phi * (1.0 / c2)) - 1.0;
-            p.isw = isw; p.iswold = iswold; p.lambda = lambda; p.s = sacc;
-            if (!is_empty(data)) {
-                ratio = p.a * p.a * K.ratio_k;
-                dl = (ploc.cell >= 0 ? cell_extent(ploc.level) : 0.0) * ratio;
-                last_data_dt = data.dt;
-                last_dphi = dphi_last;
-                last_dl = dl_last;
-                if (ploc.cell != here.cell) stat(st, ST_CELL_CHANGE);
-                here = ploc;
-                ++k;
-                stat(st, ST_STEPS);
-                if (P.jacobian) {
-                    float h3[3];
-                    jac_fast(T, here, p.x, p.y, p.z, h3, st);
-                    const double dr = p.chi - b.chi;
-                    chim2 = chim1; chim1 = b.chi;
-    #pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        J.ckm1(q) = J.ck(q); J.ckm1(3 + q) = J.ck(3 + q);
-                        const double hd = (double)h3[q] * dr;
-                        const double c1 = p.chi * hd, c2v = p.chi * p.chi * hd;
-                        J.ck(q) = c1;
-                        J.ck(3 + q) = c2v;
-                        J.S(q) += c1;
-                        J.S(3 + q) += c2v;
-                    }
-                }
-                while (next_plane < np) {
-                    const int kind = skind;
-                    const double q1 = (kind == STOP_R) ? p.chi : (kind == STOP_LAMBDA) ? p.lambda : (kind == STOP_T) ? p.t
-                                    : (kind == STOP_A) ? p.a : (kind == STOP_S) ? p.s : p.red;
-                    const double ref = SRC ? stop_ref : P.planes[next_plane];
-                    if (!((kind == STOP_A) ? (q1 < ref) : (q1 > ref))) break;
-                    const int j = next_plane++;
-                    cross_k[j] = k;
-                    if (prow) {
-                        double* o = prow + j * rec_fields;
-                        const double q0 = (kind == STOP_R) ? b.chi : (kind == STOP_LAMBDA) ? b.lambda : (kind == STOP_T) ? b.t
-                                        : (kind == STOP_A) ? b.a : (kind == STOP_S) ? b.s : b.red;
-                        const double f = (q1 - ref) / (q1 - q0);
-                        const double px = b.x * f + p.x * (1 - f), py = b.y * f + p.y * (1 - f), pz = b.z * f + p.z * (1 - f);
-                        const double dist = sqrt(px * px + py * py + pz * pz);
-                        o[0] = (double)(k - 1); o[1] = f; o[2] = px; o[3] = py; o[4] = pz; o[5] = dist;
-                        o[9] = b.t * f + p.t * (1 - f);
-                        o[10] = b.a * f + p.a * (1 - f);
-                        o[11] = b.red * f + p.red * (1 - f);
-                        o[12] = b.chi * f + p.chi * (1 - f);
-                        o[13] = b.lambda * f + p.lambda * (1 - f);
-                        o[14] = b.s * f + p.s * (1 - f);
-                        o[15] = b.isw * f + p.isw * (1 - f);
-                        o[16] = (double)b.rho * f + (double)p.rho * (1 - f);
-                        o[17] = b.phi * f + p.phi * (1 - f);
-                        o[18] = have_rmax ? rmax : 0.0;
-                        o[19] = 1.0;
-                        if (SRC) {
-                            o[20] = b.k0 * f + p.k0 * (1 - f);
-                            o[21] = b.k1 * f + p.k1 * (1 - f);
-                            o[22] = b.k2 * f + p.k2 * (1 - f);
-                            o[23] = b.k3 * f + p.k3 * (1 - f);
-                        }
-                        if (P.jacobian) {
-                            // at the surface's distance, or at the source radius in source mode
-                            const double jd = SRC ? ref : dist;
-                            double s1[3], s2[3];
-                            bool ok = true;
-                            if (p.chi <= jd) {
-                                for (int q = 0; q < 3; ++q) { s1[q] = J.S(q); s2[q] = J.S(3 + q); }
-                            } else if (chim1 <= jd) {
-                                for (int q = 0; q < 3; ++q) { s1[q] = J.S(q) - J.ck(q); s2[q] = J.S(3 + q) - J.ck(3 + q); }
-                            } else if (k >= 2 && chim2 <= jd) {
-                                for (int q = 0; q < 3; ++q) {
-                                    s1[q] = J.S(q) - J.ck(q) - J.ckm1(q);
-                                    s2[q] = J.S(3 + q) - J.ck(3 + q) - J.ckm1(3 + q);
-                                }
-                            } else {
-                                ok = false;
-                                status |= 2u;
-                            }
-                            if (ok) {
-                                const double idist = 1.0 / jd;
-                                o[6] = 1.0 - 2.0 * (s1[0] - s2[0] * idist) / c2 * P.length;
-                                o[7] = -2.0 * (s1[1] - s2[1] * idist) / c2 * P.length;
-                                o[8] = 1.0 - 2.0 * (s1[2] - s2[2] * idist) / c2 * P.length;
-                            } else {
-                                o[6] = 1.0; o[7] = 0.0; o[8] = 1.0;
+                    if (P.jacobian) {
+                        // at the surface's distance, or at the source radius in source mode
+                        const double jd = SRC ? ref : dist;
+                        double s1[3], s2[3];
+                        bool ok = true;
+                        if (p.chi <= jd) {
+                            for (int q = 0; q < 3; ++q) { s1[q] = J.S(q); s2[q] = J.S(3 + q); }
+                        } else if (chim1 <= jd) {
+                            for (int q = 0; q < 3; ++q) { s1[q] = J.S(q) - J.ck(q); s2[q] = J.S(3 + q) - J.ck(3 + q); }
+                        } else if (k >= 2 && chim2 <= jd) {
+                            for (int q = 0; q < 3; ++q) {
+                                s1[q] = J.S(q) - J.ck(q) - J.ckm1(q);
+                                s2[q] = J.S(3 + q) - J.ck(3 + q) - J.ckm1(3 + q);
                             }
                         } else {
-                            o[6] = o[7] = o[8] = 0.0;
+                            ok = false;
+                            status |= 2u;
                         }
+                        if (ok) {
+                            const double idist = 1.0 / jd;
+                            o[6] = 1.0 - 2.0 * (s1[0] - s2[0] * idist) / c2 * P.length;
+                            o[7] = -2.0 * (s1[1] - s2[1] * idist) / c2 * P.length;
+                            o[8] = 1.0 - 2.0 * (s1[2] - s2[2] * idist) / c2 * P.length;
+                        } else {
+                            o[6] = 1.0; o[7] = 0.0; o[8] = 1.0;
+                        }
+                    } else {
+                        o[6] = o[7] = o[8] = 0.0;
                     }
                 }
-                if (!have_rmax || rmax < (double)b.rho) rmax = b.rho;
-                have_rmax = true;
-                b = p;
-                inv_a = inv_pa;
             }
-            bool stop;
-            switch (skind) {
-            case STOP_R: stop = b.chi > stop_ref; break;
-            case STOP_LAMBDA: stop = b.lambda > stop_ref; break;
-            case STOP_REDSHIFT: stop = b.red > stop_ref; break;
-            case STOP_T: stop = b.t > stop_ref; break;
-            case STOP_A: stop = b.a < stop_ref; break;
-            case STOP_PLANE: stop = (p.x * P.ki[0] + p.y * P.ki[1] + p.z * P.ki[2]) > stop_ref; break;
-            case STOP_S: stop = b.s > stop_ref; break;
-            default: stop = true;
-            }
-        return !stop && !is_empty(data);
-    }
-
-    __device__ __forceinline__ void finish(const PropParams& P, const PropOut& O)
-    {
-        const double c2 = kC * kC;
-        const int np = SRC ? 1 : P.nplanes;
-        long long size = k + 1;
-        if (signbit(b.red) || signbit(b.a)) size -= 1;
-        O.steps[i] = size;
-        if (O.final_rec) {
-            double* o = O.final_rec + i * kPhotonFields;
-            if (size == k + 1) {
-                Rec r;
-                r.a = b.a; r.t = b.t; r.x = b.x; r.y = b.y; r.z = b.z; r.k0 = b.k0; r.k1 = b.k1; r.k2 = b.k2; r.k3 = b.k3;
-                r.level = b.level; r.ah = b.ah; r.rho = b.rho; r.phi = b.phi;
-                r.dx = b.dx; r.dy = b.dy; r.dz = b.dz; r.dt = b.dt;
-                r.dphidl = (k > 0) ? ((double)last_data_dt * b.k0 + ((double)b.dx * b.k1 + (double)b.dy * b.k2 + (double)b.dz * b.k3)) : 0.0;
-                r.lap = (k > 0) ? (double)last_dphi / last_dl : 0.0;
-                const double kk = b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3;
-                r.ds2 = (b.a * b.a) * (-(c2 * (1.0 + 2.0 * (b.phi / c2)) * b.k0 * b.k0) + ((1.0 - 2.0 * (b.phi / c2)) * kk));
-                r.err = 1.0 - ((1.0 - 2.0 * (b.phi / c2)) * kk) / (c2 * (1.0 + 2.0 * (b.phi / c2)) * b.k0 * b.k0);
-                r.red = b.red; r.isw = b.isw; r.iswold = b.iswold; r.chi = b.chi; r.lambda = b.lambda; r.s = b.s;
-                r.index = (double)k;
-                write_rec(o, r);
-            } else {
-                for (int q = 0; q < kPhotonFields; ++q) o[q] = 0.0;
-                status |= 4u;
-            }
+            if (!have_rmax || rmax < (double)b.rho) rmax = b.rho;
+            have_rmax = true;
+            b = p;
+            inv_a = inv_pa;
         }
-        if (SRC && prow) {
-            const long long ck = cross_k[0];
-            const bool ok = (ck >= 1) && (ck < size);
-            if (!ok) {
-                for (int q = 0; q < 24; ++q) prow[q] = 0.0;
-                const long long marked = size - 1;
-                prow[0] = (double)(marked - (marked > 0));
-            }
-            prow[19] = ok ? 1.0 : 0.0;
-        } else if (prow) {
-            for (int j = 0; j < np; ++j) {
-                double* o = prow + j * kPlaneFields;
-                const long long ck = cross_k[j];
-                const bool found = (ck >= 1) && (ck < size);
-                const bool valid = found && !((ck - 1) == size - 1 || (ck - 1) == 0);
-                if (ck < 0 || ck == 0 || ck >= size) {
-                    for (int q = 0; q < kPlaneFields; ++q) o[q] = 0.0;
-                    o[0] = (ck == 0) ? 0.0 : (double)(size - 1);
-                }
-                o[19] = valid ? 1.0 : 0.0;
-            }
+        bool stop;
+        switch (skind) {
+        case STOP_R: stop = b.chi > stop_ref; break;
+        case STOP_LAMBDA: stop = b.lambda > stop_ref; break;
+        case STOP_REDSHIFT: stop = b.red > stop_ref; break;
+        case STOP_T: stop = b.t > stop_ref; break;
+        case STOP_A: stop = b.a < stop_ref; break;
+        case STOP_PLANE: stop = (p.x * P.ki[0] + p.y * P.ki[1] + p.z * P.ki[2]) > stop_ref; break;
+        case STOP_S: stop = b.s > stop_ref; break;
+        default: stop = true;
         }
-        if (status) atomicOr(O.status, status);
+        if (stop) break;
     }
-};
+    long long size = k + 1;
+    if (signbit(b.red) || signbit(b.a)) size -= 1;
+    O.steps[i] = size;
+    if (O.final_rec) {
+        double* o = O.final_rec + i * kPhotonFields;
+        if (size == k + 1) {
+            Rec r;
+            r.a = b.a; r.t = b.t; r.x = b.x; r.y = b.y; r.z = b.z; r.k0 = b.k0; r.k1 = b.k1; r.k2 = b.k2; r.k3 = b.k3;
+            r.level = b.level; r.ah = b.ah; r.rho = b.rho; r.phi = b.phi;
+            r.dx = b.dx; r.dy = b.dy; r.dz = b.dz; r.dt = b.dt;
+            r.dphidl = (k > 0) ? ((double)last_data_dt * b.k0 + ((double)b.dx * b.k1 + (double)b.dy * b.k2 + (double)b.dz * b.k3)) : 0.0;
+            r.lap = (k > 0) ? (double)last_dphi / last_dl : 0.0;
+            const double kk = b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3;
+            r.ds2 = (b.a * b.a) * (-(c2 * (1.0 + 2.0 * (b.phi / c2)) * b.k0 * b.k0) + ((1.0 - 2.0 * (b.phi / c2)) * kk));
+            r.err = 1.0 - ((1.0 - 2.0 * (b.phi / c2)) * kk) / (c2 * (1.0 + 2.0 * (b.phi / c2)) * b.k0 * b.k0);
+            r.red = b.red; r.isw = b.isw; r.iswold = b.iswold; r.chi = b.chi; r.lambda = b.lambda; r.s = b.s;
+            r.index = (double)k;
+            write_rec(o, r);
+        } else {
+            for (int q = 0; q < kPhotonFields; ++q) o[q] = 0.0;
+            status |= 4u;
+        }
+    }
+    if (SRC && prow) {
+        const long long ck = cross_k[0];
+        const bool ok = (ck >= 1) && (ck < size);
+        if (!ok) {
+            for (int q = 0; q < 24; ++q) prow[q] = 0.0;
+            const long long marked = size - 1;
+            prow[0] = (double)(marked - (marked > 0));
+        }
+        prow[19] = ok ? 1.0 : 0.0;
+    } else if (prow) {
+        for (int j = 0; j < np; ++j) {
+            double* o = prow + j * kPlaneFields;
+            const long long ck = cross_k[j];
+            const bool found = (ck >= 1) && (ck < size);
+            const bool valid = found && !((ck - 1) == size - 1 || (ck - 1) == 0);
+            if (ck < 0 || ck == 0 || ck >= size) {
+                for (int q = 0; q < kPlaneFields; ++q) o[q] = 0.0;
+                o[0] = (ck == 0) ? 0.0 : (double)(size - 1);
+            }
+            o[19] = valid ? 1.0 : 0.0;
+        }
+    }
+    if (status) atomicOr(O.status, status);
+}
 
 
 // Persistent launch: each warp takes the next 32 rays from a global counter
 // until the batch is exhausted, so uneven path lengths do not leave tail
 // waves.  `queue` is zeroed before the launch.
-// Persistent launch with lane-level refill: every lane owns one ray at a time;
-// lanes whose ray has ended take the next rays from a global counter (one
-// atomic per warp and round), so uneven path lengths leave neither idle lanes
-// in a warp nor tail waves.  `queue` is zeroed before the launch.
 template <int ORDER, bool SRC>
 __global__ void __launch_bounds__(kFastThreads, MPF_FAST_MINB) k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
                                                                     const double* __restrict__ launch, long long n, PropOut O,
@@ -855,33 +807,15 @@ __global__ void __launch_bounds__(kFastThreads, MPF_FAST_MINB) k_propagate_fast(
 {
     __shared__ double jac_sh[18 * kFastThreads];
     const JacSums J{jac_sh + threadIdx.x};
-    const FastK K{1.0 / P.length, (P.length / kC) / P.nsteps};
-    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    FastRay<ORDER, SRC> r;
-    bool active = false, exhausted = false;
     for (;;) {
-        const unsigned need = __ballot_sync(full, !active && !exhausted);
-        if (need) {
-            const int leader = __ffs(need) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(need));
-            base = __shfl_sync(full, base, leader);
-            if (!active && !exhausted) {
-                const long long i = (long long)base + __popc(need & ((1u << lane) - 1u));
-                if (i < n) {
-                    r.start(T, C, P, K, launch + 6 * i, i, O, J);
-                    active = true;
-                } else {
-                    exhausted = true;
-                }
-            }
-        }
-        if (__all_sync(full, exhausted && !active)) break;
-        if (active && !r.advance(T, C, P, K, O, J)) {
-            r.finish(P, O);
-            active = false;
-        }
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(queue, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= (unsigned long long)n) break;
+        const long long i = (long long)base + lane;
+        if (i < n) propagate_fast<ORDER, SRC>(T, C, P, launch + 6 * i, i, O, J);
+        __syncwarp();
     }
 }
 
