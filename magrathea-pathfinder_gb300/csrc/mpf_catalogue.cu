@@ -11,6 +11,10 @@
 //   k_cat_update  measures the miss, writes the row, and either finishes the
 //                 source or takes a Newton step and queues it for the next
 //                 round (atomic compaction into the other active list).
+// The sources are sorted by the direction of their first ray (a 2-D Morton
+// key of phi, theta) and every compaction keeps that order, so each warp
+// traces 32 neighbouring rays: their gathers share cells and cache lines
+// (rays of unrelated directions in one warp run several times slower).
 // Rounds 0-2 use the identity as Newton Jacobian (catalogues.h:507-513) and
 // trace without the lensing Jacobian; a source that converges there is traced
 // once more with it after the last round (the ray is the same: the launch
@@ -36,9 +40,27 @@ struct CatState {
     double pad;
 };
 
+// 2-D Morton key of a direction: 16 bits of phi in [-pi, pi] and of theta in [0, pi], interleaved.
+__device__ __forceinline__ uint32_t spread16(uint32_t v)
+{
+    v &= 0xffffu;
+    v = (v | (v << 8)) & 0x00ff00ffu;
+    v = (v | (v << 4)) & 0x0f0f0f0fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+__device__ __forceinline__ uint32_t direction_key(double phi, double theta)
+{
+    const double pi = 3.14159265358979323846;
+    const double u = fmin(fmax((phi + pi) * (1.0 / (2.0 * pi)), 0.0), 1.0);
+    const double v = fmin(fmax(theta * (1.0 / pi), 0.0), 1.0);
+    return spread16((uint32_t)(u * 65535.0)) | (spread16((uint32_t)(v * 65535.0)) << 1);
+}
+
 __global__ void k_cat_init(long long n, const double* __restrict__ src, int stride, CatRotation rot, int has_rot,
-                           CatState* __restrict__ state, double* __restrict__ rows, int* __restrict__ active,
-                           unsigned* __restrict__ count)
+                           CatState* __restrict__ state, double* __restrict__ rows, uint32_t* __restrict__ key,
+                           int* __restrict__ val, unsigned* __restrict__ count)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -67,9 +89,12 @@ __global__ void k_cat_init(long long n, const double* __restrict__ src, int stri
     for (int k = 0; k < kCatalogueFields; ++k) r[k] = 0.0;
     r[0] = S.phi;
     r[1] = S.theta;
+    val[i] = (int)i;
     if (S.dist > 0.0 && isfinite(S.dist) && isfinite(S.phi) && isfinite(S.theta)) {
-        active[atomicAdd(count, 1u)] = (int)i;
+        key[i] = direction_key(S.phi, S.theta) & 0x7fffffffu;   // below the key of the excluded sources
+        atomicAdd(count, 1u);
     } else {
+        key[i] = 0xffffffffu;
         // a source at the observer (or with non-finite coordinates) has no
         // direction: reported as unreachable
         r[2] = 42.0; r[3] = 42.0;
@@ -97,11 +122,13 @@ __global__ void k_cat_rays(long long m, const int* __restrict__ list, const CatS
 __global__ void k_cat_update(long long m, int iteration, int traced_jacobian, CatConst K,
                              const int* __restrict__ list, CatState* __restrict__ state, double* __restrict__ rows,
                              const long long* __restrict__ steps, const double* __restrict__ rec,
-                             int* __restrict__ next, unsigned* __restrict__ next_count, int* __restrict__ retrace,
-                             unsigned* __restrict__ retrace_count, unsigned long long* __restrict__ photon_steps)
+                             int* __restrict__ cont, int* __restrict__ retrace_flag,
+                             unsigned long long* __restrict__ photon_steps)
 {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= m) return;
+    if (j > m) return;
+    cont[j] = 0;   // continue flag, scanned into the next round's list (entry m closes the scan)
+    if (j == m) return;
     const double c = kC, c2 = kC * kC;
     const int s = list[j];
     CatState S = state[s];
@@ -164,7 +191,7 @@ __global__ void k_cat_update(long long m, int iteration, int traced_jacobian, Ca
         S.phi = nphi;
         S.theta = ntheta;
         state[s] = S;
-        next[atomicAdd(next_count, 1u)] = s;
+        cont[j] = 1;
         return;
     }
     // converged (catalogues.h:658-726)
@@ -172,7 +199,7 @@ __global__ void k_cat_update(long long m, int iteration, int traced_jacobian, Ca
     if (traced_jacobian) {
         row[12] = o[6]; row[13] = o[7]; row[14] = o[7]; row[15] = o[8];
     } else {
-        retrace[atomicAdd(retrace_count, 1u)] = s;
+        retrace_flag[s] = 1;
     }
     const double potential = o[17];
     const double isw = o[15];
@@ -216,11 +243,62 @@ __global__ void k_cat_jacobian(long long m, const int* __restrict__ list, const 
     row[12] = o[6]; row[13] = o[7]; row[14] = o[7]; row[15] = o[8];
 }
 
+// Stable LSD radix sort of (key, value) pairs: 4-bit digits, each thread
+// walks one tile of kSortTile consecutive entries in order.
+constexpr int kSortTile = 256;
+
+__global__ void k_sort_hist(const uint32_t* __restrict__ key, long long n, int shift, int* __restrict__ hist,
+                            long long ntiles)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    int h[16];
+    for (int d = 0; d < 16; ++d) h[d] = 0;
+    const long long e = min(n, (t + 1) * kSortTile);
+    for (long long i = t * kSortTile; i < e; ++i) ++h[(key[i] >> shift) & 15u];
+    for (int d = 0; d < 16; ++d) hist[d * ntiles + t] = h[d];
+}
+
+__global__ void k_sort_scatter(const uint32_t* __restrict__ key, const int* __restrict__ val, long long n, int shift,
+                               const int* __restrict__ off, long long ntiles, uint32_t* __restrict__ key2,
+                               int* __restrict__ val2)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    int o[16];
+    for (int d = 0; d < 16; ++d) o[d] = off[d * ntiles + t];
+    const long long e = min(n, (t + 1) * kSortTile);
+    for (long long i = t * kSortTile; i < e; ++i) {
+        const uint32_t k = key[i];
+        const int j = o[(k >> shift) & 15u]++;
+        key2[j] = k;
+        val2[j] = val[i];
+    }
+}
+
+// Order-keeping compaction: scan holds the exclusive prefix sum of the flags
+// over m + 1 entries.
+__global__ void k_compact(long long m, const int* __restrict__ from, const int* __restrict__ scan, int* __restrict__ to)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    if (scan[j + 1] > scan[j]) to[scan[j]] = from[j];
+}
+
+// Flags of a list's entries from a per-source flag array (entry m = 0).
+__global__ void k_list_flags(long long m, const int* __restrict__ list, const int* __restrict__ per_source,
+                             int* __restrict__ flags)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > m) return;
+    flags[j] = (j < m) ? per_source[list[j]] : 0;
+}
+
 namespace {
 unsigned blocks(long long n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
 
 struct CatBuffers {
-    void* p[10] = {};
+    void* p[13] = {};
     ~CatBuffers()
     {
         for (void* q : p)
@@ -241,41 +319,63 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     stats->launches = 0;
     if (n <= 0) return cudaSuccess;
     const int tpb = 128;
+    const long long ntiles = (n + kSortTile - 1) / kSortTile;
     CatBuffers B;
-    CatState* state = nullptr;
-    int *act0 = nullptr, *act1 = nullptr, *retr = nullptr;
-    unsigned* counters = nullptr;            // [0] active, [1] next, [2] retrace, [3] status
-    unsigned long long* psteps = nullptr;
-    double *launch = nullptr, *radius = nullptr, *rec = nullptr;
-    long long* steps = nullptr;
     cudaError_t e = cudaSuccess;
     auto alloc = [&](int k, size_t bytes) -> void* {
         if (e != cudaSuccess) return nullptr;
         e = cudaMalloc(&B.p[k], bytes);
         return (e == cudaSuccess) ? B.p[k] : nullptr;
     };
-    state = (CatState*)alloc(0, (size_t)n * sizeof(CatState));
-    act0 = (int*)alloc(1, (size_t)n * sizeof(int));
-    act1 = (int*)alloc(2, (size_t)n * sizeof(int));
-    retr = (int*)alloc(3, (size_t)n * sizeof(int));
-    counters = (unsigned*)alloc(4, 8 * sizeof(unsigned));
-    psteps = (unsigned long long*)alloc(5, 2 * sizeof(unsigned long long));
-    launch = (double*)alloc(6, (size_t)n * 6 * sizeof(double));
-    radius = (double*)alloc(7, (size_t)n * sizeof(double));
-    rec = (double*)alloc(8, (size_t)n * kSourceFields * sizeof(double));
-    steps = (long long*)alloc(9, (size_t)n * sizeof(long long));
+    CatState* state = (CatState*)alloc(0, (size_t)n * sizeof(CatState));
+    int* act0 = (int*)alloc(1, (size_t)n * sizeof(int));
+    int* act1 = (int*)alloc(2, (size_t)n * sizeof(int));
+    int* rflag = (int*)alloc(3, (size_t)n * sizeof(int));
+    unsigned* counters = (unsigned*)alloc(4, 8 * sizeof(unsigned));   // [0] valid sources, [3] status
+    unsigned long long* psteps = (unsigned long long*)alloc(5, 2 * sizeof(unsigned long long));
+    double* launch = (double*)alloc(6, (size_t)n * 6 * sizeof(double));
+    double* radius = (double*)alloc(7, (size_t)n * sizeof(double));
+    double* rec = (double*)alloc(8, (size_t)n * kSourceFields * sizeof(double));
+    long long* steps = (long long*)alloc(9, (size_t)n * sizeof(long long));
+    uint32_t* key0 = (uint32_t*)alloc(10, (size_t)n * sizeof(uint32_t));
+    uint32_t* key1 = (uint32_t*)alloc(11, (size_t)n * sizeof(uint32_t));
+    int* scan = (int*)alloc(12, (size_t)(std::max<long long>(n, 16 * ntiles) + 1) * sizeof(int));
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(counters, 0, 8 * sizeof(unsigned), stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(psteps, 0, 2 * sizeof(unsigned long long), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(rflag, 0, (size_t)n * sizeof(int), stream);
     if (e != cudaSuccess) return e;
     CatRotation R{};
     if (rot) R = *rot;
-    k_cat_init<<<blocks(n, tpb), tpb, 0, stream>>>(n, d_src, stride, R, rot ? 1 : 0, state, d_rows, act0, counters);
+    k_cat_init<<<blocks(n, tpb), tpb, 0, stream>>>(n, d_src, stride, R, rot ? 1 : 0, state, d_rows, key0, act0, counters);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     stats->launches = 1;
+    // sources in direction order; the unreachable ones (key 0xffffffff) sort last
+    {
+        uint32_t *ka = key0, *kb = key1;
+        int *va = act0, *vb = act1;
+        for (int shift = 0; shift < 32; shift += 4) {
+            k_sort_hist<<<blocks(ntiles, tpb), tpb, 0, stream>>>(ka, n, shift, scan, ntiles);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            exclusive_scan(scan, 16 * ntiles, stream);
+            k_sort_scatter<<<blocks(ntiles, tpb), tpb, 0, stream>>>(ka, va, n, shift, scan, ntiles, kb, vb);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            std::swap(ka, kb);
+            std::swap(va, vb);
+            stats->launches += 2;
+        }
+        // eight passes: the sorted values are back in act0
+    }
     unsigned m = 0;
     if ((e = cudaMemcpyAsync(&m, counters, sizeof(unsigned), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
+    const unsigned m_valid = m;
+    // act0 keeps the valid sources in direction order (for the re-trace); the
+    // rounds compact between act1 and the key buffer, free after the sort
+    int* sorted = act0;
+    int* cur = act1;
+    int* nxt = reinterpret_cast<int*>(key0);
+    if ((e = cudaMemcpyAsync(cur, sorted, (size_t)m * sizeof(int), cudaMemcpyDeviceToDevice, stream)) != cudaSuccess) return e;
 
     PropParams P;
     memset(&P, 0, sizeof(P));
@@ -287,8 +387,6 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     P.nplanes = 1;
     P.ray_stop = radius;
     PropOut O{steps, nullptr, rec, counters + 3, nullptr};
-    int* cur = act0;
-    int* nxt = act1;
     for (int it = 0; it <= K.max_iterations && m > 0; ++it) {
         const int jac = (it >= 3) ? 1 : 0;
         P.jacobian = jac;
@@ -296,31 +394,35 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         e = exact ? launch_propagate<true>(T, Cs, P, launch, m, O, stream) : launch_propagate<false>(T, Cs, P, launch, m, O, stream);
         if (e != cudaSuccess) return e;
-        if ((e = cudaMemsetAsync(counters + 1, 0, sizeof(unsigned), stream)) != cudaSuccess) return e;
-        k_cat_update<<<blocks(m, tpb), tpb, 0, stream>>>(m, it, jac, K, cur, state, d_rows, steps, rec, nxt, counters + 1,
-                                                          retr, counters + 2, psteps);
+        k_cat_update<<<blocks(m + 1, tpb), tpb, 0, stream>>>(m, it, jac, K, cur, state, d_rows, steps, rec, scan, rflag,
+                                                              psteps);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        const int64_t next_m = exclusive_scan(scan, (int64_t)m + 1, stream);
+        k_compact<<<blocks(m, tpb), tpb, 0, stream>>>(m, cur, scan, nxt);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         stats->rays += m;
         stats->iterations = it + 1;
-        stats->launches += 3;
-        if ((e = cudaMemcpyAsync(&m, counters + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
-        if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
+        stats->launches += 4;
+        m = (unsigned)next_m;
         std::swap(cur, nxt);
     }
-    // Jacobian of the sources that converged in the identity-Jacobian rounds
-    unsigned r = 0;
-    if ((e = cudaMemcpyAsync(&r, counters + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
-    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
+    // Jacobian of the sources that converged in the identity-Jacobian rounds,
+    // re-traced in direction order
+    k_list_flags<<<blocks((long long)m_valid + 1, tpb), tpb, 0, stream>>>(m_valid, sorted, rflag, scan);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const int64_t r = exclusive_scan(scan, (int64_t)m_valid + 1, stream);
+    stats->launches += 1;
     if (r > 0) {
+        k_compact<<<blocks(m_valid, tpb), tpb, 0, stream>>>(m_valid, sorted, scan, cur);
         P.jacobian = 1;
-        k_cat_rays<<<blocks(r, tpb), tpb, 0, stream>>>(r, retr, state, launch, radius);
+        k_cat_rays<<<blocks(r, tpb), tpb, 0, stream>>>(r, cur, state, launch, radius);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         e = exact ? launch_propagate<true>(T, Cs, P, launch, r, O, stream) : launch_propagate<false>(T, Cs, P, launch, r, O, stream);
         if (e != cudaSuccess) return e;
-        k_cat_jacobian<<<blocks(r, tpb), tpb, 0, stream>>>(r, retr, rec, steps, d_rows, psteps);
+        k_cat_jacobian<<<blocks(r, tpb), tpb, 0, stream>>>(r, cur, rec, steps, d_rows, psteps);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         stats->rays += r;
-        stats->launches += 3;
+        stats->launches += 4;
     }
     unsigned long long ps[2] = {0, 0};
     if ((e = cudaMemcpyAsync(ps, psteps, sizeof(ps), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
