@@ -46,9 +46,11 @@ UNIT = "photon-steps/s"
 # payload bytes requested per photon-step, TSC + Jacobian: 4 RK stages x 27 cells x 16 B
 # + post-step 27 x 28 B + Jacobian 6 x 27 x 12 B
 BYTES_PER_PHOTON_STEP = 4 * 27 * 16 + 27 * 28 + 6 * 27 * 12
-# DRAM bytes per photon-step of the propagate kernel measured with ncu on the AMR
-# workload (profiles/propagate_tsc_amr.md); None until measured
-DRAM_BYTES_PER_PHOTON_STEP = 6.8   # measured: (43.6 + 427.5) MB over 6.95e7 photon-steps, medium octree
+# DRAM bytes per photon-step of the propagate kernel, from one ncu capture of the
+# same kernel on the medium octree (profiles/propagate_fast_medium_full.md):
+# (37.12 + 1.10) MB over 6.95e7 photon-steps; the bench's per-launch traffic is
+# this figure times the photon-steps of a launch
+DRAM_BYTES_PER_PHOTON_STEP = 0.55
 
 
 def workload_spec(synth, workload: str):
