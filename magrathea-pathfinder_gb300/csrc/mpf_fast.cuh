@@ -800,8 +800,13 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
 // Persistent launch: each warp takes the next 32 rays from a global counter
 // until the batch is exhausted, so uneven path lengths do not leave tail
 // waves.  `queue` is zeroed before the launch.
+#if defined(MPF_FAST_MAXNREG)
+#define MPF_FAST_BOUNDS __maxnreg__(MPF_FAST_MAXNREG)
+#else
+#define MPF_FAST_BOUNDS __launch_bounds__(kFastThreads, MPF_FAST_MINB)
+#endif
 template <int ORDER, bool SRC>
-__global__ void __launch_bounds__(kFastThreads, MPF_FAST_MINB) k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
+__global__ void MPF_FAST_BOUNDS k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
                                                                     const double* __restrict__ launch, long long n, PropOut O,
                                                                     unsigned long long* queue)
 {
