@@ -457,118 +457,25 @@ __device__ __forceinline__ void rhs_math(const DevCosmo& C, const Field7& g, con
 
 // Jacobian terms (d1d1, d1d2, d2d2 of lensing.h:430-447) at a trajectory
 // point located at `here`: six TSC gathers at +-1 cell.
-// The six TSC differences of the Jacobian in one pass.  The points x +- one
-// cell (and likewise along y, z) have the same in-cell offset as x, so when
-// each of the six face neighbours is a leaf of x's level with all 27 stencil
-// cells at that level (the case the record path of tsc_rec handles), the
-// difference of the two TSC sums is one sum over a 5 x 3 x 3 block with the
-// weights w(i - 1) - w(i + 1) along the axis:
-//     tsc(x + e) - tsc(x - e) = sum_{i=-2..2} (w(i-1) - w(i+1)) w(j) w(k) g(c + (i, j, k)).
-// The 81 cells (27 around c, 9 on each face) are read once instead of the
-// 162 of six separate gathers.  D = {xx, xy, yy, xz, yz, zz} differences
-// (dphidx at +-x; dphidx, dphidy at +-y; dphidx, dphidy, dphidz at +-z).
-// Returns false when a neighbour does not qualify (the caller then gathers
-// the six points one by one).
-__device__ __forceinline__ bool jac_fused(const DevTree& T, const Loc& here, float* D)
-{
-    if (here.cell < 0) return false;
-    // record slots of the face neighbours: -x +x -y +y -z +z
-    constexpr int kFace[6] = {4, 22, 10, 16, 12, 14};
-    int nb[6];
-#pragma unroll
-    for (int a = 0; a < 6; ++a) {
-        const int e = rec_entry(T, here.cell, kFace[a]);
-        if (e < 0) return false;
-        const int fl = rec_flags(T, e);
-        if ((fl & 256) || (fl & 255) != here.level) return false;
-        if ((unsigned)__ldg(&T.stencil[8 * (size_t)e + 7].x) != kFullMask) return false;
-        nb[a] = e;
-    }
-    float w[3][3];
-    tsc_w3(here.fd[0], w[0]);
-    tsc_w3(here.fd[1], w[1]);
-    tsc_w3(here.fd[2], w[2]);
-    // difference weights at offsets -2..2 along each axis
-    float dw[3][5];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        dw[d][0] = -w[d][0];
-        dw[d][1] = -w[d][1];
-        dw[d][2] = w[d][0] - w[d][2];
-        dw[d][3] = w[d][1];
-        dw[d][4] = w[d][2];
-    }
-    float X = 0.f, Yx = 0.f, Yy = 0.f, Zx = 0.f, Zy = 0.f, Zz = 0.f;
-    const int* rc = reinterpret_cast<const int*>(T.stencil + 8 * (size_t)here.cell);
-#pragma unroll
-    for (int j = 0; j < 27; ++j) {   // the 27 cells around c
-        const int i = j / 9, jj = (j / 3) % 3, k = j % 3;
-        const float4 g = __ldg(T.grad + __ldg(rc + j));
-        const float cx = dw[0][i + 1] * w[1][jj] * w[2][k];
-        const float cy = w[0][i] * dw[1][jj + 1] * w[2][k];
-        const float cz = w[0][i] * w[1][jj] * dw[2][k + 1];
-        X = fmaf(cx, g.x, X);
-        Yx = fmaf(cy, g.x, Yx); Yy = fmaf(cy, g.y, Yy);
-        Zx = fmaf(cz, g.x, Zx); Zy = fmaf(cz, g.y, Zy); Zz = fmaf(cz, g.z, Zz);
-    }
-    const int* rxm = reinterpret_cast<const int*>(T.stencil + 8 * (size_t)nb[0]);
-    const int* rxp = reinterpret_cast<const int*>(T.stencil + 8 * (size_t)nb[1]);
-    const int* rym = reinterpret_cast<const int*>(T.stencil + 8 * (size_t)nb[2]);
-    const int* ryp = reinterpret_cast<const int*>(T.stencil + 8 * (size_t)nb[3]);
-    const int* rzm = reinterpret_cast<const int*>(T.stencil + 8 * (size_t)nb[4]);
-    const int* rzp = reinterpret_cast<const int*>(T.stencil + 8 * (size_t)nb[5]);
-#pragma unroll
-    for (int m = 0; m < 9; ++m) {    // the faces at offset -2 / +2
-        const int u = m / 3, v = m % 3;
-        {   // x faces: cells (-+2, u-1, v-1): slots 0..8 of -x, 18..26 of +x
-            const float c = w[1][u] * w[2][v];
-            const float4 gm = __ldg(T.grad + __ldg(rxm + m)), gp = __ldg(T.grad + __ldg(rxp + 18 + m));
-            X = fmaf(dw[0][0] * c, gm.x, X);
-            X = fmaf(dw[0][4] * c, gp.x, X);
-        }
-        {   // y faces: cells (u-1, -+2, v-1): slots u*9 + v of -y, u*9 + 6 + v of +y
-            const float c = w[0][u] * w[2][v];
-            const float4 gm = __ldg(T.grad + __ldg(rym + u * 9 + v)), gp = __ldg(T.grad + __ldg(ryp + u * 9 + 6 + v));
-            Yx = fmaf(dw[1][0] * c, gm.x, Yx); Yy = fmaf(dw[1][0] * c, gm.y, Yy);
-            Yx = fmaf(dw[1][4] * c, gp.x, Yx); Yy = fmaf(dw[1][4] * c, gp.y, Yy);
-        }
-        {   // z faces: cells (u-1, v-1, -+2): slots u*9 + v*3 of -z, u*9 + v*3 + 2 of +z
-            const float c = w[0][u] * w[1][v];
-            const float4 gm = __ldg(T.grad + __ldg(rzm + u * 9 + v * 3)), gp = __ldg(T.grad + __ldg(rzp + u * 9 + v * 3 + 2));
-            Zx = fmaf(dw[2][0] * c, gm.x, Zx); Zy = fmaf(dw[2][0] * c, gm.y, Zy); Zz = fmaf(dw[2][0] * c, gm.z, Zz);
-            Zx = fmaf(dw[2][4] * c, gp.x, Zx); Zy = fmaf(dw[2][4] * c, gp.y, Zy); Zz = fmaf(dw[2][4] * c, gp.z, Zz);
-        }
-    }
-    D[0] = X; D[1] = Yx; D[2] = Yy; D[3] = Zx; D[4] = Zy; D[5] = Zz;
-    return true;
-}
-
 __device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, double x, double y, double z, float* out3,
                                          unsigned long long* st)
 {
-    const float idl = __int_as_float((127 + here.level - kLevelShift - 1) << 23);   // 1 / dl, exact
-    float dxx, dxy, dxz, dyy, dyz, dzz;
-    float D[6];
-    if (jac_fused(T, here, D)) {
-        stat(st, ST_JAC_REC);
-        dxx = D[0] * idl; dxy = D[1] * idl; dyy = D[2] * idl; dxz = D[3] * idl; dyz = D[4] * idl; dzz = D[5] * idl;
-    } else {
-        // dl = 2^-(level - 1 - log2 EXTENT) (lensing.h:430); h = dl / 2 = one cell of the point's level
-        const double h = pow2(kLevelShift - here.level);
-        float g[6][3];
+    // dl = 2^-(level - 1 - log2 EXTENT) (lensing.h:430); h = dl / 2 = one cell of the point's level
+    const double h = pow2(kLevelShift - here.level);
+    float g[6][3];
 #pragma unroll 1
-        for (int a = 0; a < 6; ++a) {
-            const int ax = a >> 1;
-            const int sgn = (a & 1) ? 1 : -1;
-            const double moved = ((ax == 0) ? x : (ax == 1) ? y : z) + ((a & 1) ? h : -h);
-            const double qx = (ax == 0) ? moved : x, qy = (ax == 1) ? moved : y, qz = (ax == 2) ? moved : z;
-            const Loc d = step_cell(T, here, ax, sgn, qx, qy, qz);
-            const Field7 f = gather_at<2>(T, d, PosAt{qx, qy, qz}, false, st, ST_JAC_REC, false);
-            g[a][0] = f.dx; g[a][1] = f.dy; g[a][2] = f.dz;
-        }
-        dxx = (g[1][0] - g[0][0]) * idl; dxy = (g[3][0] - g[2][0]) * idl; dxz = (g[5][0] - g[4][0]) * idl;
-        dyy = (g[3][1] - g[2][1]) * idl; dyz = (g[5][1] - g[4][1]) * idl; dzz = (g[5][2] - g[4][2]) * idl;
+    for (int a = 0; a < 6; ++a) {
+        const int ax = a >> 1;
+        const int sgn = (a & 1) ? 1 : -1;
+        const double moved = ((ax == 0) ? x : (ax == 1) ? y : z) + ((a & 1) ? h : -h);
+        const double qx = (ax == 0) ? moved : x, qy = (ax == 1) ? moved : y, qz = (ax == 2) ? moved : z;
+        const Loc d = step_cell(T, here, ax, sgn, qx, qy, qz);
+        const Field7 f = gather_at<2>(T, d, PosAt{qx, qy, qz}, false, st, ST_JAC_REC, false);
+        g[a][0] = f.dx; g[a][1] = f.dy; g[a][2] = f.dz;
     }
+    const float idl = __int_as_float((127 + here.level - kLevelShift - 1) << 23);   // 1 / dl, exact
+    const float dxx = (g[1][0] - g[0][0]) * idl, dxy = (g[3][0] - g[2][0]) * idl, dxz = (g[5][0] - g[4][0]) * idl;
+    const float dyy = (g[3][1] - g[2][1]) * idl, dyz = (g[5][1] - g[4][1]) * idl, dzz = (g[5][2] - g[4][2]) * idl;
     const float fx = (float)x, fy = (float)y, fz = (float)z;
     const float rho = sqrtf(fx * fx + fy * fy);
     const float r = sqrtf(fx * fx + fy * fy + fz * fz);
