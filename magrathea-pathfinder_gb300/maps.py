@@ -18,16 +18,18 @@ F = {k: i for i, k in enumerate("firstid f x y z distance A11 A12 A22 t a redshi
                                  "valid".split())}
 
 
-def nmaps(components) -> int:
-    return sum(ROWS.get(c, 1) for c in components)
+def nmaps(components, bundle: bool = False) -> int:
+    return sum((5 if bundle else 4) if c == "lensing" else ROWS.get(c, 1) for c in components)
 
 
-def assemble(planes: np.ndarray, directions: np.ndarray, homogeneous: np.ndarray, components) -> np.ndarray:
+def assemble(planes: np.ndarray, directions: np.ndarray, homogeneous: np.ndarray, components,
+             bundle_jac: np.ndarray = None) -> np.ndarray:
     """planes: [npix, nz, 20]; directions: [npix, 3] launch directions;
-    homogeneous: [nz, 5] = t, chi, lambda, a, z of the FLRW ray at each surface.
-    Returns float32 maps [nz, nmaps, npix]."""
+    homogeneous: [nz, 5] = t, chi, lambda, a, z of the FLRW ray at each surface;
+    bundle_jac: [npix, nz, 4] (a11 a12 a21 a22) of the bundle Jacobian, or None
+    for the infinitesimal one.  Returns float32 maps [nz, nmaps, npix]."""
     npix, nz = planes.shape[0], planes.shape[1]
-    out = np.zeros((nz, nmaps(components), npix), dtype=np.float32)
+    out = np.zeros((nz, nmaps(components, bundle_jac is not None), npix), dtype=np.float32)
     ph = np.arctan2(directions[:, 1], directions[:, 0])
     th = np.arccos(directions[:, 2])
     for iz in range(nz):
@@ -35,7 +37,15 @@ def assemble(planes: np.ndarray, directions: np.ndarray, homogeneous: np.ndarray
         valid = p[:, F["valid"]] > 0
         rows = []
         for c in components:
-            if c == "lensing":
+            if c == "lensing" and bundle_jac is not None:
+                # hmaps.h:725-747: image rotation w, then kappa, gamma1, gamma2, w, 1/mu;
+                # a Jacobian flagged 42 zeroes the whole surface
+                b11, b12, b21, b22 = (bundle_jac[:, iz, q] for q in range(4))
+                valid = valid & (b11 != 42)
+                w = -np.arctan2(b12 - b21, b11 + b22)
+                rows += [1 - (b11 + b22) * 0.5 / np.cos(w), -0.5 * (np.cos(w) * (b11 - b22) + np.sin(w) * (b12 + b21)),
+                         -0.5 * (np.cos(w) * (b12 + b21) + np.sin(w) * (b22 - b11)), w, b11 * b22 - b12 * b21]
+            elif c == "lensing":
                 a11, a12, a22 = p[:, F["A11"]], p[:, F["A12"]], p[:, F["A22"]]
                 rows += [1 - (a11 + a22) * 0.5, -0.5 * (a11 - a22), -a12, a11 * a22 - a12 * a12]
             elif c == "dr":

@@ -932,6 +932,199 @@ int mpfo_catalogue(const mpfo_tree* T, const mpfo_cosmo* C, int order, double le
     return 0;
 }
 
+/* ---------------------------------------------------------------------- */
+/* bundle Jacobian                                                         */
+/* ---------------------------------------------------------------------- */
+static double plane_dot(const double* p, const double* ki) { return p[PX] * ki[0] + p[PY] * ki[1] + p[PZ] * ki[2]; }
+
+/* Lensing::dbetadtheta (lensing.h:148-336) for one central direction: four
+ * rays on a screen at +-tan(openingmin), integrated with the stop_bundle
+ * criterion to the last surface value, their crossings of every surface and
+ * the finite-difference Jacobian projected on the screen of kiTargets[iref].
+ * J: np x 4 (a11 a12 a21 a22), value-initialised to 0 as the reference's. */
+static void dbetadtheta(ctx_t* c, traj_t* tr, unsigned nsteps, int stop_bundle, double openingmin, int np,
+                        const double* ki /* np x 3 */, const double* iref_v, const double* dist, double phiInit,
+                        double thetaInit, double* J)
+{
+    for (int i = 0; i < 4 * np; ++i) J[i] = 0.0;
+    double* fp = (double*)calloc((size_t)np * 12, sizeof(double));   /* [iref][ray][3] */
+    const double cp = cos(phiInit), sp = sin(phiInit), ct = cos(thetaInit), st = sin(thetaInit);
+    double target[3], e1[3], e2[3], rini[4][3];
+    target[0] = cp * st; target[1] = sp * st; target[2] = ct;
+    e1[0] = -sp; e1[1] = cp; e1[2] = 0;
+    e2[0] = -cp * ct; e2[1] = -sp * ct; e2[2] = st;
+    const double to = tan(openingmin);
+    rini[0][0] = target[0] + to * e1[0]; rini[0][1] = target[1] + to * e1[1]; rini[0][2] = target[2];
+    rini[1][0] = target[0] - to * e1[0]; rini[1][1] = target[1] - to * e1[1]; rini[1][2] = target[2];
+    rini[2][0] = target[0] - to * e2[0]; rini[2][1] = target[1] - to * e2[1]; rini[2][2] = target[2] - to * e2[2];
+    rini[3][0] = target[0] + to * e2[0]; rini[3][1] = target[1] + to * e2[1]; rini[3][2] = target[2] + to * e2[2];
+    const int q = stop_quantity(stop_bundle);
+    for (int r = 0; r < 4; ++r) {
+        const double L[6] = {0, 0, 0, rini[r][0], rini[r][1], rini[r][2]};
+        tr->n = 0;
+        launch6(L, traj_push(tr));
+        integrate(c, tr, nsteps, stop_bundle, iref_v[np - 1], ki + 3 * (np - 1));
+        const double* back = tr->p + MPFO_PHOTON * (tr->n - 1);
+        for (int i = 0; i < np; ++i) {
+            int fail;
+            if (stop_bundle == MPFO_STOP_A) fail = back[PA] > iref_v[i];
+            else if (stop_bundle == MPFO_STOP_PLANE) fail = plane_dot(back, ki + 3 * i) < iref_v[i];
+            else fail = back[q] < iref_v[i];
+            if (fail) {
+                if (stop_bundle == MPFO_STOP_A) {
+                    J[4 * i + 0] = 42; J[4 * i + 1] = 42; J[4 * i + 2] = 1; J[4 * i + 3] = 3;
+                } else {
+                    for (int k = 0; k < np; ++k) { J[4 * k + 0] = 42; J[4 * k + 1] = 42; J[4 * k + 2] = 1; J[4 * k + 3] = 0; }
+                }
+                free(fp);
+                return;
+            }
+            int64_t marked;
+            double next, previous;
+            if (stop_bundle == MPFO_STOP_PLANE) {
+                int64_t first = 0, count = tr->n;   /* upper_bound with val < x . ki */
+                while (count > 0) {
+                    const int64_t step = count / 2, it = first + step;
+                    if (!(iref_v[i] < plane_dot(tr->p + MPFO_PHOTON * it, ki + 3 * i))) { first = it + 1; count -= step + 1; }
+                    else count = step;
+                }
+                marked = first;
+            } else {
+                marked = upper_by(tr, q, iref_v[i], stop_bundle == MPFO_STOP_A);
+            }
+            const int64_t fid = marked - (marked > 0);
+            const double* P0 = tr->p + MPFO_PHOTON * fid;
+            const double* P1 = P0 + MPFO_PHOTON;
+            if (stop_bundle == MPFO_STOP_PLANE) {
+                next = plane_dot(P1, ki + 3 * i);
+                previous = plane_dot(P0, ki + 3 * i);
+            } else {
+                next = P1[q];
+                previous = P0[q];
+            }
+            const double f = (next - iref_v[i]) / (next - previous);
+            double* o = fp + 12 * i + 3 * r;
+            o[0] = P0[PX] * f + P1[PX] * (1 - f);
+            o[1] = P0[PY] * f + P1[PY] * (1 - f);
+            o[2] = P0[PZ] * f + P1[PZ] * (1 - f);
+        }
+    }
+    for (int i = 0; i < np; ++i) {
+        const double* f0 = fp + 12 * i;
+        double rh[3], rv[3];
+        for (int d = 0; d < 3; ++d) {
+            rh[d] = f0[0 + d] - f0[3 + d];
+            rv[d] = f0[6 + d] - f0[9 + d];
+        }
+        const double kx = ki[3 * i], ky = ki[3 * i + 1], kz = ki[3 * i + 2];
+        const double phik = atan2(ky, kx);
+        const double thetak = acos(kz / sqrt(kx * kx + ky * ky + kz * kz));
+        const double cpk = cos(phik), spk = sin(phik), ctk = cos(thetak), stk = sin(thetak);
+        double a1[3], a2[3];
+        a1[0] = -spk; a1[1] = cpk; a1[2] = 0;
+        a2[0] = -cpk * ctk; a2[1] = -spk * ctk; a2[2] = stk;
+        J[4 * i + 0] = (rh[0] * a1[0] + rh[1] * a1[1]) / (2 * dist[i] * to);
+        J[4 * i + 1] = (rv[0] * a1[0] + rv[1] * a1[1]) / (2 * dist[i] * to);
+        J[4 * i + 2] = (rh[0] * a2[0] + rh[1] * a2[1] + rh[2] * a2[2]) / (-2 * dist[i] * to);
+        J[4 * i + 3] = (rv[0] * a2[0] + rv[1] * a2[1] + rv[2] * a2[2]) / (-2 * dist[i] * to);
+    }
+    free(fp);
+}
+
+typedef struct {
+    const mpfo_tree* T;
+    const mpfo_cosmo* C;
+    int order, stop_kind, np, plane_sachs, stop_bundle;
+    double length, openingmin;
+    unsigned nsteps;
+    const double* launch;
+    const double* planes;
+    double* plane_out;
+    double* jac_out;
+    int64_t n, next;
+    pthread_mutex_t mu;
+} bjob_t;
+
+static void* bworker(void* arg)
+{
+    bjob_t* J = (bjob_t*)arg;
+    ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+    traj_t tr = {0, 0, 0}, trb = {0, 0, 0};
+    const int np = J->np;
+    double* ki = (double*)malloc(sizeof(double) * 3 * (size_t)np);
+    double* iv = (double*)malloc(sizeof(double) * (size_t)np);
+    double* dist = (double*)malloc(sizeof(double) * (size_t)np);
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        const int64_t i = J->next++;
+        pthread_mutex_unlock(&J->mu);
+        if (i >= J->n) break;
+        c->T = J->T; c->C = J->C; c->order = J->order; c->length = J->length;
+        cache_init(&c->cache);
+        const double* L = J->launch + 6 * i;
+        tr.n = 0;
+        launch6(L, traj_push(&tr));
+        integrate(c, &tr, J->nsteps, J->stop_kind, J->planes[np - 1], (const double[3]){0, 0, 0});
+        double* po = J->plane_out + (int64_t)MPFO_PLANE * np * i;
+        planes_of(c, &tr, J->stop_kind, np, J->planes, 0, po);
+        /* FillMap's targets for the bundle (hmaps.h:653-693) */
+        for (int s = 0; s < np; ++s) {
+            const double* o = po + MPFO_PLANE * s;
+            const int64_t fid = (int64_t)o[0];
+            const double f = o[1];
+            const int ok = fid + 1 < tr.n;
+            double* k = ki + 3 * s;
+            if (J->plane_sachs && ok) {
+                const double* P0 = tr.p + MPFO_PHOTON * fid;
+                const double* P1 = P0 + MPFO_PHOTON;
+                k[0] = P0[PK1] * f + P1[PK1] * (1 - f);
+                k[1] = P0[PK2] * f + P1[PK2] * (1 - f);
+                k[2] = P0[PK3] * f + P1[PK3] * (1 - f);
+            } else {
+                k[0] = o[2]; k[1] = o[3]; k[2] = o[4];
+            }
+            dist[s] = o[5];
+            switch (J->stop_bundle) {
+            case MPFO_STOP_LAMBDA: iv[s] = o[13]; break;
+            case MPFO_STOP_R: iv[s] = o[12]; break;
+            case MPFO_STOP_REDSHIFT: iv[s] = o[11]; break;
+            case MPFO_STOP_A: iv[s] = o[10]; break;
+            case MPFO_STOP_T: iv[s] = o[9]; break;
+            default: iv[s] = k[0] * o[2] + k[1] * o[3] + k[2] * o[4]; break;
+            }
+        }
+        const double phi = atan2(L[4], L[3]);
+        const double theta = acos(L[5]);
+        dbetadtheta(c, &trb, J->nsteps, J->stop_bundle, J->openingmin, np, ki, iv, dist, phi, theta,
+                    J->jac_out + 4 * (int64_t)np * i);
+    }
+    free(ki); free(iv); free(dist);
+    free(tr.p); free(trb.p);
+    free(c);
+    return 0;
+}
+
+int mpfo_bundle(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps, int stop_kind,
+                int64_t n, const double* launch, int np, const double* planes, int plane_sachs, int stop_bundle,
+                double openingmin, double* plane_out, double* jac_out, int nthreads)
+{
+    if (!T || !C || (order != 1 && order != 2) || nsteps == 0 || n < 0 || np < 1 || !planes) return -1;
+    bjob_t J;
+    J.T = T; J.C = C; J.order = order; J.stop_kind = stop_kind; J.np = np; J.plane_sachs = plane_sachs;
+    J.stop_bundle = stop_bundle; J.length = length; J.openingmin = openingmin; J.nsteps = nsteps;
+    J.launch = launch; J.planes = planes; J.plane_out = plane_out; J.jac_out = jac_out; J.n = n; J.next = 0;
+    pthread_mutex_init(&J.mu, 0);
+    if (nthreads <= 1) bworker(&J);
+    else {
+        pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+        for (int t = 0; t < nthreads; ++t) pthread_create(&th[t], 0, bworker, &J);
+        for (int t = 0; t < nthreads; ++t) pthread_join(th[t], 0);
+        free(th);
+    }
+    pthread_mutex_destroy(&J.mu);
+    return 0;
+}
+
 typedef struct {
     const mpfo_tree* T;
     int64_t n;

@@ -78,6 +78,15 @@ int mpfo_catalogue(const mpfo_tree* T, const mpfo_cosmo* C, int order, double le
                    int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
                    double h, double mpc, int max_iterations, double* out, int nthreads);
 
+/* Hmaps::FillMap with jacobiantype = "bundle": the central rays' surfaces
+ * (plane_out, n x np x 20 as mpfo_propagate, without the infinitesimal
+ * Jacobian) and Lensing::dbetadtheta's 2x2 Jacobian at each surface (jac_out,
+ * n x np x 4: a11 a12 a21 a22).  plane_sachs: kiTarget = interpolated
+ * direction (1) or position (0); stop_bundle: an MPFO_STOP_* value. */
+int mpfo_bundle(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps, int stop_kind,
+                int64_t n, const double* launch, int np, const double* planes, int plane_sachs, int stop_bundle,
+                double openingmin, double* plane_out, double* jac_out, int nthreads);
+
 void mpfo_batch_locate(const mpfo_tree* T, int64_t n, const double* xyz, int64_t* out, int nthreads);
 void mpfo_batch_cic(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads);
 void mpfo_batch_tsc(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads);

@@ -62,6 +62,9 @@ def lib():
                                      C.c_int, _p, _p, _p, C.c_int]
         L.mpfo_trajectory.restype = _i64
         L.mpfo_trajectory.argtypes = [_p, _p, C.c_int, _d, C.c_uint, C.c_int, _d, _p, _p, _i64]
+        L.mpfo_bundle.restype = C.c_int
+        L.mpfo_bundle.argtypes = [_p, _p, C.c_int, _d, C.c_uint, C.c_int, _i64, _p, C.c_int, _p, C.c_int, C.c_int, _d,
+                                  _p, _p, C.c_int]
         L.mpfo_catalogue.restype = C.c_int
         L.mpfo_catalogue.argtypes = [_p, _p, C.c_int, _d, C.c_uint, _i64, _p, _p, _p, _d, _d, _d, C.c_int, _p,
                                      C.c_int]
@@ -151,3 +154,18 @@ class Oracle:
         if rc != 0:
             raise ValueError("oracle catalogue failed: %d" % rc)
         return out
+
+    def bundle(self, launch, planes, order=2, nsteps=10, stop="redshift", plane="sachs", stop_bundle="redshift",
+               openingmin=0.0, nthreads=None):
+        """FillMap with the bundle Jacobian: (surface records n x np x 20, Jacobians n x np x 4)."""
+        launch = np.ascontiguousarray(launch, dtype=np.float64)
+        pl = np.ascontiguousarray(planes, dtype=np.float64)
+        n, npl = launch.shape[0], pl.shape[0]
+        pout = np.zeros((n, npl, 20))
+        jac = np.zeros((n, npl, 4))
+        rc = self.L.mpfo_bundle(C.byref(self.tree), C.byref(self.cosmo), order, self.length, nsteps, STOP[stop], n,
+                                _ptr(launch), npl, _ptr(pl), 1 if plane == "sachs" else 0, STOP[stop_bundle],
+                                float(openingmin), _ptr(pout), _ptr(jac), int(nthreads or self.nthreads))
+        if rc != 0:
+            raise ValueError("oracle bundle failed: %d" % rc)
+        return pout, jac

@@ -329,16 +329,19 @@ int ref_homogeneous(int nz, const double* zs, double* out)
 // (a comma list among dr dl dt da dz ds isw dens dens_max steps phi
 // deflection), one ray per pixel of `pixels`.  maps: nmaps*nz rows of npix
 // floats, row-major, the layout of the reference's map vector.
-int ref_fillmap(long nside, int nz, const double* zvals, const char* stop_ray, const char* comps, unsigned nsteps,
-                int64_t npixels, const long* pixels, float* maps, int* nmaps_out)
+int ref_fillmap_jac(long nside, int nz, const double* zvals, const char* stop_ray, const char* comps, unsigned nsteps,
+                    int64_t npixels, const long* pixels, float* maps, int* nmaps_out, const char* jacobiantype,
+                    const char* plane, const char* stop_bundle, double openingmin)
 {
     parameters.nside = nside;
     parameters.nb_z_maps = nz;
     parameters.nsteps = nsteps;
     parameters.stop_ray = stop_ray;
-    parameters.jacobiantype = "infinitesimal";
-    parameters.plane = "normal";
-    parameters.stop_bundle = "redshift";
+    parameters.jacobiantype = jacobiantype;
+    parameters.plane = plane;
+    parameters.stop_bundle = stop_bundle;
+    parameters.openingmin = openingmin;
+    const bool bundle = parameters.jacobiantype == "bundle";
     parameters.map_components = comps;
     std::vector<std::string> map_components;
     {
@@ -358,7 +361,7 @@ int ref_fillmap(long nside, int nz, const double* zvals, const char* stop_ray, c
         auto it = ids.find(map_components[i]);
         if (it == ids.end() || it->second == 1) return -1;
         index_components[i] = it->second;
-        nmaps += (it->second == 0) ? 4 : (it->second == 13 ? 2 : 1);
+        nmaps += (it->second == 0) ? (bundle ? 5 : 4) : (it->second == 13 ? 2 : 1);
     }
     *nmaps_out = (int)nmaps;
     std::vector<double> hom(5 * (size_t)nz);
@@ -389,6 +392,13 @@ int ref_fillmap(long nside, int nz, const double* zvals, const char* stop_ray, c
     for (size_t r = 0; r < map.size(); ++r)
         for (int64_t k = 0; k < npixels; ++k) maps[r * npixels + k] = map[r][pix[k]];
     return 0;
+}
+
+int ref_fillmap(long nside, int nz, const double* zvals, const char* stop_ray, const char* comps, unsigned nsteps,
+                int64_t npixels, const long* pixels, float* maps, int* nmaps_out)
+{
+    return ref_fillmap_jac(nside, nz, zvals, stop_ray, comps, nsteps, npixels, pixels, maps, nmaps_out, "infinitesimal",
+                           "normal", "redshift", 0.0);
 }
 
 void ref_pix2vec_ring(long nside, int64_t n, const long* pix, double* vec)

@@ -61,6 +61,9 @@ def lib(order: int = 2):
         L.ref_homogeneous.argtypes = [C.c_int, _p, _p]
         L.ref_fillmap.restype = C.c_int
         L.ref_fillmap.argtypes = [C.c_long, C.c_int, _p, C.c_char_p, C.c_char_p, C.c_uint, _i64, _p, _p, _p]
+        L.ref_fillmap_jac.restype = C.c_int
+        L.ref_fillmap_jac.argtypes = [C.c_long, C.c_int, _p, C.c_char_p, C.c_char_p, C.c_uint, _i64, _p, _p, _p,
+                                      C.c_char_p, C.c_char_p, C.c_char_p, _d]
         L.ref_pix2vec_ring.argtypes = [C.c_long, _i64, _p, _p]
         L.ref_catalogue.argtypes = [_i64, _p, _p, _p, _d, C.c_uint, _d, _d, _p, C.c_int]
         _LIBS[order] = L
@@ -154,14 +157,16 @@ class Reference:
             raise RuntimeError("homogeneous quantities failed")
         return out
 
-    def fillmap(self, nside, zs, pixels, stop_ray="redshift", comps="lensing", nsteps=10):
+    def fillmap(self, nside, zs, pixels, stop_ray="redshift", comps="lensing", nsteps=10, jacobiantype="infinitesimal",
+                plane="normal", stop_bundle="redshift", openingmin=0.0):
         zs = np.ascontiguousarray(zs, dtype=np.float64)
         pix = np.ascontiguousarray(pixels, dtype=np.int64)
         nmaps_guess = 32
         maps = np.zeros(nmaps_guess * zs.shape[0] * pix.shape[0], dtype=np.float32)
         nm = C.c_int(0)
-        rc = self.L.ref_fillmap(nside, zs.shape[0], _ptr(zs), stop_ray.encode(), comps.encode(), nsteps,
-                                pix.shape[0], _ptr(pix), _ptr(maps), C.byref(nm))
+        rc = self.L.ref_fillmap_jac(nside, zs.shape[0], _ptr(zs), stop_ray.encode(), comps.encode(), nsteps,
+                                    pix.shape[0], _ptr(pix), _ptr(maps), C.byref(nm), jacobiantype.encode(),
+                                    plane.encode(), stop_bundle.encode(), float(openingmin))
         if rc != 0:
             raise RuntimeError("ref_fillmap failed: %d" % rc)
         return maps[: nm.value * zs.shape[0] * pix.shape[0]].reshape(zs.shape[0], nm.value, pix.shape[0])

@@ -11,7 +11,9 @@ the reference derived from its evolution file (Input::acquire + correct), and
 the reference's outputs: locate / cic / tsc at random points, per-ray step
 counts and final photon records (Integrator::integrate), FillMap maps, and
 catalogue rows (Catalogues::iterateNewtonMethod through relCat's per-source
-setup) for seeded sources at three accuracies, with and without a rotation.
+setup) for seeded sources at three accuracies, with and without a rotation,
+and FillMap maps with the bundle Jacobian (Lensing::dbetadtheta) for two
+screen / stop_bundle choices.
 """
 from __future__ import annotations
 
@@ -52,6 +54,9 @@ def cone_pixels(R, nside, half_deg):
     return allp[sel]
 
 
+# bundle Jacobian (jacobiantype = bundle): screen plane and stop_bundle pairs, opening 0.2 arcmin
+BUNDLES = (("sachs", "redshift"), ("normal", "r"))
+OPENING = 0.2 / 60.0 * 3.141592653589793 / 180.0
 CAT_ACCURACIES = (1e-8, 1e-13, 0.0)   # job default; deep enough for the Jacobian steps; never met (rejects)
 CAT_VOBS = (1e-4, -2e-4, 5e-5)
 
@@ -125,6 +130,9 @@ def make(name, cfg):
         out["pixels"] = pix
         out["pixel_dirs"] = R.pix2vec(cfg["nside"], pix)
         out["ref_maps_o%d" % order] = R.fillmap(cfg["nside"], out["zs"], pix, "redshift", COMPONENTS, cfg["nsteps"])
+        for plane, sb in BUNDLES:
+            out["ref_maps_bundle_o%d_%s_%s" % (order, plane, sb)] = R.fillmap(
+                cfg["nside"], out["zs"], pix, "redshift", COMPONENTS, cfg["nsteps"], "bundle", plane, sb, OPENING)
         if order == 1:
             crng = np.random.default_rng(23)
             src = catalogue_sources(crng, 40, spec.chi_max / spec.lbox)

@@ -52,6 +52,28 @@ def test_oracle_maps_bit_exact(golden, oracle_mod, maps_mod, order):
     np.testing.assert_array_equal(maps.view(np.uint32), ref.view(np.uint32))
 
 
+BUNDLES = (("sachs", "redshift"), ("normal", "r"))
+OPENING = 0.2 / 60.0 * 3.141592653589793 / 180.0
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("plane,stop_bundle", BUNDLES)
+def test_oracle_bundle_maps_bit_exact(golden, oracle_mod, maps_mod, order, plane, stop_bundle):
+    """FillMap with jacobiantype = bundle (Lensing::dbetadtheta): the oracle's
+    surfaces and four-ray Jacobians, assembled into maps, equal the reference's."""
+    O = _oracle(golden, oracle_mod)
+    dirs = golden["pixel_dirs"]
+    launch = np.zeros((dirs.shape[0], 6))
+    launch[:, 3:] = dirs
+    planes, jac = O.bundle(launch, golden["zs"], order=order, nsteps=int(golden["nsteps"]), stop="redshift",
+                           plane=plane, stop_bundle=stop_bundle, openingmin=OPENING)
+    comps = str(golden["components"]).split(",")
+    maps = maps_mod.assemble(planes, dirs, golden["homogeneous"], comps, bundle_jac=jac)
+    ref = golden["ref_maps_bundle_o%d_%s_%s" % (order, plane, stop_bundle)]
+    assert maps.shape == ref.shape
+    np.testing.assert_array_equal(maps.view(np.uint32), ref.view(np.uint32))
+
+
 @pytest.mark.parametrize("order", [1, 2])
 def test_oracle_catalogue_bit_exact(golden, oracle_mod, order):
     """Catalogue rows (Newton root-finder) of the C oracle == the reference's
