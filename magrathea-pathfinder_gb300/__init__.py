@@ -198,24 +198,33 @@ def catalogue_stats(st) -> dict:
 
 def hmaps_fill(octree: Octree, cosmology: Cosmology, nside: int, pixels, surfaces, homogeneous, components,
                length: float, nsteps: int = 10, order: int = 2, stop: str = "redshift", exact: bool = False,
-               max_steps: int = 0):
+               max_steps: int = 0, jacobian: str = "infinitesimal", plane: str = "sachs",
+               stop_bundle: str = "redshift", openingmin: float = 0.0):
     """Hmaps::FillMap for the given RING pixels: float maps [nsurfaces, nmaps, npix].
 
     surfaces: the stop-quantity values of the map surfaces (interpRefvec);
     homogeneous: [nsurfaces, 5] = t, chi, lambda, a, z of the FLRW ray there;
-    components: the reference's map component names, in order.
+    components: the reference's map component names, in order;
+    jacobian: "infinitesimal" or "bundle" (then plane, stop_bundle and
+    openingmin, in radians, as the reference's parameters).
     """
     L = capi.load()
     pix = np.ascontiguousarray(pixels, dtype=np.int64)
     comps = [capi.MAP_COMPONENTS[c] for c in components]
-    nm = sum(4 if c == 0 else 2 if c == 13 else 1 for c in comps)
+    bundle = jacobian == "bundle"
+    nm = sum((5 if bundle else 4) if c == 0 else 2 if c == 13 else 1 for c in comps)
     p, keep = capi.make_params(length, nsteps, order, stop, 0.0, surfaces, True, exact, max_steps)
     hom = np.ascontiguousarray(homogeneous, dtype=np.float64).reshape(-1, 5)
     cc = np.ascontiguousarray(comps, dtype=np.int32)
     nz = p.nplanes
     maps = np.zeros((nz, nm, pix.shape[0]), dtype=np.float32)
-    rc = L.mpf_hmaps_fill(octree._h, cosmology._h, C.byref(p), int(nside), pix.shape[0], capi.ptr(pix), len(comps),
-                          capi.ptr(cc), capi.ptr(hom), capi.ptr(maps))
+    if bundle:
+        rc = L.mpf_hmaps_fill_bundle(octree._h, cosmology._h, C.byref(p), int(nside), pix.shape[0], capi.ptr(pix),
+                                     len(comps), capi.ptr(cc), capi.ptr(hom), 1 if plane == "sachs" else 0,
+                                     capi.STOP[stop_bundle], float(openingmin), capi.ptr(maps))
+    else:
+        rc = L.mpf_hmaps_fill(octree._h, cosmology._h, C.byref(p), int(nside), pix.shape[0], capi.ptr(pix),
+                              len(comps), capi.ptr(cc), capi.ptr(hom), capi.ptr(maps))
     capi.check(rc)
     del keep
     return maps

@@ -27,7 +27,7 @@ EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_uplo
            "mpf_octree_get_info", "mpf_octree_destroy", "mpf_cosmology_upload", "mpf_cosmology_destroy", "mpf_locate",
            "mpf_interpolate", "mpf_propagate", "mpf_propagate_device", "mpf_propagate_noalloc",
            "mpf_noalloc_last_error", "mpf_catalogue_newton",
-           "mpf_catalogue_newton_device", "mpf_hmaps_fill", "mpf_pix2vec_ring")
+           "mpf_catalogue_newton_device", "mpf_hmaps_fill", "mpf_hmaps_fill_bundle", "mpf_pix2vec_ring")
 
 # map component names (the reference's map_components keys) -> mpf_map_component
 MAP_COMPONENTS = {"lensing": 0, "dr": 2, "dl": 3, "dt": 4, "da": 5, "dz": 6, "ds": 7, "isw": 8, "dens": 9,
@@ -99,6 +99,8 @@ def load(path: str = LIB_PATH):
     L.mpf_catalogue_newton_device.argtypes = [vp, vp, C.POINTER(CatalogueParams), i64, vp, i64, vp,
                                               C.POINTER(CatalogueStats), vp]
     L.mpf_hmaps_fill.argtypes = [vp, vp, C.POINTER(Params), i64, i64, vp, C.c_int, vp, vp, vp]
+    L.mpf_hmaps_fill_bundle.argtypes = [vp, vp, C.POINTER(Params), i64, i64, vp, C.c_int, vp, vp, C.c_int, C.c_int, d,
+                                        vp]
     L.mpf_pix2vec_ring.argtypes = [i64, i64, vp, vp]
     for name in EXPORTS:
         if name not in ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_destroy",

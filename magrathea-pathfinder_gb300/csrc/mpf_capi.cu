@@ -357,8 +357,10 @@ int mpf_catalogue_newton(const mpf_octree* o, const mpf_cosmology* c, const mpf_
     return rc;
 }
 
-int mpf_hmaps_fill(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t nside, int64_t npix,
-                   const int64_t* pixels, int ncomp, const int* components, const double* homogeneous, float* maps)
+namespace {
+int hmaps_fill_impl(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t nside, int64_t npix,
+                    const int64_t* pixels, int ncomp, const int* components, const double* homogeneous, float* maps,
+                    int bundle, int plane_sachs, int stop_bundle, double openingmin)
 {
     mpf::PropParams P;
     if (!o || !c || !fill_params(p, P) || npix < 0 || (npix > 0 && (!pixels || !maps)) || nside < 1 ||
@@ -374,7 +376,17 @@ int mpf_hmaps_fill(const mpf_octree* o, const mpf_cosmology* c, const mpf_params
         if (k < 0 || k > 13 || k == 1)
             return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill: unknown map component (lensing_born is not built)");
         M.comp[q] = k;
-        M.nmaps += (k == MPF_MAP_LENSING) ? 4 : (k == MPF_MAP_DEFLECTION) ? 2 : 1;
+        M.nmaps += (k == MPF_MAP_LENSING) ? (bundle ? 5 : 4) : (k == MPF_MAP_DEFLECTION) ? 2 : 1;
+    }
+    if (bundle) {
+        if (stop_bundle < 0 || stop_bundle > 6 || stop_bundle == MPF_STOP_PLANE || stop_bundle == MPF_STOP_S ||
+            !(openingmin > 0.0) || !(openingmin < 1.0))
+            return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill_bundle: stop_bundle must be redshift, r, lambda, t or a, "
+                                          "and 0 < openingmin < 1 radian");
+        M.bundle = 1;
+        M.plane_sachs = plane_sachs ? 1 : 0;
+        M.stop_bundle = stop_bundle;
+        M.openingmin = openingmin;
     }
     for (int iz = 0; iz < p->nplanes; ++iz)
         for (int k = 0; k < 5; ++k) M.homogeneous[iz][k] = homogeneous[5 * iz + k];
@@ -397,6 +409,21 @@ int mpf_hmaps_fill(const mpf_octree* o, const mpf_cosmology* c, const mpf_params
     if (e != cudaSuccess) return cuda_err(e, "mpf_hmaps_fill");
     if (status & 1u) return set_err(MPF_WARN_MAX_STEPS, "mpf_hmaps_fill: a ray reached max_steps");
     return MPF_OK;
+}
+}  // namespace
+
+int mpf_hmaps_fill(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t nside, int64_t npix,
+                   const int64_t* pixels, int ncomp, const int* components, const double* homogeneous, float* maps)
+{
+    return hmaps_fill_impl(o, c, p, nside, npix, pixels, ncomp, components, homogeneous, maps, 0, 0, 0, 0.0);
+}
+
+int mpf_hmaps_fill_bundle(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t nside, int64_t npix,
+                          const int64_t* pixels, int ncomp, const int* components, const double* homogeneous,
+                          int plane_sachs, int stop_bundle, double openingmin, float* maps)
+{
+    return hmaps_fill_impl(o, c, p, nside, npix, pixels, ncomp, components, homogeneous, maps, 1, plane_sachs,
+                           stop_bundle, openingmin);
 }
 
 int mpf_pix2vec_ring(int64_t nside, int64_t n, const int64_t* pixels, double* vec)

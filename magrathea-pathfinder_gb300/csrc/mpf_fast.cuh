@@ -509,8 +509,9 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     const double inv_scale = 1.0 / scale;
     const int np = SRC ? 1 : P.nplanes;
     const int skind = SRC ? (int)STOP_R : P.stop_kind;
-    const double stop_ref = SRC ? P.ray_stop[i] : P.stop_ref;
-    const int rec_fields = SRC ? kSourceFields : kPlaneFields;
+    const double* rpl = (!SRC && P.ray_planes) ? P.ray_planes + i * np : P.planes;   // this ray's surfaces
+    const double stop_ref = SRC ? P.ray_stop[i] : (P.ray_planes ? rpl[np - 1] : P.stop_ref);
+    const int rec_fields = SRC ? kSourceFields : (P.wide ? kWideFields : kPlaneFields);
     unsigned long long* const st = O.stats;
     FastRec b;
     if (SRC) {
@@ -553,10 +554,10 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         prow[24] = b.a; prow[25] = b.phi; prow[26] = b.k1; prow[27] = b.k2; prow[28] = b.k3;
         prow[29] = prow[30] = prow[31] = 0.0;
     }
-    while (next_plane < np && ((skind == STOP_A) ? (b.a < (SRC ? stop_ref : P.planes[next_plane]))
+    while (next_plane < np && ((skind == STOP_A) ? (b.a < (SRC ? stop_ref : rpl[next_plane]))
                                                   : (((skind == STOP_R) ? b.chi : (skind == STOP_LAMBDA) ? b.lambda
                                                       : (skind == STOP_T) ? b.t : (skind == STOP_S) ? b.s : b.red) >
-                                                     (SRC ? stop_ref : P.planes[next_plane])))) {
+                                                     (SRC ? stop_ref : rpl[next_plane])))) {
         cross_k[next_plane] = 0;
         ++next_plane;
     }
@@ -670,7 +671,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                 const int kind = skind;
                 const double q1 = (kind == STOP_R) ? p.chi : (kind == STOP_LAMBDA) ? p.lambda : (kind == STOP_T) ? p.t
                                 : (kind == STOP_A) ? p.a : (kind == STOP_S) ? p.s : p.red;
-                const double ref = SRC ? stop_ref : P.planes[next_plane];
+                const double ref = SRC ? stop_ref : rpl[next_plane];
                 if (!((kind == STOP_A) ? (q1 < ref) : (q1 > ref))) break;
                 const int j = next_plane++;
                 cross_k[j] = k;
@@ -693,7 +694,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                     o[17] = b.phi * f + p.phi * (1 - f);
                     o[18] = have_rmax ? rmax : 0.0;
                     o[19] = 1.0;
-                    if (SRC) {
+                    if (SRC || P.wide) {
                         o[20] = b.k0 * f + p.k0 * (1 - f);
                         o[21] = b.k1 * f + p.k1 * (1 - f);
                         o[22] = b.k2 * f + p.k2 * (1 - f);
@@ -782,15 +783,16 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         prow[19] = ok ? 1.0 : 0.0;
     } else if (prow) {
         for (int j = 0; j < np; ++j) {
-            double* o = prow + j * kPlaneFields;
+            double* o = prow + j * rec_fields;
             const long long ck = cross_k[j];
             const bool found = (ck >= 1) && (ck < size);
             const bool valid = found && !((ck - 1) == size - 1 || (ck - 1) == 0);
             if (ck < 0 || ck == 0 || ck >= size) {
-                for (int q = 0; q < kPlaneFields; ++q) o[q] = 0.0;
+                for (int q = 0; q < (P.wide ? 24 : kPlaneFields); ++q) o[q] = 0.0;
                 o[0] = (ck == 0) ? 0.0 : (double)(size - 1);
             }
             o[19] = valid ? 1.0 : 0.0;
+            if (P.wide) o[24] = found ? 1.0 : 0.0;
         }
     }
     if (status) atomicOr(O.status, status);

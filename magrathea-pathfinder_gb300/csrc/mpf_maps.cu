@@ -63,17 +63,21 @@ __global__ void k_pix_launch(long long n, long long nside, const long long* __re
 }
 
 // One thread per (pixel, surface): the map rows of hmaps.h:716-829.
+// rec_fields: stride of the surface records; jac: the bundle Jacobians
+// (n x nz x 4: a11 a12 a21 a22) or null for the infinitesimal one.
 __global__ void k_fill_maps(long long n, int nz, MapSpec M, const double* __restrict__ launch,
-                            const double* __restrict__ rec, float* __restrict__ maps, long long row_stride,
-                            long long col0)
+                            const double* __restrict__ rec, int rec_fields, const double* __restrict__ jac,
+                            float* __restrict__ maps, long long row_stride, long long col0)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n * nz) return;
     const long long j = t % n;
     const int iz = (int)(t / n);
-    const double* o = rec + ((long long)j * nz + iz) * kPlaneFields;
+    const double* o = rec + ((long long)j * nz + iz) * rec_fields;
+    const double* bj = jac ? jac + ((long long)j * nz + iz) * 4 : nullptr;
     float* out = maps + (long long)M.nmaps * iz * row_stride + col0 + j;
-    if (o[19] == 0.0) {
+    // an unusable crossing, or a bundle Jacobian flagged 42, zeroes the surface (hmaps.h:719-738)
+    if (o[19] == 0.0 || (bj && bj[0] == 42.0)) {
         for (int r = 0; r < M.nmaps; ++r) out[(long long)r * row_stride] = 0.0f;
         return;
     }
@@ -82,6 +86,18 @@ __global__ void k_fill_maps(long long n, int nz, MapSpec M, const double* __rest
     for (int q = 0; q < M.ncomp; ++q) {
         switch (M.comp[q]) {
         case 0: {
+            if (bj) {
+                // bundle: image rotation w first (hmaps.h:725-733), five rows
+                const double a11 = bj[0], a12 = bj[1], a21 = bj[2], a22 = bj[3];
+                const double w = -atan2(a12 - a21, a11 + a22);
+                out[(long long)(row + 0) * row_stride] = (float)(1 - (a11 + a22) * 0.5 / cos(w));
+                out[(long long)(row + 1) * row_stride] = (float)(-0.5 * (cos(w) * (a11 - a22) + sin(w) * (a12 + a21)));
+                out[(long long)(row + 2) * row_stride] = (float)(-0.5 * (cos(w) * (a12 + a21) + sin(w) * (a22 - a11)));
+                out[(long long)(row + 3) * row_stride] = (float)w;
+                out[(long long)(row + 4) * row_stride] = (float)(a11 * a22 - a12 * a21);
+                row += 5;
+                break;
+            }
             const double a11 = o[6], a12 = o[7], a22 = o[8];
             out[(long long)(row + 0) * row_stride] = (float)(1 - (a11 + a22) * 0.5);
             out[(long long)(row + 1) * row_stride] = (float)(-0.5 * (a11 - a22));
@@ -117,6 +133,103 @@ __global__ void k_fill_maps(long long n, int nz, MapSpec M, const double* __rest
     }
 }
 
+// Bundle rays of each pixel (Lensing::dbetadtheta, lensing.h:160-196) and
+// their surfaces from the central ray's crossings (hmaps.h:653-693):
+// kiTargets (the interpolated direction, or position), the stop_bundle value
+// at each surface and the surface distance.
+__global__ void k_bundle_prepare(long long n, int nz, MapSpec M, const double* __restrict__ planes,
+                                 const double* __restrict__ launch, const double* __restrict__ rec,
+                                 double* __restrict__ blaunch, double* __restrict__ bplanes, double* __restrict__ ki,
+                                 double* __restrict__ dist)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    for (int iz = 0; iz < nz; ++iz) {
+        const double* o = rec + ((long long)j * nz + iz) * kWideFields;
+        double* k = ki + ((long long)j * nz + iz) * 3;
+        const bool found = o[24] != 0.0;
+        if (M.plane_sachs && found) {
+            k[0] = o[21]; k[1] = o[22]; k[2] = o[23];
+        } else {
+            k[0] = o[2]; k[1] = o[3]; k[2] = o[4];
+        }
+        dist[(long long)j * nz + iz] = o[5];
+        double v;
+        switch (M.stop_bundle) {
+        case STOP_LAMBDA: v = o[13]; break;
+        case STOP_R: v = o[12]; break;
+        case STOP_REDSHIFT: v = o[11]; break;
+        case STOP_A: v = o[10]; break;
+        case STOP_T: v = o[9]; break;
+        default: v = o[11];
+        }
+        // a surface the central ray never reached has no interpolated value
+        // (the reference reads past the trajectory there); its own value stands in
+        if (!found) v = planes[iz];
+        for (int r = 0; r < 4; ++r) bplanes[(4 * j + r) * nz + iz] = v;
+    }
+    // the screen around the pixel direction
+    const double* L = launch + 6 * j;
+    const double phi = atan2(L[4], L[3]), theta = acos(L[5]);
+    const double cp = cos(phi), sp = sin(phi), ct = cos(theta), st = sin(theta);
+    const double tx = cp * st, ty = sp * st, tz = ct;
+    const double e1x = -sp, e1y = cp;
+    const double e2x = -cp * ct, e2y = -sp * ct, e2z = st;
+    const double to = tan(M.openingmin);
+    double* B = blaunch + 24 * j;
+    for (int r = 0; r < 4; ++r) { B[6 * r] = 0.0; B[6 * r + 1] = 0.0; B[6 * r + 2] = 0.0; }
+    B[3] = tx + to * e1x; B[4] = ty + to * e1y; B[5] = tz;
+    B[9] = tx - to * e1x; B[10] = ty - to * e1y; B[11] = tz;
+    B[15] = tx - to * e2x; B[16] = ty - to * e2y; B[17] = tz - to * e2z;
+    B[21] = tx + to * e2x; B[22] = ty + to * e2y; B[23] = tz + to * e2z;
+}
+
+// Finite-difference Jacobian of the four bundle rays at each surface
+// (lensing.h:198-334).  A ray that ended before a surface flags the
+// Jacobians with 42 as the reference does (all surfaces; for stop_bundle =
+// "a" only that surface).
+__global__ void k_bundle_jacobian(long long n, int nz, MapSpec M, const double* __restrict__ brec,
+                                  const double* __restrict__ ki, const double* __restrict__ dist,
+                                  double* __restrict__ jac)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double* J = jac + (long long)j * nz * 4;
+    for (int q = 0; q < 4 * nz; ++q) J[q] = 0.0;
+    for (int r = 0; r < 4; ++r) {
+        for (int iz = 0; iz < nz; ++iz) {
+            if (brec[((4 * j + r) * nz + iz) * kWideFields + 24] != 0.0) continue;
+            if (M.stop_bundle == STOP_A) {
+                J[4 * iz] = 42; J[4 * iz + 1] = 42; J[4 * iz + 2] = 1; J[4 * iz + 3] = 3;
+            } else {
+                for (int q = 0; q < nz; ++q) { J[4 * q] = 42; J[4 * q + 1] = 42; J[4 * q + 2] = 1; J[4 * q + 3] = 0; }
+            }
+            return;
+        }
+    }
+    const double to = tan(M.openingmin);
+    for (int iz = 0; iz < nz; ++iz) {
+        const double* r0 = brec + ((4 * j + 0) * nz + iz) * kWideFields;
+        const double* r1 = brec + ((4 * j + 1) * nz + iz) * kWideFields;
+        const double* r2 = brec + ((4 * j + 2) * nz + iz) * kWideFields;
+        const double* r3 = brec + ((4 * j + 3) * nz + iz) * kWideFields;
+        double rh[3], rv[3];
+        for (int d = 0; d < 3; ++d) {
+            rh[d] = r0[2 + d] - r1[2 + d];
+            rv[d] = r2[2 + d] - r3[2 + d];
+        }
+        const double* k = ki + ((long long)j * nz + iz) * 3;
+        const double phik = atan2(k[1], k[0]);
+        const double thetak = acos(k[2] / sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]));
+        const double cpk = cos(phik), spk = sin(phik), ctk = cos(thetak), stk = sin(thetak);
+        const double d2 = 2 * dist[(long long)j * nz + iz] * to;
+        J[4 * iz + 0] = (rh[0] * -spk + rh[1] * cpk) / d2;
+        J[4 * iz + 1] = (rv[0] * -spk + rv[1] * cpk) / d2;
+        J[4 * iz + 2] = (rh[0] * (-cpk * ctk) + rh[1] * (-spk * ctk) + rh[2] * stk) / (-d2);
+        J[4 * iz + 3] = (rv[0] * (-cpk * ctk) + rv[1] * (-spk * ctk) + rv[2] * stk) / (-d2);
+    }
+}
+
 namespace {
 unsigned blocks(long long n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
 }  // namespace
@@ -138,14 +251,61 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
     if (e == cudaSuccess) e = cudaMalloc(&status, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, sizeof(unsigned), stream);
     PropOut O{steps, nullptr, rec, status, nullptr};
-    for (long long c0 = 0; e == cudaSuccess && c0 < npix; c0 += cap) {
+    for (long long c0 = 0; !M.bundle && e == cudaSuccess && c0 < npix; c0 += cap) {
         const long long m = (npix - c0 < cap) ? npix - c0 : cap;
         k_pix_launch<<<blocks(m, 128), 128, 0, stream>>>(m, nside, d_pixels + c0, launch);
         if ((e = cudaGetLastError()) != cudaSuccess) break;
         e = exact ? launch_propagate<true>(T, C, P, launch, m, O, stream) : launch_propagate<false>(T, C, P, launch, m, O, stream);
         if (e != cudaSuccess) break;
-        k_fill_maps<<<blocks(m * nz, 128), 128, 0, stream>>>(m, nz, M, launch, rec, d_maps, npix, c0);
+        k_fill_maps<<<blocks(m * nz, 128), 128, 0, stream>>>(m, nz, M, launch, rec, kPlaneFields, nullptr, d_maps, npix, c0);
         e = cudaGetLastError();
+    }
+    if (M.bundle && e == cudaSuccess) {
+        // central rays with wide records, then four bundle rays per pixel to
+        // their own stop_bundle surfaces, then the Jacobians and the rows
+        double *wrec = nullptr, *blaunch = nullptr, *bplanes = nullptr, *brec = nullptr, *ki = nullptr, *dist = nullptr,
+               *jac = nullptr, *dplanes = nullptr;
+        long long* bsteps = nullptr;
+        e = cudaMalloc(&wrec, (size_t)cap * nz * kWideFields * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&blaunch, (size_t)cap * 24 * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&bplanes, (size_t)cap * 4 * nz * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&brec, (size_t)cap * 4 * nz * kWideFields * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&ki, (size_t)cap * nz * 3 * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&dist, (size_t)cap * nz * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&jac, (size_t)cap * nz * 4 * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&bsteps, (size_t)cap * 4 * sizeof(long long));
+        if (e == cudaSuccess) e = cudaMalloc(&dplanes, (size_t)nz * sizeof(double));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dplanes, P.planes, (size_t)nz * sizeof(double), cudaMemcpyHostToDevice, stream);
+        PropParams Pc = P;
+        Pc.wide = 1;
+        Pc.jacobian = 0;
+        PropParams Pb = P;
+        Pb.wide = 1;
+        Pb.jacobian = 0;
+        Pb.stop_kind = M.stop_bundle;
+        Pb.ray_planes = bplanes;
+        const PropOut Oc{steps, nullptr, wrec, status, nullptr};
+        const PropOut Ob{bsteps, nullptr, brec, status, nullptr};
+        for (long long c0 = 0; e == cudaSuccess && c0 < npix; c0 += cap) {
+            const long long m = (npix - c0 < cap) ? npix - c0 : cap;
+            k_pix_launch<<<blocks(m, 128), 128, 0, stream>>>(m, nside, d_pixels + c0, launch);
+            if ((e = cudaGetLastError()) != cudaSuccess) break;
+            e = exact ? launch_propagate<true>(T, C, Pc, launch, m, Oc, stream) : launch_propagate<false>(T, C, Pc, launch, m, Oc, stream);
+            if (e != cudaSuccess) break;
+            k_bundle_prepare<<<blocks(m, 128), 128, 0, stream>>>(m, nz, M, dplanes, launch, wrec, blaunch, bplanes, ki, dist);
+            if ((e = cudaGetLastError()) != cudaSuccess) break;
+            e = exact ? launch_propagate<true>(T, C, Pb, blaunch, 4 * m, Ob, stream)
+                      : launch_propagate<false>(T, C, Pb, blaunch, 4 * m, Ob, stream);
+            if (e != cudaSuccess) break;
+            k_bundle_jacobian<<<blocks(m, 128), 128, 0, stream>>>(m, nz, M, brec, ki, dist, jac);
+            if ((e = cudaGetLastError()) != cudaSuccess) break;
+            k_fill_maps<<<blocks(m * nz, 128), 128, 0, stream>>>(m, nz, M, launch, wrec, kWideFields, jac, d_maps, npix, c0);
+            e = cudaGetLastError();
+        }
+        cudaStreamSynchronize(stream);
+        for (void* q : {(void*)wrec, (void*)blaunch, (void*)bplanes, (void*)brec, (void*)ki, (void*)dist, (void*)jac,
+                        (void*)bsteps, (void*)dplanes})
+            if (q) cudaFree(q);
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_status, status, sizeof(unsigned), cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);

@@ -14,6 +14,11 @@ struct MapSpec {
     int comp[kMaxMapComponents];      // index_components of hmaps.cpp (0 lensing, 2-13 the others)
     int nmaps;                        // rows per surface
     double homogeneous[kMaxPlanes][5];   // per surface: t chi lambda a z of the FLRW ray
+    // jacobiantype = "bundle" (Lensing::dbetadtheta): 4 rays per pixel
+    int bundle;
+    int plane_sachs;                  // screen normal: interpolated direction (1) or position (0)
+    int stop_bundle;                  // StopKind of the bundle rays' surfaces
+    double openingmin;                // bundle opening (radians)
 };
 
 // d_pixels: npix RING pixel ids on the device; d_maps: nmaps * nplanes rows of

@@ -25,6 +25,10 @@ constexpr int kPlaneFields = 20;
 // radius: the 20 surface fields, then dtdl dxdl dydl dzdl interpolated at the
 // radius (20-23) and the launch point's a, phi, dxdl, dydl, dzdl (24-28).
 constexpr int kSourceFields = 32;
+// Wide surface records (bundle Jacobian): the 20 surface fields, dtdl dxdl
+// dydl dzdl interpolated at the surface (20-23) and whether the kept
+// trajectory reached the surface at all (24).
+constexpr int kWideFields = 32;
 
 enum StopKind { STOP_REDSHIFT = 0, STOP_R = 1, STOP_LAMBDA = 2, STOP_T = 3, STOP_A = 4, STOP_PLANE = 5, STOP_S = 6 };
 
@@ -56,6 +60,10 @@ struct PropParams {
     // source mode: per-ray stop radius; the launch record is the start point
     // and a unit direction (Integrator::launch, (phi, theta) form)
     const double* ray_stop;
+    // per-ray surface values (n x nplanes; the last one is the stop value), or null
+    const double* ray_planes;
+    // surface records of kWideFields doubles instead of kPlaneFields
+    int wide;
 };
 
 struct PropOut {
@@ -198,8 +206,9 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
     const double scale = P.length;
     const int np = SRC ? 1 : P.nplanes;
     const int kind = SRC ? (int)STOP_R : P.stop_kind;
-    const double stop_ref = SRC ? P.ray_stop[i] : P.stop_ref;
-    const int rec_fields = SRC ? kSourceFields : kPlaneFields;
+    const double* rpl = (!SRC && P.ray_planes) ? P.ray_planes + i * np : P.planes;   // this ray's surfaces
+    const double stop_ref = SRC ? P.ray_stop[i] : (P.ray_planes ? rpl[np - 1] : P.stop_ref);
+    const int rec_fields = SRC ? kSourceFields : (P.wide ? kWideFields : kPlaneFields);
     Rec b;
     if (SRC) {
         // launch, (phi, theta) form (src/integrator.h:305-329): direction given
@@ -247,7 +256,7 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
         prow[29] = prow[30] = prow[31] = 0.0;
     }
     // a surface crossed by the first point lies at firstid 0: invalid in the map driver
-    while (next_plane < np && plane_crossed(kind, b, SRC ? stop_ref : P.planes[next_plane])) {
+    while (next_plane < np && plane_crossed(kind, b, SRC ? stop_ref : rpl[next_plane])) {
         cross_k[next_plane] = 0;
         ++next_plane;
     }
@@ -321,12 +330,12 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
                     S.s2[q] += p.chi * p.chi * H[q];
                 }
             }
-            while (next_plane < np && plane_crossed(kind, p, SRC ? stop_ref : P.planes[next_plane])) {
+            while (next_plane < np && plane_crossed(kind, p, SRC ? stop_ref : rpl[next_plane])) {
                 const int j = next_plane++;
                 cross_k[j] = k;
                 if (prow) {
                     double* o = prow + j * rec_fields;
-                    const double ref = SRC ? stop_ref : P.planes[j];
+                    const double ref = SRC ? stop_ref : rpl[j];
                     const double q1 = plane_q(kind, p), q0 = plane_q(kind, b);
                     const double f = (q1 - ref) / (q1 - q0);
                     const double px = b.x * f + p.x * (1 - f), py = b.y * f + p.y * (1 - f), pz = b.z * f + p.z * (1 - f);
@@ -344,7 +353,7 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
                     // max rho over points [0, firstid) = [0, k-1): all points before b
                     o[18] = have_rmax ? rmax_before_b : 0.0;
                     o[19] = 1.0;
-                    if (SRC) {
+                    if (SRC || P.wide) {
                         o[20] = b.k0 * f + p.k0 * (1 - f);
                         o[21] = b.k1 * f + p.k1 * (1 - f);
                         o[22] = b.k2 * f + p.k2 * (1 - f);
@@ -422,16 +431,17 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
         prow[19] = ok ? 1.0 : 0.0;
     } else if (prow) {
         for (int j = 0; j < np; ++j) {
-            double* o = prow + j * kPlaneFields;
+            double* o = prow + j * rec_fields;
             const long long ck = cross_k[j];
             const bool found = (ck >= 1) && (ck < size);
             // map driver: firstid == size-1 or firstid == 0 -> invalid
             const bool valid = found && !((ck - 1) == size - 1 || (ck - 1) == 0);
             if (ck < 0 || ck == 0 || ck >= size) {
-                for (int q = 0; q < kPlaneFields; ++q) o[q] = 0.0;
+                for (int q = 0; q < (P.wide ? 24 : kPlaneFields); ++q) o[q] = 0.0;
                 o[0] = (ck == 0) ? 0.0 : (double)(size - 1);
             }
             o[19] = valid ? 1.0 : 0.0;
+            if (P.wide) o[24] = found ? 1.0 : 0.0;
         }
     }
     if (status) atomicOr(O.status, status);

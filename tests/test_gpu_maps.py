@@ -42,3 +42,34 @@ def test_hmaps_fill_matches_reference_fillmap(gpu_lib, pkg, golden, order, exact
     for row in range(4, ref.shape[1]):
         scale = np.abs(ref[:, row]).max() + 1e-30
         assert np.abs(got[:, row] - ref[:, row]).max() <= 2e-6 * scale + 1e-12, row
+
+
+BUNDLES = (("sachs", "redshift"), ("normal", "r"))
+OPENING = 0.2 / 60.0 * 3.141592653589793 / 180.0
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("exact", [True, False])
+@pytest.mark.parametrize("plane,stop_bundle", BUNDLES)
+def test_hmaps_fill_bundle_matches_reference(gpu_lib, pkg, golden, order, exact, plane, stop_bundle):
+    """jacobiantype = bundle: the four-ray Jacobian is a finite difference over
+    a 0.2 arcmin screen, so position errors are divided by ~6e-5 of the
+    distance: exact mode (ulp-level launch differences) agrees to 1e-6 of the
+    lensing rows' scale, fast mode (FP32 gathers) to 1e-3."""
+    tree = pkg.Octree.from_records(golden["records"])
+    cos = pkg.Cosmology(golden["cosmo_t"], golden["cosmo_a"], golden["cosmo_dadt"], golden["cosmo_d2adt2"])
+    comps = str(golden["components"]).split(",")
+    got = pkg.hmaps_fill(tree, cos, int(golden["nside"]), golden["pixels"], golden["zs"], golden["homogeneous"], comps,
+                         float(golden["cosmo_length"]), nsteps=int(golden["nsteps"]), order=order, exact=exact,
+                         jacobian="bundle", plane=plane, stop_bundle=stop_bundle, openingmin=OPENING)
+    ref = golden["ref_maps_bundle_o%d_%s_%s" % (order, plane, stop_bundle)]
+    assert got.shape == ref.shape
+    srow = 5 + comps.index("steps") - 1
+    np.testing.assert_array_equal(got[:, srow] != 0, ref[:, srow] != 0)
+    tol = 1e-6 if exact else 1e-3
+    for row in range(5):
+        scale = max(np.abs(ref[:, row]).max(), 1e-9)
+        assert np.abs(got[:, row] - ref[:, row]).max() <= tol * scale + 2e-7 * (row == 4), (row, exact)
+    for row in range(5, ref.shape[1]):
+        scale = np.abs(ref[:, row]).max() + 1e-30
+        assert np.abs(got[:, row] - ref[:, row]).max() <= 2e-6 * scale + 1e-12, row
