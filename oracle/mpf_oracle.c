@@ -734,7 +734,8 @@ typedef struct {
     const mpfo_tree* T;
     const mpfo_cosmo* C;
     int order, max_iterations;
-    double length, accuracy, h, mpc;
+    int bundle, plane_sachs, stop_bundle;   /* jacobiantype = bundle, plane = sachs, stop_bundle kind */
+    double length, accuracy, h, mpc, openingmin;
     unsigned nsteps;
     const double* src;
     const double* rot;
@@ -744,12 +745,17 @@ typedef struct {
     pthread_mutex_t mu;
 } cjob_t;
 
+static void dbetadtheta(ctx_t* c, traj_t* tr, unsigned nsteps, int stop_bundle, double openingmin, int np,
+                        const double* ki, const double* iref_v, const double* dist, double phiInit,
+                        double thetaInit, double* J);
+
 /* One Catalogues::newtonMethod2d call (catalogues.h:410-727) with
  * jacobiantype = infinitesimal and use_previous_catalogues = 0: res =
  * {{phi', theta'}, {miss, firstid}}; jac and z are updated in place as the
  * reference updates its jacobian and redshifts arguments. */
-static void newton2d(ctx_t* c, traj_t* tr, const cjob_t* J, const double* target, const double* vel, double dist,
-                     double phi, double theta, unsigned iteration, double res[2][2], double jac[2][2], double* z)
+static void newton2d(ctx_t* c, traj_t* tr, traj_t* trb, const cjob_t* J, const double* target, const double* vel,
+                     double dist, double phi, double theta, unsigned iteration, double res[2][2], double jac[2][2],
+                     double* z)
 {
     static const double cl = C_LIGHT, c2 = C_LIGHT * C_LIGHT;
     tr->n = 0;
@@ -771,11 +777,44 @@ static void newton2d(ctx_t* c, traj_t* tr, const cjob_t* J, const double* target
     fp[0] = P0[PX] * f + P1[PX] * (1 - f);
     fp[1] = P0[PY] * f + P1[PY] * (1 - f);
     fp[2] = P0[PZ] * f + P1[PZ] * (1 - f);
+    /* jacobiantype = bundle: the screen normal and the bundle's stop value (catalogues.h:458-495) */
+    double kiT[3] = {0, 0, 0}, iref = 0;
+    if (J->bundle) {
+        if (J->plane_sachs) {
+            kiT[0] = P0[PK1] * f + P1[PK1] * (1 - f);
+            kiT[1] = P0[PK2] * f + P1[PK2] * (1 - f);
+            kiT[2] = P0[PK3] * f + P1[PK3] * (1 - f);
+        } else {
+            kiT[0] = fp[0]; kiT[1] = fp[1]; kiT[2] = fp[2];
+        }
+        switch (J->stop_bundle) {
+        case MPFO_STOP_REDSHIFT: iref = z[1]; break;
+        case MPFO_STOP_A: iref = scale_factor; break;
+        case MPFO_STOP_T: iref = P0[PT] * f + P1[PT] * (1 - f); break;
+        case MPFO_STOP_LAMBDA: iref = P0[PLAMBDA] * f + P1[PLAMBDA] * (1 - f); break;
+        case MPFO_STOP_R: iref = dist; break;
+        default: iref = kiT[0] * fp[0] + kiT[1] * fp[1] + kiT[2] * fp[2]; break;
+        }
+    }
     const double dist_sep = sqrt(pow(target[0] - fp[0], 2) + pow(target[1] - fp[1], 2) + pow(target[2] - fp[2], 2));
     res[1][0] = dist_sep / dist;
     if (res[1][0] > J->accuracy) {
         double ji[2][2] = {{1, 0}, {0, 1}};
-        if (iteration >= 3) {
+        if (iteration >= 5 && J->bundle) {
+            double B[4];
+            dbetadtheta(c, trb, J->nsteps, J->stop_bundle, J->openingmin, 1, kiT, &iref, &dist, phi, theta, B);
+            if (B[0] == 42 && B[1] == 42) {
+                /* catalogues.h:521-528; the reference leaves result[1][1] unset here */
+                res[0][0] = 42; res[0][1] = 42; res[1][0] = 22; res[1][1] = 0;
+                return;
+            }
+            jac[0][0] = B[0]; jac[0][1] = B[1]; jac[1][0] = B[2]; jac[1][1] = B[3];
+            const double invdet = 1. / (jac[0][0] * jac[1][1] - jac[0][1] * jac[1][0]);
+            ji[0][0] = jac[1][1] * invdet;
+            ji[0][1] = -jac[0][1] * invdet;
+            ji[1][0] = -jac[1][0] * invdet;
+            ji[1][1] = jac[0][0] * invdet;
+        } else if (iteration >= 3) {
             double A[3];
             jacobian(c, tr, 1, &dist, A);
             jac[0][0] = A[0]; jac[0][1] = A[1]; jac[1][0] = A[1]; jac[1][1] = A[2];
@@ -814,7 +853,15 @@ static void newton2d(ctx_t* c, traj_t* tr, const cjob_t* J, const double* target
         return;
     }
     /* converged: Jacobian and redshift decomposition (catalogues.h:660-723) */
-    {
+    if (J->bundle) {
+        double B[4];
+        dbetadtheta(c, trb, J->nsteps, J->stop_bundle, J->openingmin, 1, kiT, &iref, &dist, phi, theta, B);
+        jac[0][0] = B[0]; jac[0][1] = B[1]; jac[1][0] = B[2]; jac[1][1] = B[3];
+        if (B[0] == 42 && B[1] == 42) {
+            res[0][0] = 42; res[0][1] = 42; res[1][0] = 22; res[1][1] = 0;
+            return;
+        }
+    } else {
         double A[3];
         jacobian(c, tr, 1, &dist, A);
         jac[0][0] = A[0]; jac[0][1] = A[1]; jac[1][0] = A[1]; jac[1][1] = A[2];
@@ -848,7 +895,7 @@ static void newton2d(ctx_t* c, traj_t* tr, const cjob_t* J, const double* target
 
 /* Catalogues::iterateNewtonMethod (catalogues.h:757-783) behind relCat's
  * per-source setup and row (catalogues.h:811-856). */
-static void catalogue_one(ctx_t* c, traj_t* tr, const cjob_t* J, int64_t i)
+static void catalogue_one(ctx_t* c, traj_t* tr, traj_t* trb, const cjob_t* J, int64_t i)
 {
     const double* s = J->src + 6 * i;
     double target[3], vel[3];
@@ -870,7 +917,7 @@ static void catalogue_one(ctx_t* c, traj_t* tr, const cjob_t* J, int64_t i)
     unsigned iteration = 0;
     for (;;) {
         const double p0 = res[0][0], t0 = res[0][1];
-        newton2d(c, tr, J, target, vel, dist, p0, t0, iteration, res, jac, z);
+        newton2d(c, tr, trb, J, target, vel, dist, p0, t0, iteration, res, jac, z);
         iteration++;
         if (res[0][0] == 42 && res[0][1] == 42) break;
         if (iteration > (unsigned)J->max_iterations && res[1][0] > J->accuracy) {
@@ -893,7 +940,7 @@ static void* cworker(void* arg)
 {
     cjob_t* J = (cjob_t*)arg;
     ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
-    traj_t tr = {0, 0, 0};
+    traj_t tr = {0, 0, 0}, trb = {0, 0, 0};
     for (;;) {
         pthread_mutex_lock(&J->mu);
         const int64_t i = J->next++;
@@ -904,9 +951,10 @@ static void* cworker(void* arg)
         c->order = J->order;
         c->length = J->length;
         cache_init(&c->cache);
-        catalogue_one(c, &tr, J, i);
+        catalogue_one(c, &tr, &trb, J, i);
     }
     free(tr.p);
+    free(trb.p);
     free(c);
     return 0;
 }
@@ -915,8 +963,18 @@ int mpfo_catalogue(const mpfo_tree* T, const mpfo_cosmo* C, int order, double le
                    int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
                    double h, double mpc, int max_iterations, double* out, int nthreads)
 {
+    return mpfo_catalogue_jac(T, C, order, length, nsteps, n, src, rotm1, vobs, cat_accuracy, h, mpc, max_iterations,
+                              0, 0, 0, 0.0, out, nthreads);
+}
+
+int mpfo_catalogue_jac(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
+                       int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
+                       double h, double mpc, int max_iterations, int bundle, int plane_sachs, int stop_bundle,
+                       double openingmin, double* out, int nthreads)
+{
     if (!T || !C || (order != 1 && order != 2) || nsteps == 0 || n < 0 || !vobs) return -1;
     cjob_t J;
+    J.bundle = bundle; J.plane_sachs = plane_sachs; J.stop_bundle = stop_bundle; J.openingmin = openingmin;
     J.T = T; J.C = C; J.order = order; J.max_iterations = max_iterations; J.length = length;
     J.accuracy = cat_accuracy; J.h = h; J.mpc = mpc; J.nsteps = nsteps; J.src = src; J.rot = rotm1;
     J.vobs = vobs; J.out = out; J.n = n; J.next = 0;

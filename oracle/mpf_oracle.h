@@ -77,6 +77,14 @@ int64_t mpfo_trajectory(const mpfo_tree* T, const mpfo_cosmo* C, int order, doub
 int mpfo_catalogue(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
                    int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
                    double h, double mpc, int max_iterations, double* out, int nthreads);
+/* Same with the Jacobian type: bundle != 0 is jacobiantype = "bundle" (the
+ * four-ray Lensing::dbetadtheta from iteration 5 and at convergence), with
+ * plane_sachs (1: "sachs", 0: "normal"), stop_bundle (MPFO_STOP_*) and
+ * openingmin (radians). */
+int mpfo_catalogue_jac(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
+                       int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
+                       double h, double mpc, int max_iterations, int bundle, int plane_sachs, int stop_bundle,
+                       double openingmin, double* out, int nthreads);
 
 /* Hmaps::FillMap with jacobiantype = "bundle": the central rays' surfaces
  * (plane_out, n x np x 20 as mpfo_propagate, without the infinitesimal

@@ -65,6 +65,9 @@ def lib():
         L.mpfo_bundle.restype = C.c_int
         L.mpfo_bundle.argtypes = [_p, _p, C.c_int, _d, C.c_uint, C.c_int, _i64, _p, C.c_int, _p, C.c_int, C.c_int, _d,
                                   _p, _p, C.c_int]
+        L.mpfo_catalogue_jac.restype = C.c_int
+        L.mpfo_catalogue_jac.argtypes = [_p, _p, C.c_int, _d, C.c_uint, _i64, _p, _p, _p, _d, _d, _d, C.c_int,
+                                         C.c_int, C.c_int, C.c_int, _d, _p, C.c_int]
         L.mpfo_catalogue.restype = C.c_int
         L.mpfo_catalogue.argtypes = [_p, _p, C.c_int, _d, C.c_uint, _i64, _p, _p, _p, _d, _d, _d, C.c_int, _p,
                                      C.c_int]
@@ -141,16 +144,18 @@ class Oracle:
         return out[:min(m, cap)]
 
     def catalogue(self, sources, order=2, nsteps=10, cat_accuracy=1e-8, h=0.68, mpc=3.08568e22,
-                  vobs=(0.0, 0.0, 0.0), rotm1=None, max_iterations=10, nthreads=None):
+                  vobs=(0.0, 0.0, 0.0), rotm1=None, max_iterations=10, nthreads=None, jacobiantype="infinitesimal",
+                  plane="normal", stop_bundle="r", openingmin=0.0):
         """relCat rows (n x 16) for sources (n x 6: x y z vx vy vz)."""
         src = np.ascontiguousarray(np.asarray(sources)[:, :6], dtype=np.float64)
         vo = np.ascontiguousarray(vobs, dtype=np.float64)
         rot = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64).reshape(9)
         out = np.zeros((src.shape[0], 16))
-        rc = self.L.mpfo_catalogue(C.byref(self.tree), C.byref(self.cosmo), order, self.length, nsteps,
-                                   src.shape[0], _ptr(src), _ptr(rot) if rot is not None else None, _ptr(vo),
-                                   float(cat_accuracy), float(h), float(mpc), int(max_iterations), _ptr(out),
-                                   int(nthreads or self.nthreads))
+        rc = self.L.mpfo_catalogue_jac(C.byref(self.tree), C.byref(self.cosmo), order, self.length, nsteps,
+                                       src.shape[0], _ptr(src), _ptr(rot) if rot is not None else None, _ptr(vo),
+                                       float(cat_accuracy), float(h), float(mpc), int(max_iterations),
+                                       1 if jacobiantype == "bundle" else 0, 1 if plane == "sachs" else 0,
+                                       STOP[stop_bundle], float(openingmin), _ptr(out), int(nthreads or self.nthreads))
         if rc != 0:
             raise ValueError("oracle catalogue failed: %d" % rc)
         return out

@@ -412,19 +412,20 @@ void ref_pix2vec_ring(long nside, int64_t n, const long* pix, double* vec)
 // infinitesimal Jacobian, and the 16-double catalog row.
 // src: n x 6 (x y z vx vy vz); rotm1: 3x3 row-major or null; vobs: 3;
 // out: n x 16.
-void ref_catalogue(int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
-                   unsigned nsteps, double h, double mpc, double* out, int nthreads)
+void ref_catalogue_jac(int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
+                       unsigned nsteps, double h, double mpc, double* out, int nthreads, const char* jacobiantype,
+                       const char* plane, const char* stop_bundle, double openingmin)
 {
     catalogues_parameters_t P;
     P.isfullsky = rotm1 ? 0 : 1;
     P.mpc = mpc;
     P.cat_accuracy = cat_accuracy;
-    P.jacobiantype = "infinitesimal";
-    P.plane = "normal";
-    P.stop_bundle = "r";
+    P.jacobiantype = jacobiantype;
+    P.plane = plane;
+    P.stop_bundle = stop_bundle;
     P.nsteps = nsteps;
     P.use_previous_catalogues = 0;
-    P.openingmin = 0;
+    P.openingmin = openingmin;
     const point vo{{vobs[0], vobs[1], vobs[2]}};
     const point observer{{0., 0., 0.}};
     std::array<std::array<double, 3>, 3> rot{};
@@ -450,6 +451,8 @@ void ref_catalogue(int64_t n, const double* src, const double* rotm1, const doub
                                             trueTarget[2] * trueTarget[2]);
         const double theta = std::acos(trueTarget[2] / distTarget);
         const double phi = std::atan2(trueTarget[1], trueTarget[0]);
+        // (newtonMethod2d leaves result[1][1] unset when a bundle Jacobian
+        // fails, catalogues.h:525-529, 670-675: that column is undefined there)
         auto result = Catalogues::iterateNewtonMethod(vo, observer, phi, theta, trueTarget, velocityTarget, jacobian, P,
                                                       g_cosmo, g_octree, g_length, h, redshifts, interpRef);
         double* o = out + 16 * i;
@@ -458,6 +461,12 @@ void ref_catalogue(int64_t n, const double* src, const double* rotm1, const doub
         for (int k = 0; k < 6; ++k) o[6 + k] = redshifts[k];
         o[12] = jacobian[0][0]; o[13] = jacobian[0][1]; o[14] = jacobian[1][0]; o[15] = jacobian[1][1];
     });
+}
+
+void ref_catalogue(int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
+                   unsigned nsteps, double h, double mpc, double* out, int nthreads)
+{
+    ref_catalogue_jac(n, src, rotm1, vobs, cat_accuracy, nsteps, h, mpc, out, nthreads, "infinitesimal", "normal", "r", 0.0);
 }
 
 }  // extern "C"

@@ -66,6 +66,8 @@ def lib(order: int = 2):
                                       C.c_char_p, C.c_char_p, C.c_char_p, _d]
         L.ref_pix2vec_ring.argtypes = [C.c_long, _i64, _p, _p]
         L.ref_catalogue.argtypes = [_i64, _p, _p, _p, _d, C.c_uint, _d, _d, _p, C.c_int]
+        L.ref_catalogue_jac.argtypes = [_i64, _p, _p, _p, _d, C.c_uint, _d, _d, _p, C.c_int, C.c_char_p, C.c_char_p,
+                                        C.c_char_p, _d]
         _LIBS[order] = L
     return _LIBS[order]
 
@@ -177,12 +179,14 @@ class Reference:
         self.L.ref_pix2vec_ring(nside, pix.shape[0], _ptr(pix), _ptr(out))
         return out
 
-    def catalogue(self, sources, cat_accuracy=1e-8, nsteps=10, h=0.68, mpc=3.08568e22, vobs=(0.0, 0.0, 0.0), rotm1=None):
+    def catalogue(self, sources, cat_accuracy=1e-8, nsteps=10, h=0.68, mpc=3.08568e22, vobs=(0.0, 0.0, 0.0), rotm1=None,
+                  jacobiantype="infinitesimal", plane="normal", stop_bundle="r", openingmin=0.0):
         """relCat rows (n x 16) for sources (n x 6: x y z vx vy vz)."""
         src = np.ascontiguousarray(sources[:, :6], dtype=np.float64)
         vo = np.ascontiguousarray(vobs, dtype=np.float64)
         rot = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64).reshape(9)
         out = np.zeros((src.shape[0], 16))
-        self.L.ref_catalogue(src.shape[0], _ptr(src), _ptr(rot) if rot is not None else None, _ptr(vo),
-                             float(cat_accuracy), int(nsteps), float(h), float(mpc), _ptr(out), self.nthreads)
+        self.L.ref_catalogue_jac(src.shape[0], _ptr(src), _ptr(rot) if rot is not None else None, _ptr(vo),
+                                 float(cat_accuracy), int(nsteps), float(h), float(mpc), _ptr(out), self.nthreads,
+                                 jacobiantype.encode(), plane.encode(), stop_bundle.encode(), float(openingmin))
         return out

@@ -150,6 +150,12 @@ def make(name, cfg):
                                                                out["cosmo_mpc"], CAT_VOBS)
         out["ref_cat_rot_o%d" % order] = R.catalogue(out["cat_src_rotated"], CAT_ACCURACIES[0], cfg["nsteps"],
                                                      out["cosmo_h"], out["cosmo_mpc"], CAT_VOBS, out["cat_rotm1"])
+        # jacobiantype = bundle: converged at 1e-8, and every source through the bundle Newton rounds at 0
+        for ia in (0, 2):
+            for plane, sb in BUNDLES:
+                out["ref_cat_bundle_o%d_a%d_%s_%s" % (order, ia, plane, sb)] = R.catalogue(
+                    out["cat_src"], CAT_ACCURACIES[ia], cfg["nsteps"], out["cosmo_h"], out["cosmo_mpc"], CAT_VOBS,
+                    None, "bundle", plane, sb, OPENING)
     path = os.path.join(HERE, "%s.npz" % name)
     np.savez_compressed(path, **out)
     print("%s: %d cells (levels %d-%d), %d rays, %d pixels -> %s (%d KB)" % (

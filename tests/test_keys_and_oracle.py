@@ -89,6 +89,20 @@ def test_oracle_catalogue_bit_exact(golden, oracle_mod, order):
     np.testing.assert_array_equal(rows.view(np.uint64), golden["ref_cat_rot_o%d" % order].view(np.uint64))
 
 
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("plane,stop_bundle", BUNDLES)
+def test_oracle_catalogue_bundle_bit_exact(golden, oracle_mod, order, plane, stop_bundle):
+    """jacobiantype = bundle: the Newton rounds from iteration 5 and the final
+    Jacobian use Lensing::dbetadtheta; the oracle's rows equal the reference's."""
+    O = _oracle(golden, oracle_mod)
+    kw = dict(order=order, nsteps=int(golden["nsteps"]), h=float(golden["cosmo_h"]), mpc=float(golden["cosmo_mpc"]),
+              vobs=golden["cat_vobs"], jacobiantype="bundle", plane=plane, stop_bundle=stop_bundle, openingmin=OPENING)
+    for ia in (0, 2):
+        rows = O.catalogue(golden["cat_src"], cat_accuracy=float(golden["cat_accuracy"][ia]), **kw)
+        ref = golden["ref_cat_bundle_o%d_a%d_%s_%s" % (order, ia, plane, stop_bundle)]
+        np.testing.assert_array_equal(rows.view(np.uint64), ref.view(np.uint64))
+
+
 def test_catalogue_fixture_covers_every_outcome(golden):
     """The fixture holds converged (2-4 rays, so the infinitesimal-Jacobian
     steps run), rejected (42 after 11 rays) and failed (phi = theta = 42) sources."""
