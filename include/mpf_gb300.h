@@ -162,6 +162,15 @@ typedef struct {
     int order;                 /* 1 = CIC, 2 = TSC */
     int exact;                 /* 1: reference float64 order; 0: FP32 gathers */
     int max_iterations;        /* 10 in the reference (use_previous_catalogues = 0) */
+    /* jacobiantype (catalogues.h:505-529, 660-676): 0 = "infinitesimal";
+     * 1 = "bundle", the four-ray Lensing::dbetadtheta from the sixth ray on and
+     * at convergence, with the screen normal plane_sachs (1: "sachs", 0:
+     * "normal"), the stop criterion stop_bundle (an mpf_stop: redshift, r,
+     * lambda, t or a) and the opening openingmin (radians) */
+    int jacobian_bundle;
+    int plane_sachs;
+    int stop_bundle;
+    double openingmin;
 } mpf_catalogue_params;
 
 #define MPF_CATALOGUE_FIELDS 16

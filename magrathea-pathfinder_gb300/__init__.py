@@ -158,7 +158,8 @@ def propagate(octree: Octree, cosmology: Cosmology, launch, length: float, nstep
 
 def catalogue(octree: Octree, cosmology: Cosmology, sources, length: float, h: float, mpc: float = 3.08568e22,
               cat_accuracy: float = 1e-8, nsteps: int = 10, order: int = 2, vobs=(0.0, 0.0, 0.0), rotm1=None,
-              exact: bool = False, max_iterations: int = 10):
+              exact: bool = False, max_iterations: int = 10, jacobian: str = "infinitesimal", plane: str = "normal",
+              stop_bundle: str = "r", openingmin: float = 0.0):
     """Catalogues::relCat for a batch of sources (rows of >= 6 doubles: x y z vx vy vz ...).
 
     Returns (rows[n, 16] in relCat's column order, stats dict, status).
@@ -168,7 +169,8 @@ def catalogue(octree: Octree, cosmology: Cosmology, sources, length: float, h: f
     if src.ndim != 2 or src.shape[1] < 6:
         raise ValueError("sources must be n x (>= 6)")
     n, stride = src.shape
-    p, rot = catalogue_params(length, h, mpc, cat_accuracy, nsteps, order, vobs, rotm1, exact, max_iterations)
+    p, rot = catalogue_params(length, h, mpc, cat_accuracy, nsteps, order, vobs, rotm1, exact, max_iterations,
+                              jacobian, plane, stop_bundle, openingmin)
     rows = np.zeros((n, capi.MPF_CATALOGUE_FIELDS))
     st = capi.CatalogueStats()
     rc = L.mpf_catalogue_newton(octree._h, cosmology._h, C.byref(p), n, capi.ptr(src), stride, capi.ptr(rows),
@@ -179,7 +181,8 @@ def catalogue(octree: Octree, cosmology: Cosmology, sources, length: float, h: f
 
 
 def catalogue_params(length, h, mpc=3.08568e22, cat_accuracy=1e-8, nsteps=10, order=2, vobs=(0.0, 0.0, 0.0),
-                     rotm1=None, exact=False, max_iterations=10):
+                     rotm1=None, exact=False, max_iterations=10, jacobian="infinitesimal", plane="normal",
+                     stop_bundle="r", openingmin=0.0):
     """mpf_catalogue_params plus the rotation array that must outlive the call."""
     p = capi.CatalogueParams()
     p.length, p.h, p.mpc, p.cat_accuracy = float(length), float(h), float(mpc), float(cat_accuracy)
@@ -188,6 +191,10 @@ def catalogue_params(length, h, mpc=3.08568e22, cat_accuracy=1e-8, nsteps=10, or
     rot = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64).reshape(9)
     p.rotm1 = rot.ctypes.data if rot is not None else None
     p.nsteps, p.order, p.exact, p.max_iterations = int(nsteps), int(order), int(bool(exact)), int(max_iterations)
+    p.jacobian_bundle = 1 if jacobian == "bundle" else 0
+    p.plane_sachs = 1 if plane == "sachs" else 0
+    p.stop_bundle = capi.STOP[stop_bundle]
+    p.openingmin = float(openingmin)
     return p, rot
 
 

@@ -56,7 +56,8 @@ class Params(C.Structure):
 class CatalogueParams(C.Structure):
     _fields_ = [("length", C.c_double), ("h", C.c_double), ("mpc", C.c_double), ("cat_accuracy", C.c_double),
                 ("vobs", C.c_double * 3), ("rotm1", C.c_void_p), ("nsteps", C.c_uint), ("order", C.c_int),
-                ("exact", C.c_int), ("max_iterations", C.c_int)]
+                ("exact", C.c_int), ("max_iterations", C.c_int), ("jacobian_bundle", C.c_int),
+                ("plane_sachs", C.c_int), ("stop_bundle", C.c_int), ("openingmin", C.c_double)]
 
 
 class CatalogueStats(C.Structure):

@@ -298,6 +298,12 @@ bool catalogue_consts(const mpf_catalogue_params* p, mpf::CatConst& K, mpf::CatR
     K.length = p->length; K.h = p->h; K.mpc = p->mpc; K.accuracy = p->cat_accuracy;
     for (int k = 0; k < 3; ++k) K.vobs[k] = p->vobs[k];
     K.max_iterations = p->max_iterations;
+    K.bundle = p->jacobian_bundle ? 1 : 0;
+    K.plane_sachs = p->plane_sachs ? 1 : 0;
+    K.stop_bundle = p->stop_bundle;
+    K.openingmin = p->openingmin;
+    if (K.bundle && (p->stop_bundle < 0 || p->stop_bundle > 4 || !(p->openingmin > 0.0) || !(p->openingmin < 1.0)))
+        return false;
     if (p->rotm1)
         for (int j = 0; j < 3; ++j)
             for (int k = 0; k < 3; ++k) R.m[j][k] = p->rotm1[3 * j + k];

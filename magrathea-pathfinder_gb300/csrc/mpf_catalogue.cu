@@ -37,8 +37,37 @@ struct CatState {
     double vx, vy, vz;       // source velocity in the octree frame
     double dist;             // |x_s|
     double phi, theta;       // current launch angles
-    double pad;
+    // bundle Jacobian (jacobiantype = bundle): the last ray's end point and
+    // miss, the screen normal and the bundle's stop value (catalogues.h:458-495)
+    double fx, fy, fz, miss;
+    double kx, ky, kz, iref;
 };
+
+// Newton step in the screen basis (catalogues.h:625-655) with the inverse
+// Jacobian ji; returns the new launch angles.
+__device__ __forceinline__ void newton_step(const CatState& S, double fx, double fy, double fz, double ji00, double ji01,
+                                            double ji10, double ji11, double& nphi, double& ntheta)
+{
+    const double cp = cos(S.phi), sp = sin(S.phi), ct = cos(S.theta), st = sin(S.theta);
+    const double e10 = -sp, e11 = cp;
+    const double e20 = -cp * ct, e21 = -sp * ct, e22 = st;
+    const double g0 = S.dist * cp * st, g1 = S.dist * sp * st, g2 = S.dist * ct;
+    const double sep0 = fx - S.tx, sep1 = fy - S.ty, sep2 = fz - S.tz;
+    const double pos0 = g0 - S.tx, pos1 = g1 - S.ty, pos2 = g2 - S.tz;
+    const double sepx = sep0 * e10 + sep1 * e11;
+    const double sepy = sep0 * e20 + sep1 * e21 + sep2 * e22;
+    const double posx = pos0 * e10 + pos1 * e11;
+    const double posy = pos0 * e20 + pos1 * e21 + pos2 * e22;
+    const double sepxnew = ji00 * sepx + ji01 * sepy;
+    const double sepynew = ji10 * sepx + ji11 * sepy;
+    const double posxnew = posx - sepxnew;
+    const double posynew = posy - sepynew;
+    const double xnew = S.tx + (posxnew * e10 + posynew * e20);
+    const double ynew = S.ty + (posxnew * e11 + posynew * e21);
+    const double znew = S.tz + posynew * e22;
+    nphi = atan2(ynew, xnew);
+    ntheta = acos(znew / sqrt(xnew * xnew + ynew * ynew + znew * znew));
+}
 
 // 2-D Morton key of a direction: 16 bits of phi in [-pi, pi] and of theta in [0, pi], interleaved.
 __device__ __forceinline__ uint32_t spread16(uint32_t v)
@@ -83,7 +112,8 @@ __global__ void k_cat_init(long long n, const double* __restrict__ src, int stri
     // comoving first guess (catalogues.h:832-836)
     S.theta = acos(t[2] / S.dist);
     S.phi = atan2(t[1], t[0]);
-    S.pad = 0.0;
+    S.fx = S.fy = S.fz = S.miss = 0.0;
+    S.kx = S.ky = S.kz = S.iref = 0.0;
     state[i] = S;
     double* r = rows + (long long)kCatalogueFields * i;
     for (int k = 0; k < kCatalogueFields; ++k) r[k] = 0.0;
@@ -122,12 +152,13 @@ __global__ void k_cat_rays(long long m, const int* __restrict__ list, const CatS
 __global__ void k_cat_update(long long m, int iteration, int traced_jacobian, CatConst K,
                              const int* __restrict__ list, CatState* __restrict__ state, double* __restrict__ rows,
                              const long long* __restrict__ steps, const double* __restrict__ rec,
-                             int* __restrict__ cont, int* __restrict__ retrace_flag,
+                             int* __restrict__ cont, int* __restrict__ retrace_flag, int* __restrict__ pend,
                              unsigned long long* __restrict__ photon_steps)
 {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j > m) return;
     cont[j] = 0;   // continue flag, scanned into the next round's list (entry m closes the scan)
+    pend[j] = 0;   // waiting for a bundle Jacobian before its Newton step
     if (j == m) return;
     const double c = kC, c2 = kC * kC;
     const int s = list[j];
@@ -151,6 +182,24 @@ __global__ void k_cat_update(long long m, int iteration, int traced_jacobian, Ca
     const double ex = S.tx - fx, ey = S.ty - fy, ez = S.tz - fz;
     const double dist_sep = sqrt(ex * ex + ey * ey + ez * ez);
     const double miss = dist_sep / S.dist;
+    if (K.bundle) {
+        // the bundle's screen normal and stop value at this ray's end (catalogues.h:458-495)
+        if (K.plane_sachs) { S.kx = o[21]; S.ky = o[22]; S.kz = o[23]; }
+        else { S.kx = fx; S.ky = fy; S.kz = fz; }
+        switch (K.stop_bundle) {
+        case STOP_REDSHIFT: S.iref = o[11]; break;
+        case STOP_A: S.iref = scale_factor; break;
+        case STOP_T: S.iref = o[9]; break;
+        case STOP_LAMBDA: S.iref = o[13]; break;
+        default: S.iref = S.dist; break;   // "r"
+        }
+        S.fx = fx; S.fy = fy; S.fz = fz; S.miss = miss;
+        state[s] = S;
+    }
+    if (miss > K.accuracy && K.bundle && iteration >= 5) {
+        pend[j] = 1;   // the Newton step needs the four-ray Jacobian first
+        return;
+    }
     if (miss > K.accuracy) {
         double ji00 = 1.0, ji01 = 0.0, ji10 = 0.0, ji11 = 1.0;
         if (iteration >= 3) {
@@ -163,26 +212,8 @@ __global__ void k_cat_update(long long m, int iteration, int traced_jacobian, Ca
             ji10 = -a10 * invdet;
             ji11 = a00 * invdet;
         }
-        // Newton step in the screen basis (catalogues.h:625-655)
-        const double cp = cos(S.phi), sp = sin(S.phi), ct = cos(S.theta), st = sin(S.theta);
-        const double e10 = -sp, e11 = cp;
-        const double e20 = -cp * ct, e21 = -sp * ct, e22 = st;
-        const double g0 = S.dist * cp * st, g1 = S.dist * sp * st, g2 = S.dist * ct;
-        const double sep0 = fx - S.tx, sep1 = fy - S.ty, sep2 = fz - S.tz;
-        const double pos0 = g0 - S.tx, pos1 = g1 - S.ty, pos2 = g2 - S.tz;
-        const double sepx = sep0 * e10 + sep1 * e11;
-        const double sepy = sep0 * e20 + sep1 * e21 + sep2 * e22;
-        const double posx = pos0 * e10 + pos1 * e11;
-        const double posy = pos0 * e20 + pos1 * e21 + pos2 * e22;
-        const double sepxnew = ji00 * sepx + ji01 * sepy;
-        const double sepynew = ji10 * sepx + ji11 * sepy;
-        const double posxnew = posx - sepxnew;
-        const double posynew = posy - sepynew;
-        const double xnew = S.tx + (posxnew * e10 + posynew * e20);
-        const double ynew = S.ty + (posxnew * e11 + posynew * e21);
-        const double znew = S.tz + posynew * e22;
-        const double nphi = atan2(ynew, xnew);
-        const double ntheta = acos(znew / sqrt(xnew * xnew + ynew * ynew + znew * znew));
+        double nphi, ntheta;
+        newton_step(S, fx, fy, fz, ji00, ji01, ji10, ji11, nphi, ntheta);
         row[2] = nphi; row[3] = ntheta; row[4] = miss;
         if (count > (unsigned)K.max_iterations) {
             row[5] = 42.0;   // rejected
@@ -196,7 +227,9 @@ __global__ void k_cat_update(long long m, int iteration, int traced_jacobian, Ca
     }
     // converged (catalogues.h:658-726)
     row[2] = S.phi; row[3] = S.theta; row[4] = miss; row[5] = (double)count;
-    if (traced_jacobian) {
+    if (K.bundle) {
+        retrace_flag[s] = 1;   // its Jacobian comes from the four-ray bundle after the last round
+    } else if (traced_jacobian) {
         row[12] = o[6]; row[13] = o[7]; row[14] = o[7]; row[15] = o[8];
     } else {
         retrace_flag[s] = 1;
@@ -241,6 +274,122 @@ __global__ void k_cat_jacobian(long long m, const int* __restrict__ list, const 
     double* row = rows + (long long)kCatalogueFields * list[j];
     if (o[19] == 0.0) return;
     row[12] = o[6]; row[13] = o[7]; row[14] = o[7]; row[15] = o[8];
+}
+
+// Four bundle rays per listed source (Lensing::dbetadtheta, lensing.h:160-196)
+// around its current launch direction, each with the single surface iref.
+__global__ void k_cat_bundle_rays(long long nb, const int* __restrict__ srcs, const CatState* __restrict__ state,
+                                  CatConst K, double* __restrict__ blaunch, double* __restrict__ bplanes)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nb) return;
+    const CatState& S = state[srcs[k]];
+    const double cp = cos(S.phi), sp = sin(S.phi), ct = cos(S.theta), st = sin(S.theta);
+    const double tx = cp * st, ty = sp * st, tz = ct;
+    const double e1x = -sp, e1y = cp;
+    const double e2x = -cp * ct, e2y = -sp * ct, e2z = st;
+    const double to = tan(K.openingmin);
+    double* B = blaunch + 24 * k;
+    for (int r = 0; r < 4; ++r) {
+        B[6 * r] = 0.0; B[6 * r + 1] = 0.0; B[6 * r + 2] = 0.0;
+        bplanes[4 * k + r] = S.iref;
+    }
+    B[3] = tx + to * e1x; B[4] = ty + to * e1y; B[5] = tz;
+    B[9] = tx - to * e1x; B[10] = ty - to * e1y; B[11] = tz;
+    B[15] = tx - to * e2x; B[16] = ty - to * e2y; B[17] = tz - to * e2z;
+    B[21] = tx + to * e2x; B[22] = ty + to * e2y; B[23] = tz + to * e2z;
+}
+
+// The four-ray Jacobian at the source distance (lensing.h:198-334, one
+// surface); false when a bundle ray ended before the surface (J = 42 42 1 0,
+// or 42 42 1 3 for stop_bundle = "a").
+__device__ bool cat_bundle_jacobian(const double* r4, const CatState& S, const CatConst& K, double* J)
+{
+    for (int r = 0; r < 4; ++r) {
+        if (r4[r * kWideFields + 24] == 0.0) {
+            J[0] = 42; J[1] = 42; J[2] = 1; J[3] = (K.stop_bundle == STOP_A) ? 3 : 0;
+            return false;
+        }
+    }
+    const double* r0 = r4;
+    const double* r1 = r4 + kWideFields;
+    const double* r2 = r4 + 2 * kWideFields;
+    const double* r3 = r4 + 3 * kWideFields;
+    double rh[3], rv[3];
+    for (int d = 0; d < 3; ++d) {
+        rh[d] = r0[2 + d] - r1[2 + d];
+        rv[d] = r2[2 + d] - r3[2 + d];
+    }
+    const double phik = atan2(S.ky, S.kx);
+    const double thetak = acos(S.kz / sqrt(S.kx * S.kx + S.ky * S.ky + S.kz * S.kz));
+    const double cpk = cos(phik), spk = sin(phik), ctk = cos(thetak), stk = sin(thetak);
+    const double to = tan(K.openingmin);
+    const double d2 = 2 * S.dist * to;
+    J[0] = (rh[0] * -spk + rh[1] * cpk) / d2;
+    J[1] = (rv[0] * -spk + rv[1] * cpk) / d2;
+    J[2] = (rh[0] * (-cpk * ctk) + rh[1] * (-spk * ctk) + rh[2] * stk) / (-d2);
+    J[3] = (rv[0] * (-cpk * ctk) + rv[1] * (-spk * ctk) + rv[2] * stk) / (-d2);
+    return true;
+}
+
+// Newton step of the sources that waited for their bundle Jacobian (round >= 5).
+__global__ void k_cat_bundle_newton(long long nb, int iteration, CatConst K, const int* __restrict__ srcs,
+                                    CatState* __restrict__ state, double* __restrict__ rows,
+                                    const double* __restrict__ brec, int* __restrict__ cont_src)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nb) return;
+    const int s = srcs[k];
+    CatState S = state[s];
+    double* row = rows + (long long)kCatalogueFields * s;
+    double J[4];
+    const bool ok = cat_bundle_jacobian(brec + 4 * k * kWideFields, S, K, J);
+    row[12] = J[0]; row[13] = J[1]; row[14] = J[2]; row[15] = J[3];
+    if (!ok) {
+        // catalogues.h:521-528 (the reference leaves column 5 unset there)
+        row[2] = 42.0; row[3] = 42.0; row[4] = 22.0; row[5] = 0.0;
+        return;
+    }
+    const double invdet = 1. / (J[0] * J[3] - J[1] * J[2]);
+    double nphi, ntheta;
+    newton_step(S, S.fx, S.fy, S.fz, J[3] * invdet, -J[1] * invdet, -J[2] * invdet, J[0] * invdet, nphi, ntheta);
+    row[2] = nphi; row[3] = ntheta; row[4] = S.miss;
+    if ((unsigned)iteration + 1u > (unsigned)K.max_iterations) {
+        row[5] = 42.0;   // rejected
+        return;
+    }
+    S.phi = nphi;
+    S.theta = ntheta;
+    state[s] = S;
+    cont_src[s] = 1;
+}
+
+// Bundle Jacobian of the converged sources (catalogues.h:661-676); a failed
+// bundle turns the source into a failure row as the reference does.
+__global__ void k_cat_bundle_final(long long nb, CatConst K, const int* __restrict__ srcs,
+                                   const CatState* __restrict__ state, double* __restrict__ rows,
+                                   const double* __restrict__ brec)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nb) return;
+    const int s = srcs[k];
+    double* row = rows + (long long)kCatalogueFields * s;
+    double J[4];
+    const bool ok = cat_bundle_jacobian(brec + 4 * k * kWideFields, state[s], K, J);
+    row[12] = J[0]; row[13] = J[1]; row[14] = J[2]; row[15] = J[3];
+    if (!ok) {
+        row[2] = 42.0; row[3] = 42.0; row[4] = 22.0; row[5] = 0.0;
+        row[6] = 0.0; row[8] = 0.0; row[9] = 0.0; row[10] = 0.0; row[11] = 0.0;
+    }
+}
+
+// Next round's flags: the in-round continuations and the bundle Newton ones.
+__global__ void k_merge_cont(long long m, const int* __restrict__ list, const int* __restrict__ cont_src,
+                             int* __restrict__ cont)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    if (cont_src[list[j]]) cont[j] = 1;
 }
 
 // Stable LSD radix sort of (key, value) pairs: 4-bit digits, each thread
@@ -298,7 +447,7 @@ namespace {
 unsigned blocks(long long n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
 
 struct CatBuffers {
-    void* p[13] = {};
+    void* p[20] = {};
     ~CatBuffers()
     {
         for (void* q : p)
@@ -340,6 +489,19 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     uint32_t* key0 = (uint32_t*)alloc(10, (size_t)n * sizeof(uint32_t));
     uint32_t* key1 = (uint32_t*)alloc(11, (size_t)n * sizeof(uint32_t));
     int* scan = (int*)alloc(12, (size_t)(std::max<long long>(n, 16 * ntiles) + 1) * sizeof(int));
+    int* pend = (int*)alloc(13, (size_t)(n + 1) * sizeof(int));
+    // bundle Jacobian (jacobiantype = bundle): four rays per source in a pass
+    int *plist = nullptr, *cont_src = nullptr;
+    double *blaunch = nullptr, *bplanes = nullptr, *brec = nullptr;
+    long long* bsteps = nullptr;
+    if (K.bundle) {
+        plist = (int*)alloc(14, (size_t)n * sizeof(int));
+        cont_src = (int*)alloc(15, (size_t)n * sizeof(int));
+        blaunch = (double*)alloc(16, (size_t)n * 24 * sizeof(double));
+        bplanes = (double*)alloc(17, (size_t)n * 4 * sizeof(double));
+        brec = (double*)alloc(18, (size_t)n * 4 * kWideFields * sizeof(double));
+        bsteps = (long long*)alloc(19, (size_t)n * 4 * sizeof(long long));
+    }
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(counters, 0, 8 * sizeof(unsigned), stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(psteps, 0, 2 * sizeof(unsigned long long), stream);
@@ -387,16 +549,47 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     P.nplanes = 1;
     P.ray_stop = radius;
     PropOut O{steps, nullptr, rec, counters + 3, nullptr};
+    // the bundle rays: their own stop criterion and one surface each
+    PropParams Pb = P;
+    Pb.ray_stop = nullptr;
+    Pb.stop_kind = K.stop_bundle;
+    Pb.ray_planes = bplanes;
+    Pb.wide = 1;
+    Pb.jacobian = 0;
+    const PropOut Ob{bsteps, nullptr, brec, counters + 3, nullptr};
+    auto bundle_pass = [&](long long nb, const int* srcs) -> cudaError_t {
+        k_cat_bundle_rays<<<blocks(nb, tpb), tpb, 0, stream>>>(nb, srcs, state, K, blaunch, bplanes);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        stats->rays += 4 * nb;
+        stats->launches += 2;
+        return exact ? launch_propagate<true>(T, Cs, Pb, blaunch, 4 * nb, Ob, stream)
+                     : launch_propagate<false>(T, Cs, Pb, blaunch, 4 * nb, Ob, stream);
+    };
     for (int it = 0; it <= K.max_iterations && m > 0; ++it) {
-        const int jac = (it >= 3) ? 1 : 0;
+        // the infinitesimal Jacobian serves rounds 3 and up, or 3 and 4 before the bundle rounds
+        const int jac = (it >= 3 && !(K.bundle && it >= 5)) ? 1 : 0;
         P.jacobian = jac;
         k_cat_rays<<<blocks(m, tpb), tpb, 0, stream>>>(m, cur, state, launch, radius);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         e = exact ? launch_propagate<true>(T, Cs, P, launch, m, O, stream) : launch_propagate<false>(T, Cs, P, launch, m, O, stream);
         if (e != cudaSuccess) return e;
         k_cat_update<<<blocks(m + 1, tpb), tpb, 0, stream>>>(m, it, jac, K, cur, state, d_rows, steps, rec, scan, rflag,
-                                                              psteps);
+                                                              pend, psteps);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (K.bundle && it >= 5) {
+            const int64_t npend = exclusive_scan(pend, (int64_t)m + 1, stream);
+            if (npend > 0) {
+                k_compact<<<blocks(m, tpb), tpb, 0, stream>>>(m, cur, pend, plist);
+                if ((e = cudaMemsetAsync(cont_src, 0, (size_t)n * sizeof(int), stream)) != cudaSuccess) return e;
+                if ((e = bundle_pass(npend, plist)) != cudaSuccess) return e;
+                k_cat_bundle_newton<<<blocks(npend, tpb), tpb, 0, stream>>>(npend, it, K, plist, state, d_rows, brec,
+                                                                            cont_src);
+                k_merge_cont<<<blocks(m, tpb), tpb, 0, stream>>>(m, cur, cont_src, scan);
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                stats->launches += 3;
+            }
+        }
         const int64_t next_m = exclusive_scan(scan, (int64_t)m + 1, stream);
         k_compact<<<blocks(m, tpb), tpb, 0, stream>>>(m, cur, scan, nxt);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -412,7 +605,14 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int64_t r = exclusive_scan(scan, (int64_t)m_valid + 1, stream);
     stats->launches += 1;
-    if (r > 0) {
+    if (r > 0 && K.bundle) {
+        // converged sources: the four-ray Jacobian
+        k_compact<<<blocks(m_valid, tpb), tpb, 0, stream>>>(m_valid, sorted, scan, cur);
+        if ((e = bundle_pass(r, cur)) != cudaSuccess) return e;
+        k_cat_bundle_final<<<blocks(r, tpb), tpb, 0, stream>>>(r, K, cur, state, d_rows, brec);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        stats->launches += 2;
+    } else if (r > 0) {
         k_compact<<<blocks(m_valid, tpb), tpb, 0, stream>>>(m_valid, sorted, scan, cur);
         P.jacobian = 1;
         k_cat_rays<<<blocks(r, tpb), tpb, 0, stream>>>(r, cur, state, launch, radius);

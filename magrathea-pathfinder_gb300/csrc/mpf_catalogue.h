@@ -13,6 +13,11 @@ struct CatConst {
     double length, h, mpc, accuracy;
     double vobs[3];
     int max_iterations;
+    // jacobiantype = "bundle": Lensing::dbetadtheta from round 5 and at convergence
+    int bundle;
+    int plane_sachs;      // screen normal: interpolated direction (1) or position (0)
+    int stop_bundle;      // StopKind of the bundle rays
+    double openingmin;    // radians
 };
 
 struct CatRotation {

@@ -134,3 +134,40 @@ def test_catalogue_larger_batch_against_oracle(gpu_lib, pkg, oracle_mod):
         rows, _, rc = _run(pkg, g, tree, cos, order, True, 1e-8, src=src)
         assert rc == 0
         _compare(rows, ref, True, 0)
+
+
+OPENING = 0.2 / 60.0 * 3.141592653589793 / 180.0
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("exact", [True, False])
+@pytest.mark.parametrize("plane,stop_bundle", [("sachs", "redshift"), ("normal", "r")])
+def test_catalogue_bundle_matches_reference(cat_setup, pkg, order, exact, plane, stop_bundle):
+    """jacobiantype = bundle: four-ray Jacobians from the sixth ray on and at
+    convergence.  The finite difference over a 0.2 arcmin screen divides ray
+    position errors by ~6e-5 of the distance, so the Jacobian columns agree to
+    1e-6 (exact) / 1e-2 (fast); angles and redshifts as in the infinitesimal
+    case (the Newton iteration converges to the same root)."""
+    g, tree, cos = cat_setup
+    for ia in (0, 2):
+        acc = float(g["cat_accuracy"][ia])
+        rows, stats, rc = pkg.catalogue(tree, cos, g["cat_src"], float(g["cosmo_length"]), float(g["cosmo_h"]),
+                                        float(g["cosmo_mpc"]), cat_accuracy=acc, nsteps=int(g["nsteps"]), order=order,
+                                        vobs=g["cat_vobs"], exact=exact, jacobian="bundle", plane=plane,
+                                        stop_bundle=stop_bundle, openingmin=OPENING)
+        assert rc == 0
+        ref = g["ref_cat_bundle_o%d_a%d_%s_%s" % (order, ia, plane, stop_bundle)]
+        tol = TOL[exact]
+        failed = ref[:, 2] == 42
+        np.testing.assert_array_equal(rows[:, 2] == 42, failed)
+        np.testing.assert_array_equal(rows[failed, 5], ref[failed, 5])
+        same = ~failed & (rows[:, 5] == ref[:, 5])
+        assert (~failed).sum() - same.sum() <= 0
+        # rejected sources went through 6 bundle Newton steps: the angle error is the Jacobian's times the miss
+        atol = tol["angle"] if ia == 0 else (1e-10 if exact else 1e-8)
+        assert np.abs(rows[same, 2:4] - ref[same, 2:4]).max(initial=0) <= atol
+        conv = same & (ref[:, 5] != 42)
+        assert np.abs(rows[conv, 6:12] - ref[conv, 6:12]).max(initial=0) <= tol["z"]
+        jtol = 1e-6 if exact else 1e-2
+        assert np.abs(rows[same, 12:16] - ref[same, 12:16]).max(initial=0) <= jtol
+        assert stats["rays"] > (~failed).sum()
