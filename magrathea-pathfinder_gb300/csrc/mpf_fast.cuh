@@ -499,7 +499,10 @@ struct JacSums {
     __device__ __forceinline__ double& ckm1(int q) const { return base[(12 + q) * kFastThreads]; }
 };
 
-template <int ORDER, bool SRC>
+// SRC: source mode (one surface at the ray's own radius); WIDE: per-ray
+// surfaces and wide surface records (bundle rays).  The plain instantiation,
+// the map and benchmark path, carries neither.
+template <int ORDER, bool SRC, bool WIDE>
 __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* L, long long i,
                                const PropOut& O, JacSums J)
 {
@@ -509,9 +512,9 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     const double inv_scale = 1.0 / scale;
     const int np = SRC ? 1 : P.nplanes;
     const int skind = SRC ? (int)STOP_R : P.stop_kind;
-    const double* rpl = (!SRC && P.ray_planes) ? P.ray_planes + i * np : P.planes;   // this ray's surfaces
-    const double stop_ref = SRC ? P.ray_stop[i] : (P.ray_planes ? rpl[np - 1] : P.stop_ref);
-    const int rec_fields = SRC ? kSourceFields : (P.wide ? kWideFields : kPlaneFields);
+    const double* rpl = (WIDE && P.ray_planes) ? P.ray_planes + i * np : P.planes;   // this ray's surfaces
+    const double stop_ref = SRC ? P.ray_stop[i] : ((WIDE && P.ray_planes) ? rpl[np - 1] : P.stop_ref);
+    const int rec_fields = SRC ? kSourceFields : (WIDE ? kWideFields : kPlaneFields);
     unsigned long long* const st = O.stats;
     FastRec b;
     if (SRC) {
@@ -694,7 +697,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                     o[17] = b.phi * f + p.phi * (1 - f);
                     o[18] = have_rmax ? rmax : 0.0;
                     o[19] = 1.0;
-                    if (SRC || P.wide) {
+                    if (SRC || WIDE) {
                         o[20] = b.k0 * f + p.k0 * (1 - f);
                         o[21] = b.k1 * f + p.k1 * (1 - f);
                         o[22] = b.k2 * f + p.k2 * (1 - f);
@@ -788,11 +791,11 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             const bool found = (ck >= 1) && (ck < size);
             const bool valid = found && !((ck - 1) == size - 1 || (ck - 1) == 0);
             if (ck < 0 || ck == 0 || ck >= size) {
-                for (int q = 0; q < (P.wide ? 24 : kPlaneFields); ++q) o[q] = 0.0;
+                for (int q = 0; q < (WIDE ? 24 : kPlaneFields); ++q) o[q] = 0.0;
                 o[0] = (ck == 0) ? 0.0 : (double)(size - 1);
             }
             o[19] = valid ? 1.0 : 0.0;
-            if (P.wide) o[24] = found ? 1.0 : 0.0;
+            if (WIDE) o[24] = found ? 1.0 : 0.0;
         }
     }
     if (status) atomicOr(O.status, status);
@@ -807,7 +810,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
 #else
 #define MPF_FAST_BOUNDS __launch_bounds__(kFastThreads, MPF_FAST_MINB)
 #endif
-template <int ORDER, bool SRC>
+template <int ORDER, bool SRC, bool WIDE>
 __global__ void MPF_FAST_BOUNDS k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
                                                                     const double* __restrict__ launch, long long n, PropOut O,
                                                                     unsigned long long* queue)
@@ -821,7 +824,7 @@ __global__ void MPF_FAST_BOUNDS k_propagate_fast(DevTree T, DevCosmo C, PropPara
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= (unsigned long long)n) break;
         const long long i = (long long)base + lane;
-        if (i < n) propagate_fast<ORDER, SRC>(T, C, P, launch + 6 * i, i, O, J);
+        if (i < n) propagate_fast<ORDER, SRC, WIDE>(T, C, P, launch + 6 * i, i, O, J);
         __syncwarp();
     }
 }

@@ -8,18 +8,21 @@
 #include <cstdlib>
 
 namespace mpf {
-// one instantiation per interpolation order, and per mode (surfaces / sources)
+// one instantiation per interpolation order, and per mode (surfaces / sources / wide surfaces)
 static void launch_fast_kernel(long long grid, int tpb, const DevTree& T, const DevCosmo& C, const PropParams& P,
                                const double* d_launch, long long n, const PropOut& O, unsigned long long* queue,
                                cudaStream_t stream)
 {
     const unsigned g = (unsigned)grid;
     if (P.ray_stop) {
-        if (P.order == 1) k_propagate_fast<1, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
-        else k_propagate_fast<2, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
+        if (P.order == 1) k_propagate_fast<1, true, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
+        else k_propagate_fast<2, true, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
+    } else if (P.wide || P.ray_planes) {
+        if (P.order == 1) k_propagate_fast<1, false, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
+        else k_propagate_fast<2, false, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
     } else {
-        if (P.order == 1) k_propagate_fast<1, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
-        else k_propagate_fast<2, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
+        if (P.order == 1) k_propagate_fast<1, false, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
+        else k_propagate_fast<2, false, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
     }
 }
 
@@ -32,7 +35,7 @@ cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const P
     static int blocks_per_sm = 0, sms = 0;
     static unsigned long long* queue = nullptr;   // one work counter per process (calls on a stream are ordered)
     if (blocks_per_sm == 0) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_propagate_fast<2, false>, tpb, 0);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_propagate_fast<2, false, false>, tpb, 0);
         int dev = 0;
         if (e == cudaSuccess) e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -81,7 +84,7 @@ cudaError_t launch_propagate_fast_with_queue(const DevTree& T, const DevCosmo& C
     if (n <= 0) return cudaSuccess;
     const int tpb = kFastThreads;
     int blocks_per_sm = 0, sms = 0, dev = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_propagate_fast<2, false>, tpb, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_propagate_fast<2, false, false>, tpb, 0);
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
