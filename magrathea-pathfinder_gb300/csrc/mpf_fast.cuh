@@ -125,6 +125,16 @@ __device__ __forceinline__ void stat(unsigned long long* st, int k)
     if (st) atomicAdd(st + k, 1ull);
 }
 
+// Build-time diagnostics (-DMPF_DIAG=1): counts of the rare paths, read by
+// the launcher when MPF_STATS is set.  [0] gather restarts at a coarser
+// cell, [1] full walks from the top grid.
+#if MPF_DIAG
+__device__ unsigned long long g_diag[4];
+#define MPF_DIAG_COUNT(k) atomicAdd(&g_diag[k], 1ull)
+#else
+#define MPF_DIAG_COUNT(k) ((void)0)
+#endif
+
 // Out-of-line slow paths (reference semantics with full walks), single copies
 // so that the hot loop stays small in the instruction cache.
 __device__ __noinline__ Field7 tsc_slow(const DevTree& T, double x, double y, double z, int need_all)
@@ -170,6 +180,7 @@ __device__ __forceinline__ float cells_per_unit(int L) { return __int_as_float((
 // full location by a walk from the top grid (float64 coordinates)
 __device__ __noinline__ Loc locate_full(const DevTree& T, double x, double y, double z)
 {
+    MPF_DIAG_COUNT(1);
     Loc r;
     const Found f = locate(T, x, y, z);
     r.cell = f.cell;
@@ -320,6 +331,7 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
             return true;
         }
         const int lc = rec_flags(T, e) & 255;
+        MPF_DIAG_COUNT(0);
         const double x = pos.px(), y = pos.py(), z = pos.pz();
         const Found f = find_cell(T, lc, axis_coord(lc, x), axis_coord(lc, y), axis_coord(lc, z));
         if (f.cell < 0 || f.level != lc) return false;
@@ -365,6 +377,7 @@ __device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, const P&
             else res = Field7{rho, phi, gx, gy, gz, a, gt};
             return true;
         }
+        MPF_DIAG_COUNT(0);
         const double x = pos.px(), y = pos.py(), z = pos.pz();
         const Found f = find_cell(T, lvl, axis_coord(lvl, x), axis_coord(lvl, y), axis_coord(lvl, z));
         if (f.cell < 0 || f.level != lvl) return false;

@@ -63,6 +63,11 @@ cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const P
         cudaStreamSynchronize(stream);
         fprintf(stderr, "mpf_stats rk_rec %llu rk_slow %llu post_rec %llu post_slow %llu jac_rec %llu jac_slow %llu cell_changes %llu steps %llu\n",
                 h[0], h[1], h[2], h[3], h[4], h[5], h[6], h[7]);
+#if MPF_DIAG
+        unsigned long long dg[4] = {0, 0, 0, 0};
+        cudaMemcpyFromSymbol(dg, g_diag, sizeof(dg));
+        fprintf(stderr, "mpf_diag restarts %llu full_walks %llu\n", dg[0], dg[1]);
+#endif
         cudaFree(dstats);
     }
     return e;
