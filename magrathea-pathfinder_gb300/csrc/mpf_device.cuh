@@ -37,6 +37,7 @@ struct DevTree {
     //   int 27      level | has_children << 8
     //   int 28      bit j set: entry j is at exactly the cell's level
     //   int 29      node index of the cell
+    //   int 30      the parent cell (one level up), or -1
     const int4* stencil;
     int64_t n;
     int Lt;                // level of the top grid

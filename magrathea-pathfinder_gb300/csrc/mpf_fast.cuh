@@ -192,6 +192,93 @@ __device__ __noinline__ Loc locate_full(const DevTree& T, double x, double y, do
     return r;
 }
 
+// A point in the neighbour e (record entry (ox, oy, oz) of the located cell
+// h) when e is not a leaf of h's level: a refined cell of h's level (the
+// point's deepest cell is found by following e's children along the point's
+// octants) or a coarser leaf (the point lies in it).  fx, fy, fz: the point's
+// offset from the neighbour's centre in units of h's cells.  The tree is
+// navigated through the node array and the offsets carried in FP32, instead
+// of a float64 walk from the top grid; r.cell = -2 when neither case applies
+// (a wrapped key, a partly refined node) and the caller walks.
+__device__ __noinline__ Loc neighbour_other(const DevTree& T, const Loc& h, int e, int fl, int ox, int oy, int oz,
+                                            float fx, float fy, float fz)
+{
+    Loc r;
+    r.cell = -2;
+    const int L = h.level;
+    const int le = fl & 255;
+    const uint32_t lim = (uint32_t)((1ull << L) - 1ull);
+    const uint32_t nc[3] = {h.c[0] + (uint32_t)ox, h.c[1] + (uint32_t)oy, h.c[2] + (uint32_t)oz};
+    if (nc[0] > lim || nc[1] > lim || nc[2] > lim) return r;
+    if (le == L && (fl & 256)) {
+        const double w = cell_extent(L);
+        double cen[3] = {h.cen[0] + (ox > 0 ? w : (ox < 0 ? -w : 0.0)), h.cen[1] + (oy > 0 ? w : (oy < 0 ? -w : 0.0)),
+                         h.cen[2] + (oz > 0 ? w : (oz < 0 ? -w : 0.0))};
+        uint32_t c[3] = {nc[0], nc[1], nc[2]};
+        float f[3] = {fx, fy, fz};
+        int cell = e, lev = L;
+        int nd = __ldg(&T.stencil[8 * (size_t)e + 7].y);
+        for (int guard = 0; guard < kMaxLevel; ++guard) {
+            const int2 node = __ldg(T.node + nd);
+            if (node.x < 0) break;   // e's descendant containing the point is a leaf
+            const int b[3] = {f[0] >= 0.f ? 1 : 0, f[1] >= 0.f ? 1 : 0, f[2] >= 0.f ? 1 : 0};
+            const int nd2 = node.x + (b[0] | (b[1] << 1) | (b[2] << 2));
+            const int2 child = __ldg(T.node + nd2);
+            if (child.y < 0) return r;
+            const double q = pow2(kLevelShift - lev - 2);   // half the child's size
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                cen[d] += b[d] ? q : -q;
+                c[d] = 2u * c[d] + (uint32_t)b[d];
+                f[d] = 2.f * f[d] + 0.5f - (float)b[d];
+            }
+            cell = child.y;
+            nd = nd2;
+            ++lev;
+        }
+        r.cell = cell;
+        r.level = lev;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) { r.c[d] = c[d]; r.cen[d] = cen[d]; r.fd[d] = f[d]; }
+        return r;
+    }
+    if (le < L && !(fl & 256)) {
+        const int k = L - le;
+        const float sk = __int_as_float((127 - k) << 23);   // 2^-k
+        const float fn[3] = {fx, fy, fz};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            r.c[d] = nc[d] >> k;
+            const uint32_t low = nc[d] - (r.c[d] << k);
+            r.fd[d] = ((float)low + 0.5f + fn[d]) * sk - 0.5f;
+            r.cen[d] = coord_center(le, r.c[d]);
+        }
+        r.cell = e;
+        r.level = le;
+        return r;
+    }
+    return r;
+}
+
+// Ancestor of a located cell at the coarser level lc, through the parents
+// stored in the records; c and fd follow (fd' = (fd + bit - 1/2) / 2 per
+// level).  -1 when a parent is missing.
+__device__ __forceinline__ int ancestor_up(const DevTree& T, int cell, int L, int lc, uint32_t* c, float* fd)
+{
+    for (int guard = 0; guard < kMaxLevel && L > lc; ++guard) {
+        const int p = __ldg(&T.stencil[8 * (size_t)cell + 7].z);
+        if (p < 0) return -1;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            fd[d] = (fd[d] + (float)(c[d] & 1u) - 0.5f) * 0.5f;
+            c[d] >>= 1;
+        }
+        cell = p;
+        --L;
+    }
+    return (L == lc) ? cell : -1;
+}
+
 // Deepest cell of point (x, y, z) given a nearby located cell `h`: the offset
 // from h's centre is formed in float64 (one subtraction per axis) and the rest
 // in FP32; the cell is h or one of its 26 neighbours read from h's record when
@@ -223,6 +310,8 @@ __device__ __forceinline__ Loc locate_rel(const DevTree& T, const Loc& h, float 
                     r.fd[0] = rx - (float)ox; r.fd[1] = ry - (float)oy; r.fd[2] = rz - (float)oz;
                     return r;
                 }
+                const Loc r = neighbour_other(T, h, e, fl, ox, oy, oz, rx - (float)ox, ry - (float)oy, rz - (float)oz);
+                if (r.cell != -2) return r;
             }
         }
     }
@@ -261,6 +350,8 @@ __device__ __forceinline__ Loc step_cell(const DevTree& T, const Loc& h, int axi
             else r.cen[2] = moved;
             return r;
         }
+        const Loc r = neighbour_other(T, h, e, fl, ox, oy, oz, h.fd[0], h.fd[1], h.fd[2]);
+        if (r.cell != -2) return r;
     }
     return locate_full(T, x, y, z);
 }
@@ -273,6 +364,7 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
 {
     int cell = d.cell, L = d.level;
     float fd[3] = {d.fd[0], d.fd[1], d.fd[2]};
+    uint32_t c[3] = {d.c[0], d.c[1], d.c[2]};
     for (int guard = 0; guard <= kMaxLevel; ++guard) {
         const int4* rp = T.stencil + 8 * (size_t)cell;
         const int4 r7 = __ldg(rp + 7);
@@ -332,12 +424,18 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
         }
         const int lc = rec_flags(T, e) & 255;
         MPF_DIAG_COUNT(0);
+        // the restart cell is the point's ancestor at level lc
+        const int up = ancestor_up(T, cell, L, lc, c, fd);
+        if (up >= 0) {
+            cell = up;
+            L = lc;
+            continue;
+        }
         const double x = pos.px(), y = pos.py(), z = pos.pz();
         const Found f = find_cell(T, lc, axis_coord(lc, x), axis_coord(lc, y), axis_coord(lc, z));
         if (f.cell < 0 || f.level != lc) return false;
         cell = f.cell;
         L = lc;
-        uint32_t c[3];
         point_cell(L, x, y, z, c, fd);
     }
     return false;
@@ -349,6 +447,7 @@ __device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, const P&
 {
     int cell = d.cell, L = d.level;
     float fd[3] = {d.fd[0], d.fd[1], d.fd[2]};
+    uint32_t c[3] = {d.c[0], d.c[1], d.c[2]};
     for (int guard = 0; guard <= kMaxLevel; ++guard) {
         const int sx = (fd[0] >= 0.f) ? 1 : -1, sy = (fd[1] >= 0.f) ? 1 : -1, sz = (fd[2] >= 0.f) ? 1 : -1;
         const float ax = fabsf(fd[0]), ay = fabsf(fd[1]), az = fabsf(fd[2]);
@@ -378,12 +477,17 @@ __device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, const P&
             return true;
         }
         MPF_DIAG_COUNT(0);
+        const int up = ancestor_up(T, cell, L, lvl, c, fd);
+        if (up >= 0) {
+            cell = up;
+            L = lvl;
+            continue;
+        }
         const double x = pos.px(), y = pos.py(), z = pos.pz();
         const Found f = find_cell(T, lvl, axis_coord(lvl, x), axis_coord(lvl, y), axis_coord(lvl, z));
         if (f.cell < 0 || f.level != lvl) return false;
         cell = f.cell;
         L = lvl;
-        uint32_t c[3];
         point_cell(L, x, y, z, c, fd);
     }
     return false;

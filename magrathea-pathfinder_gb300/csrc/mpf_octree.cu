@@ -209,7 +209,13 @@ __global__ void k_stencil(DevTree T, const int* cell_node, int4* out)
     e[27] = L | ((T.node[nd].x >= 0) ? 256 : 0);
     e[28] = (int)exact;
     e[29] = nd;
-    e[30] = 0;
+    // the parent cell (one level up), for restarts at coarser levels
+    int parent = -1;
+    if (L - 1 >= T.Lt) {
+        const Found f = find_cell(T, L - 1, cx >> 1, cy >> 1, cz >> 1);
+        if (f.cell >= 0 && f.level == L - 1) parent = f.cell;
+    }
+    e[30] = parent;
     e[31] = 0;
     int4* o = out + 8 * i;
     for (int q = 0; q < 8; ++q) o[q] = make_int4(e[4 * q], e[4 * q + 1], e[4 * q + 2], e[4 * q + 3]);
