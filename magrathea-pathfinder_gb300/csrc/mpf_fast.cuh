@@ -35,11 +35,6 @@ constexpr unsigned kFullMask = (1u << 27) - 1u;
 #ifndef MPF_FAST_MINB
 #define MPF_FAST_MINB 2
 #endif
-// 1: the TSC gather runs as a loop over three x-slabs (smaller code, fewer
-// registers); 0: fully unrolled over the 27 cells.
-#ifndef MPF_TSC_SLABS
-#define MPF_TSC_SLABS 0
-#endif
 constexpr int kFastThreads = MPF_FAST_THREADS;
 
 // Utility::interpolate with the uniform index table (same bracketing interval
@@ -375,26 +370,6 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
             tsc_w3(fd[1], wy);
             tsc_w3(fd[2], wz);
             float gx = 0.f, gy = 0.f, gz = 0.f, gt = 0.f, rho = 0.f, phi = 0.f, a = 0.f;
-#if MPF_TSC_SLABS
-            // three x-slabs of 9 cells, one loop body: a third of the code and
-            // of the loads in flight (the accumulation order is unchanged)
-            const int* re = reinterpret_cast<const int*>(rp);
-#pragma unroll 1
-            for (int sx = 0; sx < 3; ++sx) {
-                const float wxs = (sx == 0) ? wx[0] : (sx == 1) ? wx[1] : wx[2];
-#pragma unroll
-                for (int jj = 0; jj < 9; ++jj) {
-                    const int ej = __ldg(re + 9 * sx + jj);
-                    const float wt = wxs * wy[jj / 3] * wz[jj % 3];
-                    const float4 g = __ldg(T.grad + ej);
-                    gx = fmaf(g.x, wt, gx); gy = fmaf(g.y, wt, gy); gz = fmaf(g.z, wt, gz); gt = fmaf(g.w, wt, gt);
-                    if (need_all) {
-                        const float4 s = __ldg(T.scal + ej);
-                        rho = fmaf(s.x, wt, rho); phi = fmaf(s.y, wt, phi); a = fmaf(s.z, wt, a);
-                    }
-                }
-            }
-#else
             int e[28];
 #pragma unroll
             for (int q = 0; q < 7; ++q) {
@@ -411,7 +386,6 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
                     rho = fmaf(s.x, wt, rho); phi = fmaf(s.y, wt, phi); a = fmaf(s.z, wt, a);
                 }
             }
-#endif
             res = Field7{rho, phi, gx, gy, gz, a, gt};
             return true;
         }
