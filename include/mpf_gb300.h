@@ -249,6 +249,92 @@ int mpf_hmaps_fill_bundle(const mpf_octree* o, const mpf_cosmology* c, const mpf
  * launches): vec[3n]. */
 int mpf_pix2vec_ring(int64_t nside, int64_t n, const int64_t* pixels, double* vec);
 
+/* ------------------------------------------------------------------------ */
+/* Learned field surrogate                                                   */
+/* ------------------------------------------------------------------------ */
+/* A per-cone neural field that stands in for the octree gather
+ * (SimpleHyperOctree::tsc / cic, src/magrathea/simplehyperoctree.h:1410-1644)
+ * inside the RK4 stages of Integrator::integrate (src/integrator.h:648-824).
+ * It has no counterpart in the reference; the octree path stays its judge and
+ * fallback.  Network: (x, y, z, a) normalised to [-1, 1]^4 -> 64 Fourier
+ * frequencies (sin, cos: 128 features) -> 4 hidden layers of 128 with SiLU ->
+ * 5 outputs (phi, dphidx, dphidy, dphidz, dphidt), BF16 weights and FP32
+ * accumulation on the tensor cores at inference, FP32 training. */
+typedef struct mpf_surrogate mpf_surrogate;
+
+#define MPF_SURROGATE_PARAMS 68112   /* W1 b1 W2 b2 W3 b3 W4 b4 (128x128, 128) W5 (16x128) b5 (16); W row-major [out][in] */
+#define MPF_SURROGATE_NORM 274       /* lo[4] sc[4] freq[64][4] mean[5] std[5]: u = (p - lo) * sc - 1, s_j = freq_j . u */
+
+typedef struct {
+    double tan_half[2];        /* tangents of the cone's half-openings about +x, in y and z */
+    double r_min, r_max;       /* radial range of the training samples (octree units) */
+    double a_min, a_max;       /* range of the scale-factor input */
+    double freq_sigma[4];      /* standard deviation of the Fourier frequencies (cycles over the
+                                  normalised range [-1, 1]) for x, y, z, a */
+    uint64_t seed;             /* frequencies, initial weights and the sample stream */
+} mpf_surrogate_domain;
+
+typedef struct {
+    int64_t samples;           /* training samples (a fresh batch per step, samples / batch steps) */
+    int64_t batch;             /* >= 256 */
+    double lr;                 /* Adam learning rate, cosine decay to lr / 100 */
+    int64_t stat_samples;      /* samples for the output normalisation (mean / std) */
+} mpf_surrogate_train_params;
+
+typedef struct {
+    double loss_first, loss_last;   /* mean normalised loss over the first / last 1% of the steps */
+    int64_t steps;
+    double seconds;
+    double samples_per_second;
+    int kernel_launches_per_step;   /* kernels in the captured training step */
+} mpf_surrogate_train_stats;
+
+typedef struct {
+    double tolerance;          /* relative drift of the checkpointed deflection that flags a photon */
+    int check_every;           /* octree re-check period in RK4 steps (>= 1) */
+    int fallback;              /* 1: flagged photons are re-run on the plain octree path in the call */
+} mpf_surrogate_prop_params;
+
+typedef struct {
+    int64_t photon_steps;      /* RK4 steps taken with the surrogate */
+    int64_t flagged_photons;
+    int64_t fallback_photons;  /* re-run on the octree */
+    int64_t fallback_steps;
+    double surrogate_seconds;  /* device time of the surrogate launch */
+    double fallback_seconds;
+} mpf_surrogate_prop_stats;
+
+int mpf_surrogate_create(const mpf_surrogate_domain* d, mpf_surrogate** out);
+void mpf_surrogate_destroy(mpf_surrogate* s);
+/* Draw `samples` points uniform in the cone and fit the network to the
+ * octree's TSC field there (MSE on outputs normalised by their mean / std). */
+int mpf_surrogate_train(mpf_surrogate* s, const mpf_octree* o, const mpf_surrogate_train_params* p,
+                        mpf_surrogate_train_stats* stats);
+/* n training samples of the stream from index `first`: inputs n x 4 (x y z a),
+ * targets n x 5 (phi dphidx dphidy dphidz dphidt from the octree's TSC). */
+int mpf_surrogate_sample(const mpf_surrogate* s, const mpf_octree* o, uint64_t first, int64_t n, float* inputs,
+                         float* targets);
+/* Parameters (MPF_SURROGATE_PARAMS floats) and normalisation (MPF_SURROGATE_NORM
+ * floats); either pointer may be NULL. */
+int mpf_surrogate_get_params(const mpf_surrogate* s, float* params, float* norm);
+int mpf_surrogate_set_params(mpf_surrogate* s, const float* params, const float* norm);
+/* Training loss and its gradient (MPF_SURROGATE_PARAMS floats) on a given
+ * batch, through the training kernels. */
+int mpf_surrogate_loss_grad(mpf_surrogate* s, int64_t n, const float* inputs, const float* targets, double* loss,
+                            float* grad);
+/* Network outputs (n x 5) through the tensor-core inference path. */
+int mpf_surrogate_eval(mpf_surrogate* s, int64_t n, const float* inputs, float* out);
+/* Integrator::integrate with the surrogate in the RK4 stages (no surfaces, no
+ * Jacobian): p gives length, nsteps, order (of the octree re-checks), stop and
+ * stop_value, max_steps; launch[6n] as mpf_propagate.  Outputs (host):
+ * steps[n], final_rec[28n] (may be NULL; rho and ah are 0 for surrogate
+ * photons), flags[n] (bit 0: drift above tolerance, bit 1: max_steps),
+ * drift[n] (may be NULL).  With sp->fallback, flagged photons' steps and
+ * records come from the plain octree path (mpf_propagate, FP32 gathers). */
+int mpf_surrogate_propagate(mpf_surrogate* s, const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p,
+                            const mpf_surrogate_prop_params* sp, int64_t n, const double* launch, int64_t* steps,
+                            double* final_rec, uint8_t* flags, float* drift, mpf_surrogate_prop_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

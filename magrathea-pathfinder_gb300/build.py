@@ -27,6 +27,7 @@ UNITS = [
     ("mpf_noalloc.cu", []),
     ("mpf_catalogue.cu", ["-fmad=false"]),
     ("mpf_maps.cu", ["-fmad=false"]),
+    ("mpf_surrogate.cu", []),
 ]
 
 

@@ -27,7 +27,13 @@ EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_uplo
            "mpf_octree_get_info", "mpf_octree_destroy", "mpf_cosmology_upload", "mpf_cosmology_destroy", "mpf_locate",
            "mpf_interpolate", "mpf_propagate", "mpf_propagate_device", "mpf_propagate_noalloc",
            "mpf_noalloc_last_error", "mpf_catalogue_newton",
-           "mpf_catalogue_newton_device", "mpf_hmaps_fill", "mpf_hmaps_fill_bundle", "mpf_pix2vec_ring")
+           "mpf_catalogue_newton_device", "mpf_hmaps_fill", "mpf_hmaps_fill_bundle", "mpf_pix2vec_ring",
+           "mpf_surrogate_create", "mpf_surrogate_destroy", "mpf_surrogate_train", "mpf_surrogate_sample",
+           "mpf_surrogate_get_params", "mpf_surrogate_set_params", "mpf_surrogate_loss_grad", "mpf_surrogate_eval",
+           "mpf_surrogate_propagate")
+
+MPF_SURROGATE_PARAMS = 68112
+MPF_SURROGATE_NORM = 274
 
 # map component names (the reference's map_components keys) -> mpf_map_component
 MAP_COMPONENTS = {"lensing": 0, "dr": 2, "dl": 3, "dt": 4, "da": 5, "dz": 6, "ds": 7, "isw": 8, "dens": 9,
@@ -63,6 +69,29 @@ class CatalogueParams(C.Structure):
 class CatalogueStats(C.Structure):
     _fields_ = [("rays", C.c_int64), ("photon_steps", C.c_int64), ("photon_steps_jacobian", C.c_int64),
                 ("iterations", C.c_int), ("kernel_launches", C.c_int)]
+
+
+class SurrogateDomain(C.Structure):
+    _fields_ = [("tan_half", C.c_double * 2), ("r_min", C.c_double), ("r_max", C.c_double), ("a_min", C.c_double),
+                ("a_max", C.c_double), ("freq_sigma", C.c_double * 4), ("seed", C.c_uint64)]
+
+
+class SurrogateTrainParams(C.Structure):
+    _fields_ = [("samples", C.c_int64), ("batch", C.c_int64), ("lr", C.c_double), ("stat_samples", C.c_int64)]
+
+
+class SurrogateTrainStats(C.Structure):
+    _fields_ = [("loss_first", C.c_double), ("loss_last", C.c_double), ("steps", C.c_int64), ("seconds", C.c_double),
+                ("samples_per_second", C.c_double), ("kernel_launches_per_step", C.c_int)]
+
+
+class SurrogatePropParams(C.Structure):
+    _fields_ = [("tolerance", C.c_double), ("check_every", C.c_int), ("fallback", C.c_int)]
+
+
+class SurrogatePropStats(C.Structure):
+    _fields_ = [("photon_steps", C.c_int64), ("flagged_photons", C.c_int64), ("fallback_photons", C.c_int64),
+                ("fallback_steps", C.c_int64), ("surrogate_seconds", C.c_double), ("fallback_seconds", C.c_double)]
 
 
 _lib = None
@@ -103,9 +132,20 @@ def load(path: str = LIB_PATH):
     L.mpf_hmaps_fill_bundle.argtypes = [vp, vp, C.POINTER(Params), i64, i64, vp, C.c_int, vp, vp, C.c_int, C.c_int, d,
                                         vp]
     L.mpf_pix2vec_ring.argtypes = [i64, i64, vp, vp]
+    L.mpf_surrogate_create.argtypes = [C.POINTER(SurrogateDomain), C.POINTER(vp)]
+    L.mpf_surrogate_destroy.argtypes = [vp]
+    L.mpf_surrogate_destroy.restype = None
+    L.mpf_surrogate_train.argtypes = [vp, vp, C.POINTER(SurrogateTrainParams), C.POINTER(SurrogateTrainStats)]
+    L.mpf_surrogate_sample.argtypes = [vp, vp, C.c_uint64, i64, vp, vp]
+    L.mpf_surrogate_get_params.argtypes = [vp, vp, vp]
+    L.mpf_surrogate_set_params.argtypes = [vp, vp, vp]
+    L.mpf_surrogate_loss_grad.argtypes = [vp, i64, vp, vp, C.POINTER(d), vp]
+    L.mpf_surrogate_eval.argtypes = [vp, i64, vp, vp]
+    L.mpf_surrogate_propagate.argtypes = [vp, vp, vp, C.POINTER(Params), C.POINTER(SurrogatePropParams), i64, vp, vp,
+                                          vp, vp, vp, C.POINTER(SurrogatePropStats)]
     for name in EXPORTS:
         if name not in ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_destroy",
-                        "mpf_cosmology_destroy", "mpf_noalloc_last_error"):
+                        "mpf_cosmology_destroy", "mpf_noalloc_last_error", "mpf_surrogate_destroy"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L

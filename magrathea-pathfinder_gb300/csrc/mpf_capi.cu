@@ -77,6 +77,8 @@ bool fill_params(const mpf_params* p, mpf::PropParams& P)
 
 }  // namespace
 
+int mpf_internal_set_error(int code, const char* msg) { return set_err(code, msg ? msg : ""); }
+
 extern "C" {
 
 int mpf_version(void) { return 1; }

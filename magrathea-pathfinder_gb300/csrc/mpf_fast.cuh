@@ -132,15 +132,15 @@ __device__ unsigned long long g_diag[4];
 
 // Out-of-line slow paths (reference semantics with full walks), single copies
 // so that the hot loop stays small in the instruction cache.
-__device__ __noinline__ Field7 tsc_slow(const DevTree& T, double x, double y, double z, int need_all)
+static __device__ __noinline__ Field7 tsc_slow(const DevTree& T, double x, double y, double z, int need_all)
 {
     return tsc<false>(T, x, y, z, need_all != 0);
 }
-__device__ __noinline__ Field7 cic_slow(const DevTree& T, double x, double y, double z, int need_all)
+static __device__ __noinline__ Field7 cic_slow(const DevTree& T, double x, double y, double z, int need_all)
 {
     return cic<false>(T, x, y, z, need_all != 0);
 }
-__device__ __noinline__ Found locate_slow(const DevTree& T, double x, double y, double z) { return locate(T, x, y, z); }
+static __device__ __noinline__ Found locate_slow(const DevTree& T, double x, double y, double z) { return locate(T, x, y, z); }
 
 // A point given by its float64 coordinates.
 struct PosAt {
@@ -173,7 +173,7 @@ struct Loc {
 __device__ __forceinline__ float cells_per_unit(int L) { return __int_as_float((127 + L - kLevelShift) << 23); }
 
 // full location by a walk from the top grid (float64 coordinates)
-__device__ __noinline__ Loc locate_full(const DevTree& T, double x, double y, double z)
+static __device__ __noinline__ Loc locate_full(const DevTree& T, double x, double y, double z)
 {
     MPF_DIAG_COUNT(1);
     Loc r;
@@ -195,7 +195,7 @@ __device__ __noinline__ Loc locate_full(const DevTree& T, double x, double y, do
 // navigated through the node array and the offsets carried in FP32, instead
 // of a float64 walk from the top grid; r.cell = -2 when neither case applies
 // (a wrapped key, a partly refined node) and the caller walks.
-__device__ __noinline__ Loc neighbour_other(const DevTree& T, const Loc& h, int e, int fl, int ox, int oy, int oz,
+static __device__ __noinline__ Loc neighbour_other(const DevTree& T, const Loc& h, int e, int fl, int ox, int oy, int oz,
                                             float fx, float fy, float fz)
 {
     Loc r;
@@ -921,7 +921,7 @@ __global__ void MPF_FAST_BOUNDS k_propagate_fast(DevTree T, DevCosmo C, PropPara
 }
 
 // Fast-mode gathers through the stencil records (tests / mpf_interpolate).
-__global__ void k_gather_rec(DevTree T, int kind, const double* __restrict__ xyz, long long n, void* out)
+static __global__ void k_gather_rec(DevTree T, int kind, const double* __restrict__ xyz, long long n, void* out)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;

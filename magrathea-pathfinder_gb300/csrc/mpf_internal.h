@@ -34,6 +34,9 @@ struct mpf_cosmology {
     double* slope_dadt;
 };
 
+// sets the calling thread's mpf_last_error() message; returns code
+int mpf_internal_set_error(int code, const char* msg);
+
 namespace mpf {
 
 // exclusive scan of n int32 values in place on `stream`; returns the total

@@ -1,0 +1,176 @@
+"""GPU tests of the learned field surrogate (mpf_surrogate_* through the C ABI).
+
+Tolerances:
+  training kernels (FP32) against the float64 restatement: loss within 1e-5
+    relative, every gradient within 2e-3 relative of the largest gradient of
+    its block;
+  tensor-core inference against the restatement with bfloat16 features,
+    weights and activations: normalised outputs within 0.03 absolute (the
+    FP32 accumulation order and the bfloat16 rounding of a few activations
+    near ties differ);
+  fallback: photons re-run on the octree are bit-identical to mpf_propagate.
+"""
+import numpy as np
+import pytest
+
+import surrogate_mlp as M
+
+pytestmark = pytest.mark.gpu
+
+Z_STOP = 0.5
+
+
+@pytest.fixture(scope="module")
+def cone(gpu_lib, pkg, synth):
+    """The small uniform cone: a 64^3 periodic field at octree level 8 over a
+    5 x 5 degree cone to z = 0.5."""
+    cos = synth.Cosmology()
+    chi = float(cos.chi_of_z(Z_STOP)[0])
+    spec = synth.OctreeSpec(base_level=8, box_cells=64, lbox=2048.0, half_y=2.5, half_z=2.5, chi_max=chi * 1.05,
+                            halos=0, max_level=8)
+    tree = pkg.Octree.from_records(synth.make_octree(spec))
+    cosmo = pkg.Cosmology(*cos.conformal_table(n=4000, amin=0.05))
+    length = spec.lbox * synth.MPC / spec.cosmo.h
+    r_max = chi * 1.02 / spec.lbox
+    yield dict(tree=tree, cosmo=cosmo, length=length, r_max=r_max, spec=spec, synth=synth)
+    tree.close()
+    cosmo.close()
+
+
+def _surrogate(cone, seed=7):
+    import importlib
+    S = importlib.import_module("magrathea-pathfinder_gb300.surrogate")
+    t = np.tan(np.radians(2.5))
+    return S.Surrogate((t, t), r_max=cone["r_max"], a_min=1.0 / (1.0 + Z_STOP) - 0.05, freq_sigma=(6.0, 1.5, 1.5, 0.5),
+                       seed=seed)
+
+
+def _random_norm(s, seed=5):
+    _, norm = s.get_params()
+    rng = np.random.default_rng(seed)
+    o = 8 + 4 * M.FREQ
+    norm[o:o + M.OUT] = rng.normal(0, 1e-3, M.OUT)
+    norm[o + M.OUT:o + 2 * M.OUT] = rng.uniform(0.5, 2.0, M.OUT) * 1e-2
+    return norm
+
+
+def test_sample_labels_are_octree_tsc(cone):
+    s = _surrogate(cone)
+    x, t = s.sample(cone["tree"], 2000)
+    # x (the depth along the axis) is in [r_min, r_max]; |y|, |z| <= x tan(2.5 deg)
+    assert np.all((x[:, 0] >= 0) & (x[:, 0] <= cone["r_max"] * (1 + 1e-6)))
+    ty = np.tan(np.radians(2.5))
+    assert np.all(np.abs(x[:, 1]) <= x[:, 0] * ty * (1 + 1e-5) + 1e-7)
+    # the labels were gathered at the float64 point; the float32 copy differs by one rounding
+    f = cone["tree"].tsc(x[:, :3].astype(np.float64), exact=False)    # rho phi dx dy dz a dt
+    ref = f[:, [1, 2, 3, 4, 6]]
+    assert np.all(np.abs(t - ref) <= 1e-4 * np.abs(ref).max(axis=0))
+    assert np.all(np.abs(x[:, 3] - f[:, 5]) <= 1e-6)
+    s.close()
+
+
+def test_training_gradient_matches_oracle(cone):
+    s = _surrogate(cone)
+    params = M.random_params(11)
+    norm = _random_norm(s)
+    s.set_params(params, norm)
+    x, t = s.sample(cone["tree"], 1000, first=123)
+    loss, g = s.loss_grad(x, t)
+    ref_loss, ref_g = M.loss_grad(params.astype(np.float64), norm, x, t)
+    assert abs(loss - ref_loss) <= 1e-5 * abs(ref_loss)
+    blocks = [(l * M.LAYER, l * M.LAYER + M.WIDTH * M.WIDTH) for l in range(M.HIDDEN)]
+    blocks += [(l * M.LAYER + M.WIDTH * M.WIDTH, (l + 1) * M.LAYER) for l in range(M.HIDDEN)]
+    blocks += [(M.W5, M.B5), (M.B5, M.NPARAMS)]
+    for a, b in blocks:
+        scale = np.abs(ref_g[a:b]).max()
+        assert np.all(np.abs(g[a:b] - ref_g[a:b]) <= 2e-3 * scale), (a, b)
+    s.close()
+
+
+def test_tensor_core_inference_matches_oracle(cone):
+    s = _surrogate(cone)
+    params = M.random_params(13)
+    norm = _random_norm(s)
+    s.set_params(params, norm)
+    x, _ = s.sample(cone["tree"], 1000, first=77)    # 1000 rows: 7 full tiles and a ragged one
+    got = s.eval(x)
+    _, _, _, mean, std = M.unpack_norm(norm)
+    yn = (got.astype(np.float64) - mean) / std
+    ref = M.forward(params, norm, x, emulate_bf16=True)
+    assert np.abs(yn - ref).max() <= 0.03, np.abs(yn - ref).max()
+    # the FP64 network is within the bfloat16 error of both
+    assert np.abs(yn - M.forward(params, norm, x)).max() <= 0.1
+    assert s.eval(np.zeros((0, 4), dtype=np.float32)).shape == (0, 5)
+    s.close()
+
+
+@pytest.fixture(scope="module")
+def trained(cone):
+    s = _surrogate(cone, seed=3)
+    stats = s.train(cone["tree"], samples=4_000_000, batch=8192, lr=2e-3)
+    yield s, stats
+    s.close()
+
+
+def test_training_reduces_loss(trained):
+    _, st = trained
+    assert st["steps"] == 4_000_000 // 8192
+    assert st["loss_last"] < 0.1 * st["loss_first"], st
+
+
+def test_trained_network_beats_untrained(cone, trained):
+    """What training gains: the field error on held-out points against the
+    same network before training."""
+    s, _ = trained
+    x, t = s.sample(cone["tree"], 20000, first=10 ** 12)
+    err_trained = np.abs(s.eval(x) - t)
+    fresh = _surrogate(cone, seed=3)
+    _, norm_trained = s.get_params()
+    fresh.set_params(None, norm_trained)
+    err_fresh = np.abs(fresh.eval(x) - t)
+    fresh.close()
+    scale = t.std(axis=0)
+    # gradient outputs (the RK4 stages read them): mean error well under the untrained one
+    for q in (1, 2, 3):
+        assert err_trained[:, q].mean() < 0.25 * err_fresh[:, q].mean(), q
+        assert err_trained[:, q].mean() < 0.5 * scale[q], q
+
+
+def _deflection(launch, final):
+    d = launch[:, 3:]
+    x = final[:, 2:5]
+    return np.arctan2(np.linalg.norm(np.cross(d, x), axis=1), np.sum(d * x, axis=1))
+
+
+def test_fallback_photons_equal_plain_path(cone, trained, pkg):
+    s, _ = trained
+    launch = cone["synth"].photon_grid(16, 2.5, 2.5)
+    kw = dict(nsteps=10, order=2, stop="redshift", stop_value=Z_STOP)
+    ref_steps, ref_final, _, _ = pkg.propagate(cone["tree"], cone["cosmo"], launch, cone["length"], jacobian=False,
+                                               exact=False, **kw)
+    # tolerance 0 flags every photon: all results come from the octree path
+    steps, final, flags, drift, st = s.propagate(cone["tree"], cone["cosmo"], launch, cone["length"], tolerance=0.0, **kw)
+    assert np.all(flags & 1) and st["fallback_photons"] == launch.shape[0]
+    np.testing.assert_array_equal(steps, ref_steps)
+    np.testing.assert_array_equal(final.view(np.uint64), ref_final.view(np.uint64))
+
+
+def test_surrogate_photons_track_plain_path(cone, trained, pkg):
+    s, _ = trained
+    launch = cone["synth"].photon_grid(24, 2.5, 2.5)
+    kw = dict(nsteps=10, order=2, stop="redshift", stop_value=Z_STOP)
+    ref_steps, ref_final, _, _ = pkg.propagate(cone["tree"], cone["cosmo"], launch, cone["length"], jacobian=False,
+                                               exact=False, **kw)
+    steps, final, flags, drift, st = s.propagate(cone["tree"], cone["cosmo"], launch, cone["length"], tolerance=np.inf,
+                                                 fallback=False, **kw)
+    assert not np.any(flags & 1) and st["fallback_photons"] == 0
+    assert st["photon_steps"] == int((steps - 1).sum())
+    # same stop: step counts within a few steps, redshift at the stop within the step's increment
+    assert np.all(np.abs(steps - ref_steps) <= 3)
+    assert np.all(np.abs(final[:, 19] - ref_final[:, 19]) <= 2e-3)
+    dref = _deflection(launch, ref_final)
+    dsur = _deflection(launch, final)
+    rel = np.abs(dsur - dref) / dref
+    assert np.median(rel) < 0.2, np.median(rel)
+    # the drift estimate is computed and finite for every photon
+    assert np.all(np.isfinite(drift)) and np.all(drift >= 0)
