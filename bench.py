@@ -14,6 +14,13 @@ than L2, so no flush is needed between steps.
 Metric: RK4 photon-steps per second (one accepted RK4 step of one ray =
 one photon-step, src/integrator.h:776).
 
+--mode surrogate measures the learned field surrogate (a third line): the
+64^3 field at octree level 8 over a 5 x 5 degree cone to z = 2, 1000 x 1000
+rays, the network trained on 50M octree-labelled samples first; value = the
+surrogate form's photon-steps/s with flagged rays re-run on the octree, with
+the plain octree path on the same rays and the measured deflection error
+beside it.
+
 --mode catalogue measures the catalogue root-finder instead (a second JSON
 line, not the headline): one step = one batch of sources on the same octree,
 uniform in comoving volume inside the cone out to z = 2, solved to
@@ -197,6 +204,172 @@ def catalogue_sources(synth, n, seed, zmax=2.0, half_deg=4.5):
     return src
 
 
+SURR_UNIT = UNIT
+# tensor-core work per network evaluation of one point: 4 hidden layers 128x128
+# and the output layer 16x128 (multiply-add = 2 FLOP); evaluations per step:
+# RK4 stages 2-4 and the post-step point
+SURR_FLOP_PER_EVAL = 2 * (4 * 128 * 128 + 16 * 128)
+SURR_EVALS_PER_STEP = 4
+SURR_TOLERANCE = 1e-3
+
+
+def surrogate_workload(synth):
+    """The uniform 64^3 field (octree level 8) over a 5 x 5 degree cone to z = 2."""
+    cosmo = synth.Cosmology()
+    chi2 = float(cosmo.chi_of_z(2.0)[0])
+    return synth.OctreeSpec(base_level=8, box_cells=64, lbox=2048.0, half_y=2.5, half_z=2.5, chi_max=chi2 * 1.02,
+                            halos=0, max_level=8, seed=42), chi2
+
+
+def measured_peak_bf16():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def _deflection_vec(launch, final):
+    x = final[:, 2:5]
+    return np.cross(launch[:, 3:], x) / np.linalg.norm(x, axis=1)[:, None]
+
+
+def run_surrogate(args, synth, world, rank, local, dist):
+    spec, chi2 = surrogate_workload(synth)
+    cos = cosmology_table(synth)
+    length = spec.lbox * synth.MPC / spec.cosmo.h
+    train_samples = int(args.surrogate_samples)
+    config = {"workload": "64^3 periodic field at octree level 8 over a 5x5 deg cone to z=2; 1000x1000 rays; TSC, "
+                          "10 steps/cell; surrogate: 64 Fourier frequencies, 4x128 SiLU, 5 outputs, trained on %d "
+                          "octree-labelled samples; octree re-check every 64 steps, fallback above %g relative "
+                          "deflection drift" % (train_samples, SURR_TOLERANCE),
+              "rays": 1000 * 1000, "batch_rays": args.batch, "order": "TSC", "nsteps": 10, "z_stop": 2.0,
+              "l2": "inputs and octree re-checks only; the network lives in shared memory",
+              "parallelism": "replicas" if world > 1 else "single GPU"}
+    kw = dict(nsteps=10, order=2, stop="redshift", stop_value=2.0)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import oracle as oracle_mod
+        oracle_mod.build()
+        rec = synth.make_octree(spec)
+        launch = ray_grid(1000, 2.5)
+        nthreads = os.cpu_count() or 1
+        O = oracle_mod.Oracle(rec, {"t": cos[0], "a": cos[1], "dadt": cos[2]}, length, nthreads=nthreads)
+        rng = np.random.default_rng(3)
+        per_step = 8 * nthreads
+        times, counts = [], []
+        for k in range(args.warmup + args.steps):
+            idx = rng.choice(launch.shape[0], size=per_step, replace=False)
+            t0 = time.perf_counter()
+            st, _, _ = O.propagate(launch[idx], order=2, nsteps=10, stop="redshift", planes=np.array([2.0]),
+                                   jacobian=False)
+            dt = time.perf_counter() - t0
+            if k >= args.warmup:
+                times.append(dt)
+                counts.append(int(st.sum()))
+        value = sum(counts) / sum(times)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "impl": "reference",
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                                 "sample": "%d random rays per step, C oracle restating the reference's octree "
+                                           "path (the reference has no surrogate)" % per_step},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    pkg = importlib.import_module(PKG)
+    importlib.import_module(PKG + ".build").build()
+    lib = pkg.library()
+    capi = importlib.import_module(PKG + ".capi")
+    Sur = importlib.import_module(PKG + ".surrogate").Surrogate
+    tree = pkg.Octree.from_records(synth.make_octree(spec))
+    cosmo = pkg.Cosmology(*cos)
+    t = np.tan(np.radians(2.5))
+    sur = Sur((t, t), r_max=chi2 * 1.02 / spec.lbox, a_min=1.0 / 3.0 - 0.05, freq_sigma=(6.0, 1.5, 1.5, 0.5),
+              seed=42 + rank)
+    train = sur.train(tree, samples=train_samples, batch=16384, lr=2e-3)
+    launch = ray_grid(1000, 2.5)
+    B = min(args.batch, launch.shape[0])
+    nb = launch.shape[0] // B
+    dev = torch.device("cuda", local)
+    replicas = importlib.import_module(PKG + ".replicas")
+    d_launch = torch.from_numpy(launch).to(dev)
+    d_steps = torch.zeros(B, dtype=torch.int64, device=dev)
+    d_final = torch.zeros(B * capi.MPF_PHOTON_FIELDS, dtype=torch.float64, device=dev)
+    d_status = torch.zeros(1, dtype=torch.int32, device=dev)
+    p, keep = capi.make_params(length, jacobian=False, exact=False, **kw)
+    stream = torch.cuda.current_stream(dev)
+    plain_ms, plain_steps, sur_s, sur_steps, rel_all, flagged = [], 0, [], 0, [], 0
+    whole_s, whole_steps, e2e_t = [], 0, []
+    with Clocks(local) as clk:
+        for k in range(args.warmup + args.steps):
+            off = replicas.batch_ids(k, rank, world, nb) * B
+            h = np.ascontiguousarray(launch[off:off + B])
+            # plain octree path, device-resident inputs
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            capi.check(lib.mpf_propagate_device(tree._h, cosmo._h, C.byref(p), B, C.c_void_p(d_launch.data_ptr() + off * 48),
+                                                C.c_void_p(d_steps.data_ptr()), C.c_void_p(d_final.data_ptr()), None,
+                                                C.c_void_p(d_status.data_ptr()), C.c_void_p(stream.cuda_stream)))
+            b.record(stream)
+            torch.cuda.synchronize()
+            ref_final = d_final.view(B, -1).cpu().numpy()
+            ref_steps = d_steps.cpu().numpy()
+            # surrogate kernel alone (no fallback): speed and measured accuracy
+            st, fin, fl, drift, ss = sur.propagate(tree, cosmo, h, length, tolerance=np.inf, fallback=False, **kw)
+            # the surrogate form at the tolerance, through the public call (host buffers, fallback included)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st2, _, fl2, _, ss2 = sur.propagate(tree, cosmo, h, length, tolerance=SURR_TOLERANCE, fallback=True,
+                                                want_final=False, **kw)
+            e2e = time.perf_counter() - t0
+            if k < args.warmup:
+                continue
+            plain_ms.append(a.elapsed_time(b))
+            plain_steps += int((ref_steps - 1).sum())
+            sur_s.append(ss["surrogate_seconds"])
+            sur_steps += ss["photon_steps"]
+            rel_all.append(np.linalg.norm(_deflection_vec(h, fin) - _deflection_vec(h, ref_final), axis=1) /
+                           np.linalg.norm(_deflection_vec(h, ref_final), axis=1))
+            flagged += int((fl2 & 1).sum())
+            delivered = int((st2 - 1).sum())
+            whole_s.append(ss2["surrogate_seconds"] + ss2["fallback_seconds"])
+            whole_steps += delivered
+            e2e_t.append(e2e)
+    rel = np.concatenate(rel_all)
+    n_rays = B * args.steps
+    value = whole_steps / sum(whole_s)
+    plain_value = plain_steps / (sum(plain_ms) / 1000.0)
+    sur_value = sur_steps / sum(sur_s)
+    peak, peak_kind = measured_peak_bf16()
+    achieved = sur_value * SURR_EVALS_PER_STEP * SURR_FLOP_PER_EVAL / 1e12
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * sum(whole_s) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 state, bf16 network", "data": "synthetic",
+            "config": config,
+            "form": "surrogate with octree fallback at %g relative deflection drift" % SURR_TOLERANCE,
+            "surrogate": {"kernel_steps_per_s": sur_value, "plain_steps_per_s": plain_value,
+                          "kernel_vs_plain": sur_value / plain_value,
+                          "flagged_fraction": flagged / n_rays,
+                          "rel_deflection_error": {"median": float(np.median(rel)), "p90": float(np.percentile(rel, 90)),
+                                                   "max": float(rel.max())},
+                          "training": train},
+            "e2e": {"value": whole_steps / sum(e2e_t), "unit": UNIT, "h2d_bytes_per_step": B * 6 * 8,
+                    "d2h_bytes_per_step": B * (8 + 1 + 4)},
+            "gpu_launches": 2 * args.steps,
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "traffic": None, "peak_source": peak_kind + " (MEASURED_PEAKS.json bf16_tflops)",
+                         "flop_per_photon_step": SURR_EVALS_PER_STEP * SURR_FLOP_PER_EVAL},
+            "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -221,8 +394,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--zstop", type=float, default=2.0, help="stop redshift (profiling captures use a short path)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--mode", default="propagate", choices=["propagate", "catalogue"],
-                    help="propagate = the headline ray-tracing benchmark; catalogue = the Newton root-finder")
+    ap.add_argument("--mode", default="propagate", choices=["propagate", "catalogue", "surrogate"],
+                    help="propagate = the headline ray-tracing benchmark; catalogue = the Newton root-finder; "
+                         "surrogate = the learned field in the RK4 stages against the plain octree")
+    ap.add_argument("--surrogate-samples", type=float, default=50e6, help="training samples of the surrogate")
     ap.add_argument("--sources", type=int, default=65536, help="catalogue sources per step")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
@@ -239,6 +414,8 @@ def main():
     planes = np.array([args.zstop])
     if args.mode == "catalogue":
         return run_catalogue(args, synth, spec, cos, length, world, rank, local, dist)
+    if args.mode == "surrogate":
+        return run_surrogate(args, synth, world, rank, local, dist)
 
     if args.impl == "reference":
         if rank != 0:

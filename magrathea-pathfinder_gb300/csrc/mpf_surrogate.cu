@@ -74,7 +74,18 @@ static_assert(kPackBytes % 16 == 0, "operand tiles must stay 16-byte aligned");
 static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
 static_assert(kSmemSlot + 16 <= kSmemBytes, "barriers inside the allocation");
 
-__device__ __forceinline__ float silu(float x) { return __fdividef(x, 1.f + __expf(-x)); }
+// silu(x) = h + h tanh(h) with h = x / 2, on a pair of values packed as
+// bfloat16 (one tanh per pair on the special-function unit, one packed FMA);
+// h0, h1 are the halved pre-activations in FP32
+__device__ __forceinline__ uint32_t silu2_bf16(float h0, float h1)
+{
+    const __nv_bfloat162 hh = __floats2bfloat162_rn(h0, h1);
+    const uint32_t h = *reinterpret_cast<const uint32_t*>(&hh);
+    uint32_t t, y;
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(h));
+    asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(y) : "r"(h), "r"(t));
+    return y;
+}
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
 {
@@ -191,7 +202,8 @@ __device__ __forceinline__ void evaluate(Group& g, const Spec& S, const float* p
                     for (int q = 0; q < 16; ++q) v[q] = 0.f;
                 uint32_t w[8];
 #pragma unroll
-                for (int q = 0; q < 8; ++q) w[q] = pack_bf16(silu(v[2 * q] + bl[16 * c + 2 * q]), silu(v[2 * q + 1] + bl[16 * c + 2 * q + 1]));
+                for (int q = 0; q < 8; ++q)   // the packed image holds b / 2 for the hidden layers
+                    w[q] = silu2_bf16(fmaf(v[2 * q], 0.5f, bl[16 * c + 2 * q]), fmaf(v[2 * q + 1], 0.5f, bl[16 * c + 2 * q + 1]));
                 *reinterpret_cast<uint4*>(g.act + umma::tile_offset(128, g.tid, 16 * c)) = make_uint4(w[0], w[1], w[2], w[3]);
                 *reinterpret_cast<uint4*>(g.act + umma::tile_offset(128, g.tid, 16 * c + 8)) = make_uint4(w[4], w[5], w[6], w[7]);
             }
@@ -672,7 +684,8 @@ __global__ void k_adam(int np, float* w, const float* __restrict__ g, float* m, 
 
 __global__ void k_step_inc(long long* step) { *step += 1; }
 
-// FP32 parameters -> inference image (BF16 tiles in the operand layout, FP32 biases)
+// FP32 parameters -> inference image (BF16 tiles in the operand layout; FP32
+// biases, those of the hidden layers halved for silu2_bf16)
 __global__ void k_pack(const float* __restrict__ prm, unsigned char* out)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -687,7 +700,7 @@ __global__ void k_pack(const float* __restrict__ prm, unsigned char* out)
     }
     if (q < kHidden * kWidth) {
         const int l = q / kWidth, c = q % kWidth;
-        reinterpret_cast<float*>(out + kPackB)[q] = prm[l * kLayerStride + kWidth * kWidth + c];
+        reinterpret_cast<float*>(out + kPackB)[q] = 0.5f * prm[l * kLayerStride + kWidth * kWidth + c];   // halved: see silu2_bf16
     }
     if (q < kOutPad) reinterpret_cast<float*>(out + kPackB5)[q] = prm[kB5 + q];
 }

@@ -26,7 +26,8 @@ constexpr int kB5 = kW5 + kOutPad * kWidth;              // output bias [16]
 constexpr int kParams = kB5 + kOutPad;
 
 // Inference image of the parameters (bytes): BF16 weight tiles in the
-// tensor-core operand layout (mpf_umma.cuh), FP32 biases.
+// tensor-core operand layout (mpf_umma.cuh), FP32 biases (those of the hidden
+// layers halved: the activation is formed from z / 2).
 constexpr int kPackW5 = kHidden * kWidth * kWidth * 2;
 constexpr int kPackB = kPackW5 + kOutPad * kWidth * 2;
 constexpr int kPackB5 = kPackB + kHidden * kWidth * 4;

@@ -68,17 +68,21 @@ def bf16(a):
 
 
 def forward(params, norm, x, emulate_bf16: bool = False):
-    """Normalised outputs (n x 5).  emulate_bf16: round features, weights and
-    hidden activations to bfloat16 as the tensor-core path stores them."""
+    """Normalised outputs (n x 5).  emulate_bf16: the tensor-core path's
+    roundings: bfloat16 features and weights, and the activation formed on
+    bfloat16 pairs as h + h tanh(h) with h = z / 2 rounded to bfloat16."""
     Ws, bs = unpack_params(params)
     h = features(norm, x)
     if emulate_bf16:
         h = bf16(h)
         Ws = [bf16(W) for W in Ws]
     for l in range(HIDDEN):
-        h = _silu(h @ Ws[l].T + bs[l])
+        z = h @ Ws[l].T + bs[l]
         if emulate_bf16:
-            h = bf16(h)
+            hh = bf16(0.5 * z)
+            h = bf16(hh + hh * bf16(np.tanh(hh)))
+        else:
+            h = _silu(z)
     y = h @ Ws[HIDDEN].T + bs[HIDDEN]
     return y[:, :OUT]
 
