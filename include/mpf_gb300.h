@@ -250,6 +250,37 @@ int mpf_hmaps_fill_bundle(const mpf_octree* o, const mpf_cosmology* c, const mpf
 int mpf_pix2vec_ring(int64_t nside, int64_t n, const int64_t* pixels, double* vec);
 
 /* ------------------------------------------------------------------------ */
+/* Ray bundles (the rays driver)                                             */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int count;                 /* nbundle: photons on the circle around each central photon */
+    double angle;              /* opening: half-angle of the bundle's cone (radians) */
+    int interpolation;         /* stop_ray, the reference parameter the bundle rays are compared at:
+                                  MPF_STOP_REDSHIFT, _A (1/a - 1), _T, _LAMBDA or _RADIUS (distance from
+                                  the start); any other value is read as redshift, as the reference does */
+    double amin;               /* 0, or the scale factor (of the data) every ray must reach */
+    int64_t capacity;          /* trajectory points kept per ray; a longer ray is an error */
+} mpf_bundle_params;
+
+#define MPF_TRAJECTORY_FIELDS 29
+
+/* Integrator::propagate (src/integrator.h:861-1015), the per-photon body of
+ * the rays driver (src/rays.cpp:278, 322), for n central photons:
+ * photons[6n] = start x y z and direction dtdl-normalised as launched (dxdl
+ * dydl dzdl, not renormalised); rotation[n] (may be NULL: 0) the circle's
+ * rotation.  Each bundle (the photon and `count` photons at `angle` around it,
+ * Integrator::launch integrator.h:346-380) is integrated without a stop
+ * criterion (integrator.h:477-618), checked, and the central ray's angular
+ * diameter distance computed.  Outputs: sizes[n] = central trajectory size (0
+ * when the bundle is rejected), central[n x capacity x 29] = its points in the
+ * trajectory file's column order (index a t x y z dtdl dxdl dydl dzdl level ah
+ * rho phi dphidx dphidy dphidz dphidl laplacian redshift dsdl2 error distance
+ * isw iswold chi lambda dphidt s; src/output.h:200-211, README 6.3).
+ * p: length, nsteps, order, exact, max_steps (stop, planes, Jacobian unused). */
+int mpf_rays_propagate(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, const mpf_bundle_params* bp,
+                       int64_t n, const double* photons, const double* rotation, int64_t* sizes, double* central);
+
+/* ------------------------------------------------------------------------ */
 /* Learned field surrogate                                                   */
 /* ------------------------------------------------------------------------ */
 /* A per-cone neural field that stands in for the octree gather

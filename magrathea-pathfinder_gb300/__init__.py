@@ -17,6 +17,8 @@ Integrator::integrate       ``propagate(...)`` (batched over rays), with
 Catalogues::relCat /        ``catalogue(...)``: the Newton root-finder for a
   iterateNewtonMethod       batch of sources, relCat's 16-column rows
 Hmaps::FillMap              ``hmaps_fill(...)``: pixels in, float map rows out
+Integrator::propagate       ``rays_propagate(...)``: the rays driver's bundles
+ (rays)                      and the central ray's angular diameter distance
 pix2vec_ring                ``pix2vec_ring(nside, pixels)`` (device)
 ==========================  ==================================================
 """
@@ -37,7 +39,7 @@ PLANE_FIELDS = ("firstid f x y z distance A11 A12 A22 t a redshift chi lambda s 
 CATALOGUE_FIELDS = ("phi theta phi_obs theta_obs miss iterations z_flrw z_pot z_dopp z_tdopp z_isw z_gr "
                     "a11 a12 a21 a22").split()
 
-__all__ = ["Octree", "Cosmology", "propagate", "catalogue", "hmaps_fill", "pix2vec_ring", "MpfError", "PHOTON_FIELDS", "PLANE_FIELDS",
+__all__ = ["Octree", "Cosmology", "propagate", "rays_propagate", "catalogue", "hmaps_fill", "pix2vec_ring", "MpfError", "PHOTON_FIELDS", "PLANE_FIELDS",
            "CATALOGUE_FIELDS", "library"]
 
 
@@ -154,6 +156,33 @@ def propagate(octree: Octree, cosmology: Cosmology, launch, length: float, nstep
     capi.check(rc)
     del keep
     return steps, final, pout, rc
+
+
+def rays_propagate(octree: Octree, cosmology: Cosmology, photons, length: float, count: int, angle: float,
+                   rotation=None, interpolation: str = "redshift", amin: float = 0.0, nsteps: int = 10, order: int = 2,
+                   exact: bool = False, capacity: int = 20000, max_steps: int = 0):
+    """Integrator::propagate for n central photons (the rays driver's bundles).
+
+    photons[n, 6]: start x y z and the launch direction (not renormalised);
+    rotation[n]: the circle's rotation (None: 0).  Returns (sizes[n],
+    central[n, capacity, 29]): each central trajectory in the trajectory
+    file's column order with its angular diameter distance; size 0 when the
+    bundle is rejected.
+    """
+    L = capi.load()
+    ph = np.ascontiguousarray(photons, dtype=np.float64).reshape(-1, 6)
+    n = ph.shape[0]
+    rot = None if rotation is None else np.ascontiguousarray(rotation, dtype=np.float64).reshape(n)
+    p, keep = capi.make_params(length, nsteps, order, "r", 0.0, None, False, exact, max_steps)
+    bp = capi.BundleParams()
+    bp.count, bp.angle, bp.amin, bp.capacity = int(count), float(angle), float(amin), int(capacity)
+    bp.interpolation = capi.STOP.get(interpolation, 0)
+    sizes = np.zeros(n, dtype=np.int64)
+    central = np.zeros((n, int(capacity), capi.MPF_TRAJECTORY_FIELDS))
+    capi.check(L.mpf_rays_propagate(octree._h, cosmology._h, C.byref(p), C.byref(bp), n, capi.ptr(ph), capi.ptr(rot),
+                                    capi.ptr(sizes), capi.ptr(central)))
+    del keep
+    return sizes, central
 
 
 def catalogue(octree: Octree, cosmology: Cosmology, sources, length: float, h: float, mpc: float = 3.08568e22,

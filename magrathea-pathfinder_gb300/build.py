@@ -1,9 +1,11 @@
 """Build recipe of the native library (libmpf_gb300.so) for sm_103a.
 
 Compiles each CUDA translation unit with nvcc in parallel and links a shared
-library next to this file.  The reference-order translation unit and the
-catalogue root-finder are built with -fmad=false so their float64 arithmetic
-keeps the reference's rounding; the others keep FMA contraction.
+library next to this file.  The reference-order translation unit, the
+catalogue root-finder, the map rows and the ray bundles are built with
+-fmad=false so their float64 arithmetic keeps the reference's rounding (the
+bundles' host code also without FMA contraction); the others keep FMA
+contraction.
 """
 from __future__ import annotations
 
@@ -28,6 +30,7 @@ UNITS = [
     ("mpf_catalogue.cu", ["-fmad=false"]),
     ("mpf_maps.cu", ["-fmad=false"]),
     ("mpf_surrogate.cu", []),
+    ("mpf_rays.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
 ]
 
 

@@ -30,7 +30,9 @@ EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_uplo
            "mpf_catalogue_newton_device", "mpf_hmaps_fill", "mpf_hmaps_fill_bundle", "mpf_pix2vec_ring",
            "mpf_surrogate_create", "mpf_surrogate_destroy", "mpf_surrogate_train", "mpf_surrogate_sample",
            "mpf_surrogate_get_params", "mpf_surrogate_set_params", "mpf_surrogate_loss_grad", "mpf_surrogate_eval",
-           "mpf_surrogate_propagate")
+           "mpf_surrogate_propagate", "mpf_rays_propagate")
+
+MPF_TRAJECTORY_FIELDS = 29
 
 MPF_SURROGATE_PARAMS = 68112
 MPF_SURROGATE_NORM = 274
@@ -69,6 +71,11 @@ class CatalogueParams(C.Structure):
 class CatalogueStats(C.Structure):
     _fields_ = [("rays", C.c_int64), ("photon_steps", C.c_int64), ("photon_steps_jacobian", C.c_int64),
                 ("iterations", C.c_int), ("kernel_launches", C.c_int)]
+
+
+class BundleParams(C.Structure):
+    _fields_ = [("count", C.c_int), ("angle", C.c_double), ("interpolation", C.c_int), ("amin", C.c_double),
+                ("capacity", C.c_int64)]
 
 
 class SurrogateDomain(C.Structure):
@@ -132,6 +139,7 @@ def load(path: str = LIB_PATH):
     L.mpf_hmaps_fill_bundle.argtypes = [vp, vp, C.POINTER(Params), i64, i64, vp, C.c_int, vp, vp, C.c_int, C.c_int, d,
                                         vp]
     L.mpf_pix2vec_ring.argtypes = [i64, i64, vp, vp]
+    L.mpf_rays_propagate.argtypes = [vp, vp, C.POINTER(Params), C.POINTER(BundleParams), i64, vp, vp, vp, vp]
     L.mpf_surrogate_create.argtypes = [C.POINTER(SurrogateDomain), C.POINTER(vp)]
     L.mpf_surrogate_destroy.argtypes = [vp]
     L.mpf_surrogate_destroy.restype = None

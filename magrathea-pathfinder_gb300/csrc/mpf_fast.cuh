@@ -546,6 +546,26 @@ __device__ __forceinline__ void rhs_math(const DevCosmo& C, const Field7& g, con
     out[8] = fma(coef, in[8], -(double)(g.dz * k02));
 }
 
+// The photon record (Photon<double,3> fields) of a fast-mode trajectory point;
+// data_dt: the field's dphidt there, dphi_over_dl: the laplacian column
+// ((phi - previous phi) / dl), k: the point's index.
+__device__ __forceinline__ Rec fast_record(const FastRec& b, float data_dt, double dphi_over_dl, long long k)
+{
+    const double c2 = kC * kC;
+    Rec r;
+    r.a = b.a; r.t = b.t; r.x = b.x; r.y = b.y; r.z = b.z; r.k0 = b.k0; r.k1 = b.k1; r.k2 = b.k2; r.k3 = b.k3;
+    r.level = b.level; r.ah = b.ah; r.rho = b.rho; r.phi = b.phi;
+    r.dx = b.dx; r.dy = b.dy; r.dz = b.dz; r.dt = b.dt;
+    r.dphidl = (k > 0) ? ((double)data_dt * b.k0 + ((double)b.dx * b.k1 + (double)b.dy * b.k2 + (double)b.dz * b.k3)) : 0.0;
+    r.lap = (k > 0) ? dphi_over_dl : 0.0;
+    const double kk = b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3;
+    r.ds2 = (b.a * b.a) * (-(c2 * (1.0 + 2.0 * (b.phi / c2)) * b.k0 * b.k0) + ((1.0 - 2.0 * (b.phi / c2)) * kk));
+    r.err = 1.0 - ((1.0 - 2.0 * (b.phi / c2)) * kk) / (c2 * (1.0 + 2.0 * (b.phi / c2)) * b.k0 * b.k0);
+    r.red = b.red; r.isw = b.isw; r.iswold = b.iswold; r.chi = b.chi; r.lambda = b.lambda; r.s = b.s;
+    r.index = (double)k;
+    return r;
+}
+
 // Jacobian terms (d1d1, d1d2, d2d2 of lensing.h:430-447) at a trajectory
 // point located at `here`: six TSC gathers at +-1 cell.
 __device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, double x, double y, double z, float* out3,
@@ -608,8 +628,8 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     const int rec_fields = SRC ? kSourceFields : (WIDE ? kWideFields : kPlaneFields);
     unsigned long long* const st = O.stats;
     FastRec b;
-    if (SRC) {
-        // (phi, theta) launch form: the direction is given
+    if (SRC || (WIDE && P.direct)) {
+        // (phi, theta) launch form or a bundle photon: the direction is given
         b.a = 1.0; b.t = 0.0; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = 1.0;
         b.k1 = L[3]; b.k2 = L[4]; b.k3 = L[5];
     } else {
@@ -640,6 +660,9 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     float last_dphi = 0.f;
     double last_dl = 1.0;
 
+    // every trajectory point (bundle rays), wide instantiation only
+    double* const traj = (WIDE && O.traj) ? O.traj + i * O.traj_cap * kPhotonFields : nullptr;
+    if (WIDE && traj && O.traj_cap > 0) write_rec(traj, fast_record(b, 0.f, 0.0, 0));
     int next_plane = 0;
     long long cross_k[kMaxPlanes];
     for (int j = 0; j < np; ++j) cross_k[j] = -1;
@@ -829,6 +852,10 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             have_rmax = true;
             b = p;
             inv_a = inv_pa;
+            if (WIDE && traj) {
+                if (k < O.traj_cap) write_rec(traj + k * kPhotonFields, fast_record(b, last_data_dt, (double)last_dphi / last_dl, k));
+                else status |= 8u;
+            }
         }
         bool stop;
         switch (skind) {
@@ -849,18 +876,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     if (O.final_rec) {
         double* o = O.final_rec + i * kPhotonFields;
         if (size == k + 1) {
-            Rec r;
-            r.a = b.a; r.t = b.t; r.x = b.x; r.y = b.y; r.z = b.z; r.k0 = b.k0; r.k1 = b.k1; r.k2 = b.k2; r.k3 = b.k3;
-            r.level = b.level; r.ah = b.ah; r.rho = b.rho; r.phi = b.phi;
-            r.dx = b.dx; r.dy = b.dy; r.dz = b.dz; r.dt = b.dt;
-            r.dphidl = (k > 0) ? ((double)last_data_dt * b.k0 + ((double)b.dx * b.k1 + (double)b.dy * b.k2 + (double)b.dz * b.k3)) : 0.0;
-            r.lap = (k > 0) ? (double)last_dphi / last_dl : 0.0;
-            const double kk = b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3;
-            r.ds2 = (b.a * b.a) * (-(c2 * (1.0 + 2.0 * (b.phi / c2)) * b.k0 * b.k0) + ((1.0 - 2.0 * (b.phi / c2)) * kk));
-            r.err = 1.0 - ((1.0 - 2.0 * (b.phi / c2)) * kk) / (c2 * (1.0 + 2.0 * (b.phi / c2)) * b.k0 * b.k0);
-            r.red = b.red; r.isw = b.isw; r.iswold = b.iswold; r.chi = b.chi; r.lambda = b.lambda; r.s = b.s;
-            r.index = (double)k;
-            write_rec(o, r);
+            write_rec(o, fast_record(b, last_data_dt, (double)last_dphi / last_dl, k));
         } else {
             for (int q = 0; q < kPhotonFields; ++q) o[q] = 0.0;
             status |= 4u;

@@ -8,7 +8,8 @@
 #include <cstdlib>
 
 namespace mpf {
-// one instantiation per interpolation order, and per mode (surfaces / sources / wide surfaces)
+// one instantiation per interpolation order, and per mode (surfaces / sources /
+// wide surfaces, per-ray surfaces, direction launches, trajectories)
 static void launch_fast_kernel(long long grid, int tpb, const DevTree& T, const DevCosmo& C, const PropParams& P,
                                const double* d_launch, long long n, const PropOut& O, unsigned long long* queue,
                                cudaStream_t stream)
@@ -17,7 +18,7 @@ static void launch_fast_kernel(long long grid, int tpb, const DevTree& T, const 
     if (P.ray_stop) {
         if (P.order == 1) k_propagate_fast<1, true, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
         else k_propagate_fast<2, true, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
-    } else if (P.wide || P.ray_planes) {
+    } else if (P.wide || P.ray_planes || P.direct || O.traj) {
         if (P.order == 1) k_propagate_fast<1, false, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
         else k_propagate_fast<2, false, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
     } else {

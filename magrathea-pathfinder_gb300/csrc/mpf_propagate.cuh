@@ -64,6 +64,10 @@ struct PropParams {
     const double* ray_planes;
     // surface records of kWideFields doubles instead of kPlaneFields
     int wide;
+    // launch records give the start point and the direction itself (the
+    // bundle photons of Integrator::launch(photon, count, angle, rotation),
+    // whose direction is not renormalised before integrate)
+    int direct;
 };
 
 struct PropOut {
@@ -72,6 +76,8 @@ struct PropOut {
     double* plane_rec;     // n x nplanes x 20, or null
     unsigned* status;      // bit 0: a ray hit max_steps
     unsigned long long* stats;   // optional path counters (fast mode), or null
+    double* traj;          // n x traj_cap x 28: every trajectory point, or null
+    long long traj_cap;    // points kept per ray (status bit 3 when a ray has more)
 };
 
 // Utility::interpolate (src/utility.h:441-449)
@@ -210,8 +216,9 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
     const double stop_ref = SRC ? P.ray_stop[i] : (P.ray_planes ? rpl[np - 1] : P.stop_ref);
     const int rec_fields = SRC ? kSourceFields : (P.wide ? kWideFields : kPlaneFields);
     Rec b;
-    if (SRC) {
-        // launch, (phi, theta) form (src/integrator.h:305-329): direction given
+    if (SRC || P.direct) {
+        // launch, (phi, theta) form (src/integrator.h:305-329), or a bundle
+        // photon (integrator.h:346-380): direction given
         b.a = one; b.t = zero; b.x = L[0]; b.y = L[1]; b.z = L[2]; b.k0 = one;
         b.k1 = L[3]; b.k2 = L[4]; b.k3 = L[5];
         b.index = 0.0;
@@ -244,6 +251,8 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
     double dl = (loc.cell >= 0 ? cell_extent(loc.level) : 0.0) * ratio;
     const double a0 = b.a;
     const double phi0c2 = b.phi / c2;
+    double* const traj = O.traj ? O.traj + i * O.traj_cap * kPhotonFields : nullptr;
+    if (traj && O.traj_cap > 0) write_rec(traj, b);
 
     // surfaces
     int next_plane = 0;
@@ -389,6 +398,10 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
             if (!have_rmax || rmax_before_b < b.rho) rmax_before_b = b.rho;
             have_rmax = true;
             b = p;
+            if (traj) {
+                if (k < O.traj_cap) write_rec(traj + k * kPhotonFields, b);
+                else status |= 8u;
+            }
         }
         // stop test on trajectory.back()
         bool stop = false;

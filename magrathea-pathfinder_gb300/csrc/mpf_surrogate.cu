@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_propagate_surrogate(DevTree T, 
                 b.k1 *= nk; b.k2 *= nk; b.k3 *= nk;
                 b.a = interp_fast(C, b.t, C.a, C.slope_a);
                 b.level = (here.cell >= 0) ? here.level : 0;
-                b.ah = data.a;
+                b.ah = 0.f;   // integrator.h:684-685 overwrites data.a() with zero at the start
                 b.rho = data.rho; b.phi = data.phi; b.dx = data.dx; b.dy = data.dy; b.dz = data.dz; b.dt = data.dt;
                 b.red = 0.0; b.isw = 0.0; b.chi = 0.0; b.iswold = 0.0; b.lambda = 0.0; b.s = 0.0;
                 dl = (here.cell >= 0 ? cell_extent(here.level) : 0.0) * (b.a * b.a * ratio_k);

@@ -6,6 +6,8 @@
   sources the rays cannot reach (id and columns 0-4 then column 4 again, at
   the stream's default 6 significant digits) and ``<name>_reject.txt`` for
   sources that did not converge (same columns as the main file).
+* Ray trajectories as the rays driver writes them (Output::save,
+  src/output.h:200-211): 29 columns per point, 17 significant digits.
 * HEALPix maps as FITS binary tables (the reference calls chealpix's
   write_healpix_map, src/hmaps.cpp:496-510): one float column, RING (or
   NESTED) ordering, the HEALPix keywords, non-normal values replaced by
@@ -52,6 +54,32 @@ def write_catalogue(name: str, rows: np.ndarray, sources: np.ndarray) -> tuple:
             else:
                 fr.write(" ".join([_g(s[6], 17)] + [_g(v, 17) for v in c] + [_g(s[7], 17)]) + "\n")
     return good, err, rej
+
+
+# --------------------------------------------------------------------------
+# trajectories
+# --------------------------------------------------------------------------
+TRAJECTORY_COLUMNS = ("index a t x y z dtdl dxdl dydl dzdl level ah rho phi dphidx dphidy dphidz dphidl laplacian "
+                      "redshift dsdl2 error distance isw iswold chi lambda dphidt s").split()
+
+
+def trajectory_text(points: np.ndarray) -> str:
+    """A trajectory as Output::save writes it (src/output.h:200-211): one
+    photon per line, its 29 values separated by spaces at 17 significant
+    digits (the step index as an integer)."""
+    pts = np.asarray(points, dtype=np.float64)
+    if pts.ndim != 2 or pts.shape[1] != len(TRAJECTORY_COLUMNS):
+        raise ValueError("a trajectory is m x 29")
+    lines = []
+    for row in pts:
+        lines.append(" ".join(["%d" % int(row[0])] + [_g(v, 17) for v in row[1:]]))
+    return "".join(l + "\n" for l in lines)
+
+
+def write_trajectory(path: str, points: np.ndarray) -> str:
+    with open(path, "w") as f:
+        f.write(trajectory_text(points))
+    return path
 
 
 # --------------------------------------------------------------------------

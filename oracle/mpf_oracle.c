@@ -717,6 +717,142 @@ int64_t mpfo_trajectory(const mpfo_tree* T, const mpfo_cosmo* C, int order, doub
 }
 
 /* ---------------------------------------------------------------------- */
+/* ray bundles: Integrator::propagate (integrator.h:861-1015)              */
+/* ---------------------------------------------------------------------- */
+/* reference parameter of point k (integrator.h:925-969) */
+static double bundle_ref(const double* tr, int64_t k, int kind)
+{
+    const double* p = tr + MPFO_PHOTON * k;
+    switch (kind) {
+    case MPFO_STOP_A: return 1 / p[PA] - 1;
+    case MPFO_STOP_T: return p[PT];
+    case MPFO_STOP_LAMBDA: return p[PLAMBDA];
+    case MPFO_STOP_R: {
+        const double dx = p[PX] - tr[PX], dy = p[PY] - tr[PY], dz = p[PZ] - tr[PZ];
+        return sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    default: return p[PZRED];
+    }
+}
+
+/* Utility::interpolate (utility.h:441-449) of coordinate q of a ray at x0 */
+static double bundle_interp(double x0, const double* tr, int64_t n, int kind, int q)
+{
+    int64_t first = 0, count = n;
+    while (count > 0) {
+        const int64_t step = count >> 1, it = first + step;
+        if (!(x0 < bundle_ref(tr, it, kind))) { first = it + 1; count -= step + 1; }
+        else count = step;
+    }
+    int64_t i = first;
+    i += (n > 1) * ((i <= 0) - (i >= n));
+    if (n > 1) {
+        const double xm = bundle_ref(tr, i - 1, kind), xi = bundle_ref(tr, i, kind);
+        const double ym = tr[MPFO_PHOTON * (i - 1) + q], yi = tr[MPFO_PHOTON * i + q];
+        return ym + ((yi - ym) * (x0 - xm) / (xi - xm));
+    }
+    return (n > 0) ? tr[q] : 0.0;
+}
+
+int64_t mpfo_propagate_bundle(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
+                              const double* photon, unsigned count, double angle, double rotation, int kind, double amin,
+                              double* out, int64_t cap)
+{
+    static const double zero3[3] = {0, 0, 0};
+    const unsigned total = count + 1;
+    /* Integrator::launch(photon, count, angle, rotation), centre first (integrator.h:346-380) */
+    double* dirs = (double*)malloc(sizeof(double) * 3 * total);
+    {
+        const double zero = 0, one = 1, four = 4;
+        const double pi = four * atan(one);
+        const double step = (pi + pi) / (double)(count + (!count));
+        const double* k = photon + 3;
+        const double r = sqrt((k[0] * k[0]) + (k[1] * k[1]) + (k[2] * k[2]));
+        const double rcos = r * cos(angle), rsin = r * sin(angle);
+        const double costheta = cos(acos(k[2] / r)), sintheta = sin(acos(k[2] / r));
+        const double cosphi = cos(atan2(k[1], k[0])), sinphi = sin(atan2(k[1], k[0]));
+        const double cospsi = cos(rotation), sinpsi = sin(rotation);
+        for (unsigned q = 0; q < total; ++q)
+            for (int d = 0; d < 3; ++d) dirs[3 * q + d] = k[d];
+        if (r > zero) {
+            for (unsigned istep = 0; istep < count; ++istep) {
+                const double x = rsin * cos(istep * step), y = rsin * sin(istep * step), z = rcos;
+                double* o = dirs + 3 * (istep + 1);
+                o[0] = -cosphi * sinpsi * costheta * x - cosphi * cospsi * costheta * y + cosphi * sintheta * z + sinphi * sinpsi * y -
+                       sinphi * cospsi * x;
+                o[1] = -sinphi * sinpsi * costheta * x - sinphi * cospsi * costheta * y - cosphi * sinpsi * y + cosphi * cospsi * x +
+                       sintheta * sinphi * z;
+                o[2] = sintheta * sinpsi * x + sintheta * cospsi * y + costheta * z;
+            }
+        }
+    }
+    /* each ray integrated without a stop criterion (integrator.h:477-618) */
+    ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+    c->T = T; c->C = C; c->order = order; c->length = length;
+    traj_t* trs = (traj_t*)calloc(total, sizeof(traj_t));
+    double* last = (double*)calloc(total, sizeof(double));
+    const double quarter = (4.0 / (2.0 * 1.0)) / 2.0, limit = 1.0 / (2.0 * 2.0 * 2.0);
+    unsigned nt = total;
+    for (unsigned it = 0; it < nt; ++it) {
+        cache_init(&c->cache);
+        double* p = traj_push(&trs[it]);
+        launch6(photon, p);   /* a t x y z, then the given direction as is */
+        p[PK1] = dirs[3 * it]; p[PK2] = dirs[3 * it + 1]; p[PK3] = dirs[3 * it + 2];
+        integrate(c, &trs[it], nsteps, MPFO_STOP_R, INFINITY, zero3);
+        const int64_t size = trs[it].n;
+        if (!size) {
+            nt = 0;
+        } else {
+            const double* front = trs[it].p;
+            const double* back = trs[it].p + MPFO_PHOTON * (size - 1);
+            const double cx = back[PX] - front[PX], cy = back[PY] - front[PY], cz = back[PZ] - front[PZ];
+            last[it] = sqrt(cx * cx + cy * cy + cz * cz);
+            nt *= (last[it] > quarter);
+            nt *= (!(isnormal(amin) && isnormal(back[PAH]) && (back[PAH] < 1.0))) || (!(back[PAH] > amin));
+        }
+    }
+    double mx = last[0], mn = last[0];
+    for (unsigned it = 1; it < total; ++it) {
+        if (last[it] > mx) mx = last[it];
+        if (last[it] < mn) mn = last[it];
+    }
+    nt *= (fabs(mx - mn) / mx < limit);
+    int64_t m = 0;
+    if (nt > 0) {
+        const double* T0 = trs[0].p;
+        m = trs[0].n;
+        for (int64_t k = 0; k < m && k < cap; ++k) {
+            const double* p = T0 + MPFO_PHOTON * k;
+            double d = 0.0;
+            if (nt > 1) {
+                const double x0 = bundle_ref(T0, k, kind);
+                for (unsigned it = 1; it < nt; ++it) {
+                    const double cx = bundle_interp(x0, trs[it].p, trs[it].n, kind, PX) - p[PX];
+                    const double cy = bundle_interp(x0, trs[it].p, trs[it].n, kind, PY) - p[PY];
+                    const double cz = bundle_interp(x0, trs[it].p, trs[it].n, kind, PZ) - p[PZ];
+                    d += sqrt(cx * cx + cy * cy + cz * cz);
+                }
+                d /= (double)(nt - 1);
+                d *= (length * p[PA]) / angle;
+            }
+            double* o = out + 29 * k;
+            o[0] = p[PINDEX];
+            for (int q = 0; q < 9; ++q) o[1 + q] = p[q];
+            o[10] = p[PLEVEL]; o[11] = p[PAH]; o[12] = p[PRHO]; o[13] = p[PPHI];
+            o[14] = p[PDX]; o[15] = p[PDY]; o[16] = p[PDZ]; o[17] = p[PDL]; o[18] = p[PLAP];
+            o[19] = p[PZRED]; o[20] = p[PDS2]; o[21] = p[PERR]; o[22] = d;
+            o[23] = p[PISW]; o[24] = p[PISWOLD]; o[25] = p[PCHI]; o[26] = p[PLAMBDA]; o[27] = p[PDT]; o[28] = p[PS];
+        }
+    }
+    for (unsigned it = 0; it < total; ++it) free(trs[it].p);
+    free(trs);
+    free(last);
+    free(dirs);
+    free(c);
+    return m;
+}
+
+/* ---------------------------------------------------------------------- */
 /* catalogue root-finder                                                   */
 /* ---------------------------------------------------------------------- */
 /* Integrator::launch, (phi, theta) form (integrator.h:305-329). */

@@ -91,6 +91,16 @@ int mpfo_catalogue_jac(const mpfo_tree* T, const mpfo_cosmo* C, int order, doubl
  * Jacobian) and Lensing::dbetadtheta's 2x2 Jacobian at each surface (jac_out,
  * n x np x 4: a11 a12 a21 a22).  plane_sachs: kiTarget = interpolated
  * direction (1) or position (0); stop_bundle: an MPFO_STOP_* value. */
+/* Integrator::propagate (integrator.h:861-1015): the photon (start xyz,
+ * direction as launched) and `count` photons at `angle` around it, integrated
+ * without a stop criterion, the bundle checks and the central ray's angular
+ * diameter distance; kind: the reference parameter (an MPFO_STOP_ value).
+ * out: m x 29 in the trajectory file's column order.  Returns the central
+ * trajectory's size, 0 when the bundle is rejected. */
+int64_t mpfo_propagate_bundle(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
+                              const double* photon, unsigned count, double angle, double rotation, int kind, double amin,
+                              double* out, int64_t cap);
+
 int mpfo_bundle(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps, int stop_kind,
                 int64_t n, const double* launch, int np, const double* planes, int plane_sachs, int stop_bundle,
                 double openingmin, double* plane_out, double* jac_out, int nthreads);

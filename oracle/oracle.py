@@ -62,6 +62,8 @@ def lib():
                                      C.c_int, _p, _p, _p, C.c_int]
         L.mpfo_trajectory.restype = _i64
         L.mpfo_trajectory.argtypes = [_p, _p, C.c_int, _d, C.c_uint, C.c_int, _d, _p, _p, _i64]
+        L.mpfo_propagate_bundle.restype = _i64
+        L.mpfo_propagate_bundle.argtypes = [_p, _p, C.c_int, _d, C.c_uint, _p, C.c_uint, _d, _d, C.c_int, _d, _p, _i64]
         L.mpfo_bundle.restype = C.c_int
         L.mpfo_bundle.argtypes = [_p, _p, C.c_int, _d, C.c_uint, C.c_int, _i64, _p, C.c_int, _p, C.c_int, C.c_int, _d,
                                   _p, _p, C.c_int]
@@ -141,6 +143,17 @@ class Oracle:
         out = np.zeros((cap, 28))
         m = self.L.mpfo_trajectory(C.byref(self.tree), C.byref(self.cosmo), order, self.length, nsteps,
                                    STOP[stop], stop_ref, _ptr(L), _ptr(out), cap)
+        return out[:min(m, cap)]
+
+    def propagate_bundle(self, photon, count, angle, rotation=0.0, interp="redshift", amin=0.0, order=2, nsteps=10,
+                         cap=100000):
+        """Integrator::propagate: photon = start xyz + direction as launched.
+        Returns the central trajectory (m x 29, file column order); empty when rejected."""
+        ph = np.ascontiguousarray(photon, dtype=np.float64)
+        out = np.zeros((cap, 29))
+        m = self.L.mpfo_propagate_bundle(C.byref(self.tree), C.byref(self.cosmo), order, self.length, nsteps, _ptr(ph),
+                                         int(count), float(angle), float(rotation), STOP.get(interp, 0), float(amin),
+                                         _ptr(out), cap)
         return out[:min(m, cap)]
 
     def catalogue(self, sources, order=2, nsteps=10, cat_accuracy=1e-8, h=0.68, mpc=3.08568e22,

@@ -17,6 +17,7 @@
 #include <vector>
 #include <array>
 #include <map>
+#include <sstream>
 #include <atomic>
 #include <thread>
 #include <mpi.h>
@@ -467,6 +468,45 @@ void ref_catalogue(int64_t n, const double* src, const double* rotm1, const doub
                    unsigned nsteps, double h, double mpc, double* out, int nthreads)
 {
     ref_catalogue_jac(n, src, rotm1, vobs, cat_accuracy, nsteps, h, mpc, out, nthreads, "infinitesimal", "normal", "r", 0.0);
+}
+
+// Integrator::propagate (integrator.h:861-1015): the launched photon L (start
+// x y z, end x y z) and `count` photons on a circle of half-angle `angle`
+// around it (rotated by `rotation`), each integrated with the no-stop
+// Integrator::integrate, the bundle checks, and the central ray's angular
+// diameter distance.  out: up to cap points x 29 in the trajectory file's
+// column order (photon_file29); text (up to text_cap bytes, NUL-terminated)
+// receives Output::save of the central trajectory at max_digits10, as the rays
+// driver writes it (output.h:200-211).  Returns the central trajectory's size,
+// 0 when the bundle is rejected.
+static void photon_file29(const Photon<double, 3>& p, double* o)
+{
+    o[0] = (double)p.index(); o[1] = p.a(); o[2] = p.t(); o[3] = p.x(); o[4] = p.y(); o[5] = p.z();
+    o[6] = p.dtdl(); o[7] = p.dxdl(); o[8] = p.dydl(); o[9] = p.dzdl();
+    o[10] = p.level(); o[11] = p.ah(); o[12] = p.rho(); o[13] = p.phi();
+    o[14] = p.dphidx(); o[15] = p.dphidy(); o[16] = p.dphidz(); o[17] = p.dphidl(); o[18] = p.laplacian();
+    o[19] = p.redshift(); o[20] = p.dsdl2(); o[21] = p.error(); o[22] = p.distance();
+    o[23] = p.isw(); o[24] = p.iswold(); o[25] = p.chi(); o[26] = p.lambda(); o[27] = p.dphidt(); o[28] = p.s();
+}
+
+int64_t ref_propagate_bundle(const double* L, unsigned count, double angle, double rotation, const char* interp,
+                             double amin, unsigned nsteps, double* out, int64_t cap, char* text, int64_t text_cap)
+{
+    const std::array<double, 3> v0{0, 0, 0};
+    const Photon<double, 3> ph = Integrator::launch(L[0], L[1], L[2], L[3], L[4], L[5]);
+    Traj t = Integrator::propagate(ph, count, angle, rotation, std::string(interp), g_cosmo, g_octree, v0, g_length,
+                                   nsteps, amin);
+    const int64_t m = (int64_t)t.size();
+    for (int64_t k = 0; k < m && k < cap; ++k) photon_file29(t[k], out + 29 * k);
+    if (text && text_cap > 0) {
+        std::ostringstream os;
+        Output::save(os, t, std::numeric_limits<double>::max_digits10);
+        const std::string str = os.str();
+        const size_t n = std::min<size_t>(str.size(), (size_t)text_cap - 1);
+        std::memcpy(text, str.data(), n);
+        text[n] = 0;
+    }
+    return m;
 }
 
 }  // extern "C"

@@ -68,6 +68,8 @@ def lib(order: int = 2):
         L.ref_catalogue.argtypes = [_i64, _p, _p, _p, _d, C.c_uint, _d, _d, _p, C.c_int]
         L.ref_catalogue_jac.argtypes = [_i64, _p, _p, _p, _d, C.c_uint, _d, _d, _p, C.c_int, C.c_char_p, C.c_char_p,
                                         C.c_char_p, _d]
+        L.ref_propagate_bundle.restype = _i64
+        L.ref_propagate_bundle.argtypes = [_p, C.c_uint, _d, _d, C.c_char_p, _d, C.c_uint, _p, _i64, C.c_char_p, _i64]
         _LIBS[order] = L
     return _LIBS[order]
 
@@ -151,6 +153,17 @@ class Reference:
         out = np.zeros((cap, 28))
         m = self.L.ref_trajectory(_ptr(L), stop.encode(), stop_ref, nsteps, _ptr(out), cap)
         return out[:min(m, cap)]
+
+    def propagate_bundle(self, launch, count, angle, rotation, interp="redshift", amin=0.0, nsteps=10, cap=100000,
+                         text_cap=1 << 24):
+        """Integrator::propagate: the central trajectory (m x 29, file column
+        order) and its Output::save text; (empty, "") when rejected."""
+        L = np.ascontiguousarray(launch, dtype=np.float64)
+        out = np.zeros((cap, 29))
+        buf = C.create_string_buffer(text_cap)
+        m = self.L.ref_propagate_bundle(_ptr(L), int(count), float(angle), float(rotation), interp.encode(), float(amin),
+                                        int(nsteps), _ptr(out), cap, buf, text_cap)
+        return out[:min(m, cap)], buf.value.decode()
 
     def homogeneous(self, zs):
         zs = np.ascontiguousarray(zs, dtype=np.float64)

@@ -162,6 +162,70 @@ def make(name, cfg):
         name, rec.shape[0], levels.min(), levels.max(), launch.shape[0], pix.shape[0], path, os.path.getsize(path) // 1024))
 
 
+# rays bundles (Integrator::propagate): a cone deep enough for the bundle checks
+# (the rays must travel more than a quarter of the extent), a few haloes
+RAYS_SPEC = dict(base_level=6, box_cells=16, lbox=2048.0, half_y=2.5, half_z=2.5, chi_max=2600.0, halos=3,
+                 max_level=8, mass_min=3e14, mass_max=2e15, refine_cells=1.5, seed=5)
+RAYS_NSTEPS = 4
+# (direction offsets in degrees (y, z), count, opening in degrees, rotation, interpolation, amin)
+RAYS_CASES = (
+    ((0.3, -0.2), 4, 0.5, 0.3, "redshift", 0.0),
+    ((-0.6, 0.4), 8, 0.2, 1.1, "r", 0.0),
+    ((0.1, 0.9), 3, 0.3, 0.0, "a", 0.0),
+    ((-0.2, -0.7), 4, 0.3, 2.0, "lambda", 0.0),
+    ((0.8, 0.1), 4, 0.3, 0.5, "t", 0.0),
+    ((0.0, 0.0), 4, 0.3, 0.5, "redshift", 0.2),     # rejected: the last a of the data is above amin
+    ((0.4, 0.4), 0, 0.3, 0.0, "redshift", 0.0),     # no bundle: the central ray alone, distance 0
+    ((2.0, 0.0), 4, 1.5, 0.0, "redshift", 0.0),     # a wide opening near the cone's edge
+    ((30.0, 0.0), 4, 0.5, 0.0, "redshift", 0.0),    # leaves the cone at once: rejected (a quarter of the extent)
+)
+
+
+def make_rays():
+    spec = S.OctreeSpec(**RAYS_SPEC)
+    rec = S.make_octree(spec)
+    tmp = tempfile.mkdtemp(prefix="mpf_golden_")
+    binpath = os.path.join(tmp, "cone.bin")
+    S.write_bin(binpath, rec)
+    celldir, pf, ef = S.write_param_files(tmp, spec.cosmo, spec.lbox)
+    launch = np.zeros((len(RAYS_CASES), 6))
+    for i, ((dy, dz), *_rest) in enumerate(RAYS_CASES):
+        ph, th = np.radians(dy), np.pi / 2 + np.radians(dz)
+        launch[i, 3:] = (np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th))
+    out = dict(records=rec, nsteps=RAYS_NSTEPS, launch=launch,
+               count=np.array([c[1] for c in RAYS_CASES]), angle=np.radians([c[2] for c in RAYS_CASES]),
+               rotation=np.array([c[3] for c in RAYS_CASES]), interp=np.array([c[4] for c in RAYS_CASES]),
+               amin=np.array([c[5] for c in RAYS_CASES]))
+    for order in (1, 2):
+        R = Reference(order)
+        cos = R.cosmology(celldir, pf, ef)
+        R.load(binpath)
+        if order == 1:
+            for k in ("t", "a", "dadt", "d2adt2", "length"):
+                out["cosmo_" + k] = cos[k]
+        sizes, trajs = [], []
+        for i, (_, count, ang, rot, interp, amin) in enumerate(RAYS_CASES):
+            traj, text = R.propagate_bundle(launch[i], count, np.radians(ang), rot, interp, amin, RAYS_NSTEPS)
+            sizes.append(traj.shape[0])
+            trajs.append(traj)
+            if i == 0:
+                out["ref_text_o%d" % order] = np.array(text)
+        cap = max(sizes)
+        T = np.zeros((len(trajs), cap, 29))
+        for i, t in enumerate(trajs):
+            T[i, :t.shape[0]] = t
+        out["ref_sizes_o%d" % order] = np.array(sizes, dtype=np.int64)
+        out["ref_traj_o%d" % order] = T
+    path = os.path.join(HERE, "rays.npz")
+    np.savez_compressed(path, **out)
+    print("rays: %d cells, sizes o1 %s o2 %s -> %s (%d KB)" % (rec.shape[0], out["ref_sizes_o1"].tolist(),
+                                                            out["ref_sizes_o2"].tolist(), path, os.path.getsize(path) // 1024))
+
+
 if __name__ == "__main__":
-    for name, cfg in CASES.items():
-        make(name, cfg)
+    names = sys.argv[1:] or list(CASES) + ["rays"]
+    for name in names:
+        if name == "rays":
+            make_rays()
+        else:
+            make(name, CASES[name])
