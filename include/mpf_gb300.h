@@ -260,6 +260,9 @@ typedef struct {
                                   the start); any other value is read as redshift, as the reference does */
     double amin;               /* 0, or the scale factor (of the data) every ray must reach */
     int64_t capacity;          /* trajectory points kept per ray; a longer ray is an error */
+    int homogeneous_level;     /* -1: the octree's field; >= 0: the FLRW reference of the rays driver
+                                  (Order = -1 on a uniform octree of this level, rays.cpp:246-249,
+                                  integrator.h:497-500), always with the reference float64 order */
 } mpf_bundle_params;
 
 #define MPF_TRAJECTORY_FIELDS 29

@@ -160,14 +160,16 @@ def propagate(octree: Octree, cosmology: Cosmology, launch, length: float, nstep
 
 def rays_propagate(octree: Octree, cosmology: Cosmology, photons, length: float, count: int, angle: float,
                    rotation=None, interpolation: str = "redshift", amin: float = 0.0, nsteps: int = 10, order: int = 2,
-                   exact: bool = False, capacity: int = 20000, max_steps: int = 0):
+                   exact: bool = False, capacity: int = 20000, max_steps: int = 0, homogeneous_level: int = -1):
     """Integrator::propagate for n central photons (the rays driver's bundles).
 
     photons[n, 6]: start x y z and the launch direction (not renormalised);
     rotation[n]: the circle's rotation (None: 0).  Returns (sizes[n],
     central[n, capacity, 29]): each central trajectory in the trajectory
     file's column order with its angular diameter distance; size 0 when the
-    bundle is rejected.
+    bundle is rejected.  homogeneous_level >= 0: the FLRW reference bundle
+    (the homogeneous field on a uniform octree of that level; the octree
+    argument is not read).
     """
     L = capi.load()
     ph = np.ascontiguousarray(photons, dtype=np.float64).reshape(-1, 6)
@@ -177,6 +179,7 @@ def rays_propagate(octree: Octree, cosmology: Cosmology, photons, length: float,
     bp = capi.BundleParams()
     bp.count, bp.angle, bp.amin, bp.capacity = int(count), float(angle), float(amin), int(capacity)
     bp.interpolation = capi.STOP.get(interpolation, 0)
+    bp.homogeneous_level = int(homogeneous_level)
     sizes = np.zeros(n, dtype=np.int64)
     central = np.zeros((n, int(capacity), capi.MPF_TRAJECTORY_FIELDS))
     capi.check(L.mpf_rays_propagate(octree._h, cosmology._h, C.byref(p), C.byref(bp), n, capi.ptr(ph), capi.ptr(rot),

@@ -75,7 +75,7 @@ class CatalogueStats(C.Structure):
 
 class BundleParams(C.Structure):
     _fields_ = [("count", C.c_int), ("angle", C.c_double), ("interpolation", C.c_int), ("amin", C.c_double),
-                ("capacity", C.c_int64)]
+                ("capacity", C.c_int64), ("homogeneous_level", C.c_int)]
 
 
 class SurrogateDomain(C.Structure):

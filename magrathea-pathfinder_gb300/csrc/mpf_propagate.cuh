@@ -68,6 +68,12 @@ struct PropParams {
     // bundle photons of Integrator::launch(photon, count, angle, rotation),
     // whose direction is not renormalised before integrate)
     int direct;
+    // Order = -1 of the reference (the FLRW reference ray of the rays driver,
+    // integrated on a uniform octree of level hom_level): every gather gives
+    // the homogeneous field (a = 1, the rest 0), every cell is of level
+    // hom_level; exact kernel only
+    int homogeneous;
+    int hom_level;
 };
 
 struct PropOut {
@@ -115,12 +121,31 @@ __device__ __forceinline__ void write_rec(double* o, const Rec& r)
 
 constexpr double kC = 299792458.0;
 
+// the field at a point: the octree's CIC / TSC, or the homogeneous field
+template <bool EXACT>
+__device__ __forceinline__ Field7 field_at(const DevTree& T, const PropParams& P, double x, double y, double z, bool need_all)
+{
+    if (P.homogeneous) {
+        Field7 h;
+        clear(h);
+        h.a = 1.f;
+        return h;
+    }
+    return gather<EXACT>(T, P.order, x, y, z, need_all);
+}
+
+__device__ __forceinline__ Found locate_at(const DevTree& T, const PropParams& P, double x, double y, double z)
+{
+    if (P.homogeneous) return Found{0, P.hom_level};
+    return locate(T, x, y, z);
+}
+
 template <bool EXACT>
 __device__ __forceinline__ void rhs(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* in, double* out)
 {
     const double two = 2.0;
     const double c2 = kC * kC;
-    const Field7 d = gather<EXACT>(T, P.order, in[2], in[3], in[4], false);
+    const Field7 d = field_at<EXACT>(T, P, in[2], in[3], in[4], false);
     const double dphidl = (double)d.dt * in[5] + ((double)d.dx * in[6] + (double)d.dy * in[7] + (double)d.dz * in[8]);
     const double dadt = interpolate(in[1], C.t, C.dadt, C.n);
     const double scale = P.length;
@@ -229,14 +254,14 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
         b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
         b.index = 0.0;
     }
-    Field7 data = gather<EXACT>(T, P.order, b.x, b.y, b.z, true);
+    Field7 data = field_at<EXACT>(T, P, b.x, b.y, b.z, true);
     {
         const double ph = (double)data.phi / c2;
         const double norm = sqrt((c2 * (one + two * ph) * b.k0 * b.k0) / ((one - two * ph) * (b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3)));
         b.k1 *= norm; b.k2 *= norm; b.k3 *= norm;
     }
     b.a = interpolate(b.t, C.t, C.a, C.n);
-    Found loc = locate(T, b.x, b.y, b.z);
+    Found loc = locate_at(T, P, b.x, b.y, b.z);
     b.level = (loc.cell >= 0) ? (double)loc.level : 0.0;
     b.ah = zero;
     b.rho = data.rho; b.phi = data.phi; b.dx = data.dx; b.dy = data.dy; b.dz = data.dz; b.dt = data.dt;
@@ -298,9 +323,9 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
         for (int q = 0; q < 9; ++q) core[q] = bcore[q] + (dl / six) * (dc0[q] + two * dc1[q] + two * dc2[q] + dc3[q]);
         p.a = core[0]; p.t = core[1]; p.x = core[2]; p.y = core[3]; p.z = core[4];
         p.k0 = core[5]; p.k1 = core[6]; p.k2 = core[7]; p.k3 = core[8];
-        data = gather<EXACT>(T, P.order, p.x, p.y, p.z, true);
+        data = field_at<EXACT>(T, P, p.x, p.y, p.z, true);
         if (!(!(p.a < zero) && ((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx)))) clear(data);
-        loc = locate(T, p.x, p.y, p.z);
+        loc = locate_at(T, P, p.x, p.y, p.z);
         p.level = (loc.cell >= 0) ? (double)loc.level : 0.0;
         p.ah = data.a;
         p.rho = data.rho; p.phi = data.phi; p.dx = data.dx; p.dy = data.dy; p.dz = data.dz;

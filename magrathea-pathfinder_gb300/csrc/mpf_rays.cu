@@ -211,7 +211,7 @@ extern "C" int mpf_rays_propagate(const mpf_octree* o, const mpf_cosmology* c, c
     if (!o || !c || !p || !bp || n < 0 || (n > 0 && (!photons || !sizes || !central)))
         return fail(MPF_BAD_INPUT, "mpf_rays_propagate: bad argument");
     if (bp->count < 0 || !(bp->angle > 0.0) || bp->capacity < 1 || p->nsteps == 0 || (p->order != 1 && p->order != 2) ||
-        !(p->length > 0.0) || bp->interpolation < 0 || bp->interpolation > 6)
+        !(p->length > 0.0) || bp->interpolation < 0 || bp->interpolation > 6 || bp->homogeneous_level > 30)
         return fail(MPF_BAD_INPUT, "mpf_rays_propagate: bad parameters");
     if (n == 0) return MPF_OK;
     const int nt = bp->count + 1;
@@ -227,6 +227,9 @@ extern "C" int mpf_rays_propagate(const mpf_octree* o, const mpf_cosmology* c, c
     P.order = p->order;
     P.stop_kind = STOP_R;
     P.direct = 1;
+    const bool hom = bp->homogeneous_level >= 0;
+    P.homogeneous = hom ? 1 : 0;
+    P.hom_level = hom ? bp->homogeneous_level : 0;
     const DevCosmo C{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
     Dev dl, dsteps, dtraj, dout, dsizes, dstatus;
     cudaError_t e = dl.alloc((size_t)chunk * nt * 6 * sizeof(double));
@@ -253,7 +256,7 @@ extern "C" int mpf_rays_propagate(const mpf_octree* o, const mpf_cosmology* c, c
         if (e == cudaSuccess) e = cudaMemset(dstatus.p, 0, sizeof(unsigned));
         if (e != cudaSuccess) return cuda_fail(e, "mpf_rays_propagate");
         PropOut O{(long long*)dsteps.p, nullptr, nullptr, (unsigned*)dstatus.p, nullptr, (double*)dtraj.p, cap};
-        e = p->exact ? launch_propagate<true>(o->tree, C, P, (const double*)dl.p, m * nt, O, 0)
+        e = (p->exact || hom) ? launch_propagate<true>(o->tree, C, P, (const double*)dl.p, m * nt, O, 0)
                      : launch_propagate<false>(o->tree, C, P, (const double*)dl.p, m * nt, O, 0);
         unsigned hs = 0;
         if (e == cudaSuccess) e = cudaMemcpy(&hs, dstatus.p, sizeof(unsigned), cudaMemcpyDeviceToHost);

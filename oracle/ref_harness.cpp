@@ -509,4 +509,21 @@ int64_t ref_propagate_bundle(const double* L, unsigned count, double angle, doub
     return m;
 }
 
+// The FLRW reference bundle of the rays driver (rays.cpp:244-249): the same
+// Integrator::propagate at Order = -1 on a uniform octree of `level`
+// (homotree.assign(level, 0)).  Output as ref_propagate_bundle.
+int64_t ref_propagate_bundle_flrw(const double* L, unsigned count, double angle, const char* interp, unsigned nsteps,
+                                  unsigned level, double* out, int64_t cap)
+{
+    const std::array<double, 3> v0{0, 0, 0};
+    Oct homotree;
+    homotree.assign(level, 0);
+    const Photon<double, 3> ph = Integrator::launch(L[0], L[1], L[2], L[3], L[4], L[5]);
+    Traj t = Integrator::propagate<-1>(ph, count, angle, 0.0, std::string(interp), g_cosmo, homotree, v0, g_length,
+                                       nsteps, 0.0);
+    const int64_t m = (int64_t)t.size();
+    for (int64_t k = 0; k < m && k < cap; ++k) photon_file29(t[k], out + 29 * k);
+    return m;
+}
+
 }  // extern "C"

@@ -70,6 +70,8 @@ def lib(order: int = 2):
                                         C.c_char_p, _d]
         L.ref_propagate_bundle.restype = _i64
         L.ref_propagate_bundle.argtypes = [_p, C.c_uint, _d, _d, C.c_char_p, _d, C.c_uint, _p, _i64, C.c_char_p, _i64]
+        L.ref_propagate_bundle_flrw.restype = _i64
+        L.ref_propagate_bundle_flrw.argtypes = [_p, C.c_uint, _d, C.c_char_p, C.c_uint, C.c_uint, _p, _i64]
         _LIBS[order] = L
     return _LIBS[order]
 
@@ -164,6 +166,14 @@ class Reference:
         m = self.L.ref_propagate_bundle(_ptr(L), int(count), float(angle), float(rotation), interp.encode(), float(amin),
                                         int(nsteps), _ptr(out), cap, buf, text_cap)
         return out[:min(m, cap)], buf.value.decode()
+
+    def propagate_bundle_flrw(self, launch, count, angle, interp="redshift", nsteps=10, level=4, cap=200000):
+        """The rays driver's FLRW reference bundle (Order = -1 on a uniform level-`level` octree)."""
+        L = np.ascontiguousarray(launch, dtype=np.float64)
+        out = np.zeros((cap, 29))
+        m = self.L.ref_propagate_bundle_flrw(_ptr(L), int(count), float(angle), interp.encode(), int(nsteps), int(level),
+                                             _ptr(out), cap)
+        return out[:min(m, cap)]
 
     def homogeneous(self, zs):
         zs = np.ascontiguousarray(zs, dtype=np.float64)

@@ -181,6 +181,14 @@ RAYS_CASES = (
 )
 
 
+# the rays driver's FLRW reference bundle (rays.cpp:244-249): Order = -1 on a
+# uniform octree of level ncoarse / 2, nsteps = EXTENT nsteps 2^(ncoarse - ncoarse/2) 2,
+# launched from the centre toward +x; (count, opening in degrees, interpolation)
+FLRW_NCOARSE = 6
+FLRW_CASES = ((4, 0.3, "redshift"), (6, 0.2, "r"))
+FLRW_EVERY = 8     # points kept in the fixture: every 8th, and the last
+
+
 def make_rays():
     spec = S.OctreeSpec(**RAYS_SPEC)
     rec = S.make_octree(spec)
@@ -203,6 +211,19 @@ def make_rays():
         if order == 1:
             for k in ("t", "a", "dadt", "d2adt2", "length"):
                 out["cosmo_" + k] = cos[k]
+            level = FLRW_NCOARSE // 2
+            nst = 4 * RAYS_NSTEPS * (1 << (FLRW_NCOARSE - level)) * 2
+            out["flrw_level"], out["flrw_nsteps"] = level, nst
+            out["flrw_count"] = np.array([c[0] for c in FLRW_CASES])
+            out["flrw_angle"] = np.radians([c[1] for c in FLRW_CASES])
+            out["flrw_interp"] = np.array([c[2] for c in FLRW_CASES])
+            out["flrw_every"] = FLRW_EVERY
+            for j, (count, ang, interp) in enumerate(FLRW_CASES):
+                t = R.propagate_bundle_flrw(np.array([0.0, 0.0, 0.0, 2.0, 0.0, 0.0]), count, np.radians(ang), interp, nst,
+                                            level)
+                out["flrw_size_%d" % j] = t.shape[0]
+                out["flrw_traj_%d" % j] = t[::FLRW_EVERY]
+                out["flrw_last_%d" % j] = t[-1]
         sizes, trajs = [], []
         for i, (_, count, ang, rot, interp, amin) in enumerate(RAYS_CASES):
             traj, text = R.propagate_bundle(launch[i], count, np.radians(ang), rot, interp, amin, RAYS_NSTEPS)

@@ -83,3 +83,19 @@ def test_capacity_too_small_is_an_error(rays_dev, pkg):
     g, tree, cos = rays_dev
     with pytest.raises(pkg.MpfError):
         _run(pkg, g, tree, cos, 0, 2, True, cap=10)
+
+
+def test_flrw_reference_bundle_bit_exact(rays_dev, pkg):
+    """The rays driver's FLRW reference bundle (Order = -1 on a uniform octree)
+    against the reference's own, every 8th point and the last."""
+    g, tree, cos = rays_dev
+    level, nst, every = int(g["flrw_level"]), int(g["flrw_nsteps"]), int(g["flrw_every"])
+    ph = np.array([[0.0, 0.0, 0.0, 1.0, 0.0, 0.0]])     # Integrator::launch(0, 0, 0, 2, 0, 0)
+    for j in range(g["flrw_count"].shape[0]):
+        size = int(g["flrw_size_%d" % j])
+        sizes, traj = pkg.rays_propagate(tree, cos, ph, float(g["cosmo_length"]), int(g["flrw_count"][j]),
+                                         float(g["flrw_angle"][j]), interpolation=str(g["flrw_interp"][j]), nsteps=nst,
+                                         order=1, exact=True, capacity=size + 8, homogeneous_level=level)
+        assert sizes[0] == size
+        np.testing.assert_array_equal(traj[0, :size:every].view(np.uint64), g["flrw_traj_%d" % j].view(np.uint64))
+        np.testing.assert_array_equal(traj[0, size - 1].view(np.uint64), g["flrw_last_%d" % j].view(np.uint64))
