@@ -227,7 +227,7 @@ def gaussian_field(n: int, seed: int, kc_over_2pi: float = 16.0) -> np.ndarray:
     amp = np.sqrt(kk ** -3.0 * np.exp(-(kk / kc) ** 2))
     amp[0, 0, 0] = 0.0
     noise = np.fft.rfftn(rng.standard_normal((n, n, n)))
-    f = np.fft.irfftn(noise * amp, s=(n, n, n))
+    f = np.fft.irfftn(noise * amp, s=(n, n, n), axes=(0, 1, 2))
     return f / f.std()
 
 
