@@ -250,6 +250,35 @@ int mpf_hmaps_fill_bundle(const mpf_octree* o, const mpf_cosmology* c, const mpf
 int mpf_pix2vec_ring(int64_t nside, int64_t n, const int64_t* pixels, double* vec);
 
 /* ------------------------------------------------------------------------ */
+/* Cone octree construction from simulation cells (create_octree, ASCII)     */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    double cone_vertex[3], cone_base[3], cone_angle;   /* the cone the cells are kept in (Input::collide) */
+    double sphere_center[3], sphere_radius;            /* the microsphere around the observer */
+    const double* rotm1;       /* 3x3 row-major rotation of a narrow cone's cells, or NULL (full sky) */
+    double h, omegam, lboxmpch, mpc;
+    int coarseonly;            /* keep only the cells of file level ncoarse */
+    int ncoarse;
+    int correction;            /* must be 1: refined values from the parents, incomplete octs completed */
+    int coarsecorrection;      /* coarse non-normal densities from their neighbours */
+    int acorrection;           /* must be 0 (not supported) */
+    int order;                 /* gather of the completed children: 1 CIC, 2 TSC (the reference's ORDER) */
+} mpf_cells_params;
+
+/* Create_octree::PreparationASCII's per-cone body (src/create_octree.h:544-580):
+ * Input::importascii (src/input.h:996-1067) of the cell rows with the cone /
+ * sphere filter, Miscellaneous::correctOctree (src/miscellaneous.h:467-479:
+ * Input::sistemize, SimpleHyperOctree::update, Input::correct, dphidt * da/dt)
+ * on the device.  rows: n x 10 floats (level, x, y, z, rho, phi, force x y z,
+ * a) as the reference reads them; records: capacity x 48-byte cone records,
+ * sorted by key (what Input::save writes); count: the cells produced. */
+int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_params* cp, const mpf_cosmology* c, void* records,
+                    int64_t capacity, int64_t* count);
+/* The reference's ASCII cell reads (stream >> unsigned >> 9 floats): text of
+ * length bytes -> rows[count x 10] (capacity rows at most). */
+int mpf_cells_parse(const char* text, int64_t length, float* rows, int64_t capacity, int64_t* count);
+
+/* ------------------------------------------------------------------------ */
 /* Ray bundles (the rays driver)                                             */
 /* ------------------------------------------------------------------------ */
 typedef struct {

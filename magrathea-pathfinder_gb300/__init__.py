@@ -17,6 +17,8 @@ Integrator::integrate       ``propagate(...)`` (batched over rays), with
 Catalogues::relCat /        ``catalogue(...)``: the Newton root-finder for a
   iterateNewtonMethod       batch of sources, relCat's 16-column rows
 Hmaps::FillMap              ``hmaps_fill(...)``: pixels in, float map rows out
+create_octree (ASCII)       ``cells_parse`` + ``cells_build``: cell rows in,
+ importascii+correctOctree   sorted 48-byte cone records out
 Integrator::propagate       ``rays_propagate(...)``: the rays driver's bundles
  (rays)                      and the central ray's angular diameter distance
 pix2vec_ring                ``pix2vec_ring(nside, pixels)`` (device)
@@ -186,6 +188,41 @@ def rays_propagate(octree: Octree, cosmology: Cosmology, photons, length: float,
                                     capi.ptr(sizes), capi.ptr(central)))
     del keep
     return sizes, central
+
+
+def cells_parse(text) -> np.ndarray:
+    """ASCII cell rows (level x y z rho phi fx fy fz a) read as the reference
+    reads them (an unsigned level, then floats): float32 array n x 10."""
+    L = capi.load()
+    raw = text.encode() if isinstance(text, str) else bytes(text)
+    n = C.c_int64()
+    L.mpf_cells_parse(raw, len(raw), None, 0, C.byref(n))
+    rows = np.zeros((n.value, 10), dtype=np.float32)
+    capi.check(L.mpf_cells_parse(raw, len(raw), capi.ptr(rows), n.value, C.byref(n)))
+    return rows
+
+
+def cells_build(rows, cosmology: Cosmology, cone_vertex, cone_base, cone_angle, sphere_center, sphere_radius,
+                h: float, omegam: float, lboxmpch: float, mpc: float = 3.08568e22, rotm1=None, coarseonly: bool = False,
+                ncoarse: int = 0, coarsecorrection: bool = True, order: int = 2) -> np.ndarray:
+    """create_octree's per-cone build (importascii + correctOctree) on the
+    device: the 48-byte cone records, sorted by key, as a uint8 array."""
+    L = capi.load()
+    rows = np.ascontiguousarray(rows, dtype=np.float32).reshape(-1, 10)
+    p = capi.CellsParams()
+    for d in range(3):
+        p.cone_vertex[d], p.cone_base[d], p.sphere_center[d] = cone_vertex[d], cone_base[d], sphere_center[d]
+    p.cone_angle, p.sphere_radius = float(cone_angle), float(sphere_radius)
+    rot = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64).reshape(9)
+    p.rotm1 = rot.ctypes.data if rot is not None else None
+    p.h, p.omegam, p.lboxmpch, p.mpc = float(h), float(omegam), float(lboxmpch), float(mpc)
+    p.coarseonly, p.ncoarse, p.correction, p.coarsecorrection = int(bool(coarseonly)), int(ncoarse), 1, int(bool(coarsecorrection))
+    p.acorrection, p.order = 0, int(order)
+    cap = 2 * rows.shape[0] + 64
+    out = np.zeros(cap * 48, dtype=np.uint8)
+    n = C.c_int64()
+    capi.check(L.mpf_cells_build(capi.ptr(rows), rows.shape[0], C.byref(p), cosmology._h, capi.ptr(out), cap, C.byref(n)))
+    return out[:48 * n.value].copy()
 
 
 def catalogue(octree: Octree, cosmology: Cosmology, sources, length: float, h: float, mpc: float = 3.08568e22,

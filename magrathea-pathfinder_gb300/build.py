@@ -31,6 +31,7 @@ UNITS = [
     ("mpf_maps.cu", ["-fmad=false"]),
     ("mpf_surrogate.cu", []),
     ("mpf_rays.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
+    ("mpf_build.cu", ["-fmad=false"]),
 ]
 
 

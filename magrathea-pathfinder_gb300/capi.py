@@ -30,7 +30,7 @@ EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_uplo
            "mpf_catalogue_newton_device", "mpf_hmaps_fill", "mpf_hmaps_fill_bundle", "mpf_pix2vec_ring",
            "mpf_surrogate_create", "mpf_surrogate_destroy", "mpf_surrogate_train", "mpf_surrogate_sample",
            "mpf_surrogate_get_params", "mpf_surrogate_set_params", "mpf_surrogate_loss_grad", "mpf_surrogate_eval",
-           "mpf_surrogate_propagate", "mpf_rays_propagate")
+           "mpf_surrogate_propagate", "mpf_rays_propagate", "mpf_cells_build", "mpf_cells_parse")
 
 MPF_TRAJECTORY_FIELDS = 29
 
@@ -71,6 +71,14 @@ class CatalogueParams(C.Structure):
 class CatalogueStats(C.Structure):
     _fields_ = [("rays", C.c_int64), ("photon_steps", C.c_int64), ("photon_steps_jacobian", C.c_int64),
                 ("iterations", C.c_int), ("kernel_launches", C.c_int)]
+
+
+class CellsParams(C.Structure):
+    _fields_ = [("cone_vertex", C.c_double * 3), ("cone_base", C.c_double * 3), ("cone_angle", C.c_double),
+                ("sphere_center", C.c_double * 3), ("sphere_radius", C.c_double), ("rotm1", C.c_void_p),
+                ("h", C.c_double), ("omegam", C.c_double), ("lboxmpch", C.c_double), ("mpc", C.c_double),
+                ("coarseonly", C.c_int), ("ncoarse", C.c_int), ("correction", C.c_int), ("coarsecorrection", C.c_int),
+                ("acorrection", C.c_int), ("order", C.c_int)]
 
 
 class BundleParams(C.Structure):
@@ -139,6 +147,8 @@ def load(path: str = LIB_PATH):
     L.mpf_hmaps_fill_bundle.argtypes = [vp, vp, C.POINTER(Params), i64, i64, vp, C.c_int, vp, vp, C.c_int, C.c_int, d,
                                         vp]
     L.mpf_pix2vec_ring.argtypes = [i64, i64, vp, vp]
+    L.mpf_cells_build.argtypes = [vp, i64, C.POINTER(CellsParams), vp, vp, i64, C.POINTER(i64)]
+    L.mpf_cells_parse.argtypes = [C.c_char_p, i64, vp, i64, C.POINTER(i64)]
     L.mpf_rays_propagate.argtypes = [vp, vp, C.POINTER(Params), C.POINTER(BundleParams), i64, vp, vp, vp, vp]
     L.mpf_surrogate_create.argtypes = [C.POINTER(SurrogateDomain), C.POINTER(vp)]
     L.mpf_surrogate_destroy.argtypes = [vp]

@@ -1,0 +1,580 @@
+// Cone octree construction from simulation cells, the ASCII path of
+// create_octree (Create_octree::PreparationASCII, create_octree.h:544-580),
+// on the device:
+//
+//   Input::importascii (input.h:996-1067)   k_prepare: file level + log2 EXTENT,
+//       narrow-cone rotation, the cell key (Index::compute in float, as the
+//       reference instantiates it), the cone / sphere filter
+//       (Input::collide, input.h:216-226; Utility::collide, utility.h:392-421);
+//       order-keeping compaction of the selected cells
+//   Input::sistemize (input.h:368-379)      k_sistemize: RAMSES -> SI
+//   SimpleHyperOctree::update               radix sort of the 128-bit keys,
+//       (simplehyperoctree.h:1270-1310)     k_collapse: cells with one key keep
+//                                           the smallest a; dphidt = dphi/da
+//   Input::correct (input.h:1381-1516)      coarse densities from their
+//       neighbours, refined dphidt / rho from the parent level by level,
+//       incomplete octs completed from the gather at the children's centres
+//   correctOctree (miscellaneous.h:467-479) dphidt *= da/dt(a)
+//
+// Float32 data arithmetic follows the reference's types (Gravity<float, 3>,
+// Real = float in importascii); the unit is compiled with -fmad=false.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mpf_gb300.h"
+#include "mpf_internal.h"
+
+extern "C" int mpf_internal_octree_build(const void* records, int64_t n, int on_device, cudaStream_t stream,
+                                         mpf_octree** out, char* err, int errlen);
+
+namespace mpf {
+namespace build {
+
+// one cell: the 48-byte cone record (key, Gravity<float, 3>, pad)
+struct Rec48 {
+    unsigned long long lo, hi;
+    float dt, a, dx, dy, dz, phi, rho;
+    int pad;
+};
+static_assert(sizeof(Rec48) == 48, "cone record");
+
+struct Geometry {
+    double vertex[3], base[3], angle;
+    double sc[3], sr;
+    double rot[9];
+    int rotate;
+    double h, lbox, mpc;
+};
+
+__device__ __forceinline__ Key rkey(const Rec48& r) { return Key{r.hi, r.lo}; }
+
+__device__ __forceinline__ bool normal_f(float x)
+{
+    const float a = fabsf(x);
+    return a >= 1.17549435e-38f && a <= 3.40282347e38f;
+}
+
+// Index::compute<float, ratio<0>, ratio<EXTENT>> along one axis
+__device__ __forceinline__ uint64_t axis_coord_f(int level, float x)
+{
+    const float scale = (1.0f / 4.0f) * (float)(1ull << level);
+    const float v = scale * (x - (-2.0f));
+    uint64_t c = (v > 0.0f) ? (uint64_t)v : 0ull;
+    return (level >= 64) ? c : (c & ((1ull << level) - 1ull));
+}
+
+__device__ __forceinline__ bool collide(const Geometry& G, int L, const double* pos)
+{
+    // the cell as a sphere of radius extent sqrt(3) / 2
+    const double r = cell_extent(L) * sqrt(3.0) / 2.0;
+    {
+        const double d0 = pos[0] - G.sc[0], d1 = pos[1] - G.sc[1], d2 = pos[2] - G.sc[2];
+        if (sqrt(d0 * d0 + (d1 * d1 + (d2 * d2 + 0.0))) < (r + G.sr)) return true;
+    }
+    double norm = 0.0;
+    for (int d = 0; d < 3; ++d) norm += (G.base[d] - G.vertex[d]) * (G.base[d] - G.vertex[d]);
+    norm = sqrt(norm);
+    double length = 0.0;
+    for (int d = 0; d < 3; ++d) length += (G.base[d] - G.vertex[d]) * (pos[d] - G.vertex[d]);
+    length /= norm;
+    double distance = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        const double e = pos[d] - (G.vertex[d] + (G.base[d] - G.vertex[d]) * (length / norm));
+        distance += e * e;
+    }
+    const double R = G.sr;
+    const double q = length - R * cos(G.angle);
+    return (sqrt(distance) < 5 * r + length * tan(G.angle) + 0.4 * R * exp(-0.7 * q * q / (R * R))) && !(length < 0.0) &&
+           (length < norm + r * 2.0);
+}
+
+// rows: level x y z rho phi fx fy fz a (floats, as the reference reads them)
+__global__ void k_prepare(const float* __restrict__ rows, long long n, Geometry G, int* flag, Rec48* out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* w = rows + 10 * i;
+    const int L = (int)(unsigned)w[0] + kLevelShift;
+    float c[3] = {w[1], w[2], w[3]}, f[3] = {w[6], w[7], w[8]};
+    if (G.rotate) {
+        const float ct[3] = {c[0], c[1], c[2]}, ft[3] = {f[0], f[1], f[2]};
+        for (int r = 0; r < 3; ++r) {
+            c[r] = (float)((double)ct[0] * G.rot[3 * r] + (double)ct[1] * G.rot[3 * r + 1] + (double)ct[2] * G.rot[3 * r + 2]);
+            f[r] = (float)((double)ft[0] * G.rot[3 * r] + (double)ft[1] * G.rot[3 * r + 1] + (double)ft[2] * G.rot[3 * r + 2]);
+        }
+    }
+    const uint64_t ix = axis_coord_f(L, c[0]), iy = axis_coord_f(L, c[1]), iz = axis_coord_f(L, c[2]);
+    const Key k = key_from_coords(L, ix, iy, iz);
+    const double pos[3] = {coord_center(L, ix), coord_center(L, iy), coord_center(L, iz)};
+    flag[i] = collide(G, L, pos) ? 1 : 0;
+    Rec48 r;
+    r.lo = k.lo; r.hi = k.hi;
+    r.dt = 0.f; r.a = w[9]; r.dx = f[0]; r.dy = f[1]; r.dz = f[2]; r.phi = w[5]; r.rho = w[4];
+    r.pad = L;
+    out[i] = r;
+}
+
+// order-keeping compaction: scan = exclusive prefix sum of flag over n + 1 entries
+__global__ void k_select(long long n, const Rec48* __restrict__ in, const int* __restrict__ scan, Rec48* out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (scan[i + 1] > scan[i]) out[scan[i]] = in[i];
+}
+
+__global__ void k_level_flag(long long n, const Rec48* __restrict__ in, int level, int* flag)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flag[i] = (in[i].pad == level) ? 1 : 0;
+}
+
+// Input::sistemize, then dphidt = 0
+__global__ void k_sistemize(long long n, Rec48* r, Geometry G)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double a = (double)r[i].a;
+    const double t = (a * a * G.mpc) / (G.h * 100 * 1000);
+    const double l = (a * G.lbox * G.mpc) / G.h;
+    r[i].phi = (float)((double)r[i].phi * ((l * l) / (t * t)));
+    const double g = (l / (t * t)) * (-a);
+    r[i].dx = (float)((double)r[i].dx * g);
+    r[i].dy = (float)((double)r[i].dy * g);
+    r[i].dz = (float)((double)r[i].dz * g);
+    r[i].dt = 0.f;
+}
+
+// ---- stable LSD radix sort of (hi, lo) with the record index as payload ----
+constexpr int kTile = 256;
+__global__ void k_keys(long long n, const Rec48* __restrict__ r, unsigned long long* hi, unsigned long long* lo, int* idx)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    hi[i] = r[i].hi;
+    lo[i] = r[i].lo;
+    idx[i] = (int)i;
+}
+__device__ __forceinline__ unsigned digit(const unsigned long long* hi, const unsigned long long* lo, long long i, int pass)
+{
+    // passes 0-15 take lo's nibbles from the lowest, 16-31 hi's
+    const unsigned long long w = (pass < 16) ? lo[i] : hi[i];
+    return (unsigned)((w >> (4 * (pass & 15))) & 15ull);
+}
+__global__ void k_hist(long long n, const unsigned long long* __restrict__ hi, const unsigned long long* __restrict__ lo,
+                       int pass, int* hist, long long ntiles)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    int h[16];
+    for (int d = 0; d < 16; ++d) h[d] = 0;
+    const long long e = min(n, (t + 1) * kTile);
+    for (long long i = t * kTile; i < e; ++i) ++h[digit(hi, lo, i, pass)];
+    for (int d = 0; d < 16; ++d) hist[d * ntiles + t] = h[d];
+}
+__global__ void k_scatter(long long n, const unsigned long long* __restrict__ hi, const unsigned long long* __restrict__ lo,
+                          const int* __restrict__ idx, int pass, const int* __restrict__ off, long long ntiles,
+                          unsigned long long* hi2, unsigned long long* lo2, int* idx2)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    int o[16];
+    for (int d = 0; d < 16; ++d) o[d] = off[d * ntiles + t];
+    const long long e = min(n, (t + 1) * kTile);
+    for (long long i = t * kTile; i < e; ++i) {
+        const int j = o[digit(hi, lo, i, pass)]++;
+        hi2[j] = hi[i];
+        lo2[j] = lo[i];
+        idx2[j] = idx[i];
+    }
+}
+__global__ void k_gather(long long n, const Rec48* __restrict__ in, const int* __restrict__ idx, Rec48* out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[idx[i]];
+}
+
+// SimpleHyperOctree::update's collapse: a run of cells with one key keeps the
+// data of its smallest a (the first of them in sorted order) and, when the
+// run's a values differ by more than 1e-6, dphidt = (phi - phi') / (a - a')
+// between the smallest and the largest a.  flag: 1 on the first of each key.
+__global__ void k_collapse(long long n, Rec48* r, int* flag)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Key k = rkey(r[i]);
+    const bool head = (i == 0) || !key_eq(rkey(r[i - 1]), k);
+    flag[i] = head ? 1 : 0;
+    if (!head) return;
+    long long e = i + 1;
+    while (e < n && key_eq(rkey(r[e]), k)) ++e;
+    if (e == i + 1) return;
+    long long lo_i = i, hi_i = i;
+    for (long long j = i + 1; j < e; ++j) {
+        if (r[j].a < r[lo_i].a) lo_i = j;
+        if (!(r[j].a < r[hi_i].a)) hi_i = j;
+    }
+    Rec48 keep = r[lo_i];
+    const float fa = r[lo_i].a, ba = r[hi_i].a;
+    if (fabs((double)(fa - ba)) > 1e-6) keep.dt = (r[lo_i].phi - r[hi_i].phi) / (fa - ba);
+    keep.pad = r[i].pad;
+    r[i] = keep;
+}
+
+// exact-key search in the sorted records
+__device__ __forceinline__ long long find_key(const Rec48* r, long long n, Key k)
+{
+    long long lo = 0, hi = n;
+    while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (key_less(rkey(r[mid]), k)) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < n && key_eq(rkey(r[lo]), k)) ? lo : -1;
+}
+
+__device__ __forceinline__ void key_coords(Key k, int L, uint64_t* c)
+{
+    c[0] = c[1] = c[2] = 0;
+    for (int i = 1; i <= L; ++i) {
+        const uint64_t nib = (i <= 16) ? (k.hi >> (64 - 4 * i)) & 15ull : (k.lo >> (128 - 4 * i)) & 15ull;
+        c[0] = (c[0] << 1) | (nib & 1ull);
+        c[1] = (c[1] << 1) | ((nib >> 1) & 1ull);
+        c[2] = (c[2] << 1) | ((nib >> 2) & 1ull);
+    }
+}
+
+// Input::mean over the 26 same-level neighbours with a normal density
+// (input.h:244-276), for coarse cells with a non-normal density; rho0 is the
+// density before any correction
+__global__ void k_coarse_rho(long long n, Rec48* r, const float* __restrict__ rho0, int ncoarse)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (r[i].pad != ncoarse || normal_f(rho0[i])) return;
+    const int L = ncoarse;
+    uint64_t c[3];
+    key_coords(rkey(r[i]), L, c);
+    const uint64_t mask = (L >= 64) ? ~0ull : ((1ull << L) - 1ull);
+    float result = 0.f;
+    unsigned count = 0;
+    for (int ix = -1; ix <= 1; ++ix)
+        for (int iy = -1; iy <= 1; ++iy)
+            for (int iz = -1; iz <= 1; ++iz) {
+                if (ix == 0 && iy == 0 && iz == 0) continue;
+                const Key nk = key_from_coords(L, (c[0] + (uint64_t)(int64_t)ix) & mask, (c[1] + (uint64_t)(int64_t)iy) & mask,
+                                               (c[2] + (uint64_t)(int64_t)iz) & mask);
+                const long long j = find_key(r, n, nk);
+                if (j >= 0 && normal_f(rho0[j])) {
+                    result += rho0[j];
+                    ++count;
+                }
+            }
+    r[i].rho = result / (float)(count + (count == 0));
+}
+
+__global__ void k_copy_rho(long long n, const Rec48* __restrict__ r, float* rho0)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) rho0[i] = r[i].rho;
+}
+
+// refined cells of level L whose dphidt (which = 0) or rho (which = 1) is not
+// normal take their parent's
+__global__ void k_from_parent(long long n, Rec48* r, int L, int which)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (r[i].pad != L) return;
+    const float v = which ? r[i].rho : r[i].dt;
+    if (normal_f(v)) return;
+    uint64_t c[3];
+    key_coords(rkey(r[i]), L, c);
+    const long long p = find_key(r, n, key_from_coords(L - 1, c[0] >> 1, c[1] >> 1, c[2] >> 1));
+    if (p < 0) return;   // the reference dereferences end() there; the cell keeps its value
+    if (which) r[i].rho = r[p].rho;
+    else r[i].dt = r[p].dt;
+}
+
+// non-leaf cells (the next cell is a descendant) with some of their 8
+// children missing: flag = 1
+__global__ void k_incomplete(long long n, const Rec48* __restrict__ r, int* flag)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flag[i] = 0;
+    if (i + 1 >= n) return;
+    const int L = r[i].pad;
+    const Key k = rkey(r[i]), nk = rkey(r[i + 1]);
+    // containing: nk's first L levels equal k's and nk is deeper
+    const int Ln = r[i + 1].pad;
+    if (Ln <= L) return;
+    uint64_t c[3], cn[3];
+    key_coords(k, L, c);
+    key_coords(nk, Ln, cn);
+    const int s = Ln - L;
+    if ((cn[0] >> s) != c[0] || (cn[1] >> s) != c[1] || (cn[2] >> s) != c[2]) return;
+    int missing = 0;
+    for (int site = 0; site < 8; ++site) {
+        const Key ck = key_from_coords(L + 1, 2 * c[0] + (site & 1), 2 * c[1] + ((site >> 1) & 1), 2 * c[2] + ((site >> 2) & 1));
+        missing += (find_key(r, n, ck) < 0);
+    }
+    flag[i] = missing > 0;
+}
+
+// the 8 children of each incomplete cell, data from the gather at the child's
+// centre, or the parent's when the gather is empty (input.h:1460-1480)
+__global__ void k_children(long long m, const Rec48* __restrict__ r, const int* __restrict__ list, DevTree T, int order,
+                           Rec48* out)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= m * 8) return;
+    const Rec48& p = r[list[q >> 3]];
+    const int site = (int)(q & 7), L = p.pad;
+    uint64_t c[3];
+    key_coords(rkey(p), L, c);
+    const uint64_t cx = 2 * c[0] + (site & 1), cy = 2 * c[1] + ((site >> 1) & 1), cz = 2 * c[2] + ((site >> 2) & 1);
+    const Key ck = key_from_coords(L + 1, cx, cy, cz);
+    const Field7 f = gather<true>(T, order, coord_center(L + 1, cx), coord_center(L + 1, cy), coord_center(L + 1, cz), true);
+    Rec48 o = p;
+    o.lo = ck.lo; o.hi = ck.hi;
+    o.pad = L + 1;
+    if (!is_empty(f)) {
+        o.rho = f.rho; o.phi = f.phi; o.dx = f.dx; o.dy = f.dy; o.dz = f.dz; o.a = f.a; o.dt = f.dt;
+    }
+    out[q] = o;
+}
+
+// Utility::interpolate2 (utility.h:461-468): descending table, float result
+__device__ __forceinline__ float interpolate2(float x0, const double* x, const double* y, long long n)
+{
+    long long first = 0, count = n;
+    while (count > 0) {
+        const long long step = count >> 1, it = first + step;
+        if (!((double)x0 > x[it])) { first = it + 1; count -= step + 1; }
+        else count = step;
+    }
+    long long i = first;
+    i += (n > 1) * ((i <= 0) - (i >= n));
+    if (n > 1) return (float)(y[i - 1] + ((y[i] - y[i - 1]) * ((double)x0 - x[i - 1]) / (x[i] - x[i - 1])));
+    return (n > 0) ? (float)y[0] : 0.f;
+}
+
+__global__ void k_dphidt(long long n, Rec48* r, const double* __restrict__ ca, const double* __restrict__ cdadt, long long nc)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    r[i].dt *= interpolate2(r[i].a, ca, cdadt, nc);
+    r[i].pad = 0;
+}
+
+inline unsigned blk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace build
+}  // namespace mpf
+
+using namespace mpf;
+using namespace mpf::build;
+
+namespace {
+int fail(int code, const std::string& m) { return mpf_internal_set_error(code, m.c_str()); }
+
+struct Arena {
+    std::vector<void*> ptrs;
+    cudaError_t err = cudaSuccess;
+    template <class T>
+    T* get(size_t count)
+    {
+        void* p = nullptr;
+        if (err == cudaSuccess && count) err = cudaMalloc(&p, count * sizeof(T));
+        if (p) ptrs.push_back(p);
+        return (T*)p;
+    }
+    ~Arena()
+    {
+        for (void* p : ptrs) cudaFree(p);
+    }
+};
+
+// compact `in` (n records) by flag into out; returns the count
+long long compact(Arena& A, const Rec48* in, long long n, int* flag, Rec48* out, cudaStream_t s)
+{
+    cudaMemsetAsync(flag + n, 0, sizeof(int), s);
+    const long long total = exclusive_scan(flag, n + 1, s);
+    k_select<<<blk(n, 256), 256, 0, s>>>(n, in, flag, out);
+    return total;
+}
+
+// sort n records by key (stable) into out
+void sort_records(Arena& A, const Rec48* in, long long n, Rec48* out, cudaStream_t s)
+{
+    unsigned long long *hi = A.get<unsigned long long>(n), *lo = A.get<unsigned long long>(n);
+    unsigned long long *hi2 = A.get<unsigned long long>(n), *lo2 = A.get<unsigned long long>(n);
+    int *idx = A.get<int>(n), *idx2 = A.get<int>(n);
+    const long long ntiles = (n + kTile - 1) / kTile;
+    int* hist = A.get<int>((size_t)16 * ntiles + 1);
+    if (A.err != cudaSuccess) return;
+    k_keys<<<blk(n, 256), 256, 0, s>>>(n, in, hi, lo, idx);
+    for (int pass = 0; pass < 32; ++pass) {
+        k_hist<<<blk(ntiles, 128), 128, 0, s>>>(n, hi, lo, pass, hist, ntiles);
+        exclusive_scan(hist, 16 * ntiles, s);
+        k_scatter<<<blk(ntiles, 128), 128, 0, s>>>(n, hi, lo, idx, pass, hist, ntiles, hi2, lo2, idx2);
+        std::swap(hi, hi2);
+        std::swap(lo, lo2);
+        std::swap(idx, idx2);
+    }
+    k_gather<<<blk(n, 256), 256, 0, s>>>(n, in, idx, out);
+}
+
+// SimpleHyperOctree::update on device records: sort, collapse, compact
+long long update(Arena& A, Rec48* r, long long n, Rec48* tmp, int* flag, cudaStream_t s)
+{
+    sort_records(A, r, n, tmp, s);
+    if (A.err != cudaSuccess) return -1;
+    k_collapse<<<blk(n, 256), 256, 0, s>>>(n, tmp, flag);
+    return compact(A, tmp, n, flag, r, s);
+}
+}  // namespace
+
+extern "C" int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_params* cp, const mpf_cosmology* c, void* records,
+                               int64_t capacity, int64_t* count)
+{
+    if (!rows || n <= 0 || !cp || !c || !count || (capacity > 0 && !records))
+        return fail(MPF_BAD_INPUT, "mpf_cells_build: bad argument");
+    if (cp->acorrection) return fail(MPF_BAD_INPUT, "mpf_cells_build: acorrection is not supported");
+    if (!cp->correction && cp->coarsecorrection)
+        return fail(MPF_BAD_INPUT, "mpf_cells_build: coarsecorrection without correction is not supported");
+    if (cp->correction == 0) return fail(MPF_BAD_INPUT, "mpf_cells_build: correction = 0 (coarsening) is not supported");
+    if (cp->order != 1 && cp->order != 2) return fail(MPF_BAD_INPUT, "mpf_cells_build: order must be 1 or 2");
+    Geometry G;
+    std::memset(&G, 0, sizeof(G));
+    for (int d = 0; d < 3; ++d) {
+        G.vertex[d] = cp->cone_vertex[d];
+        G.base[d] = cp->cone_base[d];
+        G.sc[d] = cp->sphere_center[d];
+    }
+    G.angle = cp->cone_angle;
+    G.sr = cp->sphere_radius;
+    G.rotate = cp->rotm1 != nullptr;
+    if (cp->rotm1)
+        for (int q = 0; q < 9; ++q) G.rot[q] = cp->rotm1[q];
+    G.h = cp->h;
+    G.lbox = cp->lboxmpch;
+    G.mpc = cp->mpc;
+    cudaStream_t s = 0;
+    Arena A;
+    float* drows = A.get<float>((size_t)n * 10);
+    Rec48 *r0 = A.get<Rec48>(n), *r1 = A.get<Rec48>(n);
+    int* flag = A.get<int>(n + 1);
+    if (A.err != cudaSuccess) return fail(MPF_OUT_OF_MEMORY, "mpf_cells_build: device memory");
+    cudaError_t e = cudaMemcpy(drows, rows, (size_t)n * 10 * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
+    // importascii: keys, filter, compaction (file order kept)
+    k_prepare<<<blk(n, 256), 256, 0, s>>>(drows, n, G, flag, r0);
+    long long m = compact(A, r0, n, flag, r1, s);
+    if (cp->coarseonly) {
+        k_level_flag<<<blk(m, 256), 256, 0, s>>>(m, r1, cp->ncoarse + kLevelShift, flag);
+        m = compact(A, r1, m, flag, r0, s);
+        std::swap(r0, r1);
+    }
+    if (m <= 0) {
+        *count = 0;
+        return MPF_OK;
+    }
+    // sistemize, dphidt = 0, update
+    k_sistemize<<<blk(m, 256), 256, 0, s>>>(m, r1, G);
+    m = update(A, r1, m, r0, flag, s);
+    if (A.err != cudaSuccess || m < 0) return fail(MPF_OUT_OF_MEMORY, "mpf_cells_build: device memory");
+    // Input::correct
+    std::vector<Rec48> h((size_t)m);
+    e = cudaMemcpy(h.data(), r1, (size_t)m * sizeof(Rec48), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
+    int ncoarse = 64, nmax = 0;
+    for (const Rec48& x : h) {
+        ncoarse = std::min(ncoarse, x.pad);
+        nmax = std::max(nmax, x.pad);
+    }
+    if (cp->coarsecorrection) {
+        float* rho0 = A.get<float>(m);
+        if (A.err != cudaSuccess) return fail(MPF_OUT_OF_MEMORY, "mpf_cells_build: device memory");
+        k_copy_rho<<<blk(m, 256), 256, 0, s>>>(m, r1, rho0);
+        k_coarse_rho<<<blk(m, 128), 128, 0, s>>>(m, r1, rho0, ncoarse);
+    }
+    for (int L = ncoarse + 1; L <= nmax; ++L) k_from_parent<<<blk(m, 256), 256, 0, s>>>(m, r1, L, 0);
+    for (int L = ncoarse + 1; L <= nmax; ++L) k_from_parent<<<blk(m, 256), 256, 0, s>>>(m, r1, L, 1);
+    // incomplete octs: the 8 children from the gather on the octree so far
+    k_incomplete<<<blk(m, 128), 128, 0, s>>>(m, r1, flag);
+    cudaMemsetAsync(flag + m, 0, sizeof(int), s);
+    const long long ninc = exclusive_scan(flag, m + 1, s);
+    if (ninc > 0) {
+        int* list = A.get<int>(ninc);
+        Rec48* grown = A.get<Rec48>(m + 8 * ninc);
+        Rec48* tmp = A.get<Rec48>(m + 8 * ninc);
+        int* flag2 = A.get<int>(m + 8 * ninc + 1);
+        if (A.err != cudaSuccess) return fail(MPF_OUT_OF_MEMORY, "mpf_cells_build: device memory");
+        // the list of incomplete cells, in key order
+        std::vector<int> hflag((size_t)m + 1), hl;
+        cudaMemcpy(hflag.data(), flag, (size_t)(m + 1) * sizeof(int), cudaMemcpyDeviceToHost);
+        for (long long i = 0; i < m; ++i)
+            if (hflag[i + 1] > hflag[i]) hl.push_back((int)i);
+        cudaMemcpy(list, hl.data(), hl.size() * sizeof(int), cudaMemcpyHostToDevice);
+        // the octree as it stands (records without the level in the pad)
+        std::vector<Rec48> cur((size_t)m);
+        cudaMemcpy(cur.data(), r1, (size_t)m * sizeof(Rec48), cudaMemcpyDeviceToHost);
+        for (Rec48& x : cur) x.pad = 0;
+        mpf_octree* T = nullptr;
+        char err[256] = {0};
+        const int rc = mpf_internal_octree_build(cur.data(), m, 0, s, &T, err, sizeof(err));
+        if (rc != 0) return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: intermediate octree: ") + err);
+        cudaMemcpy(grown, r1, (size_t)m * sizeof(Rec48), cudaMemcpyDeviceToDevice);
+        k_children<<<blk(8 * ninc, 128), 128, 0, s>>>(ninc, r1, list, T->tree, cp->order, grown + m);
+        e = cudaStreamSynchronize(s);
+        mpf_octree_destroy(T);
+        if (e != cudaSuccess) return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
+        m = update(A, grown, m + 8 * ninc, tmp, flag2, s);
+        if (A.err != cudaSuccess || m < 0) return fail(MPF_OUT_OF_MEMORY, "mpf_cells_build: device memory");
+        r1 = grown;
+    }
+    // dphidt *= da/dt at the cell's a
+    k_dphidt<<<blk(m, 256), 256, 0, s>>>(m, r1, c->a, c->dadt, c->n);
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
+    *count = m;
+    if (m > capacity) return fail(MPF_BAD_INPUT, "mpf_cells_build: more cells than capacity (see count)");
+    e = cudaMemcpy(records, r1, (size_t)m * sizeof(Rec48), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
+    return MPF_OK;
+}
+
+extern "C" int mpf_cells_parse(const char* text, int64_t length, float* rows, int64_t capacity, int64_t* count)
+{
+    if (!text || length < 0 || !count || (capacity > 0 && !rows)) return fail(MPF_BAD_INPUT, "mpf_cells_parse: bad argument");
+    // whitespace-separated: an unsigned level then 9 floats per cell (the
+    // reference's stream >> unsigned >> float ... reads)
+    std::string buf(text, (size_t)length);
+    const char* p = buf.c_str();
+    char* end = nullptr;
+    int64_t k = 0;
+    for (;;) {
+        while (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r') ++p;
+        if (!*p) break;
+        float v[10];
+        const unsigned long lv = std::strtoul(p, &end, 10);
+        if (end == p) return fail(MPF_BAD_INPUT, "mpf_cells_parse: malformed level");
+        p = end;
+        v[0] = (float)lv;
+        for (int q = 1; q < 10; ++q) {
+            v[q] = std::strtof(p, &end);
+            if (end == p) return fail(MPF_BAD_INPUT, "mpf_cells_parse: malformed row");
+            p = end;
+        }
+        if (k < capacity)
+            for (int q = 0; q < 10; ++q) rows[10 * k + q] = v[q];
+        ++k;
+    }
+    *count = k;
+    return (k > capacity) ? fail(MPF_BAD_INPUT, "mpf_cells_parse: more rows than capacity (see count)") : MPF_OK;
+}

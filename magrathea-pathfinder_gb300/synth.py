@@ -452,6 +452,38 @@ def make_octree(spec: OctreeSpec, verbose: bool = False) -> np.ndarray:
     return out[order]
 
 
+def cells_ramses(records: np.ndarray, spec: OctreeSpec) -> np.ndarray:
+    """The cells of an octree as the 10-column ASCII rows create_octree reads
+    (level, x, y, z, rho, phi, force x y z, a; input.h:1023-1025): RAMSES file
+    level (octree level - log2 EXTENT), centre in octree units, and phi and
+    force in RAMSES units -- the inverse of Input::sistemize (input.h:368-379):
+    phi_SI = phi (l/t)^2, dphidx_SI = force (l/t^2)(-a), l = a lbox mpc / h,
+    t = a^2 mpc / (h 1e5).  dphidt is not an input (create_octree derives it)."""
+    lev = key_level(records["hi"], records["lo"]).astype(np.int64)
+    out = np.zeros((records.shape[0], 10))
+    for L in np.unique(lev):
+        m = lev == L
+        out[m, 1:4] = cell_center(int(L), key_coords(records["hi"][m], records["lo"][m], int(L)))
+    out[:, 0] = lev - int(np.log2(EXTENT))
+    a = records["a"].astype(np.float64)
+    h = spec.cosmo.h
+    t = a * a * MPC / (h * 1e5)
+    l = a * spec.lbox * MPC / h
+    out[:, 4] = records["rho"]
+    out[:, 5] = records["phi"] * (t / l) ** 2
+    for q, name in enumerate(("dphidx", "dphidy", "dphidz")):
+        out[:, 6 + q] = records[name] / ((l / (t * t)) * (-a))
+    out[:, 9] = a
+    return out
+
+
+def write_cells(path: str, rows: np.ndarray) -> None:
+    """ASCII cell file: integer level, then 9 values at float precision."""
+    with open(path, "w") as f:
+        for r in rows:
+            f.write("%d %s\n" % (int(r[0]), " ".join("%.9g" % v for v in r[1:])))
+
+
 def write_bin(path: str, records: np.ndarray) -> None:
     records.astype(RECORD, copy=False).tofile(path)
 

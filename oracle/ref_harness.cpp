@@ -526,4 +526,42 @@ int64_t ref_propagate_bundle_flrw(const double* L, unsigned count, double angle,
     return m;
 }
 
+// create_octree for one cone from one ASCII cell file (Create_octree::
+// PreparationASCII, create_octree.h:544-580): Input::importascii with the
+// reference's cone / sphere collision filter (input.h:996-1067, 216-226),
+// then Miscellaneous::correctOctree (miscellaneous.h:467-479: sistemize,
+// dphidt = 0, Input::correct, dphidt *= da/dt(a)) on the loaded cosmology.
+// cone7: vertex xyz, base xyz, angle; sphere4: centre xyz, radius; rotm1:
+// 3x3 row-major or NULL (full sky).  out: up to cap 48-byte records (what
+// Input::save writes).  Returns the cell count; *amin_out receives amin.
+struct HarnessBuildParams {
+    unsigned isfullsky, coarseonly, ncoarse, correction, coarsecorrection, acorrection;
+    double mpc;
+};
+
+int64_t ref_build_cone(const char* cellfile, const double* cone7, const double* sphere4, const double* rotm1,
+                       unsigned coarseonly, unsigned ncoarse, unsigned correction, unsigned coarsecorrection,
+                       unsigned acorrection, double mpc, double h, double omegam, double lboxmpch, void* out, int64_t cap,
+                       double* amin_out)
+{
+    HarnessBuildParams prm{rotm1 ? 0u : 1u, coarseonly, ncoarse, correction, coarsecorrection, acorrection, mpc};
+    std::array<std::array<double, 3>, 3> rot = {{{0, 0, 0}}};
+    if (rotm1)
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) rot[r][c] = rotm1[3 * r + c];
+    const point vertex{cone7[0], cone7[1], cone7[2]}, base{cone7[3], cone7[4], cone7[5]};
+    const Cone<point> cone(vertex, base, cone7[6]);
+    const HyperSphere<3, point> sphere(point{sphere4[0], sphere4[1], sphere4[2]}, sphere4[3]);
+    Oct octree;
+    using Element = std::remove_cv<std::remove_reference<decltype(octree[0])>::type>::type;
+    Input::importascii<std::ratio<0>, std::ratio<EXTENT>>(prm, rot, octree, std::string(cellfile),
+                                                          [&](const Element& e) { return Input::collide(octree, std::get<0>(e), sphere, cone); });
+    double amin = 0.0;
+    Miscellaneous::correctOctree(octree, g_cosmo, prm, h, omegam, lboxmpch, amin);
+    const int64_t m = (int64_t)octree.size();
+    for (int64_t k = 0; k < m && k < cap; ++k) std::memcpy((char*)out + 48 * k, &octree[k], 48);
+    if (amin_out) *amin_out = amin;
+    return m;
+}
+
 }  // extern "C"

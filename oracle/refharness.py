@@ -72,6 +72,9 @@ def lib(order: int = 2):
         L.ref_propagate_bundle.argtypes = [_p, C.c_uint, _d, _d, C.c_char_p, _d, C.c_uint, _p, _i64, C.c_char_p, _i64]
         L.ref_propagate_bundle_flrw.restype = _i64
         L.ref_propagate_bundle_flrw.argtypes = [_p, C.c_uint, _d, C.c_char_p, C.c_uint, C.c_uint, _p, _i64]
+        L.ref_build_cone.restype = _i64
+        L.ref_build_cone.argtypes = [C.c_char_p, _p, _p, _p, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, _d, _d, _d,
+                                     _d, _p, _i64, _p]
         _LIBS[order] = L
     return _LIBS[order]
 
@@ -174,6 +177,20 @@ class Reference:
         m = self.L.ref_propagate_bundle_flrw(_ptr(L), int(count), float(angle), interp.encode(), int(nsteps), int(level),
                                              _ptr(out), cap)
         return out[:min(m, cap)]
+
+    def build_cone(self, cellfile, cone7, sphere4, rotm1=None, coarseonly=0, ncoarse=0, correction=1,
+                   coarsecorrection=1, acorrection=0, mpc=3.08568e22, h=0.68, omegam=0.31, lboxmpch=2048.0,
+                   cap=1 << 22):
+        """create_octree for one cone from one ASCII cell file: (48-byte records, amin)."""
+        rec = np.zeros(cap * 48, dtype=np.uint8)
+        amin = np.zeros(1)
+        c7 = np.ascontiguousarray(cone7, dtype=np.float64)
+        s4 = np.ascontiguousarray(sphere4, dtype=np.float64)
+        rm = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64)
+        m = self.L.ref_build_cone(cellfile.encode(), _ptr(c7), _ptr(s4), _ptr(rm) if rm is not None else None,
+                                  coarseonly, ncoarse, correction, coarsecorrection, acorrection, mpc, h, omegam,
+                                  lboxmpch, _ptr(rec), cap, _ptr(amin))
+        return rec[:48 * min(m, cap)].copy(), float(amin[0])
 
     def homogeneous(self, zs):
         zs = np.ascontiguousarray(zs, dtype=np.float64)

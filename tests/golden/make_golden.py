@@ -243,10 +243,65 @@ def make_rays():
                                                             out["ref_sizes_o2"].tolist(), path, os.path.getsize(path) // 1024))
 
 
+# create_octree from ASCII cells (Input::importascii + Miscellaneous::correctOctree):
+# the synthetic cone written as RAMSES-unit rows, with duplicated cells of a
+# neighbouring light-cone shell (different a and phi), non-normal densities
+# at the coarse and refined levels, and refined cells missing some children
+CELLS_SPEC = dict(base_level=6, box_cells=16, lbox=2048.0, half_y=2.5, half_z=2.5, chi_max=1000.0, halos=3,
+                  max_level=8, mass_min=3e14, mass_max=2e15, refine_cells=1.5, seed=9)
+
+
+def make_cells():
+    spec = S.OctreeSpec(**CELLS_SPEC)
+    rec = S.make_octree(spec)
+    rows = S.cells_ramses(rec, spec)
+    rng = np.random.default_rng(31)
+    lev = rows[:, 0].astype(int)
+    coarse = np.flatnonzero(lev == lev.min())
+    fine = np.flatnonzero(lev > lev.min())
+    rows[rng.choice(coarse, 6, replace=False), 4] = 0.0        # non-normal coarse densities
+    rows[rng.choice(fine, 6, replace=False), 4] = 0.0          # non-normal refined densities
+    dup = rng.choice(rows.shape[0], rows.shape[0] // 20, replace=False)
+    extra = rows[dup].copy()
+    extra[:, 9] *= 1.0 - 3e-4                                  # the neighbouring shell: earlier a ...
+    extra[:, 5] *= 1.02                                        # ... and a different potential
+    # a refined parent whose children are partly missing
+    deep = np.flatnonzero(lev == lev.max())
+    drop = deep[:3] if deep.shape[0] >= 8 else np.zeros(0, dtype=int)
+    keep = np.ones(rows.shape[0], dtype=bool)
+    keep[drop] = False
+    allrows = np.concatenate([rows[keep], extra])
+    allrows = allrows[rng.permutation(allrows.shape[0])]
+    tmp = tempfile.mkdtemp(prefix="mpf_golden_")
+    cellfile = os.path.join(tmp, "cells_00000.dat")
+    S.write_cells(cellfile, allrows)
+    celldir, pf, ef = S.write_param_files(tmp, spec.cosmo, spec.lbox)
+    cone7 = np.array([0.0, 0.0, 0.0, spec.chi_max / spec.lbox, 0.0, 0.0, np.radians(2.0)])
+    sphere4 = np.array([0.0, 0.0, 0.0, 1.0 / 32.0])
+    text = open(cellfile).read()
+    out = dict(cells_text=np.array(text), cone7=cone7, sphere4=sphere4, lboxmpch=spec.lbox, h=spec.cosmo.h,
+               omegam=spec.cosmo.omega_m, mpc=S.MPC)
+    R = Reference(2)
+    cos = R.cosmology(celldir, pf, ef)
+    for k in ("t", "a", "dadt", "d2adt2", "length"):
+        out["cosmo_" + k] = cos[k]
+    for name, kw in (("full", dict(correction=1, coarsecorrection=1)), ("nocorr", dict(correction=0, coarsecorrection=0))):
+        recs, amin = R.build_cone(cellfile, cone7, sphere4, mpc=S.MPC, h=spec.cosmo.h, omegam=spec.cosmo.omega_m,
+                                  lboxmpch=spec.lbox, **kw)
+        out["ref_records_" + name] = recs
+        out["ref_amin_" + name] = amin
+        print("cells %s: %d rows in, %d cells out" % (name, allrows.shape[0], recs.shape[0] // 48))
+    path = os.path.join(HERE, "cells.npz")
+    np.savez_compressed(path, **out)
+    print("cells -> %s (%d KB)" % (path, os.path.getsize(path) // 1024))
+
+
 if __name__ == "__main__":
-    names = sys.argv[1:] or list(CASES) + ["rays"]
+    names = sys.argv[1:] or list(CASES) + ["rays", "cells"]
     for name in names:
         if name == "rays":
             make_rays()
+        elif name == "cells":
+            make_cells()
         else:
             make(name, CASES[name])
