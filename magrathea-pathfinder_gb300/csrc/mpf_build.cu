@@ -224,16 +224,27 @@ __global__ void k_collapse(long long n, Rec48* r, int* flag)
     r[i] = keep;
 }
 
-// exact-key search in the sorted records
-__device__ __forceinline__ long long find_key(const Rec48* r, long long n, Key k)
+__device__ __forceinline__ void key_coords(Key k, int L, uint64_t* c);
+
+// SimpleHyperOctree::find (simplehyperoctree.h:842-847): the last record with
+// a key <= K if it contains K (K itself or an ancestor of K), else -1
+__device__ __forceinline__ long long find_containing(const Rec48* r, long long n, Key k, int Lk)
 {
     long long lo = 0, hi = n;
     while (lo < hi) {
         const long long mid = (lo + hi) >> 1;
-        if (key_less(rkey(r[mid]), k)) lo = mid + 1;
+        if (!key_less(k, rkey(r[mid]))) lo = mid + 1;
         else hi = mid;
     }
-    return (lo < n && key_eq(rkey(r[lo]), k)) ? lo : -1;
+    const long long j = lo - (lo > 0);
+    if (n <= 0) return -1;
+    const int Lj = r[j].pad;
+    if (Lj > Lk) return -1;
+    uint64_t cj[3], ck[3];
+    key_coords(rkey(r[j]), Lj, cj);
+    key_coords(k, Lk, ck);
+    const int s = Lk - Lj;
+    return ((ck[0] >> s) == cj[0] && (ck[1] >> s) == cj[1] && (ck[2] >> s) == cj[2] && key_le(rkey(r[j]), k)) ? j : -1;
 }
 
 __device__ __forceinline__ void key_coords(Key k, int L, uint64_t* c)
@@ -267,7 +278,7 @@ __global__ void k_coarse_rho(long long n, Rec48* r, const float* __restrict__ rh
                 if (ix == 0 && iy == 0 && iz == 0) continue;
                 const Key nk = key_from_coords(L, (c[0] + (uint64_t)(int64_t)ix) & mask, (c[1] + (uint64_t)(int64_t)iy) & mask,
                                                (c[2] + (uint64_t)(int64_t)iz) & mask);
-                const long long j = find_key(r, n, nk);
+                const long long j = find_containing(r, n, nk, L);
                 if (j >= 0 && normal_f(rho0[j])) {
                     result += rho0[j];
                     ++count;
@@ -293,14 +304,16 @@ __global__ void k_from_parent(long long n, Rec48* r, int L, int which)
     if (normal_f(v)) return;
     uint64_t c[3];
     key_coords(rkey(r[i]), L, c);
-    const long long p = find_key(r, n, key_from_coords(L - 1, c[0] >> 1, c[1] >> 1, c[2] >> 1));
+    const long long p = find_containing(r, n, key_from_coords(L - 1, c[0] >> 1, c[1] >> 1, c[2] >> 1), L - 1);
     if (p < 0) return;   // the reference dereferences end() there; the cell keeps its value
     if (which) r[i].rho = r[p].rho;
     else r[i].dt = r[p].dt;
 }
 
-// non-leaf cells (the next cell is a descendant) with some of their 8
-// children missing: flag = 1
+// non-leaf cells (the next cell is a descendant) with a child that
+// SimpleHyperOctree::find does not resolve (no record at or above the child's
+// key contains it; a missing child that sorts right after its parent is
+// resolved to the parent and not completed, as in the reference): flag = 1
 __global__ void k_incomplete(long long n, const Rec48* __restrict__ r, int* flag)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -320,7 +333,7 @@ __global__ void k_incomplete(long long n, const Rec48* __restrict__ r, int* flag
     int missing = 0;
     for (int site = 0; site < 8; ++site) {
         const Key ck = key_from_coords(L + 1, 2 * c[0] + (site & 1), 2 * c[1] + ((site >> 1) & 1), 2 * c[2] + ((site >> 2) & 1));
-        missing += (find_key(r, n, ck) < 0);
+        missing += (find_containing(r, n, ck, L + 1) < 0);
     }
     flag[i] = missing > 0;
 }
