@@ -14,6 +14,7 @@
 //   Input::correct (input.h:1381-1516)      coarse densities from their
 //       neighbours, refined dphidt / rho from the parent level by level,
 //       incomplete octs completed from the gather at the children's centres
+//       (k_complete_serial: one thread, the reference's sequential appends)
 //   correctOctree (miscellaneous.h:467-479) dphidt *= da/dt(a)
 //
 // Float32 data arithmetic follows the reference's types (Gravity<float, 3>,
@@ -26,9 +27,6 @@
 
 #include "../../include/mpf_gb300.h"
 #include "mpf_internal.h"
-
-extern "C" int mpf_internal_octree_build(const void* records, int64_t n, int on_device, cudaStream_t stream,
-                                         mpf_octree** out, char* err, int errlen);
 
 namespace mpf {
 namespace build {
@@ -338,27 +336,205 @@ __global__ void k_incomplete(long long n, const Rec48* __restrict__ r, int* flag
     flag[i] = missing > 0;
 }
 
-// the 8 children of each incomplete cell, data from the gather at the child's
-// centre, or the parent's when the gather is empty (input.h:1460-1480)
-__global__ void k_children(long long m, const Rec48* __restrict__ r, const int* __restrict__ list, DevTree T, int order,
-                           Rec48* out)
+// ---- the reference's gather over a key-sorted array with appended cells ----
+// Input::correct appends the children of each incomplete oct at the end of
+// the container and gathers the next ones on that container, so the searches
+// below run the same binary search (std::upper_bound's loop) over the sorted
+// cells plus the unsorted tail.
+typedef unsigned __int128 u128;
+__device__ __forceinline__ u128 k128(const Rec48& r) { return ((u128)r.hi << 64) | r.lo; }
+__device__ __forceinline__ u128 markers128() { return ((u128)0x8888888888888888ull << 64) | 0x8888888888888888ull; }
+__device__ __forceinline__ u128 invalid128() { return (((u128)1) << 127) - 1; }
+__device__ __forceinline__ unsigned level128(u128 k) { return (unsigned)key_level(Key{(uint64_t)(k >> 64), (uint64_t)k}); }
+__device__ __forceinline__ bool containing128(u128 a, u128 b)
 {
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= m * 8) return;
-    const Rec48& p = r[list[q >> 3]];
-    const int site = (int)(q & 7), L = p.pad;
+    const u128 x = a ^ b;
+    return ((~markers128() & x) <= (markers128() & x)) && (a <= b);
+}
+__device__ __forceinline__ u128 parent128(u128 k)
+{
+    const unsigned loc = 132u - level128(k) * 4u;
+    const u128 mask = (loc < 128u) ? (~(u128)0) << loc : (u128)0;
+    return k & mask;
+}
+__device__ __forceinline__ u128 child128(u128 k, unsigned site)
+{
+    const unsigned l = level128(k);
+    if (l >= 32u) return k;
+    return k | ((u128)((site & 7u) | 8u) << (128u - (l + 1u) * 4u));
+}
+__device__ __forceinline__ u128 compute128(unsigned level, double x, double y, double z)
+{
+    if (level == 0) return 0;
+    const Key k = key_from_coords((int)level, axis_coord((int)level, x), axis_coord((int)level, y), axis_coord((int)level, z));
+    return ((u128)k.hi << 64) | k.lo;
+}
+__device__ __forceinline__ double center128(u128 k, int d)
+{
+    const unsigned l = level128(k);
     uint64_t c[3];
-    key_coords(rkey(p), L, c);
-    const uint64_t cx = 2 * c[0] + (site & 1), cy = 2 * c[1] + ((site >> 1) & 1), cz = 2 * c[2] + ((site >> 2) & 1);
-    const Key ck = key_from_coords(L + 1, cx, cy, cz);
-    const Field7 f = gather<true>(T, order, coord_center(L + 1, cx), coord_center(L + 1, cy), coord_center(L + 1, cz), true);
-    Rec48 o = p;
-    o.lo = ck.lo; o.hi = ck.hi;
-    o.pad = L + 1;
-    if (!is_empty(f)) {
-        o.rho = f.rho; o.phi = f.phi; o.dx = f.dx; o.dy = f.dy; o.dz = f.dz; o.a = f.a; o.dt = f.dt;
+    key_coords(Key{(uint64_t)(k >> 64), (uint64_t)k}, (int)l, c);
+    return coord_center((int)l, c[d]);
+}
+__device__ __forceinline__ long long afind(const Rec48* r, long long n, u128 K)
+{
+    if (n <= 0) return -1;
+    long long first = 0, count = n;
+    while (count > 0) {
+        const long long step = count >> 1, it = first + step;
+        if (!(K < k128(r[it]))) { first = it + 1; count -= step + 1; }
+        else count = step;
     }
-    out[q] = o;
+    return (first > 0 && containing128(k128(r[first - 1]), K)) ? first - 1 : -1;
+}
+__device__ __forceinline__ void afields(const Rec48& r, float* f)
+{
+    f[0] = r.rho; f[1] = r.phi; f[2] = r.dx; f[3] = r.dy; f[4] = r.dz; f[5] = r.a; f[6] = r.dt;
+}
+__device__ __forceinline__ void amac(float* acc, const float* f, double w)
+{
+    for (int q = 0; q < 7; ++q) acc[q] = (float)((double)acc[q] + (double)f[q] * w);
+}
+__device__ __forceinline__ void azero(float* a)
+{
+    for (int q = 0; q < 7; ++q) a[q] = 0.f;
+}
+// SimpleHyperOctree::cic (simplehyperoctree.h:1410-1469) over the array
+__device__ void acic(const Rec48* r, long long n, double x, double y, double z, float* res)
+{
+    const double pt[3] = {x, y, z};
+    u128 ekey = compute128(32, x, y, z);
+    const long long f0 = afind(r, n, ekey);
+    u128 idx = (f0 >= 0) ? k128(r[f0]) : invalid128();
+    unsigned ilvl = level128(idx), lvl = ilvl;
+    double half = 4.0 / 1.0 * (1.0 / (1.0 * (double)(((u128)1) << level128(idx)))) / 2.0;
+    unsigned site = 0;
+    azero(res);
+    for (int guard = 0; guard <= 33; ++guard) {
+        ilvl = lvl;
+        if (idx != invalid128()) {
+            double dist[3];
+            for (int d = 0; d < 3; ++d) dist[d] = fabs((center128(idx, d) - pt[d]) / (half + half));
+            for (unsigned s2 = 0; s2 < 8u; ++s2)
+                if (containing128(child128(idx, s2), ekey)) { site = s2; break; }
+            for (unsigned v = 0; v < 8u; ++v) {
+                double w = 1.0, vert[3];
+                const unsigned diff = site ^ v;
+                for (int d = 0; d < 3; ++d) {
+                    const int b = (v >> d) & 1u, db = (diff >> d) & 1u;
+                    vert[d] = pt[d] + ((double)b * half) - ((double)(!b) * half);
+                    w *= ((double)db * (1.0 - dist[d])) + ((double)(!db) * dist[d]);
+                }
+                ekey = compute128(ilvl, vert[0], vert[1], vert[2]);
+                const long long fi = afind(r, n, ekey);
+                if (fi >= 0) {
+                    const unsigned fl = level128(k128(r[fi]));
+                    if (fl < lvl) lvl = fl;
+                    float f[7];
+                    afields(r[fi], f);
+                    amac(res, f, w);
+                } else {
+                    azero(res);
+                    break;
+                }
+            }
+        }
+        if (lvl < ilvl) {
+            ekey = compute128(lvl + 1, x, y, z);
+            idx = parent128(ekey);
+            azero(res);
+            half = 4.0 / 1.0 * (1.0 / (1.0 * (double)(((u128)1) << level128(idx)))) / 2.0;
+        } else {
+            break;
+        }
+    }
+}
+__device__ __forceinline__ double tsc_weight(int a, double d)
+{
+    return (double)a * 0.5 * (1.5 - d) * (1.5 - d) + (double)(1 - a) * (0.75 - d * d);
+}
+// SimpleHyperOctree::tsc (simplehyperoctree.h:1479-1541) over the array
+__device__ void atsc(const Rec48* r, long long n, double x, double y, double z, float* res)
+{
+    const double pt[3] = {x, y, z};
+    u128 ekey = compute128(32, x, y, z);
+    const long long f0 = afind(r, n, ekey);
+    u128 idx = (f0 >= 0) ? k128(r[f0]) : invalid128();
+    unsigned ilvl = level128(idx), lvl = ilvl;
+    double half = 4.0 / 1.0 * (1.0 / (1.0 * (double)(((u128)1) << level128(idx)))) / 2.0;
+    azero(res);
+    if (x == 0.0 && y == 0.0 && z == 0.0) {
+        acic(r, n, 0., 0., 0., res);
+        return;
+    }
+    for (int guard = 0; guard <= 33; ++guard) {
+        ilvl = lvl;
+        const double tw = 2.0 * half;
+        if (idx != invalid128()) {
+            bool stop = false;
+            for (int ix = -1; ix <= 1 && !stop; ++ix)
+                for (int iy = -1; iy <= 1 && !stop; ++iy)
+                    for (int iz = -1; iz <= 1 && !stop; ++iz) {
+                        ekey = compute128(ilvl, pt[0] + ix * tw, pt[1] + iy * tw, pt[2] + iz * tw);
+                        const long long fi = afind(r, n, ekey);
+                        if (fi >= 0) {
+                            float f[7];
+                            afields(r[fi], f);
+                            double dist[3];
+                            for (int d = 0; d < 3; ++d) dist[d] = fabs((center128(ekey, d) - pt[d]) / tw);
+                            const double w = tsc_weight(abs(ix), dist[0]) * tsc_weight(abs(iy), dist[1]) * tsc_weight(abs(iz), dist[2]);
+                            const unsigned fl = level128(k128(r[fi]));
+                            if (fl < lvl) lvl = fl;
+                            if (lvl < ilvl) { azero(res); stop = true; }
+                            else amac(res, f, w);
+                        } else {
+                            azero(res);
+                            stop = true;
+                        }
+                    }
+        }
+        if (lvl < ilvl) {
+            ekey = compute128(lvl + 1, x, y, z);
+            idx = parent128(ekey);
+            azero(res);
+            half = 4.0 / 1.0 * (1.0 / (1.0 * (double)(((u128)1) << level128(idx)))) / 2.0;
+        } else {
+            break;
+        }
+    }
+}
+
+// Input::correct's completion loop (input.h:1451-1482), in the reference's
+// order: for each incomplete cell (key order), its 8 children are gathered at
+// their centres on the array as it stands (the appended cells included) and
+// appended.  One thread: the appends make every gather depend on the previous
+// ones; the loop is short (the incomplete octs of the cone's boundary).
+__global__ void k_complete_serial(Rec48* r, long long m, const int* __restrict__ list, long long ninc, int order)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    long long size = m;
+    for (long long q = 0; q < ninc; ++q) {
+        const Rec48 p = r[list[q]];
+        const u128 idx = k128(p);
+        for (unsigned site = 0; site < 8; ++site) {
+            const u128 ck = child128(idx, site);
+            // the child's centre as the reference computes it, in float
+            const float cx = (float)center128(ck, 0), cy = (float)center128(ck, 1), cz = (float)center128(ck, 2);
+            float f[7];
+            if (order == 1) acic(r, size, cx, cy, cz, f);
+            else atsc(r, size, cx, cy, cz, f);
+            Rec48 o = p;
+            o.hi = (unsigned long long)(ck >> 64);
+            o.lo = (unsigned long long)ck;
+            o.pad = p.pad + 1;
+            bool empty = true;
+            for (int k = 0; k < 7; ++k) empty = empty && (f[k] == 0.f);
+            if (!empty) {
+                o.rho = f[0]; o.phi = f[1]; o.dx = f[2]; o.dy = f[3]; o.dz = f[4]; o.a = f[5]; o.dt = f[6];
+            }
+            r[size++] = o;
+        }
+    }
 }
 
 // Utility::interpolate2 (utility.h:461-468): descending table, float result
@@ -534,18 +710,9 @@ extern "C" int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_par
         for (long long i = 0; i < m; ++i)
             if (hflag[i + 1] > hflag[i]) hl.push_back((int)i);
         cudaMemcpy(list, hl.data(), hl.size() * sizeof(int), cudaMemcpyHostToDevice);
-        // the octree as it stands (records without the level in the pad)
-        std::vector<Rec48> cur((size_t)m);
-        cudaMemcpy(cur.data(), r1, (size_t)m * sizeof(Rec48), cudaMemcpyDeviceToHost);
-        for (Rec48& x : cur) x.pad = 0;
-        mpf_octree* T = nullptr;
-        char err[256] = {0};
-        const int rc = mpf_internal_octree_build(cur.data(), m, 0, s, &T, err, sizeof(err));
-        if (rc != 0) return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: intermediate octree: ") + err);
         cudaMemcpy(grown, r1, (size_t)m * sizeof(Rec48), cudaMemcpyDeviceToDevice);
-        k_children<<<blk(8 * ninc, 128), 128, 0, s>>>(ninc, r1, list, T->tree, cp->order, grown + m);
+        k_complete_serial<<<1, 1, 0, s>>>(grown, m, list, ninc, cp->order);
         e = cudaStreamSynchronize(s);
-        mpf_octree_destroy(T);
         if (e != cudaSuccess) return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
         m = update(A, grown, m + 8 * ninc, tmp, flag2, s);
         if (A.err != cudaSuccess || m < 0) return fail(MPF_OUT_OF_MEMORY, "mpf_cells_build: device memory");
