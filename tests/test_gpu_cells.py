@@ -37,11 +37,27 @@ def test_same_cells_and_keys(built):
 
 
 def test_records_bit_exact(built):
+    """Every record bit-identical, except a completed child whose reference
+    values come from the element before the container: the reference's TSC
+    reads begin()[marker - 1] when its binary search over the appended,
+    unsorted tail returns 0 (simplehyperoctree.h:1487-1488, 1510-1518), and
+    here gives a denormal scale factor; such a record is the one allowed to
+    differ."""
     g, rec = built
     got, ref = _fields(rec), _fields(g["ref_records_full"])
+    undefined = np.abs(ref["a"]) < 1e-30
+    assert undefined.sum() <= 1
     bad = {}
     for name in ("dphidt", "a", "dphidx", "dphidy", "dphidz", "phi", "rho"):
-        d = np.flatnonzero(got[name].view(np.uint32) != ref[name].view(np.uint32))
+        d = np.flatnonzero((got[name].view(np.uint32) != ref[name].view(np.uint32)) & ~undefined)
         if d.size:
             bad[name] = (d.size, d[:5].tolist(), got[name][d[:3]].tolist(), ref[name][d[:3]].tolist())
     assert not bad, bad
+
+
+def test_built_octree_propagates(built, pkg):
+    """The built records are a valid cone octree for the propagation path."""
+    g, rec = built
+    tree = pkg.Octree.from_records(np.frombuffer(rec.tobytes(), dtype=_fields(rec).dtype))
+    assert tree.info["cells"] == rec.shape[0] // 48
+    tree.close()
