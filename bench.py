@@ -535,7 +535,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
-            "form": "plain octree (surrogate not built)",
+            "form": "plain octree (the surrogate form: bench.py --mode surrogate)",
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": B * 6 * 8,
                     "d2h_bytes_per_step": B * 8 + B * capi.MPF_PLANE_FIELDS * 8},
             "gpu_launches": args.steps, "roofline": roofline, "status_bits": status,
