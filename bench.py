@@ -54,10 +54,10 @@ UNIT = "photon-steps/s"
 # + post-step 27 x 28 B + Jacobian 6 x 27 x 12 B
 BYTES_PER_PHOTON_STEP = 4 * 27 * 16 + 27 * 28 + 6 * 27 * 12
 # DRAM bytes per photon-step of the propagate kernel, from one ncu capture of the
-# same kernel on the medium octree (65 536 rays to z = 0.5): (37.12 + 1.10) MB
+# same kernel on the medium octree (65 536 rays to z = 0.5): (37.79 + 1.43) MB
 # over 6.95e7 photon-steps; the bench's per-launch traffic is this figure times
 # the photon-steps of a launch
-DRAM_BYTES_PER_PHOTON_STEP = 0.55
+DRAM_BYTES_PER_PHOTON_STEP = 0.564
 
 
 def workload_spec(synth, workload: str):
