@@ -236,10 +236,13 @@ int mpf_hmaps_fill(const mpf_octree* o, const mpf_cosmology* c, const mpf_params
 /* Same with jacobiantype = "bundle" (Lensing::dbetadtheta, src/lensing.h:148-336;
  * FillMap hmaps.h:653-695, 725-747): four extra rays per pixel on a screen at
  * +-tan(openingmin) (radians) around the pixel direction, integrated with the
- * stop criterion stop_bundle (an mpf_stop other than MPF_STOP_PLANE or
- * MPF_STOP_S) to the central ray's value of that quantity at each surface;
- * the screen normal is the central ray's direction (plane_sachs = 1, the
- * reference's plane = "sachs") or position (0, "normal").  Lensing gives 5
+ * stop criterion stop_bundle (an mpf_stop other than MPF_STOP_S, which the
+ * reference's dbetadtheta does not accept either) to the central ray's value
+ * of that quantity at each surface; the screen normal is the central ray's
+ * direction (plane_sachs = 1, the reference's plane = "sachs") or position
+ * (0, "normal").  With MPF_STOP_PLANE each surface stops the four rays on the
+ * plane through the central ray's crossing point normal to that screen normal
+ * (lensing.h:201, 281-294: kiTarget . position = kiTarget . posTarget).  Lensing gives 5
  * rows per surface: kappa, gamma1, gamma2, w (image rotation), 1/mu. */
 int mpf_hmaps_fill_bundle(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t nside, int64_t npix,
                           const int64_t* pixels, int ncomp, const int* components, const double* homogeneous,

@@ -387,9 +387,9 @@ int hmaps_fill_impl(const mpf_octree* o, const mpf_cosmology* c, const mpf_param
         M.nmaps += (k == MPF_MAP_LENSING) ? (bundle ? 5 : 4) : (k == MPF_MAP_DEFLECTION) ? 2 : 1;
     }
     if (bundle) {
-        if (stop_bundle < 0 || stop_bundle > 6 || stop_bundle == MPF_STOP_PLANE || stop_bundle == MPF_STOP_S ||
-            !(openingmin > 0.0) || !(openingmin < 1.0))
-            return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill_bundle: stop_bundle must be redshift, r, lambda, t or a, "
+        // Lensing::dbetadtheta knows lambda, r, redshift, a, t and plane (lensing.h:198-296)
+        if (stop_bundle < 0 || stop_bundle > 5 || !(openingmin > 0.0) || !(openingmin < 1.0))
+            return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill_bundle: stop_bundle must be redshift, r, lambda, t, a or plane, "
                                           "and 0 < openingmin < 1 radian");
         M.bundle = 1;
         M.plane_sachs = plane_sachs ? 1 : 0;

@@ -671,10 +671,15 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         prow[24] = b.a; prow[25] = b.phi; prow[26] = b.k1; prow[27] = b.k2; prow[28] = b.k3;
         prow[29] = prow[30] = prow[31] = 0.0;
     }
+    // this ray's plane normals (stop criterion "plane" with per-ray surfaces; wide instantiation)
+    const double* rki = (WIDE && P.ray_ki) ? P.ray_ki + i * np * 3 : nullptr;
+    auto start_q = [&](int jn) -> double {
+        if (rki && skind == STOP_PLANE) return b.x * rki[3 * jn] + b.y * rki[3 * jn + 1] + b.z * rki[3 * jn + 2];
+        return (skind == STOP_R) ? b.chi : (skind == STOP_LAMBDA) ? b.lambda : (skind == STOP_T) ? b.t
+             : (skind == STOP_S) ? b.s : b.red;
+    };
     while (next_plane < np && ((skind == STOP_A) ? (b.a < (SRC ? stop_ref : rpl[next_plane]))
-                                                  : (((skind == STOP_R) ? b.chi : (skind == STOP_LAMBDA) ? b.lambda
-                                                      : (skind == STOP_T) ? b.t : (skind == STOP_S) ? b.s : b.red) >
-                                                     (SRC ? stop_ref : rpl[next_plane])))) {
+                                                  : (start_q(next_plane) > (SRC ? stop_ref : rpl[next_plane])))) {
         cross_k[next_plane] = 0;
         ++next_plane;
     }
@@ -786,7 +791,9 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             }
             while (next_plane < np) {
                 const int kind = skind;
-                const double q1 = (kind == STOP_R) ? p.chi : (kind == STOP_LAMBDA) ? p.lambda : (kind == STOP_T) ? p.t
+                const double* kj = (WIDE && rki && kind == STOP_PLANE) ? rki + 3 * next_plane : nullptr;
+                const double q1 = kj ? (p.x * kj[0] + p.y * kj[1] + p.z * kj[2])
+                                : (kind == STOP_R) ? p.chi : (kind == STOP_LAMBDA) ? p.lambda : (kind == STOP_T) ? p.t
                                 : (kind == STOP_A) ? p.a : (kind == STOP_S) ? p.s : p.red;
                 const double ref = SRC ? stop_ref : rpl[next_plane];
                 if (!((kind == STOP_A) ? (q1 < ref) : (q1 > ref))) break;
@@ -794,7 +801,8 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                 cross_k[j] = k;
                 if (prow) {
                     double* o = prow + j * rec_fields;
-                    const double q0 = (kind == STOP_R) ? b.chi : (kind == STOP_LAMBDA) ? b.lambda : (kind == STOP_T) ? b.t
+                    const double q0 = kj ? (b.x * kj[0] + b.y * kj[1] + b.z * kj[2])
+                                    : (kind == STOP_R) ? b.chi : (kind == STOP_LAMBDA) ? b.lambda : (kind == STOP_T) ? b.t
                                     : (kind == STOP_A) ? b.a : (kind == STOP_S) ? b.s : b.red;
                     const double f = (q1 - ref) / (q1 - q0);
                     const double px = b.x * f + p.x * (1 - f), py = b.y * f + p.y * (1 - f), pz = b.z * f + p.z * (1 - f);
@@ -864,7 +872,11 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         case STOP_REDSHIFT: stop = b.red > stop_ref; break;
         case STOP_T: stop = b.t > stop_ref; break;
         case STOP_A: stop = b.a < stop_ref; break;
-        case STOP_PLANE: stop = (p.x * P.ki[0] + p.y * P.ki[1] + p.z * P.ki[2]) > stop_ref; break;
+        case STOP_PLANE: {
+            const double* kk = (WIDE && rki) ? rki + 3 * (np - 1) : P.ki;
+            stop = (p.x * kk[0] + p.y * kk[1] + p.z * kk[2]) > stop_ref;
+            break;
+        }
         case STOP_S: stop = b.s > stop_ref; break;
         default: stop = true;
         }

@@ -140,7 +140,7 @@ __global__ void k_fill_maps(long long n, int nz, MapSpec M, const double* __rest
 __global__ void k_bundle_prepare(long long n, int nz, MapSpec M, const double* __restrict__ planes,
                                  const double* __restrict__ launch, const double* __restrict__ rec,
                                  double* __restrict__ blaunch, double* __restrict__ bplanes, double* __restrict__ ki,
-                                 double* __restrict__ dist)
+                                 double* __restrict__ dist, double* __restrict__ bki)
 {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
@@ -161,12 +161,17 @@ __global__ void k_bundle_prepare(long long n, int nz, MapSpec M, const double* _
         case STOP_REDSHIFT: v = o[11]; break;
         case STOP_A: v = o[10]; break;
         case STOP_T: v = o[9]; break;
+        case STOP_PLANE: v = k[0] * o[2] + k[1] * o[3] + k[2] * o[4]; break;   // kiTarget . posTarget
         default: v = o[11];
         }
         // a surface the central ray never reached has no interpolated value
         // (the reference reads past the trajectory there); its own value stands in
         if (!found) v = planes[iz];
-        for (int r = 0; r < 4; ++r) bplanes[(4 * j + r) * nz + iz] = v;
+        for (int r = 0; r < 4; ++r) {
+            bplanes[(4 * j + r) * nz + iz] = v;
+            if (bki)
+                for (int d = 0; d < 3; ++d) bki[((4 * j + r) * nz + iz) * 3 + d] = k[d];
+        }
     }
     // the screen around the pixel direction
     const double* L = launch + 6 * j;
@@ -264,7 +269,7 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
         // central rays with wide records, then four bundle rays per pixel to
         // their own stop_bundle surfaces, then the Jacobians and the rows
         double *wrec = nullptr, *blaunch = nullptr, *bplanes = nullptr, *brec = nullptr, *ki = nullptr, *dist = nullptr,
-               *jac = nullptr, *dplanes = nullptr;
+               *jac = nullptr, *dplanes = nullptr, *bki = nullptr;
         long long* bsteps = nullptr;
         e = cudaMalloc(&wrec, (size_t)cap * nz * kWideFields * sizeof(double));
         if (e == cudaSuccess) e = cudaMalloc(&blaunch, (size_t)cap * 24 * sizeof(double));
@@ -275,6 +280,8 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
         if (e == cudaSuccess) e = cudaMalloc(&jac, (size_t)cap * nz * 4 * sizeof(double));
         if (e == cudaSuccess) e = cudaMalloc(&bsteps, (size_t)cap * 4 * sizeof(long long));
         if (e == cudaSuccess) e = cudaMalloc(&dplanes, (size_t)nz * sizeof(double));
+        // stop_bundle = plane: each bundle ray's surfaces are planes of normal kiTarget
+        if (e == cudaSuccess && M.stop_bundle == STOP_PLANE) e = cudaMalloc(&bki, (size_t)cap * 4 * nz * 3 * sizeof(double));
         if (e == cudaSuccess) e = cudaMemcpyAsync(dplanes, P.planes, (size_t)nz * sizeof(double), cudaMemcpyHostToDevice, stream);
         PropParams Pc = P;
         Pc.wide = 1;
@@ -284,6 +291,7 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
         Pb.jacobian = 0;
         Pb.stop_kind = M.stop_bundle;
         Pb.ray_planes = bplanes;
+        Pb.ray_ki = bki;
         const PropOut Oc{steps, nullptr, wrec, status, nullptr};
         const PropOut Ob{bsteps, nullptr, brec, status, nullptr};
         for (long long c0 = 0; e == cudaSuccess && c0 < npix; c0 += cap) {
@@ -292,7 +300,8 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             e = exact ? launch_propagate<true>(T, C, Pc, launch, m, Oc, stream) : launch_propagate<false>(T, C, Pc, launch, m, Oc, stream);
             if (e != cudaSuccess) break;
-            k_bundle_prepare<<<blocks(m, 128), 128, 0, stream>>>(m, nz, M, dplanes, launch, wrec, blaunch, bplanes, ki, dist);
+            k_bundle_prepare<<<blocks(m, 128), 128, 0, stream>>>(m, nz, M, dplanes, launch, wrec, blaunch, bplanes, ki, dist,
+                                                                  bki);
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             e = exact ? launch_propagate<true>(T, C, Pb, blaunch, 4 * m, Ob, stream)
                       : launch_propagate<false>(T, C, Pb, blaunch, 4 * m, Ob, stream);
@@ -304,7 +313,7 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
         }
         cudaStreamSynchronize(stream);
         for (void* q : {(void*)wrec, (void*)blaunch, (void*)bplanes, (void*)brec, (void*)ki, (void*)dist, (void*)jac,
-                        (void*)bsteps, (void*)dplanes})
+                        (void*)bsteps, (void*)dplanes, (void*)bki})
             if (q) cudaFree(q);
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_status, status, sizeof(unsigned), cudaMemcpyDeviceToHost, stream);

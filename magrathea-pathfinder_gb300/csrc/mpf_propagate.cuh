@@ -74,6 +74,9 @@ struct PropParams {
     // hom_level; exact kernel only
     int homogeneous;
     int hom_level;
+    // per-ray plane normals for the stop criterion "plane" with per-ray
+    // surfaces (n x nplanes x 3; the last one is the stop plane's), or null
+    const double* ray_ki;
 };
 
 struct PropOut {
@@ -162,8 +165,9 @@ __device__ __forceinline__ void rhs(const DevTree& T, const DevCosmo& C, const P
     out[8] = -(hub * in[8]) + (g * in[8]) - (two * (double)d.dz * in[5] * in[5]);
 }
 
-__device__ __forceinline__ double plane_q(int kind, const Rec& r)
+__device__ __forceinline__ double plane_q(int kind, const Rec& r, const double* ki = nullptr)
 {
+    if (kind == STOP_PLANE && ki) return r.x * ki[0] + r.y * ki[1] + r.z * ki[2];
     switch (kind) {
     case STOP_R: return r.chi;
     case STOP_LAMBDA: return r.lambda;
@@ -174,9 +178,9 @@ __device__ __forceinline__ double plane_q(int kind, const Rec& r)
     }
 }
 
-__device__ __forceinline__ bool plane_crossed(int kind, const Rec& r, double ref)
+__device__ __forceinline__ bool plane_crossed(int kind, const Rec& r, double ref, const double* ki = nullptr)
 {
-    return (kind == STOP_A) ? (r.a < ref) : (plane_q(kind, r) > ref);
+    return (kind == STOP_A) ? (r.a < ref) : (plane_q(kind, r, ki) > ref);
 }
 
 // Jacobian running sums at one trajectory point (S1: chi H dr, S2: chi^2 H dr).
@@ -290,7 +294,9 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
         prow[29] = prow[30] = prow[31] = 0.0;
     }
     // a surface crossed by the first point lies at firstid 0: invalid in the map driver
-    while (next_plane < np && plane_crossed(kind, b, SRC ? stop_ref : rpl[next_plane])) {
+    // this ray's plane normals (stop criterion "plane" with per-ray surfaces)
+    const double* rki = (!SRC && P.ray_ki) ? P.ray_ki + (long long)i * np * 3 : nullptr;
+    while (next_plane < np && plane_crossed(kind, b, SRC ? stop_ref : rpl[next_plane], rki ? rki + 3 * next_plane : nullptr)) {
         cross_k[next_plane] = 0;
         ++next_plane;
     }
@@ -364,13 +370,14 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
                     S.s2[q] += p.chi * p.chi * H[q];
                 }
             }
-            while (next_plane < np && plane_crossed(kind, p, SRC ? stop_ref : rpl[next_plane])) {
+            while (next_plane < np && plane_crossed(kind, p, SRC ? stop_ref : rpl[next_plane], rki ? rki + 3 * next_plane : nullptr)) {
                 const int j = next_plane++;
                 cross_k[j] = k;
                 if (prow) {
                     double* o = prow + j * rec_fields;
                     const double ref = SRC ? stop_ref : rpl[j];
-                    const double q1 = plane_q(kind, p), q0 = plane_q(kind, b);
+                    const double* kj = rki ? rki + 3 * j : nullptr;
+                    const double q1 = plane_q(kind, p, kj), q0 = plane_q(kind, b, kj);
                     const double f = (q1 - ref) / (q1 - q0);
                     const double px = b.x * f + p.x * (1 - f), py = b.y * f + p.y * (1 - f), pz = b.z * f + p.z * (1 - f);
                     const double dist = sqrt(px * px + py * py + pz * pz);
@@ -436,7 +443,11 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
         case STOP_REDSHIFT: stop = b.red > stop_ref; break;
         case STOP_T: stop = b.t > stop_ref; break;
         case STOP_A: stop = b.a < stop_ref; break;
-        case STOP_PLANE: stop = (p.x * P.ki[0] + p.y * P.ki[1] + p.z * P.ki[2]) > stop_ref; break;
+        case STOP_PLANE: {
+            const double* kk = rki ? rki + 3 * (np - 1) : P.ki;
+            stop = (p.x * kk[0] + p.y * kk[1] + p.z * kk[2]) > stop_ref;
+            break;
+        }
         case STOP_S: stop = b.s > stop_ref; break;
         default: stop = true;
         }

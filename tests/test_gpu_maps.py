@@ -44,7 +44,7 @@ def test_hmaps_fill_matches_reference_fillmap(gpu_lib, pkg, golden, order, exact
         assert np.abs(got[:, row] - ref[:, row]).max() <= 2e-6 * scale + 1e-12, row
 
 
-BUNDLES = (("sachs", "redshift"), ("normal", "r"))
+BUNDLES = (("sachs", "redshift"), ("normal", "r"), ("sachs", "plane"), ("normal", "plane"))
 OPENING = 0.2 / 60.0 * 3.141592653589793 / 180.0
 
 
