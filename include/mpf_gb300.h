@@ -166,7 +166,9 @@ typedef struct {
      * 1 = "bundle", the four-ray Lensing::dbetadtheta from the sixth ray on and
      * at convergence, with the screen normal plane_sachs (1: "sachs", 0:
      * "normal"), the stop criterion stop_bundle (an mpf_stop: redshift, r,
-     * lambda, t or a) and the opening openingmin (radians) */
+     * lambda, t, a, or plane: the plane through the ray's end point normal to
+     * the screen normal, catalogues.h:486-487) and the opening openingmin
+     * (radians) */
     int jacobian_bundle;
     int plane_sachs;
     int stop_bundle;

@@ -304,7 +304,7 @@ bool catalogue_consts(const mpf_catalogue_params* p, mpf::CatConst& K, mpf::CatR
     K.plane_sachs = p->plane_sachs ? 1 : 0;
     K.stop_bundle = p->stop_bundle;
     K.openingmin = p->openingmin;
-    if (K.bundle && (p->stop_bundle < 0 || p->stop_bundle > 4 || !(p->openingmin > 0.0) || !(p->openingmin < 1.0)))
+    if (K.bundle && (p->stop_bundle < 0 || p->stop_bundle > 5 || !(p->openingmin > 0.0) || !(p->openingmin < 1.0)))
         return false;
     if (p->rotm1)
         for (int j = 0; j < 3; ++j)

@@ -191,6 +191,7 @@ __global__ void k_cat_update(long long m, int iteration, int traced_jacobian, Ca
         case STOP_A: S.iref = scale_factor; break;
         case STOP_T: S.iref = o[9]; break;
         case STOP_LAMBDA: S.iref = o[13]; break;
+        case STOP_PLANE: S.iref = S.kx * fx + S.ky * fy + S.kz * fz; break;
         default: S.iref = S.dist; break;   // "r"
         }
         S.fx = fx; S.fy = fy; S.fz = fz; S.miss = miss;
@@ -279,7 +280,8 @@ __global__ void k_cat_jacobian(long long m, const int* __restrict__ list, const 
 // Four bundle rays per listed source (Lensing::dbetadtheta, lensing.h:160-196)
 // around its current launch direction, each with the single surface iref.
 __global__ void k_cat_bundle_rays(long long nb, const int* __restrict__ srcs, const CatState* __restrict__ state,
-                                  CatConst K, double* __restrict__ blaunch, double* __restrict__ bplanes)
+                                  CatConst K, double* __restrict__ blaunch, double* __restrict__ bplanes,
+                                  double* __restrict__ bki)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nb) return;
@@ -293,6 +295,9 @@ __global__ void k_cat_bundle_rays(long long nb, const int* __restrict__ srcs, co
     for (int r = 0; r < 4; ++r) {
         B[6 * r] = 0.0; B[6 * r + 1] = 0.0; B[6 * r + 2] = 0.0;
         bplanes[4 * k + r] = S.iref;
+        if (bki) {   // stop_bundle = "plane": the screen normal is the stop plane's normal
+            bki[12 * k + 3 * r] = S.kx; bki[12 * k + 3 * r + 1] = S.ky; bki[12 * k + 3 * r + 2] = S.kz;
+        }
     }
     B[3] = tx + to * e1x; B[4] = ty + to * e1y; B[5] = tz;
     B[9] = tx - to * e1x; B[10] = ty - to * e1y; B[11] = tz;
@@ -447,7 +452,7 @@ namespace {
 unsigned blocks(long long n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
 
 struct CatBuffers {
-    void* p[20] = {};
+    void* p[21] = {};
     ~CatBuffers()
     {
         for (void* q : p)
@@ -492,7 +497,7 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     int* pend = (int*)alloc(13, (size_t)(n + 1) * sizeof(int));
     // bundle Jacobian (jacobiantype = bundle): four rays per source in a pass
     int *plist = nullptr, *cont_src = nullptr;
-    double *blaunch = nullptr, *bplanes = nullptr, *brec = nullptr;
+    double *blaunch = nullptr, *bplanes = nullptr, *brec = nullptr, *bki = nullptr;
     long long* bsteps = nullptr;
     if (K.bundle) {
         plist = (int*)alloc(14, (size_t)n * sizeof(int));
@@ -501,6 +506,7 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
         bplanes = (double*)alloc(17, (size_t)n * 4 * sizeof(double));
         brec = (double*)alloc(18, (size_t)n * 4 * kWideFields * sizeof(double));
         bsteps = (long long*)alloc(19, (size_t)n * 4 * sizeof(long long));
+        if (K.stop_bundle == STOP_PLANE) bki = (double*)alloc(20, (size_t)n * 12 * sizeof(double));
     }
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(counters, 0, 8 * sizeof(unsigned), stream);
@@ -554,11 +560,12 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     Pb.ray_stop = nullptr;
     Pb.stop_kind = K.stop_bundle;
     Pb.ray_planes = bplanes;
+    Pb.ray_ki = bki;
     Pb.wide = 1;
     Pb.jacobian = 0;
     const PropOut Ob{bsteps, nullptr, brec, counters + 3, nullptr};
     auto bundle_pass = [&](long long nb, const int* srcs) -> cudaError_t {
-        k_cat_bundle_rays<<<blocks(nb, tpb), tpb, 0, stream>>>(nb, srcs, state, K, blaunch, bplanes);
+        k_cat_bundle_rays<<<blocks(nb, tpb), tpb, 0, stream>>>(nb, srcs, state, K, blaunch, bplanes, bki);
         cudaError_t err = cudaGetLastError();
         if (err != cudaSuccess) return err;
         stats->rays += 4 * nb;

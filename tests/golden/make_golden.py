@@ -55,9 +55,7 @@ def cone_pixels(R, nside, half_deg):
 
 
 # bundle Jacobian (jacobiantype = bundle): screen plane and stop_bundle pairs, opening 0.2 arcmin
-BUNDLES = (("sachs", "redshift"), ("normal", "r"))
-# the maps also with stop_bundle = plane (screens of normal kiTarget)
-MAP_BUNDLES = BUNDLES + (("sachs", "plane"), ("normal", "plane"))
+BUNDLES = (("sachs", "redshift"), ("normal", "r"), ("sachs", "plane"), ("normal", "plane"))
 OPENING = 0.2 / 60.0 * 3.141592653589793 / 180.0
 CAT_ACCURACIES = (1e-8, 1e-13, 0.0)   # job default; deep enough for the Jacobian steps; never met (rejects)
 CAT_VOBS = (1e-4, -2e-4, 5e-5)
@@ -132,7 +130,7 @@ def make(name, cfg):
         out["pixels"] = pix
         out["pixel_dirs"] = R.pix2vec(cfg["nside"], pix)
         out["ref_maps_o%d" % order] = R.fillmap(cfg["nside"], out["zs"], pix, "redshift", COMPONENTS, cfg["nsteps"])
-        for plane, sb in MAP_BUNDLES:
+        for plane, sb in BUNDLES:
             out["ref_maps_bundle_o%d_%s_%s" % (order, plane, sb)] = R.fillmap(
                 cfg["nside"], out["zs"], pix, "redshift", COMPONENTS, cfg["nsteps"], "bundle", plane, sb, OPENING)
         if order == 1:

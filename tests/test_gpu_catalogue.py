@@ -141,7 +141,7 @@ OPENING = 0.2 / 60.0 * 3.141592653589793 / 180.0
 
 @pytest.mark.parametrize("order", [1, 2])
 @pytest.mark.parametrize("exact", [True, False])
-@pytest.mark.parametrize("plane,stop_bundle", [("sachs", "redshift"), ("normal", "r")])
+@pytest.mark.parametrize("plane,stop_bundle", [("sachs", "redshift"), ("normal", "r"), ("sachs", "plane"), ("normal", "plane")])
 def test_catalogue_bundle_matches_reference(cat_setup, pkg, order, exact, plane, stop_bundle):
     """jacobiantype = bundle: four-ray Jacobians from the sixth ray on and at
     convergence.  The finite difference over a 0.2 arcmin screen divides ray

@@ -52,13 +52,12 @@ def test_oracle_maps_bit_exact(golden, oracle_mod, maps_mod, order):
     np.testing.assert_array_equal(maps.view(np.uint32), ref.view(np.uint32))
 
 
-BUNDLES = (("sachs", "redshift"), ("normal", "r"))
-MAP_BUNDLES = BUNDLES + (("sachs", "plane"), ("normal", "plane"))
+BUNDLES = (("sachs", "redshift"), ("normal", "r"), ("sachs", "plane"), ("normal", "plane"))
 OPENING = 0.2 / 60.0 * 3.141592653589793 / 180.0
 
 
 @pytest.mark.parametrize("order", [1, 2])
-@pytest.mark.parametrize("plane,stop_bundle", MAP_BUNDLES)
+@pytest.mark.parametrize("plane,stop_bundle", BUNDLES)
 def test_oracle_bundle_maps_bit_exact(golden, oracle_mod, maps_mod, order, plane, stop_bundle):
     """FillMap with jacobiantype = bundle (Lensing::dbetadtheta): the oracle's
     surfaces and four-ray Jacobians, assembled into maps, equal the reference's."""
