@@ -264,7 +264,9 @@ typedef struct {
     double h, omegam, lboxmpch, mpc;
     int coarseonly;            /* keep only the cells of file level ncoarse */
     int ncoarse;
-    int correction;            /* must be 1: refined values from the parents, incomplete octs completed */
+    int correction;            /* 1: refined non-normal dphidt / rho from the parents, incomplete octs
+                                  completed; 0: the parents of refined cells with a non-normal rho and
+                                  the incomplete octs coarsened (input.h:1413-1482) */
     int coarsecorrection;      /* coarse non-normal densities from their neighbours */
     int acorrection;           /* must be 0 (not supported) */
     int order;                 /* gather of the completed children: 1 CIC, 2 TSC (the reference's ORDER) */

@@ -204,9 +204,12 @@ def cells_parse(text) -> np.ndarray:
 
 def cells_build(rows, cosmology: Cosmology, cone_vertex, cone_base, cone_angle, sphere_center, sphere_radius,
                 h: float, omegam: float, lboxmpch: float, mpc: float = 3.08568e22, rotm1=None, coarseonly: bool = False,
-                ncoarse: int = 0, coarsecorrection: bool = True, order: int = 2) -> np.ndarray:
+                ncoarse: int = 0, coarsecorrection: bool = True, order: int = 2, correction: bool = True) -> np.ndarray:
     """create_octree's per-cone build (importascii + correctOctree) on the
-    device: the 48-byte cone records, sorted by key, as a uint8 array."""
+    device: the 48-byte cone records, sorted by key, as a uint8 array.
+    correction: refined cells' non-normal dphidt / rho from their parent and
+    incomplete octs completed (True), or the parents of refined cells with a
+    non-normal rho and the incomplete octs coarsened (False)."""
     L = capi.load()
     rows = np.ascontiguousarray(rows, dtype=np.float32).reshape(-1, 10)
     p = capi.CellsParams()
@@ -216,7 +219,7 @@ def cells_build(rows, cosmology: Cosmology, cone_vertex, cone_base, cone_angle, 
     rot = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64).reshape(9)
     p.rotm1 = rot.ctypes.data if rot is not None else None
     p.h, p.omegam, p.lboxmpch, p.mpc = float(h), float(omegam), float(lboxmpch), float(mpc)
-    p.coarseonly, p.ncoarse, p.correction, p.coarsecorrection = int(bool(coarseonly)), int(ncoarse), 1, int(bool(coarsecorrection))
+    p.coarseonly, p.ncoarse, p.correction, p.coarsecorrection = int(bool(coarseonly)), int(ncoarse), int(bool(correction)), int(bool(coarsecorrection))
     p.acorrection, p.order = 0, int(order)
     cap = 2 * rows.shape[0] + 64
     out = np.zeros(cap * 48, dtype=np.uint8)

@@ -336,6 +336,46 @@ __global__ void k_incomplete(long long n, const Rec48* __restrict__ r, int* flag
     flag[i] = missing > 0;
 }
 
+// correction = 0 (input.h:1417-1428): a refined cell whose rho is not normal
+// marks the cell that SimpleHyperOctree::find returns for its parent key (the
+// parent, or the nearest ancestor present); a parent that find does not
+// resolve is where the reference coarsens one past its last element, and
+// nothing is marked here
+__global__ void k_mark_parent(long long n, const Rec48* __restrict__ r, int ncoarse, int* mark)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int L = r[i].pad;
+    if (L <= ncoarse || normal_f(r[i].rho)) return;
+    uint64_t c[3];
+    key_coords(rkey(r[i]), L, c);
+    const long long p = find_containing(r, n, key_from_coords(L - 1, c[0] >> 1, c[1] >> 1, c[2] >> 1), L - 1);
+    if (p >= 0) mark[p] = 1;
+}
+
+// SimpleHyperOctree::coarsen (simplehyperoctree.h:1375-1381) of every marked
+// cell, then update's removal of the invalidated ones: coarsen invalidates the
+// run of cells after the marked one that it contains, which in key order is
+// all of its descendants, so a cell is dropped when a strict ancestor of it is
+// marked (coarsening the cells of an already invalidated run in index order
+// adds nothing).  keep[i] = 1 for the cells that stay.
+__global__ void k_coarsen(long long n, const Rec48* __restrict__ r, const int* __restrict__ mark, int ncoarse, int* keep)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int L = r[i].pad;
+    uint64_t c[3];
+    key_coords(rkey(r[i]), L, c);
+    int k = 1;
+    for (int La = L - 1; La >= ncoarse && k; --La) {
+        const int s = L - La;
+        const Key ak = key_from_coords(La, c[0] >> s, c[1] >> s, c[2] >> s);
+        const long long j = find_containing(r, n, ak, La);
+        if (j >= 0 && r[j].pad == La && mark[j]) k = 0;
+    }
+    keep[i] = k;
+}
+
 // ---- the reference's gather over a key-sorted array with appended cells ----
 // Input::correct appends the children of each incomplete oct at the end of
 // the container and gathers the next ones on that container, so the searches
@@ -634,9 +674,6 @@ extern "C" int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_par
     if (!rows || n <= 0 || !cp || !c || !count || (capacity > 0 && !records))
         return fail(MPF_BAD_INPUT, "mpf_cells_build: bad argument");
     if (cp->acorrection) return fail(MPF_BAD_INPUT, "mpf_cells_build: acorrection is not supported");
-    if (!cp->correction && cp->coarsecorrection)
-        return fail(MPF_BAD_INPUT, "mpf_cells_build: coarsecorrection without correction is not supported");
-    if (cp->correction == 0) return fail(MPF_BAD_INPUT, "mpf_cells_build: correction = 0 (coarsening) is not supported");
     if (cp->order != 1 && cp->order != 2) return fail(MPF_BAD_INPUT, "mpf_cells_build: order must be 1 or 2");
     Geometry G;
     std::memset(&G, 0, sizeof(G));
@@ -692,12 +729,29 @@ extern "C" int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_par
         k_copy_rho<<<blk(m, 256), 256, 0, s>>>(m, r1, rho0);
         k_coarse_rho<<<blk(m, 128), 128, 0, s>>>(m, r1, rho0, ncoarse);
     }
-    for (int L = ncoarse + 1; L <= nmax; ++L) k_from_parent<<<blk(m, 256), 256, 0, s>>>(m, r1, L, 0);
-    for (int L = ncoarse + 1; L <= nmax; ++L) k_from_parent<<<blk(m, 256), 256, 0, s>>>(m, r1, L, 1);
+    if (!cp->correction) {
+        // refined cells with a non-normal rho: their parents coarsened, then
+        // the incomplete octs coarsened too (input.h:1417-1428, 1472-1481)
+        int* mark = A.get<int>(m);
+        if (A.err != cudaSuccess) return fail(MPF_OUT_OF_MEMORY, "mpf_cells_build: device memory");
+        cudaMemsetAsync(mark, 0, (size_t)m * sizeof(int), s);
+        k_mark_parent<<<blk(m, 256), 256, 0, s>>>(m, r1, ncoarse, mark);
+        k_coarsen<<<blk(m, 128), 128, 0, s>>>(m, r1, mark, ncoarse, flag);
+        m = compact(A, r1, m, flag, r0, s);
+        k_incomplete<<<blk(m, 128), 128, 0, s>>>(m, r0, mark);
+        k_coarsen<<<blk(m, 128), 128, 0, s>>>(m, r0, mark, ncoarse, flag);
+        m = compact(A, r0, m, flag, r1, s);
+    } else {
+        for (int L = ncoarse + 1; L <= nmax; ++L) k_from_parent<<<blk(m, 256), 256, 0, s>>>(m, r1, L, 0);
+        for (int L = ncoarse + 1; L <= nmax; ++L) k_from_parent<<<blk(m, 256), 256, 0, s>>>(m, r1, L, 1);
+    }
     // incomplete octs: the 8 children from the gather on the octree so far
-    k_incomplete<<<blk(m, 128), 128, 0, s>>>(m, r1, flag);
-    cudaMemsetAsync(flag + m, 0, sizeof(int), s);
-    const long long ninc = exclusive_scan(flag, m + 1, s);
+    long long ninc = 0;
+    if (cp->correction) {
+        k_incomplete<<<blk(m, 128), 128, 0, s>>>(m, r1, flag);
+        cudaMemsetAsync(flag + m, 0, sizeof(int), s);
+        ninc = exclusive_scan(flag, m + 1, s);
+    }
     if (ninc > 0) {
         int* list = A.get<int>(ninc);
         Rec48* grown = A.get<Rec48>(m + 8 * ninc);

@@ -251,6 +251,12 @@ CELLS_SPEC = dict(base_level=6, box_cells=16, lbox=2048.0, half_y=2.5, half_z=2.
                   max_level=8, mass_min=3e14, mass_max=2e15, refine_cells=1.5, seed=9)
 
 
+# correction / coarsecorrection pairs of Input::correct (input.h:1398-1482)
+CELLS_CORRECTIONS = {"full": dict(correction=1, coarsecorrection=1), "nocorr": dict(correction=0, coarsecorrection=0),
+                     "nocorr_coarse": dict(correction=0, coarsecorrection=1),
+                     "corr_nocoarse": dict(correction=1, coarsecorrection=0)}
+
+
 def make_cells():
     spec = S.OctreeSpec(**CELLS_SPEC)
     rec = S.make_octree(spec)
@@ -285,7 +291,7 @@ def make_cells():
     cos = R.cosmology(celldir, pf, ef)
     for k in ("t", "a", "dadt", "d2adt2", "length"):
         out["cosmo_" + k] = cos[k]
-    for name, kw in (("full", dict(correction=1, coarsecorrection=1)), ("nocorr", dict(correction=0, coarsecorrection=0))):
+    for name, kw in CELLS_CORRECTIONS.items():
         recs, amin = R.build_cone(cellfile, cone7, sphere4, mpc=S.MPC, h=spec.cosmo.h, omegam=spec.cosmo.omega_m,
                                   lboxmpch=spec.lbox, **kw)
         out["ref_records_" + name] = recs

@@ -11,15 +11,21 @@ from conftest import load_golden
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def built(gpu_lib, pkg):
+# correction / coarsecorrection of Input::correct, as in the fixture
+CORRECTIONS = {"full": (1, 1), "nocorr": (0, 0), "nocorr_coarse": (0, 1), "corr_nocoarse": (1, 0)}
+
+
+@pytest.fixture(scope="module", params=sorted(CORRECTIONS))
+def built(request, gpu_lib, pkg):
     g = load_golden("cells")
     cos = pkg.Cosmology(g["cosmo_t"], g["cosmo_a"], g["cosmo_dadt"], g["cosmo_d2adt2"])
     rows = pkg.cells_parse(str(g["cells_text"]))
     c7, s4 = g["cone7"], g["sphere4"]
+    corr, coarse = CORRECTIONS[request.param]
     rec = pkg.cells_build(rows, cos, c7[:3], c7[3:6], c7[6], s4[:3], s4[3], float(g["h"]), float(g["omegam"]),
-                          float(g["lboxmpch"]), float(g["mpc"]), order=2)
-    yield g, rec
+                          float(g["lboxmpch"]), float(g["mpc"]), order=2, correction=bool(corr),
+                          coarsecorrection=bool(coarse))
+    yield g, rec, g["ref_records_" + request.param]
     cos.close()
 
 
@@ -29,8 +35,8 @@ def _fields(b):
 
 
 def test_same_cells_and_keys(built):
-    g, rec = built
-    got, ref = _fields(rec), _fields(g["ref_records_full"])
+    g, rec, ref = built
+    got, ref = _fields(rec), _fields(ref)
     assert got.shape == ref.shape, (got.shape, ref.shape)
     np.testing.assert_array_equal(got["hi"], ref["hi"])
     np.testing.assert_array_equal(got["lo"], ref["lo"])
@@ -43,8 +49,8 @@ def test_records_bit_exact(built):
     unsorted tail returns 0 (simplehyperoctree.h:1487-1488, 1510-1518), and
     here gives a denormal scale factor; such a record is the one allowed to
     differ."""
-    g, rec = built
-    got, ref = _fields(rec), _fields(g["ref_records_full"])
+    g, rec, ref = built
+    got, ref = _fields(rec), _fields(ref)
     undefined = np.abs(ref["a"]) < 1e-30
     assert undefined.sum() <= 1
     bad = {}
@@ -57,7 +63,7 @@ def test_records_bit_exact(built):
 
 def test_built_octree_propagates(built, pkg):
     """The built records are a valid cone octree for the propagation path."""
-    g, rec = built
+    g, rec, _ = built
     tree = pkg.Octree.from_records(np.frombuffer(rec.tobytes(), dtype=_fields(rec).dtype))
     assert tree.info["cells"] == rec.shape[0] // 48
     tree.close()
