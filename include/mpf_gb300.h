@@ -268,8 +268,12 @@ typedef struct {
                                   completed; 0: the parents of refined cells with a non-normal rho and
                                   the incomplete octs coarsened (input.h:1413-1482) */
     int coarsecorrection;      /* coarse non-normal densities from their neighbours */
-    int acorrection;           /* must be 0 (not supported) */
+    int acorrection;           /* 1: each cell's a snapped to the next lower value of the table of the
+                                  cells' distinct scale factors, extended one shell below (Full Universe
+                                  Run outputs, input.h:1485-1506) */
     int order;                 /* gather of the completed children: 1 CIC, 2 TSC (the reference's ORDER) */
+    double* amin;              /* acorrection: receives the table's first value (Input::correct's amin);
+                                  may be NULL, left unchanged otherwise */
 } mpf_cells_params;
 
 /* Create_octree::PreparationASCII's per-cone body (src/create_octree.h:544-580):

@@ -204,12 +204,15 @@ def cells_parse(text) -> np.ndarray:
 
 def cells_build(rows, cosmology: Cosmology, cone_vertex, cone_base, cone_angle, sphere_center, sphere_radius,
                 h: float, omegam: float, lboxmpch: float, mpc: float = 3.08568e22, rotm1=None, coarseonly: bool = False,
-                ncoarse: int = 0, coarsecorrection: bool = True, order: int = 2, correction: bool = True) -> np.ndarray:
+                ncoarse: int = 0, coarsecorrection: bool = True, order: int = 2, correction: bool = True,
+                acorrection: bool = False):
     """create_octree's per-cone build (importascii + correctOctree) on the
     device: the 48-byte cone records, sorted by key, as a uint8 array.
     correction: refined cells' non-normal dphidt / rho from their parent and
     incomplete octs completed (True), or the parents of refined cells with a
-    non-normal rho and the incomplete octs coarsened (False)."""
+    non-normal rho and the incomplete octs coarsened (False).  acorrection:
+    the scale factors snapped to their table (Full Universe Run); then the
+    result is (records, amin)."""
     L = capi.load()
     rows = np.ascontiguousarray(rows, dtype=np.float32).reshape(-1, 10)
     p = capi.CellsParams()
@@ -220,12 +223,14 @@ def cells_build(rows, cosmology: Cosmology, cone_vertex, cone_base, cone_angle, 
     p.rotm1 = rot.ctypes.data if rot is not None else None
     p.h, p.omegam, p.lboxmpch, p.mpc = float(h), float(omegam), float(lboxmpch), float(mpc)
     p.coarseonly, p.ncoarse, p.correction, p.coarsecorrection = int(bool(coarseonly)), int(ncoarse), int(bool(correction)), int(bool(coarsecorrection))
-    p.acorrection, p.order = 0, int(order)
+    amin = np.zeros(1)
+    p.acorrection, p.order, p.amin = int(bool(acorrection)), int(order), amin.ctypes.data
     cap = 2 * rows.shape[0] + 64
     out = np.zeros(cap * 48, dtype=np.uint8)
     n = C.c_int64()
     capi.check(L.mpf_cells_build(capi.ptr(rows), rows.shape[0], C.byref(p), cosmology._h, capi.ptr(out), cap, C.byref(n)))
-    return out[:48 * n.value].copy()
+    rec = out[:48 * n.value].copy()
+    return (rec, float(amin[0])) if acorrection else rec
 
 
 def catalogue(octree: Octree, cosmology: Cosmology, sources, length: float, h: float, mpc: float = 3.08568e22,

@@ -4,8 +4,8 @@ Compiles each CUDA translation unit with nvcc in parallel and links a shared
 library next to this file.  The reference-order translation unit, the
 catalogue root-finder, the map rows and the ray bundles are built with
 -fmad=false so their float64 arithmetic keeps the reference's rounding (the
-bundles' host code also without FMA contraction); the others keep FMA
-contraction.
+bundles' and the cell build's host code also without FMA contraction); the
+others keep FMA contraction.
 """
 from __future__ import annotations
 
@@ -31,7 +31,7 @@ UNITS = [
     ("mpf_maps.cu", ["-fmad=false"]),
     ("mpf_surrogate.cu", []),
     ("mpf_rays.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
-    ("mpf_build.cu", ["-fmad=false"]),
+    ("mpf_build.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
 ]
 
 

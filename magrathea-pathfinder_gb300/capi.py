@@ -78,7 +78,7 @@ class CellsParams(C.Structure):
                 ("sphere_center", C.c_double * 3), ("sphere_radius", C.c_double), ("rotm1", C.c_void_p),
                 ("h", C.c_double), ("omegam", C.c_double), ("lboxmpch", C.c_double), ("mpc", C.c_double),
                 ("coarseonly", C.c_int), ("ncoarse", C.c_int), ("correction", C.c_int), ("coarsecorrection", C.c_int),
-                ("acorrection", C.c_int), ("order", C.c_int)]
+                ("acorrection", C.c_int), ("order", C.c_int), ("amin", C.c_void_p)]
 
 
 class BundleParams(C.Structure):

@@ -15,11 +15,17 @@
 //       neighbours, refined dphidt / rho from the parent level by level,
 //       incomplete octs completed from the gather at the children's centres
 //       (k_complete_serial: one thread, the reference's sequential appends)
+//       or, with correction = 0, the coarsening of the parents of refined
+//       cells with a non-normal density and of the incomplete octs;
+//       acorrection: the scale factors snapped to the next lower one of
+//       their table, extended one shell below by a forward derivative
 //   correctOctree (miscellaneous.h:467-479) dphidt *= da/dt(a)
 //
 // Float32 data arithmetic follows the reference's types (Gravity<float, 3>,
-// Real = float in importascii); the unit is compiled with -fmad=false.
+// Real = float in importascii); the unit is compiled with -fmad=false and
+// its host code without FMA contraction.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -592,6 +598,52 @@ __device__ __forceinline__ float interpolate2(float x0, const double* x, const d
     return (n > 0) ? (float)y[0] : 0.f;
 }
 
+// acorrection (input.h:1485-1506), the Full Universe Run scale-factor
+// snapping.  The cells' scale factors as sortable 32-bit keys (non-negative
+// floats order as their bit patterns); the values the reference drops from its
+// table (sign bit set, or not normal) get 0xffffffff and sort last.
+__global__ void k_a_keys(long long n, const Rec48* __restrict__ r, unsigned long long* hi, unsigned long long* lo, int* idx)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float a = r[i].a;
+    hi[i] = 0ull;
+    lo[i] = (!signbit(a) && normal_f(a)) ? (unsigned long long)__float_as_uint(a) : 0xffffffffull;
+    idx[i] = (int)i;
+}
+
+// the first of each run of equal sorted keys, the dropped values excluded
+__global__ void k_a_unique(long long n, const unsigned long long* __restrict__ lo, int* flag)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flag[i] = (lo[i] != 0xffffffffull && (i == 0 || lo[i] != lo[i - 1])) ? 1 : 0;
+}
+
+__global__ void k_a_select(long long n, const unsigned long long* __restrict__ lo, const int* __restrict__ scan, float* table)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (scan[i + 1] > scan[i]) table[scan[i]] = __uint_as_float((unsigned)lo[i]);
+}
+
+// each cell's a becomes the table's value below it, *(lower_bound(a) - 1);
+// a cell whose a is the table's first value or was dropped from the table
+// reads before the table in the reference (undefined) and keeps its a here
+__global__ void k_a_snap(long long n, Rec48* r, const float* __restrict__ table, int T)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float a = r[i].a;
+    int lo = 0, hi = T;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (table[mid] < a) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo > 0) r[i].a = table[lo - 1];
+}
+
 __global__ void k_dphidt(long long n, Rec48* r, const double* __restrict__ ca, const double* __restrict__ cdadt, long long nc)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -628,6 +680,32 @@ struct Arena {
     }
 };
 
+// Utility::interpolate (utility.h:440-447) over float tables: upper_bound,
+// then the bracketing segment, clamped to the end segments
+float interpolate_f(float x0, const std::vector<float>& x, const std::vector<float>& y)
+{
+    const long long n = (long long)std::min(x.size(), y.size());
+    long long i = std::upper_bound(x.begin(), x.begin() + n, x0) - x.begin();
+    i += (n > 1) * ((i <= 0) - (i >= n));
+    return (n > 1) ? (y[i - 1] + ((y[i] - y[i - 1]) * (x0 - x[i - 1]) / (x[i] - x[i - 1]))) : ((n > 0) ? y[0] : 0.f);
+}
+
+// Utility::differentiate<1> (utility.h:527-551) with neighbourhood 1: the
+// nine-point one-sided (forward) finite-difference weights of Fornberg's
+// method, step = the abscissae's spacing at x0, in float
+float forward_derivative_f(float x0, const std::vector<float>& x, const std::vector<float>& y)
+{
+    const float w[9] = {-761.f / 280.f, 8.f, -14.f, 56.f / 3.f, -35.f / 2.f, 56.f / 5.f, -14.f / 3.f, 8.f / 7.f, -1.f / 8.f};
+    const long long n = (long long)std::min(x.size(), y.size());
+    const long long i = std::upper_bound(x.begin(), x.begin() + n, x0) - x.begin();
+    const long long j = i + ((n > 1) * ((i <= 0) - (i >= n)));
+    const float h = (n > 1) ? ((x[j] - x[j - 1]) * 1u) : 0.f;
+    float result = 0.f;
+    if (n > 1)
+        for (int k = 0; k < 9; ++k) result += w[8 - k] * interpolate_f(x0 + (float)(8 - k) * h, x, y);
+    return result / h;
+}
+
 // compact `in` (n records) by flag into out; returns the count
 long long compact(Arena& A, const Rec48* in, long long n, int* flag, Rec48* out, cudaStream_t s)
 {
@@ -658,6 +736,57 @@ void sort_records(Arena& A, const Rec48* in, long long n, Rec48* out, cudaStream
     k_gather<<<blk(n, 256), 256, 0, s>>>(n, in, idx, out);
 }
 
+// Input::correct's acorrection over the n records of r as the container
+// holds them then (appended or invalidated cells included): the table of
+// the distinct scale factors (sorted on the device), one shell below it
+// extrapolated against the table's index (1, 2, ...) when that gives a
+// positive normal value below the first, then every cell's a snapped to the
+// table value below it.  amin: the table's first value.
+cudaError_t acorrect(Arena& A, Rec48* r, long long n, double* amin, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    // the table of the cells' distinct scale factors, sorted on the device
+    unsigned long long *hi = A.get<unsigned long long>(n), *lo = A.get<unsigned long long>(n);
+    unsigned long long *hi2 = A.get<unsigned long long>(n), *lo2 = A.get<unsigned long long>(n);
+    int *idx = A.get<int>(n), *idx2 = A.get<int>(n), *uflag = A.get<int>(n + 1);
+    float* dtable = A.get<float>(n + 1);
+    const long long ntiles = (n + kTile - 1) / kTile;
+    int* hist = A.get<int>((size_t)16 * ntiles + 1);
+    if (A.err != cudaSuccess) return A.err;
+    k_a_keys<<<blk(n, 256), 256, 0, s>>>(n, r, hi, lo, idx);
+    for (int pass = 0; pass < 8; ++pass) {
+        k_hist<<<blk(ntiles, 128), 128, 0, s>>>(n, hi, lo, pass, hist, ntiles);
+        exclusive_scan(hist, 16 * ntiles, s);
+        k_scatter<<<blk(ntiles, 128), 128, 0, s>>>(n, hi, lo, idx, pass, hist, ntiles, hi2, lo2, idx2);
+        std::swap(hi, hi2);
+        std::swap(lo, lo2);
+        std::swap(idx, idx2);
+    }
+    k_a_unique<<<blk(n, 256), 256, 0, s>>>(n, lo, uflag);
+    cudaMemsetAsync(uflag + n, 0, sizeof(int), s);
+    const long long asize = exclusive_scan(uflag, n + 1, s);
+    k_a_select<<<blk(n, 256), 256, 0, s>>>(n, lo, uflag, dtable);
+    std::vector<float> table((size_t)asize);
+    cudaError_t e = cudaSuccess;
+    if (asize > 0) e = cudaMemcpy(table.data(), dtable, (size_t)asize * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    // one shell below the first, extrapolated from the table against its
+    // index (1, 2, ...) when that gives a positive normal value below it
+    if (asize > 1) {
+        std::vector<float> index((size_t)asize);
+        for (long long k = 0; k < asize; ++k) index[(size_t)k] = (float)(k + 1);
+        const float below = table[0] - forward_derivative_f(0.f, index, table);
+        if (!std::signbit(below) && std::isnormal(below) && below < table[0]) table.insert(table.begin(), below);
+    }
+    if (!table.empty()) {
+        e = cudaMemcpy(dtable, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return e;
+        k_a_snap<<<blk(n, 256), 256, 0, s>>>(n, r, dtable, (int)table.size());
+        if (amin) *amin = (double)table[0];
+    }
+    return cudaGetLastError();
+}
+
 // SimpleHyperOctree::update on device records: sort, collapse, compact
 long long update(Arena& A, Rec48* r, long long n, Rec48* tmp, int* flag, cudaStream_t s)
 {
@@ -673,7 +802,6 @@ extern "C" int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_par
 {
     if (!rows || n <= 0 || !cp || !c || !count || (capacity > 0 && !records))
         return fail(MPF_BAD_INPUT, "mpf_cells_build: bad argument");
-    if (cp->acorrection) return fail(MPF_BAD_INPUT, "mpf_cells_build: acorrection is not supported");
     if (cp->order != 1 && cp->order != 2) return fail(MPF_BAD_INPUT, "mpf_cells_build: order must be 1 or 2");
     Geometry G;
     std::memset(&G, 0, sizeof(G));
@@ -740,6 +868,9 @@ extern "C" int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_par
         m = compact(A, r1, m, flag, r0, s);
         k_incomplete<<<blk(m, 128), 128, 0, s>>>(m, r0, mark);
         k_coarsen<<<blk(m, 128), 128, 0, s>>>(m, r0, mark, ncoarse, flag);
+        // the invalidated cells stay in the container until the final update
+        if (cp->acorrection && (e = acorrect(A, r0, m, cp->amin, s)) != cudaSuccess)
+            return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
         m = compact(A, r0, m, flag, r1, s);
     } else {
         for (int L = ncoarse + 1; L <= nmax; ++L) k_from_parent<<<blk(m, 256), 256, 0, s>>>(m, r1, L, 0);
@@ -768,9 +899,14 @@ extern "C" int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_par
         k_complete_serial<<<1, 1, 0, s>>>(grown, m, list, ninc, cp->order);
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
+        // acorrection runs on the container with its appended children, before the final update
+        if (cp->acorrection && (e = acorrect(A, grown, m + 8 * ninc, cp->amin, s)) != cudaSuccess)
+            return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
         m = update(A, grown, m + 8 * ninc, tmp, flag2, s);
         if (A.err != cudaSuccess || m < 0) return fail(MPF_OUT_OF_MEMORY, "mpf_cells_build: device memory");
         r1 = grown;
+    } else if (cp->correction && cp->acorrection && (e = acorrect(A, r1, m, cp->amin, s)) != cudaSuccess) {
+        return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
     }
     // dphidt *= da/dt at the cell's a
     k_dphidt<<<blk(m, 256), 256, 0, s>>>(m, r1, c->a, c->dadt, c->n);

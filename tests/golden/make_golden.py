@@ -254,7 +254,9 @@ CELLS_SPEC = dict(base_level=6, box_cells=16, lbox=2048.0, half_y=2.5, half_z=2.
 # correction / coarsecorrection pairs of Input::correct (input.h:1398-1482)
 CELLS_CORRECTIONS = {"full": dict(correction=1, coarsecorrection=1), "nocorr": dict(correction=0, coarsecorrection=0),
                      "nocorr_coarse": dict(correction=0, coarsecorrection=1),
-                     "corr_nocoarse": dict(correction=1, coarsecorrection=0)}
+                     "corr_nocoarse": dict(correction=1, coarsecorrection=0),
+                     "acorr": dict(correction=1, coarsecorrection=1, acorrection=1),
+                     "nocorr_acorr": dict(correction=0, coarsecorrection=0, acorrection=1)}
 
 
 def make_cells():
