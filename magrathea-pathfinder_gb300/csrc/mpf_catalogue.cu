@@ -121,7 +121,12 @@ __global__ void k_cat_init(long long n, const double* __restrict__ src, int stri
     r[1] = S.theta;
     val[i] = (int)i;
     if (S.dist > 0.0 && isfinite(S.dist) && isfinite(S.phi) && isfinite(S.theta)) {
-        key[i] = direction_key(S.phi, S.theta) & 0x7fffffffu;   // below the key of the excluded sources
+        // farthest sources first, in 1/8-octave radius bins (the float's
+        // exponent and 3 mantissa bits), then by direction: a warp's rays have
+        // about the same length, and the persistent queue starts the long ones
+        // first; below the key of the excluded sources
+        const uint32_t rbin = __float_as_uint((float)S.dist) >> 20;
+        key[i] = ((0x7ffu - min(rbin, 0x7ffu)) << 20) | (direction_key(S.phi, S.theta) >> 12);
         atomicAdd(count, 1u);
     } else {
         key[i] = 0xffffffffu;
@@ -518,7 +523,7 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     k_cat_init<<<blocks(n, tpb), tpb, 0, stream>>>(n, d_src, stride, R, rot ? 1 : 0, state, d_rows, key0, act0, counters);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     stats->launches = 1;
-    // sources in direction order; the unreachable ones (key 0xffffffff) sort last
+    // sources in radius-bin and direction order; the unreachable ones (key 0xffffffff) sort last
     {
         uint32_t *ka = key0, *kb = key1;
         int *va = act0, *vb = act1;
@@ -538,7 +543,7 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     if ((e = cudaMemcpyAsync(&m, counters, sizeof(unsigned), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
     const unsigned m_valid = m;
-    // act0 keeps the valid sources in direction order (for the re-trace); the
+    // act0 keeps the valid sources in that order (for the re-trace); the
     // rounds compact between act1 and the key buffer, free after the sort
     int* sorted = act0;
     int* cur = act1;
@@ -607,7 +612,7 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
         std::swap(cur, nxt);
     }
     // Jacobian of the sources that converged in the identity-Jacobian rounds,
-    // re-traced in direction order
+    // re-traced in radius-bin and direction order
     k_list_flags<<<blocks((long long)m_valid + 1, tpb), tpb, 0, stream>>>(m_valid, sorted, rflag, scan);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int64_t r = exclusive_scan(scan, (int64_t)m_valid + 1, stream);
