@@ -579,8 +579,11 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
                      : launch_propagate<false>(T, Cs, Pb, blaunch, 4 * nb, Ob, stream);
     };
     for (int it = 0; it <= K.max_iterations && m > 0; ++it) {
-        // the infinitesimal Jacobian serves rounds 3 and up, or 3 and 4 before the bundle rounds
-        const int jac = (it >= 3 && !(K.bundle && it >= 5)) ? 1 : 0;
+        // the infinitesimal Jacobian serves the Newton steps of rounds 3 and up
+        // (3 and 4 before the bundle rounds); round 2 traces it too, so that
+        // the sources converging there (most of them) need no re-trace for
+        // their final Jacobian
+        const int jac = K.bundle ? ((it >= 3 && it < 5) ? 1 : 0) : ((it >= 2) ? 1 : 0);
         P.jacobian = jac;
         k_cat_rays<<<blocks(m, tpb), tpb, 0, stream>>>(m, cur, state, launch, radius);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -611,7 +614,7 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
         m = (unsigned)next_m;
         std::swap(cur, nxt);
     }
-    // Jacobian of the sources that converged in the identity-Jacobian rounds,
+    // Jacobian of the sources that converged in rounds traced without it,
     // re-traced in radius-bin and direction order
     k_list_flags<<<blocks((long long)m_valid + 1, tpb), tpb, 0, stream>>>(m_valid, sorted, rflag, scan);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
