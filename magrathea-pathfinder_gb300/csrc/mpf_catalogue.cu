@@ -585,10 +585,32 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
         // their final Jacobian
         const int jac = K.bundle ? ((it >= 3 && it < 5) ? 1 : 0) : ((it >= 2) ? 1 : 0);
         P.jacobian = jac;
-        k_cat_rays<<<blocks(m, tpb), tpb, 0, stream>>>(m, cur, state, launch, radius);
+        // round 2 also re-traces, with the Jacobian, the sources that converged
+        // in rounds 0 and 1 (appended after the active ones): their final
+        // Jacobian then costs no launch of its own at the end
+        long long nre = 0;
+        if (it == 2 && !K.bundle) {
+            k_list_flags<<<blocks((long long)m_valid + 1, tpb), tpb, 0, stream>>>(m_valid, sorted, rflag, scan);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            nre = exclusive_scan(scan, (int64_t)m_valid + 1, stream);
+            if (nre > 0) {
+                k_compact<<<blocks(m_valid, tpb), tpb, 0, stream>>>(m_valid, sorted, scan, cur + m);
+                if ((e = cudaMemsetAsync(rflag, 0, (size_t)n * sizeof(int), stream)) != cudaSuccess) return e;
+            }
+            stats->launches += 2;
+        }
+        const long long mt = (long long)m + nre;
+        k_cat_rays<<<blocks(mt, tpb), tpb, 0, stream>>>(mt, cur, state, launch, radius);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        e = exact ? launch_propagate<true>(T, Cs, P, launch, m, O, stream) : launch_propagate<false>(T, Cs, P, launch, m, O, stream);
+        e = exact ? launch_propagate<true>(T, Cs, P, launch, mt, O, stream) : launch_propagate<false>(T, Cs, P, launch, mt, O, stream);
         if (e != cudaSuccess) return e;
+        if (nre > 0) {
+            k_cat_jacobian<<<blocks(nre, tpb), tpb, 0, stream>>>(nre, cur + m, rec + (long long)kSourceFields * m, steps + m,
+                                                                  d_rows, psteps);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            stats->rays += nre;
+            stats->launches += 1;
+        }
         k_cat_update<<<blocks(m + 1, tpb), tpb, 0, stream>>>(m, it, jac, K, cur, state, d_rows, steps, rec, scan, rflag,
                                                               pend, psteps);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
