@@ -398,7 +398,9 @@ def main():
                     help="propagate = the headline ray-tracing benchmark; catalogue = the Newton root-finder; "
                          "surrogate = the learned field in the RK4 stages against the plain octree")
     ap.add_argument("--surrogate-samples", type=float, default=50e6, help="training samples of the surrogate")
-    ap.add_argument("--sources", type=int, default=65536, help="catalogue sources per step")
+    ap.add_argument("--sources", type=int, default=262144,
+                    help="catalogue sources per step (a call's rounds wait for its slowest sources, whose up to 11 "
+                         "sequential rays cross halo cores; 2^18 sources amortise that chain)")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     synth = importlib.import_module(PKG + ".synth")
