@@ -27,6 +27,27 @@ static void launch_fast_kernel(long long grid, int tpb, const DevTree& T, const 
     }
 }
 
+// Launch shape of the persistent kernel.  A batch that fills every SM's
+// warp slots runs as blocks of kFastThreads, as many as are resident.  A
+// smaller one (the catalogue's last Newton rounds, small ray batches) runs as
+// one-warp blocks, one per 32 rays, so that the block scheduler spreads its
+// warps over the SMs instead of packing four to an SM: each warp then has an
+// SM's FP64 pipe and load slots to itself and its rays finish sooner.
+// The kernel's shared-memory layout is sized for kFastThreads and takes any
+// smaller block.
+static int fast_launch_shape(long long n, int blocks_per_sm, int sms, long long* grid)
+{
+    const long long warps = (n + 31) / 32;
+    const long long slots = (long long)blocks_per_sm * sms * (kFastThreads / 32);
+    if (warps < slots) {
+        *grid = warps;
+        return 32;
+    }
+    const long long need = (n + kFastThreads - 1) / kFastThreads;
+    *grid = std::min<long long>(need, (long long)blocks_per_sm * sms);
+    return kFastThreads;
+}
+
 template <>
 cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* d_launch, long long n,
                                     const PropOut& O, cudaStream_t stream)
@@ -46,8 +67,8 @@ cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const P
     }
     cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
-    const long long need = (n + tpb - 1) / tpb;
-    const long long grid = std::min<long long>(need, (long long)blocks_per_sm * sms);
+    long long grid = 0;
+    const int tpb_used = fast_launch_shape(n, blocks_per_sm, sms, &grid);
     // MPF_STATS=1: count record-path gathers and slow-path fallbacks (diagnostics; serialises the call)
     static const bool want_stats = getenv("MPF_STATS") != nullptr;
     PropOut o2 = O;
@@ -56,7 +77,7 @@ cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const P
         cudaMemsetAsync(dstats, 0, ST_N * sizeof(unsigned long long), stream);
         o2.stats = dstats;
     }
-    launch_fast_kernel(grid, tpb, T, C, P, d_launch, n, o2, queue, stream);
+    launch_fast_kernel(grid, tpb_used, T, C, P, d_launch, n, o2, queue, stream);
     e = cudaGetLastError();
     if (dstats) {
         unsigned long long h[ST_N];
@@ -95,9 +116,9 @@ cudaError_t launch_propagate_fast_with_queue(const DevTree& T, const DevCosmo& C
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     if (blocks_per_sm < 1) blocks_per_sm = 1;
-    const long long need = (n + tpb - 1) / tpb;
-    const long long grid = std::min<long long>(need, (long long)blocks_per_sm * sms);
-    launch_fast_kernel(grid, tpb, T, C, P, d_launch, n, O, queue, stream);
+    long long grid = 0;
+    const int tpb_used = fast_launch_shape(n, blocks_per_sm, sms, &grid);
+    launch_fast_kernel(grid, tpb_used, T, C, P, d_launch, n, O, queue, stream);
     return cudaGetLastError();
 }
 }  // namespace mpf
