@@ -228,7 +228,12 @@ def cells_build(rows, cosmology: Cosmology, cone_vertex, cone_base, cone_angle, 
     cap = 2 * rows.shape[0] + 64
     out = np.zeros(cap * 48, dtype=np.uint8)
     n = C.c_int64()
-    capi.check(L.mpf_cells_build(capi.ptr(rows), rows.shape[0], C.byref(p), cosmology._h, capi.ptr(out), cap, C.byref(n)))
+    rc = L.mpf_cells_build(capi.ptr(rows), rows.shape[0], C.byref(p), cosmology._h, capi.ptr(out), cap, C.byref(n))
+    if rc == -1 and n.value > cap:   # MPF_BAD_INPUT: more cells than the first guess; build again at the size
+        cap = n.value
+        out = np.zeros(cap * 48, dtype=np.uint8)
+        rc = L.mpf_cells_build(capi.ptr(rows), rows.shape[0], C.byref(p), cosmology._h, capi.ptr(out), cap, C.byref(n))
+    capi.check(rc)
     rec = out[:48 * n.value].copy()
     return (rec, float(amin[0])) if acorrection else rec
 

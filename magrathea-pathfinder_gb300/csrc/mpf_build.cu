@@ -800,9 +800,13 @@ long long update(Arena& A, Rec48* r, long long n, Rec48* tmp, int* flag, cudaStr
 extern "C" int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_params* cp, const mpf_cosmology* c, void* records,
                                int64_t capacity, int64_t* count)
 {
-    if (!rows || n <= 0 || !cp || !c || !count || (capacity > 0 && !records))
+    if ((n > 0 && !rows) || n < 0 || !cp || !c || !count || (capacity > 0 && !records))
         return fail(MPF_BAD_INPUT, "mpf_cells_build: bad argument");
     if (cp->order != 1 && cp->order != 2) return fail(MPF_BAD_INPUT, "mpf_cells_build: order must be 1 or 2");
+    if (n == 0) {   // no cell files for this cone: an empty octree, as the reference saves it
+        *count = 0;
+        return MPF_OK;
+    }
     Geometry G;
     std::memset(&G, 0, sizeof(G));
     for (int d = 0; d < 3; ++d) {

@@ -256,7 +256,9 @@ CELLS_CORRECTIONS = {"full": dict(correction=1, coarsecorrection=1), "nocorr": d
                      "nocorr_coarse": dict(correction=0, coarsecorrection=1),
                      "corr_nocoarse": dict(correction=1, coarsecorrection=0),
                      "acorr": dict(correction=1, coarsecorrection=1, acorrection=1),
-                     "nocorr_acorr": dict(correction=0, coarsecorrection=0, acorrection=1)}
+                     "nocorr_acorr": dict(correction=0, coarsecorrection=0, acorrection=1),
+                     # the reference built with ORDER=1: CIC gathers for the completed children
+                     "full_o1": dict(correction=1, coarsecorrection=1, order=1)}
 
 
 def make_cells():
@@ -293,9 +295,15 @@ def make_cells():
     cos = R.cosmology(celldir, pf, ef)
     for k in ("t", "a", "dadt", "d2adt2", "length"):
         out["cosmo_" + k] = cos[k]
+    refs = {2: R}
     for name, kw in CELLS_CORRECTIONS.items():
-        recs, amin = R.build_cone(cellfile, cone7, sphere4, mpc=S.MPC, h=spec.cosmo.h, omegam=spec.cosmo.omega_m,
-                                  lboxmpch=spec.lbox, **kw)
+        kw = dict(kw)
+        order = kw.pop("order", 2)
+        if order not in refs:
+            refs[order] = Reference(order)
+            refs[order].cosmology(celldir, pf, ef)
+        recs, amin = refs[order].build_cone(cellfile, cone7, sphere4, mpc=S.MPC, h=spec.cosmo.h,
+                                            omegam=spec.cosmo.omega_m, lboxmpch=spec.lbox, **kw)
         out["ref_records_" + name] = recs
         out["ref_amin_" + name] = amin
         print("cells %s: %d rows in, %d cells out" % (name, allrows.shape[0], recs.shape[0] // 48))

@@ -11,9 +11,10 @@ from conftest import load_golden
 pytestmark = pytest.mark.gpu
 
 
-# correction / coarsecorrection / acorrection of Input::correct, as in the fixture
-CORRECTIONS = {"full": (1, 1, 0), "nocorr": (0, 0, 0), "nocorr_coarse": (0, 1, 0), "corr_nocoarse": (1, 0, 0),
-               "acorr": (1, 1, 1), "nocorr_acorr": (0, 0, 1)}
+# correction / coarsecorrection / acorrection of Input::correct and the
+# gather order of the completed children, as in the fixture
+CORRECTIONS = {"full": (1, 1, 0, 2), "nocorr": (0, 0, 0, 2), "nocorr_coarse": (0, 1, 0, 2), "corr_nocoarse": (1, 0, 0, 2),
+               "acorr": (1, 1, 1, 2), "nocorr_acorr": (0, 0, 1, 2), "full_o1": (1, 1, 0, 1)}
 
 
 @pytest.fixture(scope="module", params=sorted(CORRECTIONS))
@@ -22,9 +23,9 @@ def built(request, gpu_lib, pkg):
     cos = pkg.Cosmology(g["cosmo_t"], g["cosmo_a"], g["cosmo_dadt"], g["cosmo_d2adt2"])
     rows = pkg.cells_parse(str(g["cells_text"]))
     c7, s4 = g["cone7"], g["sphere4"]
-    corr, coarse, acorr = CORRECTIONS[request.param]
+    corr, coarse, acorr, order = CORRECTIONS[request.param]
     rec = pkg.cells_build(rows, cos, c7[:3], c7[3:6], c7[6], s4[:3], s4[3], float(g["h"]), float(g["omegam"]),
-                          float(g["lboxmpch"]), float(g["mpc"]), order=2, correction=bool(corr),
+                          float(g["lboxmpch"]), float(g["mpc"]), order=order, correction=bool(corr),
                           coarsecorrection=bool(coarse), acorrection=bool(acorr))
     if acorr:
         rec, amin = rec
@@ -73,3 +74,21 @@ def test_built_octree_propagates(built, pkg):
     tree = pkg.Octree.from_records(np.frombuffer(rec.tobytes(), dtype=_fields(rec).dtype))
     assert tree.info["cells"] == rec.shape[0] // 48
     tree.close()
+
+
+def test_empty_and_filtered_inputs(gpu_lib, pkg):
+    """No rows, and rows that all fall outside the cone: an empty octree (the
+    reference saves an empty cone file); a bad order is rejected."""
+    g = load_golden("cells")
+    cos = pkg.Cosmology(g["cosmo_t"], g["cosmo_a"], g["cosmo_dadt"], g["cosmo_d2adt2"])
+    c7, s4 = g["cone7"], g["sphere4"]
+    args = (c7[:3], c7[3:6], c7[6], s4[:3], s4[3], float(g["h"]), float(g["omegam"]), float(g["lboxmpch"]),
+            float(g["mpc"]))
+    assert pkg.cells_build(np.zeros((0, 10), dtype=np.float32), cos, *args).shape == (0,)
+    rows = pkg.cells_parse(str(g["cells_text"]))
+    far = rows.copy()
+    far[:, 1:4] = -1.9                     # every cell behind the observer, outside the microsphere
+    assert pkg.cells_build(far, cos, *args).shape == (0,)
+    with pytest.raises(RuntimeError):
+        pkg.cells_build(rows, cos, *args, order=3)
+    cos.close()
