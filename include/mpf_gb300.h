@@ -28,7 +28,8 @@ typedef enum {
     MPF_CUDA_ERROR = -3,
     MPF_NOT_SORTED = -4,         /* cone records must be sorted by key */
     MPF_NO_DEVICE = -5,
-    MPF_IO_ERROR = -6
+    MPF_IO_ERROR = -6,
+    MPF_DEVICE_TIMEOUT = -7      /* a bounded device wait ran out; the context stays usable */
 } mpf_status;
 
 typedef enum {                    /* stop_ray / stop criterion, src/integrator.h:779-811 */

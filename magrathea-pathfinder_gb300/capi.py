@@ -18,7 +18,7 @@ MPF_PLANE_FIELDS = 20
 MPF_MAX_PLANES = 16
 
 STATUS = {0: "MPF_OK", 1: "MPF_WARN_MAX_STEPS", -1: "MPF_BAD_INPUT", -2: "MPF_OUT_OF_MEMORY", -3: "MPF_CUDA_ERROR",
-          -4: "MPF_NOT_SORTED", -5: "MPF_NO_DEVICE", -6: "MPF_IO_ERROR"}
+          -4: "MPF_NOT_SORTED", -5: "MPF_NO_DEVICE", -6: "MPF_IO_ERROR", -7: "MPF_DEVICE_TIMEOUT"}
 
 STOP = {"redshift": 0, "r": 1, "radius": 1, "lambda": 2, "t": 3, "eta": 3, "a": 4, "plane": 5, "s": 6}
 

@@ -103,6 +103,7 @@ struct Group {
     int wg, tid;
     unsigned* err;          // bit 0: an MMA wait ran out
     bool ok;
+    bool hold;              // test of the bounded wait: the MMAs are never issued
 };
 
 // Copy the packed parameters to shared memory, allocate TMEM, initialise the
@@ -136,6 +137,7 @@ __device__ __forceinline__ Group setup(unsigned char* sm, const unsigned char* _
     g.phase = 0;
     g.err = err;
     g.ok = true;
+    g.hold = false;
     return g;
 }
 
@@ -174,7 +176,7 @@ __device__ __forceinline__ void evaluate(Group& g, const Spec& S, const float* p
     for (int l = 0; l <= kHidden; ++l) {
         umma::fence_proxy_async();
         umma::bar_sync(1 + g.wg, 128);
-        if (g.tid == 0 && g.ok) {
+        if (g.tid == 0 && g.ok && !g.hold) {
             umma::fence_after_sync();
             const uint32_t a = umma::smem_u32(g.act);
             const int N = (l < kHidden) ? kWidth : kOutPad;
@@ -223,10 +225,12 @@ __device__ __forceinline__ void evaluate(Group& g, const Spec& S, const float* p
 // inference over a list of points
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads, 1) k_eval(Spec S, const unsigned char* __restrict__ packed,
-                                                      const float* __restrict__ in, long long n, float* out, unsigned* err)
+                                                      const float* __restrict__ in, long long n, float* out, unsigned* err,
+                                                      int hold)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
     Group g = setup(sm, packed, err);
+    g.hold = hold != 0;
     const long long tiles = (n + 127) / 128;
     for (long long t = (long long)blockIdx.x * kWG + g.wg; t < tiles; t += (long long)gridDim.x * kWG) {
         const long long i = t * 128 + g.tid;
@@ -1075,7 +1079,8 @@ int mpf_surrogate_train(mpf_surrogate* s, const mpf_octree* o, const mpf_surroga
     return MPF_OK;
 }
 
-int mpf_surrogate_eval(mpf_surrogate* s, int64_t n, const float* inputs, float* out)
+namespace {
+int surrogate_eval(mpf_surrogate* s, int64_t n, const float* inputs, float* out, int hold)
 {
     if (!s || n < 0 || (n > 0 && (!inputs || !out))) return fail(MPF_BAD_INPUT, "mpf_surrogate_eval: bad argument");
     if (n == 0) return MPF_OK;
@@ -1091,14 +1096,30 @@ int mpf_surrogate_eval(mpf_surrogate* s, int64_t n, const float* inputs, float* 
     if (e != cudaSuccess) return cuda_fail(e, "mpf_surrogate_eval");
     const long long tiles = (n + 127) / 128;
     const unsigned grid = (unsigned)std::min<long long>((tiles + kWG - 1) / kWG, sm_count());
-    k_eval<<<grid, kThreads, kSmemBytes>>>(s->spec, s->packed, x, n, y, err);
+    k_eval<<<grid, kThreads, kSmemBytes>>>(s->spec, s->packed, x, n, y, err, hold);
     e = cudaGetLastError();
     unsigned herr = 0;
     if (e == cudaSuccess) e = cudaMemcpy(out, y, (size_t)n * kOut * sizeof(float), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(&herr, err, sizeof(unsigned), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "mpf_surrogate_eval");
-    if (herr) return fail(MPF_CUDA_ERROR, "mpf_surrogate_eval: a tensor-core wait ran out");
+    if (herr) return fail(MPF_DEVICE_TIMEOUT, "mpf_surrogate_eval: a tensor-core wait ran out");
     return MPF_OK;
+}
+}  // namespace
+
+int mpf_surrogate_eval(mpf_surrogate* s, int64_t n, const float* inputs, float* out)
+{
+    return surrogate_eval(s, n, inputs, out, 0);
+}
+
+// Test of the bounded tensor-core wait (no reference counterpart): the same
+// evaluation with the MMAs withheld, so that each warpgroup's first
+// completion wait runs out after its limit (1 s).  Nothing is left in flight
+// (nothing was issued), TMEM is released as usual, and the call returns
+// MPF_DEVICE_TIMEOUT with the context still usable.
+extern "C" int mpf_internal_surrogate_wait_test(mpf_surrogate* s, int64_t n, const float* inputs, float* out)
+{
+    return surrogate_eval(s, n, inputs, out, 1);
 }
 
 int mpf_surrogate_propagate(mpf_surrogate* s, const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p,
@@ -1167,7 +1188,7 @@ int mpf_surrogate_propagate(mpf_surrogate* s, const mpf_octree* o, const mpf_cos
     }
     if (hs[1]) {
         for (auto& x : ev) cudaEventDestroy(x);
-        return fail(MPF_CUDA_ERROR, "mpf_surrogate_propagate: a tensor-core wait ran out");
+        return fail(MPF_DEVICE_TIMEOUT, "mpf_surrogate_propagate: a tensor-core wait ran out");
     }
     // fallback: flagged photons re-run on the plain octree path
     long long fb = 0, fb_steps = 0;

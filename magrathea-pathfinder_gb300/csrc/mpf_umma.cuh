@@ -114,15 +114,17 @@ __device__ __forceinline__ uint64_t globaltimer_ns()
 }
 // Wait for the phase with the given parity to complete; false once
 // `timeout_ns` of wall time have passed (each try_wait suspends the thread for
-// at most a short, system-dependent time).
+// at most a short, system-dependent time), or after 2^26 tries whatever the
+// timer reads.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t timeout_ns)
 {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
-    for (;;) {
+    for (uint32_t tries = 0; tries < (1u << 26); ++tries) {
         if (mbar_try_wait(bar, parity)) return true;
         if (globaltimer_ns() - t0 > timeout_ns) return false;
     }
+    return false;
 }
 
 // ---- MMA --------------------------------------------------------------------

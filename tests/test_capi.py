@@ -55,3 +55,18 @@ def test_bad_input_is_a_status_not_a_crash(pkg):
     if L.mpf_device_count() == 0:
         rec = np.zeros(2, dtype=np.dtype([("b", "u1", 48)]))
         assert L.mpf_octree_upload(ctypes.c_void_p(rec.ctypes.data), 2, ctypes.byref(h)) == -5
+
+
+def test_corrupt_cone_file_is_an_io_error(pkg, tmp_path):
+    """A cone .bin whose size is not a whole number of 48-byte records (a
+    truncated write), or an empty one, is refused before any device work."""
+    L = pkg.library()
+    h = ctypes.c_void_p()
+    bad = tmp_path / "truncated.bin"
+    bad.write_bytes(b"\0" * (48 * 3 + 17))
+    assert L.mpf_octree_load(str(bad).encode(), ctypes.byref(h)) == -6
+    assert b"multiple of 48" in L.mpf_last_error()
+    empty = tmp_path / "empty.bin"
+    empty.write_bytes(b"")
+    assert L.mpf_octree_load(str(empty).encode(), ctypes.byref(h)) == -6
+    assert not h.value

@@ -162,3 +162,15 @@ def test_edge_cases(gpu_lib, pkg, oracle_mod, golden):
     s, f, _, rc = pkg.propagate(tree, cos, launch[2:], L, nsteps=10, order=2, stop="redshift", stop_value=0.2,
                                 max_steps=5)
     assert rc == 1 and s[0] <= 6
+
+
+def test_unsorted_records_are_refused(gpu_lib, pkg, golden):
+    """The upload checks the key order the reference's binary searches rely
+    on: two swapped records give MPF_NOT_SORTED, not a wrong octree."""
+    import ctypes
+    rec = np.array(golden["records"]).copy()
+    rec[[10, 11]] = rec[[11, 10]]
+    L = pkg.library()
+    h = ctypes.c_void_p()
+    assert L.mpf_octree_upload(ctypes.c_void_p(rec.ctypes.data), rec.shape[0], ctypes.byref(h)) == -4
+    assert not h.value

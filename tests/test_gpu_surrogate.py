@@ -104,6 +104,26 @@ def test_tensor_core_inference_matches_oracle(cone):
     s.close()
 
 
+def test_tensor_core_wait_runs_out_with_a_status(cone, pkg):
+    """The completion wait of the tensor-core network is bounded (1 s): with
+    the MMAs withheld (a completion that never comes) the evaluation returns
+    MPF_DEVICE_TIMEOUT, and the same context then evaluates normally."""
+    import ctypes
+    s = _surrogate(cone)
+    params = M.random_params(5)
+    s.set_params(params, _random_norm(s))
+    x, _ = s.sample(cone["tree"], 128, first=3)
+    out = np.zeros((x.shape[0], 5), dtype=np.float32)
+    L = pkg.library()
+    L.mpf_internal_surrogate_wait_test.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
+    rc = L.mpf_internal_surrogate_wait_test(s._h, x.shape[0], x.ctypes.data, out.ctypes.data)
+    assert rc == -7, rc
+    assert b"wait ran out" in L.mpf_last_error()
+    good = s.eval(x)
+    assert np.all(np.isfinite(good)) and np.abs(good).max() > 0
+    s.close()
+
+
 @pytest.fixture(scope="module")
 def trained(cone):
     s = _surrogate(cone, seed=3)
