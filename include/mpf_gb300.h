@@ -174,6 +174,11 @@ typedef struct {
     int plane_sachs;
     int stop_bundle;
     double openingmin;
+    /* 1 = "infinitesimal_born" (catalogues.h:515, 670-673): the Newton steps
+     * as "infinitesimal", the converged source's Jacobian along the FLRW (Born)
+     * ray of its observed direction to its radius; exclusive with
+     * jacobian_bundle */
+    int jacobian_born;
 } mpf_catalogue_params;
 
 #define MPF_CATALOGUE_FIELDS 16
@@ -213,10 +218,13 @@ int mpf_catalogue_newton_device(const mpf_octree* o, const mpf_cosmology* c, con
 /* ------------------------------------------------------------------------ */
 /* Map components, the reference's index_components (src/hmaps.cpp:196-269,
  * hmaps.h:716-829): rows per surface in the order given; lensing gives 4
- * rows (kappa, gamma1, gamma2, 1/mu), deflection 2 (phi - beta1,
- * theta - beta2), the others 1. */
+ * rows (kappa, gamma1, gamma2, 1/mu; 5 with the bundle Jacobian: w before
+ * 1/mu), lensing_born 4 (the same from the Jacobian along the pixel's FLRW
+ * ray, hmaps.h:706-712, 771-785), deflection 2 (phi - beta1, theta - beta2),
+ * the others 1. */
 typedef enum {
     MPF_MAP_LENSING = 0,
+    MPF_MAP_LENSING_BORN = 1,     /* kappa gamma1 gamma2 1/mu along the FLRW (Born) ray of the pixel */
     MPF_MAP_DR = 2, MPF_MAP_DL = 3, MPF_MAP_DT = 4, MPF_MAP_DA = 5, MPF_MAP_DZ = 6, MPF_MAP_DS = 7,
     MPF_MAP_ISW = 8, MPF_MAP_DENS = 9, MPF_MAP_DENS_MAX = 10, MPF_MAP_STEPS = 11, MPF_MAP_PHI = 12,
     MPF_MAP_DEFLECTION = 13

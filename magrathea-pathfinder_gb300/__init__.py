@@ -273,7 +273,10 @@ def catalogue_params(length, h, mpc=3.08568e22, cat_accuracy=1e-8, nsteps=10, or
     rot = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64).reshape(9)
     p.rotm1 = rot.ctypes.data if rot is not None else None
     p.nsteps, p.order, p.exact, p.max_iterations = int(nsteps), int(order), int(bool(exact)), int(max_iterations)
+    if jacobian not in ("infinitesimal", "bundle", "infinitesimal_born"):
+        raise ValueError("jacobian must be infinitesimal, bundle or infinitesimal_born")
     p.jacobian_bundle = 1 if jacobian == "bundle" else 0
+    p.jacobian_born = 1 if jacobian == "infinitesimal_born" else 0
     p.plane_sachs = 1 if plane == "sachs" else 0
     p.stop_bundle = capi.STOP[stop_bundle]
     p.openingmin = float(openingmin)
@@ -293,7 +296,9 @@ def hmaps_fill(octree: Octree, cosmology: Cosmology, nside: int, pixels, surface
 
     surfaces: the stop-quantity values of the map surfaces (interpRefvec);
     homogeneous: [nsurfaces, 5] = t, chi, lambda, a, z of the FLRW ray there;
-    components: the reference's map component names, in order;
+    components: the reference's map component names, in order ("lensing_born":
+    the infinitesimal Jacobian along each pixel's FLRW ray, traced through the
+    float64 kernel);
     jacobian: "infinitesimal" or "bundle" (then plane, stop_bundle and
     openingmin, in radians, as the reference's parameters).
     """
@@ -301,7 +306,7 @@ def hmaps_fill(octree: Octree, cosmology: Cosmology, nside: int, pixels, surface
     pix = np.ascontiguousarray(pixels, dtype=np.int64)
     comps = [capi.MAP_COMPONENTS[c] for c in components]
     bundle = jacobian == "bundle"
-    nm = sum((5 if bundle else 4) if c == 0 else 2 if c == 13 else 1 for c in comps)
+    nm = sum((5 if bundle else 4) if c == 0 else 4 if c == 1 else 2 if c == 13 else 1 for c in comps)
     p, keep = capi.make_params(length, nsteps, order, stop, 0.0, surfaces, True, exact, max_steps)
     hom = np.ascontiguousarray(homogeneous, dtype=np.float64).reshape(-1, 5)
     cc = np.ascontiguousarray(comps, dtype=np.int32)

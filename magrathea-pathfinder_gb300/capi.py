@@ -38,7 +38,7 @@ MPF_SURROGATE_PARAMS = 68112
 MPF_SURROGATE_NORM = 274
 
 # map component names (the reference's map_components keys) -> mpf_map_component
-MAP_COMPONENTS = {"lensing": 0, "dr": 2, "dl": 3, "dt": 4, "da": 5, "dz": 6, "ds": 7, "isw": 8, "dens": 9,
+MAP_COMPONENTS = {"lensing": 0, "lensing_born": 1, "dr": 2, "dl": 3, "dt": 4, "da": 5, "dz": 6, "ds": 7, "isw": 8, "dens": 9,
                   "dens_max": 10, "steps": 11, "phi": 12, "deflection": 13}
 
 MPF_CATALOGUE_FIELDS = 16
@@ -65,7 +65,8 @@ class CatalogueParams(C.Structure):
     _fields_ = [("length", C.c_double), ("h", C.c_double), ("mpc", C.c_double), ("cat_accuracy", C.c_double),
                 ("vobs", C.c_double * 3), ("rotm1", C.c_void_p), ("nsteps", C.c_uint), ("order", C.c_int),
                 ("exact", C.c_int), ("max_iterations", C.c_int), ("jacobian_bundle", C.c_int),
-                ("plane_sachs", C.c_int), ("stop_bundle", C.c_int), ("openingmin", C.c_double)]
+                ("plane_sachs", C.c_int), ("stop_bundle", C.c_int), ("openingmin", C.c_double),
+                ("jacobian_born", C.c_int)]
 
 
 class CatalogueStats(C.Structure):

@@ -304,6 +304,8 @@ bool catalogue_consts(const mpf_catalogue_params* p, mpf::CatConst& K, mpf::CatR
     K.plane_sachs = p->plane_sachs ? 1 : 0;
     K.stop_bundle = p->stop_bundle;
     K.openingmin = p->openingmin;
+    K.born = p->jacobian_born ? 1 : 0;
+    if (K.born && K.bundle) return false;
     if (K.bundle && (p->stop_bundle < 0 || p->stop_bundle > 5 || !(p->openingmin > 0.0) || !(p->openingmin < 1.0)))
         return false;
     if (p->rotm1)
@@ -381,11 +383,13 @@ int hmaps_fill_impl(const mpf_octree* o, const mpf_cosmology* c, const mpf_param
     M.ncomp = ncomp;
     for (int q = 0; q < ncomp; ++q) {
         const int k = components[q];
-        if (k < 0 || k > 13 || k == 1)
-            return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill: unknown map component (lensing_born is not built)");
+        if (k < 0 || k > 13) return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill: unknown map component");
         M.comp[q] = k;
-        M.nmaps += (k == MPF_MAP_LENSING) ? (bundle ? 5 : 4) : (k == MPF_MAP_DEFLECTION) ? 2 : 1;
+        M.nmaps += (k == MPF_MAP_LENSING) ? (bundle ? 5 : 4) : (k == MPF_MAP_LENSING_BORN) ? 4 : (k == MPF_MAP_DEFLECTION) ? 2 : 1;
+        if (k == MPF_MAP_LENSING_BORN) M.born = 1;
     }
+    // lensing_born alone: no ray is traced through the field (hmaps.h:594, 604-605)
+    M.only_born = (ncomp == 1 && components[0] == MPF_MAP_LENSING_BORN) ? 1 : 0;
     if (bundle) {
         // Lensing::dbetadtheta knows lambda, r, redshift, a, t and plane (lensing.h:198-296)
         if (stop_bundle < 0 || stop_bundle > 5 || !(openingmin > 0.0) || !(openingmin < 1.0))

@@ -233,8 +233,8 @@ __global__ void k_cat_update(long long m, int iteration, int traced_jacobian, Ca
     }
     // converged (catalogues.h:658-726)
     row[2] = S.phi; row[3] = S.theta; row[4] = miss; row[5] = (double)count;
-    if (K.bundle) {
-        retrace_flag[s] = 1;   // its Jacobian comes from the four-ray bundle after the last round
+    if (K.bundle || K.born) {
+        retrace_flag[s] = 1;   // its Jacobian comes from the four-ray bundle or the Born ray after the last round
     } else if (traced_jacobian) {
         row[12] = o[6]; row[13] = o[7]; row[14] = o[7]; row[15] = o[8];
     } else {
@@ -266,10 +266,11 @@ __global__ void k_cat_update(long long m, int iteration, int traced_jacobian, Ca
     row[6] = z0; row[7] = z1; row[8] = z2; row[9] = z3; row[10] = z4; row[11] = z5;
 }
 
-// Jacobian of a converged source whose last ray was traced without it.
+// Jacobian of a converged source whose last ray was traced without it, or
+// (jacobiantype = infinitesimal_born) the one of its Born ray.
 __global__ void k_cat_jacobian(long long m, const int* __restrict__ list, const double* __restrict__ rec,
                                const long long* __restrict__ steps, double* __restrict__ rows,
-                               unsigned long long* __restrict__ photon_steps)
+                               unsigned long long* __restrict__ photon_steps, int born)
 {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m) return;
@@ -278,7 +279,8 @@ __global__ void k_cat_jacobian(long long m, const int* __restrict__ list, const 
     atomicAdd(photon_steps + 1, ns);
     const double* o = rec + (long long)kSourceFields * j;
     double* row = rows + (long long)kCatalogueFields * list[j];
-    if (o[19] == 0.0) return;
+    // a Born ray short of the radius carries the Jacobian at its last point
+    if (o[19] == 0.0 && !born) return;
     row[12] = o[6]; row[13] = o[7]; row[14] = o[7]; row[15] = o[8];
 }
 
@@ -583,13 +585,13 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
         // (3 and 4 before the bundle rounds); round 2 traces it too, so that
         // the sources converging there (most of them) need no re-trace for
         // their final Jacobian
-        const int jac = K.bundle ? ((it >= 3 && it < 5) ? 1 : 0) : ((it >= 2) ? 1 : 0);
+        const int jac = K.bundle ? ((it >= 3 && it < 5) ? 1 : 0) : K.born ? ((it >= 3) ? 1 : 0) : ((it >= 2) ? 1 : 0);
         P.jacobian = jac;
         // round 2 also re-traces, with the Jacobian, the sources that converged
         // in rounds 0 and 1 (appended after the active ones): their final
         // Jacobian then costs no launch of its own at the end
         long long nre = 0;
-        if (it == 2 && !K.bundle) {
+        if (it == 2 && !K.bundle && !K.born) {
             k_list_flags<<<blocks((long long)m_valid + 1, tpb), tpb, 0, stream>>>(m_valid, sorted, rflag, scan);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             nre = exclusive_scan(scan, (int64_t)m_valid + 1, stream);
@@ -606,7 +608,7 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
         if (e != cudaSuccess) return e;
         if (nre > 0) {
             k_cat_jacobian<<<blocks(nre, tpb), tpb, 0, stream>>>(nre, cur + m, rec + (long long)kSourceFields * m, steps + m,
-                                                                  d_rows, psteps);
+                                                                  d_rows, psteps, 0);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             stats->rays += nre;
             stats->launches += 1;
@@ -654,9 +656,18 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
         P.jacobian = 1;
         k_cat_rays<<<blocks(r, tpb), tpb, 0, stream>>>(r, cur, state, launch, radius);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        e = exact ? launch_propagate<true>(T, Cs, P, launch, r, O, stream) : launch_propagate<false>(T, Cs, P, launch, r, O, stream);
+        if (K.born) {
+            // the Born ray of the converged direction to the source radius
+            // (catalogues.h:670-673), through the float64 kernel (Born mode is
+            // not in the FP32-gather kernel)
+            PropParams Pn = P;
+            Pn.homogeneous = 2;
+            e = launch_propagate<true>(T, Cs, Pn, launch, r, O, stream);
+        } else {
+            e = exact ? launch_propagate<true>(T, Cs, P, launch, r, O, stream) : launch_propagate<false>(T, Cs, P, launch, r, O, stream);
+        }
         if (e != cudaSuccess) return e;
-        k_cat_jacobian<<<blocks(r, tpb), tpb, 0, stream>>>(r, cur, rec, steps, d_rows, psteps);
+        k_cat_jacobian<<<blocks(r, tpb), tpb, 0, stream>>>(r, cur, rec, steps, d_rows, psteps, K.born);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         stats->rays += r;
         stats->launches += 4;

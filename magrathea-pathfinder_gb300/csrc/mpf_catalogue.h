@@ -18,6 +18,9 @@ struct CatConst {
     int plane_sachs;      // screen normal: interpolated direction (1) or position (0)
     int stop_bundle;      // StopKind of the bundle rays
     double openingmin;    // radians
+    // jacobiantype = "infinitesimal_born": the converged sources' Jacobian
+    // along their Born ray (homogeneous field on the octree's levels)
+    int born;
 };
 
 struct CatRotation {

@@ -63,21 +63,26 @@ __global__ void k_pix_launch(long long n, long long nside, const long long* __re
 }
 
 // One thread per (pixel, surface): the map rows of hmaps.h:716-829.
-// rec_fields: stride of the surface records; jac: the bundle Jacobians
-// (n x nz x 4: a11 a12 a21 a22) or null for the infinitesimal one.
+// rec_fields: stride of the surface records (unused with only_born); jac: the
+// bundle Jacobians (n x nz x 4: a11 a12 a21 a22) or null for the
+// infinitesimal one; born: the Born rays' surface records (n x nz x 20) or
+// null.
 __global__ void k_fill_maps(long long n, int nz, MapSpec M, const double* __restrict__ launch,
                             const double* __restrict__ rec, int rec_fields, const double* __restrict__ jac,
-                            float* __restrict__ maps, long long row_stride, long long col0)
+                            const double* __restrict__ born, float* __restrict__ maps, long long row_stride,
+                            long long col0)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n * nz) return;
     const long long j = t % n;
     const int iz = (int)(t / n);
-    const double* o = rec + ((long long)j * nz + iz) * rec_fields;
+    const double* o = M.only_born ? nullptr : rec + ((long long)j * nz + iz) * rec_fields;
     const double* bj = jac ? jac + ((long long)j * nz + iz) * 4 : nullptr;
+    const double* ob = born ? born + ((long long)j * nz + iz) * kPlaneFields : nullptr;
     float* out = maps + (long long)M.nmaps * iz * row_stride + col0 + j;
-    // an unusable crossing, or a bundle Jacobian flagged 42, zeroes the surface (hmaps.h:719-738)
-    if (o[19] == 0.0 || (bj && bj[0] == 42.0)) {
+    // a Born ray that took no step, an unusable crossing of the traced ray, or
+    // a bundle Jacobian flagged 42, zeroes the surface (hmaps.h:719-738)
+    if ((ob && ob[19] == 0.0) || (o && o[19] == 0.0) || (bj && bj[0] == 42.0)) {
         for (int r = 0; r < M.nmaps; ++r) out[(long long)r * row_stride] = 0.0f;
         return;
     }
@@ -99,6 +104,16 @@ __global__ void k_fill_maps(long long n, int nz, MapSpec M, const double* __rest
                 break;
             }
             const double a11 = o[6], a12 = o[7], a22 = o[8];
+            out[(long long)(row + 0) * row_stride] = (float)(1 - (a11 + a22) * 0.5);
+            out[(long long)(row + 1) * row_stride] = (float)(-0.5 * (a11 - a22));
+            out[(long long)(row + 2) * row_stride] = (float)(-a12);
+            out[(long long)(row + 3) * row_stride] = (float)(a11 * a22 - a12 * a12);
+            row += 4;
+            break;
+        }
+        case 1: {
+            // lensing_born (hmaps.h:771-785)
+            const double a11 = ob[6], a12 = ob[7], a22 = ob[8];
             out[(long long)(row + 0) * row_stride] = (float)(1 - (a11 + a22) * 0.5);
             out[(long long)(row + 1) * row_stride] = (float)(-0.5 * (a11 - a22));
             out[(long long)(row + 2) * row_stride] = (float)(-a12);
@@ -256,16 +271,44 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
     if (e == cudaSuccess) e = cudaMalloc(&status, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, sizeof(unsigned), stream);
     PropOut O{steps, nullptr, rec, status, nullptr};
-    for (long long c0 = 0; !M.bundle && e == cudaSuccess && c0 < npix; c0 += cap) {
+    // lensing_born: one Born ray per pixel (hmaps.h:706-712) with radius
+    // surfaces at the FLRW distances of the map surfaces, through the float64
+    // kernel (Born mode is not in the FP32-gather kernel)
+    double* brn = nullptr;
+    long long* brn_steps = nullptr;
+    PropParams Pn = P;
+    if (M.born) {
+        if (e == cudaSuccess) e = cudaMalloc(&brn, (size_t)cap * nz * kPlaneFields * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&brn_steps, (size_t)cap * sizeof(long long));
+        Pn.homogeneous = 2;
+        Pn.stop_kind = STOP_R;
+        Pn.jacobian = 1;
+        Pn.wide = 0;
+        Pn.direct = 0;
+        Pn.ray_planes = nullptr;
+        Pn.ray_ki = nullptr;
+        for (int iz = 0; iz < nz; ++iz) Pn.planes[iz] = M.homogeneous[iz][1];
+        Pn.stop_ref = M.homogeneous[nz - 1][1];
+    }
+    const PropOut On{brn_steps, nullptr, brn, status, nullptr};
+    auto born_pass = [&](long long m) -> cudaError_t {
+        return M.born ? launch_propagate<true>(T, C, Pn, launch, m, On, stream) : cudaSuccess;
+    };
+    // (lensing_born alone traces neither the central nor the bundle rays)
+    for (long long c0 = 0; (!M.bundle || M.only_born) && e == cudaSuccess && c0 < npix; c0 += cap) {
         const long long m = (npix - c0 < cap) ? npix - c0 : cap;
         k_pix_launch<<<blocks(m, 128), 128, 0, stream>>>(m, nside, d_pixels + c0, launch);
         if ((e = cudaGetLastError()) != cudaSuccess) break;
-        e = exact ? launch_propagate<true>(T, C, P, launch, m, O, stream) : launch_propagate<false>(T, C, P, launch, m, O, stream);
-        if (e != cudaSuccess) break;
-        k_fill_maps<<<blocks(m * nz, 128), 128, 0, stream>>>(m, nz, M, launch, rec, kPlaneFields, nullptr, d_maps, npix, c0);
+        if (!M.only_born) {
+            e = exact ? launch_propagate<true>(T, C, P, launch, m, O, stream) : launch_propagate<false>(T, C, P, launch, m, O, stream);
+            if (e != cudaSuccess) break;
+        }
+        if ((e = born_pass(m)) != cudaSuccess) break;
+        k_fill_maps<<<blocks(m * nz, 128), 128, 0, stream>>>(m, nz, M, launch, rec, kPlaneFields, nullptr, brn, d_maps,
+                                                               npix, c0);
         e = cudaGetLastError();
     }
-    if (M.bundle && e == cudaSuccess) {
+    if (M.bundle && !M.only_born && e == cudaSuccess) {
         // central rays with wide records, then four bundle rays per pixel to
         // their own stop_bundle surfaces, then the Jacobians and the rows
         double *wrec = nullptr, *blaunch = nullptr, *bplanes = nullptr, *brec = nullptr, *ki = nullptr, *dist = nullptr,
@@ -308,7 +351,9 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
             if (e != cudaSuccess) break;
             k_bundle_jacobian<<<blocks(m, 128), 128, 0, stream>>>(m, nz, M, brec, ki, dist, jac);
             if ((e = cudaGetLastError()) != cudaSuccess) break;
-            k_fill_maps<<<blocks(m * nz, 128), 128, 0, stream>>>(m, nz, M, launch, wrec, kWideFields, jac, d_maps, npix, c0);
+            if ((e = born_pass(m)) != cudaSuccess) break;
+            k_fill_maps<<<blocks(m * nz, 128), 128, 0, stream>>>(m, nz, M, launch, wrec, kWideFields, jac, brn, d_maps, npix,
+                                                                   c0);
             e = cudaGetLastError();
         }
         cudaStreamSynchronize(stream);
@@ -320,6 +365,8 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (launch) cudaFree(launch);
     if (rec) cudaFree(rec);
+    if (brn) cudaFree(brn);
+    if (brn_steps) cudaFree(brn_steps);
     if (steps) cudaFree(steps);
     if (status) cudaFree(status);
     return e;

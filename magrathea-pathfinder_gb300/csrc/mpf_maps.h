@@ -11,7 +11,7 @@ constexpr int kMaxMapComponents = 16;
 
 struct MapSpec {
     int ncomp;
-    int comp[kMaxMapComponents];      // index_components of hmaps.cpp (0 lensing, 2-13 the others)
+    int comp[kMaxMapComponents];      // index_components of hmaps.cpp (0 lensing, 1 lensing_born, 2-13 the others)
     int nmaps;                        // rows per surface
     double homogeneous[kMaxPlanes][5];   // per surface: t chi lambda a z of the FLRW ray
     // jacobiantype = "bundle" (Lensing::dbetadtheta): 4 rays per pixel
@@ -19,6 +19,10 @@ struct MapSpec {
     int plane_sachs;                  // screen normal: interpolated direction (1) or position (0)
     int stop_bundle;                  // StopKind of the bundle rays' surfaces
     double openingmin;                // bundle opening (radians)
+    // lensing_born: a Born ray per pixel (homogeneous field on the octree's
+    // levels, Jacobian at the FLRW surface radii); only_born: no traced ray
+    int born;
+    int only_born;
 };
 
 // d_pixels: npix RING pixel ids on the device; d_maps: nmaps * nplanes rows of

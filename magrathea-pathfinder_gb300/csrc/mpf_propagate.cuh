@@ -68,10 +68,14 @@ struct PropParams {
     // bundle photons of Integrator::launch(photon, count, angle, rotation),
     // whose direction is not renormalised before integrate)
     int direct;
-    // Order = -1 of the reference (the FLRW reference ray of the rays driver,
-    // integrated on a uniform octree of level hom_level): every gather gives
-    // the homogeneous field (a = 1, the rest 0), every cell is of level
-    // hom_level; exact kernel only
+    // Order = -1 of the reference: every gather gives the homogeneous field
+    // (a = 1, the rest 0).  1: the FLRW reference ray of the rays driver,
+    // integrated on a uniform octree of level hom_level (every cell is of
+    // that level); 2: the Born ray of hmaps / catalogues (hmaps.h:706-712,
+    // catalogues.h:670-673), on the octree itself (its levels set the steps,
+    // its field the Jacobian), with the Jacobian at each surface's value (a
+    // radius) and, for a surface the ray never reaches, at its last point.
+    // Exact kernel only.
     int homogeneous;
     int hom_level;
     // per-ray plane normals for the stop criterion "plane" with per-ray
@@ -139,7 +143,7 @@ __device__ __forceinline__ Field7 field_at(const DevTree& T, const PropParams& P
 
 __device__ __forceinline__ Found locate_at(const DevTree& T, const PropParams& P, double x, double y, double z)
 {
-    if (P.homogeneous) return Found{0, P.hom_level};
+    if (P.homogeneous == 1) return Found{0, P.hom_level};
     return locate(T, x, y, z);
 }
 
@@ -187,6 +191,19 @@ __device__ __forceinline__ bool plane_crossed(int kind, const Rec& r, double ref
 struct JSum {
     double s1[3], s2[3];
 };
+
+// a11 a12 a22 of the infinitesimal Jacobian at distance d from the sums at
+// the last point with chi <= d (lensing.h:459-469)
+__device__ __forceinline__ void jac_from_sums(const JSum& J, double d, double length, double* A)
+{
+    const double c2 = 299792458.0 * 299792458.0;
+    const double a11 = J.s1[0] - J.s2[0] / d;
+    const double a12 = J.s1[1] - J.s2[1] / d;
+    const double a22 = J.s1[2] - J.s2[2] / d;
+    A[0] = 1 - 2 * a11 / c2 * length;
+    A[1] = -2 * a12 / c2 * length;
+    A[2] = 1 - 2 * a22 / c2 * length;
+}
 
 template <bool EXACT>
 __device__ void jac_point(const DevTree& T, const Rec& p, double dr, double* H)
@@ -402,8 +419,9 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
                     }
                     if (P.jacobian) {
                         // the Jacobian at the surface's distance (hmaps.h:653-656),
-                        // or at the source radius itself (catalogues.h:517)
-                        const double jd = SRC ? ref : dist;
+                        // or at the source radius or Born surface radius itself
+                        // (catalogues.h:517, hmaps.h:712)
+                        const double jd = (SRC || P.homogeneous == 2) ? ref : dist;
                         // last point with chi <= jd among k, k-1, k-2
                         const JSum* J = nullptr;
                         if (p.chi <= jd) J = &S;
@@ -411,12 +429,7 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
                         else if (k >= 2 && chim2 <= jd) J = &Sm2;
                         double A[3] = {1.0, 0.0, 1.0};
                         if (J) {
-                            const double a11 = J->s1[0] - J->s2[0] / jd;
-                            const double a12 = J->s1[1] - J->s2[1] / jd;
-                            const double a22 = J->s1[2] - J->s2[2] / jd;
-                            A[0] = 1 - 2 * a11 / c2 * P.length;
-                            A[1] = -2 * a12 / c2 * P.length;
-                            A[2] = 1 - 2 * a22 / c2 * P.length;
+                            jac_from_sums(*J, jd, P.length, A);
                         } else {
                             status |= 2u;
                         }
@@ -476,6 +489,8 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
             for (int q = 0; q < 24; ++q) prow[q] = 0.0;
             const long long marked = size - 1;
             prow[0] = (double)(marked - (marked > 0));
+            // a Born ray that ends short of the radius: the Jacobian at its last point
+            if (P.homogeneous == 2 && P.jacobian && ck < 0) jac_from_sums(S, stop_ref, P.length, prow + 6);
         }
         prow[19] = ok ? 1.0 : 0.0;
     } else if (prow) {
@@ -491,6 +506,13 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
             }
             o[19] = valid ? 1.0 : 0.0;
             if (P.wide) o[24] = found ? 1.0 : 0.0;
+            if (P.homogeneous == 2) {
+                // Born ray (hmaps.h:712, 719): the Jacobian at the surface radius
+                // (from the last point when the ray never got there); only a
+                // ray that could not take a step is unusable
+                if (P.jacobian && ck < 0) jac_from_sums(S, rpl[j], P.length, o + 6);
+                o[19] = (size > 1) ? 1.0 : 0.0;
+            }
         }
     }
     if (status) atomicOr(O.status, status);

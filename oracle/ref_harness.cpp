@@ -360,9 +360,10 @@ int ref_fillmap_jac(long nside, int nz, const double* zvals, const char* stop_ra
     uint nmaps = 0;
     for (size_t i = 0; i < map_components.size(); ++i) {
         auto it = ids.find(map_components[i]);
-        if (it == ids.end() || it->second == 1) return -1;
+        if (it == ids.end()) return -1;
         index_components[i] = it->second;
-        nmaps += (it->second == 0) ? (bundle ? 5 : 4) : (it->second == 13 ? 2 : 1);
+        // rows per component as hmaps.cpp:196-250 counts them
+        nmaps += (it->second == 0) ? (bundle ? 5 : 4) : (it->second == 1) ? 4 : (it->second == 13 ? 2 : 1);
     }
     *nmaps_out = (int)nmaps;
     std::vector<double> hom(5 * (size_t)nz);

@@ -57,6 +57,9 @@ def cone_pixels(R, nside, half_deg):
 # bundle Jacobian (jacobiantype = bundle): screen plane and stop_bundle pairs, opening 0.2 arcmin
 BUNDLES = (("sachs", "redshift"), ("normal", "r"), ("sachs", "plane"), ("normal", "plane"))
 OPENING = 0.2 / 60.0 * 3.141592653589793 / 180.0
+# lensing_born maps: (fixture key, components, jacobiantype)
+BORN_MAPS = (("born", "lensing,lensing_born,dz,steps", "infinitesimal"), ("bornonly", "lensing_born", "infinitesimal"),
+             ("born_bundle", "lensing_born,lensing,dr", "bundle"))
 CAT_ACCURACIES = (1e-8, 1e-13, 0.0)   # job default; deep enough for the Jacobian steps; never met (rejects)
 CAT_VOBS = (1e-4, -2e-4, 5e-5)
 
@@ -133,6 +136,11 @@ def make(name, cfg):
         for plane, sb in BUNDLES:
             out["ref_maps_bundle_o%d_%s_%s" % (order, plane, sb)] = R.fillmap(
                 cfg["nside"], out["zs"], pix, "redshift", COMPONENTS, cfg["nsteps"], "bundle", plane, sb, OPENING)
+        # lensing_born (hmaps.h:706-712, 771-785): the Jacobian along the FLRW ray of each pixel, with the
+        # traced ray's components, alone (no traced ray), and beside a bundle Jacobian
+        for key, comps, jt in BORN_MAPS:
+            out["ref_maps_%s_o%d" % (key, order)] = R.fillmap(cfg["nside"], out["zs"], pix, "redshift", comps,
+                                                              cfg["nsteps"], jt, "sachs", "redshift", OPENING)
         if order == 1:
             crng = np.random.default_rng(23)
             src = catalogue_sources(crng, 40, spec.chi_max / spec.lbox)
@@ -150,6 +158,11 @@ def make(name, cfg):
                                                                out["cosmo_mpc"], CAT_VOBS)
         out["ref_cat_rot_o%d" % order] = R.catalogue(out["cat_src_rotated"], CAT_ACCURACIES[0], cfg["nsteps"],
                                                      out["cosmo_h"], out["cosmo_mpc"], CAT_VOBS, out["cat_rotm1"])
+        # jacobiantype = infinitesimal_born: the final Jacobian along the FLRW ray (catalogues.h:670-673)
+        for ia in (0, 1):
+            out["ref_cat_born_o%d_a%d" % (order, ia)] = R.catalogue(
+                out["cat_src"], CAT_ACCURACIES[ia], cfg["nsteps"], out["cosmo_h"], out["cosmo_mpc"], CAT_VOBS, None,
+                "infinitesimal_born")
         # jacobiantype = bundle: converged at 1e-8, and every source through the bundle Newton rounds at 0
         for ia in (0, 2):
             for plane, sb in BUNDLES:

@@ -73,3 +73,43 @@ def test_hmaps_fill_bundle_matches_reference(gpu_lib, pkg, golden, order, exact,
     for row in range(5, ref.shape[1]):
         scale = np.abs(ref[:, row]).max() + 1e-30
         assert np.abs(got[:, row] - ref[:, row]).max() <= 2e-6 * scale + 1e-12, row
+
+
+# lensing_born (hmaps.h:706-712, 771-785): the Jacobian along each pixel's
+# FLRW ray, with the traced ray's rows, alone, and beside the bundle Jacobian
+BORN_MAPS = (("born", "lensing,lensing_born,dz,steps", "infinitesimal"), ("bornonly", "lensing_born", "infinitesimal"),
+             ("born_bundle", "lensing_born,lensing,dr", "bundle"))
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("exact", [True, False])
+@pytest.mark.parametrize("key,comps,jt", BORN_MAPS)
+def test_hmaps_fill_born_matches_reference(gpu_lib, pkg, golden, order, exact, key, comps, jt):
+    """The Born rows run through the float64 kernel in both modes and agree to
+    1e-6 of their scale (the Jacobian sums are re-associated); the other rows
+    keep the tolerances of the tests above (bundle rows 1e-3 in fast mode)."""
+    tree = pkg.Octree.from_records(golden["records"])
+    cos = pkg.Cosmology(golden["cosmo_t"], golden["cosmo_a"], golden["cosmo_dadt"], golden["cosmo_d2adt2"])
+    names = comps.split(",")
+    got = pkg.hmaps_fill(tree, cos, int(golden["nside"]), golden["pixels"], golden["zs"], golden["homogeneous"], names,
+                         float(golden["cosmo_length"]), nsteps=int(golden["nsteps"]), order=order, exact=exact,
+                         jacobian=jt, plane="sachs", stop_bundle="redshift", openingmin=OPENING)
+    ref = golden["ref_maps_%s_o%d" % (key, order)]
+    assert got.shape == ref.shape
+    # the zeroed (pixel, surface) pairs agree
+    np.testing.assert_array_equal(np.all(got == 0, axis=1), np.all(ref == 0, axis=1))
+    row = 0
+    for c in names:
+        nrow = {"lensing": 5 if jt == "bundle" else 4, "lensing_born": 4, "deflection": 2}.get(c, 1)
+        for r in range(row, row + nrow):
+            scale = max(np.abs(ref[:, r]).max(), 1e-6)
+            if c == "lensing_born" or (c == "lensing" and jt != "bundle"):
+                tol = 1e-6 * scale + 2e-7 * (r - row == 3)
+            elif c == "lensing":
+                tol = (1e-6 if exact else 1e-3) * scale
+            else:
+                tol = 2e-6 * (np.abs(ref[:, r]).max() + 1e-30) + 1e-12
+            assert np.abs(got[:, r] - ref[:, r]).max() <= tol, (c, r, np.abs(got[:, r] - ref[:, r]).max(), tol)
+        row += nrow
+    tree.close()
+    cos.close()
