@@ -12,7 +12,7 @@ from __future__ import annotations
 
 import numpy as np
 
-ROWS = {"lensing": 4, "deflection": 2}
+ROWS = {"lensing": 4, "lensing_born": 4, "deflection": 2}
 # plane record columns
 F = {k: i for i, k in enumerate("firstid f x y z distance A11 A12 A22 t a redshift chi lambda s isw rho phi rho_max "
                                  "valid".split())}
@@ -28,6 +28,8 @@ def assemble(planes: np.ndarray, directions: np.ndarray, homogeneous: np.ndarray
     homogeneous: [nz, 5] = t, chi, lambda, a, z of the FLRW ray at each surface;
     bundle_jac: [npix, nz, 4] (a11 a12 a21 a22) of the bundle Jacobian, or None
     for the infinitesimal one.  Returns float32 maps [nz, nmaps, npix]."""
+    if "lensing_born" in components:
+        raise ValueError("lensing_born needs the Born rays' surface records: hmaps_fill computes it")
     npix, nz = planes.shape[0], planes.shape[1]
     out = np.zeros((nz, nmaps(components, bundle_jac is not None), npix), dtype=np.float32)
     ph = np.arctan2(directions[:, 1], directions[:, 0])
