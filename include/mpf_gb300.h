@@ -63,7 +63,8 @@ typedef struct {
     const double* planes;      /* surfaces (values of the stop quantity), ascending; host memory */
     int nplanes;               /* <= MPF_MAX_PLANES */
     unsigned nsteps;           /* steps per cell */
-    int order;                 /* 1 = CIC, 2 = TSC (the reference's ORDER) */
+    int order;                 /* 0 = NGP, 1 = CIC, 2 = TSC (the reference's ORDER); NGP runs the
+                                  float64 kernel whatever `exact` says (no interpolation arithmetic) */
     int stop;                  /* mpf_stop */
     int jacobian;              /* infinitesimal Jacobian at each surface */
     int exact;                 /* 1: the reference's float64 gather arithmetic, bit-exact
@@ -108,7 +109,7 @@ void mpf_cosmology_destroy(mpf_cosmology* c);
  * records) or -1, for n positions xyz[3n]. */
 int mpf_locate(const mpf_octree* o, int64_t n, const double* xyz, int64_t* cell);
 
-/* SimpleHyperOctree::cic (order 1) / tsc (order 2): 7 floats per position in
+/* SimpleHyperOctree::ngp (order 0) / cic (order 1) / tsc (order 2): 7 floats per position in
  * the order rho phi dphidx dphidy dphidz a dphidt. */
 int mpf_interpolate(const mpf_octree* o, int order, int exact, int64_t n, const double* xyz, float* out7);
 
@@ -160,7 +161,7 @@ typedef struct {
     const double* rotm1;       /* 3x3 row-major rotation into the octree frame (narrow cones,
                                   relCat catalogues.h:818-826), or NULL (isfullsky) */
     unsigned nsteps;           /* RK4 steps per cell */
-    int order;                 /* 1 = CIC, 2 = TSC */
+    int order;                 /* 0 = NGP, 1 = CIC, 2 = TSC */
     int exact;                 /* 1: reference float64 order; 0: FP32 gathers */
     int max_iterations;        /* 10 in the reference (use_previous_catalogues = 0) */
     /* jacobiantype (catalogues.h:505-529, 660-676): 0 = "infinitesimal";
@@ -280,7 +281,7 @@ typedef struct {
     int acorrection;           /* 1: each cell's a snapped to the next lower value of the table of the
                                   cells' distinct scale factors, extended one shell below (Full Universe
                                   Run outputs, input.h:1485-1506) */
-    int order;                 /* gather of the completed children: 1 CIC, 2 TSC (the reference's ORDER) */
+    int order;                 /* gather of the completed children: 0 NGP, 1 CIC, 2 TSC (the reference's ORDER) */
     double* amin;              /* acorrection: receives the table's first value (Input::correct's amin);
                                   may be NULL, left unchanged otherwise */
 } mpf_cells_params;

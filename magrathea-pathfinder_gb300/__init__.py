@@ -101,6 +101,10 @@ class Octree:
     def tsc(self, xyz, exact: bool = True) -> np.ndarray:
         return self._interp(2, xyz, exact)
 
+    def ngp(self, xyz) -> np.ndarray:
+        """The containing cell's record (the reference's ORDER = 0)."""
+        return self._interp(0, xyz, True)
+
     def close(self):
         if self._h:
             self._lib.mpf_octree_destroy(self._h)

@@ -445,6 +445,14 @@ __device__ __forceinline__ void azero(float* a)
 {
     for (int q = 0; q < 7; ++q) a[q] = 0.f;
 }
+// SimpleHyperOctree::ngp (simplehyperoctree.h:1396-1401) over the array: the
+// record the containing search finds at the position's level-32 key
+__device__ void angp(const Rec48* r, long long n, double x, double y, double z, float* res)
+{
+    const long long f0 = afind(r, n, compute128(32, x, y, z));
+    if (f0 >= 0) afields(r[f0], res);
+    else azero(res);
+}
 // SimpleHyperOctree::cic (simplehyperoctree.h:1410-1469) over the array
 __device__ void acic(const Rec48* r, long long n, double x, double y, double z, float* res)
 {
@@ -567,7 +575,8 @@ __global__ void k_complete_serial(Rec48* r, long long m, const int* __restrict__
             // the child's centre as the reference computes it, in float
             const float cx = (float)center128(ck, 0), cy = (float)center128(ck, 1), cz = (float)center128(ck, 2);
             float f[7];
-            if (order == 1) acic(r, size, cx, cy, cz, f);
+            if (order == 0) angp(r, size, cx, cy, cz, f);
+            else if (order == 1) acic(r, size, cx, cy, cz, f);
             else atsc(r, size, cx, cy, cz, f);
             Rec48 o = p;
             o.hi = (unsigned long long)(ck >> 64);
@@ -802,7 +811,7 @@ extern "C" int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_par
 {
     if ((n > 0 && !rows) || n < 0 || !cp || !c || !count || (capacity > 0 && !records))
         return fail(MPF_BAD_INPUT, "mpf_cells_build: bad argument");
-    if (cp->order != 1 && cp->order != 2) return fail(MPF_BAD_INPUT, "mpf_cells_build: order must be 1 or 2");
+    if (cp->order < 0 || cp->order > 2) return fail(MPF_BAD_INPUT, "mpf_cells_build: order must be 0, 1 or 2");
     if (n == 0) {   // no cell files for this cone: an empty octree, as the reference saves it
         *count = 0;
         return MPF_OK;

@@ -56,7 +56,7 @@ struct DBuf {
 
 bool fill_params(const mpf_params* p, mpf::PropParams& P)
 {
-    if (!p || p->nsteps == 0 || (p->order != 1 && p->order != 2) || p->stop < 0 || p->stop > 6 || p->nplanes < 0 ||
+    if (!p || p->nsteps == 0 || p->order < 0 || p->order > 2 || p->stop < 0 || p->stop > 6 || p->nplanes < 0 ||
         p->nplanes > MPF_MAX_PLANES || !(p->length > 0.0))
         return false;
     if (p->nplanes > 0 && !p->planes) return false;
@@ -241,8 +241,10 @@ int mpf_locate(const mpf_octree* o, int64_t n, const double* xyz, int64_t* cell)
 
 int mpf_interpolate(const mpf_octree* o, int order, int exact, int64_t n, const double* xyz, float* out7)
 {
-    if (order != 1 && order != 2) return set_err(MPF_BAD_INPUT, "mpf_interpolate: order must be 1 (CIC) or 2 (TSC)");
-    return gather_host(o, order, exact, n, xyz, out7, 7 * sizeof(float));
+    if (order < 0 || order > 2) return set_err(MPF_BAD_INPUT, "mpf_interpolate: order must be 0 (NGP), 1 (CIC) or 2 (TSC)");
+    // NGP copies the cell's record: no arithmetic to differ between the modes
+    return (order == 0) ? gather_host(o, 3, 1, n, xyz, out7, 7 * sizeof(float))
+                        : gather_host(o, order, exact, n, xyz, out7, 7 * sizeof(float));
 }
 
 int mpf_propagate_device(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t n,
@@ -294,7 +296,7 @@ int mpf_propagate(const mpf_octree* o, const mpf_cosmology* c, const mpf_params*
 namespace {
 bool catalogue_consts(const mpf_catalogue_params* p, mpf::CatConst& K, mpf::CatRotation& R)
 {
-    if (!p || p->nsteps == 0 || (p->order != 1 && p->order != 2) || !(p->length > 0.0) || !(p->h > 0.0) ||
+    if (!p || p->nsteps == 0 || p->order < 0 || p->order > 2 || !(p->length > 0.0) || !(p->h > 0.0) ||
         !(p->mpc > 0.0) || p->max_iterations < 0 || p->max_iterations > 1000 || !(p->cat_accuracy >= 0.0))
         return false;
     K.length = p->length; K.h = p->h; K.mpc = p->mpc; K.accuracy = p->cat_accuracy;

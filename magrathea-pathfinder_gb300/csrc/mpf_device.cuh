@@ -290,9 +290,25 @@ __device__ Field7 tsc(const DevTree& T, double x, double y, double z, bool need_
     return res;
 }
 
+// Nearest grid point (simplehyperoctree.h:1396-1401): the data of the
+// deepest cell containing the position, or the empty record.
+__device__ __forceinline__ Field7 ngp(const DevTree& T, double x, double y, double z)
+{
+    Field7 f;
+    clear(f);
+    const Found c = locate(T, x, y, z);
+    if (c.cell < 0) return f;
+    const float4 g = __ldg(T.grad + c.cell);
+    const float4 s = __ldg(T.scal + c.cell);
+    f.rho = s.x; f.phi = s.y; f.a = s.z;
+    f.dx = g.x; f.dy = g.y; f.dz = g.z; f.dt = g.w;
+    return f;
+}
+
 template <bool EXACT>
 __device__ __forceinline__ Field7 gather(const DevTree& T, int order, double x, double y, double z, bool need_all)
 {
+    if (order == 0) return ngp(T, x, y, z);
     return (order == 1) ? cic<EXACT>(T, x, y, z, need_all) : tsc<EXACT>(T, x, y, z, need_all);
 }
 

@@ -8,6 +8,8 @@
 #include <cstdlib>
 
 namespace mpf {
+cudaError_t launch_gather_exact(const DevTree& T, int kind, const double* d_xyz, long long n, void* d_out, cudaStream_t stream);
+
 // one instantiation per interpolation order, and per mode (surfaces / sources /
 // wide surfaces, per-ray surfaces, direction launches, trajectories)
 static void launch_fast_kernel(long long grid, int tpb, const DevTree& T, const DevCosmo& C, const PropParams& P,
@@ -53,6 +55,8 @@ cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const P
                                     const PropOut& O, cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
+    // NGP (ORDER = 0) has no interpolation arithmetic to lighten: the float64 kernel
+    if (P.order == 0) return launch_propagate<true>(T, C, P, d_launch, n, O, stream);
     const int tpb = kFastThreads;
     static int blocks_per_sm = 0, sms = 0;
     static unsigned long long* queue = nullptr;   // one work counter per process (calls on a stream are ordered)
@@ -97,6 +101,7 @@ cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const P
 cudaError_t launch_gather_fast(const DevTree& T, int kind, const double* d_xyz, long long n, void* d_out, cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
+    if (kind == 3) return launch_gather_exact(T, kind, d_xyz, n, d_out, stream);   // NGP: a copy of the cell's record
     k_gather_rec<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(T, kind, d_xyz, n, d_out);
     return cudaGetLastError();
 }

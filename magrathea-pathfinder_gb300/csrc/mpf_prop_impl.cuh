@@ -17,7 +17,8 @@ __global__ void k_gather(DevTree T, int kind, const double* __restrict__ xyz, lo
         ((long long*)out)[i] = locate(T, x, y, z).cell;
         return;
     }
-    const Field7 f = (kind == 1) ? cic<EXACT>(T, x, y, z, true) : tsc<EXACT>(T, x, y, z, true);
+    // kind 1: CIC, 2: TSC, 3: NGP
+    const Field7 f = (kind == 1) ? cic<EXACT>(T, x, y, z, true) : (kind == 3) ? ngp(T, x, y, z) : tsc<EXACT>(T, x, y, z, true);
     float* o = (float*)out + 7 * i;
     o[0] = f.rho; o[1] = f.phi; o[2] = f.dx; o[3] = f.dy; o[4] = f.dz; o[5] = f.a; o[6] = f.dt;
 }

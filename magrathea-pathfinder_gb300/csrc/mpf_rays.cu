@@ -210,7 +210,7 @@ extern "C" int mpf_rays_propagate(const mpf_octree* o, const mpf_cosmology* c, c
 {
     if (!o || !c || !p || !bp || n < 0 || (n > 0 && (!photons || !sizes || !central)))
         return fail(MPF_BAD_INPUT, "mpf_rays_propagate: bad argument");
-    if (bp->count < 0 || !(bp->angle > 0.0) || bp->capacity < 1 || p->nsteps == 0 || (p->order != 1 && p->order != 2) ||
+    if (bp->count < 0 || !(bp->angle > 0.0) || bp->capacity < 1 || p->nsteps == 0 || p->order < 0 || p->order > 2 ||
         !(p->length > 0.0) || bp->interpolation < 0 || bp->interpolation > 6 || bp->homogeneous_level > 30)
         return fail(MPF_BAD_INPUT, "mpf_rays_propagate: bad parameters");
     if (n == 0) return MPF_OK;

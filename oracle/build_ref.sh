@@ -11,7 +11,7 @@
 #  2. Compile with the reference Makefile's flags (-O3 -std=c++17 -DEXTENT=4
 #     -DSIZEOFOCTREE=48 -DIOGROUPSIZE=1 -DMEMORY_SAVING, no -march), with
 #     single-rank MPI and inert HDF5 stand-ins from oracle/stubs/.
-#     Outputs: libref_o1.so / libref_o2.so (ref_harness.cpp at ORDER=1 / 2)
+#     Outputs: libref_o0.so / libref_o1.so / libref_o2.so (ref_harness.cpp at ORDER=0 / 1 / 2)
 #     and the reference's own create_octree executable.
 #  -ffp-contract=off keeps the x86 and Arm builds free of FMA contraction, as
 #  the reference's x86-64 build is.
@@ -30,7 +30,7 @@ CXX="${CXX:-g++}"
 FLAGS=(-O3 -std=c++17 -ffp-contract=off -DEXTENT=4 -DSIZEOFOCTREE=48 -DIOGROUPSIZE=1 -DMEMORY_SAVING
        -w -I"$HERE/stubs" -I"$OUT/patched" -I"$SRC" -I"$SRC/magrathea")
 pids=()
-for o in 1 2; do
+for o in 0 1 2; do
     "$CXX" "${FLAGS[@]}" -DORDER=$o -fPIC -shared "$HERE/ref_harness.cpp" -o "$OUT/libref_o$o.so" -lpthread &
     pids+=($!)
 done

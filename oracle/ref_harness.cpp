@@ -191,6 +191,11 @@ void ref_batch_locate(int64_t n, const double* xyz, int64_t* out, int nthreads)
     run_threads(n, nthreads, [&](int64_t i) { out[i] = ref_locate(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]); });
 }
 
+void ref_batch_ngp(int64_t n, const double* xyz, float* out, int nthreads)
+{
+    run_threads(n, nthreads, [&](int64_t i) { data7(g_octree.ngp(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]), out + 7 * i); });
+}
+
 void ref_batch_cic(int64_t n, const double* xyz, float* out, int nthreads)
 {
     run_threads(n, nthreads, [&](int64_t i) { data7(g_octree.cic(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]), out + 7 * i); });

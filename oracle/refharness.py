@@ -45,7 +45,7 @@ def lib(order: int = 2):
         L.ref_key_containing.argtypes = [C.c_uint64] * 4
         L.ref_locate.restype = _i64
         L.ref_locate.argtypes = [_d, _d, _d]
-        for f in ("ref_batch_locate", "ref_batch_cic", "ref_batch_tsc"):
+        for f in ("ref_batch_locate", "ref_batch_cic", "ref_batch_tsc", "ref_batch_ngp"):
             getattr(L, f).argtypes = [_i64, _p, _p, C.c_int]
         L.ref_seq_tsc.argtypes = [_i64, _p, _p]
         L.ref_cosmology.restype = _i64
@@ -113,6 +113,12 @@ class Reference:
         xyz = np.ascontiguousarray(xyz, dtype=np.float64)
         out = np.zeros(xyz.shape[0], dtype=np.int64)
         self.L.ref_batch_locate(xyz.shape[0], _ptr(xyz), _ptr(out), self.nthreads)
+        return out
+
+    def ngp(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        out = np.zeros((xyz.shape[0], 7), dtype=np.float32)
+        self.L.ref_batch_ngp(xyz.shape[0], _ptr(xyz), _ptr(out), self.nthreads)
         return out
 
     def cic(self, xyz):

@@ -169,6 +169,16 @@ def make(name, cfg):
                 out["ref_cat_bundle_o%d_a%d_%s_%s" % (order, ia, plane, sb)] = R.catalogue(
                     out["cat_src"], CAT_ACCURACIES[ia], cfg["nsteps"], out["cosmo_h"], out["cosmo_mpc"], CAT_VOBS,
                     None, "bundle", plane, sb, OPENING)
+    # ORDER = 0 (nearest grid point, simplehyperoctree.h:1396-1401): point
+    # gathers, rays, maps and catalogue rows of the reference built with it
+    R = Reference(0)
+    R.cosmology(celldir, pf, ef)
+    R.load(binpath)
+    out["ref_ngp"] = R.ngp(pts)
+    out["ref_steps_o0"], out["ref_final_o0"], _ = R.integrate(launch, "redshift", cfg["zs"][-1], cfg["nsteps"])
+    out["ref_maps_o0"] = R.fillmap(cfg["nside"], out["zs"], pix, "redshift", COMPONENTS, cfg["nsteps"])
+    out["ref_cat_o0_a0"] = R.catalogue(out["cat_src"], CAT_ACCURACIES[0], cfg["nsteps"], out["cosmo_h"],
+                                       out["cosmo_mpc"], CAT_VOBS)
     path = os.path.join(HERE, "%s.npz" % name)
     np.savez_compressed(path, **out)
     print("%s: %d cells (levels %d-%d), %d rays, %d pixels -> %s (%d KB)" % (
@@ -271,7 +281,8 @@ CELLS_CORRECTIONS = {"full": dict(correction=1, coarsecorrection=1), "nocorr": d
                      "acorr": dict(correction=1, coarsecorrection=1, acorrection=1),
                      "nocorr_acorr": dict(correction=0, coarsecorrection=0, acorrection=1),
                      # the reference built with ORDER=1: CIC gathers for the completed children
-                     "full_o1": dict(correction=1, coarsecorrection=1, order=1)}
+                     "full_o1": dict(correction=1, coarsecorrection=1, order=1),
+                     "full_o0": dict(correction=1, coarsecorrection=1, order=0)}
 
 
 def make_cells():

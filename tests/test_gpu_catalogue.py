@@ -192,3 +192,13 @@ def test_catalogue_born_matches_reference(cat_setup, pkg, order, exact):
         plain = g["ref_cat_o%d_a%d" % (order, ia)]
         conv = (ref[:, 5] != 42) & (ref[:, 2] != 42)
         assert np.abs(ref[conv, 12:16] - plain[conv, 12:16]).max() > 1e-9
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_catalogue_ngp_matches_reference(cat_setup, pkg, exact):
+    """ORDER = 0: the catalogue of the reference built with NGP gathers (the
+    rays run through the float64 kernel in both modes)."""
+    g, tree, cos = cat_setup
+    rows, stats, rc = _run(pkg, g, tree, cos, 0, exact, float(g["cat_accuracy"][0]))
+    assert rc == 0
+    assert _compare(rows, g["ref_cat_o0_a0"], True) >= 30

@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 # correction / coarsecorrection / acorrection of Input::correct and the
 # gather order of the completed children, as in the fixture
 CORRECTIONS = {"full": (1, 1, 0, 2), "nocorr": (0, 0, 0, 2), "nocorr_coarse": (0, 1, 0, 2), "corr_nocoarse": (1, 0, 0, 2),
-               "acorr": (1, 1, 1, 2), "nocorr_acorr": (0, 0, 1, 2), "full_o1": (1, 1, 0, 1)}
+               "acorr": (1, 1, 1, 2), "nocorr_acorr": (0, 0, 1, 2), "full_o1": (1, 1, 0, 1), "full_o0": (1, 1, 0, 0)}
 
 
 @pytest.fixture(scope="module", params=sorted(CORRECTIONS))

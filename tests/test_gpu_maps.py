@@ -24,7 +24,7 @@ def test_pix2vec_matches_harness(gpu_lib, pkg, golden):
     assert abs(allv[:, 2].mean()) < 1e-12     # equal-area pixels: zero mean z
 
 
-@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("order", [0, 1, 2])
 @pytest.mark.parametrize("exact", [True, False])
 def test_hmaps_fill_matches_reference_fillmap(gpu_lib, pkg, golden, order, exact):
     tree = pkg.Octree.from_records(golden["records"])

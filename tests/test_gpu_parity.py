@@ -174,3 +174,22 @@ def test_unsorted_records_are_refused(gpu_lib, pkg, golden):
     h = ctypes.c_void_p()
     assert L.mpf_octree_upload(ctypes.c_void_p(rec.ctypes.data), rec.shape[0], ctypes.byref(h)) == -4
     assert not h.value
+
+
+# ORDER = 0 (nearest grid point, simplehyperoctree.h:1396-1401): the reference
+# built with it gives the fixture's ref_*_o0 entries; NGP has no interpolation
+# arithmetic, so both modes run the float64 kernel and match bit for bit.
+def test_ngp_bit_exact(dev, golden):
+    tree, _ = dev
+    np.testing.assert_array_equal(tree.ngp(golden["pts"]).view(np.uint32), golden["ref_ngp"].view(np.uint32))
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_propagate_ngp_bit_exact(dev, golden, pkg, exact):
+    tree, cos = dev
+    steps, final, _, rc = pkg.propagate(tree, cos, golden["launch"], float(golden["cosmo_length"]),
+                                        nsteps=int(golden["nsteps"]), order=0, stop="redshift",
+                                        stop_value=float(golden["zs"][-1]), exact=exact, jacobian=False)
+    assert rc == 0
+    np.testing.assert_array_equal(steps, golden["ref_steps_o0"])
+    np.testing.assert_array_equal(final.view(np.uint64), golden["ref_final_o0"].view(np.uint64))
