@@ -29,7 +29,10 @@ def built(request, gpu_lib, pkg):
                           coarsecorrection=bool(coarse), acorrection=bool(acorr))
     if acorr:
         rec, amin = rec
-        # the table's first value: one shell below the smallest a, extrapolated
+        # the table's first value: one shell below the smallest a, extrapolated.  The
+        # reference's table also holds the last cell's a, which its update() combines
+        # with the element past the container (undefined there); the fixture comes from a
+        # fresh process, where that element's a is 0 and stays out of the table.
         assert amin == float(g["ref_amin_" + request.param])
     yield g, rec, g["ref_records_" + request.param]
     cos.close()
