@@ -387,7 +387,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=131072)
+    ap.add_argument("--batch", type=int, default=262144,
+                    help="rays per step (the persistent launch's tail of long rays is a smaller share of a larger batch)")
     ap.add_argument("--workload", default="amr", choices=["amr", "medium", "small"],
                     help="amr = the benchmark configuration; medium / small for profiling and debugging")
     ap.add_argument("--exact", action="store_true", help="reference float64 gather order")
