@@ -6,6 +6,9 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <map>
+#include <mutex>
+#include <utility>
 
 namespace mpf {
 cudaError_t launch_gather_exact(const DevTree& T, int kind, const double* d_xyz, long long n, void* d_out, cudaStream_t stream);
@@ -50,6 +53,36 @@ static int fast_launch_shape(long long n, int blocks_per_sm, int sms, long long*
     return kFastThreads;
 }
 
+// Work-queue counter and occupancy of the persistent kernel, per (device,
+// stream): calls on one stream are ordered and may share a counter; calls on
+// different streams (or devices) may run at the same time and must not.
+struct FastLaunchState {
+    unsigned long long* queue = nullptr;
+    int blocks_per_sm = 0, sms = 0;
+};
+static cudaError_t fast_launch_state(cudaStream_t stream, FastLaunchState* out)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, cudaStream_t>, FastLaunchState> states;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    FastLaunchState& s = states[{dev, stream}];
+    if (!s.queue) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s.blocks_per_sm, k_propagate_fast<2, false, false>, kFastThreads, 0);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s.sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaMalloc(&s.queue, sizeof(unsigned long long));
+        if (e != cudaSuccess) {
+            s = FastLaunchState{};
+            return e;
+        }
+        if (s.blocks_per_sm < 1) s.blocks_per_sm = 1;
+    }
+    *out = s;
+    return cudaSuccess;
+}
+
 template <>
 cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* d_launch, long long n,
                                     const PropOut& O, cudaStream_t stream)
@@ -57,22 +90,14 @@ cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const P
     if (n <= 0) return cudaSuccess;
     // NGP (ORDER = 0) has no interpolation arithmetic to lighten: the float64 kernel
     if (P.order == 0) return launch_propagate<true>(T, C, P, d_launch, n, O, stream);
-    const int tpb = kFastThreads;
-    static int blocks_per_sm = 0, sms = 0;
-    static unsigned long long* queue = nullptr;   // one work counter per process (calls on a stream are ordered)
-    if (blocks_per_sm == 0) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_propagate_fast<2, false, false>, tpb, 0);
-        int dev = 0;
-        if (e == cudaSuccess) e = cudaGetDevice(&dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = cudaMalloc(&queue, sizeof(unsigned long long));
-        if (e != cudaSuccess) { blocks_per_sm = 0; return e; }
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
-    }
-    cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), stream);
+    FastLaunchState st;
+    cudaError_t e = fast_launch_state(stream, &st);
+    if (e != cudaSuccess) return e;
+    unsigned long long* const queue = st.queue;
+    e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     long long grid = 0;
-    const int tpb_used = fast_launch_shape(n, blocks_per_sm, sms, &grid);
+    const int tpb_used = fast_launch_shape(n, st.blocks_per_sm, st.sms, &grid);
     // MPF_STATS=1: count record-path gathers and slow-path fallbacks (diagnostics; serialises the call)
     static const bool want_stats = getenv("MPF_STATS") != nullptr;
     PropOut o2 = O;
