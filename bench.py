@@ -411,6 +411,7 @@ def main():
                           if args.workload == "amr" else "%s octree (profiling / debugging)" % args.workload,
               "rays": 1000 * 1000, "batch_rays": args.batch, "order": "TSC", "nsteps": 8, "z_stop": args.zstop,
               "gather_arithmetic": "float64 reference order" if args.exact else "fp32 gather, fp64 state",
+              "streams": "steps alternate between 2 CUDA streams (a batch's tail overlaps the next batch)",
               "l2": "octree larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single GPU"}
     cos = cosmology_table(synth)
     length = spec.lbox * synth.MPC / spec.cosmo.h
@@ -470,19 +471,23 @@ def main():
     dev = torch.device("cuda", local)
     d_launch = torch.from_numpy(launch).to(dev)
     d_steps = torch.zeros((args.warmup + args.steps, B), dtype=torch.int64, device=dev)
-    d_planes = torch.zeros(B * 1 * capi.MPF_PLANE_FIELDS, dtype=torch.float64, device=dev)
+    # two streams: step k runs on streams[k % 2] with its own output buffer, so
+    # a batch's last long rays overlap the start of the next batch instead of
+    # leaving SMs idle (the map driver gets the same from its 4M-pixel launches)
+    streams = [torch.cuda.current_stream(dev), torch.cuda.Stream(dev)]
+    d_planes = [torch.zeros(B * 1 * capi.MPF_PLANE_FIELDS, dtype=torch.float64, device=dev) for _ in streams]
     d_status = torch.zeros(1, dtype=torch.int32, device=dev)
     p, keep = capi.make_params(length, nsteps=8, order=2, stop="redshift", planes=planes, jacobian=True,
                                exact=args.exact)
-    stream = torch.cuda.current_stream(dev)
+    stream = streams[0]
 
     replicas = importlib.import_module(PKG + ".replicas")
 
     def step(k):
         off = replicas.batch_ids(k, rank, world, nb) * B
         rc = lib.mpf_propagate_device(tree._h, cosmo._h, C.byref(p), B, C.c_void_p(d_launch.data_ptr() + off * 48),
-                                      C.c_void_p(d_steps[k].data_ptr()), None, C.c_void_p(d_planes.data_ptr()),
-                                      C.c_void_p(d_status.data_ptr()), C.c_void_p(stream.cuda_stream))
+                                      C.c_void_p(d_steps[k].data_ptr()), None, C.c_void_p(d_planes[k % 2].data_ptr()),
+                                      C.c_void_p(d_status.data_ptr()), C.c_void_p(streams[k % 2].cuda_stream))
         capi.check(rc)
 
     for k in range(args.warmup):
@@ -492,21 +497,17 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    launch_ms = []
     with Clocks(local) as clk:
         ev0.record(stream)
+        streams[1].wait_event(ev0)
         for k in range(args.steps):
-            e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e_a.record(stream)
             step(args.warmup + k)
-            e_b.record(stream)
-            launch_ms.append((e_a, e_b))
+        stream.wait_stream(streams[1])
         ev1.record(stream)
         torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
     elapsed_ms = ev0.elapsed_time(ev1)
-    per_launch = [a.elapsed_time(b) for a, b in launch_ms]
     photon_steps = int(d_steps[args.warmup:].sum().item())
     status = int(d_status.item())
     t_max, total_steps = replicas.reduce_counters(dist, elapsed_ms, photon_steps, dev)
@@ -528,7 +529,9 @@ def main():
     e2e_value = e2e_steps / sum(e2e_t) if e2e_t else None
 
     peak, peak_kind = measured_peak_hbm()
-    avg_launch_s = (sum(per_launch) / len(per_launch)) / 1000.0
+    # consecutive launches overlap (two streams): a launch's share of the
+    # timed region is its duration
+    avg_launch_s = (elapsed_ms / args.steps) / 1000.0
     bytes_per_launch = (photon_steps / args.steps) * BYTES_PER_PHOTON_STEP
     achieved = bytes_per_launch / avg_launch_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
