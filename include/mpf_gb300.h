@@ -5,8 +5,9 @@
  * warning); mpf_last_error() gives a message for the calling thread.
  *
  * Handles (mpf_octree, mpf_cosmology) own device memory on the device that
- * was current when they were created; they are not re-entrant: one host
- * thread at a time per handle.  Buffers passed to the mpf_* calls below are
+ * was current when they were created and are read-only afterwards: calls
+ * from several host threads on different streams may share them.  An
+ * mpf_surrogate changes when it is trained: one host thread at a time.  Buffers passed to the mpf_* calls below are
  * HOST memory unless the name ends in _device.
  *
  * Each entry point names the reference interface it stands in for

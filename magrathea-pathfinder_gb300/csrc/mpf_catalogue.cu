@@ -458,12 +458,16 @@ __global__ void k_list_flags(long long m, const int* __restrict__ list, const in
 namespace {
 unsigned blocks(long long n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
 
+// Scratch of one call, stream-ordered (cudaMallocAsync / cudaFreeAsync), so
+// that calls on different streams neither wait for one another nor for the
+// whole device when they free.
 struct CatBuffers {
     void* p[21] = {};
+    cudaStream_t stream = nullptr;
     ~CatBuffers()
     {
         for (void* q : p)
-            if (q) cudaFree(q);
+            if (q) cudaFreeAsync(q, stream);
     }
 };
 }  // namespace
@@ -482,10 +486,11 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
     const int tpb = 128;
     const long long ntiles = (n + kSortTile - 1) / kSortTile;
     CatBuffers B;
+    B.stream = stream;
     cudaError_t e = cudaSuccess;
     auto alloc = [&](int k, size_t bytes) -> void* {
         if (e != cudaSuccess) return nullptr;
-        e = cudaMalloc(&B.p[k], bytes);
+        e = cudaMallocAsync(&B.p[k], bytes, stream);
         return (e == cudaSuccess) ? B.p[k] : nullptr;
     };
     CatState* state = (CatState*)alloc(0, (size_t)n * sizeof(CatState));
