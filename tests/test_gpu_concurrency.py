@@ -1,0 +1,63 @@
+"""Concurrent calls: two host threads, each on its own CUDA stream, sharing
+one octree and one cosmology handle (read-only after creation).  The
+persistent fast kernel keeps one work-queue counter per (device, stream), so
+the two launches may overlap; each thread's results equal those of the same
+batch traced alone."""
+import ctypes as C
+import threading
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_two_streams_share_the_handles(gpu_lib, pkg, golden):
+    torch = pytest.importorskip("torch")
+    from importlib import import_module
+    capi = import_module(pkg.__name__ + ".capi")
+    tree = pkg.Octree.from_records(golden["records"])
+    cos = pkg.Cosmology(golden["cosmo_t"], golden["cosmo_a"], golden["cosmo_dadt"], golden["cosmo_d2adt2"])
+    length = float(golden["cosmo_length"])
+    base = np.asarray(golden["launch"], dtype=np.float64)
+    # two different batches: the golden rays and the same rays mirrored in y
+    batches = [np.tile(base, (16, 1)), np.tile(base * np.array([1, -1, 1, 1, -1, 1.0]), (16, 1))]
+    ref = [pkg.propagate(tree, cos, b, length, nsteps=int(golden["nsteps"]), order=2, stop="redshift",
+                         stop_value=float(golden["zs"][-1]), exact=False, jacobian=True)[0] for b in batches]
+    p, keep = capi.make_params(length, int(golden["nsteps"]), 2, "redshift", float(golden["zs"][-1]), None, True, False, 0)
+    L = pkg.library()
+    dev = torch.device("cuda", 0)
+    out = [None, None]
+    errors = []
+
+    def lane(j):
+        try:
+            torch.cuda.set_device(0)
+            s = torch.cuda.Stream(dev)
+            n = batches[j].shape[0]
+            d_l = torch.from_numpy(batches[j]).to(dev)
+            d_s = torch.zeros(n, dtype=torch.int64, device=dev)
+            d_st = torch.zeros(1, dtype=torch.int32, device=dev)
+            torch.cuda.synchronize()
+            for _ in range(3):
+                rc = L.mpf_propagate_device(tree._h, cos._h, C.byref(p), n, C.c_void_p(d_l.data_ptr()),
+                                            C.c_void_p(d_s.data_ptr()), None, None, C.c_void_p(d_st.data_ptr()),
+                                            C.c_void_p(s.cuda_stream))
+                if rc < 0:
+                    raise RuntimeError(rc)
+            s.synchronize()
+            out[j] = d_s.cpu().numpy()
+        except Exception as e:   # reported by the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=lane, args=(j,)) for j in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for j in range(2):
+        np.testing.assert_array_equal(out[j], ref[j])
+    del keep
+    tree.close()
+    cos.close()
