@@ -136,6 +136,14 @@ int64_t mpfo_locate(const mpfo_tree* T, double x, double y, double z)
     return find(T, key_compute(32, x, y, z));
 }
 
+/* SimpleHyperOctree::ngp (simplehyperoctree.h:1396-1401): the record of the
+   cell found for the position's level-32 key, or the empty record */
+void mpfo_ngp(const mpfo_tree* T, double x, double y, double z, float* res)
+{
+    const int64_t i = find(T, key_compute(32, x, y, z));
+    for (int k = 0; k < 7; ++k) res[k] = (i >= 0) ? T->fields[7 * i + k] : 0.0f;
+}
+
 void mpfo_key_compute(unsigned level, double x, double y, double z, uint64_t* out)
 {
     const u128 k = key_compute(level, x, y, z);
@@ -314,7 +322,8 @@ typedef struct {
 
 static inline void gather(ctx_t* c, double x, double y, double z, float* d)
 {
-    if (c->order == 1) mpfo_cic(c->T, x, y, z, d);
+    if (c->order == 0) mpfo_ngp(c->T, x, y, z, d);
+    else if (c->order == 1) mpfo_cic(c->T, x, y, z, d);
     else tsc_cached(c->T, &c->cache, x, y, z, d);
 }
 
@@ -680,7 +689,7 @@ int mpfo_propagate(const mpfo_tree* T, const mpfo_cosmo* C, int order, double le
                    int64_t n, const double* launch, int nplanes, const double* planes, int jacobian_on,
                    int64_t* steps, double* final_out, double* plane_out, int nthreads)
 {
-    if (!T || !C || (order != 1 && order != 2) || nsteps == 0 || n < 0) return -1;
+    if (!T || !C || (order < 0 || order > 2) || nsteps == 0 || n < 0) return -1;
     static const double zero3[3] = {0, 0, 0};
     job_t J;
     J.T = T; J.C = C; J.order = order; J.stop_kind = stop_kind; J.nplanes = nplanes; J.jac = jacobian_on;
@@ -1108,7 +1117,7 @@ int mpfo_catalogue_jac(const mpfo_tree* T, const mpfo_cosmo* C, int order, doubl
                        double h, double mpc, int max_iterations, int bundle, int plane_sachs, int stop_bundle,
                        double openingmin, double* out, int nthreads)
 {
-    if (!T || !C || (order != 1 && order != 2) || nsteps == 0 || n < 0 || !vobs) return -1;
+    if (!T || !C || (order < 0 || order > 2) || nsteps == 0 || n < 0 || !vobs) return -1;
     cjob_t J;
     J.bundle = bundle; J.plane_sachs = plane_sachs; J.stop_bundle = stop_bundle; J.openingmin = openingmin;
     J.T = T; J.C = C; J.order = order; J.max_iterations = max_iterations; J.length = length;
@@ -1302,7 +1311,7 @@ int mpfo_bundle(const mpfo_tree* T, const mpfo_cosmo* C, int order, double lengt
                 int64_t n, const double* launch, int np, const double* planes, int plane_sachs, int stop_bundle,
                 double openingmin, double* plane_out, double* jac_out, int nthreads)
 {
-    if (!T || !C || (order != 1 && order != 2) || nsteps == 0 || n < 0 || np < 1 || !planes) return -1;
+    if (!T || !C || (order < 0 || order > 2) || nsteps == 0 || n < 0 || np < 1 || !planes) return -1;
     bjob_t J;
     J.T = T; J.C = C; J.order = order; J.stop_kind = stop_kind; J.np = np; J.plane_sachs = plane_sachs;
     J.stop_bundle = stop_bundle; J.length = length; J.openingmin = openingmin; J.nsteps = nsteps;
@@ -1335,6 +1344,7 @@ static void* gworker(void* arg)
         const double* p = g->xyz + 3 * i;
         if (g->kind == 0) ((int64_t*)g->out)[i] = mpfo_locate(g->T, p[0], p[1], p[2]);
         else if (g->kind == 1) mpfo_cic(g->T, p[0], p[1], p[2], (float*)g->out + 7 * i);
+        else if (g->kind == 3) mpfo_ngp(g->T, p[0], p[1], p[2], (float*)g->out + 7 * i);
         else mpfo_tsc(g->T, p[0], p[1], p[2], (float*)g->out + 7 * i);
     }
     return 0;
@@ -1357,3 +1367,4 @@ static void gbatch(const mpfo_tree* T, int64_t n, const double* xyz, void* out, 
 void mpfo_batch_locate(const mpfo_tree* T, int64_t n, const double* xyz, int64_t* out, int nthreads) { gbatch(T, n, xyz, out, 0, nthreads); }
 void mpfo_batch_cic(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads) { gbatch(T, n, xyz, out, 1, nthreads); }
 void mpfo_batch_tsc(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads) { gbatch(T, n, xyz, out, 2, nthreads); }
+void mpfo_batch_ngp(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads) { gbatch(T, n, xyz, out, 3, nthreads); }

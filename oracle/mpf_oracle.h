@@ -50,6 +50,7 @@ unsigned mpfo_key_level(uint64_t hi, uint64_t lo);
 int64_t mpfo_locate(const mpfo_tree* T, double x, double y, double z);
 void mpfo_cic(const mpfo_tree* T, double x, double y, double z, float* out7);
 void mpfo_tsc(const mpfo_tree* T, double x, double y, double z, float* out7);
+void mpfo_ngp(const mpfo_tree* T, double x, double y, double z, float* out7);
 double mpfo_interpolate(double x0, const double* x, const double* y, int64_t n);
 
 /* Batch of rays.  launch: n x 6 (start xyz, end xyz, the 6-argument
@@ -108,6 +109,7 @@ int mpfo_bundle(const mpfo_tree* T, const mpfo_cosmo* C, int order, double lengt
 void mpfo_batch_locate(const mpfo_tree* T, int64_t n, const double* xyz, int64_t* out, int nthreads);
 void mpfo_batch_cic(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads);
 void mpfo_batch_tsc(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads);
+void mpfo_batch_ngp(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads);
 
 #ifdef __cplusplus
 }

@@ -73,7 +73,7 @@ def lib():
         L.mpfo_catalogue.restype = C.c_int
         L.mpfo_catalogue.argtypes = [_p, _p, C.c_int, _d, C.c_uint, _i64, _p, _p, _p, _d, _d, _d, C.c_int, _p,
                                      C.c_int]
-        for f in ("mpfo_batch_locate", "mpfo_batch_cic", "mpfo_batch_tsc"):
+        for f in ("mpfo_batch_locate", "mpfo_batch_cic", "mpfo_batch_tsc", "mpfo_batch_ngp"):
             getattr(L, f).argtypes = [_p, _i64, _p, _p, C.c_int]
         _lib = L
     return _lib
@@ -118,6 +118,12 @@ class Oracle:
         xyz = np.ascontiguousarray(xyz, dtype=np.float64)
         out = np.zeros((xyz.shape[0], 7), dtype=np.float32)
         self.L.mpfo_batch_tsc(C.byref(self.tree), xyz.shape[0], _ptr(xyz), _ptr(out), self.nthreads)
+        return out
+
+    def ngp(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        out = np.zeros((xyz.shape[0], 7), dtype=np.float32)
+        self.L.mpfo_batch_ngp(C.byref(self.tree), xyz.shape[0], _ptr(xyz), _ptr(out), self.nthreads)
         return out
 
     def propagate(self, launch, order=2, nsteps=10, stop="redshift", stop_ref=0.5, planes=None, jacobian=True,

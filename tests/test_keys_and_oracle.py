@@ -125,3 +125,23 @@ def test_amr_fixture_exercises_levels(synth):
     assert lev.max() - lev.min() >= 3
     # some reference rays end in refined cells and some are longer than uniform ones
     assert len(np.unique(g["ref_final_o2"][:, 9])) >= 2
+
+
+def test_oracle_ngp_bit_exact(golden, oracle_mod, maps_mod):
+    """ORDER = 0 (nearest grid point): the oracle's point gathers, rays, maps
+    and catalogue rows equal those of the reference built at ORDER=0."""
+    O = _oracle(golden, oracle_mod)
+    np.testing.assert_array_equal(O.ngp(golden["pts"]).view(np.uint32), golden["ref_ngp"].view(np.uint32))
+    n = int(golden["nsteps"])
+    steps, final, _ = O.propagate(golden["launch"], order=0, nsteps=n, stop="redshift", stop_ref=float(golden["zs"][-1]))
+    np.testing.assert_array_equal(steps, golden["ref_steps_o0"])
+    np.testing.assert_array_equal(final.view(np.uint64), golden["ref_final_o0"].view(np.uint64))
+    dirs = golden["pixel_dirs"]
+    launch = np.zeros((dirs.shape[0], 6))
+    launch[:, 3:] = dirs
+    _, _, planes = O.propagate(launch, order=0, nsteps=n, stop="redshift", planes=golden["zs"], jacobian=True)
+    maps = maps_mod.assemble(planes, dirs, golden["homogeneous"], str(golden["components"]).split(","))
+    np.testing.assert_array_equal(maps.view(np.uint32), golden["ref_maps_o0"].view(np.uint32))
+    rows = O.catalogue(golden["cat_src"], cat_accuracy=float(golden["cat_accuracy"][0]), order=0, nsteps=n,
+                       h=float(golden["cosmo_h"]), mpc=float(golden["cosmo_mpc"]), vobs=golden["cat_vobs"])
+    np.testing.assert_array_equal(rows.view(np.uint64), golden["ref_cat_o0_a0"].view(np.uint64))
