@@ -318,10 +318,16 @@ typedef struct {
     int order;
     double length;
     tsc_cache cache;
+    int homogeneous;   /* Order = -1 (integrator.h:425, 676, 744): the homogeneous field, the octree's levels */
 } ctx_t;
 
 static inline void gather(ctx_t* c, double x, double y, double z, float* d)
 {
+    if (c->homogeneous) {   /* a = 1, the rest 0; dphotondl reads only the zero gradient and dphidt */
+        zero7(d);
+        d[5] = 1.0f;   /* a, the record order rho phi dx dy dz a dt */
+        return;
+    }
     if (c->order == 0) mpfo_ngp(c->T, x, y, z, d);
     else if (c->order == 1) mpfo_cic(c->T, x, y, z, d);
     else tsc_cached(c->T, &c->cache, x, y, z, d);
@@ -659,7 +665,7 @@ static int64_t take(job_t* J)
 static void* worker(void* arg)
 {
     job_t* J = (job_t*)arg;
-    ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+    ctx_t* c = (ctx_t*)calloc(1, sizeof(ctx_t));
     traj_t tr = {0, 0, 0};
     for (int64_t i; (i = take(J)) < J->n;) {
         c->T = J->T;
@@ -712,7 +718,7 @@ int64_t mpfo_trajectory(const mpfo_tree* T, const mpfo_cosmo* C, int order, doub
                         int stop_kind, double stop_ref, const double* launch, double* out, int64_t cap)
 {
     static const double zero3[3] = {0, 0, 0};
-    ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+    ctx_t* c = (ctx_t*)calloc(1, sizeof(ctx_t));
     c->T = T; c->C = C; c->order = order; c->length = length;
     cache_init(&c->cache);
     traj_t tr = {0, 0, 0};
@@ -796,7 +802,7 @@ int64_t mpfo_propagate_bundle(const mpfo_tree* T, const mpfo_cosmo* C, int order
         }
     }
     /* each ray integrated without a stop criterion (integrator.h:477-618) */
-    ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+    ctx_t* c = (ctx_t*)calloc(1, sizeof(ctx_t));
     c->T = T; c->C = C; c->order = order; c->length = length;
     traj_t* trs = (traj_t*)calloc(total, sizeof(traj_t));
     double* last = (double*)calloc(total, sizeof(double));
@@ -924,7 +930,7 @@ static void newton2d(ctx_t* c, traj_t* tr, traj_t* trb, const cjob_t* J, const d
     fp[2] = P0[PZ] * f + P1[PZ] * (1 - f);
     /* jacobiantype = bundle: the screen normal and the bundle's stop value (catalogues.h:458-495) */
     double kiT[3] = {0, 0, 0}, iref = 0;
-    if (J->bundle) {
+    if (J->bundle == 1) {
         if (J->plane_sachs) {
             kiT[0] = P0[PK1] * f + P1[PK1] * (1 - f);
             kiT[1] = P0[PK2] * f + P1[PK2] * (1 - f);
@@ -945,7 +951,7 @@ static void newton2d(ctx_t* c, traj_t* tr, traj_t* trb, const cjob_t* J, const d
     res[1][0] = dist_sep / dist;
     if (res[1][0] > J->accuracy) {
         double ji[2][2] = {{1, 0}, {0, 1}};
-        if (iteration >= 5 && J->bundle) {
+        if (iteration >= 5 && J->bundle == 1) {
             double B[4];
             dbetadtheta(c, trb, J->nsteps, J->stop_bundle, J->openingmin, 1, kiT, &iref, &dist, phi, theta, B);
             if (B[0] == 42 && B[1] == 42) {
@@ -998,7 +1004,18 @@ static void newton2d(ctx_t* c, traj_t* tr, traj_t* trb, const cjob_t* J, const d
         return;
     }
     /* converged: Jacobian and redshift decomposition (catalogues.h:660-723) */
-    if (J->bundle) {
+    if (J->bundle == 2) {
+        /* infinitesimal_born (catalogues.h:670-673): the Order = -1 ray of the
+           same launch to the source radius, the Jacobian along it */
+        ctx_t cb = *c;
+        cb.homogeneous = 1;
+        trb->n = 0;
+        launch5(phi, theta, traj_push(trb));
+        integrate(&cb, trb, J->nsteps, MPFO_STOP_R, dist, (const double[3]){0, 0, 0});
+        double A[3];
+        jacobian(&cb, trb, 1, &dist, A);
+        jac[0][0] = A[0]; jac[0][1] = A[1]; jac[1][0] = A[1]; jac[1][1] = A[2];
+    } else if (J->bundle) {
         double B[4];
         dbetadtheta(c, trb, J->nsteps, J->stop_bundle, J->openingmin, 1, kiT, &iref, &dist, phi, theta, B);
         jac[0][0] = B[0]; jac[0][1] = B[1]; jac[1][0] = B[2]; jac[1][1] = B[3];
@@ -1036,6 +1053,36 @@ static void newton2d(ctx_t* c, traj_t* tr, traj_t* trb, const cjob_t* J, const d
     z[5] = gK / gref - 1;
     res[0][0] = phi;
     res[0][1] = theta;
+}
+
+/* FillMap's lensing_born rays (hmaps.h:706-712): per launch (6-argument
+ * form), the Order = -1 ray (homogeneous field, the octree's levels for the
+ * steps) to stop_ref of stop_kind, then Lensing::dbetadtheta_infinitesimal
+ * along it at the nd distances (the FLRW surface distances).  size: the
+ * Born trajectory sizes; A: n x nd x 3 (a11 a12 a22). */
+int mpfo_born(const mpfo_tree* T, const mpfo_cosmo* C, double length, unsigned nsteps, int stop_kind, double stop_ref,
+              int64_t n, const double* launch, int nd, const double* dist, int64_t* size, double* A)
+{
+    if (!T || !C || nsteps == 0 || n < 0 || nd < 1 || !launch || !dist || !size || !A) return -1;
+    ctx_t* c = (ctx_t*)calloc(1, sizeof(ctx_t));
+    traj_t tr = {0, 0, 0};
+    const double zero3[3] = {0, 0, 0};
+    for (int64_t i = 0; i < n; ++i) {
+        c->T = T;
+        c->C = C;
+        c->order = 2;
+        c->length = length;
+        c->homogeneous = 1;
+        cache_init(&c->cache);
+        tr.n = 0;
+        launch6(launch + 6 * i, traj_push(&tr));
+        integrate(c, &tr, nsteps, stop_kind, stop_ref, zero3);
+        size[i] = tr.n;
+        jacobian(c, &tr, nd, dist, A + (int64_t)3 * nd * i);
+    }
+    free(tr.p);
+    free(c);
+    return 0;
 }
 
 /* Catalogues::iterateNewtonMethod (catalogues.h:757-783) behind relCat's
@@ -1084,7 +1131,7 @@ static void catalogue_one(ctx_t* c, traj_t* tr, traj_t* trb, const cjob_t* J, in
 static void* cworker(void* arg)
 {
     cjob_t* J = (cjob_t*)arg;
-    ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+    ctx_t* c = (ctx_t*)calloc(1, sizeof(ctx_t));
     traj_t tr = {0, 0, 0}, trb = {0, 0, 0};
     for (;;) {
         pthread_mutex_lock(&J->mu);
@@ -1251,7 +1298,7 @@ typedef struct {
 static void* bworker(void* arg)
 {
     bjob_t* J = (bjob_t*)arg;
-    ctx_t* c = (ctx_t*)malloc(sizeof(ctx_t));
+    ctx_t* c = (ctx_t*)calloc(1, sizeof(ctx_t));
     traj_t tr = {0, 0, 0}, trb = {0, 0, 0};
     const int np = J->np;
     double* ki = (double*)malloc(sizeof(double) * 3 * (size_t)np);

@@ -78,14 +78,21 @@ int64_t mpfo_trajectory(const mpfo_tree* T, const mpfo_cosmo* C, int order, doub
 int mpfo_catalogue(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
                    int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
                    double h, double mpc, int max_iterations, double* out, int nthreads);
-/* Same with the Jacobian type: bundle != 0 is jacobiantype = "bundle" (the
+/* Same with the Jacobian type: bundle = 1 is jacobiantype = "bundle" (the
  * four-ray Lensing::dbetadtheta from iteration 5 and at convergence), with
  * plane_sachs (1: "sachs", 0: "normal"), stop_bundle (MPFO_STOP_*) and
- * openingmin (radians). */
+ * openingmin (radians); bundle = 2 is "infinitesimal_born" (the converged
+ * source's Jacobian along its Order = -1 ray). */
 int mpfo_catalogue_jac(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps,
                        int64_t n, const double* src, const double* rotm1, const double* vobs, double cat_accuracy,
                        double h, double mpc, int max_iterations, int bundle, int plane_sachs, int stop_bundle,
                        double openingmin, double* out, int nthreads);
+
+/* FillMap's lensing_born rays (hmaps.h:706-712): the Order = -1 ray of each
+ * 6-argument launch to stop_ref, and the infinitesimal Jacobian along it at
+ * the nd distances dist; size[n], A[n x nd x 3] (a11 a12 a22). */
+int mpfo_born(const mpfo_tree* T, const mpfo_cosmo* C, double length, unsigned nsteps, int stop_kind, double stop_ref,
+              int64_t n, const double* launch, int nd, const double* dist, int64_t* size, double* A);
 
 /* Hmaps::FillMap with jacobiantype = "bundle": the central rays' surfaces
  * (plane_out, n x np x 20 as mpfo_propagate, without the infinitesimal

@@ -70,6 +70,8 @@ def lib():
         L.mpfo_catalogue_jac.restype = C.c_int
         L.mpfo_catalogue_jac.argtypes = [_p, _p, C.c_int, _d, C.c_uint, _i64, _p, _p, _p, _d, _d, _d, C.c_int,
                                          C.c_int, C.c_int, C.c_int, _d, _p, C.c_int]
+        L.mpfo_born.restype = C.c_int
+        L.mpfo_born.argtypes = [_p, _p, _d, C.c_uint, C.c_int, _d, _i64, _p, C.c_int, _p, _p, _p]
         L.mpfo_catalogue.restype = C.c_int
         L.mpfo_catalogue.argtypes = [_p, _p, C.c_int, _d, C.c_uint, _i64, _p, _p, _p, _d, _d, _d, C.c_int, _p,
                                      C.c_int]
@@ -173,11 +175,25 @@ class Oracle:
         rc = self.L.mpfo_catalogue_jac(C.byref(self.tree), C.byref(self.cosmo), order, self.length, nsteps,
                                        src.shape[0], _ptr(src), _ptr(rot) if rot is not None else None, _ptr(vo),
                                        float(cat_accuracy), float(h), float(mpc), int(max_iterations),
-                                       1 if jacobiantype == "bundle" else 0, 1 if plane == "sachs" else 0,
+                                       {"bundle": 1, "infinitesimal_born": 2}.get(jacobiantype, 0),
+                                       1 if plane == "sachs" else 0,
                                        STOP[stop_bundle], float(openingmin), _ptr(out), int(nthreads or self.nthreads))
         if rc != 0:
             raise ValueError("oracle catalogue failed: %d" % rc)
         return out
+
+    def born(self, launch, dist, nsteps=10, stop="redshift", stop_ref=0.5):
+        """FillMap's lensing_born rays: (Born trajectory sizes n, Jacobians n x nd x 3)."""
+        launch = np.ascontiguousarray(launch, dtype=np.float64)
+        dist = np.ascontiguousarray(dist, dtype=np.float64)
+        n = launch.shape[0]
+        size = np.zeros(n, dtype=np.int64)
+        A = np.zeros((n, dist.shape[0], 3))
+        rc = self.L.mpfo_born(C.byref(self.tree), C.byref(self.cosmo), self.length, nsteps, STOP[stop], float(stop_ref),
+                              n, _ptr(launch), dist.shape[0], _ptr(dist), _ptr(size), _ptr(A))
+        if rc != 0:
+            raise ValueError("oracle born failed: %d" % rc)
+        return size, A
 
     def bundle(self, launch, planes, order=2, nsteps=10, stop="redshift", plane="sachs", stop_bundle="redshift",
                openingmin=0.0, nthreads=None):

@@ -145,3 +145,26 @@ def test_oracle_ngp_bit_exact(golden, oracle_mod, maps_mod):
     rows = O.catalogue(golden["cat_src"], cat_accuracy=float(golden["cat_accuracy"][0]), order=0, nsteps=n,
                        h=float(golden["cosmo_h"]), mpc=float(golden["cosmo_mpc"]), vobs=golden["cat_vobs"])
     np.testing.assert_array_equal(rows.view(np.uint64), golden["ref_cat_o0_a0"].view(np.uint64))
+
+
+def test_oracle_born_bit_exact(golden, oracle_mod, maps_mod):
+    """lensing_born (hmaps.h:706-712, 771-785) and jacobiantype =
+    infinitesimal_born (catalogues.h:670-673): the oracle's Order = -1 rays and
+    the Jacobian along them give the reference's Born map rows and catalogue
+    rows bit for bit."""
+    O = _oracle(golden, oracle_mod)
+    n = int(golden["nsteps"])
+    dirs = golden["pixel_dirs"]
+    launch = np.zeros((dirs.shape[0], 6))
+    launch[:, 3:] = dirs
+    size, A = O.born(launch, golden["homogeneous"][:, 1], nsteps=n, stop="redshift", stop_ref=float(golden["zs"][-1]))
+    a11, a12, a22 = A[..., 0], A[..., 1], A[..., 2]
+    born = np.stack([1 - (a11 + a22) * 0.5, -0.5 * (a11 - a22), -a12, a11 * a22 - a12 * a12], axis=0)  # 4 x npix x nz
+    ref = golden["ref_maps_bornonly_o2"]                                                                # nz x 4 x npix
+    got = np.where((size > 1)[None, :, None], born, 0.0).transpose(2, 0, 1).astype(np.float32)
+    np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32))
+    for ia in (0, 1):
+        rows = O.catalogue(golden["cat_src"], cat_accuracy=float(golden["cat_accuracy"][ia]), order=1, nsteps=n,
+                           h=float(golden["cosmo_h"]), mpc=float(golden["cosmo_mpc"]), vobs=golden["cat_vobs"],
+                           jacobiantype="infinitesimal_born")
+        np.testing.assert_array_equal(rows.view(np.uint64), golden["ref_cat_born_o1_a%d" % ia].view(np.uint64))
