@@ -663,11 +663,10 @@ cudaError_t catalogue_newton(const DevTree& T, const DevCosmo& Cs, const CatCons
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (K.born) {
             // the Born ray of the converged direction to the source radius
-            // (catalogues.h:670-673), through the float64 kernel (Born mode is
-            // not in the FP32-gather kernel)
+            // (catalogues.h:670-673)
             PropParams Pn = P;
             Pn.homogeneous = 2;
-            e = launch_propagate<true>(T, Cs, Pn, launch, r, O, stream);
+            e = exact ? launch_propagate<true>(T, Cs, Pn, launch, r, O, stream) : launch_propagate<false>(T, Cs, Pn, launch, r, O, stream);
         } else {
             e = exact ? launch_propagate<true>(T, Cs, P, launch, r, O, stream) : launch_propagate<false>(T, Cs, P, launch, r, O, stream);
         }

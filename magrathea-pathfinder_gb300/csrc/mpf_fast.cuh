@@ -613,7 +613,7 @@ struct JacSums {
 // SRC: source mode (one surface at the ray's own radius); WIDE: per-ray
 // surfaces and wide surface records (bundle rays).  The plain instantiation,
 // the map and benchmark path, carries neither.
-template <int ORDER, bool SRC, bool WIDE>
+template <int ORDER, bool SRC, bool WIDE, bool BORN = false>
 __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* L, long long i,
                                const PropOut& O, JacSums J)
 {
@@ -627,6 +627,14 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     const double stop_ref = SRC ? P.ray_stop[i] : ((WIDE && P.ray_planes) ? rpl[np - 1] : P.stop_ref);
     const int rec_fields = SRC ? kSourceFields : (WIDE ? kWideFields : kPlaneFields);
     unsigned long long* const st = O.stats;
+    // Born ray (Order = -1 on the octree itself: hmaps.h:706-712,
+    // catalogues.h:670-673), an instantiation of its own: the homogeneous
+    // field in the stages and after each step, the octree's levels for the
+    // step length, its field for the Jacobian
+    constexpr bool born = BORN;
+    Field7 hom;
+    clear(hom);
+    hom.a = 1.f;
     FastRec b;
     if (SRC || (WIDE && P.direct)) {
         // (phi, theta) launch form or a bundle photon: the direction is given
@@ -638,7 +646,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
     }
     Loc here = locate_full(T, b.x, b.y, b.z);
-    Field7 data = gather_at<ORDER>(T, here, PosAt{b.x, b.y, b.z}, true, st, ST_POST_REC, true);
+    Field7 data = born ? hom : gather_at<ORDER>(T, here, PosAt{b.x, b.y, b.z}, true, st, ST_POST_REC, true);
     {
         const double ph = (double)data.phi / c2;
         const double norm = sqrt((c2 * (1.0 + 2.0 * ph) * b.k0 * b.k0) / ((1.0 - 2.0 * ph) * (b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3)));
@@ -708,11 +716,14 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             if (sg == 0) {
                 rhs_math(C, data, bc, inv_a, tb, dc, kfs);
             } else {
-                const float cc = (float)pc * cells_per_unit(here.level);
-                const PosStage ps{bc[2], bc[3], bc[4], pc, pk[0], pk[1], pk[2]};
-                const Loc d = locate_rel(T, here, fmaf(cc, kfs[0], here.fd[0]), fmaf(cc, kfs[1], here.fd[1]),
-                                         fmaf(cc, kfs[2], here.fd[2]), ps);
-                const Field7 g = gather_at<ORDER>(T, d, ps, false, st, ST_RK_REC, false);
+                Field7 g = hom;
+                if (!born) {
+                    const float cc = (float)pc * cells_per_unit(here.level);
+                    const PosStage ps{bc[2], bc[3], bc[4], pc, pk[0], pk[1], pk[2]};
+                    const Loc d = locate_rel(T, here, fmaf(cc, kfs[0], here.fd[0]), fmaf(cc, kfs[1], here.fd[1]),
+                                             fmaf(cc, kfs[2], here.fd[2]), ps);
+                    g = gather_at<ORDER>(T, d, ps, false, st, ST_RK_REC, false);
+                }
                 rhs_math(C, g, core, recip(core[0]), tb, dc, kfs);
             }
             const double cs = (sg < 2) ? 0.5 * dl : dl;
@@ -734,7 +745,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         p.a = core[0]; p.t = core[1]; p.x = core[2]; p.y = core[3]; p.z = core[4];
         p.k0 = core[5]; p.k1 = core[6]; p.k2 = core[7]; p.k3 = core[8];
         const Loc ploc = locate_near(T, here, p.x, p.y, p.z);
-        data = gather_at<ORDER>(T, ploc, PosAt{p.x, p.y, p.z}, true, st, ST_POST_REC, false);
+        data = born ? hom : gather_at<ORDER>(T, ploc, PosAt{p.x, p.y, p.z}, true, st, ST_POST_REC, false);
         {
             // the extent test (integrator.h:757): a point in a located cell away from
             // the domain faces is inside; only cells on a face (or wrapped keys)
@@ -826,8 +837,9 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                         o[23] = b.k3 * f + p.k3 * (1 - f);
                     }
                     if (P.jacobian) {
-                        // at the surface's distance, or at the source radius in source mode
-                        const double jd = SRC ? ref : dist;
+                        // at the surface's distance, or at the source radius in source
+                        // mode, or at the surface radius itself for a Born ray
+                        const double jd = (SRC || born) ? ref : dist;
                         double s1[3], s2[3];
                         bool ok = true;
                         if (p.chi <= jd) {
@@ -901,6 +913,13 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             for (int q = 0; q < 24; ++q) prow[q] = 0.0;
             const long long marked = size - 1;
             prow[0] = (double)(marked - (marked > 0));
+            if (born && P.jacobian && ck < 0) {
+                // a Born ray that ends short of the radius: the Jacobian at its last point
+                const double idist = 1.0 / stop_ref;
+                prow[6] = 1.0 - 2.0 * (J.S(0) - J.S(3) * idist) / c2 * P.length;
+                prow[7] = -2.0 * (J.S(1) - J.S(4) * idist) / c2 * P.length;
+                prow[8] = 1.0 - 2.0 * (J.S(2) - J.S(5) * idist) / c2 * P.length;
+            }
         }
         prow[19] = ok ? 1.0 : 0.0;
     } else if (prow) {
@@ -915,6 +934,18 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             }
             o[19] = valid ? 1.0 : 0.0;
             if (WIDE) o[24] = found ? 1.0 : 0.0;
+            if (born) {
+                // Born ray (hmaps.h:712, 719): the Jacobian at the surface radius,
+                // from the last point when the ray never got there; only a ray
+                // that could not take a step is unusable
+                if (P.jacobian && ck < 0) {
+                    const double idist = 1.0 / rpl[j];
+                    o[6] = 1.0 - 2.0 * (J.S(0) - J.S(3) * idist) / c2 * P.length;
+                    o[7] = -2.0 * (J.S(1) - J.S(4) * idist) / c2 * P.length;
+                    o[8] = 1.0 - 2.0 * (J.S(2) - J.S(5) * idist) / c2 * P.length;
+                }
+                o[19] = (size > 1) ? 1.0 : 0.0;
+            }
         }
     }
     if (status) atomicOr(O.status, status);
@@ -929,7 +960,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
 #else
 #define MPF_FAST_BOUNDS __launch_bounds__(kFastThreads, MPF_FAST_MINB)
 #endif
-template <int ORDER, bool SRC, bool WIDE>
+template <int ORDER, bool SRC, bool WIDE, bool BORN = false>
 __global__ void MPF_FAST_BOUNDS k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
                                                                     const double* __restrict__ launch, long long n, PropOut O,
                                                                     unsigned long long* queue)
@@ -943,7 +974,7 @@ __global__ void MPF_FAST_BOUNDS k_propagate_fast(DevTree T, DevCosmo C, PropPara
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= (unsigned long long)n) break;
         const long long i = (long long)base + lane;
-        if (i < n) propagate_fast<ORDER, SRC, WIDE>(T, C, P, launch + 6 * i, i, O, J);
+        if (i < n) propagate_fast<ORDER, SRC, WIDE, BORN>(T, C, P, launch + 6 * i, i, O, J);
         __syncwarp();
     }
 }

@@ -65,8 +65,8 @@ __global__ void k_pix_launch(long long n, long long nside, const long long* __re
 // One thread per (pixel, surface): the map rows of hmaps.h:716-829.
 // rec_fields: stride of the surface records (unused with only_born); jac: the
 // bundle Jacobians (n x nz x 4: a11 a12 a21 a22) or null for the
-// infinitesimal one; born: the Born rays' surface records (n x nz x 20) or
-// null.
+// infinitesimal one; born: the Born rays' wide surface records (n x nz x 32)
+// or null.
 __global__ void k_fill_maps(long long n, int nz, MapSpec M, const double* __restrict__ launch,
                             const double* __restrict__ rec, int rec_fields, const double* __restrict__ jac,
                             const double* __restrict__ born, float* __restrict__ maps, long long row_stride,
@@ -78,7 +78,7 @@ __global__ void k_fill_maps(long long n, int nz, MapSpec M, const double* __rest
     const int iz = (int)(t / n);
     const double* o = M.only_born ? nullptr : rec + ((long long)j * nz + iz) * rec_fields;
     const double* bj = jac ? jac + ((long long)j * nz + iz) * 4 : nullptr;
-    const double* ob = born ? born + ((long long)j * nz + iz) * kPlaneFields : nullptr;
+    const double* ob = born ? born + ((long long)j * nz + iz) * kWideFields : nullptr;
     float* out = maps + (long long)M.nmaps * iz * row_stride + col0 + j;
     // a Born ray that took no step, an unusable crossing of the traced ray, or
     // a bundle Jacobian flagged 42, zeroes the surface (hmaps.h:719-738)
@@ -272,18 +272,17 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
     if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, sizeof(unsigned), stream);
     PropOut O{steps, nullptr, rec, status, nullptr};
     // lensing_born: one Born ray per pixel (hmaps.h:706-712) with radius
-    // surfaces at the FLRW distances of the map surfaces, through the float64
-    // kernel (Born mode is not in the FP32-gather kernel)
+    // surfaces at the FLRW distances of the map surfaces (wide records)
     double* brn = nullptr;
     long long* brn_steps = nullptr;
     PropParams Pn = P;
     if (M.born) {
-        if (e == cudaSuccess) e = cudaMalloc(&brn, (size_t)cap * nz * kPlaneFields * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&brn, (size_t)cap * nz * kWideFields * sizeof(double));
         if (e == cudaSuccess) e = cudaMalloc(&brn_steps, (size_t)cap * sizeof(long long));
         Pn.homogeneous = 2;
         Pn.stop_kind = STOP_R;
         Pn.jacobian = 1;
-        Pn.wide = 0;
+        Pn.wide = 1;
         Pn.direct = 0;
         Pn.ray_planes = nullptr;
         Pn.ray_ki = nullptr;
@@ -292,7 +291,8 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
     }
     const PropOut On{brn_steps, nullptr, brn, status, nullptr};
     auto born_pass = [&](long long m) -> cudaError_t {
-        return M.born ? launch_propagate<true>(T, C, Pn, launch, m, On, stream) : cudaSuccess;
+        if (!M.born) return cudaSuccess;
+        return exact ? launch_propagate<true>(T, C, Pn, launch, m, On, stream) : launch_propagate<false>(T, C, Pn, launch, m, On, stream);
     };
     // (lensing_born alone traces neither the central nor the bundle rays)
     for (long long c0 = 0; (!M.bundle || M.only_born) && e == cudaSuccess && c0 < npix; c0 += cap) {

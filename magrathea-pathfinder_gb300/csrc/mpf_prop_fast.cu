@@ -20,7 +20,12 @@ static void launch_fast_kernel(long long grid, int tpb, const DevTree& T, const 
                                cudaStream_t stream)
 {
     const unsigned g = (unsigned)grid;
-    if (P.ray_stop) {
+    if (P.homogeneous == 2) {
+        // Born rays: the field is homogeneous, so the interpolation order does
+        // not enter (the Jacobian gathers are TSC)
+        if (P.ray_stop) k_propagate_fast<2, true, false, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
+        else k_propagate_fast<2, false, true, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
+    } else if (P.ray_stop) {
         if (P.order == 1) k_propagate_fast<1, true, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
         else k_propagate_fast<2, true, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue);
     } else if (P.wide || P.ray_planes || P.direct || O.traj) {

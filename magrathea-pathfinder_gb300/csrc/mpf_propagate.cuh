@@ -75,7 +75,8 @@ struct PropParams {
     // catalogues.h:670-673), on the octree itself (its levels set the steps,
     // its field the Jacobian), with the Jacobian at each surface's value (a
     // radius) and, for a surface the ray never reaches, at its last point.
-    // Exact kernel only.
+    // Mode 1: exact kernel only; mode 2: both kernels (the fast kernel's
+    // source and wide instantiations).
     int homogeneous;
     int hom_level;
     // per-ray plane normals for the stop criterion "plane" with per-ray
