@@ -301,8 +301,7 @@ def hmaps_fill(octree: Octree, cosmology: Cosmology, nside: int, pixels, surface
     surfaces: the stop-quantity values of the map surfaces (interpRefvec);
     homogeneous: [nsurfaces, 5] = t, chi, lambda, a, z of the FLRW ray there;
     components: the reference's map component names, in order ("lensing_born":
-    the infinitesimal Jacobian along each pixel's FLRW ray, traced through the
-    float64 kernel);
+    the infinitesimal Jacobian along each pixel's FLRW ray);
     jacobian: "infinitesimal" or "bundle" (then plane, stop_bundle and
     openingmin, in radians, as the reference's parameters).
     """

@@ -76,7 +76,7 @@ struct PropParams {
     // its field the Jacobian), with the Jacobian at each surface's value (a
     // radius) and, for a surface the ray never reaches, at its last point.
     // Mode 1: exact kernel only; mode 2: both kernels (the fast kernel's
-    // source and wide instantiations).
+    // Born instantiations).
     int homogeneous;
     int hom_level;
     // per-ray plane normals for the stop criterion "plane" with per-ray
