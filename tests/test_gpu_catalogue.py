@@ -178,7 +178,7 @@ def test_catalogue_bundle_matches_reference(cat_setup, pkg, order, exact, plane,
 def test_catalogue_born_matches_reference(cat_setup, pkg, order, exact):
     """jacobiantype = infinitesimal_born: the Newton rounds as "infinitesimal",
     the converged rows' Jacobian along the Born ray of the observed direction
-    (catalogues.h:670-673), traced through the float64 kernel in both modes."""
+    (catalogues.h:670-673), traced by the Born instantiation of each mode's kernel."""
     g, tree, cos = cat_setup
     for ia in (0, 1):
         acc = float(g["cat_accuracy"][ia])

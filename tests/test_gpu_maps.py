@@ -85,8 +85,8 @@ BORN_MAPS = (("born", "lensing,lensing_born,dz,steps", "infinitesimal"), ("borno
 @pytest.mark.parametrize("exact", [True, False])
 @pytest.mark.parametrize("key,comps,jt", BORN_MAPS)
 def test_hmaps_fill_born_matches_reference(gpu_lib, pkg, golden, order, exact, key, comps, jt):
-    """The Born rows run through the float64 kernel in both modes and agree to
-    1e-6 of their scale (the Jacobian sums are re-associated); the other rows
+    """The Born rows (each mode's Born kernel: float64 gathers, or FP32 ones for
+    the Jacobian) agree to 1e-6 of their scale; the other rows
     keep the tolerances of the tests above (bundle rows 1e-3 in fast mode)."""
     tree = pkg.Octree.from_records(golden["records"])
     cos = pkg.Cosmology(golden["cosmo_t"], golden["cosmo_a"], golden["cosmo_dadt"], golden["cosmo_d2adt2"])
