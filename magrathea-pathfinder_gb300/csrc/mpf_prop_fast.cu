@@ -60,7 +60,8 @@ static int fast_launch_shape(long long n, int blocks_per_sm, int sms, long long*
 
 // Work-queue counter and occupancy of the persistent kernel, per (device,
 // stream): calls on one stream are ordered and may share a counter; calls on
-// different streams (or devices) may run at the same time and must not.
+// different streams (or devices) may run at the same time and must not.  One
+// 8-byte counter per stream handle seen, kept for the process's lifetime.
 struct FastLaunchState {
     unsigned long long* queue = nullptr;
     int blocks_per_sm = 0, sms = 0;
