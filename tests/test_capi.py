@@ -5,6 +5,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 from conftest import ROOT, PKG
 
@@ -70,3 +71,17 @@ def test_corrupt_cone_file_is_an_io_error(pkg, tmp_path):
     empty.write_bytes(b"")
     assert L.mpf_octree_load(str(empty).encode(), ctypes.byref(h)) == -6
     assert not h.value
+
+
+def test_host_side_argument_checks(pkg):
+    """Choices the host layer refuses before any library call."""
+    from importlib import import_module
+    maps = import_module(pkg.__name__ + ".maps")
+    with pytest.raises(ValueError):
+        pkg.catalogue_params(1.0, 0.68, jacobian="exact")    # the reference's plane = "exact" is not implemented either
+    p, _ = pkg.catalogue_params(1.0, 0.68, jacobian="infinitesimal_born")
+    assert p.jacobian_born == 1 and p.jacobian_bundle == 0
+    planes = np.zeros((2, 1, 20))
+    with pytest.raises(ValueError):
+        maps.assemble(planes, np.zeros((2, 3)), np.ones((1, 5)), ["lensing_born"])
+    assert maps.nmaps(["lensing", "lensing_born", "deflection", "dz"]) == 11
