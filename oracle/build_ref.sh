@@ -1,6 +1,7 @@
 #!/usr/bin/env bash
 # Builds the reference CPU oracle into oracle/_ref/ from the reference sources
-# where they lie (default /root/reference/src; override with MPF_REFERENCE_SRC).
+# where they lie: MPF_REFERENCE_SRC, else the reference checked out beside
+# this repository (../reference/src relative to the repository root).
 #
 # Steps:
 #  1. Write a patched copy of magrathea/simplehyperoctree.h into
@@ -17,7 +18,7 @@
 #  the reference's x86-64 build is.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-SRC="${MPF_REFERENCE_SRC:-/root/reference/src}"
+SRC="${MPF_REFERENCE_SRC:-$HERE/../../reference/src}"
 OUT="$HERE/_ref"
 if [ ! -f "$SRC/magrathea/simplehyperoctree.h" ]; then
     echo "reference sources not found at $SRC" >&2
