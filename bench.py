@@ -166,18 +166,36 @@ def measured_peak_hbm():
 
 def cpu_baseline(oracle_mod, records, cos, length, launch, planes, per_thread=24, seed=1):
     """The C oracle (restated reference algorithm, binary search over sorted
-    keys, trajectory then Jacobian post-pass) on a bounded random sample."""
+    keys, trajectory then Jacobian post-pass) on a bounded random sample.
+    Returns the baseline entry and the sample with the oracle's outputs
+    (launch records, steps, final records, surface records)."""
     nthreads = os.cpu_count() or 1
     O = oracle_mod.Oracle(records, {"t": cos[0], "a": cos[1], "dadt": cos[2]}, length, nthreads=nthreads)
     rng = np.random.default_rng(seed)
     idx = rng.choice(launch.shape[0], size=per_thread * nthreads, replace=False)
+    sample = np.ascontiguousarray(launch[idx])
     t0 = time.perf_counter()
-    steps, _, _ = O.propagate(launch[idx], order=2, nsteps=8, stop="redshift", planes=planes, jacobian=True)
+    steps, final, pl = O.propagate(sample, order=2, nsteps=8, stop="redshift", planes=planes, jacobian=True)
     dt = time.perf_counter() - t0
     total = int(steps.sum())
-    return {"value": total / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": "%d rays drawn from the grid, %d photon-steps, %.1f s, %d threads (C oracle, Jacobian post-pass)"
-                      % (idx.shape[0], total, dt, nthreads)}
+    entry = {"value": total / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+             "sample": "%d rays drawn from the grid, %d photon-steps, %.1f s, %d threads (C oracle, Jacobian post-pass)"
+                       % (idx.shape[0], total, dt, nthreads)}
+    return entry, (sample, steps, final, pl)
+
+
+def parity_entry(pkg, tree, cosmo, length, planes, oracle_run, exact=False):
+    """The benchmarked kernel on the oracle's sample rays, compared output by
+    output with the oracle (the reference's float64 algorithm)."""
+    acc = importlib.import_module(PKG + ".accuracy")
+    sample, s_ref, f_ref, p_ref = oracle_run
+    s, f, pl, _ = pkg.propagate(tree, cosmo, sample, length, nsteps=8, order=2, stop="redshift", planes=planes,
+                                jacobian=True, exact=exact)
+    rep = acc.compare(sample, s, f, pl, s_ref, f_ref, p_ref)
+    rep["against"] = "C oracle (the reference's float64 algorithm, bit-exact with its own build on the fixtures)"
+    rep["tolerance"] = {"deflection_rel": 1e-6, "redshift_rel": 1e-6, "lensing_of_scale": 1e-6}
+    rep["within_tolerance"] = bool(acc.within(rep))
+    return rep
 
 
 CAT_METRIC = "catalogue sources/s (Newton root-finder to cat_accuracy 1e-8, TSC, <=11 rays per source)"
@@ -549,7 +567,8 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         import oracle as oracle_mod
         oracle_mod.build()
-        line["cpu_baseline"] = cpu_baseline(oracle_mod, rec, cos, length, launch, planes)
+        line["cpu_baseline"], oracle_run = cpu_baseline(oracle_mod, rec, cos, length, launch, planes)
+        line["parity"] = parity_entry(pkg, tree, cosmo, length, planes, oracle_run, exact=args.exact)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -141,7 +141,10 @@ int mpf_propagate_device(const mpf_octree* o, const mpf_cosmology* c, const mpf_
  * process exits; a batch that does not fit is rejected with MPF_BAD_INPUT.
  * All calls share that array: calls that overlap on the GPU race, so
  * serialise them.  The first call on a device looks up the array's address
- * (cudaGetSymbolAddress): make it before any stream capture.  Message of a
+ * (cudaGetSymbolAddress): make it before any stream capture.  That address is
+ * kept for the process's life, so it does not survive a cudaDeviceReset of
+ * the device.  Arguments as for mpf_propagate (order 0 runs the float64
+ * kernel; steps, final_rec and plane_rec may each be NULL).  Message of a
  * failed call: mpf_noalloc_last_error(). */
 #define MPF_NOALLOC_SCRATCH_BYTES (16u << 20)
 int mpf_propagate_noalloc(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t n, const double* launch,

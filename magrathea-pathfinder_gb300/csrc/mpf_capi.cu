@@ -54,7 +54,11 @@ struct DBuf {
     }
 };
 
-bool fill_params(const mpf_params* p, mpf::PropParams& P)
+}  // namespace
+
+// Parameter checks and the device parameter block of every propagation call
+// (mpf_propagate, mpf_propagate_device, mpf_propagate_noalloc, the map calls).
+bool mpf_internal_fill_params(const mpf_params* p, mpf::PropParams& P)
 {
     if (!p || p->nsteps == 0 || p->order < 0 || p->order > 2 || p->stop < 0 || p->stop > 6 || p->nplanes < 0 ||
         p->nplanes > MPF_MAX_PLANES || !(p->length > 0.0))
@@ -75,6 +79,8 @@ bool fill_params(const mpf_params* p, mpf::PropParams& P)
     return true;
 }
 
+namespace {
+bool fill_params(const mpf_params* p, mpf::PropParams& P) { return mpf_internal_fill_params(p, P); }
 }  // namespace
 
 int mpf_internal_set_error(int code, const char* msg) { return set_err(code, msg ? msg : ""); }
@@ -178,9 +184,11 @@ int mpf_cosmology_upload(const double* t, const double* a, const double* dadt, c
         }
     }
     std::vector<double> sa((size_t)n, 0.0), sd((size_t)n, 0.0);
+    std::vector<float2> seg((size_t)n, make_float2(0.f, 0.f));
     for (int64_t i = 0; i + 1 < n; ++i) {
         sa[(size_t)i] = (a[i + 1] - a[i]) / (t[i + 1] - t[i]);
         sd[(size_t)i] = (dadt[i + 1] - dadt[i]) / (t[i + 1] - t[i]);
+        seg[(size_t)i] = make_float2((float)sd[(size_t)i], (float)(t[i + 1] - t[i]));
     }
     const size_t bytes = (size_t)n * sizeof(double);
     cudaError_t e = cudaMalloc(&c->t, bytes);
@@ -190,6 +198,8 @@ int mpf_cosmology_upload(const double* t, const double* a, const double* dadt, c
     if (e == cudaSuccess) e = cudaMalloc(&c->slope_a, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&c->slope_dadt, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&c->lut, lut.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->seg, seg.size() * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemcpy(c->seg, seg.data(), seg.size() * sizeof(float2), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(c->t, t, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(c->a, a, bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(c->dadt, dadt, bytes, cudaMemcpyHostToDevice);
@@ -214,6 +224,7 @@ void mpf_cosmology_destroy(mpf_cosmology* c)
     cudaFree(c->d2adt2);
     cudaFree(c->slope_a);
     cudaFree(c->slope_dadt);
+    cudaFree(c->seg);
     cudaFree(c->lut);
     delete c;
 }
@@ -254,7 +265,7 @@ int mpf_propagate_device(const mpf_octree* o, const mpf_cosmology* c, const mpf_
     mpf::PropParams P;
     if (!o || !c || !fill_params(p, P) || n < 0 || (n > 0 && (!launch_device || !steps_device || !status_device)))
         return set_err(MPF_BAD_INPUT, "mpf_propagate_device: bad argument");
-    mpf::DevCosmo C{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
+    const mpf::DevCosmo C = dev_cosmo(c);
     mpf::PropOut O{(long long*)steps_device, final_device, plane_device, (unsigned*)status_device, nullptr};
     const cudaError_t e = p->exact ? mpf::launch_propagate<true>(o->tree, C, P, launch_device, n, O, (cudaStream_t)stream)
                                    : mpf::launch_propagate<false>(o->tree, C, P, launch_device, n, O, (cudaStream_t)stream);
@@ -329,7 +340,7 @@ int mpf_catalogue_newton_device(const mpf_octree* o, const mpf_cosmology* c, con
     if (n > 0x7fffffffll) return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: at most 2^31 - 1 sources per call");
     if (stats) std::memset(stats, 0, sizeof(*stats));
     if (n == 0) return MPF_OK;
-    mpf::DevCosmo C{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
+    const mpf::DevCosmo C = dev_cosmo(c);
     mpf::CatRunStats st;
     unsigned status = 0;
     const cudaError_t e = mpf::catalogue_newton(o->tree, C, K, p->rotm1 ? &R : nullptr, p->exact != 0, p->order, p->nsteps,
@@ -409,7 +420,7 @@ int hmaps_fill_impl(const mpf_octree* o, const mpf_cosmology* c, const mpf_param
         if (pixels[i] < 0 || pixels[i] >= npixall) return set_err(MPF_BAD_INPUT, "mpf_hmaps_fill: pixel id out of range");
     P.jacobian = 1;
     if (npix == 0) return MPF_OK;
-    mpf::DevCosmo C{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
+    const mpf::DevCosmo C = dev_cosmo(c);
     const size_t map_bytes = (size_t)M.nmaps * (size_t)p->nplanes * (size_t)npix * sizeof(float);
     DBuf dpix, dmaps;
     cudaError_t e = dpix.alloc((size_t)npix * sizeof(int64_t));

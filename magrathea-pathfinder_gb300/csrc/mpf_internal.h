@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "mpf_gb300.h"
 #include "mpf_device.cuh"
 #include "mpf_propagate.cuh"
 
@@ -32,10 +33,20 @@ struct mpf_cosmology {
     double t0, lut_scale;
     double* slope_a;
     double* slope_dadt;
+    float2* seg;
 };
+
+// device view of a cosmology table
+inline mpf::DevCosmo dev_cosmo(const mpf_cosmology* c)
+{
+    return mpf::DevCosmo{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt, c->seg};
+}
 
 // sets the calling thread's mpf_last_error() message; returns code
 int mpf_internal_set_error(int code, const char* msg);
+
+// checks an mpf_params block and fills the device parameters (false: bad input)
+bool mpf_internal_fill_params(const mpf_params* p, mpf::PropParams& P);
 
 namespace mpf {
 

@@ -25,7 +25,11 @@
 //    race on the array, so callers serialise them;
 //  * the device address of the array is looked up with cudaGetSymbolAddress
 //    the first time the call runs on a device (with that device current);
-//    make that first call before any stream capture begins.
+//    make that first call before any stream capture begins.  The address is
+//    kept for the life of the process: it does not survive a cudaDeviceReset
+//    of that device (the module, and with it the array, is loaded anew), so
+//    a process that resets a device must not call this entry point on it
+//    afterwards.
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -80,14 +84,14 @@ extern "C" const char* mpf_noalloc_last_error(void) { return g_noalloc_err.c_str
 extern "C" int mpf_propagate_noalloc(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t n,
                                      const double* launch, int64_t* steps, double* final_rec, double* plane_rec)
 {
-    if (!o || !c || !p || n < 0 || (n > 0 && (!launch || !steps)))
-        return fail(MPF_BAD_INPUT, "mpf_propagate_noalloc: null handle, parameters or buffer");
-    if (p->nsteps == 0 || (p->order != 1 && p->order != 2) || p->stop < 0 || p->stop > 6 || p->nplanes < 0 ||
-        p->nplanes > MPF_MAX_PLANES || !(p->length > 0.0) || (p->nplanes > 0 && (!p->planes || p->stop == MPF_STOP_PLANE)))
-        return fail(MPF_BAD_INPUT, "mpf_propagate_noalloc: bad parameters");
+    // the same argument rules as mpf_propagate: steps, final_rec and plane_rec may each be NULL
+    mpf::PropParams P;
+    if (!o || !c || !mpf_internal_fill_params(p, P) || n < 0 || (n > 0 && !launch))
+        return fail(MPF_BAD_INPUT, "mpf_propagate_noalloc: bad argument");
     if (n == 0) return MPF_OK;
     const int np = p->nplanes;
-    // staging layout: [control 256 B][launch][steps][final][surfaces], 256-B aligned
+    // staging layout: [control 256 B][launch][steps][final][surfaces], 256-B aligned; the
+    // kernel writes every ray's step count, so steps are staged even when not copied back
     const size_t b_ctl = 256;
     const size_t b_launch = up256((size_t)n * 6 * sizeof(double));
     const size_t b_steps = up256((size_t)n * sizeof(int64_t));
@@ -109,29 +113,19 @@ extern "C" int mpf_propagate_noalloc(const mpf_octree* o, const mpf_cosmology* c
     double* d_final = b_final ? (double*)(s + b_ctl + b_launch + b_steps) : nullptr;
     double* d_planes = b_planes ? (double*)(s + b_ctl + b_launch + b_steps + b_final) : nullptr;
 
-    mpf::PropParams P;
-    std::memset(&P, 0, sizeof(P));
-    P.length = p->length;
-    P.stop_ref = (np > 0) ? p->planes[np - 1] : p->stop_value;
-    for (int k = 0; k < 3; ++k) P.ki[k] = p->plane_normal[k];
-    for (int k = 0; k < np; ++k) P.planes[k] = p->planes[k];
-    P.max_steps = (p->max_steps > 0) ? p->max_steps : 100000000ll;
-    P.nsteps = p->nsteps;
-    P.order = p->order;
-    P.stop_kind = p->stop;
-    P.nplanes = np;
-    P.jacobian = p->jacobian ? 1 : 0;
-    mpf::DevCosmo C{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
+    const mpf::DevCosmo C = dev_cosmo(c);
     mpf::PropOut O{d_steps, d_final, d_planes, status, nullptr};
 
     e = cudaMemset(s, 0, b_ctl);   // queue counter and status word start at zero
     if (e == cudaSuccess) e = cudaMemcpy(d_launch, launch, (size_t)n * 6 * sizeof(double), cudaMemcpyHostToDevice);
+    // ORDER = 0 (NGP) runs the float64 kernel in both modes, as in mpf_propagate; that
+    // kernel needs no work-queue counter
     if (e == cudaSuccess)
-        e = p->exact ? mpf::launch_propagate<true>(o->tree, C, P, d_launch, n, O, 0)
-                     : mpf::launch_propagate_fast_with_queue(o->tree, C, P, d_launch, n, O, queue, 0);
+        e = (p->exact || P.order == 0) ? mpf::launch_propagate<true>(o->tree, C, P, d_launch, n, O, 0)
+                                       : mpf::launch_propagate_fast_with_queue(o->tree, C, P, d_launch, n, O, queue, 0);
     unsigned st = 0;
     if (e == cudaSuccess) e = cudaMemcpy(&st, status, sizeof(st), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(steps, d_steps, (size_t)n * sizeof(int64_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && steps) e = cudaMemcpy(steps, d_steps, (size_t)n * sizeof(int64_t), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && d_final)
         e = cudaMemcpy(final_rec, d_final, (size_t)n * MPF_PHOTON_FIELDS * sizeof(double), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && d_planes)

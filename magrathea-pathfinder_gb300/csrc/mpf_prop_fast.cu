@@ -8,6 +8,8 @@
 #include <cstdlib>
 #include <map>
 #include <mutex>
+#include <thread>
+#include <tuple>
 #include <utility>
 
 namespace mpf {
@@ -62,6 +64,11 @@ static int fast_launch_shape(long long n, int blocks_per_sm, int sms, long long*
 // stream): calls on one stream are ordered and may share a counter; calls on
 // different streams (or devices) may run at the same time and must not.  One
 // 8-byte counter per stream handle seen, kept for the process's lifetime.
+// cudaStreamPerThread is one handle value for as many streams as there are
+// host threads, so it is keyed per calling thread as well.  The counter is
+// zeroed by an asynchronous memset before each launch, so a stream must not
+// be shared by host threads that call at the same time (their memsets and
+// launches could interleave): each concurrent caller passes its own stream.
 struct FastLaunchState {
     unsigned long long* queue = nullptr;
     int blocks_per_sm = 0, sms = 0;
@@ -69,12 +76,13 @@ struct FastLaunchState {
 static cudaError_t fast_launch_state(cudaStream_t stream, FastLaunchState* out)
 {
     static std::mutex mu;
-    static std::map<std::pair<int, cudaStream_t>, FastLaunchState> states;
+    static std::map<std::tuple<int, cudaStream_t, std::thread::id>, FastLaunchState> states;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    const std::thread::id who = (stream == cudaStreamPerThread) ? std::this_thread::get_id() : std::thread::id();
     std::lock_guard<std::mutex> lock(mu);
-    FastLaunchState& s = states[{dev, stream}];
+    FastLaunchState& s = states[std::make_tuple(dev, stream, who)];
     if (!s.queue) {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s.blocks_per_sm, k_propagate_fast<2, false, false>, kFastThreads, 0);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s.sms, cudaDevAttrMultiProcessorCount, dev);

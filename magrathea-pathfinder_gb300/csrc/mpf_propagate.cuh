@@ -44,6 +44,9 @@ struct DevCosmo {
     double t0, lut_scale;
     const double* slope_a;
     const double* slope_dadt;
+    // per interval k (t[k], t[k+1]): slope of da/dt and width t[k+1] - t[k], in
+    // FP32 (the RK4 stages' increments of da/dt from the step's start)
+    const float2* seg;
 };
 
 struct PropParams {

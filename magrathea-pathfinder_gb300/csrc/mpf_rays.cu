@@ -230,7 +230,7 @@ extern "C" int mpf_rays_propagate(const mpf_octree* o, const mpf_cosmology* c, c
     const bool hom = bp->homogeneous_level >= 0;
     P.homogeneous = hom ? 1 : 0;
     P.hom_level = hom ? bp->homogeneous_level : 0;
-    const DevCosmo C{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
+    const DevCosmo C = dev_cosmo(c);
     Dev dl, dsteps, dtraj, dout, dsizes, dstatus;
     cudaError_t e = dl.alloc((size_t)chunk * nt * 6 * sizeof(double));
     if (e == cudaSuccess) e = dsteps.alloc((size_t)chunk * nt * sizeof(long long));

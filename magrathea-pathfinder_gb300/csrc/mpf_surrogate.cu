@@ -839,11 +839,6 @@ int cuda_fail(cudaError_t e, const char* where)
     return fail(e == cudaErrorMemoryAllocation ? MPF_OUT_OF_MEMORY : MPF_CUDA_ERROR, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
-mpf::DevCosmo dev_cosmo(const mpf_cosmology* c)
-{
-    return mpf::DevCosmo{c->t, c->a, c->dadt, c->n, c->lut, c->nlut, c->t0, c->lut_scale, c->slope_a, c->slope_dadt};
-}
-
 int pack(mpf_surrogate* s)
 {
     k_pack<<<blocks_for(kHidden * kWidth * kWidth, 256), 256>>>(s->params, s->packed);

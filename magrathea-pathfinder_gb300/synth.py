@@ -282,10 +282,46 @@ class OctreeSpec:
     concentration: float = 5.0
     refine_cells: float = 2.5
     cosmo: Cosmology = field(default_factory=Cosmology)
+    axis_deg: tuple = None   # (phi, theta) of the cone axis (narrow_cone_axis); None: +x
+
+    def frame(self) -> np.ndarray:
+        """3x3 rotation whose columns are the cone frame's axes in octree
+        coordinates (column 0: the cone axis)."""
+        return np.eye(3) if self.axis_deg is None else cone_frame(*self.axis_deg)
+
+
+def narrow_cone_axis(phi_deg: float, theta_deg: float) -> np.ndarray:
+    """Axis of a narrow cone of the reference's cone parameters (phi, theta):
+    (cos(theta) cos(phi), -sin(phi), cos(phi) sin(theta)) (src/miscellaneous.h:315-325,
+    src/input.h:1030-1040)."""
+    ph, th = math.radians(phi_deg), math.radians(theta_deg)
+    return np.array([math.cos(th) * math.cos(ph), -math.sin(ph), math.cos(ph) * math.sin(th)])
+
+
+def cone_frame(phi_deg: float, theta_deg: float) -> np.ndarray:
+    """Right-handed orthonormal frame with the narrow cone's axis as its
+    first column; the second column is horizontal (no z component)."""
+    n = narrow_cone_axis(phi_deg, theta_deg)
+    ey = np.cross([0.0, 0.0, 1.0], n)
+    ey /= np.linalg.norm(ey)
+    ez = np.cross(n, ey)
+    return np.stack([n, ey, ez], axis=1)
+
+
+def uniform_grid_cone(z_max: float = 0.5, axis_deg=(20.0, 20.0), lbox: float = 2048.0, half_deg: float = 2.5,
+                      seed: int = 42) -> OctreeSpec:
+    """The 64^3 periodic field at file level 6 (octree level 8, no refinement)
+    over a 2 half_deg square cone along the narrow cone axis (phi, theta) =
+    axis_deg, deep enough for rays to z_max."""
+    cosmo = Cosmology()
+    chi = float(cosmo.chi_of_z(z_max)[0])
+    return OctreeSpec(base_level=8, box_cells=64, lbox=lbox, half_y=half_deg, half_z=half_deg, chi_max=chi * 1.02,
+                      halos=0, max_level=8, seed=seed, axis_deg=tuple(axis_deg))
 
 
 def _cone_mask(centers: np.ndarray, spec: OctreeSpec, cell: float) -> np.ndarray:
-    x, y, z = centers[:, 0], centers[:, 1], centers[:, 2]
+    local = centers @ spec.frame()          # coordinates in the cone frame
+    x, y, z = local[:, 0], local[:, 1], local[:, 2]
     pad = spec.margin * cell
     ty = math.tan(math.radians(spec.half_y))
     tz = math.tan(math.radians(spec.half_z))
@@ -304,8 +340,11 @@ def _base_cells(spec: OctreeSpec) -> np.ndarray:
     ty = math.tan(math.radians(spec.half_y))
     tz = math.tan(math.radians(spec.half_z))
     xmax = spec.chi_max / spec.lbox + pad
-    lo = coords(L, np.array([-pad - cell, -(xmax * ty + pad), -(xmax * tz + pad)]))
-    hi = coords(L, np.array([xmax + cell, xmax * ty + pad + cell, xmax * tz + pad + cell]))
+    # bounding box of the cone frame's box around the cone, in octree coordinates
+    corners = np.array([[x, y, z] for x in (-pad - cell, xmax + cell) for y in (-(xmax * ty + pad), xmax * ty + pad + cell)
+                        for z in (-(xmax * tz + pad), xmax * tz + pad + cell)]) @ spec.frame().T
+    lo = coords(L, np.maximum(corners.min(axis=0) - cell, -EXTENT / 2.0))
+    hi = coords(L, np.minimum(corners.max(axis=0) + cell, EXTENT / 2.0 - 1e-12))
     out = []
     ys = np.arange(int(lo[1]), int(hi[1]) + 1, dtype=np.int64)
     zs = np.arange(int(lo[2]), int(hi[2]) + 1, dtype=np.int64)
@@ -330,6 +369,7 @@ def _nfw_halos(spec: OctreeSpec, rng: np.random.Generator):
     x = np.maximum(x, 0.05 * xmax)
     y = (2 * rng.random(n) - 1) * x * ty
     z = (2 * rng.random(n) - 1) * x * tz
+    centres = np.stack([x, y, z], axis=1) @ spec.frame().T
     mass = np.exp(rng.uniform(math.log(spec.mass_min), math.log(spec.mass_max), n))  # Msun/h
     rho_c = 2.775e11  # h^2 Msun / Mpc^3
     r200 = (3 * mass / (4 * math.pi * 200 * rho_c)) ** (1.0 / 3.0)  # Mpc/h comoving
@@ -338,7 +378,7 @@ def _nfw_halos(spec: OctreeSpec, rng: np.random.Generator):
     mu = math.log(1 + cc) - cc / (1 + cc)
     # 4 pi G rho_s r_s^3 = G M / mu  (SI, with M in kg)
     gm = G_NEWTON * mass / cosmo.h * MSUN / mu
-    return np.stack([x, y, z], axis=1), rs, r200, gm
+    return centres, rs, r200, gm
 
 
 def _nfw_phi_grad(d_m: np.ndarray, rs_m: float, gm: float, rc_m: float):
@@ -492,15 +532,18 @@ def read_bin(path: str) -> np.ndarray:
     return np.fromfile(path, dtype=RECORD)
 
 
-def photon_grid(n_side: int, half_y_deg: float, half_z_deg: float) -> np.ndarray:
+def photon_grid(n_side: int, half_y_deg: float, half_z_deg: float, frame=None) -> np.ndarray:
     """Launch records (x0 y0 z0 x1 y1 z1) for an n_side x n_side grid of
     directions filling the square cone about +x, in the reference's
-    narrow-cone angles (|phi| < half_y, |theta - pi/2| < half_z)."""
+    narrow-cone angles (|phi| < half_y, |theta - pi/2| < half_z); with
+    `frame` (OctreeSpec.frame()), about that frame's first axis."""
     t = (np.arange(n_side) + 0.5) / n_side * 2.0 - 1.0
     ph = np.radians(half_y_deg) * t
     th = np.pi / 2 + np.radians(half_z_deg) * t
     P, T = np.meshgrid(ph, th, indexing="ij")
     d = np.stack([np.sin(T) * np.cos(P), np.sin(T) * np.sin(P), np.cos(T)], axis=-1).reshape(-1, 3)
+    if frame is not None:
+        d = d @ np.asarray(frame).T
     out = np.zeros((d.shape[0], 6))
     out[:, 3:] = d
     return out

@@ -336,10 +336,57 @@ def make_cells():
     print("cells -> %s (%d KB)" % (path, os.path.getsize(path) // 1024))
 
 
+def records_sha(rec) -> str:
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(rec).tobytes()).hexdigest()
+
+
+def whole_rays_specs():
+    """Two whole-ray workloads: the AMR construction of the benchmark octree at
+    a small size (64^3 base at octree level 8, refined to 11 in 50 NFW haloes)
+    to z = 2, and the uniform 64^3 cone along phi = theta = 20 deg to z = 0.5."""
+    chi2 = float(S.Cosmology().chi_of_z(2.0)[0])
+    amr = S.OctreeSpec(base_level=8, box_cells=64, lbox=2048.0, half_y=5.0, half_z=5.0, chi_max=chi2 * 1.02, halos=50,
+                       max_level=11, refine_cells=2.5, seed=42)
+    return {"amr_z2": (amr, S.photon_grid(8, 4.5, 4.5), 2.0, 8, (1, 2)),
+            "cone20_z05": (S.uniform_grid_cone(0.5, (20.0, 20.0)), None, 0.5, 10, (1,))}
+
+
+def make_whole_rays():
+    """The reference's Integrator::integrate on whole rays of the two
+    workloads (step counts and final photon records), with the records' hash
+    so that a test regenerates exactly the same octree."""
+    out = {}
+    table = S.Cosmology().conformal_table(n=4000, amin=0.05)
+    for name, (spec, launch, zstop, nsteps, orders) in whole_rays_specs().items():
+        rec = S.make_octree(spec)
+        if launch is None:
+            launch = S.photon_grid(8, 2.5, 2.5, spec.frame())
+        tmp = tempfile.mkdtemp(prefix="mpf_golden_")
+        binpath = os.path.join(tmp, "cone.bin")
+        S.write_bin(binpath, rec)
+        length = spec.lbox * S.MPC / spec.cosmo.h
+        out[name + "_sha"] = np.array(records_sha(rec))
+        out[name + "_launch"] = launch
+        for order in orders:
+            R = Reference(order)
+            R.set_cosmology(*table, length)
+            R.load(binpath)
+            steps, final, _ = R.integrate(launch, "redshift", zstop, nsteps)
+            out["%s_steps_o%d" % (name, order)] = steps
+            out["%s_final_o%d" % (name, order)] = final
+            print("%s order %d: %d rays, %.0f steps on average" % (name, order, launch.shape[0], steps.mean()))
+    path = os.path.join(HERE, "whole_rays.npz")
+    np.savez_compressed(path, **out)
+    print("whole rays -> %s (%d KB)" % (path, os.path.getsize(path) // 1024))
+
+
 if __name__ == "__main__":
-    names = sys.argv[1:] or list(CASES) + ["rays", "cells"]
+    names = sys.argv[1:] or list(CASES) + ["rays", "cells", "whole_rays"]
     for name in names:
-        if name == "rays":
+        if name == "whole_rays":
+            make_whole_rays()
+        elif name == "rays":
             make_rays()
         elif name == "cells":
             if names == ["cells"]:

@@ -57,6 +57,38 @@ def test_noalloc_matches_allocating_call_twice(gpu_lib, pkg, exact):
     del keep
 
 
+@pytest.mark.parametrize("exact", [False, True])
+def test_noalloc_ngp_and_optional_outputs(gpu_lib, pkg, exact):
+    """ORDER = 0 (nearest grid point) is accepted as by mpf_propagate, which
+    runs it in the float64 kernel whatever `exact` says, and the step counts
+    are optional (NULL) as there."""
+    import importlib
+    capi = importlib.import_module("magrathea-pathfinder_gb300.capi")
+    g = load_golden("amr")
+    tree = pkg.Octree.from_records(g["records"])
+    cos = pkg.Cosmology(g["cosmo_t"], g["cosmo_a"], g["cosmo_dadt"], g["cosmo_d2adt2"])
+    length = float(g["cosmo_length"])
+    zs = g["zs"]
+    launch = np.ascontiguousarray(g["launch"])
+    ref_steps, ref_final, ref_planes, rc = pkg.propagate(tree, cos, launch, length, nsteps=8, order=0, stop="redshift",
+                                                         planes=zs, jacobian=True, exact=exact)
+    assert rc == 0
+    p, keep = capi.make_params(length, nsteps=8, order=0, stop="redshift", planes=zs, jacobian=True, exact=exact)
+    for _ in range(2):
+        rc, steps, final, planes = _noalloc(gpu_lib, capi, tree, cos, p, launch, zs.shape[0])
+        assert rc == 0, gpu_lib.mpf_noalloc_last_error()
+        np.testing.assert_array_equal(steps, ref_steps)
+        np.testing.assert_array_equal(final.view(np.uint64), ref_final.view(np.uint64))
+        np.testing.assert_array_equal(planes.view(np.uint64), ref_planes.view(np.uint64))
+    # steps = NULL: the other outputs are still written
+    final = np.zeros((launch.shape[0], capi.MPF_PHOTON_FIELDS))
+    rc = gpu_lib.mpf_propagate_noalloc(tree._h, cos._h, ctypes.byref(p), launch.shape[0], capi.ptr(launch), None,
+                                       capi.ptr(final), None)
+    assert rc == 0, gpu_lib.mpf_noalloc_last_error()
+    np.testing.assert_array_equal(final.view(np.uint64), ref_final.view(np.uint64))
+    del keep
+
+
 def test_noalloc_rejects_batches_beyond_the_scratch(gpu_lib, pkg):
     import importlib
     capi = importlib.import_module("magrathea-pathfinder_gb300.capi")
