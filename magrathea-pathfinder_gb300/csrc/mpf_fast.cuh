@@ -600,14 +600,16 @@ __device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, doub
 }
 
 // Per-thread Jacobian running sums kept in shared memory (touched once per
-// step, so they need not occupy 36 registers through the gathers): S (6), the
-// last point's contribution c_k (6) and the one before it c_km1 (6), strided
-// by the block size.
+// step, so they need not occupy registers through the gathers): the FP64
+// sums S (6), and the last point's contribution c_k (6) and the one before it
+// c_km1 (6), FP32 products of the point's FP32 Hessian terms; strided by the
+// block size.
 struct JacSums {
-    double* base;   // this thread's slot 0
-    __device__ __forceinline__ double& S(int q) const { return base[q * kFastThreads]; }
-    __device__ __forceinline__ double& ck(int q) const { return base[(6 + q) * kFastThreads]; }
-    __device__ __forceinline__ double& ckm1(int q) const { return base[(12 + q) * kFastThreads]; }
+    double* sums;   // this thread's slot 0 of S
+    float* terms;   // this thread's slot 0 of c_k, c_km1
+    __device__ __forceinline__ double& S(int q) const { return sums[q * kFastThreads]; }
+    __device__ __forceinline__ float& ck(int q) const { return terms[q * kFastThreads]; }
+    __device__ __forceinline__ float& ckm1(int q) const { return terms[(6 + q) * kFastThreads]; }
 };
 
 // SRC: source mode (one surface at the ray's own radius); WIDE: per-ray
@@ -661,7 +663,6 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     double ratio = b.a * b.a * ratio_k;
     double dl = (here.cell >= 0 ? cell_extent(here.level) : 0.0) * ratio;
     const double a0 = b.a;
-    double inv_a = recip(b.a);          // 1 / a at b (stage 1 of the next step)
     int tb = bracket_lut(C, b.t);       // cosmology-table bracket of the ray's conformal time
     const double phi0c2 = b.phi / c2;
     float last_data_dt = data.dt;
@@ -693,57 +694,165 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     }
     double rmax = 0.0;
     bool have_rmax = false;
-    for (int q = 0; q < 6; ++q) { J.S(q) = 0.0; J.ck(q) = 0.0; J.ckm1(q) = 0.0; }
+    for (int q = 0; q < 6; ++q) { J.S(q) = 0.0; J.ck(q) = 0.f; J.ckm1(q) = 0.f; }
     double chim1 = 0.0, chim2 = 0.0;
     long long k = 0;
     unsigned status = 0;
     double isw = 0.0, iswold = 0.0, lambda = 0.0, sacc = 0.0;
-    double core[9], dc[9], acc[9];
+    // A point's redshift (integrator.h:769) is formed only where it is read:
+    // surface records, the end of the ray, trajectory records.  The stop and
+    // crossing tests compare a0 (1 + phi0/c^2 - phi/c^2) with (1 + z) a
+    // instead, which needs no division.  The starting point's redshift is 0.
+    const double opc = 1.0 + phi0c2;
+    const double inv_c2 = 1.0 / c2;
+    auto red_of = [&](const FastRec& r) -> double { return a0 * recip(r.a) * (opc - r.phi * inv_c2) - 1.0; };
+    auto red_above = [&](const FastRec& r, double zref) -> bool { return a0 * (opc - r.phi * inv_c2) > (1.0 + zref) * r.a; };
+    bool b_red_ok = true;     // b.red holds b's redshift
+    const float two_c2 = (float)(2.0 / c2);
+    const float inv_c2f = (float)(1.0 / c2);
     FastRec p;
     while (!is_empty(data)) {
         if (k >= P.max_steps) { status |= 1u; break; }
-        const double bc[9] = {b.a, b.t, b.x, b.y, b.z, b.k0, b.k1, b.k2, b.k3};
-        // stages: core = b + c_s dl * d_{s-1};  acc = d0 + 2 d1 + 2 d2 + d3 (in that order)
-        // stage 1 is at b, where the previous step's post-step gather already
-        // read the field (data); stages 2-4 gather at their own points
-        // The stage points b + pc k are located and gathered from their FP32
-        // offset to b's cell (pc k is a fraction of a cell); their float64
-        // coordinates are formed only on the rare full-walk / restart paths.
-        float kfs[3];
-        double pk[3] = {0.0, 0.0, 0.0}, pc = 0.0;
-#pragma unroll 1
-        for (int sg = 0; sg < 4; ++sg) {
-            if (sg == 0) {
-                rhs_math(C, data, bc, inv_a, tb, dc, kfs);
+        // ---- RK4 step (integrator.h:718-734).  The state stays FP64 and is
+        // accumulated in FP64; the four stages are evaluated in FP32 as
+        // increments from the step's start b (c = 0, 1/2, 1/2, 1; weights
+        // w = 1, 2, 2, 1):
+        //   k_s = k_b + q_s,  q_s = c_s dl k'_{s-1},
+        //   k^i' = coef k^i - 2 dphi/dx^i k0^2,   k0' = coef0 k0,
+        //   coef = (2/c^2) dphi/dlambda - h,  coef0 = -h - (2/c^2) grad(phi).k,
+        // with h = 2 (a'/a) k0 the Hubble drag (integrator.h:437-441).  The
+        // drag sets |k| and the redshift, so it is formed once per step in FP64
+        // at b, h_b, and each stage contributes its relative change
+        // h_s = h_b (1 + eps_s) (eps ~ dl/L, FP32).  Then
+        //   k^i_new = k^i_b + dl/6 (k^i_b sum w coef_s + sum w (coef_s q^i_s - 2 dphi/dx^i k0_s^2))
+        //   x^i_new = x^i_b + dl/L k^i_b + dl/(6 L) sum w q^i_s
+        //   t_new   = t_b + dl k0_b + dl/6 sum w q0_s
+        //   a_new   = a_b + dl k0_b a'_b (1 + sum w ((1 + u_s)(1 + q0_s / k0_b) - 1) / 6)
+        // with u_s the stage's relative change of a'.  The terms that set the
+        // direction of k, |k| and the positions (k_b times the FP64 rates,
+        // dl k_b) are FP64 products; the FP32 parts are corrections of
+        // relative size dl/L (1e-4 to 1e-3 of the state).
+        // da/dt at b (FP64, from the bracket carried along the ray) and the
+        // distance to the bracket's upper node; the stages' da/dt follow the
+        // table's linear pieces in FP32 from there.
+        int ib;
+        double adb;
+        float tnext;
+        {
+            const int n = C.n;
+            while (tb < n && !(b.t < __ldg(C.t + tb))) ++tb;
+            while (tb > 0 && b.t < __ldg(C.t + tb - 1)) --tb;
+            ib = tb + (n > 1) * ((tb <= 0) - (tb >= n));
+            if (n > 1) {
+                adb = __ldg(C.dadt + ib - 1) + __ldg(C.slope_dadt + ib - 1) * (b.t - __ldg(C.t + ib - 1));
+                tnext = (ib < n - 1) ? (float)(__ldg(C.t + ib) - b.t) : __int_as_float(0x7f800000);
             } else {
-                Field7 g = hom;
-                if (!born) {
-                    const float cc = (float)pc * cells_per_unit(here.level);
-                    const PosStage ps{bc[2], bc[3], bc[4], pc, pk[0], pk[1], pk[2]};
-                    const Loc d = locate_rel(T, here, fmaf(cc, kfs[0], here.fd[0]), fmaf(cc, kfs[1], here.fd[1]),
-                                             fmaf(cc, kfs[2], here.fd[2]), ps);
-                    g = gather_at<ORDER>(T, d, ps, false, st, ST_RK_REC, false);
-                }
-                rhs_math(C, g, core, recip(core[0]), tb, dc, kfs);
-            }
-            const double cs = (sg < 2) ? 0.5 * dl : dl;
-            const double wa = (sg == 0) ? 0.0 : 2.0;
-            if (sg < 3) {
-#pragma unroll
-                for (int q = 0; q < 9; ++q) {
-                    acc[q] = (sg == 0) ? dc[q] : acc[q] + wa * dc[q];
-                    if (q < 2 || q > 4) core[q] = bc[q] + cs * dc[q];
-                }
-                pc = cs * inv_scale;   // positions: dx/dl = k / scale
-                pk[0] = dc[2]; pk[1] = dc[3]; pk[2] = dc[4];
+                adb = (n > 0) ? __ldg(C.dadt) : 0.0;
+                tnext = __int_as_float(0x7f800000);
             }
         }
-        const double dl6 = dl * (1.0 / 6.0);
-        const double dl6p = dl6 * inv_scale;
-#pragma unroll
-        for (int q = 0; q < 9; ++q) core[q] = bc[q] + ((q >= 2 && q <= 4) ? dl6p : dl6) * (acc[q] + dc[q]);
-        p.a = core[0]; p.t = core[1]; p.x = core[2]; p.y = core[3]; p.z = core[4];
-        p.k0 = core[5]; p.k1 = core[6]; p.k2 = core[7]; p.k3 = core[8];
+        // da/dt(b.t + dt) - da/dt(b.t) along the table's pieces (dt >= 0; the
+        // last piece extends past the table's end, as in Utility::interpolate)
+        auto dadot = [&](float dt) -> float {
+            if (C.n <= 1) return 0.f;
+            float tn = tnext, rem = dt, r = 0.f;
+            float sl = __ldg(&C.seg[ib - 1].x);
+            int j = ib;
+            for (int guard = 0; rem > tn && guard < 64; ++guard) {
+                r = fmaf(sl, tn, r);
+                rem -= tn;
+                const float2 sj = __ldg(C.seg + j);
+                sl = sj.x;
+                tn = (j + 2 < C.n) ? sj.y : __int_as_float(0x7f800000);
+                ++j;
+            }
+            return fmaf(sl, rem, r);
+        };
+        const double dlL = dl * inv_scale;
+        const double hubb = 2.0 * adb * recip(b.a) * b.k0;
+        const float dlf = (float)dl, dlLf = (float)dlL, hubbf = (float)hubb;
+        const float kb0 = (float)b.k0, kb1 = (float)b.k1, kb2 = (float)b.k2, kb3 = (float)b.k3;
+        const float abf = (float)b.a, adbf = (float)adb;
+        const float inv_kb0 = 1.f / kb0, inv_adbf = (adbf != 0.f) ? 1.f / adbf : 0.f;
+        const float cpu = cells_per_unit(here.level);
+        // previous stage: its k' (d0..d3), a' (dA) and k (pk0..pk3)
+        float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f, dA = 0.f;
+        float pk0 = kb0, pk1 = kb1, pk2 = kb2, pk3 = kb3;
+        // weighted sums over the stages: the gravitational parts of coef and
+        // coef0 (Gd, Gk), the drag's relative changes (Se), the second-order
+        // terms of k (E), the stage increments (S) and the a' terms (SA)
+        float Gd = 0.f, Gk = 0.f, Se = 0.f, E0 = 0.f, E1 = 0.f, E2 = 0.f, E3 = 0.f;
+        float S0 = 0.f, S1 = 0.f, S2 = 0.f, S3 = 0.f, SA = 0.f;
+        float dtf;   // the step's conformal-time increment
+#pragma unroll 1
+        for (int sg = 0; sg < 4; ++sg) {
+            const float cfr = (sg == 0) ? 0.f : ((sg < 3) ? 0.5f : 1.f);
+            const float w = (sg == 0 || sg == 3) ? 1.f : 2.f;
+            const float cdl = cfr * dlf;
+            const float q0 = cdl * d0, q1 = cdl * d1, q2 = cdl * d2, q3 = cdl * d3;
+            const float k0 = kb0 + q0, k1 = kb1 + q1, k2 = kb2 + q2, k3 = kb3 + q3;
+            const float as = fmaf(cdl, dA, abf);
+            const float dad = dadot(cdl * pk0);
+            // stage 1 is at b, where the previous step's post-step gather read
+            // the field (data); stages 2-4 are located from their FP32 offset
+            // to b's cell, their float64 coordinates formed only on the rare
+            // full-walk / restart paths
+            Field7 g = data;
+            if (sg > 0) {
+                g = hom;
+                if (!born) {
+                    const float cc = cfr * dlLf * cpu;
+                    const PosStage ps{b.x, b.y, b.z, (double)cfr * dlL, (double)pk1, (double)pk2, (double)pk3};
+                    const Loc d = locate_rel(T, here, fmaf(cc, pk1, here.fd[0]), fmaf(cc, pk2, here.fd[1]),
+                                             fmaf(cc, pk3, here.fd[2]), ps);
+                    g = gather_at<ORDER>(T, d, ps, false, st, ST_RK_REC, false);
+                }
+            }
+            const float gk = g.dx * k1 + (g.dy * k2 + g.dz * k3);
+            const float dphidl = fmaf(g.dt, k0, gk);
+            // the drag at the stage relative to b: a' (1 + u), a / (1 - v'), k0 (1 + wk)
+            const float u = dad * inv_adbf, v = -(cdl * dA) / as, wk = q0 * inv_kb0;
+            const float eps = u + v + wk + (u * v + u * wk + v * wk) + u * v * wk;
+            const float hub = hubbf * (1.f + eps);
+            const float coef = two_c2 * dphidl - hub;
+            const float coef0 = -hub - two_c2 * gk;
+            const float k02 = 2.f * k0 * k0;
+            const float G1 = g.dx * k02, G2 = g.dy * k02, G3 = g.dz * k02;
+            Gd = fmaf(w, two_c2 * dphidl, Gd);
+            Gk = fmaf(w, two_c2 * gk, Gk);
+            Se = fmaf(w, eps, Se);
+            E0 = fmaf(w, coef0 * q0, E0);
+            E1 = fmaf(w, fmaf(coef, q1, -G1), E1);
+            E2 = fmaf(w, fmaf(coef, q2, -G2), E2);
+            E3 = fmaf(w, fmaf(coef, q3, -G3), E3);
+            S0 = fmaf(w, q0, S0); S1 = fmaf(w, q1, S1); S2 = fmaf(w, q2, S2); S3 = fmaf(w, q3, S3);
+            SA = fmaf(w, u + wk + u * wk, SA);
+            d0 = coef0 * k0;
+            d1 = fmaf(coef, k1, -G1); d2 = fmaf(coef, k2, -G2); d3 = fmaf(coef, k3, -G3);
+            dA = k0 * (adbf + dad);
+            pk0 = k0; pk1 = k1; pk2 = k2; pk3 = k3;
+        }
+        {
+            const double dl6 = dl * (1.0 / 6.0), dlL6 = dlL * (1.0 / 6.0);
+            const float dl6f = (float)dl6, dlL6f = (float)dlL6;
+            const double h6 = hubb * (6.0 + (double)Se);
+            const double cd = dl6 * ((double)Gd - h6);
+            p.k0 = fma(b.k0, dl6 * (-h6 - (double)Gk), b.k0 + (double)(dl6f * E0));
+            p.k1 = fma(b.k1, cd, b.k1 + (double)(dl6f * E1));
+            p.k2 = fma(b.k2, cd, b.k2 + (double)(dl6f * E2));
+            p.k3 = fma(b.k3, cd, b.k3 + (double)(dl6f * E3));
+            p.x = fma(dlL, b.k1, b.x + (double)(dlL6f * S1));
+            p.y = fma(dlL, b.k2, b.y + (double)(dlL6f * S2));
+            p.z = fma(dlL, b.k3, b.z + (double)(dlL6f * S3));
+            p.t = fma(dl, b.k0, b.t + (double)(dl6f * S0));
+            const double da = dl * b.k0 * adb;
+            p.a = fma(da, (double)(SA * (1.f / 6.f)), b.a + da);
+            // the step's displacement and conformal-time increment in FP32
+            // (path length s and the ISW integral)
+            const float ex = fmaf(dlLf, kb1, dlL6f * S1), ey = fmaf(dlLf, kb2, dlL6f * S2), ez = fmaf(dlLf, kb3, dlL6f * S3);
+            sacc += (double)sqrtf(ex * ex + ey * ey + ez * ez);
+            dtf = fmaf(dlf, kb0, dl6f * S0);
+        }
         const Loc ploc = locate_near(T, here, p.x, p.y, p.z);
         data = born ? hom : gather_at<ORDER>(T, ploc, PosAt{p.x, p.y, p.z}, true, st, ST_POST_REC, false);
         {
@@ -762,7 +871,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         p.dt = -data.dt;
         const float dphi_last = data.phi - (float)b.phi;   // laplacian of the final record, divided at the end
         const double dl_last = dl;
-        isw += (double)(b.dt + p.dt) * (p.t - b.t) * (1.0 / c2);
+        isw += (double)((b.dt + p.dt) * dtf * inv_c2f);
         if (O.final_rec) {   // only the final photon record reports it
             iswold -= 2.0 * (p.phi - b.phi) * (1.0 / c2) -
                       (((double)b.dx + (double)p.dx) * (p.x - b.x) * scale + ((double)b.dy + (double)p.dy) * (p.y - b.y) * scale +
@@ -770,12 +879,12 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         }
         p.chi = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
         lambda += dl;
-        sacc += (double)sqrtf((float)((p.x - b.x) * (p.x - b.x) + (p.y - b.y) * (p.y - b.y) + (p.z - b.z) * (p.z - b.z)));
-        const double inv_pa = recip(p.a);
-        p.red = a0 * inv_pa * (1.0 + phi0c2 - p.phi * (1.0 / c2)) - 1.0;
         p.isw = isw; p.iswold = iswold; p.lambda = lambda; p.s = sacc;
+        bool p_red_ok = false;
+        auto need_p_red = [&]() { if (!p_red_ok) { p.red = red_of(p); p_red_ok = true; } };
+        auto need_b_red = [&]() { if (!b_red_ok) { b.red = red_of(b); b_red_ok = true; } };
         if (!is_empty(data)) {
-            ratio = p.a * p.a * ratio_k;
+            const double ratio = p.a * p.a * ratio_k;
             dl = (ploc.cell >= 0 ? cell_extent(ploc.level) : 0.0) * ratio;
             last_data_dt = data.dt;
             last_dphi = dphi_last;
@@ -787,31 +896,41 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             if (P.jacobian) {
                 float h3[3];
                 jac_fast(T, here, p.x, p.y, p.z, h3, st);
-                const double dr = p.chi - b.chi;
+                const float dr = (float)(p.chi - b.chi), chif = (float)p.chi;
                 chim2 = chim1; chim1 = b.chi;
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     J.ckm1(q) = J.ck(q); J.ckm1(3 + q) = J.ck(3 + q);
-                    const double hd = (double)h3[q] * dr;
-                    const double c1 = p.chi * hd, c2v = p.chi * p.chi * hd;
+                    const float c1 = chif * (h3[q] * dr), c2v = chif * c1;
                     J.ck(q) = c1;
                     J.ck(3 + q) = c2v;
-                    J.S(q) += c1;
-                    J.S(3 + q) += c2v;
+                    J.S(q) += (double)c1;
+                    J.S(3 + q) += (double)c2v;
                 }
             }
             while (next_plane < np) {
                 const int kind = skind;
                 const double* kj = (WIDE && rki && kind == STOP_PLANE) ? rki + 3 * next_plane : nullptr;
-                const double q1 = kj ? (p.x * kj[0] + p.y * kj[1] + p.z * kj[2])
-                                : (kind == STOP_R) ? p.chi : (kind == STOP_LAMBDA) ? p.lambda : (kind == STOP_T) ? p.t
-                                : (kind == STOP_A) ? p.a : (kind == STOP_S) ? p.s : p.red;
                 const double ref = SRC ? stop_ref : rpl[next_plane];
-                if (!((kind == STOP_A) ? (q1 < ref) : (q1 > ref))) break;
+                bool crossed;
+                if (!kj && kind == STOP_REDSHIFT) {
+                    crossed = red_above(p, ref);
+                } else {
+                    const double q1 = kj ? (p.x * kj[0] + p.y * kj[1] + p.z * kj[2])
+                                    : (kind == STOP_R) ? p.chi : (kind == STOP_LAMBDA) ? p.lambda : (kind == STOP_T) ? p.t
+                                    : (kind == STOP_A) ? p.a : (kind == STOP_S) ? p.s : (need_p_red(), p.red);
+                    crossed = (kind == STOP_A) ? (q1 < ref) : (q1 > ref);
+                }
+                if (!crossed) break;
                 const int j = next_plane++;
                 cross_k[j] = k;
                 if (prow) {
+                    need_p_red();
+                    need_b_red();
                     double* o = prow + j * rec_fields;
+                    const double q1 = kj ? (p.x * kj[0] + p.y * kj[1] + p.z * kj[2])
+                                    : (kind == STOP_R) ? p.chi : (kind == STOP_LAMBDA) ? p.lambda : (kind == STOP_T) ? p.t
+                                    : (kind == STOP_A) ? p.a : (kind == STOP_S) ? p.s : p.red;
                     const double q0 = kj ? (b.x * kj[0] + b.y * kj[1] + b.z * kj[2])
                                     : (kind == STOP_R) ? b.chi : (kind == STOP_LAMBDA) ? b.lambda : (kind == STOP_T) ? b.t
                                     : (kind == STOP_A) ? b.a : (kind == STOP_S) ? b.s : b.red;
@@ -845,11 +964,11 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                         if (p.chi <= jd) {
                             for (int q = 0; q < 3; ++q) { s1[q] = J.S(q); s2[q] = J.S(3 + q); }
                         } else if (chim1 <= jd) {
-                            for (int q = 0; q < 3; ++q) { s1[q] = J.S(q) - J.ck(q); s2[q] = J.S(3 + q) - J.ck(3 + q); }
+                            for (int q = 0; q < 3; ++q) { s1[q] = J.S(q) - (double)J.ck(q); s2[q] = J.S(3 + q) - (double)J.ck(3 + q); }
                         } else if (k >= 2 && chim2 <= jd) {
                             for (int q = 0; q < 3; ++q) {
-                                s1[q] = J.S(q) - J.ck(q) - J.ckm1(q);
-                                s2[q] = J.S(3 + q) - J.ck(3 + q) - J.ckm1(3 + q);
+                                s1[q] = J.S(q) - (double)J.ck(q) - (double)J.ckm1(q);
+                                s2[q] = J.S(3 + q) - (double)J.ck(3 + q) - (double)J.ckm1(3 + q);
                             }
                         } else {
                             ok = false;
@@ -871,8 +990,9 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             if (!have_rmax || rmax < (double)b.rho) rmax = b.rho;
             have_rmax = true;
             b = p;
-            inv_a = inv_pa;
+            b_red_ok = p_red_ok;
             if (WIDE && traj) {
+                need_b_red();
                 if (k < O.traj_cap) write_rec(traj + k * kPhotonFields, fast_record(b, last_data_dt, (double)last_dphi / last_dl, k));
                 else status |= 8u;
             }
@@ -881,7 +1001,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         switch (skind) {
         case STOP_R: stop = b.chi > stop_ref; break;
         case STOP_LAMBDA: stop = b.lambda > stop_ref; break;
-        case STOP_REDSHIFT: stop = b.red > stop_ref; break;
+        case STOP_REDSHIFT: stop = b_red_ok ? (b.red > stop_ref) : red_above(b, stop_ref); break;
         case STOP_T: stop = b.t > stop_ref; break;
         case STOP_A: stop = b.a < stop_ref; break;
         case STOP_PLANE: {
@@ -894,6 +1014,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         }
         if (stop) break;
     }
+    if (!b_red_ok) b.red = red_of(b);
     long long size = k + 1;
     if (signbit(b.red) || signbit(b.a)) size -= 1;
     O.steps[i] = size;
@@ -965,8 +1086,9 @@ __global__ void MPF_FAST_BOUNDS k_propagate_fast(DevTree T, DevCosmo C, PropPara
                                                                     const double* __restrict__ launch, long long n, PropOut O,
                                                                     unsigned long long* queue)
 {
-    __shared__ double jac_sh[18 * kFastThreads];
-    const JacSums J{jac_sh + threadIdx.x};
+    __shared__ double jac_sums[6 * kFastThreads];
+    __shared__ float jac_terms[12 * kFastThreads];
+    const JacSums J{jac_sums + threadIdx.x, jac_terms + threadIdx.x};
     const int lane = threadIdx.x & 31;
     for (;;) {
         unsigned long long base = 0;
