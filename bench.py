@@ -54,10 +54,34 @@ UNIT = "photon-steps/s"
 # + post-step 27 x 28 B + Jacobian 6 x 27 x 12 B
 BYTES_PER_PHOTON_STEP = 4 * 27 * 16 + 27 * 28 + 6 * 27 * 12
 # DRAM bytes per photon-step of the propagate kernel, from one ncu capture of the
-# same kernel on the medium octree (65 536 rays to z = 0.5): (37.79 + 1.43) MB
+# same kernel on the medium octree (65 536 rays to z = 0.5): (37.66 + 1.93) MB
 # over 6.95e7 photon-steps; the bench's per-launch traffic is this figure times
 # the photon-steps of a launch
-DRAM_BYTES_PER_PHOTON_STEP = 0.564
+DRAM_BYTES_PER_PHOTON_STEP = 0.57
+# FP64 add + fma + mul thread operations per photon-step of the same capture
+# (smsp__sass_thread_inst_executed_op_{dadd,dfma,dmul}_pred_on): the
+# arithmetic that bounds the kernel on this part, whose FP64 pipe retires 2
+# operations per SM per cycle (sm__sass_thread_inst_executed_op_dfma_pred_on
+# .sum.peak_sustained = 304 per cycle for 152 SMs)
+FP64_OPS_PER_PHOTON_STEP = 137
+FP64_OPS_PER_SM_CYCLE = 2
+
+
+def fp64_roofline(photon_steps_per_s, clocks):
+    """FP64 arithmetic throughput of the propagate kernel against the part's
+    FP64 peak at the SM clock sampled during the timed region."""
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    sms = 152
+    try:
+        import torch
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    except Exception:
+        pass
+    peak = sms * FP64_OPS_PER_SM_CYCLE * mhz * 1e6 / 1e12
+    achieved = photon_steps_per_s * FP64_OPS_PER_PHOTON_STEP / 1e12
+    return {"achieved": achieved, "peak": peak, "unit": "TFLOP/s (FP64 add/fma/mul thread ops)", "frac": achieved / peak,
+            "ops_per_photon_step": FP64_OPS_PER_PHOTON_STEP,
+            "source": "ops per photon-step from the ncu capture of the medium octree; peak = SMs x 2 x sampled SM clock"}
 
 
 def workload_spec(synth, workload: str):
@@ -556,6 +580,8 @@ def main():
                 "traffic": (DRAM_BYTES_PER_PHOTON_STEP * photon_steps / args.steps) if DRAM_BYTES_PER_PHOTON_STEP else None,
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "bytes_per_photon_step": BYTES_PER_PHOTON_STEP}
+    clk_summary = clk.summary()
+    roofline["fp64"] = fp64_roofline(value / world, clk_summary)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
@@ -563,7 +589,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": B * 6 * 8,
                     "d2h_bytes_per_step": B * 8 + B * capi.MPF_PLANE_FIELDS * 8},
             "gpu_launches": args.steps, "roofline": roofline, "status_bits": status,
-            "clocks": clk.summary()}
+            "clocks": clk_summary}
     if rank == 0 and not args.no_cpu_baseline:
         import oracle as oracle_mod
         oracle_mod.build()
