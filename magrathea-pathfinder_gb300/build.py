@@ -28,6 +28,7 @@ UNITS = [
     ("mpf_capi.cu", []),
     ("mpf_noalloc.cu", []),
     ("mpf_catalogue.cu", ["-fmad=false"]),
+    ("mpf_cat_persist.cu", []),
     ("mpf_maps.cu", ["-fmad=false"]),
     ("mpf_surrogate.cu", []),
     ("mpf_rays.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),

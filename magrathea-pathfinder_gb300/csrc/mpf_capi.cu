@@ -354,6 +354,9 @@ int mpf_catalogue_newton_device(const mpf_octree* o, const mpf_cosmology* c, con
         stats->iterations = st.iterations;
         stats->kernel_launches = st.launches;
     }
+    if (status & mpf::kCatQueueError)
+        return set_err(MPF_DEVICE_TIMEOUT, std::string("mpf_catalogue_newton: the device work queue lost a source (a bounded "
+                                                       "wait ran out): ") + mpf::catalogue_queue_message());
     if (status & 1u) return set_err(MPF_WARN_MAX_STEPS, "mpf_catalogue_newton: a ray reached max_steps");
     return MPF_OK;
 }

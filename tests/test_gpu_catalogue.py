@@ -202,3 +202,23 @@ def test_catalogue_ngp_matches_reference(cat_setup, pkg, exact):
     rows, stats, rc = _run(pkg, g, tree, cos, 0, exact, float(g["cat_accuracy"][0]))
     assert rc == 0
     assert _compare(rows, g["ref_cat_o0_a0"], True) >= 30
+
+
+def test_catalogue_work_queue_plan_reuse(cat_setup, pkg):
+    """Fast mode runs as one persistent launch fed by a device work queue,
+    from a CUDA graph kept per stream and reused by later calls with at most
+    as many sources; a larger batch builds it again.  A source's rays do not
+    depend on the other sources of the call, so its row is bit-identical
+    whatever the batch: the first call, a smaller one reusing the plan, and a
+    batch beyond the plan's capacity holding the same sources many times."""
+    g, tree, cos = cat_setup
+    src = g["cat_src"]
+    ref, st, _ = _run(pkg, g, tree, cos, 2, False, 1e-8)
+    assert st["kernel_launches"] == 1          # one graph launch
+    assert st["rays"] >= src.shape[0]
+    small, _, _ = _run(pkg, g, tree, cos, 2, False, 1e-8, src=src[:13])
+    np.testing.assert_array_equal(small.view(np.uint64), ref[:13].view(np.uint64))
+    reps = (1 << 16) // src.shape[0] + 2
+    big, st_big, _ = _run(pkg, g, tree, cos, 2, False, 1e-8, src=np.tile(src, (reps, 1)))
+    np.testing.assert_array_equal(big.view(np.uint64), np.tile(ref, (reps, 1)).view(np.uint64))
+    assert st_big["rays"] == reps * st["rays"]
