@@ -224,8 +224,11 @@ def parity_entry(pkg, tree, cosmo, length, planes, oracle_run, exact=False):
 
 CAT_METRIC = "catalogue sources/s (Newton root-finder to cat_accuracy 1e-8, TSC, <=11 rays per source)"
 CAT_UNIT = "sources/s"
-# payload bytes per photon-step without the lensing Jacobian (rounds 0-2 of the root-finder)
+# payload bytes per photon-step without the lensing Jacobian (rounds 0-1 of the root-finder)
 BYTES_PER_PHOTON_STEP_NOJAC = 4 * 27 * 16 + 27 * 28
+# CIC: 4 RK stages x 8 cells x 16 B + post-step 8 x 28 B (+ Jacobian 6 x 27 x 12 B, always TSC)
+BYTES_PER_PHOTON_STEP_CIC_NOJAC = 4 * 8 * 16 + 8 * 28
+BYTES_PER_PHOTON_STEP_CIC = BYTES_PER_PHOTON_STEP_CIC_NOJAC + 6 * 27 * 12
 
 
 def catalogue_sources(synth, n, seed, zmax=2.0, half_deg=4.5):
@@ -431,8 +434,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=262144,
                     help="rays per step (the persistent launch's tail of long rays is a smaller share of a larger batch)")
-    ap.add_argument("--workload", default="amr", choices=["amr", "medium", "small"],
-                    help="amr = the benchmark configuration; medium / small for profiling and debugging")
+    ap.add_argument("--workload", default="amr", choices=["amr", "medium", "small", "cones16"],
+                    help="amr = the benchmark configuration; cones16 = the catalogue over 16 cones of the uniform "
+                         "64^3 field (with --mode catalogue); medium / small for profiling and debugging")
     ap.add_argument("--exact", action="store_true", help="reference float64 gather order")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--zstop", type=float, default=2.0, help="stop redshift (profiling captures use a short path)")
@@ -582,6 +586,10 @@ def main():
                 "bytes_per_photon_step": BYTES_PER_PHOTON_STEP}
     clk_summary = clk.summary()
     roofline["fp64"] = fp64_roofline(value / world, clk_summary)
+    tuned = pkg.autotune_info(tree, "propagate", 2)
+    config["autotune"] = ({"threads_per_block": tuned[0], "rays_per_lane_per_claim": tuned[1],
+                           "candidates_photon_steps_per_s": dict(zip(("128x1", "64x1", "32x1", "128x2"), tuned[2]))}
+                          if tuned else None)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
@@ -601,30 +609,95 @@ def main():
         dist.destroy_process_group()
 
 
+# 16 narrow cones over the 64^3 uniform field (octree level 8) to z = 2, the
+# cones' axes on a 4 x 4 grid of narrow-cone angles (phi, theta)
+CONES16_AXES = [(p, t) for p in (-45.0, -15.0, 15.0, 45.0) for t in (-45.0, -15.0, 15.0, 45.0)]
+
+
+def cones16_records(synth):
+    """One octree shared by the 16 cones: the union of the cones' cells (the
+    field of a cell depends only on its key, so shared cells agree)."""
+    key = "cones16_v1"
+    path = os.path.join(os.environ.get("TMPDIR", "/tmp"), "mpf_bench_%s.bin" % key)
+    if os.path.exists(path):
+        return synth.read_bin(path)
+    parts = [synth.make_octree(synth.uniform_grid_cone(2.0, ax)) for ax in CONES16_AXES]
+    rec = np.concatenate(parts)
+    order = np.lexsort((rec["lo"], rec["hi"]))
+    rec = rec[order]
+    keep = np.ones(rec.shape[0], dtype=bool)
+    keep[1:] = (rec["hi"][1:] != rec["hi"][:-1]) | (rec["lo"][1:] != rec["lo"][:-1])
+    rec = rec[keep]
+    tmp = path + ".%d" % os.getpid()
+    synth.write_bin(tmp, rec)
+    os.replace(tmp, path)
+    return rec
+
+
+def cones16_sources(synth, n, seed, zmin=0.05, zmax=2.0, half_deg=2.4):
+    """Sources uniform in the light-cone volume between zmin and zmax, spread
+    evenly over the 16 cones (square 2 half_deg cones about their axes)."""
+    cosmo = synth.Cosmology()
+    c0, c1 = (float(cosmo.chi_of_z(z)[0]) / 2048.0 for z in (zmin, zmax))
+    rng = np.random.default_rng(seed)
+    d = (c0 ** 3 + (c1 ** 3 - c0 ** 3) * rng.random(n)) ** (1.0 / 3.0)
+    ph = np.radians(rng.uniform(-half_deg, half_deg, n))
+    th = np.pi / 2 + np.radians(rng.uniform(-half_deg, half_deg, n))
+    local = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], axis=1)
+    cone = np.arange(n) % len(CONES16_AXES)
+    frames = np.stack([synth.cone_frame(*ax) for ax in CONES16_AXES])
+    dirs = np.einsum("nij,nj->ni", frames[cone], local)
+    src = np.zeros((n, 8))
+    src[:, 0:3] = dirs * d[:, None]
+    src[:, 3:6] = rng.normal(0.0, 1e-3, (n, 3))
+    src[:, 6] = np.arange(n)
+    src[:, 7] = 1.0
+    return src
+
+
 def run_catalogue(args, synth, spec, cos, length, world, rank, local, dist):
     h = spec.cosmo.h
-    config = {"workload": "catalogue on the AMR cone octree (256^3 base refined to level 14 in 2000 NFW haloes): "
-                          "%d sources per step uniform in comoving volume to z=2 inside 9x9 deg, cat_accuracy 1e-8, "
-                          "TSC, 8 steps/cell" % args.sources if args.workload == "amr"
-              else "catalogue on the %s octree (profiling / debugging)" % args.workload,
-              "sources_per_step": args.sources, "streams": "steps alternate between 2 host threads / CUDA streams", "order": "TSC", "nsteps": 8, "cat_accuracy": 1e-8,
-              "max_rays_per_source": 11,
+    cones16 = args.workload == "cones16"
+    if cones16:
+        workload = ("catalogue over 16 narrow cones of the 64^3 uniform field at octree level 8 (file level 6), axes "
+                    "phi, theta in {-45,-15,15,45} deg, one shared octree to z=2: %d sources per step uniform in the "
+                    "light-cone volume between z=0.05 and z=2 (path lengths up to 24x apart), all 16 cones in each "
+                    "call, cat_accuracy 1e-8, CIC, 10 steps/cell" % args.sources)
+    elif args.workload == "amr":
+        workload = ("catalogue on the AMR cone octree (256^3 base refined to level 14 in 2000 NFW haloes): "
+                    "%d sources per step uniform in comoving volume to z=2 inside 9x9 deg, cat_accuracy 1e-8, "
+                    "TSC, 8 steps/cell" % args.sources)
+    else:
+        workload = "catalogue on the %s octree (profiling / debugging)" % args.workload
+    config = {"workload": workload, "sources_per_step": args.sources,
+              "streams": "steps alternate between 2 host threads / CUDA streams", "order": "CIC" if cones16 else "TSC",
+              "nsteps": 10 if cones16 else 8, "cat_accuracy": 1e-8, "max_rays_per_source": 11,
               "gather_arithmetic": "float64 reference order" if args.exact else "fp32 gather, fp64 state",
-              "l2": "octree larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single GPU"}
-    kw = dict(cat_accuracy=1e-8, nsteps=8, order=2, vobs=(0.0, 0.0, 0.0), max_iterations=10)
+              "execution": "one CUDA graph launch per call: set-up, sort, one persistent kernel on a device work queue"
+                           if not args.exact else "one ray launch per Newton round",
+              "l2": "octree smaller than L2 (the 16 cones of a 64^3 field)" if cones16 else "octree larger than L2 (no flush)",
+              "parallelism": "replicas" if world > 1 else "single GPU"}
+    kw = dict(cat_accuracy=1e-8, nsteps=10 if cones16 else 8, order=1 if cones16 else 2, vobs=(0.0, 0.0, 0.0),
+              max_iterations=10)
     nsrc = args.sources
+
+    def records():
+        return cones16_records(synth) if cones16 else octree_records(synth, spec)
+
+    def make_sources(count, seed):
+        return cones16_sources(synth, count, seed) if cones16 else catalogue_sources(synth, count, seed)
     if args.impl == "reference":
         if rank != 0:
             return
         import oracle as oracle_mod
         oracle_mod.build()
-        rec = octree_records(synth, spec)
+        rec = records()
         nthreads = os.cpu_count() or 1
         O = oracle_mod.Oracle(rec, {"t": cos[0], "a": cos[1], "dadt": cos[2]}, length, nthreads=nthreads)
         per_step = nthreads
         times, counts = [], 0
         for s in range(args.warmup + args.steps):
-            src = catalogue_sources(synth, per_step, 1000 + s)
+            src = make_sources(per_step, 1000 + s)
             t0 = time.perf_counter()
             O.catalogue(src, h=h, **kw)
             dt = time.perf_counter() - t0
@@ -648,14 +721,14 @@ def run_catalogue(args, synth, spec, cos, length, world, rank, local, dist):
     importlib.import_module(PKG + ".build").build()
     lib = pkg.library()
     capi = importlib.import_module(PKG + ".capi")
-    rec = octree_records(synth, spec)
+    rec = records()
     tree = pkg.Octree.from_records(rec)
     info = tree.info
     config.update({"cells": int(info["cells"]), "levels": [info["level_min"], info["level_max"]]})
     cosmo = pkg.Cosmology(*cos)
     dev = torch.device("cuda", local)
     nstep = args.warmup + args.steps
-    pool = catalogue_sources(synth, nsrc * nstep, 7 + rank)
+    pool = make_sources(nsrc * nstep, 7 + rank)
     d_src = torch.from_numpy(pool).to(dev)
     # two host threads, each with its own stream and rows, take the steps in
     # turn: the Newton rounds of one call wait on host syncs and end with a
@@ -729,13 +802,18 @@ def run_catalogue(args, synth, spec, cos, length, world, rank, local, dist):
 
     peak, peak_kind = measured_peak_hbm()
     avg_s = (elapsed_ms / args.steps) / 1000.0   # the calls overlap: each one's share of the timed region
-    alg_bytes = (BYTES_PER_PHOTON_STEP_NOJAC * (psteps - psteps_jac) + BYTES_PER_PHOTON_STEP * psteps_jac) / args.steps
+    b_jac, b_nojac = (BYTES_PER_PHOTON_STEP_CIC, BYTES_PER_PHOTON_STEP_CIC_NOJAC) if cones16 else \
+        (BYTES_PER_PHOTON_STEP, BYTES_PER_PHOTON_STEP_NOJAC)
+    alg_bytes = (b_nojac * (psteps - psteps_jac) + b_jac * psteps_jac) / args.steps
     achieved = alg_bytes / avg_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": (DRAM_BYTES_PER_PHOTON_STEP * psteps / args.steps) if DRAM_BYTES_PER_PHOTON_STEP else None,
-                "peak_source": peak_kind, "scope": "whole mpf_catalogue_newton_device call (all rounds, host syncs)",
-                "bytes_per_photon_step": {"with_jacobian": BYTES_PER_PHOTON_STEP,
-                                          "without_jacobian": BYTES_PER_PHOTON_STEP_NOJAC}}
+                "traffic": (DRAM_BYTES_PER_PHOTON_STEP * psteps / args.steps) if DRAM_BYTES_PER_PHOTON_STEP and not cones16
+                else None,
+                "peak_source": peak_kind, "scope": "whole mpf_catalogue_newton_device call (set-up, sort, persistent kernel)",
+                "bytes_per_photon_step": {"with_jacobian": b_jac, "without_jacobian": b_nojac}}
+    tuned = pkg.autotune_info(tree, "catalogue", kw["order"])
+    config["autotune"] = ({"threads_per_block": tuned[0], "candidates_photon_steps_per_s": {"128": tuned[2][0],
+                           "64": tuned[2][1], "32": tuned[2][2]}} if tuned else None)
     line = {"metric": CAT_METRIC, "value": value, "unit": CAT_UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
@@ -749,7 +827,7 @@ def run_catalogue(args, synth, spec, cos, length, world, rank, local, dist):
         oracle_mod.build()
         nthreads = os.cpu_count() or 1
         O = oracle_mod.Oracle(rec, {"t": cos[0], "a": cos[1], "dadt": cos[2]}, length, nthreads=nthreads)
-        src = catalogue_sources(synth, 2 * nthreads, 99)
+        src = make_sources(2 * nthreads, 99)
         t0 = time.perf_counter()
         O.catalogue(src, h=h, **kw)
         dt = time.perf_counter() - t0

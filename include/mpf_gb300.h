@@ -151,6 +151,19 @@ int mpf_propagate_noalloc(const mpf_octree* o, const mpf_cosmology* c, const mpf
                           int64_t* steps, double* final_rec, double* plane_rec);
 const char* mpf_noalloc_last_error(void);
 
+/* Launch shape chosen by the library's autotuner for an octree on the
+ * current device: kind 0 = the propagation kernel (mpf_propagate*,
+ * mpf_hmaps_fill; the first batch of at least 2^17 rays is traced in four
+ * slices with 128 x 1, 64 x 1, 32 x 1 and 128 x 2 threads per block x rays
+ * per lane and work-queue claim, and the fastest in photon-steps/s is kept);
+ * kind 1 = the catalogue's persistent kernel (its first three calls of at
+ * least 2^16 sources run 128, 64 and 32 threads per block).  order: 1 (CIC)
+ * or 2 (TSC).  *threads_per_block = 0 when not tuned yet; rates[4] (may be
+ * NULL): the candidates' photon-steps/s.  No counterpart in the reference,
+ * which has no device launches to tune.  MPF_AUTOTUNE=0 in the environment
+ * keeps the default shape (128 threads, one ray per lane). */
+int mpf_autotune_info(const mpf_octree* o, int kind, int order, int* threads_per_block, int* claim_depth, double* rates);
+
 /* ------------------------------------------------------------------------ */
 /* Catalogue root-finder                                                     */
 /* ------------------------------------------------------------------------ */
@@ -211,9 +224,14 @@ typedef struct {
 int mpf_catalogue_newton(const mpf_octree* o, const mpf_cosmology* c, const mpf_catalogue_params* p, int64_t n,
                          const double* sources, int64_t stride, double* rows, mpf_catalogue_stats* stats);
 /* Same, with sources and rows in device memory, on `stream` (a cudaStream_t;
- * NULL = the legacy default stream).  The call synchronises the stream once
- * per Newton round (the size of each round decides the next launch) and
- * returns when the rows are complete. */
+ * NULL = the legacy default stream); returns when the rows are complete.
+ * With the FP32-gather kernel and the infinitesimal Jacobian the call is one
+ * CUDA graph launch: the sources' set-up and sort, then one persistent kernel
+ * that takes sources from a device work queue and puts back those needing
+ * another ray; the graph and its scratch are kept per stream and reused by
+ * later calls with at most as many sources.  Otherwise (exact mode, bundle or
+ * Born Jacobians) the call runs one batched ray launch per Newton round and
+ * synchronises the stream between rounds. */
 int mpf_catalogue_newton_device(const mpf_octree* o, const mpf_cosmology* c, const mpf_catalogue_params* p, int64_t n,
                                 const double* sources_device, int64_t stride, double* rows_device,
                                 mpf_catalogue_stats* stats, void* stream);

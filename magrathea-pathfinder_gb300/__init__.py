@@ -41,7 +41,8 @@ PLANE_FIELDS = ("firstid f x y z distance A11 A12 A22 t a redshift chi lambda s 
 CATALOGUE_FIELDS = ("phi theta phi_obs theta_obs miss iterations z_flrw z_pot z_dopp z_tdopp z_isw z_gr "
                     "a11 a12 a21 a22").split()
 
-__all__ = ["Octree", "Cosmology", "propagate", "rays_propagate", "catalogue", "hmaps_fill", "pix2vec_ring", "MpfError", "PHOTON_FIELDS", "PLANE_FIELDS",
+__all__ = ["Octree", "Cosmology", "propagate", "rays_propagate", "catalogue", "hmaps_fill", "pix2vec_ring", "autotune_info",
+           "MpfError", "PHOTON_FIELDS", "PLANE_FIELDS",
            "CATALOGUE_FIELDS", "library"]
 
 
@@ -325,6 +326,20 @@ def hmaps_fill(octree: Octree, cosmology: Cosmology, nside: int, pixels, surface
     capi.check(rc)
     del keep
     return maps
+
+
+def autotune_info(octree: Octree, kind: str = "propagate", order: int = 2):
+    """The autotuned launch shape for this octree: (threads per block, rays per
+    lane per work-queue claim, candidates' photon-steps/s), or None before the
+    first batch large enough to tune.  kind: "propagate" or "catalogue"."""
+    L = capi.load()
+    tpb, depth = C.c_int(), C.c_int()
+    rates = np.zeros(4)
+    capi.check(L.mpf_autotune_info(octree._h, 0 if kind == "propagate" else 1, int(order), C.byref(tpb), C.byref(depth),
+                                   capi.ptr(rates)))
+    if tpb.value == 0:
+        return None
+    return tpb.value, depth.value, rates[: 4 if kind == "propagate" else 3].tolist()
 
 
 def pix2vec_ring(nside: int, pixels) -> np.ndarray:

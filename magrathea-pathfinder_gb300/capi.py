@@ -30,7 +30,7 @@ EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_uplo
            "mpf_catalogue_newton_device", "mpf_hmaps_fill", "mpf_hmaps_fill_bundle", "mpf_pix2vec_ring",
            "mpf_surrogate_create", "mpf_surrogate_destroy", "mpf_surrogate_train", "mpf_surrogate_sample",
            "mpf_surrogate_get_params", "mpf_surrogate_set_params", "mpf_surrogate_loss_grad", "mpf_surrogate_eval",
-           "mpf_surrogate_propagate", "mpf_rays_propagate", "mpf_cells_build", "mpf_cells_parse")
+           "mpf_surrogate_propagate", "mpf_rays_propagate", "mpf_cells_build", "mpf_cells_parse", "mpf_autotune_info")
 
 MPF_TRAJECTORY_FIELDS = 29
 
@@ -148,6 +148,7 @@ def load(path: str = LIB_PATH):
     L.mpf_hmaps_fill_bundle.argtypes = [vp, vp, C.POINTER(Params), i64, i64, vp, C.c_int, vp, vp, C.c_int, C.c_int, d,
                                         vp]
     L.mpf_pix2vec_ring.argtypes = [i64, i64, vp, vp]
+    L.mpf_autotune_info.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
     L.mpf_cells_build.argtypes = [vp, i64, C.POINTER(CellsParams), vp, vp, i64, C.POINTER(i64)]
     L.mpf_cells_parse.argtypes = [C.c_char_p, i64, vp, i64, C.POINTER(i64)]
     L.mpf_rays_propagate.argtypes = [vp, vp, C.POINTER(Params), C.POINTER(BundleParams), i64, vp, vp, vp, vp]

@@ -150,6 +150,8 @@ void mpf_octree_destroy(mpf_octree* o)
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(o->device);
+    mpf::forget_tuned_shape((const void*)o->tree.keys);
+    mpf::catalogue_forget_tuned_shape((const void*)o->tree.keys);
     cudaFree(o->keys);
     cudaFree(o->grad);
     cudaFree(o->scal);
@@ -452,6 +454,28 @@ int mpf_hmaps_fill_bundle(const mpf_octree* o, const mpf_cosmology* c, const mpf
 {
     return hmaps_fill_impl(o, c, p, nside, npix, pixels, ncomp, components, homogeneous, maps, 1, plane_sachs,
                            stop_bundle, openingmin);
+}
+
+int mpf_autotune_info(const mpf_octree* o, int kind, int order, int* threads_per_block, int* claim_depth, double* rates)
+{
+    if (!o || !threads_per_block || !claim_depth || (kind != 0 && kind != 1) || (order != 1 && order != 2))
+        return set_err(MPF_BAD_INPUT, "mpf_autotune_info: bad argument");
+    int dev = 0;
+    const cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_err(e, "mpf_autotune_info");
+    *threads_per_block = 0;
+    *claim_depth = 0;
+    double r[4] = {0, 0, 0, 0};
+    int tpb = 0, depth = 1;
+    bool ok = (kind == 0) ? mpf::tuned_shape(dev, o->tree, mpf::plain_fast_mode(order), &tpb, &depth, r)
+                          : mpf::catalogue_tuned_shape(dev, o->tree, order, &tpb, r);
+    if (ok) {
+        *threads_per_block = tpb;
+        *claim_depth = depth;
+    }
+    if (rates)
+        for (int k = 0; k < 4; ++k) rates[k] = r[k];
+    return MPF_OK;
 }
 
 int mpf_pix2vec_ring(int64_t nside, int64_t n, const int64_t* pixels, double* vec)

@@ -22,6 +22,7 @@
 // parameters, and launches the graph.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -332,6 +333,7 @@ struct CatPlan {
     cudaGraphNode_t pnode = nullptr;   // the persistent kernel's node
     cudaKernelNodeParams pparams{};
     int grid = 0, tpb = 0;
+    int kernels = 0;                   // kernel nodes of the graph
 
     ~CatPlan()
     {
@@ -439,12 +441,40 @@ cudaError_t plan_build(CatPlan& pl, const DevTree& T, const DevCosmo& C, PropPar
         kp.kernelParams = args;
         kp.extra = nullptr;
         e = cudaGraphAddKernelNode(&pl.pnode, g, deps.data(), deps.size(), &kp);
+        size_t nn = 0;
+        if (e == cudaSuccess) e = cudaGraphGetNodes(g, nullptr, &nn);
+        pl.kernels = (int)nn;
         pl.pparams = kp;
         pl.pparams.kernelParams = nullptr;
     }
     pl.graph = g;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&pl.exec, g, 0);
     return e;
+}
+
+// Autotuning of the persistent kernel's block size (the grid is every SM's
+// resident blocks at that size): the first kCatTuneN calls of at least
+// kCatTuneMin sources on a (device, octree, order) run one candidate each and
+// are timed (a call waits for its result anyway); later calls use the fastest
+// in photon-steps per second.  A source's rows do not depend on the block
+// size.  MPF_AUTOTUNE=0 keeps kFastThreads.
+constexpr int kCatTuneN = 3;
+constexpr long long kCatTuneMin = 1ll << 16;
+const int kCatTuneTpb[kCatTuneN] = {kFastThreads, 64, 32};
+struct CatTune {
+    int trials = 0;
+    int best_tpb = kFastThreads;
+    double rate[kCatTuneN] = {0, 0, 0};
+};
+std::mutex g_cat_tune_mu;
+std::map<std::tuple<int, const void*, int>, CatTune> g_cat_tune;
+
+int cat_blocks_per_sm(int order, int tpb)
+{
+    int b = 0;
+    const cudaError_t e = (order == 1) ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_cat_persistent<1>, tpb, 0)
+                                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_cat_persistent<2>, tpb, 0);
+    return (e == cudaSuccess && b > 0) ? b : 1;
 }
 
 std::mutex g_plans_mu;
@@ -454,6 +484,26 @@ thread_local char g_queue_msg[512] = "";
 }  // namespace
 
 const char* catalogue_queue_message() { return g_queue_msg; }
+
+void catalogue_forget_tuned_shape(const void* keys)
+{
+    std::lock_guard<std::mutex> lock(g_cat_tune_mu);
+    for (auto it = g_cat_tune.begin(); it != g_cat_tune.end();) {
+        if (std::get<1>(it->first) == keys) it = g_cat_tune.erase(it);
+        else ++it;
+    }
+}
+
+bool catalogue_tuned_shape(int dev, const DevTree& T, int order, int* tpb, double* rates)
+{
+    std::lock_guard<std::mutex> lock(g_cat_tune_mu);
+    auto it = g_cat_tune.find(std::make_tuple(dev, (const void*)T.keys, order));
+    if (it == g_cat_tune.end() || it->second.trials < kCatTuneN) return false;
+    *tpb = it->second.best_tpb;
+    if (rates)
+        for (int k = 0; k < kCatTuneN; ++k) rates[k] = it->second.rate[k];
+    return true;
+}
 
 bool catalogue_persistent_applies(const CatConst& K, bool exact, int order)
 {
@@ -527,9 +577,30 @@ cudaError_t catalogue_newton_persistent(const DevTree& T, const DevCosmo& Cs, co
     cudaKernelNodeParams kp = pl.pparams;
     kp.kernelParams = args;
     kp.extra = nullptr;
+    // block size: the tuned one, or this call's candidate while tuning
+    static const bool want_tune = !(getenv("MPF_AUTOTUNE") && getenv("MPF_AUTOTUNE")[0] == '0');
+    const auto tkey = std::make_tuple(dev, (const void*)T.keys, order);
+    int trial = -1, tpb = kFastThreads;
+    if (want_tune) {
+        std::lock_guard<std::mutex> lock(g_cat_tune_mu);
+        CatTune& tu = g_cat_tune[tkey];
+        if (tu.trials < kCatTuneN && n >= kCatTuneMin) trial = tu.trials++;
+        tpb = (trial >= 0) ? kCatTuneTpb[trial] : tu.best_tpb;
+    }
+    int sms = 0;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    kp.blockDim = dim3((unsigned)tpb);
+    kp.gridDim = dim3((unsigned)(cat_blocks_per_sm(order, tpb) * sms));
     e = cudaGraphExecKernelNodeSetParams(pl.exec, pl.pnode, &kp);
     if (e != cudaSuccess) return e;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (trial >= 0) {
+        cudaEventCreate(&ev0);
+        cudaEventCreate(&ev1);
+        cudaEventRecord(ev0, stream);
+    }
     e = cudaGraphLaunch(pl.exec, stream);
+    if (trial >= 0) cudaEventRecord(ev1, stream);
     if (e != cudaSuccess) return e;
     unsigned long long ctl[kQWords], ps[2];
     unsigned cnt[2], st = 0;
@@ -538,12 +609,28 @@ cudaError_t catalogue_newton_persistent(const DevTree& T, const DevCosmo& Cs, co
     if (e == cudaSuccess) e = cudaMemcpyAsync(cnt, pl.D.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&st, pl.D.status, sizeof(st), cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (trial >= 0) {
+        float ms = 0.f;
+        if (e == cudaSuccess && cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess && ms > 0.f) {
+            std::lock_guard<std::mutex> lock(g_cat_tune_mu);
+            CatTune& tu = g_cat_tune[tkey];
+            tu.rate[trial] = (double)ps[0] / (ms * 1e-3);
+            if (tu.trials == kCatTuneN) {
+                int b = 0;
+                for (int k = 1; k < kCatTuneN; ++k)
+                    if (tu.rate[k] > tu.rate[b]) b = k;
+                tu.best_tpb = kCatTuneTpb[b];
+            }
+        }
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+    }
     if (e != cudaSuccess) return e;
     stats->rays = (long long)ctl[kQRays];
     stats->photon_steps = (long long)ps[0];
     stats->photon_steps_jacobian = (long long)ps[1];
     stats->iterations = (int)ctl[kQIter];
-    stats->launches = 1;   // one graph launch
+    stats->launches = pl.kernels;   // the kernels of the one graph launch
     *h_status = st;
     *queue_error = cnt[1] != 0 || ctl[kQHead] != ctl[kQTail];
     if (*queue_error)

@@ -1073,9 +1073,11 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
 }
 
 
-// Persistent launch: each warp takes the next 32 rays from a global counter
-// until the batch is exhausted, so uneven path lengths do not leave tail
-// waves.  `queue` is zeroed before the launch.
+// Persistent launch: each warp takes the next 32 x depth rays of [lo, n) from
+// a global counter until the range is exhausted, so uneven path lengths do
+// not leave tail waves; its lanes trace them depth at a time.  `queue` is
+// zeroed before the launch.  The block size and depth are the autotuner's
+// (mpf_prop_fast.cu); the rays' results do not depend on them.
 #if defined(MPF_FAST_MAXNREG)
 #define MPF_FAST_BOUNDS __maxnreg__(MPF_FAST_MAXNREG)
 #else
@@ -1084,20 +1086,23 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
 template <int ORDER, bool SRC, bool WIDE, bool BORN = false>
 __global__ void MPF_FAST_BOUNDS k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
                                                                     const double* __restrict__ launch, long long n, PropOut O,
-                                                                    unsigned long long* queue)
+                                                                    unsigned long long* queue, int depth, long long lo)
 {
     __shared__ double jac_sums[6 * kFastThreads];
     __shared__ float jac_terms[12 * kFastThreads];
     const JacSums J{jac_sums + threadIdx.x, jac_terms + threadIdx.x};
     const int lane = threadIdx.x & 31;
+    const unsigned long long per = 32ull * (unsigned long long)depth;
     for (;;) {
         unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(queue, 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
+        if (lane == 0) base = atomicAdd(queue, per);
+        base = __shfl_sync(0xffffffffu, base, 0) + (unsigned long long)lo;
         if (base >= (unsigned long long)n) break;
-        const long long i = (long long)base + lane;
-        if (i < n) propagate_fast<ORDER, SRC, WIDE, BORN>(T, C, P, launch + 6 * i, i, O, J);
-        __syncwarp();
+        for (int d = 0; d < depth; ++d) {
+            const long long i = (long long)base + 32ll * d + lane;
+            if (i < n) propagate_fast<ORDER, SRC, WIDE, BORN>(T, C, P, launch + 6 * i, i, O, J);
+            __syncwarp();
+        }
     }
 }
 

@@ -60,4 +60,15 @@ cudaError_t launch_propagate(const DevTree& T, const DevCosmo& C, const PropPara
 cudaError_t launch_gather(const DevTree& T, int kind, bool exact, const double* d_xyz, long long n, void* d_out,
                           cudaStream_t stream);
 
+// Autotuned launch shapes (mpf_prop_fast.cu, mpf_cat_persist.cu): false until
+// tuned.  rates: photon-steps/s of the candidates (4 for the propagate kernel:
+// 128 x 1, 64 x 1, 32 x 1, 128 x 2 threads x claim depth; 3 for the
+// catalogue: 128, 64, 32 threads).
+bool tuned_shape(int dev, const DevTree& T, int mode, int* tpb, int* depth, double* rates);
+int plain_fast_mode(int order);
+bool catalogue_tuned_shape(int dev, const DevTree& T, int order, int* tpb, double* rates);
+// forget an octree's tuned shapes when its arrays are freed
+void forget_tuned_shape(const void* keys);
+void catalogue_forget_tuned_shape(const void* keys);
+
 }  // namespace mpf
