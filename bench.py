@@ -415,6 +415,85 @@ def run_surrogate(args, synth, world, rank, local, dist):
         print(json.dumps(line), flush=True)
 
 
+def surrogate_entry(pkg, synth, capi, lib, rays=131072, samples=50e6):
+    """The metric's comparison, measured in the default run: the learned field
+    surrogate (BASELINE config 4: the uniform 64^3 field over a 5 x 5 degree
+    cone to z = 2, 64 Fourier frequencies, 4 x 128 SiLU, BF16 weights, trained
+    on `samples` octree-labelled points) against the plain octree kernel on
+    the same rays, with the arithmetic bound of the 5x target."""
+    import torch
+    spec, chi2 = surrogate_workload(synth)
+    cos = cosmology_table(synth)
+    length = spec.lbox * synth.MPC / spec.cosmo.h
+    Sur = importlib.import_module(PKG + ".surrogate").Surrogate
+    tree = pkg.Octree.from_records(synth.make_octree(spec))
+    cosmo = pkg.Cosmology(*cos)
+    t = np.tan(np.radians(2.5))
+    dom = dict(r_max=chi2 * 1.02 / spec.lbox, a_min=1.0 / 3.0 - 0.05, freq_sigma=(6.0, 1.5, 1.5, 0.5))
+    sur = Sur((t, t), seed=42, **dom)
+    train = sur.train(tree, samples=int(samples), batch=16384, lr=2e-3)
+    # the same network untrained (its initial weights, the trained output
+    # normalisation): what the training gains
+    untrained = Sur((t, t), seed=42, **dom)
+    untrained.set_params(None, sur.get_params()[1])
+    launch = np.ascontiguousarray(ray_grid(1000, 2.5)[:rays])
+    kw = dict(nsteps=10, order=2, stop="redshift", stop_value=2.0)
+    # plain octree kernel, device-resident rays, CUDA events on its stream
+    dev = torch.device("cuda", torch.cuda.current_device())
+    d_launch = torch.from_numpy(launch).to(dev)
+    d_steps = torch.zeros(rays, dtype=torch.int64, device=dev)
+    d_final = torch.zeros(rays * capi.MPF_PHOTON_FIELDS, dtype=torch.float64, device=dev)
+    d_status = torch.zeros(1, dtype=torch.int32, device=dev)
+    p, keep = capi.make_params(length, jacobian=False, exact=False, **kw)
+    stream = torch.cuda.current_stream(dev)
+    plain_ms = []
+    for rep in range(3):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        capi.check(lib.mpf_propagate_device(tree._h, cosmo._h, C.byref(p), rays, C.c_void_p(d_launch.data_ptr()),
+                                            C.c_void_p(d_steps.data_ptr()), C.c_void_p(d_final.data_ptr()), None,
+                                            C.c_void_p(d_status.data_ptr()), C.c_void_p(stream.cuda_stream)))
+        b.record(stream)
+        torch.cuda.synchronize()
+        plain_ms.append(a.elapsed_time(b))
+    ref_final = d_final.view(rays, -1).cpu().numpy()
+    plain_steps = int((d_steps.cpu().numpy() - 1).sum())
+    plain_rate = plain_steps / (min(plain_ms) / 1000.0)
+    # the surrogate kernel alone (no re-check fallback): speed and accuracy
+    _, fin, _, _, ss = sur.propagate(tree, cosmo, launch, length, tolerance=np.inf, fallback=False, **kw)
+    _, fin_u, _, _, _ = untrained.propagate(tree, cosmo, launch, length, tolerance=np.inf, fallback=False, **kw)
+    sur_rate = ss["photon_steps"] / ss["surrogate_seconds"]
+    # the surrogate form at the tolerance: flagged rays re-run on the octree
+    st2, _, fl2, _, ss2 = sur.propagate(tree, cosmo, launch, length, tolerance=SURR_TOLERANCE, fallback=True,
+                                        want_final=False, **kw)
+    form_rate = int((st2 - 1).sum()) / (ss2["surrogate_seconds"] + ss2["fallback_seconds"])
+    ref_d = _deflection_vec(launch, ref_final)
+
+    def rel_err(f):
+        r = np.linalg.norm(_deflection_vec(launch, f) - ref_d, axis=1) / np.linalg.norm(ref_d, axis=1)
+        return {"median": float(np.median(r)), "p90": float(np.percentile(r, 90)), "max": float(r.max())}
+
+    peak, peak_kind = measured_peak_bf16()
+    flop_step = SURR_EVALS_PER_STEP * SURR_FLOP_PER_EVAL
+    need = 5.0 * plain_rate * flop_step / 1e12
+    out = {"workload": "64^3 uniform field at octree level 8 over a 5x5 deg cone to z=2, %d rays of the 1000x1000 grid, "
+                       "TSC, 10 steps/cell; 64 Fourier frequencies, 4x128 SiLU, BF16 weights on the tensor cores, "
+                       "trained on %d octree-labelled samples" % (rays, int(samples)),
+           "plain_steps_per_s": plain_rate, "surrogate_kernel_steps_per_s": sur_rate,
+           "surrogate_form_steps_per_s": form_rate, "form_vs_plain": form_rate / plain_rate,
+           "kernel_vs_plain": sur_rate / plain_rate,
+           "rel_deflection_error_vs_plain": rel_err(fin), "untrained_rel_deflection_error_vs_plain": rel_err(fin_u),
+           "flagged_fraction_at_tolerance": float((fl2 & 1).mean()), "tolerance": SURR_TOLERANCE,
+           "mma_tflops": sur_rate * flop_step / 1e12,
+           "bound_of_5x": {"flop_per_photon_step": flop_step, "tflops_needed": need, "bf16_peak_tflops": peak,
+                           "peak_source": peak_kind, "needed_over_peak": need / peak},
+           "training": train}
+    for o in (sur, untrained, tree, cosmo):
+        o.close()
+    del keep
+    return out
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -441,6 +520,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--zstop", type=float, default=2.0, help="stop redshift (profiling captures use a short path)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="skip the surrogate-vs-plain comparison of the default line")
     ap.add_argument("--mode", default="propagate", choices=["propagate", "catalogue", "surrogate"],
                     help="propagate = the headline ray-tracing benchmark; catalogue = the Newton root-finder; "
                          "surrogate = the learned field in the RK4 stages against the plain octree")
@@ -593,7 +674,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
-            "form": "plain octree (the surrogate form: bench.py --mode surrogate)",
+            "form": "plain octree (the surrogate form against it: the surrogate entry)",
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": B * 6 * 8,
                     "d2h_bytes_per_step": B * 8 + B * capi.MPF_PLANE_FIELDS * 8},
             "gpu_launches": args.steps, "roofline": roofline, "status_bits": status,
@@ -603,6 +684,9 @@ def main():
         oracle_mod.build()
         line["cpu_baseline"], oracle_run = cpu_baseline(oracle_mod, rec, cos, length, launch, planes)
         line["parity"] = parity_entry(pkg, tree, cosmo, length, planes, oracle_run, exact=args.exact)
+    if rank == 0 and not args.no_surrogate:
+        tree.close()      # the benchmark octree's 5 GB are not needed any more
+        line["surrogate"] = surrogate_entry(pkg, synth, capi, lib)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
