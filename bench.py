@@ -494,6 +494,194 @@ def surrogate_entry(pkg, synth, capi, lib, rays=131072, samples=50e6):
     return out
 
 
+MAPS_METRIC = "HEALPix map photon-steps/s (mpf_hmaps_fill: kappa, gamma1, gamma2, 1/mu, nside 4096, one full-sky cone)"
+MAPS_HALF_DEG = 14.7   # a square cone of (2 x 14.7 deg)^2 = 0.263 sr: 1/48 of the sky
+
+
+def maps_cone_spec(synth):
+    """One of the 48 full-sky cones of BASELINE config 5: the 512^3 periodic
+    base (octree level 11, file level 9) over lbox = 2048 Mpc/h, refined to
+    level 14 in this cone's 417 of the 20 000 NFW haloes, to z = 1."""
+    cosmo = synth.Cosmology()
+    chi1 = float(cosmo.chi_of_z(1.0)[0])
+    return synth.OctreeSpec(base_level=11, box_cells=512, lbox=2048.0, half_y=MAPS_HALF_DEG, half_z=MAPS_HALF_DEG,
+                            chi_max=chi1 * 1.02, halos=417, max_level=14, mass_min=1e12, mass_max=1e15,
+                            refine_cells=4.5, seed=48)
+
+
+def maps_cone_pixels(pkg, nside):
+    """The RING pixels of nside whose centres lie in the square cone about +x
+    (|phi| and |theta - 90 deg| at most MAPS_HALF_DEG): candidates from the
+    equatorial rings near phi = 0, centres from the library's pix2vec_ring."""
+    t = np.sin(np.radians(MAPS_HALF_DEG)) * 1.01
+    # equatorial rings i (nside <= i <= 3 nside) have z = 4/3 - 2 i / (3 nside), 4 nside pixels each
+    i_lo = int(np.floor((4.0 / 3.0 - t) * 1.5 * nside)) - 1
+    i_hi = int(np.ceil((4.0 / 3.0 + t) * 1.5 * nside)) + 1
+    rings = np.arange(max(i_lo, nside), min(i_hi, 3 * nside) + 1)
+    jmax = int(np.ceil(np.radians(MAPS_HALF_DEG) / (np.pi / (2 * nside)))) + 2
+    j = np.concatenate([np.arange(0, jmax + 1), np.arange(4 * nside - jmax - 1, 4 * nside)])
+    cand = (2 * nside * (nside - 1) + 4 * nside * (rings[:, None] - nside) + j[None, :]).ravel()
+    v = pkg.pix2vec_ring(nside, cand)
+    ph = np.degrees(np.arctan2(v[:, 1], v[:, 0]))
+    th = np.degrees(np.arccos(np.clip(v[:, 2], -1.0, 1.0)))
+    keep = (np.abs(ph) <= MAPS_HALF_DEG) & (np.abs(th - 90.0) <= MAPS_HALF_DEG)
+    return np.sort(cand[keep]), v[keep][np.argsort(cand[keep])]
+
+
+def run_maps(args, synth, world, rank, local, dist):
+    """BASELINE config 5 on one full-sky cone: the octree built on the GPU from
+    the reference's 10-column ASCII cell rows (mpf_cells_build, timed), then
+    the kappa / gamma / 1/mu maps of its nside = 4096 pixels to z_s = 1
+    (mpf_hmaps_fill, TSC, 8 steps per cell); a step = one call on a chunk of
+    the cone's pixels.  Photon-steps are read from the maps' steps row: the
+    trajectory index before the z_s = 1 crossing, where the ray stops, plus
+    one (a ray that leaves the data first has a zero row and is not
+    counted).  The FLRW values of the surface are not read by these rows."""
+    spec = maps_cone_spec(synth)
+    cos = cosmology_table(synth)
+    length = spec.lbox * synth.MPC / spec.cosmo.h
+    nside = 4096
+    chunk = args.batch
+    comps = ["lensing", "steps"]
+    config = {"workload": "one of 48 full-sky cones (a (2 x 14.7 deg)^2 square, 0.263 sr) of a 512^3 periodic field at "
+                          "octree level 11 (lbox 2048 Mpc/h) refined to level 14 in 417 NFW haloes, to z_s=1; HEALPix "
+                          "nside 4096 RING pixel centres of the cone, one ray each; TSC, 8 steps/cell, infinitesimal "
+                          "Jacobian; octree built on the GPU from the 10-column ASCII cell rows",
+              "nside": nside, "pixels_per_step": chunk, "order": "TSC", "nsteps": 8, "z_s": 1.0,
+              "gather_arithmetic": "fp32 gather, fp64 state", "maps": "kappa gamma1 gamma2 1/mu steps (float)",
+              "l2": "octree larger than L2 (no flush)", "parallelism": "single GPU"}
+    key = hashlib.sha1(repr(spec).encode()).hexdigest()[:16]
+    path = os.path.join(os.environ.get("TMPDIR", "/tmp"), "mpf_bench_%s.bin" % key)
+    t0 = time.perf_counter()
+    if os.path.exists(path):
+        rec0 = synth.read_bin(path)
+    else:
+        rec0 = synth.make_octree(spec)
+        synth.write_bin(path + ".tmp", rec0)
+        os.replace(path + ".tmp", path)
+    gen_s = time.perf_counter() - t0
+    rows = synth.cells_ramses(rec0, spec).astype(np.float32)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import oracle as oracle_mod
+        oracle_mod.build()
+        nthreads = os.cpu_count() or 1
+        O = oracle_mod.Oracle(rec0, {"t": cos[0], "a": cos[1], "dadt": cos[2]}, length, nthreads=nthreads)
+        pk = importlib.import_module(PKG)
+        _, dirs = maps_cone_pixels(pk, nside)
+        rng = np.random.default_rng(3)
+        times, counts = [], []
+        for k in range(args.warmup + args.steps):
+            idx = rng.choice(dirs.shape[0], size=2 * nthreads, replace=False)
+            launch = np.zeros((idx.shape[0], 6))
+            launch[:, 3:] = dirs[idx]
+            t1 = time.perf_counter()
+            st, _, _ = O.propagate(launch, order=2, nsteps=8, stop="redshift", planes=np.array([1.0]), jacobian=True)
+            dt = time.perf_counter() - t1
+            if k >= args.warmup:
+                times.append(dt)
+                counts.append(int(st.sum()))
+        value = sum(counts) / sum(times)
+        print(json.dumps({"metric": MAPS_METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                          "impl": "reference",
+                          "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                                           "sample": "%d random pixels per step, C oracle (trajectory then Jacobian)"
+                                                     % (2 * nthreads)},
+                          "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+              flush=True)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    pkg = importlib.import_module(PKG)
+    importlib.import_module(PKG + ".build").build()
+    capi = importlib.import_module(PKG + ".capi")
+    cosmo = pkg.Cosmology(*cos)
+    # the octree build on the GPU from the ASCII rows (importascii + correctOctree)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    built = pkg.cells_build(rows, cosmo, (0.0, 0.0, 0.0), (spec.chi_max / spec.lbox, 0.0, 0.0),
+                            np.arctan(np.sqrt(2.0) * np.tan(np.radians(MAPS_HALF_DEG))) * 1.02, (0.0, 0.0, 0.0),
+                            4.0 / 512.0, spec.cosmo.h, spec.cosmo.omega_m, spec.lbox, synth.MPC, order=2)
+    build_s = time.perf_counter() - t0
+    built = np.frombuffer(built.tobytes(), dtype=synth.RECORD)
+    t0 = time.perf_counter()
+    tree = pkg.Octree.from_records(built)
+    upload_s = time.perf_counter() - t0
+    info = tree.info
+    pixels, dirs = maps_cone_pixels(pkg, nside)
+    nb = max(1, pixels.shape[0] // chunk)
+    config.update({"cells": int(info["cells"]), "levels": [info["level_min"], info["level_max"]],
+                   "octree_device_bytes": int(info["device_bytes"]), "cone_pixels": int(pixels.shape[0]),
+                   "ascii_rows": int(rows.shape[0])})
+    cz = cosmo_mod_homogeneous(synth, cos, [1.0])
+    p, keep = capi.make_params(length, 8, 2, "redshift", 0.0, np.array([1.0]), True, args.exact, 0)
+    kw = dict(nsteps=8, order=2, exact=args.exact)
+
+    def call(k):
+        px = np.ascontiguousarray(pixels[(k % nb) * chunk:(k % nb + 1) * chunk])
+        return pkg.hmaps_fill(tree, cosmo, nside, px, np.array([1.0]), cz, comps, length, **kw)
+
+    for k in range(args.warmup):
+        call(k)
+    torch.cuda.synchronize()
+    steps_total, t_calls = 0, []
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            m = call(args.warmup + k)
+            t_calls.append(time.perf_counter() - t1)
+            fid = m[0, 4].astype(np.float64)
+            steps_total += int((fid + (fid > 0)).sum())   # a ray stopped at z_s: its steps are firstid + 1
+    value = steps_total / sum(t_calls)
+    # map-level error against the float64 (reference-order) kernel on a pixel sample
+    rng = np.random.default_rng(5)
+    sample = np.sort(rng.choice(pixels, size=min(2048, pixels.shape[0]), replace=False))
+    fast = pkg.hmaps_fill(tree, cosmo, nside, sample, np.array([1.0]), cz, comps, length, nsteps=8, order=2, exact=False)
+    exact = pkg.hmaps_fill(tree, cosmo, nside, sample, np.array([1.0]), cz, comps, length, nsteps=8, order=2, exact=True)
+    map_err = {}
+    for r, name in enumerate(("kappa", "gamma1", "gamma2", "inv_mu")):
+        e, sc = np.abs(fast[0, r] - exact[0, r]).max(), np.abs(exact[0, r]).max()
+        map_err[name] = {"abs_max": float(e), "scale": float(sc), "of_scale": float(e / max(sc, 1e-30))}
+    map_err["steps_rows_equal"] = bool(np.array_equal(fast[0, 4], exact[0, 4]))
+    map_err["sample_pixels"] = int(sample.shape[0])
+    peak, peak_kind = measured_peak_hbm()
+    achieved = value * BYTES_PER_PHOTON_STEP / 1e9
+    line = {"metric": MAPS_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * sum(t_calls) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": chunk * 8,
+                    "d2h_bytes_per_step": chunk * 5 * 4},
+            "build": {"synthetic_field_s": gen_s, "cells_build_s": build_s, "octree_upload_s": upload_s,
+                      "ascii_rows": int(rows.shape[0]), "cells": int(info["cells"])},
+            "map_error_vs_float64_kernel": map_err,
+            "gpu_launches": 3 * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_source": peak_kind, "bytes_per_photon_step": BYTES_PER_PHOTON_STEP,
+                         "scope": "whole mpf_hmaps_fill call (host pixels in, float maps out)"},
+            "clocks": clk.summary()}
+    del keep
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def cosmo_mod_homogeneous(synth, cos, zs):
+    """FillMap's per-surface FLRW values (t, chi, lambda, a, z) at redshift
+    surfaces, from the cosmology table: a = 1 / (1 + z), t and chi = c t / L
+    read off the table (the homogeneous ray's lambda is t for dt/dl = 1)."""
+    t, a = cos[0], cos[1]
+    out = np.zeros((len(zs), 5))
+    for k, z in enumerate(zs):
+        ak = 1.0 / (1.0 + z)
+        tk = float(np.interp(-ak, -a, t))
+        chi = float(synth.Cosmology().chi_of_z(z)[0]) / 2048.0
+        out[k] = (tk, chi, tk, ak, z)
+    return out
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -522,9 +710,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true",
                     help="skip the surrogate-vs-plain comparison of the default line")
-    ap.add_argument("--mode", default="propagate", choices=["propagate", "catalogue", "surrogate"],
+    ap.add_argument("--mode", default="propagate", choices=["propagate", "catalogue", "surrogate", "maps"],
                     help="propagate = the headline ray-tracing benchmark; catalogue = the Newton root-finder; "
-                         "surrogate = the learned field in the RK4 stages against the plain octree")
+                         "surrogate = the learned field in the RK4 stages against the plain octree; maps = HEALPix "
+                         "lensing maps of one full-sky cone at nside 4096")
     ap.add_argument("--surrogate-samples", type=float, default=50e6, help="training samples of the surrogate")
     ap.add_argument("--sources", type=int, default=262144,
                     help="catalogue sources per step (a call's rounds wait for its slowest sources, whose up to 11 "
@@ -547,6 +736,8 @@ def main():
         return run_catalogue(args, synth, spec, cos, length, world, rank, local, dist)
     if args.mode == "surrogate":
         return run_surrogate(args, synth, world, rank, local, dist)
+    if args.mode == "maps":
+        return run_maps(args, synth, world, rank, local, dist)
 
     if args.impl == "reference":
         if rank != 0:

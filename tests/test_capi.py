@@ -85,3 +85,24 @@ def test_host_side_argument_checks(pkg):
     with pytest.raises(ValueError):
         maps.assemble(planes, np.zeros((2, 3)), np.ones((1, 5)), ["lensing_born"])
     assert maps.nmaps(["lensing", "lensing_born", "deflection", "dz"]) == 11
+
+
+def test_cpp_call_sites_compile_against_the_header(pkg):
+    """The INTEGRATION.md call sites (tests/cpp/integration_calls.cpp) compile
+    as C++17 against include/mpf_gb300.h and link to the library; they run on
+    a GPU in tests/test_gpu_cpp_boundary.py."""
+    import os
+    import shutil
+    import subprocess
+    import tempfile
+    from conftest import ROOT
+    pkg.library()
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        import pytest
+        pytest.skip("no C++ compiler")
+    libdir = os.path.join(ROOT, "magrathea-pathfinder_gb300")
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.run([cxx, "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "integration_calls.cpp"), "-o", os.path.join(d, "ic"),
+                        "-L", libdir, "-lmpf_gb300"], check=True)
