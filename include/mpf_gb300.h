@@ -71,6 +71,10 @@ typedef struct {
     int exact;                 /* 1: the reference's float64 gather arithmetic, bit-exact
                                   trajectories; 0: FP32 gather arithmetic (faster) */
     int64_t max_steps;         /* per ray; <= 0 means 1e8 */
+    double vobs[3];            /* observer velocity (parameters v0x v0y v0z, hmaps.h:80-84, in the
+                                  units of the octree's velocity field); read only when the octree
+                                  carries a velocity field (mpf_octree_set_velocity /
+                                  mpf_velocity_deposit) */
 } mpf_params;
 
 #define MPF_MAX_PLANES 16
@@ -99,6 +103,37 @@ int mpf_octree_upload(const void* records, int64_t n, mpf_octree** out);
 int mpf_octree_load(const char* path, mpf_octree** out);
 int mpf_octree_get_info(const mpf_octree* o, mpf_octree_info* info);
 void mpf_octree_destroy(mpf_octree* o);
+
+/* Velocity field: the velocity slots of the reference's velocity-field octree
+ * (src/gravity2.h:45, the build with -DVELOCITYFIELD).  An octree that carries
+ * one is traced as that build does: the slots are interpolated with the other
+ * fields, count in the emptiness test of each step, and every redshift is
+ *   a0 / a (1 + phi0/c^2 - phi/c^2 + isw + v.k / (c k0) - v0n) - 1
+ * (src/integrator.h:537-538, 594, 707-708, 765-767), v0n = vobs.k0 / (c k0_0)
+ * with the params' vobs and the launch direction.  The catalogue root-finder
+ * and the learned surrogate reject such an octree (the reference's catalogues
+ * executable stops in that build, catalogues.cpp:290-293).  Changing the
+ * field is not safe while another call uses the octree. */
+/* v3: n x 3 floats (vx vy vz per cell, in the records' order); rho: n floats
+ * that replace the cells' rho, or NULL to keep them.  v3 = NULL removes the
+ * field (rho must then be NULL). */
+int mpf_octree_set_velocity(mpf_octree* o, const float* v3, const float* rho);
+/* The cells' velocities (zeros when the octree has none) and rho; either
+ * pointer may be NULL. */
+int mpf_octree_get_velocity(const mpf_octree* o, float* v3, float* rho);
+
+#define MPF_VELOCITY_BEGIN 1     /* zero every cell's rho and velocity first (hmaps.cpp:395-396) */
+#define MPF_VELOCITY_FINISH 2    /* then v /= rho (a zero rho read as 1) and, level by level, a cell
+                                    whose rho is not a normal float takes its parent's velocity
+                                    (hmaps.cpp:424-441) */
+/* Hmaps::CreateOctreeVelocityWithCIC (scheme 1, src/hmaps.h:439-485) /
+ * WithTSC (scheme 2, :501-550): n particles (pos n x 3 in octree units, vel
+ * n x 3) deposited at every level of the octree on the cells that hold the
+ * exact key of each of their 8 (27) vertices: rho += w, v += v_p w, in float,
+ * in particle order, as the reference computes them on one thread.  Calls
+ * with flags = 0 between a BEGIN and a FINISH accumulate further particle
+ * files, as the reference's loop over shell files does (hmaps.cpp:399-420). */
+int mpf_velocity_deposit(mpf_octree* o, int scheme, int64_t n, const float* pos, const float* vel, int flags);
 
 /* Cosmology table: conformal time, a, da/dt, d2a/dt2 rows as returned by
  * Input::acquire + Input::correct (src/input.h:1090-1224, 1329-1360). */

@@ -106,6 +106,39 @@ class Octree:
         """The containing cell's record (the reference's ORDER = 0)."""
         return self._interp(0, xyz, True)
 
+    # -- velocity field (the reference's -DVELOCITYFIELD build) --
+    def set_velocity(self, v3, rho=None):
+        """Attach per-cell velocities (n x 3, record order; None removes the
+        field); rho (n) replaces the cells' rho when given."""
+        n = self.info["cells"]
+        if v3 is None:
+            capi.check(self._lib.mpf_octree_set_velocity(self._h, None, None))
+            return
+        v = np.ascontiguousarray(v3, dtype=np.float32).reshape(n, 3)
+        r = None if rho is None else np.ascontiguousarray(rho, dtype=np.float32).reshape(n)
+        capi.check(self._lib.mpf_octree_set_velocity(self._h, capi.ptr(v), capi.ptr(r)))
+
+    def velocity(self):
+        """(velocities n x 3, rho n) of the cells."""
+        n = self.info["cells"]
+        v = np.zeros((n, 3), dtype=np.float32)
+        r = np.zeros(n, dtype=np.float32)
+        capi.check(self._lib.mpf_octree_get_velocity(self._h, capi.ptr(v), capi.ptr(r)))
+        return v, r
+
+    def deposit_velocity(self, pos, vel, scheme="cic", begin=True, finish=True):
+        """Hmaps::CreateOctreeVelocityWithCIC / WithTSC of particles (n x 3
+        positions in octree units, n x 3 velocities), with the zeroed masses
+        before (begin) and the mass normalisation and parent fill after
+        (finish)."""
+        p = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        v = np.ascontiguousarray(vel, dtype=np.float32).reshape(-1, 3)
+        if p.shape != v.shape:
+            raise ValueError("pos and vel must have the same shape")
+        flags = (capi.MPF_VELOCITY_BEGIN if begin else 0) | (capi.MPF_VELOCITY_FINISH if finish else 0)
+        sch = {"cic": 1, "tsc": 2}[scheme] if isinstance(scheme, str) else int(scheme)
+        capi.check(self._lib.mpf_velocity_deposit(self._h, sch, p.shape[0], capi.ptr(p), capi.ptr(v), flags))
+
     def close(self):
         if self._h:
             self._lib.mpf_octree_destroy(self._h)
@@ -144,16 +177,18 @@ class Cosmology:
 
 def propagate(octree: Octree, cosmology: Cosmology, launch, length: float, nsteps: int = 10, order: int = 2,
               stop: str = "redshift", stop_value: float = 0.0, planes=None, jacobian: bool = True,
-              exact: bool = False, max_steps: int = 0, plane_normal=(0.0, 0.0, 0.0), want_final: bool = True):
+              exact: bool = False, max_steps: int = 0, plane_normal=(0.0, 0.0, 0.0), want_final: bool = True,
+              vobs=(0.0, 0.0, 0.0)):
     """Integrate rays launched from launch[:, 0:3] toward launch[:, 3:6].
 
+    vobs: the observer velocity, read when the octree carries a velocity field.
     Returns (steps[n], final[n, 28] or None, planes[n, nplanes, 20] or None, status).
     """
     L = capi.load()
     launch = np.ascontiguousarray(launch, dtype=np.float64).reshape(-1, 6)
     n = launch.shape[0]
     p, keep = capi.make_params(length, nsteps, order, stop, stop_value, planes, jacobian, exact, max_steps,
-                               plane_normal)
+                               plane_normal, vobs)
     steps = np.zeros(n, dtype=np.int64)
     final = np.zeros((n, MPF_PHOTON_FIELDS)) if want_final else None
     np_ = p.nplanes
@@ -296,7 +331,7 @@ def catalogue_stats(st) -> dict:
 def hmaps_fill(octree: Octree, cosmology: Cosmology, nside: int, pixels, surfaces, homogeneous, components,
                length: float, nsteps: int = 10, order: int = 2, stop: str = "redshift", exact: bool = False,
                max_steps: int = 0, jacobian: str = "infinitesimal", plane: str = "sachs",
-               stop_bundle: str = "redshift", openingmin: float = 0.0):
+               stop_bundle: str = "redshift", openingmin: float = 0.0, vobs=(0.0, 0.0, 0.0)):
     """Hmaps::FillMap for the given RING pixels: float maps [nsurfaces, nmaps, npix].
 
     surfaces: the stop-quantity values of the map surfaces (interpRefvec);
@@ -304,14 +339,16 @@ def hmaps_fill(octree: Octree, cosmology: Cosmology, nside: int, pixels, surface
     components: the reference's map component names, in order ("lensing_born":
     the infinitesimal Jacobian along each pixel's FLRW ray);
     jacobian: "infinitesimal" or "bundle" (then plane, stop_bundle and
-    openingmin, in radians, as the reference's parameters).
+    openingmin, in radians, as the reference's parameters); vobs: the
+    observer velocity (v0x v0y v0z), read when the octree carries a velocity
+    field.
     """
     L = capi.load()
     pix = np.ascontiguousarray(pixels, dtype=np.int64)
     comps = [capi.MAP_COMPONENTS[c] for c in components]
     bundle = jacobian == "bundle"
     nm = sum((5 if bundle else 4) if c == 0 else 4 if c == 1 else 2 if c == 13 else 1 for c in comps)
-    p, keep = capi.make_params(length, nsteps, order, stop, 0.0, surfaces, True, exact, max_steps)
+    p, keep = capi.make_params(length, nsteps, order, stop, 0.0, surfaces, True, exact, max_steps, vobs=vobs)
     hom = np.ascontiguousarray(homogeneous, dtype=np.float64).reshape(-1, 5)
     cc = np.ascontiguousarray(comps, dtype=np.int32)
     nz = p.nplanes

@@ -33,6 +33,7 @@ UNITS = [
     ("mpf_surrogate.cu", []),
     ("mpf_rays.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
     ("mpf_build.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
+    ("mpf_velocity.cu", ["-fmad=false"]),
 ]
 
 

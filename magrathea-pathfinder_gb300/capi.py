@@ -30,7 +30,11 @@ EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_uplo
            "mpf_catalogue_newton_device", "mpf_hmaps_fill", "mpf_hmaps_fill_bundle", "mpf_pix2vec_ring",
            "mpf_surrogate_create", "mpf_surrogate_destroy", "mpf_surrogate_train", "mpf_surrogate_sample",
            "mpf_surrogate_get_params", "mpf_surrogate_set_params", "mpf_surrogate_loss_grad", "mpf_surrogate_eval",
-           "mpf_surrogate_propagate", "mpf_rays_propagate", "mpf_cells_build", "mpf_cells_parse", "mpf_autotune_info")
+           "mpf_surrogate_propagate", "mpf_rays_propagate", "mpf_cells_build", "mpf_cells_parse", "mpf_autotune_info",
+           "mpf_octree_set_velocity", "mpf_octree_get_velocity", "mpf_velocity_deposit")
+
+MPF_VELOCITY_BEGIN = 1
+MPF_VELOCITY_FINISH = 2
 
 MPF_TRAJECTORY_FIELDS = 29
 
@@ -58,7 +62,8 @@ class OctreeInfo(C.Structure):
 class Params(C.Structure):
     _fields_ = [("length", C.c_double), ("stop_value", C.c_double), ("plane_normal", C.c_double * 3),
                 ("planes", C.c_void_p), ("nplanes", C.c_int), ("nsteps", C.c_uint), ("order", C.c_int),
-                ("stop", C.c_int), ("jacobian", C.c_int), ("exact", C.c_int), ("max_steps", C.c_int64)]
+                ("stop", C.c_int), ("jacobian", C.c_int), ("exact", C.c_int), ("max_steps", C.c_int64),
+                ("vobs", C.c_double * 3)]
 
 
 class CatalogueParams(C.Structure):
@@ -148,6 +153,9 @@ def load(path: str = LIB_PATH):
     L.mpf_hmaps_fill_bundle.argtypes = [vp, vp, C.POINTER(Params), i64, i64, vp, C.c_int, vp, vp, C.c_int, C.c_int, d,
                                         vp]
     L.mpf_pix2vec_ring.argtypes = [i64, i64, vp, vp]
+    L.mpf_octree_set_velocity.argtypes = [vp, vp, vp]
+    L.mpf_octree_get_velocity.argtypes = [vp, vp, vp]
+    L.mpf_velocity_deposit.argtypes = [vp, C.c_int, i64, vp, vp, C.c_int]
     L.mpf_autotune_info.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
     L.mpf_cells_build.argtypes = [vp, i64, C.POINTER(CellsParams), vp, vp, i64, C.POINTER(i64)]
     L.mpf_cells_parse.argtypes = [C.c_char_p, i64, vp, i64, C.POINTER(i64)]
@@ -187,7 +195,7 @@ def ptr(a) -> C.c_void_p:
 
 
 def make_params(length, nsteps=10, order=2, stop="redshift", stop_value=0.0, planes=None, jacobian=True, exact=False,
-                max_steps=0, plane_normal=(0.0, 0.0, 0.0)):
+                max_steps=0, plane_normal=(0.0, 0.0, 0.0), vobs=(0.0, 0.0, 0.0)):
     """Params struct plus the array that must outlive the call."""
     pl = np.ascontiguousarray(planes if planes is not None else np.zeros(0), dtype=np.float64)
     if pl.shape[0] > MPF_MAX_PLANES:
@@ -205,4 +213,6 @@ def make_params(length, nsteps=10, order=2, stop="redshift", stop_value=0.0, pla
     p.jacobian = int(bool(jacobian))
     p.exact = int(bool(exact))
     p.max_steps = int(max_steps)
+    for k in range(3):
+        p.vobs[k] = float(vobs[k])
     return p, pl

@@ -1,5 +1,6 @@
 // C ABI of the photon-propagation path (declarations: include/mpf_gb300.h).
 #include <cstdio>
+#include <cmath>
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -76,6 +77,10 @@ bool mpf_internal_fill_params(const mpf_params* p, mpf::PropParams& P)
     P.stop_kind = p->stop;
     P.nplanes = p->nplanes;
     P.jacobian = p->jacobian ? 1 : 0;
+    for (int k = 0; k < 3; ++k) {
+        if (!std::isfinite(p->vobs[k])) return false;
+        P.vobs[k] = p->vobs[k];
+    }
     return true;
 }
 
@@ -158,6 +163,7 @@ void mpf_octree_destroy(mpf_octree* o)
     cudaFree(o->node);
     cudaFree(o->grid);
     cudaFree(o->stencil);
+    if (o->vel) cudaFree(o->vel);
     cudaSetDevice(cur);
     delete o;
 }
@@ -338,6 +344,9 @@ int mpf_catalogue_newton_device(const mpf_octree* o, const mpf_cosmology* c, con
     mpf::CatRotation R;
     if (!o || !c || n < 0 || (n > 0 && (!sources_device || !rows_device)) || stride < 6 || stride > 1024)
         return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: null argument or stride < 6");
+    if (o->tree.vel)
+        return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: the octree carries a velocity field; the reference's "
+                                      "catalogues do not run in that build (catalogues.cpp:290-293)");
     if (!catalogue_consts(p, K, R)) return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: bad parameters");
     if (n > 0x7fffffffll) return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: at most 2^31 - 1 sources per call");
     if (stats) std::memset(stats, 0, sizeof(*stats));
@@ -370,6 +379,9 @@ int mpf_catalogue_newton(const mpf_octree* o, const mpf_cosmology* c, const mpf_
     mpf::CatRotation R;
     if (!o || !c || n < 0 || (n > 0 && (!sources || !rows)) || stride < 6 || stride > 1024)
         return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: null argument or stride < 6");
+    if (o->tree.vel)
+        return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: the octree carries a velocity field; the reference's "
+                                      "catalogues do not run in that build (catalogues.cpp:290-293)");
     if (!catalogue_consts(p, K, R)) return set_err(MPF_BAD_INPUT, "mpf_catalogue_newton: bad parameters");
     if (stats) std::memset(stats, 0, sizeof(*stats));
     if (n == 0) return MPF_OK;
@@ -467,7 +479,7 @@ int mpf_autotune_info(const mpf_octree* o, int kind, int order, int* threads_per
     *claim_depth = 0;
     double r[4] = {0, 0, 0, 0};
     int tpb = 0, depth = 1;
-    bool ok = (kind == 0) ? mpf::tuned_shape(dev, o->tree, mpf::plain_fast_mode(order), &tpb, &depth, r)
+    bool ok = (kind == 0) ? mpf::tuned_shape(dev, o->tree, mpf::plain_fast_mode(order, o->tree.vel != nullptr), &tpb, &depth, r)
                           : mpf::catalogue_tuned_shape(dev, o->tree, order, &tpb, r);
     if (ok) {
         *threads_per_block = tpb;

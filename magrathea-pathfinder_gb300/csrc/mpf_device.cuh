@@ -9,6 +9,8 @@
 //                level-ordered and a refined node's 8 children are
 //                contiguous in site order (site = x | y<<1 | z<<2)
 //   grid[gx*gy*gz] int32 node index of each level-Lt cell of the bounding box
+//   vel[n]       float4 (vx, vy, vz, 0) per cell, in units of c: the velocity
+//                slots of the velocity-field octree (gravity2.h:45), or absent
 //
 // find_cell() returns what the reference's
 //   upper_bound(keys, K) - 1, if that key contains K          (simplehyperoctree.h:874-899)
@@ -39,6 +41,9 @@ struct DevTree {
     //   int 29      node index of the cell
     //   int 30      the parent cell (one level up), or -1
     const int4* stencil;
+    // per-cell velocity (vx, vy, vz, 0), or null: an octree without a
+    // velocity field (the reference built without -DVELOCITYFIELD)
+    const float4* vel;
     int64_t n;
     int Lt;                // level of the top grid
     int gx0, gy0, gz0;     // grid origin (integer coords at Lt)
@@ -127,6 +132,41 @@ __device__ __forceinline__ void mac_cell(const DevTree& T, Field7& acc, int cell
     }
 }
 
+// Accumulator of the CIC / TSC walks: the 7 Gravity fields and, with V, the
+// velocity slots of the velocity-field octree (gravity2.h:45), which the
+// reference's multiply-accumulate treats like the other fields
+// (simplehyperoctree.h:1887-1910: every arithmetic member of the record, with
+// the same weight and rounding).
+template <bool V>
+struct GatherAcc {
+    Field7 f;
+    float v[3];
+    bool need_all;
+    __device__ __forceinline__ void reset()
+    {
+        clear(f);
+        if (V) v[0] = v[1] = v[2] = 0.f;
+    }
+    template <bool EXACT>
+    __device__ __forceinline__ void add(const DevTree& T, int cell, double w)
+    {
+        mac_cell<EXACT>(T, f, cell, w, need_all);
+        if (V) {
+            const float4 u = __ldg(T.vel + cell);
+            if (EXACT) {
+                v[0] = mac64(v[0], u.x, w);
+                v[1] = mac64(v[1], u.y, w);
+                v[2] = mac64(v[2], u.z, w);
+            } else {
+                const float wf = (float)w;
+                v[0] = fmaf(u.x, wf, v[0]);
+                v[1] = fmaf(u.y, wf, v[1]);
+                v[2] = fmaf(u.z, wf, v[2]);
+            }
+        }
+    }
+};
+
 // Deepest cell at the position (reference locate()); -1 if none.
 __device__ __forceinline__ Found locate(const DevTree& T, double x, double y, double z)
 {
@@ -135,16 +175,15 @@ __device__ __forceinline__ Found locate(const DevTree& T, double x, double y, do
 
 // Cloud-in-cell (simplehyperoctree.h:1410-1469): trilinear over the 8 cells
 // of the located cell's level; restarts one level up when a neighbour is
-// coarser; empty when a neighbour is missing.  `need_all` = also accumulate
+// coarser; empty when a neighbour is missing.  res.need_all = also accumulate
 // rho, phi, a (the RK stages only need the gradient and dphidt).
-template <bool EXACT>
-__device__ Field7 cic(const DevTree& T, double x, double y, double z, bool need_all)
+template <bool EXACT, bool V>
+__device__ void cic_walk(const DevTree& T, double x, double y, double z, GatherAcc<V>& res)
 {
-    Field7 res;
-    clear(res);
+    res.reset();
     const uint64_t c32x = axis_coord(kMaxLevel, x), c32y = axis_coord(kMaxLevel, y), c32z = axis_coord(kMaxLevel, z);
     const Found f0 = find_cell(T, kMaxLevel, c32x, c32y, c32z);
-    if (f0.cell < 0) return res;
+    if (f0.cell < 0) return;
     int ilvl = f0.level, lvl = ilvl;
     // coordinates of the current centre cell at level ilvl
     uint64_t ccx = c32x >> (kMaxLevel - ilvl), ccy = c32y >> (kMaxLevel - ilvl), ccz = c32z >> (kMaxLevel - ilvl);
@@ -184,9 +223,9 @@ __device__ Field7 cic(const DevTree& T, double x, double y, double z, bool need_
             const Found fi = find_cell(T, ilvl, kc[0], kc[1], kc[2]);
             if (fi.cell >= 0) {
                 lvl = min(lvl, fi.level);
-                mac_cell<EXACT>(T, res, fi.cell, w, need_all);
+                res.template add<EXACT>(T, fi.cell, w);
             } else {
-                clear(res);
+                res.reset();
                 break;
             }
         }
@@ -196,11 +235,19 @@ __device__ Field7 cic(const DevTree& T, double x, double y, double z, bool need_
             const uint64_t px = c32x >> b, py = c32y >> b, pz = c32z >> b;   // coords at lvl+1
             site = (int)(px & 1ull) | ((int)(py & 1ull) << 1) | ((int)(pz & 1ull) << 2);
             ccx = px >> 1; ccy = py >> 1; ccz = pz >> 1;
-            clear(res);
+            res.reset();
             half = half_cell(lvl);
         }
     } while (lvl < ilvl);
-    return res;
+}
+
+template <bool EXACT>
+__device__ Field7 cic(const DevTree& T, double x, double y, double z, bool need_all)
+{
+    GatherAcc<false> res;
+    res.need_all = need_all;
+    cic_walk<EXACT, false>(T, x, y, z, res);
+    return res.f;
 }
 
 __device__ __forceinline__ double tsc_w1(int a, double d)
@@ -220,15 +267,17 @@ __device__ __forceinline__ float tsc_w1f(int a, float d)
 // over the 27 cells of the located cell's level, x-major (ix, iy, iz) order;
 // restarts at the level of the first coarser neighbour; empty when one is
 // missing; CIC at the exact origin.
-template <bool EXACT>
-__device__ Field7 tsc(const DevTree& T, double x, double y, double z, bool need_all)
+template <bool EXACT, bool V>
+__device__ void tsc_walk(const DevTree& T, double x, double y, double z, GatherAcc<V>& res)
 {
-    if (x == 0.0 && y == 0.0 && z == 0.0) return cic<EXACT>(T, 0., 0., 0., need_all);
-    Field7 res;
-    clear(res);
+    if (x == 0.0 && y == 0.0 && z == 0.0) {
+        cic_walk<EXACT, V>(T, 0., 0., 0., res);
+        return;
+    }
+    res.reset();
     const uint64_t c32x = axis_coord(kMaxLevel, x), c32y = axis_coord(kMaxLevel, y), c32z = axis_coord(kMaxLevel, z);
     const Found f0 = find_cell(T, kMaxLevel, c32x, c32y, c32z);
-    if (f0.cell < 0) return res;
+    if (f0.cell < 0) return;
     int ilvl = f0.level, lvl = ilvl;
     double half = half_cell(ilvl);
     const double pt[3] = {x, y, z};
@@ -273,21 +322,29 @@ __device__ Field7 tsc(const DevTree& T, double x, double y, double z, bool need_
                     const Found fi = find_cell(T, ilvl, kx, ky, kz);
                     if (fi.cell >= 0) {
                         lvl = min(lvl, fi.level);
-                        if (lvl < ilvl) { clear(res); stop = true; }
-                        else mac_cell<EXACT>(T, res, fi.cell, w, need_all);
+                        if (lvl < ilvl) { res.reset(); stop = true; }
+                        else res.template add<EXACT>(T, fi.cell, w);
                     } else {
-                        clear(res);
+                        res.reset();
                         stop = true;
                     }
                 }
             }
         }
         if (lvl < ilvl) {
-            clear(res);
+            res.reset();
             half = half_cell(lvl);
         }
     } while (lvl < ilvl);
-    return res;
+}
+
+template <bool EXACT>
+__device__ Field7 tsc(const DevTree& T, double x, double y, double z, bool need_all)
+{
+    GatherAcc<false> res;
+    res.need_all = need_all;
+    tsc_walk<EXACT, false>(T, x, y, z, res);
+    return res.f;
 }
 
 // Nearest grid point (simplehyperoctree.h:1396-1401): the data of the
@@ -310,6 +367,25 @@ __device__ __forceinline__ Field7 gather(const DevTree& T, int order, double x, 
 {
     if (order == 0) return ngp(T, x, y, z);
     return (order == 1) ? cic<EXACT>(T, x, y, z, need_all) : tsc<EXACT>(T, x, y, z, need_all);
+}
+
+// The 7 fields and the velocity v[3] at a point of a velocity-field octree
+// (T.vel set), through the same cells and weights.
+template <bool EXACT>
+__device__ Field7 gather_vel(const DevTree& T, int order, double x, double y, double z, float* v)
+{
+    if (order == 0) {
+        const Found c = locate(T, x, y, z);
+        const float4 u = (c.cell >= 0) ? __ldg(T.vel + c.cell) : make_float4(0.f, 0.f, 0.f, 0.f);
+        v[0] = u.x; v[1] = u.y; v[2] = u.z;
+        return ngp(T, x, y, z);
+    }
+    GatherAcc<true> res;
+    res.need_all = true;
+    if (order == 1) cic_walk<EXACT, true>(T, x, y, z, res);
+    else tsc_walk<EXACT, true>(T, x, y, z, res);
+    v[0] = res.v[0]; v[1] = res.v[1]; v[2] = res.v[2];
+    return res.f;
 }
 
 }  // namespace mpf

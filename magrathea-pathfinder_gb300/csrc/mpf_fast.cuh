@@ -141,6 +141,11 @@ static __device__ __noinline__ Field7 cic_slow(const DevTree& T, double x, doubl
     return cic<false>(T, x, y, z, need_all != 0);
 }
 static __device__ __noinline__ Found locate_slow(const DevTree& T, double x, double y, double z) { return locate(T, x, y, z); }
+// the 7 fields and the velocity, full walk (velocity-field octrees)
+static __device__ __noinline__ Field7 vel_slow(const DevTree& T, int order, double x, double y, double z, float* v)
+{
+    return gather_vel<false>(T, order, x, y, z, v);
+}
 
 // A point given by its float64 coordinates.
 struct PosAt {
@@ -354,8 +359,9 @@ __device__ __forceinline__ Loc step_cell(const DevTree& T, const Loc& h, int axi
 // TSC at a point whose deepest cell is `cell` (simplehyperoctree.h:1479-1541
 // through the stencil records).  Returns false when a restart centre is not
 // itself a cell (left to the slow path).
-template <class P>
-__device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P& pos, bool need_all, Field7& res)
+// VEL: also the velocity slots into vv[3] (with need_all).
+template <bool VEL, class P>
+__device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P& pos, bool need_all, Field7& res, float* vv)
 {
     int cell = d.cell, L = d.level;
     float fd[3] = {d.fd[0], d.fd[1], d.fd[2]};
@@ -370,6 +376,7 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
             tsc_w3(fd[1], wy);
             tsc_w3(fd[2], wz);
             float gx = 0.f, gy = 0.f, gz = 0.f, gt = 0.f, rho = 0.f, phi = 0.f, a = 0.f;
+            float ux = 0.f, uy = 0.f, uz = 0.f;
             int e[28];
 #pragma unroll
             for (int q = 0; q < 7; ++q) {
@@ -384,9 +391,14 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
                 if (need_all) {
                     const float4 s = __ldg(T.scal + e[j]);
                     rho = fmaf(s.x, wt, rho); phi = fmaf(s.y, wt, phi); a = fmaf(s.z, wt, a);
+                    if (VEL) {
+                        const float4 u = __ldg(T.vel + e[j]);
+                        ux = fmaf(u.x, wt, ux); uy = fmaf(u.y, wt, uy); uz = fmaf(u.z, wt, uz);
+                    }
                 }
             }
             res = Field7{rho, phi, gx, gy, gz, a, gt};
+            if (VEL) { vv[0] = ux; vv[1] = uy; vv[2] = uz; }
             return true;
         }
         // first entry (x-major) not at this level: missing -> empty, coarser -> restart there
@@ -394,6 +406,7 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
         const int e = __ldg(reinterpret_cast<const int*>(rp) + j);
         if (e < 0) {
             clear(res);
+            if (VEL) vv[0] = vv[1] = vv[2] = 0.f;
             return true;
         }
         const int lc = rec_flags(T, e) & 255;
@@ -416,8 +429,8 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
 }
 
 // CIC at a point whose deepest cell is `cell` (simplehyperoctree.h:1410-1469).
-template <class P>
-__device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, const P& pos, bool need_all, Field7& res)
+template <bool VEL, class P>
+__device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, const P& pos, bool need_all, Field7& res, float* vv)
 {
     int cell = d.cell, L = d.level;
     float fd[3] = {d.fd[0], d.fd[1], d.fd[2]};
@@ -428,6 +441,7 @@ __device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, const P&
         int lvl = L;
         bool missing = false;
         float gx = 0.f, gy = 0.f, gz = 0.f, gt = 0.f, rho = 0.f, phi = 0.f, a = 0.f;
+        float ux = 0.f, uy = 0.f, uz = 0.f;
         for (int v = 0; v < 8; ++v) {
             const int ox = (v & 1) ? ((sx > 0) ? 1 : 0) : ((sx > 0) ? 0 : -1);
             const int oy = (v & 2) ? ((sy > 0) ? 1 : 0) : ((sy > 0) ? 0 : -1);
@@ -443,11 +457,18 @@ __device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, const P&
             if (need_all) {
                 const float4 s = __ldg(T.scal + e);
                 rho = fmaf(s.x, wt, rho); phi = fmaf(s.y, wt, phi); a = fmaf(s.z, wt, a);
+                if (VEL) {
+                    const float4 u = __ldg(T.vel + e);
+                    ux = fmaf(u.x, wt, ux); uy = fmaf(u.y, wt, uy); uz = fmaf(u.z, wt, uz);
+                }
             }
         }
         if (lvl == L) {
             if (missing) clear(res);
             else res = Field7{rho, phi, gx, gy, gz, a, gt};
+            if (VEL) {
+                vv[0] = missing ? 0.f : ux; vv[1] = missing ? 0.f : uy; vv[2] = missing ? 0.f : uz;
+            }
             return true;
         }
         MPF_DIAG_COUNT(0);
@@ -469,25 +490,28 @@ __device__ __forceinline__ bool cic_rec(const DevTree& T, const Loc& d, const P&
 
 // maybe_origin: the point can be the exact origin (first step of a ray),
 // where the reference's TSC falls back to CIC (simplehyperoctree.h:1570-1571)
-template <int ORDER, class P>
+// VEL (with need_all): the velocity slots into vv[3] as well.
+template <int ORDER, bool VEL = false, class P>
 __device__ __forceinline__ Field7 gather_at(const DevTree& T, const Loc& d, const P& pos, bool need_all,
-                                            unsigned long long* st, int slot, bool maybe_origin)
+                                            unsigned long long* st, int slot, bool maybe_origin, float* vv = nullptr)
 {
     constexpr int order = ORDER;
     Field7 r;
     if (d.cell < 0) {
         clear(r);
+        if (VEL) vv[0] = vv[1] = vv[2] = 0.f;
         stat(st, slot);
         return r;
     }
     if (!(maybe_origin && pos.px() == 0.0 && pos.py() == 0.0 && pos.pz() == 0.0)) {
-        const bool ok = (order == 1) ? cic_rec(T, d, pos, need_all, r) : tsc_rec(T, d, pos, need_all, r);
+        const bool ok = (order == 1) ? cic_rec<VEL>(T, d, pos, need_all, r, vv) : tsc_rec<VEL>(T, d, pos, need_all, r, vv);
         if (ok) {
             stat(st, slot);
             return r;
         }
     }
     stat(st, slot + 1);
+    if (VEL && need_all) return vel_slow(T, order, pos.px(), pos.py(), pos.pz(), vv);
     return (order == 1) ? cic_slow(T, pos.px(), pos.py(), pos.pz(), need_all)
                         : tsc_slow(T, pos.px(), pos.py(), pos.pz(), need_all);
 }
@@ -495,6 +519,7 @@ __device__ __forceinline__ Field7 gather_at(const DevTree& T, const Loc& d, cons
 struct FastRec {
     double a, t, x, y, z, k0, k1, k2, k3;
     double phi, red, chi, lambda, s, isw, iswold;
+    double dop;   // velocity-field octrees: the point's Doppler term v.k / (c k0)
     float rho, dx, dy, dz, dt, ah;   // dt: the photon's (forward) dphidt
     int level;
 };
@@ -614,8 +639,12 @@ struct JacSums {
 
 // SRC: source mode (one surface at the ray's own radius); WIDE: per-ray
 // surfaces and wide surface records (bundle rays).  The plain instantiation,
-// the map and benchmark path, carries neither.
-template <int ORDER, bool SRC, bool WIDE, bool BORN = false>
+// the map and benchmark path, carries neither.  VEL: a velocity-field octree
+// (the reference's -DVELOCITYFIELD build): the post-step gathers also read
+// the velocity slots, an all-zero record with a velocity is not empty, and
+// the redshift takes the ISW, Doppler and observer terms
+// (integrator.h:707-708, 765-767); plain instantiations only.
+template <int ORDER, bool SRC, bool WIDE, bool BORN = false, bool VEL = false>
 __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* L, long long i,
                                const PropOut& O, JacSums J)
 {
@@ -648,12 +677,17 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
     }
     Loc here = locate_full(T, b.x, b.y, b.z);
-    Field7 data = born ? hom : gather_at<ORDER>(T, here, PosAt{b.x, b.y, b.z}, true, st, ST_POST_REC, true);
+    float vv[3] = {0.f, 0.f, 0.f};   // VEL: the velocity of the last post-step gather
+    Field7 data = born ? hom : gather_at<ORDER, VEL>(T, here, PosAt{b.x, b.y, b.z}, true, st, ST_POST_REC, true, vv);
     {
         const double ph = (double)data.phi / c2;
         const double norm = sqrt((c2 * (1.0 + 2.0 * ph) * b.k0 * b.k0) / ((1.0 - 2.0 * ph) * (b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3)));
         b.k1 *= norm; b.k2 *= norm; b.k3 *= norm;
     }
+    const double v0n = VEL ? (P.vobs[0] * b.k1 + P.vobs[1] * b.k2 + P.vobs[2] * b.k3) / (kC * b.k0) : 0.0;
+    b.dop = 0.0;
+    // data != empty (integrator.h:715): with VEL the velocity slots count too
+    auto empty = [&]() -> bool { return is_empty(data) && (!VEL || (vv[0] == 0.f && vv[1] == 0.f && vv[2] == 0.f)); };
     b.a = interp_fast(C, b.t, C.a, C.slope_a);
     b.level = (here.cell >= 0) ? here.level : 0;
     b.ah = 0.f;
@@ -705,13 +739,18 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
     // instead, which needs no division.  The starting point's redshift is 0.
     const double opc = 1.0 + phi0c2;
     const double inv_c2 = 1.0 / c2;
-    auto red_of = [&](const FastRec& r) -> double { return a0 * recip(r.a) * (opc - r.phi * inv_c2) - 1.0; };
-    auto red_above = [&](const FastRec& r, double zref) -> bool { return a0 * (opc - r.phi * inv_c2) > (1.0 + zref) * r.a; };
+    // VEL: a0 / a (1 + phi0/c^2 - phi/c^2 + isw + v.k / (c k0) - v0n) - 1
+    auto zbracket = [&](const FastRec& r) -> double {
+        if (VEL) return opc - r.phi * inv_c2 + r.isw + r.dop - v0n;
+        return opc - r.phi * inv_c2;
+    };
+    auto red_of = [&](const FastRec& r) -> double { return a0 * recip(r.a) * zbracket(r) - 1.0; };
+    auto red_above = [&](const FastRec& r, double zref) -> bool { return a0 * zbracket(r) > (1.0 + zref) * r.a; };
     bool b_red_ok = true;     // b.red holds b's redshift
     const float two_c2 = (float)(2.0 / c2);
     const float inv_c2f = (float)(1.0 / c2);
     FastRec p;
-    while (!is_empty(data)) {
+    while (!empty()) {
         if (k >= P.max_steps) { status |= 1u; break; }
         // ---- RK4 step (integrator.h:718-734).  The state stays FP64 and is
         // accumulated in FP64; the four stages are evaluated in FP32 as
@@ -854,7 +893,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             dtf = fmaf(dlf, kb0, dl6f * S0);
         }
         const Loc ploc = locate_near(T, here, p.x, p.y, p.z);
-        data = born ? hom : gather_at<ORDER>(T, ploc, PosAt{p.x, p.y, p.z}, true, st, ST_POST_REC, false);
+        data = born ? hom : gather_at<ORDER, VEL>(T, ploc, PosAt{p.x, p.y, p.z}, true, st, ST_POST_REC, false, vv);
         {
             // the extent test (integrator.h:757): a point in a located cell away from
             // the domain faces is inside; only cells on a face (or wrapped keys)
@@ -862,9 +901,12 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
             const uint32_t last = (ploc.cell >= 0) ? (uint32_t)((1ull << ploc.level) - 1ull) : 0u;
             const bool face = (ploc.cell < 0) || ploc.c[0] == 0u || ploc.c[1] == 0u || ploc.c[2] == 0u ||
                               ploc.c[0] >= last || ploc.c[1] >= last || ploc.c[2] >= last;
-            if (p.a < 0.0 || (face && !((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx))))
+            if (p.a < 0.0 || (face && !((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx)))) {
                 clear(data);
+                if (VEL) vv[0] = vv[1] = vv[2] = 0.f;
+            }
         }
+        if (VEL) p.dop = ((double)vv[0] * p.k1 + (double)vv[1] * p.k2 + (double)vv[2] * p.k3) / (kC * p.k0);
         p.level = (ploc.cell >= 0) ? ploc.level : 0;
         p.ah = data.a;
         p.rho = data.rho; p.phi = data.phi; p.dx = data.dx; p.dy = data.dy; p.dz = data.dz;
@@ -883,7 +925,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
         bool p_red_ok = false;
         auto need_p_red = [&]() { if (!p_red_ok) { p.red = red_of(p); p_red_ok = true; } };
         auto need_b_red = [&]() { if (!b_red_ok) { b.red = red_of(b); b_red_ok = true; } };
-        if (!is_empty(data)) {
+        if (!empty()) {
             const double ratio = p.a * p.a * ratio_k;
             dl = (ploc.cell >= 0 ? cell_extent(ploc.level) : 0.0) * ratio;
             last_data_dt = data.dt;
@@ -1083,7 +1125,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
 #else
 #define MPF_FAST_BOUNDS __launch_bounds__(kFastThreads, MPF_FAST_MINB)
 #endif
-template <int ORDER, bool SRC, bool WIDE, bool BORN = false>
+template <int ORDER, bool SRC, bool WIDE, bool BORN = false, bool VEL = false>
 __global__ void MPF_FAST_BOUNDS k_propagate_fast(DevTree T, DevCosmo C, PropParams P,
                                                                     const double* __restrict__ launch, long long n, PropOut O,
                                                                     unsigned long long* queue, int depth, long long lo)
@@ -1100,7 +1142,7 @@ __global__ void MPF_FAST_BOUNDS k_propagate_fast(DevTree T, DevCosmo C, PropPara
         if (base >= (unsigned long long)n) break;
         for (int d = 0; d < depth; ++d) {
             const long long i = (long long)base + 32ll * d + lane;
-            if (i < n) propagate_fast<ORDER, SRC, WIDE, BORN>(T, C, P, launch + 6 * i, i, O, J);
+            if (i < n) propagate_fast<ORDER, SRC, WIDE, BORN, VEL>(T, C, P, launch + 6 * i, i, O, J);
             __syncwarp();
         }
     }

@@ -19,6 +19,7 @@ struct mpf_octree {
     int2* node;
     int* grid;
     int4* stencil;
+    float4* vel;             // velocity field (vx, vy, vz, 0) per cell, or null
 };
 
 struct mpf_cosmology {
@@ -65,7 +66,7 @@ cudaError_t launch_gather(const DevTree& T, int kind, bool exact, const double* 
 // 128 x 1, 64 x 1, 32 x 1, 128 x 2 threads x claim depth; 3 for the
 // catalogue: 128, 64, 32 threads).
 bool tuned_shape(int dev, const DevTree& T, int mode, int* tpb, int* depth, double* rates);
-int plain_fast_mode(int order);
+int plain_fast_mode(int order, bool velocity);
 bool catalogue_tuned_shape(int dev, const DevTree& T, int order, int* tpb, double* rates);
 // forget an octree's tuned shapes when its arrays are freed
 void forget_tuned_shape(const void* keys);

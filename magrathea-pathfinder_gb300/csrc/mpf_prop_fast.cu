@@ -17,13 +17,23 @@ cudaError_t launch_gather_exact(const DevTree& T, int kind, const double* d_xyz,
 
 // The kernel instantiation a launch uses: per interpolation order and mode
 // (surfaces / sources / wide surfaces, per-ray surfaces, direction launches,
-// trajectories; Born rays).
-static int fast_mode(const PropParams& P, const PropOut& O)
+// trajectories; Born rays; a velocity-field octree, plain surfaces only).
+static int fast_mode(const DevTree& T, const PropParams& P, const PropOut& O)
 {
     if (P.homogeneous == 2) return P.ray_stop ? 0 : 1;
     if (P.ray_stop) return (P.order == 1) ? 2 : 3;
     if (P.wide || P.ray_planes || P.direct || O.traj) return (P.order == 1) ? 4 : 5;
+    if (T.vel) return (P.order == 1) ? 8 : 9;
     return (P.order == 1) ? 6 : 7;
+}
+
+// A velocity-field octree runs the FP32-gather kernel in the plain mode only
+// (surface records: propagation and maps); its other modes (Born, source,
+// bundle and trajectory rays) run the float64 kernel.
+static bool fast_mode_supported(const DevTree& T, const PropParams& P, const PropOut& O)
+{
+    const int m = fast_mode(T, P, O);
+    return !T.vel || m == 8 || m == 9;
 }
 
 // Launches rays [lo, n) of the batch as grid blocks of tpb threads, each warp
@@ -33,7 +43,7 @@ static void launch_fast_kernel(long long grid, int tpb, int depth, long long lo,
                                unsigned long long* queue, cudaStream_t stream)
 {
     const unsigned g = (unsigned)grid;
-    switch (fast_mode(P, O)) {
+    switch (fast_mode(T, P, O)) {
     // Born rays: the field is homogeneous, so the interpolation order does
     // not enter (the Jacobian gathers are TSC)
     case 0: k_propagate_fast<2, true, false, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue, depth, lo); break;
@@ -43,6 +53,8 @@ static void launch_fast_kernel(long long grid, int tpb, int depth, long long lo,
     case 4: k_propagate_fast<1, false, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue, depth, lo); break;
     case 5: k_propagate_fast<2, false, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue, depth, lo); break;
     case 6: k_propagate_fast<1, false, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue, depth, lo); break;
+    case 8: k_propagate_fast<1, false, false, false, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue, depth, lo); break;
+    case 9: k_propagate_fast<2, false, false, false, true><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue, depth, lo); break;
     default: k_propagate_fast<2, false, false><<<g, tpb, 0, stream>>>(T, C, P, d_launch, n, O, queue, depth, lo); break;
     }
 }
@@ -226,7 +238,8 @@ void forget_tuned_shape(const void* keys)
 }
 
 // the kernel mode of the plain (surface-record) instantiation for `order`
-int plain_fast_mode(int order) { return (order == 1) ? 6 : 7; }
+// (8 / 9 on a velocity-field octree)
+int plain_fast_mode(int order, bool velocity) { return velocity ? ((order == 1) ? 8 : 9) : ((order == 1) ? 6 : 7); }
 
 template <>
 cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const PropParams& P, const double* d_launch, long long n,
@@ -234,7 +247,7 @@ cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const P
 {
     if (n <= 0) return cudaSuccess;
     // NGP (ORDER = 0) has no interpolation arithmetic to lighten: the float64 kernel
-    if (P.order == 0) return launch_propagate<true>(T, C, P, d_launch, n, O, stream);
+    if (P.order == 0 || !fast_mode_supported(T, P, O)) return launch_propagate<true>(T, C, P, d_launch, n, O, stream);
     FastLaunchState st;
     cudaError_t e = fast_launch_state(stream, &st);
     if (e != cudaSuccess) return e;
@@ -251,7 +264,7 @@ cudaError_t launch_propagate<false>(const DevTree& T, const DevCosmo& C, const P
         // a batch that fills the GPU: the tuned shape of this octree and kernel mode
         int dev = 0;
         if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        const auto key = std::make_tuple(dev, (const void*)T.keys, fast_mode(P, O));
+        const auto key = std::make_tuple(dev, (const void*)T.keys, fast_mode(T, P, O));
         TuneResult res;
         bool have = false;
         {

@@ -85,6 +85,9 @@ struct PropParams {
     // per-ray plane normals for the stop criterion "plane" with per-ray
     // surfaces (n x nplanes x 3; the last one is the stop plane's), or null
     const double* ray_ki;
+    // observer velocity (parameters v0x v0y v0z, hmaps.h:80-84), read when the
+    // octree carries a velocity field (integrator.h:537-538, 707-708)
+    double vobs[3];
 };
 
 struct PropOut {
@@ -144,6 +147,23 @@ __device__ __forceinline__ Field7 field_at(const DevTree& T, const PropParams& P
     }
     return gather<EXACT>(T, P.order, x, y, z, need_all);
 }
+
+// the field and the velocity at a point of a velocity-field octree (the
+// homogeneous field has no velocity: integrator.h:663-664)
+template <bool EXACT>
+__device__ __forceinline__ Field7 field_vel_at(const DevTree& T, const PropParams& P, double x, double y, double z, float* v)
+{
+    if (P.homogeneous) {
+        v[0] = v[1] = v[2] = 0.f;
+        Field7 h;
+        clear(h);
+        h.a = 1.f;
+        return h;
+    }
+    return gather_vel<EXACT>(T, P.order, x, y, z, v);
+}
+
+__device__ __forceinline__ bool vel_zero(const float* v) { return v[0] == 0.f && v[1] == 0.f && v[2] == 0.f; }
 
 __device__ __forceinline__ Found locate_at(const DevTree& T, const PropParams& P, double x, double y, double z)
 {
@@ -279,12 +299,20 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
         b.k1 = (L[3] - L[0]) / norm; b.k2 = (L[4] - L[1]) / norm; b.k3 = (L[5] - L[2]) / norm;
         b.index = 0.0;
     }
-    Field7 data = field_at<EXACT>(T, P, b.x, b.y, b.z, true);
+    // Velocity-field octree (the reference built with -DVELOCITYFIELD): the
+    // record's velocity slots are gathered with the other fields, count in its
+    // emptiness test (data != empty compares every member), and the redshift
+    // takes the ISW, Doppler and observer terms (integrator.h:765-767).
+    const bool velf = T.vel != nullptr;
+    float vel[3] = {0.f, 0.f, 0.f};
+    Field7 data = velf ? field_vel_at<EXACT>(T, P, b.x, b.y, b.z, vel) : field_at<EXACT>(T, P, b.x, b.y, b.z, true);
     {
         const double ph = (double)data.phi / c2;
         const double norm = sqrt((c2 * (one + two * ph) * b.k0 * b.k0) / ((one - two * ph) * (b.k1 * b.k1 + b.k2 * b.k2 + b.k3 * b.k3)));
         b.k1 *= norm; b.k2 *= norm; b.k3 *= norm;
     }
+    // v0n: the observer velocity along the launch direction (integrator.h:707-708)
+    const double v0n = velf ? (P.vobs[0] * b.k1 + P.vobs[1] * b.k2 + P.vobs[2] * b.k3) / (kC * b.k0) : 0.0;
     b.a = interpolate(b.t, C.t, C.a, C.n);
     Found loc = locate_at(T, P, b.x, b.y, b.z);
     b.level = (loc.cell >= 0) ? (double)loc.level : 0.0;
@@ -332,7 +360,7 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
     Rec p = b;
     p.isw = zero; p.iswold = zero; p.lambda = zero; p.s = zero;
     double core[9], dc0[9], dc1[9], dc2[9], dc3[9];
-    while (!is_empty(data)) {
+    while (!(is_empty(data) && vel_zero(vel))) {
         if (k >= P.max_steps) { status |= 1u; break; }
         const double bcore[9] = {b.a, b.t, b.x, b.y, b.z, b.k0, b.k1, b.k2, b.k3};
         p.index = b.index + one;
@@ -350,8 +378,11 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
         for (int q = 0; q < 9; ++q) core[q] = bcore[q] + (dl / six) * (dc0[q] + two * dc1[q] + two * dc2[q] + dc3[q]);
         p.a = core[0]; p.t = core[1]; p.x = core[2]; p.y = core[3]; p.z = core[4];
         p.k0 = core[5]; p.k1 = core[6]; p.k2 = core[7]; p.k3 = core[8];
-        data = field_at<EXACT>(T, P, p.x, p.y, p.z, true);
-        if (!(!(p.a < zero) && ((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx)))) clear(data);
+        data = velf ? field_vel_at<EXACT>(T, P, p.x, p.y, p.z, vel) : field_at<EXACT>(T, P, p.x, p.y, p.z, true);
+        if (!(!(p.a < zero) && ((p.x > mn) && (p.x < mx) && (p.y > mn) && (p.y < mx) && (p.z > mn) && (p.z < mx)))) {
+            clear(data);
+            vel[0] = vel[1] = vel[2] = 0.f;
+        }
         loc = locate_at(T, P, p.x, p.y, p.z);
         p.level = (loc.cell >= 0) ? (double)loc.level : 0.0;
         p.ah = data.a;
@@ -370,9 +401,14 @@ __device__ void propagate_one(const DevTree& T, const DevCosmo& C, const PropPar
         p.chi = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
         p.lambda += dl;
         p.s += sqrt((p.x - b.x) * (p.x - b.x) + (p.y - b.y) * (p.y - b.y) + (p.z - b.z) * (p.z - b.z));
-        p.red = a0 / p.a * (one + phi0c2 - p.phi / c2) - one;
+        if (velf) {
+            const double dop = ((double)vel[0] * p.k1 + (double)vel[1] * p.k2 + (double)vel[2] * p.k3) / (kC * p.k0);
+            p.red = a0 / p.a * (one + phi0c2 - p.phi / c2 + p.isw + dop - v0n) - one;
+        } else {
+            p.red = a0 / p.a * (one + phi0c2 - p.phi / c2) - one;
+        }
         bool appended = false;
-        if (!is_empty(data)) {
+        if (!(is_empty(data) && vel_zero(vel))) {
             ratio = p.a * p.a * (scale / kC) / P.nsteps;
             dl = (loc.cell >= 0 ? cell_extent(loc.level) : 0.0) * ratio;
             appended = true;

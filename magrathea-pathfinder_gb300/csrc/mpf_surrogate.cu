@@ -1123,6 +1123,8 @@ int mpf_surrogate_propagate(mpf_surrogate* s, const mpf_octree* o, const mpf_cos
 {
     if (!s || !o || !c || !p || !sp || n < 0 || (n > 0 && (!launch || !steps || !flags)))
         return fail(MPF_BAD_INPUT, "mpf_surrogate_propagate: bad argument");
+    if (o->tree.vel)
+        return fail(MPF_BAD_INPUT, "mpf_surrogate_propagate: the surrogate has no velocity field; the octree carries one");
     if (p->nplanes != 0 || p->jacobian || p->exact || p->nsteps == 0 || (p->order != 1 && p->order != 2) || p->stop < 0 ||
         p->stop > 6 || !(p->length > 0.0) || !(sp->tolerance >= 0.0) || sp->check_every < 1)
         return fail(MPF_BAD_INPUT, "mpf_surrogate_propagate: unsupported parameters (surfaces, Jacobian and exact mode are "

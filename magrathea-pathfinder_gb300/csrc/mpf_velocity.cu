@@ -1,0 +1,395 @@
+// Velocity field of the cone octree (the reference built with -DVELOCITYFIELD):
+// the per-cell velocity slots (src/gravity2.h:45), their deposit from
+// particles with CIC or TSC weights at every level of the octree
+// (Hmaps::CreateOctreeVelocityWithCIC / WithTSC, src/hmaps.h:439-485,
+// 501-550), the zeroed masses before and the mass normalisation and parent
+// fill after (src/hmaps.cpp:396, 424-441).  Must be compiled with
+// -fmad=false: the weights are the reference's float64 expressions.
+//
+// The deposit reproduces the reference's accumulation order.  A cell's
+// float accumulators (its rho and velocity slots) take, one after another,
+// rho += w and v += v_p * w (float += double: the sum is formed in float64
+// and rounded to float) for its particles in the order a single thread
+// visits them (particle, then vertex).  On the device: every (particle,
+// level, vertex) whose cell exists becomes a pair (cell, particle << 5 |
+// vertex), the pairs are stably sorted by cell (LSD radix, 4-bit digits),
+// and one thread walks each cell's run of pairs in order.  The result is
+// deterministic and bit-identical to the reference run on one thread; the
+// reference's own multithreaded loop (Utility::parallelize, src/utility.h:
+// 127-147) adds to shared cells without atomics, so its sums vary with the
+// thread interleaving.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "mpf_internal.h"
+
+namespace mpf {
+namespace {
+
+constexpr int kVelTile = 256;                 // pairs per radix-sort tile (one thread each)
+constexpr long long kVelChunk = 1ll << 19;    // particles per pass (payload: particle << 5 | vertex)
+
+__device__ __forceinline__ int rec_level(const DevTree& T, int cell)
+{
+    return __ldg(reinterpret_cast<const int*>(T.stencil + 8 * (size_t)cell) + 27) & 255;
+}
+__device__ __forceinline__ int rec_parent(const DevTree& T, int cell)
+{
+    return __ldg(reinterpret_cast<const int*>(T.stencil + 8 * (size_t)cell) + 30);
+}
+
+// Offset of vertex v along each axis: CIC loops iz, iy, ix over {-1, 1}
+// (hmaps.h:462-464), TSC over {-1, 0, 1} (hmaps.h:525-530), ix fastest.
+__device__ __forceinline__ void vertex_offsets(int scheme, int v, int* o)
+{
+    if (scheme == 1) {
+        o[0] = 2 * (v & 1) - 1;
+        o[1] = 2 * ((v >> 1) & 1) - 1;
+        o[2] = 2 * ((v >> 2) & 1) - 1;
+    } else {
+        o[0] = v % 3 - 1;
+        o[1] = (v / 3) % 3 - 1;
+        o[2] = v / 9 - 1;
+    }
+}
+
+// The level-L cell a particle's vertex v falls in, if the octree holds that
+// exact key (hmaps.h:466-470, 532-536), else -1.  The vertex point is the
+// particle's float position plus (CIC) half a cell or (TSC) one cell times
+// the offset, in float64.
+__device__ __forceinline__ int vertex_cell(const DevTree& T, int scheme, int L, const float* p, int v)
+{
+    int o[3];
+    vertex_offsets(scheme, v, o);
+    const double half = half_cell(L);
+    const double step = (scheme == 1) ? half : __dmul_rn(2.0, half);
+    uint64_t c[3];
+    for (int d = 0; d < 3; ++d) c[d] = axis_coord(L, __dadd_rn((double)p[d], __dmul_rn(step, (double)o[d])));
+    const Found f = find_cell(T, L, c[0], c[1], c[2]);
+    return (f.cell >= 0 && f.level == L) ? f.cell : -1;
+}
+
+// The weight of a particle at p on the level-L cell reached by vertex v.
+__device__ __forceinline__ double vertex_weight(int scheme, int L, const float* p, int v)
+{
+    int o[3];
+    vertex_offsets(scheme, v, o);
+    // the cell's centre, from its integer coordinates at level L (the
+    // vertex's, which are the cell's own)
+    const double half = half_cell(L);
+    const double step = (scheme == 1) ? half : __dmul_rn(2.0, half);
+    double cen[3];
+    for (int d = 0; d < 3; ++d)
+        cen[d] = coord_center(L, axis_coord(L, __dadd_rn((double)p[d], __dmul_rn(step, (double)o[d]))));
+    if (scheme == 1) {
+        // (1 - |x - c| / extent) per axis, multiplied left to right (hmaps.h:472)
+        const double inv = pow2(L - kLevelShift);   // 1 / (EXTENT / 2^L), exact
+        double w = __dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn((double)p[0], cen[0])), inv));
+        w = __dmul_rn(w, __dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn((double)p[1], cen[1])), inv)));
+        w = __dmul_rn(w, __dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn((double)p[2], cen[2])), inv)));
+        return w;
+    }
+    // quadratic weights of |c - x| / cell (hmaps.h:539-545)
+    double w3[3];
+    for (int d = 0; d < 3; ++d) {
+        const double dist = fabs(__ddiv_rn(__dsub_rn(cen[d], (double)p[d]), step));
+        const int a = abs(o[d]);
+        const double t1 = __dmul_rn(__dmul_rn(__dmul_rn((double)a, 0.5), __dsub_rn(1.5, dist)), __dsub_rn(1.5, dist));
+        const double t2 = __dmul_rn((double)(1 - a), __dsub_rn(0.75, __dmul_rn(dist, dist)));
+        w3[d] = __dadd_rn(t1, t2);
+    }
+    return __dmul_rn(__dmul_rn(w3[0], w3[1]), w3[2]);
+}
+
+// pairs per particle: pass 0 counts them (cnt[i]), pass 1 writes them at off[i]
+__global__ void k_dep_pairs(DevTree T, int scheme, int lmin, int lmax, const float* __restrict__ pos, long long n,
+                            int* cnt, const int* __restrict__ off, unsigned* key, unsigned* pay)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    const int nv = (scheme == 1) ? 8 : 27;
+    int k = 0;
+    const long long base = off ? off[i] : 0;
+    for (int L = lmin; L <= lmax; ++L)
+        for (int v = 0; v < nv; ++v) {
+            const int cell = vertex_cell(T, scheme, L, p, v);
+            if (cell < 0) continue;
+            if (off) {
+                key[base + k] = (unsigned)cell;
+                pay[base + k] = ((unsigned)i << 5) | (unsigned)v;
+            }
+            ++k;
+        }
+    if (!off) cnt[i] = k;
+}
+
+// stable LSD radix sort of (key, pay) by key, 4-bit digits, one tile per thread
+__global__ void k_dep_hist(long long m, const unsigned* __restrict__ key, int shift, int* hist, long long ntiles)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    int h[16];
+    for (int d = 0; d < 16; ++d) h[d] = 0;
+    const long long e = min(m, (t + 1) * kVelTile);
+    for (long long j = t * kVelTile; j < e; ++j) ++h[(key[j] >> shift) & 15u];
+    for (int d = 0; d < 16; ++d) hist[d * ntiles + t] = h[d];
+}
+__global__ void k_dep_scatter(long long m, const unsigned* __restrict__ key, const unsigned* __restrict__ pay, int shift,
+                              const int* __restrict__ off, long long ntiles, unsigned* key2, unsigned* pay2)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    int o[16];
+    for (int d = 0; d < 16; ++d) o[d] = off[d * ntiles + t];
+    const long long e = min(m, (t + 1) * kVelTile);
+    for (long long j = t * kVelTile; j < e; ++j) {
+        const int q = o[(key[j] >> shift) & 15u]++;
+        key2[q] = key[j];
+        pay2[q] = pay[j];
+    }
+}
+
+// one thread per run of equal cells: the reference's sequential += in order
+__global__ void k_dep_accumulate(DevTree T, float4* scal, float4* vel, int scheme, const float* __restrict__ pos,
+                                 const float* __restrict__ pv, long long m, const unsigned* __restrict__ key,
+                                 const unsigned* __restrict__ pay)
+{
+    const long long j0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j0 >= m || (j0 > 0 && key[j0] == key[j0 - 1])) return;
+    const int cell = (int)key[j0];
+    const int L = rec_level(T, cell);
+    float rho = scal[cell].x;
+    float4 u = vel[cell];
+    for (long long j = j0; j < m && key[j] == (unsigned)cell; ++j) {
+        const long long i = pay[j] >> 5;
+        const int v = (int)(pay[j] & 31u);
+        const float p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+        const double w = vertex_weight(scheme, L, p, v);
+        rho = __double2float_rn(__dadd_rn((double)rho, w));
+        u.x = __double2float_rn(__dadd_rn((double)u.x, __dmul_rn((double)pv[3 * i], w)));
+        u.y = __double2float_rn(__dadd_rn((double)u.y, __dmul_rn((double)pv[3 * i + 1], w)));
+        u.z = __double2float_rn(__dadd_rn((double)u.z, __dmul_rn((double)pv[3 * i + 2], w)));
+    }
+    scal[cell].x = rho;
+    vel[cell] = u;
+}
+
+__global__ void k_dep_begin(long long n, float4* scal, float4* vel)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    scal[i].x = 0.f;
+    vel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// v /= mass, a zero mass read as 1 (hmaps.cpp:425-431)
+__global__ void k_dep_normalise(long long n, const float4* __restrict__ scal, float4* vel)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double mass = (double)scal[i].x;
+    mass = __dadd_rn(mass, (double)(mass == 0.0));
+    float4 u = vel[i];
+    u.x = __double2float_rn(__ddiv_rn((double)u.x, mass));
+    u.y = __double2float_rn(__ddiv_rn((double)u.y, mass));
+    u.z = __double2float_rn(__ddiv_rn((double)u.z, mass));
+    vel[i] = u;
+}
+
+// std::isnormal of a float: neither zero, subnormal, infinite nor NaN
+__device__ __forceinline__ bool normal_f(float x)
+{
+    const unsigned b = __float_as_uint(x) & 0x7fffffffu;
+    return b >= 0x00800000u && b < 0x7f800000u;
+}
+
+// cells of level L whose mass is not normal take their parent's velocity
+// (hmaps.cpp:433-441); the parent, one level up, is final already
+__global__ void k_dep_from_parent(DevTree T, long long n, int L, const float4* __restrict__ scal, float4* vel)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (rec_level(T, (int)i) != L || normal_f(scal[i].x)) return;
+    const int par = rec_parent(T, (int)i);
+    if (par < 0) return;
+    const float4 pu = vel[par];
+    float4 u = vel[i];
+    u.x = pu.x; u.y = pu.y; u.z = pu.z;
+    vel[i] = u;
+}
+
+__global__ void k_vel_set(long long n, const float* __restrict__ v3, const float* __restrict__ rho, float4* scal, float4* vel)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    vel[i] = make_float4(v3[3 * i], v3[3 * i + 1], v3[3 * i + 2], 0.f);
+    if (rho) scal[i].x = rho[i];
+}
+
+__global__ void k_vel_get(long long n, const float4* __restrict__ scal, const float4* __restrict__ vel, float* v3, float* rho)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (v3) {
+        const float4 u = vel ? vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        v3[3 * i] = u.x; v3[3 * i + 1] = u.y; v3[3 * i + 2] = u.z;
+    }
+    if (rho) rho[i] = scal[i].x;
+}
+
+inline unsigned blocks(long long n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
+
+// device buffer freed on scope exit
+struct DevMem {
+    void* p = nullptr;
+    ~DevMem() { if (p) cudaFree(p); }
+    cudaError_t alloc(size_t bytes) { return cudaMalloc(&p, bytes ? bytes : 1); }
+    template <class T> T* as() const { return (T*)p; }
+};
+
+cudaError_t ensure_velocity(mpf_octree* o)
+{
+    if (o->vel) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&o->vel, (size_t)o->n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemset(o->vel, 0, (size_t)o->n * sizeof(float4));
+    if (e != cudaSuccess) {
+        if (o->vel) cudaFree(o->vel);
+        o->vel = nullptr;
+        return e;
+    }
+    o->tree.vel = o->vel;
+    return cudaSuccess;
+}
+
+// one pass over particles [0, n) of the chunk already on the device
+cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const float* d_vel, long long n)
+{
+    const DevTree& T = o->tree;
+    DevMem cnt;
+    cudaError_t e = cnt.alloc((size_t)(n + 1) * sizeof(int));
+    if (e != cudaSuccess) return e;
+    k_dep_pairs<<<blocks(n, 128), 128>>>(T, scheme, o->level_min, o->level_max, d_pos, n, cnt.as<int>(), nullptr, nullptr,
+                                          nullptr);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaMemset(cnt.as<int>() + n, 0, sizeof(int))) != cudaSuccess) return e;
+    const long long m = exclusive_scan(cnt.as<int>(), n + 1, 0);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (m <= 0) return cudaSuccess;
+    DevMem key, pay, key2, pay2, hist;
+    const long long ntiles = (m + kVelTile - 1) / kVelTile;
+    if ((e = key.alloc((size_t)m * 4)) != cudaSuccess || (e = pay.alloc((size_t)m * 4)) != cudaSuccess ||
+        (e = key2.alloc((size_t)m * 4)) != cudaSuccess || (e = pay2.alloc((size_t)m * 4)) != cudaSuccess ||
+        (e = hist.alloc((size_t)(16 * ntiles + 1) * sizeof(int))) != cudaSuccess)
+        return e;
+    k_dep_pairs<<<blocks(n, 128), 128>>>(T, scheme, o->level_min, o->level_max, d_pos, n, nullptr, cnt.as<int>(),
+                                          key.as<unsigned>(), pay.as<unsigned>());
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // digits up to the highest bit of the largest cell index
+    int bits = 1;
+    while (bits < 31 && (1ll << bits) < o->n) ++bits;
+    unsigned *k1 = key.as<unsigned>(), *p1 = pay.as<unsigned>(), *k2 = key2.as<unsigned>(), *p2 = pay2.as<unsigned>();
+    for (int shift = 0; shift < bits; shift += 4) {
+        k_dep_hist<<<blocks(ntiles, 128), 128>>>(m, k1, shift, hist.as<int>(), ntiles);
+        exclusive_scan(hist.as<int>(), 16 * ntiles, 0);
+        k_dep_scatter<<<blocks(ntiles, 128), 128>>>(m, k1, p1, shift, hist.as<int>(), ntiles, k2, p2);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        std::swap(k1, k2);
+        std::swap(p1, p2);
+    }
+    k_dep_accumulate<<<blocks(m, 128), 128>>>(T, o->scal, o->vel, scheme, d_pos, d_vel, m, k1, p1);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return cudaDeviceSynchronize();
+}
+
+}  // namespace
+}  // namespace mpf
+
+using namespace mpf;
+
+extern "C" {
+
+int mpf_octree_set_velocity(mpf_octree* o, const float* v3, const float* rho)
+{
+    if (!o) return mpf_internal_set_error(MPF_BAD_INPUT, "mpf_octree_set_velocity: null octree");
+    if (!v3) {
+        if (rho) return mpf_internal_set_error(MPF_BAD_INPUT, "mpf_octree_set_velocity: rho without velocities");
+        if (o->vel) cudaFree(o->vel);
+        o->vel = nullptr;
+        o->tree.vel = nullptr;
+        return MPF_OK;
+    }
+    const long long n = o->n;
+    DevMem dv, dr;
+    cudaError_t e = ensure_velocity(o);
+    if (e == cudaSuccess) e = dv.alloc((size_t)n * 3 * sizeof(float));
+    if (e == cudaSuccess && rho) e = dr.alloc((size_t)n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(dv.p, v3, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && rho) e = cudaMemcpy(dr.p, rho, (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_vel_set<<<blocks(n, 256), 256>>>(n, dv.as<float>(), rho ? dr.as<float>() : nullptr, o->scal, o->vel);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return mpf_internal_set_error(MPF_CUDA_ERROR, cudaGetErrorString(e));
+    return MPF_OK;
+}
+
+int mpf_octree_get_velocity(const mpf_octree* o, float* v3, float* rho)
+{
+    if (!o || (!v3 && !rho)) return mpf_internal_set_error(MPF_BAD_INPUT, "mpf_octree_get_velocity: bad argument");
+    const long long n = o->n;
+    DevMem dv, dr;
+    cudaError_t e = cudaSuccess;
+    if (v3) e = dv.alloc((size_t)n * 3 * sizeof(float));
+    if (e == cudaSuccess && rho) e = dr.alloc((size_t)n * sizeof(float));
+    if (e == cudaSuccess) {
+        k_vel_get<<<blocks(n, 256), 256>>>(n, o->scal, o->vel, v3 ? dv.as<float>() : nullptr, rho ? dr.as<float>() : nullptr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && v3) e = cudaMemcpy(v3, dv.p, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && rho) e = cudaMemcpy(rho, dr.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return mpf_internal_set_error(MPF_CUDA_ERROR, cudaGetErrorString(e));
+    return o->vel ? MPF_OK : mpf_internal_set_error(MPF_OK, "mpf_octree_get_velocity: the octree has no velocity field");
+}
+
+int mpf_velocity_deposit(mpf_octree* o, int scheme, int64_t n, const float* pos, const float* vel, int flags)
+{
+    if (!o || (scheme != 1 && scheme != 2) || n < 0 || (n > 0 && (!pos || !vel)) || (flags & ~3))
+        return mpf_internal_set_error(MPF_BAD_INPUT, "mpf_velocity_deposit: bad argument");
+    if (!(flags & MPF_VELOCITY_BEGIN) && !o->vel)
+        return mpf_internal_set_error(MPF_BAD_INPUT,
+                                      "mpf_velocity_deposit: the octree has no velocity field (start with MPF_VELOCITY_BEGIN)");
+    if (o->n >= (1ll << 31)) return mpf_internal_set_error(MPF_BAD_INPUT, "mpf_velocity_deposit: octree too large");
+    cudaError_t e = ensure_velocity(o);
+    if (e == cudaSuccess && (flags & MPF_VELOCITY_BEGIN)) {
+        k_dep_begin<<<blocks(o->n, 256), 256>>>(o->n, o->scal, o->vel);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && n > 0) {
+        // at most kVelChunk particles and about 2^28 pairs (4 GB of sort buffers) per pass
+        const long long per = (long long)((scheme == 1) ? 8 : 27) * (o->level_max - o->level_min + 1);
+        const long long chunk = std::min<long long>(n, std::max<long long>(1024, std::min<long long>(kVelChunk, (1ll << 28) / per)));
+        DevMem dp, dv;
+        e = dp.alloc((size_t)chunk * 3 * sizeof(float));
+        if (e == cudaSuccess) e = dv.alloc((size_t)chunk * 3 * sizeof(float));
+        for (long long lo = 0; lo < n && e == cudaSuccess; lo += chunk) {
+            const long long m = std::min<long long>(chunk, n - lo);
+            e = cudaMemcpy(dp.p, pos + 3 * lo, (size_t)m * 3 * sizeof(float), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMemcpy(dv.p, vel + 3 * lo, (size_t)m * 3 * sizeof(float), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = deposit_chunk(o, scheme, dp.as<float>(), dv.as<float>(), m);
+        }
+    }
+    if (e == cudaSuccess && (flags & MPF_VELOCITY_FINISH)) {
+        k_dep_normalise<<<blocks(o->n, 256), 256>>>(o->n, o->scal, o->vel);
+        for (int L = o->level_min + 1; L <= o->level_max; ++L)
+            k_dep_from_parent<<<blocks(o->n, 256), 256>>>(o->tree, o->n, L, o->scal, o->vel);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return mpf_internal_set_error(MPF_CUDA_ERROR, cudaGetErrorString(e));
+    return MPF_OK;
+}
+
+}  // extern "C"

@@ -547,3 +547,29 @@ def photon_grid(n_side: int, half_y_deg: float, half_z_deg: float, frame=None) -
     out = np.zeros((d.shape[0], 6))
     out[:, 3:] = d
     return out
+
+
+def velocity_particles(records: np.ndarray, n: int, seed: int = 5, v_rms: float = 1e-3) -> tuple:
+    """Synthetic particles for the velocity-field deposit: positions (n x 3,
+    float32, octree units) drawn cell by cell (a uniformly chosen leaf cell,
+    then uniformly inside it, so refined regions get more particles per unit
+    volume), velocities (n x 3, float32, in units of c) along minus the
+    potential gradient of their cell, scaled to an rms of v_rms, plus 20 %
+    isotropic noise: the linear-theory flow toward the potential wells."""
+    rng = np.random.default_rng(seed)
+    lev = key_level(records["hi"], records["lo"]).astype(np.int64)
+    # leaves: cells with no next key inside them (pre-order sort: a child follows its parent)
+    nxt_level = np.append(lev[1:], 0)
+    leaf = np.flatnonzero(nxt_level <= lev)
+    pick = leaf[rng.integers(0, leaf.shape[0], n)]
+    centers = np.zeros((n, 3))
+    for L in np.unique(lev[pick]):
+        m = lev[pick] == L
+        c = key_coords(records["hi"][pick[m]], records["lo"][pick[m]], int(L))
+        centers[m] = cell_center(int(L), c)
+    size = 4.0 / 2.0 ** lev[pick]
+    pos = centers + rng.uniform(-0.5, 0.5, (n, 3)) * size[:, None]
+    g = np.stack([records["dphidx"][pick], records["dphidy"][pick], records["dphidz"][pick]], axis=1).astype(np.float64)
+    gn = np.sqrt((g ** 2).sum(1).mean()) or 1.0
+    vel = -g / gn * v_rms + rng.normal(0.0, 0.2 * v_rms / np.sqrt(3.0), (n, 3))
+    return pos.astype(np.float32), vel.astype(np.float32)

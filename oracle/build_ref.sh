@@ -12,7 +12,9 @@
 #  2. Compile with the reference Makefile's flags (-O3 -std=c++17 -DEXTENT=4
 #     -DSIZEOFOCTREE=48 -DIOGROUPSIZE=1 -DMEMORY_SAVING, no -march), with
 #     single-rank MPI and inert HDF5 stand-ins from oracle/stubs/.
-#     Outputs: libref_o0.so / libref_o1.so / libref_o2.so (ref_harness.cpp at ORDER=0 / 1 / 2)
+#     Outputs: libref_o0.so / libref_o1.so / libref_o2.so (ref_harness.cpp at ORDER=0 / 1 / 2),
+#     libref_vel_o0.so / _o1 / _o2 (the same with -DVELOCITYFIELD, the reference's
+#     velocity-field build: gravity2.h cells, the Doppler redshift, the particle deposit)
 #     and the reference's own create_octree executable.
 #  -ffp-contract=off keeps the x86 and Arm builds free of FMA contraction, as
 #  the reference's x86-64 build is.
@@ -33,6 +35,9 @@ FLAGS=(-O3 -std=c++17 -ffp-contract=off -DEXTENT=4 -DSIZEOFOCTREE=48 -DIOGROUPSI
 pids=()
 for o in 0 1 2; do
     "$CXX" "${FLAGS[@]}" -DORDER=$o -fPIC -shared "$HERE/ref_harness.cpp" -o "$OUT/libref_o$o.so" -lpthread &
+    pids+=($!)
+    "$CXX" "${FLAGS[@]}" -DORDER=$o -DVELOCITYFIELD -fPIC -shared "$HERE/ref_harness.cpp" \
+        -o "$OUT/libref_vel_o$o.so" -lpthread &
     pids+=($!)
 done
 "$CXX" "${FLAGS[@]}" -DORDER=1 -include "$OUT/patched/magrathea/simplehyperoctree.h" \

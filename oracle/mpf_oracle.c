@@ -138,10 +138,27 @@ int64_t mpfo_locate(const mpfo_tree* T, double x, double y, double z)
 
 /* SimpleHyperOctree::ngp (simplehyperoctree.h:1396-1401): the record of the
    cell found for the position's level-32 key, or the empty record */
-void mpfo_ngp(const mpfo_tree* T, double x, double y, double z, float* res)
+/* A cell's record as the gathers read it: the 7 fields, then the velocity
+   slots of a velocity-field octree (gravity2.h:45; zeros without one). */
+#define NF 10
+static inline void load_rec(const mpfo_tree* T, int64_t i, float* f)
+{
+    for (int k = 0; k < 7; ++k) f[k] = T->fields[7 * i + k];
+    for (int k = 0; k < 3; ++k) f[7 + k] = T->vel ? T->vel->v[3 * i + k] : 0.0f;
+}
+
+static void ngp10(const mpfo_tree* T, double x, double y, double z, float* res)
 {
     const int64_t i = find(T, key_compute(32, x, y, z));
-    for (int k = 0; k < 7; ++k) res[k] = (i >= 0) ? T->fields[7 * i + k] : 0.0f;
+    if (i >= 0) load_rec(T, i, res);
+    else for (int k = 0; k < NF; ++k) res[k] = 0.0f;
+}
+
+void mpfo_ngp(const mpfo_tree* T, double x, double y, double z, float* res)
+{
+    float r[NF];
+    ngp10(T, x, y, z, r);
+    memcpy(res, r, 7 * sizeof(float));
 }
 
 void mpfo_key_compute(unsigned level, double x, double y, double z, uint64_t* out)
@@ -153,20 +170,25 @@ void mpfo_key_compute(unsigned level, double x, double y, double z, uint64_t* ou
 
 unsigned mpfo_key_level(uint64_t hi, uint64_t lo) { return key_level(mk(hi, lo)); }
 
-static inline void mac7(float* acc, const float* f, double w)
+/* the reference's multiply-accumulate of every arithmetic member
+   (simplehyperoctree.h:1887-1910): float += float * double; the velocity
+   slots only when the octree has them */
+static inline void mac(const mpfo_tree* T, float* acc, const float* f, double w)
 {
-    for (int k = 0; k < 7; ++k) acc[k] = (float)((double)acc[k] + (double)f[k] * w);
+    const int nf = T->vel ? NF : 7;
+    for (int k = 0; k < nf; ++k) acc[k] = (float)((double)acc[k] + (double)f[k] * w);
 }
 
-static inline void zero7(float* a) { for (int k = 0; k < 7; ++k) a[k] = 0.0f; }
+static inline void zero7(float* a) { for (int k = 0; k < NF; ++k) a[k] = 0.0f; }
 
+/* data == empty: every member zero, the velocity slots included */
 static inline int empty7(const float* a)
 {
-    for (int k = 0; k < 7; ++k) if (a[k] != 0.0f) return 0;
+    for (int k = 0; k < NF; ++k) if (a[k] != 0.0f) return 0;
     return 1;
 }
 
-void mpfo_cic(const mpfo_tree* T, double x, double y, double z, float* res)
+static void cic10(const mpfo_tree* T, double x, double y, double z, float* res)
 {
     const double pt[3] = {x, y, z};
     u128 ekey = key_compute(32, x, y, z);
@@ -196,7 +218,9 @@ void mpfo_cic(const mpfo_tree* T, double x, double y, double z, float* res)
                 if (fi >= 0) {
                     const unsigned fl = key_level(tkey(T, fi));
                     if (fl < lvl) lvl = fl;
-                    mac7(res, T->fields + 7 * fi, w);
+                    float f[NF];
+                    load_rec(T, fi, f);
+                    mac(T, res, f, w);
                 } else {
                     zero7(res);
                     break;
@@ -212,9 +236,16 @@ void mpfo_cic(const mpfo_tree* T, double x, double y, double z, float* res)
     } while (lvl < ilvl);
 }
 
+void mpfo_cic(const mpfo_tree* T, double x, double y, double z, float* res)
+{
+    float r[NF];
+    cic10(T, x, y, z, r);
+    memcpy(res, r, 7 * sizeof(float));
+}
+
 typedef struct {
     u128 key[27];
-    float f[27][7];
+    float f[27][NF];
 } tsc_cache;
 
 static inline void cache_init(tsc_cache* c) { memset(c, 0, sizeof(*c)); }
@@ -234,7 +265,7 @@ static void tsc_cached(const mpfo_tree* T, tsc_cache* cache, double x, double y,
     double half = (double)OCT_EXTENT / 1.0 * key_extent1(idx) / 2.0;
     zero7(res);
     if (x == 0.0 && y == 0.0 && z == 0.0) {
-        mpfo_cic(T, 0., 0., 0., res);
+        cic10(T, 0., 0., 0., res);
         return;
     }
     tsc_cache tmp;
@@ -249,7 +280,7 @@ static void tsc_cached(const mpfo_tree* T, tsc_cache* cache, double x, double y,
                         double dist[3];
                         for (int d = 0; d < 3; ++d) dist[d] = fabs((key_center(cache->key[ic], d) - pt[d]) / tw);
                         const double w = tsc_w(abs(ix), dist[0]) * tsc_w(abs(iy), dist[1]) * tsc_w(abs(iz), dist[2]);
-                        mac7(res, cache->f[ic], w);
+                        mac(T, res, cache->f[ic], w);
                         ++ic;
                     }
             return;
@@ -262,14 +293,14 @@ static void tsc_cached(const mpfo_tree* T, tsc_cache* cache, double x, double y,
                         const int64_t fi = find(T, ekey);
                         if (fi >= 0) {
                             tmp.key[ic] = tkey(T, fi);
-                            memcpy(tmp.f[ic], T->fields + 7 * fi, sizeof(tmp.f[ic]));
+                            load_rec(T, fi, tmp.f[ic]);
                             double dist[3];
                             for (int d = 0; d < 3; ++d) dist[d] = fabs((key_center(ekey, d) - pt[d]) / tw);
                             const double w = tsc_w(abs(ix), dist[0]) * tsc_w(abs(iy), dist[1]) * tsc_w(abs(iz), dist[2]);
                             const unsigned fl = key_level(tmp.key[ic]);
                             if (fl < lvl) lvl = fl;
                             if (lvl < ilvl) { zero7(res); stop = 1; }
-                            else { mac7(res, tmp.f[ic], w); ++ic; }
+                            else { mac(T, res, tmp.f[ic], w); ++ic; }
                         } else {
                             zero7(res);
                             stop = 1;
@@ -290,7 +321,9 @@ void mpfo_tsc(const mpfo_tree* T, double x, double y, double z, float* out)
 {
     tsc_cache c;
     cache_init(&c);
-    tsc_cached(T, &c, x, y, z, out);
+    float r[NF];
+    tsc_cached(T, &c, x, y, z, r);
+    memcpy(out, r, 7 * sizeof(float));
 }
 
 double mpfo_interpolate(double x0, const double* x, const double* y, int64_t n)
@@ -328,19 +361,19 @@ static inline void gather(ctx_t* c, double x, double y, double z, float* d)
         d[5] = 1.0f;   /* a, the record order rho phi dx dy dz a dt */
         return;
     }
-    if (c->order == 0) mpfo_ngp(c->T, x, y, z, d);
-    else if (c->order == 1) mpfo_cic(c->T, x, y, z, d);
+    if (c->order == 0) ngp10(c->T, x, y, z, d);
+    else if (c->order == 1) cic10(c->T, x, y, z, d);
     else tsc_cached(c->T, &c->cache, x, y, z, d);
 }
 
-/* field indices in the 7-float record */
-enum { FRHO = 0, FPHI, FDX, FDY, FDZ, FA, FDT };
+/* field indices in the record: the 7 fields, then the velocity slots */
+enum { FRHO = 0, FPHI, FDX, FDY, FDZ, FA, FDT, FVX, FVY, FVZ };
 
 static void dphotondl(ctx_t* c, double* out, const double* in)
 {
     const double two = 2.0;
     const double c2 = C_LIGHT * C_LIGHT;
-    float d[7];
+    float d[NF];
     gather(c, in[PX], in[PY], in[PZ], d);
     const double dphidl = (double)d[FDT] * in[PK0] + ((double)d[FDX] * in[PK1] + (double)d[FDY] * in[PK2] + (double)d[FDZ] * in[PK3]);
     const double dadt = mpfo_interpolate(in[PT], c->C->t, c->C->dadt, c->C->n);
@@ -391,7 +424,7 @@ static void integrate(ctx_t* c, traj_t* tr, unsigned nsteps, int stop_kind, doub
     const double cl = C_LIGHT, c2 = C_LIGHT * C_LIGHT;
     const double mn = 0.0 - (double)OCT_EXTENT / two, mx = 0.0 + (double)OCT_EXTENT / two;
     const double scale = c->length;
-    float data[7];
+    float data[NF];
     double* b = tr->p + MPFO_PHOTON * (tr->n - 1);
     gather(c, b[PX], b[PY], b[PZ], data);
     const double norm = sqrt((c2 * (one + two * ((double)data[FPHI] / c2)) * b[PK0] * b[PK0]) /
@@ -424,6 +457,11 @@ static void integrate(ctx_t* c, traj_t* tr, unsigned nsteps, int stop_kind, doub
     double ratio = b[PA] * b[PA] * (scale / cl) / nsteps;
     double dl = (loc >= 0 ? key_extent4(tkey(c->T, loc)) : 0.0) * ratio;
     const double a0 = b[PA];
+    /* velocity-field octree: the observer velocity along trajectory[0]'s
+       direction (integrator.h:707-708) */
+    const mpfo_velocity* vf = c->T->vel;
+    const double* t0 = tr->p;
+    const double v0n = vf ? (vf->vobs[0] * t0[PK1] + vf->vobs[1] * t0[PK2] + vf->vobs[2] * t0[PK3]) / (cl * t0[PK0]) : 0.0;
     const double phi0c2 = b[PPHI] / c2;
     double photon[MPFO_PHOTON];
     memset(photon, 0, sizeof(photon));
@@ -467,7 +505,12 @@ static void integrate(ctx_t* c, traj_t* tr, unsigned nsteps, int stop_kind, doub
         photon[PLAMBDA] += dl;
         photon[PS] += sqrt((photon[PX] - b[PX]) * (photon[PX] - b[PX]) + (photon[PY] - b[PY]) * (photon[PY] - b[PY]) +
                            (photon[PZ] - b[PZ]) * (photon[PZ] - b[PZ]));
-        photon[PZRED] = a0 / photon[PA] * (one + phi0c2 - photon[PPHI] / c2) - one;
+        if (vf) /* integrator.h:765-767 */
+            photon[PZRED] = a0 / photon[PA] * (one + phi0c2 - photon[PPHI] / c2 + photon[PISW] +
+                                               (data[FVX] * photon[PK1] + data[FVY] * photon[PK2] + data[FVZ] * photon[PK3]) /
+                                                   (cl * photon[PK0]) - v0n) - one;
+        else
+            photon[PZRED] = a0 / photon[PA] * (one + phi0c2 - photon[PPHI] / c2) - one;
         if (!empty7(data)) {
             ratio = photon[PA] * photon[PA] * (scale / cl) / nsteps;
             dl = (loc >= 0 ? key_extent4(tkey(c->T, loc)) : 0.0) * ratio;
@@ -531,7 +574,7 @@ static void jacobian(ctx_t* c, const traj_t* tr, int nd, const double* dist, dou
         const double cp = cos(phi), sp = sin(phi), ct = cos(theta), st = sin(theta);
         const double s2p = sin(2 * phi), s2t = sin(2 * theta);
         const double dl = pow(2, -(P[PLEVEL] - 1 - LEVEL_SHIFT));
-        float xm[7], xp[7], ym[7], yp[7], zm[7], zp[7];
+        float xm[NF], xp[NF], ym[NF], yp[NF], zm[NF], zp[NF];
         tsc_cached(c->T, &cache, x - 0.5 * dl, y, z, xm);
         tsc_cached(c->T, &cache, x + 0.5 * dl, y, z, xp);
         tsc_cached(c->T, &cache, x, y - 0.5 * dl, z, ym);
@@ -1415,3 +1458,86 @@ void mpfo_batch_locate(const mpfo_tree* T, int64_t n, const double* xyz, int64_t
 void mpfo_batch_cic(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads) { gbatch(T, n, xyz, out, 1, nthreads); }
 void mpfo_batch_tsc(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads) { gbatch(T, n, xyz, out, 2, nthreads); }
 void mpfo_batch_ngp(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads) { gbatch(T, n, xyz, out, 3, nthreads); }
+
+/* ---------------------------------------------------------------------- */
+/* velocity field deposit (hmaps.h:439-550, hmaps.cpp:395-441)             */
+/* ---------------------------------------------------------------------- */
+/* The exact key's position in the sorted keys, or -1 (upper_bound, then
+   the element before it compared for equality: hmaps.h:468-470). */
+static inline int64_t find_exact(const mpfo_tree* T, u128 K)
+{
+    const int64_t m = upper(T, K);
+    const int64_t j = m - (m > 0);
+    return (T->n > 0 && tkey(T, j) == K) ? j : -1;
+}
+
+static inline double tsc_w(int a, double d);
+
+int mpfo_velocity_deposit(const mpfo_tree* T, float* fields, float* v, int scheme, int64_t npart, const float* pos,
+                          const float* pv, int flags)
+{
+    if (!T || T->n <= 0 || (scheme != 1 && scheme != 2)) return -1;
+    unsigned lmin = 64, lmax = 0;
+    for (int64_t i = 0; i < T->n; ++i) {
+        const unsigned l = key_level(tkey(T, i));
+        if (l < lmin) lmin = l;
+        if (l > lmax) lmax = l;
+    }
+    if (flags & 1) {
+        for (int64_t i = 0; i < T->n; ++i) {
+            fields[7 * i] = 0.0f;
+            v[3 * i] = v[3 * i + 1] = v[3 * i + 2] = 0.0f;
+        }
+    }
+    for (unsigned L = lmin; L <= lmax; ++L) {
+        const double half = 0.5 * OCT_EXTENT / pow(2, L);
+        const double tw = 2 * half;
+        const double invext = 1 / (OCT_EXTENT / pow(2, L));
+        for (int64_t i = 0; i < npart; ++i) {
+            const float* p = pos + 3 * i;
+            if (scheme == 1) {
+                for (int iz = -1; iz <= 1; iz += 2)
+                    for (int iy = -1; iy <= 1; iy += 2)
+                        for (int ix = -1; ix <= 1; ix += 2) {
+                            const u128 K = key_compute(L, p[0] + half * ix, p[1] + half * iy, p[2] + half * iz);
+                            const int64_t j = find_exact(T, K);
+                            if (j < 0) continue;
+                            const double w = (1 - fabs(p[0] - key_center(K, 0)) * invext) *
+                                             (1 - fabs(p[1] - key_center(K, 1)) * invext) *
+                                             (1 - fabs(p[2] - key_center(K, 2)) * invext);
+                            fields[7 * j] += w;
+                            for (int d = 0; d < 3; ++d) v[3 * j + d] += pv[3 * i + d] * w;
+                        }
+            } else {
+                for (int iz = -1; iz <= 1; ++iz)
+                    for (int iy = -1; iy <= 1; ++iy)
+                        for (int ix = -1; ix <= 1; ++ix) {
+                            const u128 K = key_compute(L, p[0] + tw * ix, p[1] + tw * iy, p[2] + tw * iz);
+                            const int64_t j = find_exact(T, K);
+                            if (j < 0) continue;
+                            double dist[3];
+                            for (int d = 0; d < 3; ++d) dist[d] = fabs((key_center(tkey(T, j), d) - p[d]) / tw);
+                            const double w = tsc_w(abs(ix), dist[0]) * tsc_w(abs(iy), dist[1]) * tsc_w(abs(iz), dist[2]);
+                            fields[7 * j] += w;
+                            for (int d = 0; d < 3; ++d) v[3 * j + d] += pv[3 * i + d] * w;
+                        }
+            }
+        }
+    }
+    if (flags & 2) {
+        for (int64_t i = 0; i < T->n; ++i) {
+            double mass = fields[7 * i];
+            mass = mass + (mass == 0);
+            for (int d = 0; d < 3; ++d) v[3 * i + d] /= mass;
+        }
+        for (unsigned L = lmin + 1; L <= lmax; ++L)
+            for (int64_t i = 0; i < T->n; ++i) {
+                const u128 k = tkey(T, i);
+                if (key_level(k) != L || isnormal(fields[7 * i])) continue;
+                const int64_t j = find_exact(T, key_parent(k));
+                if (j < 0) continue;
+                for (int d = 0; d < 3; ++d) v[3 * i + d] = v[3 * j + d];
+            }
+    }
+    return 0;
+}

@@ -19,12 +19,23 @@
 extern "C" {
 #endif
 
+/* Velocity field of the octree (the reference built with -DVELOCITYFIELD):
+ * per-cell velocities (gravity2.h:45) and the observer velocity the rays are
+ * traced with (hmaps.h:80-84). */
+typedef struct {
+    const float* v;         /* n x 3 */
+    double vobs[3];
+} mpfo_velocity;
+
 /* Sorted octree: n keys (128-bit, as hi/lo pairs) and 7 float fields per cell
- * in the order rho, phi, dphidx, dphidy, dphidz, a, dphidt. */
+ * in the order rho, phi, dphidx, dphidy, dphidz, a, dphidt; vel: NULL, or a
+ * velocity field (the gathers then carry it, and every redshift takes the
+ * ISW, Doppler and observer terms, integrator.h:765-767). */
 typedef struct {
     int64_t n;
     const uint64_t* keys;   /* n x 2: hi, lo */
     const float* fields;    /* n x 7 */
+    const mpfo_velocity* vel;
 } mpfo_tree;
 
 typedef struct {
@@ -112,6 +123,16 @@ int64_t mpfo_propagate_bundle(const mpfo_tree* T, const mpfo_cosmo* C, int order
 int mpfo_bundle(const mpfo_tree* T, const mpfo_cosmo* C, int order, double length, unsigned nsteps, int stop_kind,
                 int64_t n, const double* launch, int np, const double* planes, int plane_sachs, int stop_bundle,
                 double openingmin, double* plane_out, double* jac_out, int nthreads);
+
+/* Hmaps::CreateOctreeVelocityWithCIC (scheme 1, hmaps.h:439-485) / WithTSC
+ * (scheme 2, :501-550) on one thread: npart particles (pos, vel: npart x 3
+ * floats) deposited at every level lmin..lmax on the cells with the exact key
+ * of each vertex; rho (fields[7i], n x 7, the tree's keys) and v (n x 3)
+ * accumulate in float.  flags: 1 = zero rho and v first (hmaps.cpp:395-396),
+ * 2 = then v /= rho (zero read as 1) and, level by level, cells whose rho is
+ * not normal take the parent's v (hmaps.cpp:424-441). */
+int mpfo_velocity_deposit(const mpfo_tree* T, float* fields, float* v, int scheme, int64_t npart, const float* pos,
+                          const float* pv, int flags);
 
 void mpfo_batch_locate(const mpfo_tree* T, int64_t n, const double* xyz, int64_t* out, int nthreads);
 void mpfo_batch_cic(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads);

@@ -37,8 +37,12 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+class _Velocity(C.Structure):
+    _fields_ = [("v", _p), ("vobs", _d * 3)]
+
+
 class _Tree(C.Structure):
-    _fields_ = [("n", _i64), ("keys", _p), ("fields", _p)]
+    _fields_ = [("n", _i64), ("keys", _p), ("fields", _p), ("vel", C.POINTER(_Velocity))]
 
 
 class _Cosmo(C.Structure):
@@ -75,6 +79,8 @@ def lib():
         L.mpfo_catalogue.restype = C.c_int
         L.mpfo_catalogue.argtypes = [_p, _p, C.c_int, _d, C.c_uint, _i64, _p, _p, _p, _d, _d, _d, C.c_int, _p,
                                      C.c_int]
+        L.mpfo_velocity_deposit.restype = C.c_int
+        L.mpfo_velocity_deposit.argtypes = [_p, _p, _p, C.c_int, _i64, _p, _p, C.c_int]
         for f in ("mpfo_batch_locate", "mpfo_batch_cic", "mpfo_batch_tsc", "mpfo_batch_ngp"):
             getattr(L, f).argtypes = [_p, _i64, _p, _p, C.c_int]
         _lib = L
@@ -103,6 +109,41 @@ class Oracle:
         self.length = float(length)
         self.nthreads = nthreads or (os.cpu_count() or 1)
         self.L = lib()
+        self.vel = None
+
+    # -- velocity field (the reference's -DVELOCITYFIELD build) --
+    def set_velocity(self, v3, vobs=(0.0, 0.0, 0.0)):
+        """Trace as the velocity-field build: per-cell velocities v3 (n x 3)
+        and the observer velocity; v3 = None goes back to the plain build."""
+        if v3 is None:
+            self.vel = None
+            self.tree.vel = C.POINTER(_Velocity)()
+            return
+        self.vel = np.ascontiguousarray(v3, dtype=np.float32).reshape(-1, 3)
+        self._velstruct = _Velocity(_ptr(self.vel), (_d * 3)(*[float(x) for x in vobs]))
+        self.tree.vel = C.pointer(self._velstruct)
+
+    def set_vobs(self, vobs):
+        if self.vel is None:
+            raise ValueError("no velocity field")
+        for k in range(3):
+            self._velstruct.vobs[k] = float(vobs[k])
+
+    def deposit_velocity(self, pos, vel, scheme="cic", begin=True, finish=True):
+        """Hmaps::CreateOctreeVelocityWithCIC / WithTSC on one thread, with the
+        zeroed masses before and the normalisation and parent fill after; the
+        oracle's rho and velocity field change in place."""
+        if self.vel is None:
+            self.set_velocity(np.zeros((self.keys.shape[0], 3), dtype=np.float32))
+        p = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        v = np.ascontiguousarray(vel, dtype=np.float32).reshape(-1, 3)
+        flags = (1 if begin else 0) | (2 if finish else 0)
+        sch = {"cic": 1, "tsc": 2}[scheme] if isinstance(scheme, str) else int(scheme)
+        rc = self.L.mpfo_velocity_deposit(C.byref(self.tree), _ptr(self.fields), _ptr(self.vel), sch, p.shape[0],
+                                          _ptr(p), _ptr(v), flags)
+        if rc != 0:
+            raise ValueError("oracle deposit failed: %d" % rc)
+        return self.vel, self.fields[:, 0]
 
     def locate(self, xyz):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64)

@@ -75,7 +75,9 @@ using point = std::array<real, 3>;
 #include "input.h"
 #include "integrator.h"
 #include "lensing.h"
+#ifndef VELOCITYFIELD
 #include "gravity.h"
+#endif
 #include "miscellaneous.h"
 #include "hmaps.h"
 // catalogues.h defines a parameters_t struct and a global `parameters` of
@@ -96,6 +98,9 @@ using Cosmo = std::array<std::vector<double>, 4>;
 static Oct g_octree;
 static Cosmo g_cosmo;
 static double g_length = 0.0;
+// observer velocity of ref_integrate / ref_trajectory / ref_fillmap (read by
+// the velocity-field build only, integrator.h:537-538, 707-708)
+static std::array<double, 3> g_vobs{0, 0, 0};
 
 struct CosmoParams { std::string celldir, paramfile, evolfile; double mpc = 3.08568E22; };
 
@@ -140,10 +145,30 @@ extern "C" {
 int ref_extent() { return EXTENT; }
 int ref_order() { return ORDER; }
 
+int ref_velocityfield()
+{
+#ifdef VELOCITYFIELD
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+void ref_set_vobs(double vx, double vy, double vz) { g_vobs = {vx, vy, vz}; }
+
 int64_t ref_load(const char* path)
 {
     g_octree.fullclear();
+#ifdef VELOCITYFIELD
+    // the reference's cone loader of the velocity-field build: Input::load of
+    // the 48-byte records into the wider cells, then the field remap
+    // (miscellaneous.h:422-449)
+    std::vector<std::string> files{std::string(path)};
+    Miscellaneous::loadOctree(0u, g_octree, files);
+    if (g_octree.size() == 0) return -1;
+#else
     if (!Input::load(g_octree, std::string(path))) return -1;
+#endif
     return (int64_t)g_octree.size();
 }
 
@@ -271,7 +296,7 @@ void ref_integrate(int64_t n, const double* launch, const char* stop, double sto
                    int ndist, const double* dists, int64_t* steps, double* final28, double* jac, int nthreads)
 {
     const std::string stop_s(stop);
-    const std::array<double, 3> v0{0, 0, 0};
+    const std::array<double, 3> v0 = g_vobs;
     run_threads(n, nthreads, [&](int64_t i) {
         const double* L = launch + 6 * i;
         Traj traj;
@@ -293,7 +318,7 @@ void ref_integrate(int64_t n, const double* launch, const char* stop, double sto
 // Whole trajectory of one ray (28 doubles per step); returns its size.
 int64_t ref_trajectory(const double* L, const char* stop, double stop_ref, unsigned nsteps, double* out, int64_t cap)
 {
-    const std::array<double, 3> v0{0, 0, 0};
+    const std::array<double, 3> v0 = g_vobs;
     Traj traj;
     traj.append(Integrator::launch(L[0], L[1], L[2], L[3], L[4], L[5]));
     Integrator::integrate(traj, std::string(stop), stop_ref, g_cosmo, g_octree, v0, g_length, nsteps);
@@ -392,7 +417,7 @@ int ref_fillmap_jac(long nside, int nz, const double* zvals, const char* stop_ra
     long maxpix = 0;
     for (long p : pix) maxpix = std::max(maxpix, p);
     std::vector<std::vector<float>> map((size_t)nmaps * nz, std::vector<float>((size_t)maxpix + 1, 0.f));
-    const std::array<double, 3> v0{0, 0, 0};
+    const std::array<double, 3> v0 = g_vobs;   // the map driver's vobs (hmaps.cpp:364, 450)
     const point observer{{0., 0., 0.}};
     Hmaps::FillMap(parameters, map_components, index_components, (unsigned)npixels, 0u, g_octree, v0, map, nmaps, pix,
                    g_cosmo, observer, g_length, interpRefvec, rhomo, thomo, lambdahomo, redshifthomo, ahomo);
@@ -569,5 +594,79 @@ int64_t ref_build_cone(const char* cellfile, const double* cone7, const double* 
     if (amin_out) *amin_out = amin;
     return m;
 }
+
+
+#ifdef VELOCITYFIELD
+// The velocity-field map driver's particle stage (hmaps.cpp:395-441).
+// flags 1: every cell's rho and velocity zeroed (hmaps.cpp:396); then the
+// reference's Hmaps::CreateOctreeVelocityWithCIC (scheme 1) / WithTSC
+// (scheme 2) over the particles, fed a few particles per call so that its
+// Utility::parallelize runs them all on the calling thread, in order (the
+// reference's own threads add to shared cells without atomics); flags 2:
+// the mass normalisation and the parent fill of hmaps.cpp:424-441, written
+// out here because the reference has them inline in main().
+int ref_velocity_deposit(int scheme, int64_t n, const float* pos, const float* vel, int flags)
+{
+    if (flags & 1) {
+        for (size_t i = 0; i < g_octree.size(); ++i) {
+            std::get<1>(g_octree[i]).rho() = 0;
+            std::get<1>(g_octree[i]).vxyz() = std::array<float, 3>();
+        }
+    }
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int64_t chunk = (hw > 1) ? (int64_t)hw - 1 : 1;
+    for (int64_t lo = 0; lo < n; lo += chunk) {
+        const int64_t m = std::min<int64_t>(chunk, n - lo);
+        std::vector<float> p(pos + 3 * lo, pos + 3 * (lo + m)), v(vel + 3 * lo, vel + 3 * (lo + m));
+        if (scheme == 1) Hmaps::CreateOctreeVelocityWithCIC(g_octree, p, v);
+        else if (scheme == 2) Hmaps::CreateOctreeVelocityWithTSC(g_octree, p, v);
+        else return -1;
+    }
+    if (flags & 2) {
+        unsigned lmin = 1000, lmax = 0;
+        for (size_t i = 0; i < g_octree.size(); ++i) {
+            lmin = std::min(lmin, std::get<0>(g_octree[i]).level());
+            lmax = std::max(lmax, std::get<0>(g_octree[i]).level());
+        }
+        for (size_t i = 0; i < g_octree.size(); ++i) {
+            auto& d = std::get<1>(g_octree[i]);
+            double mass = d.rho();
+            mass = mass + (mass == 0);
+            d.vx() /= mass;
+            d.vy() /= mass;
+            d.vz() /= mass;
+        }
+        for (unsigned l = lmin + 1; l <= lmax; ++l)
+            for (size_t i = 0; i < g_octree.size(); ++i) {
+                if (std::get<0>(g_octree[i]).level() != l || std::isnormal(std::get<1>(g_octree[i]).rho())) continue;
+                const auto par = g_octree.find(std::get<0>(g_octree[i]).parent());
+                if (par == g_octree.end()) continue;
+                const auto& pd = std::get<1>(*par);
+                std::get<1>(g_octree[i]).vxyz() = {pd.vx(), pd.vy(), pd.vz()};
+            }
+    }
+    return 0;
+}
+
+// the cells' velocities (n x 3) and rho (n)
+void ref_velocity_get(float* v3, float* rho)
+{
+    for (size_t i = 0; i < g_octree.size(); ++i) {
+        const auto& d = std::get<1>(g_octree[i]);
+        v3[3 * i] = d.vx(); v3[3 * i + 1] = d.vy(); v3[3 * i + 2] = d.vz();
+        rho[i] = d.rho();
+    }
+}
+
+// sets the cells' velocities (and rho, if given)
+void ref_velocity_set(const float* v3, const float* rho)
+{
+    for (size_t i = 0; i < g_octree.size(); ++i) {
+        auto& d = std::get<1>(g_octree[i]);
+        d.vxyz() = {v3[3 * i], v3[3 * i + 1], v3[3 * i + 2]};
+        if (rho) d.rho() = rho[i];
+    }
+}
+#endif
 
 }  // extern "C"

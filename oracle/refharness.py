@@ -1,4 +1,5 @@
-"""ctypes wrapper of the reference harness (oracle/_ref/libref_o{1,2}.so).
+"""ctypes wrapper of the reference harness (oracle/_ref/libref_o{0,1,2}.so, and
+libref_vel_o{0,1,2}.so: the reference's velocity-field build, -DVELOCITYFIELD).
 
 Test infrastructure only: used to generate golden fixtures and to pin the
 C restatement (oracle/mpf_oracle.c) to the reference in this container.  The
@@ -23,13 +24,17 @@ def _ptr(a):
     return a.ctypes.data_as(_p)
 
 
-def available(order: int = 2) -> bool:
-    return os.path.exists(os.path.join(HERE, "_ref", "libref_o%d.so" % order))
+def _name(order: int, velocity: bool) -> str:
+    return os.path.join(HERE, "_ref", ("libref_vel_o%d.so" if velocity else "libref_o%d.so") % order)
 
 
-def lib(order: int = 2):
-    if order not in _LIBS:
-        path = os.path.join(HERE, "_ref", "libref_o%d.so" % order)
+def available(order: int = 2, velocity: bool = False) -> bool:
+    return os.path.exists(_name(order, velocity))
+
+
+def lib(order: int = 2, velocity: bool = False):
+    if (order, velocity) not in _LIBS:
+        path = _name(order, velocity)
         L = C.CDLL(path, mode=C.RTLD_LOCAL)
         L.ref_load.restype = _i64
         L.ref_load.argtypes = [C.c_char_p]
@@ -75,15 +80,23 @@ def lib(order: int = 2):
         L.ref_build_cone.restype = _i64
         L.ref_build_cone.argtypes = [C.c_char_p, _p, _p, _p, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, _d, _d, _d,
                                      _d, _p, _i64, _p]
-        _LIBS[order] = L
-    return _LIBS[order]
+        L.ref_velocityfield.restype = C.c_int
+        L.ref_set_vobs.argtypes = [_d, _d, _d]
+        if velocity:
+            L.ref_velocity_deposit.restype = C.c_int
+            L.ref_velocity_deposit.argtypes = [C.c_int, _i64, _p, _p, C.c_int]
+            L.ref_velocity_get.argtypes = [_p, _p]
+            L.ref_velocity_set.argtypes = [_p, _p]
+        _LIBS[(order, velocity)] = L
+    return _LIBS[(order, velocity)]
 
 
 class Reference:
     """The reference's own octree / integrator / map driver, one per ORDER."""
 
-    def __init__(self, order: int = 2, nthreads: int = 0):
-        self.L = lib(order)
+    def __init__(self, order: int = 2, nthreads: int = 0, velocity: bool = False):
+        self.L = lib(order, velocity)
+        self.velocity_build = velocity
         self.order = order
         self.nthreads = nthreads or (os.cpu_count() or 1)
 
@@ -92,6 +105,31 @@ class Reference:
         if n < 0:
             raise IOError("reference could not load %s" % path)
         return n
+
+    # -- the velocity-field build --
+    def set_vobs(self, vobs):
+        self.L.ref_set_vobs(*[float(v) for v in vobs])
+
+    def deposit_velocity(self, pos, vel, scheme="cic", begin=True, finish=True):
+        """The map driver's particle stage (hmaps.cpp:395-441) on one thread."""
+        p = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        v = np.ascontiguousarray(vel, dtype=np.float32).reshape(-1, 3)
+        flags = (1 if begin else 0) | (2 if finish else 0)
+        rc = self.L.ref_velocity_deposit({"cic": 1, "tsc": 2}[scheme], p.shape[0], _ptr(p), _ptr(v), flags)
+        if rc != 0:
+            raise RuntimeError("ref_velocity_deposit failed: %d" % rc)
+
+    def velocity(self):
+        n = self.L.ref_size()
+        v = np.zeros((n, 3), dtype=np.float32)
+        r = np.zeros(n, dtype=np.float32)
+        self.L.ref_velocity_get(_ptr(v), _ptr(r))
+        return v, r
+
+    def set_velocity(self, v3, rho=None):
+        v = np.ascontiguousarray(v3, dtype=np.float32)
+        r = None if rho is None else np.ascontiguousarray(rho, dtype=np.float32)
+        self.L.ref_velocity_set(_ptr(v), _ptr(r) if r is not None else None)
 
     def keys(self):
         n = self.L.ref_size()

@@ -13,7 +13,8 @@ counts and final photon records (Integrator::integrate), FillMap maps, and
 catalogue rows (Catalogues::iterateNewtonMethod through relCat's per-source
 setup) for seeded sources at three accuracies, with and without a rotation,
 and FillMap maps with the bundle Jacobian (Lensing::dbetadtheta) for two
-screen / stop_bundle choices.
+screen / stop_bundle choices; and the reference's velocity-field build
+(-DVELOCITYFIELD): particle deposits and rays traced with the Doppler term.
 """
 from __future__ import annotations
 
@@ -381,10 +382,54 @@ def make_whole_rays():
     print("whole rays -> %s (%d KB)" % (path, os.path.getsize(path) // 1024))
 
 
+VEL_VOBS = (3e-4, -2e-4, 1e-4)         # observer velocity, in the units of the particle velocities (c)
+VEL_COMPONENTS = "lensing,dz,isw,dens,steps"
+
+
+def make_velocity():
+    """The reference's velocity-field build (-DVELOCITYFIELD) on the AMR
+    fixture's octree: seeded particles deposited with CIC and with TSC in two
+    particle files (BEGIN + first file, second file + FINISH: the map driver's
+    loop over shell files, hmaps.cpp:395-441), the cells' velocities and
+    masses, then whole rays (Integrator::integrate) and FillMap maps traced
+    with the observer velocity: ORDER = 1 on the CIC field, 2 on the TSC one."""
+    g = np.load(os.path.join(HERE, "amr.npz"))
+    rec = g["records"]
+    tmp = tempfile.mkdtemp(prefix="mpf_golden_")
+    binpath = os.path.join(tmp, "cone.bin")
+    S.write_bin(binpath, rec)
+    pos, vel = S.velocity_particles(rec, 1500, seed=5)
+    split = 900
+    zs, nsteps, nside, pix = g["zs"], int(g["nsteps"]), int(g["nside"]), g["pixels"]
+    launch = S.photon_grid(8, 2.0, 2.0)
+    out = dict(records_sha=np.array(records_sha(rec)), part_pos=pos, part_vel=vel, part_split=split,
+               vobs=np.array(VEL_VOBS), zs=zs, nsteps=nsteps, nside=nside, pixels=pix, launch=launch,
+               components=np.array(VEL_COMPONENTS))
+    for scheme, order in (("cic", 1), ("tsc", 2)):
+        R = Reference(order, velocity=True)
+        R.set_cosmology(g["cosmo_t"], g["cosmo_a"], g["cosmo_dadt"], g["cosmo_d2adt2"], float(g["cosmo_length"]))
+        R.load(binpath)
+        R.deposit_velocity(pos[:split], vel[:split], scheme, True, False)
+        R.deposit_velocity(pos[split:], vel[split:], scheme, False, True)
+        v, rho = R.velocity()
+        out["ref_vel_" + scheme], out["ref_rho_" + scheme] = v, rho
+        R.set_vobs(VEL_VOBS)
+        steps, final, _ = R.integrate(launch, "redshift", float(zs[-1]), nsteps)
+        out["ref_steps_o%d" % order], out["ref_final_o%d" % order] = steps, final
+        out["ref_maps_o%d" % order] = R.fillmap(nside, zs, pix, "redshift", VEL_COMPONENTS, nsteps)
+        print("velocity %s: %d of %d cells without mass, %.0f steps per ray" % (scheme, int((rho == 0).sum()),
+                                                                                 rho.shape[0], steps.mean()))
+    path = os.path.join(HERE, "velocity.npz")
+    np.savez_compressed(path, **out)
+    print("velocity -> %s (%d KB)" % (path, os.path.getsize(path) // 1024))
+
+
 if __name__ == "__main__":
-    names = sys.argv[1:] or list(CASES) + ["rays", "cells", "whole_rays"]
+    names = sys.argv[1:] or list(CASES) + ["rays", "cells", "whole_rays", "velocity"]
     for name in names:
-        if name == "whole_rays":
+        if name == "velocity":
+            make_velocity()
+        elif name == "whole_rays":
             make_whole_rays()
         elif name == "rays":
             make_rays()
