@@ -710,10 +710,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true",
                     help="skip the surrogate-vs-plain comparison of the default line")
-    ap.add_argument("--mode", default="propagate", choices=["propagate", "catalogue", "surrogate", "maps"],
+    ap.add_argument("--mode", default="propagate", choices=["propagate", "catalogue", "surrogate", "maps", "velocity"],
                     help="propagate = the headline ray-tracing benchmark; catalogue = the Newton root-finder; "
                          "surrogate = the learned field in the RK4 stages against the plain octree; maps = HEALPix "
-                         "lensing maps of one full-sky cone at nside 4096")
+                         "lensing maps of one full-sky cone at nside 4096; velocity = the velocity-field "
+                         "deposit and the Doppler-redshift trace")
+    ap.add_argument("--particles", type=int, default=1 << 24, help="particles of the velocity-field deposit")
     ap.add_argument("--surrogate-samples", type=float, default=50e6, help="training samples of the surrogate")
     ap.add_argument("--sources", type=int, default=262144,
                     help="catalogue sources per step (a call's rounds wait for its slowest sources, whose up to 11 "
@@ -738,6 +740,8 @@ def main():
         return run_surrogate(args, synth, world, rank, local, dist)
     if args.mode == "maps":
         return run_maps(args, synth, world, rank, local, dist)
+    if args.mode == "velocity":
+        return run_velocity(args, synth, spec, cos, length, world, rank, local, dist)
 
     if args.impl == "reference":
         if rank != 0:
@@ -1117,3 +1121,165 @@ def run_catalogue(args, synth, spec, cos, length, world, rank, local, dist):
 
 if __name__ == "__main__":
     main()
+
+
+VEL_METRIC = "velocity-field deposit particles/s (TSC onto every level of the AMR cone octree, reference order)"
+VEL_UNIT = "particles/s"
+VEL_VOBS = (3e-4, -2e-4, 1e-4)   # observer velocity (units of c)
+
+
+def run_velocity(args, synth, spec, cos, length, world, rank, local, dist):
+    """The velocity-field build of the map driver (hmaps.cpp:360-455) on the
+    benchmark octree: one step = one complete deposit of the particles
+    (BEGIN, the particles, FINISH: Hmaps::CreateOctreeVelocityWithTSC at
+    every level, normalisation, parent fill), particles resident on the
+    device; e2e the same through mpf_velocity_deposit from host arrays.
+    Beside it, the benchmark rays traced with the deposited field and an
+    observer velocity (the Doppler redshift) against the same batches on the
+    plain octree, and parity against the C oracle: a 65 536-particle deposit
+    cell by cell and 48 rays with the Doppler term."""
+    import torch
+    torch.cuda.set_device(local)
+    pkg = importlib.import_module(PKG)
+    importlib.import_module(PKG + ".build").build()
+    capi = importlib.import_module(PKG + ".capi")
+    lib = pkg.library()
+    rec = octree_records(synth, spec)
+    tree = pkg.Octree.from_records(rec)
+    info = tree.info
+    cosmo = pkg.Cosmology(*cos)
+    npart = args.particles
+    pos, vel = synth.velocity_particles(rec, npart, seed=17)
+    dev = torch.device("cuda", local)
+    d_pos = torch.from_numpy(pos).to(dev)
+    d_vel = torch.from_numpy(vel).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+
+    def deposit():
+        tree.deposit_velocity_device(d_pos.data_ptr(), d_vel.data_ptr(), npart, "tsc", stream=sh)
+
+    for _ in range(args.warmup):
+        deposit()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            deposit()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    dep_ms = ev0.elapsed_time(ev1) / args.steps
+    value = npart / (dep_ms / 1000.0)
+    pairs = tree.deposit_pairs()
+    v_dev, rho_dev = tree.velocity()
+    # end to end: host arrays through the public call
+    e2e_t = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tree.deposit_velocity(pos, vel, "tsc")
+        e2e_t.append(time.perf_counter() - t0)
+    v2, r2 = tree.velocity()
+    deterministic = bool(np.array_equal(v2.view(np.uint32), v_dev.view(np.uint32)) and
+                         np.array_equal(r2.view(np.uint32), rho_dev.view(np.uint32)))
+    e2e_value = npart / (sum(e2e_t) / len(e2e_t))
+    peak, peak_kind = measured_peak_hbm()
+    # a scatter deposit's payload: every particle read (24 B), every contribution a
+    # read-modify-write of its cell's mass and velocity (2 x 20 B)
+    bytes_per_deposit = npart * 24 + pairs * 40
+    achieved = bytes_per_deposit / (dep_ms / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "peak_source": peak_kind,
+                "bytes_per_deposit": {"particles_x_24": npart * 24, "pairs_x_40": pairs * 40},
+                "note": "payload of a scatter deposit; the reference-order sort of the (cell, particle, vertex) "
+                        "pairs (7 radix passes of 16 B per pair) is on top of it"}
+
+    # the benchmark rays with the deposited field and an observer velocity, and on the plain octree
+    launch = ray_grid()
+    B = min(args.batch, launch.shape[0])
+    d_launch = torch.from_numpy(launch).to(dev)
+    d_steps = torch.zeros(B, dtype=torch.int64, device=dev)
+    d_planes = torch.zeros(B * capi.MPF_PLANE_FIELDS, dtype=torch.float64, device=dev)
+    d_status = torch.zeros(1, dtype=torch.int32, device=dev)
+    planes = np.array([args.zstop])
+    nb = launch.shape[0] // B
+
+    def trace(vobs):
+        p, keep = capi.make_params(length, nsteps=8, order=2, stop="redshift", planes=planes, jacobian=True,
+                                   exact=False, vobs=vobs)
+        total, ms = 0, 0.0
+        for k in range(args.warmup + args.steps):
+            off = (k % nb) * B
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            capi.check(lib.mpf_propagate_device(tree._h, cosmo._h, C.byref(p), B,
+                                                C.c_void_p(d_launch.data_ptr() + off * 48),
+                                                C.c_void_p(d_steps.data_ptr()), None, C.c_void_p(d_planes.data_ptr()),
+                                                C.c_void_p(d_status.data_ptr()), C.c_void_p(sh)))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if k >= args.warmup:
+                ms += e0.elapsed_time(e1)
+                total += int(d_steps.sum().item())
+        return total / (ms / 1000.0)
+
+    vel_rate = trace(VEL_VOBS)
+    # parity: 48 rays with the Doppler term against the C oracle on the same field
+    line_parity = {}
+    cpu = None
+    if rank == 0:
+        import oracle as oracle_mod
+        oracle_mod.build()
+        acc = importlib.import_module(PKG + ".accuracy")
+        O = oracle_mod.Oracle(rec, {"t": cos[0], "a": cos[1], "dadt": cos[2]}, length)
+        O.fields[:, 0] = rho_dev
+        O.set_velocity(v_dev, VEL_VOBS)
+        rng = np.random.default_rng(5)
+        sample = np.ascontiguousarray(launch[rng.choice(launch.shape[0], 48, replace=False)])
+        s_r, f_r, p_r = O.propagate(sample, order=2, nsteps=8, stop="redshift", planes=planes, jacobian=True)
+        s, f, pl, _ = pkg.propagate(tree, cosmo, sample, length, nsteps=8, order=2, stop="redshift", planes=planes,
+                                    jacobian=True, exact=False, vobs=VEL_VOBS)
+        rep = acc.compare(sample, s, f, pl, s_r, f_r, p_r)
+        rep["within_tolerance"] = bool(acc.within(rep))
+        line_parity["rays_with_doppler"] = rep
+        # the deposit, cell by cell, on a 65 536-particle sample (the oracle on one thread: the CPU baseline)
+        m = 65536
+        t2 = pkg.Octree.from_records(rec)
+        t2.deposit_velocity(pos[:m], vel[:m], "tsc")
+        vg, rg = t2.velocity()
+        t2.close()
+        O2 = oracle_mod.Oracle(rec, {"t": cos[0], "a": cos[1], "dadt": cos[2]}, length)
+        t0 = time.perf_counter()
+        vo, ro = O2.deposit_velocity(pos[:m], vel[:m], "tsc")
+        dt = time.perf_counter() - t0
+        same = (vg.view(np.uint32) == vo.view(np.uint32)).all(1) & (rg.view(np.uint32) == ro.view(np.uint32))
+        line_parity["deposit_sample"] = {"particles": m, "cells": int(rg.shape[0]),
+                                         "cells_bit_identical": int(same.sum()), "all_identical": bool(same.all()),
+                                         "against": "C oracle (bit-exact with the reference's -DVELOCITYFIELD build "
+                                                    "on the fixtures)"}
+        cpu = {"value": m / dt, "unit": VEL_UNIT, "cores": 1, "kind": "port",
+               "sample": "%d particles, %.1f s, one thread (C oracle restating the reference's deposit in its "
+                         "single-thread order)" % (m, dt)}
+    tree.set_velocity(None)
+    plain_rate = trace((0.0, 0.0, 0.0))
+    config = {"workload": "velocity-field deposit of %d particles (cell-uniform positions, linear-flow velocities) "
+                          "onto the AMR cone octree (256^3 base at level 10 refined to 14 in 2000 NFW haloes), TSC at "
+                          "every level, then normalisation and parent fill" % npart,
+              "particles": npart, "scheme": "TSC", "cells": int(info["cells"]),
+              "levels": [info["level_min"], info["level_max"]], "pairs_per_deposit": pairs,
+              "order": "particle then vertex per cell (the reference's single-thread order)",
+              "l2": "octree larger than L2 (no flush)", "parallelism": "single GPU"}
+    line = {"metric": VEL_METRIC, "value": value, "unit": VEL_UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dep_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+            "e2e": {"value": e2e_value, "unit": VEL_UNIT, "h2d_bytes_per_step": npart * 24, "d2h_bytes_per_step": 0},
+            "gpu_launches": None, "roofline": roofline, "deterministic": deterministic,
+            "trace": {"rays": "the benchmark's 1000x1000 grid in %d-ray batches, TSC, Jacobian at z=%g" % (B, args.zstop),
+                      "vobs": list(VEL_VOBS), "velocity_field_photon_steps_per_s": vel_rate,
+                      "plain_photon_steps_per_s": plain_rate, "ratio": vel_rate / plain_rate},
+            "parity": line_parity, "clocks": clk.summary()}
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)

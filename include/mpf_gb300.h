@@ -134,6 +134,13 @@ int mpf_octree_get_velocity(const mpf_octree* o, float* v3, float* rho);
  * with flags = 0 between a BEGIN and a FINISH accumulate further particle
  * files, as the reference's loop over shell files does (hmaps.cpp:399-420). */
 int mpf_velocity_deposit(mpf_octree* o, int scheme, int64_t n, const float* pos, const float* vel, int flags);
+/* Same with the particles in device memory, on `stream` (a cudaStream_t, or
+ * NULL for the legacy default stream); returns when the deposit is complete. */
+int mpf_velocity_deposit_device(mpf_octree* o, int scheme, int64_t n, const float* pos_device, const float* vel_device,
+                                int flags, void* stream);
+/* (cell, particle, vertex) pairs the last deposit call on the octree sorted:
+ * the work measure of its passes.  No counterpart in the reference. */
+int mpf_velocity_deposit_pairs(const mpf_octree* o, int64_t* pairs);
 
 /* Cosmology table: conformal time, a, da/dt, d2a/dt2 rows as returned by
  * Input::acquire + Input::correct (src/input.h:1090-1224, 1329-1360). */

@@ -139,6 +139,20 @@ class Octree:
         sch = {"cic": 1, "tsc": 2}[scheme] if isinstance(scheme, str) else int(scheme)
         capi.check(self._lib.mpf_velocity_deposit(self._h, sch, p.shape[0], capi.ptr(p), capi.ptr(v), flags))
 
+    def deposit_velocity_device(self, pos_ptr, vel_ptr, n, scheme="cic", begin=True, finish=True, stream=None):
+        """The same with the particles in device memory (pointers to n x 3
+        floats each), on a CUDA stream handle (None: the legacy default)."""
+        flags = (capi.MPF_VELOCITY_BEGIN if begin else 0) | (capi.MPF_VELOCITY_FINISH if finish else 0)
+        sch = {"cic": 1, "tsc": 2}[scheme] if isinstance(scheme, str) else int(scheme)
+        capi.check(self._lib.mpf_velocity_deposit_device(self._h, sch, int(n), capi.ptr(pos_ptr), capi.ptr(vel_ptr),
+                                                         flags, capi.ptr(stream)))
+
+    def deposit_pairs(self) -> int:
+        """(cell, particle, vertex) pairs the last deposit sorted."""
+        k = C.c_int64()
+        capi.check(self._lib.mpf_velocity_deposit_pairs(self._h, C.byref(k)))
+        return k.value
+
     def close(self):
         if self._h:
             self._lib.mpf_octree_destroy(self._h)

@@ -20,6 +20,7 @@ struct mpf_octree {
     int* grid;
     int4* stencil;
     float4* vel;             // velocity field (vx, vy, vz, 0) per cell, or null
+    int64_t deposit_pairs;   // (cell, particle, vertex) pairs of the last velocity deposit
 };
 
 struct mpf_cosmology {

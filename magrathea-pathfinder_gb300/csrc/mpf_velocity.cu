@@ -244,8 +244,21 @@ inline unsigned blocks(long long n, int tpb) { return (unsigned)((n + tpb - 1) /
 // device buffer freed on scope exit
 struct DevMem {
     void* p = nullptr;
+    size_t bytes = 0;
     ~DevMem() { if (p) cudaFree(p); }
-    cudaError_t alloc(size_t bytes) { return cudaMalloc(&p, bytes ? bytes : 1); }
+    cudaError_t alloc(size_t b)
+    {
+        bytes = b ? b : 1;
+        return cudaMalloc(&p, bytes);
+    }
+    // at least b bytes, keeping the buffer when it is large enough
+    cudaError_t reserve(size_t b)
+    {
+        if (p && bytes >= b) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        return alloc(b);
+    }
     template <class T> T* as() const { return (T*)p; }
 };
 
@@ -263,44 +276,102 @@ cudaError_t ensure_velocity(mpf_octree* o)
     return cudaSuccess;
 }
 
-// one pass over particles [0, n) of the chunk already on the device
-cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const float* d_vel, long long n)
+// Scratch of one deposit call, grown as its passes need: per-particle pair
+// counts, the pairs and their sorted copies, the radix histograms.
+struct DepScratch {
+    DevMem cnt, key, pay, key2, pay2, hist;
+    long long pairs = 0;   // pairs of all passes (reported by the bench)
+};
+
+// one pass over particles [0, n) of a chunk on the device, on stream s
+cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const float* d_vel, long long n, DepScratch& S,
+                          cudaStream_t s)
 {
     const DevTree& T = o->tree;
-    DevMem cnt;
-    cudaError_t e = cnt.alloc((size_t)(n + 1) * sizeof(int));
+    cudaError_t e = S.cnt.reserve((size_t)(n + 1) * sizeof(int));
     if (e != cudaSuccess) return e;
-    k_dep_pairs<<<blocks(n, 128), 128>>>(T, scheme, o->level_min, o->level_max, d_pos, n, cnt.as<int>(), nullptr, nullptr,
-                                          nullptr);
+    int* cnt = S.cnt.as<int>();
+    k_dep_pairs<<<blocks(n, 128), 128, 0, s>>>(T, scheme, o->level_min, o->level_max, d_pos, n, cnt, nullptr, nullptr,
+                                                nullptr);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if ((e = cudaMemset(cnt.as<int>() + n, 0, sizeof(int))) != cudaSuccess) return e;
-    const long long m = exclusive_scan(cnt.as<int>(), n + 1, 0);
+    if ((e = cudaMemsetAsync(cnt + n, 0, sizeof(int), s)) != cudaSuccess) return e;
+    const long long m = exclusive_scan(cnt, n + 1, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (m <= 0) return cudaSuccess;
-    DevMem key, pay, key2, pay2, hist;
+    S.pairs += m;
     const long long ntiles = (m + kVelTile - 1) / kVelTile;
-    if ((e = key.alloc((size_t)m * 4)) != cudaSuccess || (e = pay.alloc((size_t)m * 4)) != cudaSuccess ||
-        (e = key2.alloc((size_t)m * 4)) != cudaSuccess || (e = pay2.alloc((size_t)m * 4)) != cudaSuccess ||
-        (e = hist.alloc((size_t)(16 * ntiles + 1) * sizeof(int))) != cudaSuccess)
+    if ((e = S.key.reserve((size_t)m * 4)) != cudaSuccess || (e = S.pay.reserve((size_t)m * 4)) != cudaSuccess ||
+        (e = S.key2.reserve((size_t)m * 4)) != cudaSuccess || (e = S.pay2.reserve((size_t)m * 4)) != cudaSuccess ||
+        (e = S.hist.reserve((size_t)(16 * ntiles + 1) * sizeof(int))) != cudaSuccess)
         return e;
-    k_dep_pairs<<<blocks(n, 128), 128>>>(T, scheme, o->level_min, o->level_max, d_pos, n, nullptr, cnt.as<int>(),
-                                          key.as<unsigned>(), pay.as<unsigned>());
+    unsigned *k1 = S.key.as<unsigned>(), *p1 = S.pay.as<unsigned>(), *k2 = S.key2.as<unsigned>(), *p2 = S.pay2.as<unsigned>();
+    int* hist = S.hist.as<int>();
+    k_dep_pairs<<<blocks(n, 128), 128, 0, s>>>(T, scheme, o->level_min, o->level_max, d_pos, n, nullptr, cnt, k1, p1);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // digits up to the highest bit of the largest cell index
     int bits = 1;
     while (bits < 31 && (1ll << bits) < o->n) ++bits;
-    unsigned *k1 = key.as<unsigned>(), *p1 = pay.as<unsigned>(), *k2 = key2.as<unsigned>(), *p2 = pay2.as<unsigned>();
     for (int shift = 0; shift < bits; shift += 4) {
-        k_dep_hist<<<blocks(ntiles, 128), 128>>>(m, k1, shift, hist.as<int>(), ntiles);
-        exclusive_scan(hist.as<int>(), 16 * ntiles, 0);
-        k_dep_scatter<<<blocks(ntiles, 128), 128>>>(m, k1, p1, shift, hist.as<int>(), ntiles, k2, p2);
+        k_dep_hist<<<blocks(ntiles, 128), 128, 0, s>>>(m, k1, shift, hist, ntiles);
+        exclusive_scan(hist, 16 * ntiles, s);
+        k_dep_scatter<<<blocks(ntiles, 128), 128, 0, s>>>(m, k1, p1, shift, hist, ntiles, k2, p2);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         std::swap(k1, k2);
         std::swap(p1, p2);
     }
-    k_dep_accumulate<<<blocks(m, 128), 128>>>(T, o->scal, o->vel, scheme, d_pos, d_vel, m, k1, p1);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    return cudaDeviceSynchronize();
+    k_dep_accumulate<<<blocks(m, 128), 128, 0, s>>>(T, o->scal, o->vel, scheme, d_pos, d_vel, m, k1, p1);
+    return cudaGetLastError();
+}
+
+// The deposit call: particles from host (copied per pass) or device memory.
+int deposit(const char* who, mpf_octree* o, int scheme, long long n, const float* pos, const float* vel, int flags,
+            bool on_device, cudaStream_t s)
+{
+    if (!o || (scheme != 1 && scheme != 2) || n < 0 || (n > 0 && (!pos || !vel)) || (flags & ~3))
+        return mpf_internal_set_error(MPF_BAD_INPUT, who);
+    if (!(flags & MPF_VELOCITY_BEGIN) && !o->vel)
+        return mpf_internal_set_error(MPF_BAD_INPUT, "mpf_velocity_deposit: the octree has no velocity field "
+                                                     "(start with MPF_VELOCITY_BEGIN)");
+    if (o->n >= (1ll << 31)) return mpf_internal_set_error(MPF_BAD_INPUT, "mpf_velocity_deposit: octree too large");
+    cudaError_t e = ensure_velocity(o);
+    if (e == cudaSuccess && (flags & MPF_VELOCITY_BEGIN)) {
+        k_dep_begin<<<blocks(o->n, 256), 256, 0, s>>>(o->n, o->scal, o->vel);
+        e = cudaGetLastError();
+    }
+    DepScratch S;
+    if (e == cudaSuccess && n > 0) {
+        // at most kVelChunk particles and about 2^28 pairs (4 GB of sort buffers) per pass
+        const long long per = (long long)((scheme == 1) ? 8 : 27) * (o->level_max - o->level_min + 1);
+        const long long chunk = std::min<long long>(n, std::max<long long>(1024, std::min<long long>(kVelChunk, (1ll << 28) / per)));
+        DevMem dp, dv;
+        if (!on_device) {
+            e = dp.alloc((size_t)chunk * 3 * sizeof(float));
+            if (e == cudaSuccess) e = dv.alloc((size_t)chunk * 3 * sizeof(float));
+        }
+        for (long long lo = 0; lo < n && e == cudaSuccess; lo += chunk) {
+            const long long m = std::min<long long>(chunk, n - lo);
+            const float *cp = pos + 3 * lo, *cv = vel + 3 * lo;
+            if (!on_device) {
+                e = cudaMemcpyAsync(dp.p, cp, (size_t)m * 3 * sizeof(float), cudaMemcpyHostToDevice, s);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(dv.p, cv, (size_t)m * 3 * sizeof(float), cudaMemcpyHostToDevice, s);
+                cp = dp.as<float>();
+                cv = dv.as<float>();
+            }
+            if (e == cudaSuccess) e = deposit_chunk(o, scheme, cp, cv, m, S, s);
+            // the next pass reuses the particle staging and the sort buffers
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        }
+    }
+    if (e == cudaSuccess && (flags & MPF_VELOCITY_FINISH)) {
+        k_dep_normalise<<<blocks(o->n, 256), 256, 0, s>>>(o->n, o->scal, o->vel);
+        for (int L = o->level_min + 1; L <= o->level_max; ++L)
+            k_dep_from_parent<<<blocks(o->n, 256), 256, 0, s>>>(o->tree, o->n, L, o->scal, o->vel);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return mpf_internal_set_error(MPF_CUDA_ERROR, cudaGetErrorString(e));
+    o->deposit_pairs = S.pairs;
+    return MPF_OK;
 }
 
 }  // namespace
@@ -356,39 +427,20 @@ int mpf_octree_get_velocity(const mpf_octree* o, float* v3, float* rho)
 
 int mpf_velocity_deposit(mpf_octree* o, int scheme, int64_t n, const float* pos, const float* vel, int flags)
 {
-    if (!o || (scheme != 1 && scheme != 2) || n < 0 || (n > 0 && (!pos || !vel)) || (flags & ~3))
-        return mpf_internal_set_error(MPF_BAD_INPUT, "mpf_velocity_deposit: bad argument");
-    if (!(flags & MPF_VELOCITY_BEGIN) && !o->vel)
-        return mpf_internal_set_error(MPF_BAD_INPUT,
-                                      "mpf_velocity_deposit: the octree has no velocity field (start with MPF_VELOCITY_BEGIN)");
-    if (o->n >= (1ll << 31)) return mpf_internal_set_error(MPF_BAD_INPUT, "mpf_velocity_deposit: octree too large");
-    cudaError_t e = ensure_velocity(o);
-    if (e == cudaSuccess && (flags & MPF_VELOCITY_BEGIN)) {
-        k_dep_begin<<<blocks(o->n, 256), 256>>>(o->n, o->scal, o->vel);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess && n > 0) {
-        // at most kVelChunk particles and about 2^28 pairs (4 GB of sort buffers) per pass
-        const long long per = (long long)((scheme == 1) ? 8 : 27) * (o->level_max - o->level_min + 1);
-        const long long chunk = std::min<long long>(n, std::max<long long>(1024, std::min<long long>(kVelChunk, (1ll << 28) / per)));
-        DevMem dp, dv;
-        e = dp.alloc((size_t)chunk * 3 * sizeof(float));
-        if (e == cudaSuccess) e = dv.alloc((size_t)chunk * 3 * sizeof(float));
-        for (long long lo = 0; lo < n && e == cudaSuccess; lo += chunk) {
-            const long long m = std::min<long long>(chunk, n - lo);
-            e = cudaMemcpy(dp.p, pos + 3 * lo, (size_t)m * 3 * sizeof(float), cudaMemcpyHostToDevice);
-            if (e == cudaSuccess) e = cudaMemcpy(dv.p, vel + 3 * lo, (size_t)m * 3 * sizeof(float), cudaMemcpyHostToDevice);
-            if (e == cudaSuccess) e = deposit_chunk(o, scheme, dp.as<float>(), dv.as<float>(), m);
-        }
-    }
-    if (e == cudaSuccess && (flags & MPF_VELOCITY_FINISH)) {
-        k_dep_normalise<<<blocks(o->n, 256), 256>>>(o->n, o->scal, o->vel);
-        for (int L = o->level_min + 1; L <= o->level_max; ++L)
-            k_dep_from_parent<<<blocks(o->n, 256), 256>>>(o->tree, o->n, L, o->scal, o->vel);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
-    if (e != cudaSuccess) return mpf_internal_set_error(MPF_CUDA_ERROR, cudaGetErrorString(e));
+    return deposit("mpf_velocity_deposit: bad argument", o, scheme, n, pos, vel, flags, false, 0);
+}
+
+int mpf_velocity_deposit_device(mpf_octree* o, int scheme, int64_t n, const float* pos_device, const float* vel_device,
+                                int flags, void* stream)
+{
+    return deposit("mpf_velocity_deposit_device: bad argument", o, scheme, n, pos_device, vel_device, flags, true,
+                   (cudaStream_t)stream);
+}
+
+int mpf_velocity_deposit_pairs(const mpf_octree* o, int64_t* pairs)
+{
+    if (!o || !pairs) return mpf_internal_set_error(MPF_BAD_INPUT, "mpf_velocity_deposit_pairs: bad argument");
+    *pairs = o->deposit_pairs;
     return MPF_OK;
 }
 

@@ -55,7 +55,13 @@ def test_hmaps_fill_bundle_matches_reference(gpu_lib, pkg, golden, order, exact,
     """jacobiantype = bundle: the four-ray Jacobian is a finite difference over
     a 0.2 arcmin screen, so position errors are divided by ~6e-5 of the
     distance: exact mode (ulp-level launch differences) agrees to 1e-6 of the
-    lensing rows' scale, fast mode (FP32 gathers) to 1e-3."""
+    lensing rows' scale, fast mode (FP32 gathers and FP32 RK4 stage
+    corrections: the four rays' end points agree with the float64 ones to
+    ~1e-12 relative, ~2e-8 of a Jacobian entry after the division) to 1e-3
+    of the scale plus 3e-8.  The rotation w (row 3, the Jacobian's
+    antisymmetric part) is second order and several times smaller than kappa
+    and gamma; it comes out of the same four rays, so its error is measured
+    against the scale of the four Jacobian rows."""
     tree = pkg.Octree.from_records(golden["records"])
     cos = pkg.Cosmology(golden["cosmo_t"], golden["cosmo_a"], golden["cosmo_dadt"], golden["cosmo_d2adt2"])
     comps = str(golden["components"]).split(",")
@@ -67,9 +73,11 @@ def test_hmaps_fill_bundle_matches_reference(gpu_lib, pkg, golden, order, exact,
     srow = 5 + comps.index("steps") - 1
     np.testing.assert_array_equal(got[:, srow] != 0, ref[:, srow] != 0)
     tol = 1e-6 if exact else 1e-3
+    jac_scale = np.abs(ref[:, :4]).max()
     for row in range(5):
-        scale = max(np.abs(ref[:, row]).max(), 1e-9)
-        assert np.abs(got[:, row] - ref[:, row]).max() <= tol * scale + 2e-7 * (row == 4), (row, exact)
+        scale = max(np.abs(ref[:, row]).max(), 1e-9) if row != 3 else jac_scale
+        floor = 0.0 if exact else 3e-8
+        assert np.abs(got[:, row] - ref[:, row]).max() <= tol * scale + floor + 2e-7 * (row == 4), (row, exact)
     for row in range(5, ref.shape[1]):
         scale = np.abs(ref[:, row]).max() + 1e-30
         assert np.abs(got[:, row] - ref[:, row]).max() <= 2e-6 * scale + 1e-12, row
@@ -106,7 +114,9 @@ def test_hmaps_fill_born_matches_reference(gpu_lib, pkg, golden, order, exact, k
             if c == "lensing_born" or (c == "lensing" and jt != "bundle"):
                 tol = 1e-6 * scale + 2e-7 * (r - row == 3)
             elif c == "lensing":
-                tol = (1e-6 if exact else 1e-3) * scale
+                if r - row == 3:   # w: against the scale of the four Jacobian rows, as above
+                    scale = np.abs(ref[:, row:row + 4]).max()
+                tol = 1e-6 * scale if exact else 1e-3 * scale + 3e-8   # the bundle test's tolerances
             else:
                 tol = 2e-6 * (np.abs(ref[:, r]).max() + 1e-30) + 1e-12
             assert np.abs(got[:, r] - ref[:, r]).max() <= tol, (c, r, np.abs(got[:, r] - ref[:, r]).max(), tol)
