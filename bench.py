@@ -1119,8 +1119,6 @@ def run_catalogue(args, synth, spec, cos, length, world, rank, local, dist):
         dist.destroy_process_group()
 
 
-if __name__ == "__main__":
-    main()
 
 
 VEL_METRIC = "velocity-field deposit particles/s (TSC onto every level of the AMR cone octree, reference order)"
@@ -1283,3 +1281,7 @@ def run_velocity(args, synth, spec, cos, length, world, rank, local, dist):
         line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()
