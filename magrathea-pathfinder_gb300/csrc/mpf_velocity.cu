@@ -90,10 +90,12 @@ __device__ __forceinline__ double vertex_weight(int scheme, int L, const float* 
         w = __dmul_rn(w, __dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn((double)p[2], cen[2])), inv)));
         return w;
     }
-    // quadratic weights of |c - x| / cell (hmaps.h:539-545)
+    // quadratic weights of |c - x| / cell (hmaps.h:539-545); the cell size is a
+    // power of two, so dividing by it is the exact product with its inverse
+    const double inv_step = pow2(L - kLevelShift);
     double w3[3];
     for (int d = 0; d < 3; ++d) {
-        const double dist = fabs(__ddiv_rn(__dsub_rn(cen[d], (double)p[d]), step));
+        const double dist = fabs(__dmul_rn(__dsub_rn(cen[d], (double)p[d]), inv_step));
         const int a = abs(o[d]);
         const double t1 = __dmul_rn(__dmul_rn(__dmul_rn((double)a, 0.5), __dsub_rn(1.5, dist)), __dsub_rn(1.5, dist));
         const double t2 = __dmul_rn((double)(1 - a), __dsub_rn(0.75, __dmul_rn(dist, dist)));
@@ -151,29 +153,64 @@ __global__ void k_dep_scatter(long long m, const unsigned* __restrict__ key, con
     }
 }
 
-// one thread per run of equal cells: the reference's sequential += in order
+// the float64 addends of pair (particle << 5 | vertex): w and v_p w
+__device__ __forceinline__ void pair_addends(int scheme, int L, const float* __restrict__ pos, const float* __restrict__ pv,
+                                             unsigned pj, double* a)
+{
+    const long long i = pj >> 5;
+    const int v = (int)(pj & 31u);
+    const float p[3] = {__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2)};
+    const double w = vertex_weight(scheme, L, p, v);
+    a[0] = w;
+    a[1] = __dmul_rn((double)__ldg(pv + 3 * i), w);
+    a[2] = __dmul_rn((double)__ldg(pv + 3 * i + 1), w);
+    a[3] = __dmul_rn((double)__ldg(pv + 3 * i + 2), w);
+}
+
+// run starts of the sorted pairs: flag[j] = 1 where a cell's run begins
+__global__ void k_dep_run_flags(long long m, const unsigned* __restrict__ key, int* flag)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) flag[j] = (j == 0 || key[j] != key[j - 1]) ? 1 : 0;
+}
+__global__ void k_dep_run_list(long long m, const unsigned* __restrict__ key, const int* __restrict__ idx, unsigned* runs)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m && (j == 0 || key[j] != key[j - 1])) runs[idx[j]] = (unsigned)j;
+}
+
+// One thread per cell run: the reference's sequential float += in order.
+// The addends of four pairs are formed first (independent float64 work),
+// then added one after another to the float accumulators.
 __global__ void k_dep_accumulate(DevTree T, float4* scal, float4* vel, int scheme, const float* __restrict__ pos,
                                  const float* __restrict__ pv, long long m, const unsigned* __restrict__ key,
-                                 const unsigned* __restrict__ pay)
+                                 const unsigned* __restrict__ pay, const unsigned* __restrict__ runs, long long nruns)
 {
-    const long long j0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j0 >= m || (j0 > 0 && key[j0] == key[j0 - 1])) return;
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nruns) return;
+    const long long j0 = runs[r], j1 = (r + 1 < nruns) ? (long long)runs[r + 1] : m;
     const int cell = (int)key[j0];
     const int L = rec_level(T, cell);
-    float rho = scal[cell].x;
-    float4 u = vel[cell];
-    for (long long j = j0; j < m && key[j] == (unsigned)cell; ++j) {
-        const long long i = pay[j] >> 5;
-        const int v = (int)(pay[j] & 31u);
-        const float p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
-        const double w = vertex_weight(scheme, L, p, v);
-        rho = __double2float_rn(__dadd_rn((double)rho, w));
-        u.x = __double2float_rn(__dadd_rn((double)u.x, __dmul_rn((double)pv[3 * i], w)));
-        u.y = __double2float_rn(__dadd_rn((double)u.y, __dmul_rn((double)pv[3 * i + 1], w)));
-        u.z = __double2float_rn(__dadd_rn((double)u.z, __dmul_rn((double)pv[3 * i + 2], w)));
+    const float4 u0 = vel[cell];
+    float acc[4] = {scal[cell].x, u0.x, u0.y, u0.z};
+    long long j = j0;
+    for (; j + 4 <= j1; j += 4) {
+        double a[4][4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pair_addends(scheme, L, pos, pv, pay[j + q], a[q]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[c] = __double2float_rn(__dadd_rn((double)acc[c], a[q][c]));
     }
-    scal[cell].x = rho;
-    vel[cell] = u;
+    for (; j < j1; ++j) {
+        double a[4];
+        pair_addends(scheme, L, pos, pv, pay[j], a);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[c] = __double2float_rn(__dadd_rn((double)acc[c], a[c]));
+    }
+    scal[cell].x = acc[0];
+    vel[cell] = make_float4(acc[1], acc[2], acc[3], u0.w);
 }
 
 __global__ void k_dep_begin(long long n, float4* scal, float4* vel)
@@ -300,8 +337,9 @@ cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const f
     if (m <= 0) return cudaSuccess;
     S.pairs += m;
     const long long ntiles = (m + kVelTile - 1) / kVelTile;
-    if ((e = S.key.reserve((size_t)m * 4)) != cudaSuccess || (e = S.pay.reserve((size_t)m * 4)) != cudaSuccess ||
-        (e = S.key2.reserve((size_t)m * 4)) != cudaSuccess || (e = S.pay2.reserve((size_t)m * 4)) != cudaSuccess ||
+    // key buffers hold m + 1 entries: after the sort the spare one holds the run flags and their scan total
+    if ((e = S.key.reserve((size_t)(m + 1) * 4)) != cudaSuccess || (e = S.pay.reserve((size_t)m * 4)) != cudaSuccess ||
+        (e = S.key2.reserve((size_t)(m + 1) * 4)) != cudaSuccess || (e = S.pay2.reserve((size_t)m * 4)) != cudaSuccess ||
         (e = S.hist.reserve((size_t)(16 * ntiles + 1) * sizeof(int))) != cudaSuccess)
         return e;
     unsigned *k1 = S.key.as<unsigned>(), *p1 = S.pay.as<unsigned>(), *k2 = S.key2.as<unsigned>(), *p2 = S.pay2.as<unsigned>();
@@ -319,7 +357,14 @@ cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const f
         std::swap(k1, k2);
         std::swap(p1, p2);
     }
-    k_dep_accumulate<<<blocks(m, 128), 128, 0, s>>>(T, o->scal, o->vel, scheme, d_pos, d_vel, m, k1, p1);
+    // the runs of equal cells (the sort's spare buffers hold the flags and the list)
+    int* flag = reinterpret_cast<int*>(k2);
+    unsigned* runs = p2;
+    k_dep_run_flags<<<blocks(m, 256), 256, 0, s>>>(m, k1, flag);
+    if ((e = cudaMemsetAsync(flag + m, 0, sizeof(int), s)) != cudaSuccess) return e;
+    const long long nruns = exclusive_scan(flag, m + 1, s);
+    k_dep_run_list<<<blocks(m, 256), 256, 0, s>>>(m, k1, flag, runs);
+    k_dep_accumulate<<<blocks(nruns, 128), 128, 0, s>>>(T, o->scal, o->vel, scheme, d_pos, d_vel, m, k1, p1, runs, nruns);
     return cudaGetLastError();
 }
 
