@@ -13,7 +13,9 @@
 // visits them (particle, then vertex).  On the device: every (particle,
 // level, vertex) whose cell exists becomes a pair (cell, particle << 5 |
 // vertex), the pairs are stably sorted by cell (LSD radix, 4-bit digits),
-// and one thread walks each cell's run of pairs in order.  The result is
+// one thread per pair forms its float64 addends (w, v_p w), and one thread
+// per cell adds its run of addends to the float accumulators in order.  The
+// result is
 // deterministic and bit-identical to the reference run on one thread; the
 // reference's own multithreaded loop (Utility::parallelize, src/utility.h:
 // 127-147) adds to shared cells without atomics, so its sums vary with the
@@ -179,35 +181,37 @@ __global__ void k_dep_run_list(long long m, const unsigned* __restrict__ key, co
     if (j < m && (j == 0 || key[j] != key[j - 1])) runs[idx[j]] = (unsigned)j;
 }
 
-// One thread per cell run: the reference's sequential float += in order.
-// The addends of four pairs are formed first (independent float64 work),
-// then added one after another to the float accumulators.
-__global__ void k_dep_accumulate(DevTree T, float4* scal, float4* vel, int scheme, const float* __restrict__ pos,
-                                 const float* __restrict__ pv, long long m, const unsigned* __restrict__ key,
-                                 const unsigned* __restrict__ pay, const unsigned* __restrict__ runs, long long nruns)
+// The float64 addends of every sorted pair, one thread per pair (the
+// weights' float64 arithmetic, balanced over the whole grid).
+__global__ void k_dep_addends(DevTree T, int scheme, const float* __restrict__ pos, const float* __restrict__ pv,
+                              long long m, const unsigned* __restrict__ key, const unsigned* __restrict__ pay,
+                              double2* add)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    double a[4];
+    pair_addends(scheme, rec_level(T, (int)key[j]), pos, pv, pay[j], a);
+    add[2 * j] = make_double2(a[0], a[1]);
+    add[2 * j + 1] = make_double2(a[2], a[3]);
+}
+
+// One thread per cell run: the reference's sequential float += in order,
+// four independent chains (rho, vx, vy, vz).
+__global__ void k_dep_accumulate(const unsigned* __restrict__ key, float4* scal, float4* vel, long long m,
+                                 const double2* __restrict__ add, const unsigned* __restrict__ runs, long long nruns)
 {
     const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nruns) return;
     const long long j0 = runs[r], j1 = (r + 1 < nruns) ? (long long)runs[r + 1] : m;
     const int cell = (int)key[j0];
-    const int L = rec_level(T, cell);
     const float4 u0 = vel[cell];
     float acc[4] = {scal[cell].x, u0.x, u0.y, u0.z};
-    long long j = j0;
-    for (; j + 4 <= j1; j += 4) {
-        double a[4][4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) pair_addends(scheme, L, pos, pv, pay[j + q], a[q]);
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) acc[c] = __double2float_rn(__dadd_rn((double)acc[c], a[q][c]));
-    }
-    for (; j < j1; ++j) {
-        double a[4];
-        pair_addends(scheme, L, pos, pv, pay[j], a);
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[c] = __double2float_rn(__dadd_rn((double)acc[c], a[c]));
+    for (long long j = j0; j < j1; ++j) {
+        const double2 a01 = add[2 * j], a23 = add[2 * j + 1];
+        acc[0] = __double2float_rn(__dadd_rn((double)acc[0], a01.x));
+        acc[1] = __double2float_rn(__dadd_rn((double)acc[1], a01.y));
+        acc[2] = __double2float_rn(__dadd_rn((double)acc[2], a23.x));
+        acc[3] = __double2float_rn(__dadd_rn((double)acc[3], a23.y));
     }
     scal[cell].x = acc[0];
     vel[cell] = make_float4(acc[1], acc[2], acc[3], u0.w);
@@ -316,7 +320,7 @@ cudaError_t ensure_velocity(mpf_octree* o)
 // Scratch of one deposit call, grown as its passes need: per-particle pair
 // counts, the pairs and their sorted copies, the radix histograms.
 struct DepScratch {
-    DevMem cnt, key, pay, key2, pay2, hist;
+    DevMem cnt, key, pay, key2, pay2, hist, add;
     long long pairs = 0;   // pairs of all passes (reported by the bench)
 };
 
@@ -364,7 +368,10 @@ cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const f
     if ((e = cudaMemsetAsync(flag + m, 0, sizeof(int), s)) != cudaSuccess) return e;
     const long long nruns = exclusive_scan(flag, m + 1, s);
     k_dep_run_list<<<blocks(m, 256), 256, 0, s>>>(m, k1, flag, runs);
-    k_dep_accumulate<<<blocks(nruns, 128), 128, 0, s>>>(T, o->scal, o->vel, scheme, d_pos, d_vel, m, k1, p1, runs, nruns);
+    if ((e = S.add.reserve((size_t)m * 2 * sizeof(double2))) != cudaSuccess) return e;
+    double2* add = S.add.as<double2>();
+    k_dep_addends<<<blocks(m, 128), 128, 0, s>>>(T, scheme, d_pos, d_vel, m, k1, p1, add);
+    k_dep_accumulate<<<blocks(nruns, 128), 128, 0, s>>>(k1, o->scal, o->vel, m, add, runs, nruns);
     return cudaGetLastError();
 }
 
@@ -385,9 +392,10 @@ int deposit(const char* who, mpf_octree* o, int scheme, long long n, const float
     }
     DepScratch S;
     if (e == cudaSuccess && n > 0) {
-        // at most kVelChunk particles and about 2^28 pairs (4 GB of sort buffers) per pass
+        // at most kVelChunk particles and about 2^27 pairs per pass (2 GB of sort
+        // buffers, 4 GB of float64 addends)
         const long long per = (long long)((scheme == 1) ? 8 : 27) * (o->level_max - o->level_min + 1);
-        const long long chunk = std::min<long long>(n, std::max<long long>(1024, std::min<long long>(kVelChunk, (1ll << 28) / per)));
+        const long long chunk = std::min<long long>(n, std::max<long long>(1024, std::min<long long>(kVelChunk, (1ll << 27) / per)));
         DevMem dp, dv;
         if (!on_device) {
             e = dp.alloc((size_t)chunk * 3 * sizeof(float));
