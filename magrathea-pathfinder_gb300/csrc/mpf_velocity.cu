@@ -12,7 +12,8 @@
 // and rounded to float) for its particles in the order a single thread
 // visits them (particle, then vertex).  On the device: every (particle,
 // level, vertex) whose cell exists becomes a pair (cell, particle << 5 |
-// vertex), the pairs are stably sorted by cell (LSD radix, 4-bit digits),
+// vertex), the pairs are stably sorted by cell (LSD radix, 4-bit digits,
+// block-level ranking in shared memory),
 // one thread per pair forms its float64 addends (w, v_p w), and one thread
 // per cell adds its run of addends to the float accumulators in order.  The
 // result is
@@ -29,7 +30,9 @@
 namespace mpf {
 namespace {
 
-constexpr int kVelTile = 256;                 // pairs per radix-sort tile (one thread each)
+constexpr int kSortThreads = 256;             // radix-sort block
+constexpr int kSortItems = 8;                 // keys per thread
+constexpr int kSortTile = kSortThreads * kSortItems;   // keys per block and pass
 constexpr long long kVelChunk = 1ll << 19;    // particles per pass (payload: particle << 5 | vertex)
 
 __device__ __forceinline__ int rec_level(const DevTree& T, int cell)
@@ -129,29 +132,112 @@ __global__ void k_dep_pairs(DevTree T, int scheme, int lmin, int lmax, const flo
     if (!off) cnt[i] = k;
 }
 
-// stable LSD radix sort of (key, pay) by key, 4-bit digits, one tile per thread
-__global__ void k_dep_hist(long long m, const unsigned* __restrict__ key, int shift, int* hist, long long ntiles)
+// Stable LSD radix sort of (key, pay) by key, 4-bit digits.  Per pass: each
+// block of kSortThreads threads takes a tile of kSortTile consecutive pairs
+// (thread t the kSortItems pairs from t * kSortItems); k_sort_hist writes the
+// tile's digit counts (digit-major, tile-minor, so that their exclusive scan
+// gives every (digit, tile) its stable global start); k_sort_scatter ranks
+// the tile's keys by digit in shared memory (an exclusive scan over the
+// digit-major array of per-thread counts keeps the tile's order within a
+// digit) and writes each digit's run to consecutive global addresses.
+__device__ __forceinline__ void sort_load(long long m, long long tile, const unsigned* __restrict__ key, unsigned* k, int* valid)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntiles) return;
-    int h[16];
-    for (int d = 0; d < 16; ++d) h[d] = 0;
-    const long long e = min(m, (t + 1) * kVelTile);
-    for (long long j = t * kVelTile; j < e; ++j) ++h[(key[j] >> shift) & 15u];
-    for (int d = 0; d < 16; ++d) hist[d * ntiles + t] = h[d];
+    const long long j0 = tile * kSortTile + (long long)threadIdx.x * kSortItems;
+#pragma unroll
+    for (int q = 0; q < kSortItems; ++q) {
+        const long long j = j0 + q;
+        valid[q] = j < m;
+        k[q] = valid[q] ? key[j] : 0u;
+    }
 }
-__global__ void k_dep_scatter(long long m, const unsigned* __restrict__ key, const unsigned* __restrict__ pay, int shift,
-                              const int* __restrict__ off, long long ntiles, unsigned* key2, unsigned* pay2)
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_hist(long long m, const unsigned* __restrict__ key, int shift,
+                                                            int* hist, long long ntiles)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntiles) return;
-    int o[16];
-    for (int d = 0; d < 16; ++d) o[d] = off[d * ntiles + t];
-    const long long e = min(m, (t + 1) * kVelTile);
-    for (long long j = t * kVelTile; j < e; ++j) {
-        const int q = o[(key[j] >> shift) & 15u]++;
-        key2[q] = key[j];
-        pay2[q] = pay[j];
+    __shared__ int h[16];
+    if (threadIdx.x < 16) h[threadIdx.x] = 0;
+    __syncthreads();
+    unsigned k[kSortItems];
+    int valid[kSortItems];
+    sort_load(m, blockIdx.x, key, k, valid);
+#pragma unroll
+    for (int q = 0; q < kSortItems; ++q)
+        if (valid[q]) atomicAdd(&h[(k[q] >> shift) & 15u], 1);
+    __syncthreads();
+    if (threadIdx.x < 16) hist[threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(long long m, const unsigned* __restrict__ key,
+                                                               const unsigned* __restrict__ pay, int shift,
+                                                               const int* __restrict__ off, long long ntiles,
+                                                               unsigned* key2, unsigned* pay2)
+{
+    __shared__ int sc[16 * kSortThreads];   // digit-major: sc[d * kSortThreads + t]
+    __shared__ unsigned sk[kSortTile], sp[kSortTile];
+    __shared__ int wsum[kSortThreads / 32];
+    __shared__ long long goff[16];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const long long tile = blockIdx.x;
+    unsigned k[kSortItems], pv[kSortItems];
+    int valid[kSortItems];
+    sort_load(m, tile, key, k, valid);
+    const long long j0 = tile * kSortTile + (long long)t * kSortItems;
+#pragma unroll
+    for (int q = 0; q < kSortItems; ++q) pv[q] = valid[q] ? pay[j0 + q] : 0u;
+    int c[16];
+#pragma unroll
+    for (int d = 0; d < 16; ++d) c[d] = 0;
+#pragma unroll
+    for (int q = 0; q < kSortItems; ++q)
+        if (valid[q]) ++c[(k[q] >> shift) & 15u];
+#pragma unroll
+    for (int d = 0; d < 16; ++d) sc[d * kSortThreads + t] = c[d];
+    if (t < 16) goff[t] = off[t * ntiles + tile];
+    __syncthreads();
+    // exclusive scan of the flat array: thread t scans its 16 consecutive entries,
+    // then the threads' totals are scanned across the block
+    int loc[16], run = 0;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        loc[q] = run;
+        run += sc[t * 16 + q];
+    }
+    int incl = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    int before = 0;
+    for (int w = 0; w < warp; ++w) before += wsum[w];
+    const int excl = before + incl - run;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 16; ++q) sc[t * 16 + q] = excl + loc[q];
+    __syncthreads();
+    // place this thread's keys in the tile, in order within each digit
+    int base[16];
+#pragma unroll
+    for (int d = 0; d < 16; ++d) base[d] = sc[d * kSortThreads + t];
+#pragma unroll
+    for (int q = 0; q < kSortItems; ++q) {
+        if (!valid[q]) continue;
+        const int d = (k[q] >> shift) & 15u;
+        const int at = base[d]++;
+        sk[at] = k[q];
+        sp[at] = pv[q];
+    }
+    __syncthreads();
+    const long long rem = m - tile * kSortTile;
+    const int count = (int)(rem < kSortTile ? rem : kSortTile);
+    for (int i = t; i < count; i += kSortThreads) {
+        const unsigned kk = sk[i];
+        const int d = (kk >> shift) & 15u;
+        const long long dst = goff[d] + (i - sc[d * kSortThreads]);
+        key2[dst] = kk;
+        pay2[dst] = sp[i];
     }
 }
 
@@ -340,7 +426,7 @@ cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const f
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (m <= 0) return cudaSuccess;
     S.pairs += m;
-    const long long ntiles = (m + kVelTile - 1) / kVelTile;
+    const long long ntiles = (m + kSortTile - 1) / kSortTile;
     // key buffers hold m + 1 entries: after the sort the spare one holds the run flags and their scan total
     if ((e = S.key.reserve((size_t)(m + 1) * 4)) != cudaSuccess || (e = S.pay.reserve((size_t)m * 4)) != cudaSuccess ||
         (e = S.key2.reserve((size_t)(m + 1) * 4)) != cudaSuccess || (e = S.pay2.reserve((size_t)m * 4)) != cudaSuccess ||
@@ -354,9 +440,9 @@ cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const f
     int bits = 1;
     while (bits < 31 && (1ll << bits) < o->n) ++bits;
     for (int shift = 0; shift < bits; shift += 4) {
-        k_dep_hist<<<blocks(ntiles, 128), 128, 0, s>>>(m, k1, shift, hist, ntiles);
+        k_sort_hist<<<(unsigned)ntiles, kSortThreads, 0, s>>>(m, k1, shift, hist, ntiles);
         exclusive_scan(hist, 16 * ntiles, s);
-        k_dep_scatter<<<blocks(ntiles, 128), 128, 0, s>>>(m, k1, p1, shift, hist, ntiles, k2, p2);
+        k_sort_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(m, k1, p1, shift, hist, ntiles, k2, p2);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         std::swap(k1, k2);
         std::swap(p1, p2);
