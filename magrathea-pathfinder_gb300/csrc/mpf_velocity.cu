@@ -59,22 +59,6 @@ __device__ __forceinline__ void vertex_offsets(int scheme, int v, int* o)
     }
 }
 
-// The level-L cell a particle's vertex v falls in, if the octree holds that
-// exact key (hmaps.h:466-470, 532-536), else -1.  The vertex point is the
-// particle's float position plus (CIC) half a cell or (TSC) one cell times
-// the offset, in float64.
-__device__ __forceinline__ int vertex_cell(const DevTree& T, int scheme, int L, const float* p, int v)
-{
-    int o[3];
-    vertex_offsets(scheme, v, o);
-    const double half = half_cell(L);
-    const double step = (scheme == 1) ? half : __dmul_rn(2.0, half);
-    uint64_t c[3];
-    for (int d = 0; d < 3; ++d) c[d] = axis_coord(L, __dadd_rn((double)p[d], __dmul_rn(step, (double)o[d])));
-    const Found f = find_cell(T, L, c[0], c[1], c[2]);
-    return (f.cell >= 0 && f.level == L) ? f.cell : -1;
-}
-
 // The weight of a particle at p on the level-L cell reached by vertex v.
 __device__ __forceinline__ double vertex_weight(int scheme, int L, const float* p, int v)
 {
@@ -110,6 +94,7 @@ __device__ __forceinline__ double vertex_weight(int scheme, int L, const float* 
 }
 
 // pairs per particle: pass 0 counts them (cnt[i]), pass 1 writes them at off[i]
+// as (cell, particle << 5 | vertex), in the order (level, vertex)
 __global__ void k_dep_pairs(DevTree T, int scheme, int lmin, int lmax, const float* __restrict__ pos, long long n,
                             int* cnt, const int* __restrict__ off, unsigned* key, unsigned* pay)
 {
@@ -119,16 +104,29 @@ __global__ void k_dep_pairs(DevTree T, int scheme, int lmin, int lmax, const flo
     const int nv = (scheme == 1) ? 8 : 27;
     int k = 0;
     const long long base = off ? off[i] : 0;
-    for (int L = lmin; L <= lmax; ++L)
+    for (int L = lmin; L <= lmax; ++L) {
+        // the level-L cells with the exact key of each vertex (hmaps.h:466-470,
+        // 532-536): the vertex is the particle's float position plus (CIC) half a
+        // cell or (TSC) one cell times the offset, in float64; its integer
+        // coordinates per axis and offset are formed once per level
+        const double half = half_cell(L);
+        const double step = (scheme == 1) ? half : __dmul_rn(2.0, half);
+        uint64_t c[3][3];
+        for (int d = 0; d < 3; ++d)
+            for (int o = -1; o <= 1; ++o)
+                c[d][o + 1] = (scheme == 1 && o == 0) ? 0ull : axis_coord(L, __dadd_rn((double)p[d], __dmul_rn(step, (double)o)));
         for (int v = 0; v < nv; ++v) {
-            const int cell = vertex_cell(T, scheme, L, p, v);
-            if (cell < 0) continue;
+            int ov[3];
+            vertex_offsets(scheme, v, ov);
+            const Found f = find_cell(T, L, c[0][ov[0] + 1], c[1][ov[1] + 1], c[2][ov[2] + 1]);
+            if (f.cell < 0 || f.level != L) continue;
             if (off) {
-                key[base + k] = (unsigned)cell;
+                key[base + k] = (unsigned)f.cell;
                 pay[base + k] = ((unsigned)i << 5) | (unsigned)v;
             }
             ++k;
         }
+    }
     if (!off) cnt[i] = k;
 }
 
@@ -281,15 +279,31 @@ __global__ void k_dep_addends(DevTree T, int scheme, const float* __restrict__ p
     add[2 * j + 1] = make_double2(a[2], a[3]);
 }
 
-// One thread per cell run: the reference's sequential float += in order,
-// four independent chains (rho, vx, vy, vz).
-__global__ void k_dep_accumulate(const unsigned* __restrict__ key, float4* scal, float4* vel, long long m,
-                                 const double2* __restrict__ add, const unsigned* __restrict__ runs, long long nruns)
+// Length class of each run (1 + floor(log2(length)), at most 15) as a sort
+// key, with the run's start as its payload: sorted by class, the runs a warp
+// takes have about the same length.
+__global__ void k_dep_run_class(long long m, const unsigned* __restrict__ runs, long long nruns, unsigned* ckey,
+                                unsigned* cpay)
 {
     const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nruns) return;
-    const long long j0 = runs[r], j1 = (r + 1 < nruns) ? (long long)runs[r + 1] : m;
+    const long long len = ((r + 1 < nruns) ? (long long)runs[r + 1] : m) - (long long)runs[r];
+    const int cls = 64 - __clzll((unsigned long long)len);
+    ckey[r] = (unsigned)min(cls, 15);
+    cpay[r] = runs[r];
+}
+
+// One thread per cell run (the runs in length-class order): the reference's
+// sequential float += in order, four independent chains (rho, vx, vy, vz).
+__global__ void k_dep_accumulate(const unsigned* __restrict__ key, float4* scal, float4* vel, long long m,
+                                 const double2* __restrict__ add, const unsigned* __restrict__ starts, long long nruns)
+{
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nruns) return;
+    const long long j0 = starts[r];
     const int cell = (int)key[j0];
+    long long j1 = j0 + 1;
+    while (j1 < m && key[j1] == (unsigned)cell) ++j1;
     const float4 u0 = vel[cell];
     float acc[4] = {scal[cell].x, u0.x, u0.y, u0.z};
     for (long long j = j0; j < j1; ++j) {
@@ -406,7 +420,7 @@ cudaError_t ensure_velocity(mpf_octree* o)
 // Scratch of one deposit call, grown as its passes need: per-particle pair
 // counts, the pairs and their sorted copies, the radix histograms.
 struct DepScratch {
-    DevMem cnt, key, pay, key2, pay2, hist, add;
+    DevMem cnt, key, pay, key2, pay2, hist, add, runs;
     long long pairs = 0;   // pairs of all passes (reported by the bench)
 };
 
@@ -457,7 +471,15 @@ cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const f
     if ((e = S.add.reserve((size_t)m * 2 * sizeof(double2))) != cudaSuccess) return e;
     double2* add = S.add.as<double2>();
     k_dep_addends<<<blocks(m, 128), 128, 0, s>>>(T, scheme, d_pos, d_vel, m, k1, p1, add);
-    k_dep_accumulate<<<blocks(nruns, 128), 128, 0, s>>>(k1, o->scal, o->vel, m, add, runs, nruns);
+    // the runs sorted by length class (one radix pass: the class fits a digit)
+    if ((e = S.runs.reserve((size_t)nruns * 4 * sizeof(unsigned))) != cudaSuccess) return e;
+    unsigned *ck = S.runs.as<unsigned>(), *cp = ck + nruns, *ck2 = cp + nruns, *cp2 = ck2 + nruns;
+    k_dep_run_class<<<blocks(nruns, 256), 256, 0, s>>>(m, runs, nruns, ck, cp);
+    const long long rtiles = (nruns + kSortTile - 1) / kSortTile;
+    k_sort_hist<<<(unsigned)rtiles, kSortThreads, 0, s>>>(nruns, ck, 0, hist, rtiles);
+    exclusive_scan(hist, 16 * rtiles, s);
+    k_sort_scatter<<<(unsigned)rtiles, kSortThreads, 0, s>>>(nruns, ck, cp, 0, hist, rtiles, ck2, cp2);
+    k_dep_accumulate<<<blocks(nruns, 128), 128, 0, s>>>(k1, o->scal, o->vel, m, add, cp2, nruns);
     return cudaGetLastError();
 }
 
