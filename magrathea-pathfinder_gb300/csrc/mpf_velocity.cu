@@ -59,44 +59,31 @@ __device__ __forceinline__ void vertex_offsets(int scheme, int v, int* o)
     }
 }
 
-// The weight of a particle at p on the level-L cell reached by vertex v.
-__device__ __forceinline__ double vertex_weight(int scheme, int L, const float* p, int v)
+// One axis's factor of the weight of a particle at coordinate x on the level-L
+// cell whose integer coordinate along that axis is c, reached with offset o
+// (the vertex cell's centre is the cell's own).  CIC: 1 - |x - centre| /
+// extent (hmaps.h:472); TSC: the quadratic weight of |centre - x| / cell
+// (hmaps.h:539-545; the cell size is a power of two, so dividing by it is
+// the exact product with its inverse).  The weight is the product of the
+// three factors, x then y then z, as the reference multiplies them.
+__device__ __forceinline__ double axis_factor(int scheme, int L, float x, uint64_t c, int o)
 {
-    int o[3];
-    vertex_offsets(scheme, v, o);
-    // the cell's centre, from its integer coordinates at level L (the
-    // vertex's, which are the cell's own)
-    const double half = half_cell(L);
-    const double step = (scheme == 1) ? half : __dmul_rn(2.0, half);
-    double cen[3];
-    for (int d = 0; d < 3; ++d)
-        cen[d] = coord_center(L, axis_coord(L, __dadd_rn((double)p[d], __dmul_rn(step, (double)o[d]))));
-    if (scheme == 1) {
-        // (1 - |x - c| / extent) per axis, multiplied left to right (hmaps.h:472)
-        const double inv = pow2(L - kLevelShift);   // 1 / (EXTENT / 2^L), exact
-        double w = __dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn((double)p[0], cen[0])), inv));
-        w = __dmul_rn(w, __dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn((double)p[1], cen[1])), inv)));
-        w = __dmul_rn(w, __dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn((double)p[2], cen[2])), inv)));
-        return w;
-    }
-    // quadratic weights of |c - x| / cell (hmaps.h:539-545); the cell size is a
-    // power of two, so dividing by it is the exact product with its inverse
-    const double inv_step = pow2(L - kLevelShift);
-    double w3[3];
-    for (int d = 0; d < 3; ++d) {
-        const double dist = fabs(__dmul_rn(__dsub_rn(cen[d], (double)p[d]), inv_step));
-        const int a = abs(o[d]);
-        const double t1 = __dmul_rn(__dmul_rn(__dmul_rn((double)a, 0.5), __dsub_rn(1.5, dist)), __dsub_rn(1.5, dist));
-        const double t2 = __dmul_rn((double)(1 - a), __dsub_rn(0.75, __dmul_rn(dist, dist)));
-        w3[d] = __dadd_rn(t1, t2);
-    }
-    return __dmul_rn(__dmul_rn(w3[0], w3[1]), w3[2]);
+    const double cen = coord_center(L, c);
+    const double inv = pow2(L - kLevelShift);   // 1 / (EXTENT / 2^L), exact
+    if (scheme == 1) return __dsub_rn(1.0, __dmul_rn(fabs(__dsub_rn((double)x, cen)), inv));
+    const double dist = fabs(__dmul_rn(__dsub_rn(cen, (double)x), inv));
+    const int a = abs(o);
+    const double t1 = __dmul_rn(__dmul_rn(__dmul_rn((double)a, 0.5), __dsub_rn(1.5, dist)), __dsub_rn(1.5, dist));
+    const double t2 = __dmul_rn((double)(1 - a), __dsub_rn(0.75, __dmul_rn(dist, dist)));
+    return __dadd_rn(t1, t2);
 }
 
-// pairs per particle: pass 0 counts them (cnt[i]), pass 1 writes them at off[i]
-// as (cell, particle << 5 | vertex), in the order (level, vertex)
+// pairs per particle: pass 0 counts them (cnt[i]) and writes the particle's
+// axis factors per level (axw[(i * nlev + level - lmin) * 9 + 3 * axis +
+// offset + 1]); pass 1 writes the pairs at off[i] as (cell, particle << 5 |
+// vertex), in the order (level, vertex)
 __global__ void k_dep_pairs(DevTree T, int scheme, int lmin, int lmax, const float* __restrict__ pos, long long n,
-                            int* cnt, const int* __restrict__ off, unsigned* key, unsigned* pay)
+                            int* cnt, const int* __restrict__ off, unsigned* key, unsigned* pay, double* axw)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -115,6 +102,12 @@ __global__ void k_dep_pairs(DevTree T, int scheme, int lmin, int lmax, const flo
         for (int d = 0; d < 3; ++d)
             for (int o = -1; o <= 1; ++o)
                 c[d][o + 1] = (scheme == 1 && o == 0) ? 0ull : axis_coord(L, __dadd_rn((double)p[d], __dmul_rn(step, (double)o)));
+        if (!off) {
+            double* f = axw + ((long long)i * (lmax - lmin + 1) + (L - lmin)) * 9;
+            for (int d = 0; d < 3; ++d)
+                for (int o = -1; o <= 1; ++o)
+                    f[3 * d + o + 1] = (scheme == 1 && o == 0) ? 0.0 : axis_factor(scheme, L, p[d], c[d][o + 1], o);
+        }
         for (int v = 0; v < nv; ++v) {
             int ov[3];
             vertex_offsets(scheme, v, ov);
@@ -239,14 +232,16 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(long long m, cons
     }
 }
 
-// the float64 addends of pair (particle << 5 | vertex): w and v_p w
-__device__ __forceinline__ void pair_addends(int scheme, int L, const float* __restrict__ pos, const float* __restrict__ pv,
-                                             unsigned pj, double* a)
+// the float64 addends of pair (particle << 5 | vertex) on a level-L cell: w
+// (the product of the particle's three axis factors) and v_p w
+__device__ __forceinline__ void pair_addends(int scheme, int L, int lmin, int nlev, const double* __restrict__ axw,
+                                             const float* __restrict__ pv, unsigned pj, double* a)
 {
     const long long i = pj >> 5;
-    const int v = (int)(pj & 31u);
-    const float p[3] = {__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1), __ldg(pos + 3 * i + 2)};
-    const double w = vertex_weight(scheme, L, p, v);
+    int o[3];
+    vertex_offsets(scheme, (int)(pj & 31u), o);
+    const double* f = axw + (i * nlev + (L - lmin)) * 9;
+    const double w = __dmul_rn(__dmul_rn(__ldg(f + o[0] + 1), __ldg(f + 3 + o[1] + 1)), __ldg(f + 6 + o[2] + 1));
     a[0] = w;
     a[1] = __dmul_rn((double)__ldg(pv + 3 * i), w);
     a[2] = __dmul_rn((double)__ldg(pv + 3 * i + 1), w);
@@ -267,14 +262,14 @@ __global__ void k_dep_run_list(long long m, const unsigned* __restrict__ key, co
 
 // The float64 addends of every sorted pair, one thread per pair (the
 // weights' float64 arithmetic, balanced over the whole grid).
-__global__ void k_dep_addends(DevTree T, int scheme, const float* __restrict__ pos, const float* __restrict__ pv,
-                              long long m, const unsigned* __restrict__ key, const unsigned* __restrict__ pay,
-                              double2* add)
+__global__ void k_dep_addends(DevTree T, int scheme, int lmin, int nlev, const double* __restrict__ axw,
+                              const float* __restrict__ pv, long long m, const unsigned* __restrict__ key,
+                              const unsigned* __restrict__ pay, double2* add)
 {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m) return;
     double a[4];
-    pair_addends(scheme, rec_level(T, (int)key[j]), pos, pv, pay[j], a);
+    pair_addends(scheme, rec_level(T, (int)key[j]), lmin, nlev, axw, pv, pay[j], a);
     add[2 * j] = make_double2(a[0], a[1]);
     add[2 * j + 1] = make_double2(a[2], a[3]);
 }
@@ -420,7 +415,7 @@ cudaError_t ensure_velocity(mpf_octree* o)
 // Scratch of one deposit call, grown as its passes need: per-particle pair
 // counts, the pairs and their sorted copies, the radix histograms.
 struct DepScratch {
-    DevMem cnt, key, pay, key2, pay2, hist, add, runs;
+    DevMem cnt, key, pay, key2, pay2, hist, add, runs, axw;
     long long pairs = 0;   // pairs of all passes (reported by the bench)
 };
 
@@ -429,11 +424,14 @@ cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const f
                           cudaStream_t s)
 {
     const DevTree& T = o->tree;
+    const int nlev = o->level_max - o->level_min + 1;
     cudaError_t e = S.cnt.reserve((size_t)(n + 1) * sizeof(int));
+    if (e == cudaSuccess) e = S.axw.reserve((size_t)n * nlev * 9 * sizeof(double));
     if (e != cudaSuccess) return e;
     int* cnt = S.cnt.as<int>();
+    double* axw = S.axw.as<double>();
     k_dep_pairs<<<blocks(n, 128), 128, 0, s>>>(T, scheme, o->level_min, o->level_max, d_pos, n, cnt, nullptr, nullptr,
-                                                nullptr);
+                                                nullptr, axw);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(cnt + n, 0, sizeof(int), s)) != cudaSuccess) return e;
     const long long m = exclusive_scan(cnt, n + 1, s);
@@ -448,7 +446,8 @@ cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const f
         return e;
     unsigned *k1 = S.key.as<unsigned>(), *p1 = S.pay.as<unsigned>(), *k2 = S.key2.as<unsigned>(), *p2 = S.pay2.as<unsigned>();
     int* hist = S.hist.as<int>();
-    k_dep_pairs<<<blocks(n, 128), 128, 0, s>>>(T, scheme, o->level_min, o->level_max, d_pos, n, nullptr, cnt, k1, p1);
+    k_dep_pairs<<<blocks(n, 128), 128, 0, s>>>(T, scheme, o->level_min, o->level_max, d_pos, n, nullptr, cnt, k1, p1,
+                                                nullptr);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // digits up to the highest bit of the largest cell index
     int bits = 1;
@@ -470,7 +469,7 @@ cudaError_t deposit_chunk(mpf_octree* o, int scheme, const float* d_pos, const f
     k_dep_run_list<<<blocks(m, 256), 256, 0, s>>>(m, k1, flag, runs);
     if ((e = S.add.reserve((size_t)m * 2 * sizeof(double2))) != cudaSuccess) return e;
     double2* add = S.add.as<double2>();
-    k_dep_addends<<<blocks(m, 128), 128, 0, s>>>(T, scheme, d_pos, d_vel, m, k1, p1, add);
+    k_dep_addends<<<blocks(m, 128), 128, 0, s>>>(T, scheme, o->level_min, nlev, axw, d_vel, m, k1, p1, add);
     // the runs sorted by length class (one radix pass: the class fits a digit)
     if ((e = S.runs.reserve((size_t)nruns * 4 * sizeof(unsigned))) != cudaSuccess) return e;
     unsigned *ck = S.runs.as<unsigned>(), *cp = ck + nruns, *ck2 = cp + nruns, *cp2 = ck2 + nruns;
