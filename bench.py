@@ -789,7 +789,10 @@ def main():
     cosmo = pkg.Cosmology(*cos)
     launch = ray_grid()
     B = min(args.batch, launch.shape[0])
-    nb = launch.shape[0] // B
+    # batches of B rays over the whole grid, the last one shorter
+    nb = -(-launch.shape[0] // B)
+    config["batches"] = "%d of %d rays and one of %d, in turn" % (nb - 1, B, launch.shape[0] - (nb - 1) * B) \
+        if launch.shape[0] % B else "%d of %d rays, in turn" % (nb, B)
     dev = torch.device("cuda", local)
     d_launch = torch.from_numpy(launch).to(dev)
     d_steps = torch.zeros((args.warmup + args.steps, B), dtype=torch.int64, device=dev)
@@ -807,7 +810,8 @@ def main():
 
     def step(k):
         off = replicas.batch_ids(k, rank, world, nb) * B
-        rc = lib.mpf_propagate_device(tree._h, cosmo._h, C.byref(p), B, C.c_void_p(d_launch.data_ptr() + off * 48),
+        size = min(B, launch.shape[0] - off)
+        rc = lib.mpf_propagate_device(tree._h, cosmo._h, C.byref(p), size, C.c_void_p(d_launch.data_ptr() + off * 48),
                                       C.c_void_p(d_steps[k].data_ptr()), None, C.c_void_p(d_planes[k % 2].data_ptr()),
                                       C.c_void_p(d_status.data_ptr()), C.c_void_p(streams[k % 2].cuda_stream))
         capi.check(rc)
@@ -879,6 +883,13 @@ def main():
         oracle_mod.build()
         line["cpu_baseline"], oracle_run = cpu_baseline(oracle_mod, rec, cos, length, launch, planes)
         line["parity"] = parity_entry(pkg, tree, cosmo, length, planes, oracle_run, exact=args.exact)
+    if rank == 0 and not args.exact:
+        # the library's own statement of the call's error (mpf_propagate_accuracy): the same
+        # kernel against the float64 kernel on 256 rays spread over the grid
+        acc = pkg.propagate_accuracy(tree, cosmo, launch, length, sample=256, nsteps=8, order=2, stop="redshift",
+                                     planes=planes, jacobian=True)
+        acc["against"] = "the float64 kernel (the reference's operation order), mpf_propagate_accuracy"
+        line["accuracy_of_call"] = acc
     if rank == 0 and not args.no_surrogate:
         tree.close()      # the benchmark octree's 5 GB are not needed any more
         line["surrogate"] = surrogate_entry(pkg, synth, capi, lib)

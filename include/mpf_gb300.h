@@ -166,6 +166,28 @@ int mpf_interpolate(const mpf_octree* o, int order, int exact, int64_t n, const 
 int mpf_propagate(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t n, const double* launch,
                   int64_t* steps, double* final_rec, double* plane_rec);
 
+/* Errors of the FP32-gather kernel (exact = 0) against the float64 kernel,
+ * which runs the reference's operation order and gives its own build's
+ * outputs bit for bit: `sample` rays of the batch (launch records k * n /
+ * sample) traced by both, compared output by output.  Deflection (the angle
+ * between the launch direction and the ray's last position) and redshift:
+ * relative to the float64 run, per ray; kappa, gamma1, gamma2, 1/mu at each
+ * surface both runs reached: absolute, with the float64 run's largest |value|
+ * as the scale.  p as for mpf_propagate (its `exact` is not read).  No
+ * counterpart in the reference, whose every output is its own float64 run. */
+typedef struct {
+    int64_t rays;
+    int64_t step_count_differs;     /* rays whose trajectory size differs */
+    int64_t max_step_diff;
+    double deflection_rel_max, deflection_rel_median;
+    double redshift_rel_max, redshift_rel_median;
+    int64_t surface_valid_differs;  /* (ray, surface) pairs usable in one run only */
+    double lensing_abs_max[4];      /* kappa gamma1 gamma2 1/mu */
+    double lensing_scale[4];
+} mpf_accuracy;
+int mpf_propagate_accuracy(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t n,
+                           const double* launch, int64_t sample, mpf_accuracy* out);
+
 /* Same with device buffers, asynchronous on `stream` (a cudaStream_t, or NULL
  * for the legacy default stream).  status_device: one uint32 in device memory
  * that receives warning bits (bit 0: max_steps reached). */

@@ -214,6 +214,31 @@ def propagate(octree: Octree, cosmology: Cosmology, launch, length: float, nstep
     return steps, final, pout, rc
 
 
+def propagate_accuracy(octree: Octree, cosmology: Cosmology, launch, length: float, sample: int = 256,
+                       nsteps: int = 10, order: int = 2, stop: str = "redshift", stop_value: float = 0.0, planes=None,
+                       jacobian: bool = True, max_steps: int = 0, plane_normal=(0.0, 0.0, 0.0), vobs=(0.0, 0.0, 0.0)):
+    """Errors of the FP32-gather kernel against the float64 kernel (the
+    reference's operation order) on `sample` rays of the batch, as a dict in
+    the layout of accuracy.compare()."""
+    L = capi.load()
+    launch = np.ascontiguousarray(launch, dtype=np.float64).reshape(-1, 6)
+    p, keep = capi.make_params(length, nsteps, order, stop, stop_value, planes, jacobian, False, max_steps,
+                               plane_normal, vobs)
+    a = capi.Accuracy()
+    capi.check(L.mpf_propagate_accuracy(octree._h, cosmology._h, C.byref(p), launch.shape[0], capi.ptr(launch),
+                                        int(sample), C.byref(a)))
+    del keep
+    out = {"rays": a.rays, "step_count_differs": a.step_count_differs, "max_step_diff": a.max_step_diff,
+           "deflection_rel": {"max": a.deflection_rel_max, "median": a.deflection_rel_median},
+           "redshift_rel": {"max": a.redshift_rel_max, "median": a.redshift_rel_median},
+           "surface_valid_differs": a.surface_valid_differs}
+    if p.nplanes:
+        for q, name in enumerate(("kappa", "gamma1", "gamma2", "inv_mu")):
+            out[name] = {"abs_max": a.lensing_abs_max[q], "scale": a.lensing_scale[q],
+                         "of_scale": a.lensing_abs_max[q] / max(a.lensing_scale[q], 1e-300)}
+    return out
+
+
 def rays_propagate(octree: Octree, cosmology: Cosmology, photons, length: float, count: int, angle: float,
                    rotation=None, interpolation: str = "redshift", amin: float = 0.0, nsteps: int = 10, order: int = 2,
                    exact: bool = False, capacity: int = 20000, max_steps: int = 0, homogeneous_level: int = -1):

@@ -32,7 +32,7 @@ EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_uplo
            "mpf_surrogate_get_params", "mpf_surrogate_set_params", "mpf_surrogate_loss_grad", "mpf_surrogate_eval",
            "mpf_surrogate_propagate", "mpf_rays_propagate", "mpf_cells_build", "mpf_cells_parse", "mpf_autotune_info",
            "mpf_octree_set_velocity", "mpf_octree_get_velocity", "mpf_velocity_deposit",
-           "mpf_velocity_deposit_device", "mpf_velocity_deposit_pairs")
+           "mpf_velocity_deposit_device", "mpf_velocity_deposit_pairs", "mpf_propagate_accuracy")
 
 MPF_VELOCITY_BEGIN = 1
 MPF_VELOCITY_FINISH = 2
@@ -119,6 +119,14 @@ class SurrogatePropStats(C.Structure):
 _lib = None
 
 
+class Accuracy(C.Structure):
+    _fields_ = [("rays", C.c_int64), ("step_count_differs", C.c_int64), ("max_step_diff", C.c_int64),
+                ("deflection_rel_max", C.c_double), ("deflection_rel_median", C.c_double),
+                ("redshift_rel_max", C.c_double), ("redshift_rel_median", C.c_double),
+                ("surface_valid_differs", C.c_int64), ("lensing_abs_max", C.c_double * 4),
+                ("lensing_scale", C.c_double * 4)]
+
+
 def load(path: str = LIB_PATH):
     """Load the native library (raises if it has not been built)."""
     global _lib
@@ -159,6 +167,7 @@ def load(path: str = LIB_PATH):
     L.mpf_velocity_deposit.argtypes = [vp, C.c_int, i64, vp, vp, C.c_int]
     L.mpf_velocity_deposit_device.argtypes = [vp, C.c_int, i64, vp, vp, C.c_int, vp]
     L.mpf_velocity_deposit_pairs.argtypes = [vp, C.POINTER(i64)]
+    L.mpf_propagate_accuracy.argtypes = [vp, vp, C.POINTER(Params), i64, vp, i64, C.POINTER(Accuracy)]
     L.mpf_autotune_info.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
     L.mpf_cells_build.argtypes = [vp, i64, C.POINTER(CellsParams), vp, vp, i64, C.POINTER(i64)]
     L.mpf_cells_parse.argtypes = [C.c_char_p, i64, vp, i64, C.POINTER(i64)]

@@ -313,6 +313,94 @@ int mpf_propagate(const mpf_octree* o, const mpf_cosmology* c, const mpf_params*
 }
 
 namespace {
+// angle (rad) between a launch direction and the vector from the launch
+// point to the ray's last position: atan2(|d x r|, d . r)
+double deflection_of(const double* L, const double* f)
+{
+    const double d[3] = {L[3] - L[0], L[4] - L[1], L[5] - L[2]};
+    const double r[3] = {f[2] - L[0], f[3] - L[1], f[4] - L[2]};
+    const double cx = d[1] * r[2] - d[2] * r[1], cy = d[2] * r[0] - d[0] * r[2], cz = d[0] * r[1] - d[1] * r[0];
+    return std::atan2(std::sqrt(cx * cx + cy * cy + cz * cz), d[0] * r[0] + d[1] * r[1] + d[2] * r[2]);
+}
+void lensing_of(const double* rec, double* q)
+{
+    const double a11 = rec[6], a12 = rec[7], a22 = rec[8];
+    q[0] = 1.0 - (a11 + a22) * 0.5;
+    q[1] = -0.5 * (a11 - a22);
+    q[2] = -a12;
+    q[3] = a11 * a22 - a12 * a12;
+}
+double median_of(std::vector<double>& v)
+{
+    if (v.empty()) return 0.0;
+    const size_t h = v.size() / 2;
+    std::nth_element(v.begin(), v.begin() + h, v.end());
+    const double hi = v[h];
+    if (v.size() % 2) return hi;
+    return 0.5 * (*std::max_element(v.begin(), v.begin() + h) + hi);
+}
+}  // namespace
+
+extern "C" int mpf_propagate_accuracy(const mpf_octree* o, const mpf_cosmology* c, const mpf_params* p, int64_t n,
+                                      const double* launch, int64_t sample, mpf_accuracy* out)
+{
+    mpf::PropParams P;
+    if (!o || !c || !out || !fill_params(p, P) || n <= 0 || !launch || sample <= 0)
+        return set_err(MPF_BAD_INPUT, "mpf_propagate_accuracy: bad argument");
+    std::memset(out, 0, sizeof(*out));
+    const int64_t m = std::min(sample, n);
+    const int np = p->nplanes;
+    std::vector<double> L((size_t)m * 6);
+    for (int64_t k = 0; k < m; ++k) {
+        const int64_t src = (int64_t)(((__int128)k * n) / m);
+        std::memcpy(&L[(size_t)k * 6], launch + 6 * src, 6 * sizeof(double));
+    }
+    std::vector<int64_t> s0((size_t)m), s1((size_t)m);
+    std::vector<double> f0((size_t)m * MPF_PHOTON_FIELDS), f1((size_t)m * MPF_PHOTON_FIELDS);
+    std::vector<double> q0((size_t)m * np * MPF_PLANE_FIELDS + 1), q1((size_t)m * np * MPF_PLANE_FIELDS + 1);
+    mpf_params q = *p;
+    q.exact = 1;
+    const int rc0 = mpf_propagate(o, c, &q, m, L.data(), s0.data(), f0.data(), np ? q0.data() : nullptr);
+    if (rc0 < 0) return rc0;
+    q.exact = 0;
+    const int rc1 = mpf_propagate(o, c, &q, m, L.data(), s1.data(), f1.data(), np ? q1.data() : nullptr);
+    if (rc1 < 0) return rc1;
+    out->rays = m;
+    std::vector<double> dr, zr;
+    dr.reserve((size_t)m);
+    zr.reserve((size_t)m);
+    for (int64_t k = 0; k < m; ++k) {
+        const int64_t ds = s1[(size_t)k] > s0[(size_t)k] ? s1[(size_t)k] - s0[(size_t)k] : s0[(size_t)k] - s1[(size_t)k];
+        if (ds) ++out->step_count_differs;
+        out->max_step_diff = std::max(out->max_step_diff, ds);
+        const double* a = &f0[(size_t)k * MPF_PHOTON_FIELDS];
+        const double* b = &f1[(size_t)k * MPF_PHOTON_FIELDS];
+        const double t0 = deflection_of(&L[(size_t)k * 6], a), t1 = deflection_of(&L[(size_t)k * 6], b);
+        dr.push_back(std::fabs(t1 - t0) / std::max(std::fabs(t0), 1e-300));
+        zr.push_back(std::fabs(b[19] - a[19]) / std::max(std::fabs(a[19]), 1e-300));
+        for (int j = 0; j < np; ++j) {
+            const double* ra = &q0[((size_t)k * np + j) * MPF_PLANE_FIELDS];
+            const double* rb = &q1[((size_t)k * np + j) * MPF_PLANE_FIELDS];
+            const bool va = ra[19] != 0.0, vb = rb[19] != 0.0;
+            if (va != vb) ++out->surface_valid_differs;
+            if (!(va && vb)) continue;
+            double la[4], lb[4];
+            lensing_of(ra, la);
+            lensing_of(rb, lb);
+            for (int t = 0; t < 4; ++t) {
+                out->lensing_abs_max[t] = std::max(out->lensing_abs_max[t], std::fabs(lb[t] - la[t]));
+                out->lensing_scale[t] = std::max(out->lensing_scale[t], std::fabs(la[t]));
+            }
+        }
+    }
+    out->deflection_rel_max = *std::max_element(dr.begin(), dr.end());
+    out->redshift_rel_max = *std::max_element(zr.begin(), zr.end());
+    out->deflection_rel_median = median_of(dr);
+    out->redshift_rel_median = median_of(zr);
+    return (rc0 > 0 || rc1 > 0) ? set_err(MPF_WARN_MAX_STEPS, "mpf_propagate_accuracy: a ray reached max_steps") : MPF_OK;
+}
+
+namespace {
 bool catalogue_consts(const mpf_catalogue_params* p, mpf::CatConst& K, mpf::CatRotation& R)
 {
     if (!p || p->nsteps == 0 || p->order < 0 || p->order > 2 || !(p->length > 0.0) || !(p->h > 0.0) ||

@@ -130,3 +130,29 @@ def test_uniform_cone_4096_rays(uniform_cone, pkg, exact):
     else:
         rep = ACC.compare(launch, s, f, p, s_r, f_r, p_r)
         assert ACC.within(rep, 1e-6, 1e-6), rep
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_accuracy_statistic_of_the_call(amr, pkg, order):
+    """mpf_propagate_accuracy (the per-call statement of the FP32-gather
+    kernel's error against the float64 kernel) gives what the same two runs
+    compared in numpy give, and states errors inside the 1e-6 bound."""
+    tree, cosmo, O, launch, length = amr
+    planes = np.array([1.0, 2.0])
+    kw = dict(nsteps=8, order=order, stop="redshift", planes=planes, jacobian=True)
+    got = pkg.propagate_accuracy(tree, cosmo, launch, length, sample=64, **kw)
+    idx = (np.arange(64) * launch.shape[0]) // 64
+    sub = launch[idx]
+    s0, f0, p0, _ = pkg.propagate(tree, cosmo, sub, length, exact=True, **kw)
+    s1, f1, p1, _ = pkg.propagate(tree, cosmo, sub, length, exact=False, **kw)
+    ref = ACC.compare(sub, s1, f1, p1, s0, f0, p0)
+    assert got["rays"] == 64
+    for k in ("step_count_differs", "max_step_diff", "surface_valid_differs"):
+        assert got[k] == ref[k], k
+    for k in ("deflection_rel", "redshift_rel"):
+        for s in ("max", "median"):
+            assert got[k][s] == pytest.approx(ref[k][s], rel=1e-9, abs=1e-300), (k, s)
+    for k in ACC.LENSING:
+        assert got[k]["abs_max"] == pytest.approx(ref[k]["abs_max"], rel=1e-12, abs=1e-300)
+        assert got[k]["scale"] == ref[k]["scale"]
+    assert ACC.within(got, 1e-6, 1e-6), got
