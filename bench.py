@@ -699,8 +699,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=262144,
-                    help="rays per step (the persistent launch's tail of long rays is a smaller share of a larger batch)")
+    ap.add_argument("--batch", type=int, default=250000,
+                    help="rays per step (the persistent launch's tail of long rays is a smaller share of a larger batch; "
+                         "250000 = the 1000x1000 grid in 4 equal batches)")
     ap.add_argument("--workload", default="amr", choices=["amr", "medium", "small", "cones16"],
                     help="amr = the benchmark configuration; cones16 = the catalogue over 16 cones of the uniform "
                          "64^3 field (with --mode catalogue); medium / small for profiling and debugging")
