@@ -383,44 +383,18 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
                 const int4 v = __ldg(rp + q);
                 e[4 * q] = v.x; e[4 * q + 1] = v.y; e[4 * q + 2] = v.z; e[4 * q + 3] = v.w;
             }
-            // the weights are separable: sum over x of wx (sum over y of wy (sum
-            // over z of wz G)), so each component is three chains of three
-            // dependent FMAs instead of one chain of 27
 #pragma unroll
-            for (int ix = 0; ix < 3; ++ix) {
-                float tx = 0.f, ty = 0.f, tz = 0.f, tt = 0.f, tr = 0.f, tp = 0.f, ta = 0.f;
-                float tux = 0.f, tuy = 0.f, tuz = 0.f;
-#pragma unroll
-                for (int iy = 0; iy < 3; ++iy) {
-                    float sx = 0.f, sy = 0.f, sz = 0.f, st = 0.f, sr = 0.f, sp = 0.f, sa = 0.f;
-                    float sux = 0.f, suy = 0.f, suz = 0.f;
-#pragma unroll
-                    for (int iz = 0; iz < 3; ++iz) {
-                        const int j = ix * 9 + iy * 3 + iz;
-                        const float w = wz[iz];
-                        const float4 g = __ldg(T.grad + e[j]);
-                        sx = fmaf(g.x, w, sx); sy = fmaf(g.y, w, sy); sz = fmaf(g.z, w, sz); st = fmaf(g.w, w, st);
-                        if (need_all) {
-                            const float4 q = __ldg(T.scal + e[j]);
-                            sr = fmaf(q.x, w, sr); sp = fmaf(q.y, w, sp); sa = fmaf(q.z, w, sa);
-                            if (VEL) {
-                                const float4 u = __ldg(T.vel + e[j]);
-                                sux = fmaf(u.x, w, sux); suy = fmaf(u.y, w, suy); suz = fmaf(u.z, w, suz);
-                            }
-                        }
-                    }
-                    const float w = wy[iy];
-                    tx = fmaf(sx, w, tx); ty = fmaf(sy, w, ty); tz = fmaf(sz, w, tz); tt = fmaf(st, w, tt);
-                    if (need_all) {
-                        tr = fmaf(sr, w, tr); tp = fmaf(sp, w, tp); ta = fmaf(sa, w, ta);
-                        if (VEL) { tux = fmaf(sux, w, tux); tuy = fmaf(suy, w, tuy); tuz = fmaf(suz, w, tuz); }
-                    }
-                }
-                const float w = wx[ix];
-                gx = fmaf(tx, w, gx); gy = fmaf(ty, w, gy); gz = fmaf(tz, w, gz); gt = fmaf(tt, w, gt);
+            for (int j = 0; j < 27; ++j) {
+                const float wt = wx[j / 9] * wy[(j / 3) % 3] * wz[j % 3];
+                const float4 g = __ldg(T.grad + e[j]);
+                gx = fmaf(g.x, wt, gx); gy = fmaf(g.y, wt, gy); gz = fmaf(g.z, wt, gz); gt = fmaf(g.w, wt, gt);
                 if (need_all) {
-                    rho = fmaf(tr, w, rho); phi = fmaf(tp, w, phi); a = fmaf(ta, w, a);
-                    if (VEL) { ux = fmaf(tux, w, ux); uy = fmaf(tuy, w, uy); uz = fmaf(tuz, w, uz); }
+                    const float4 s = __ldg(T.scal + e[j]);
+                    rho = fmaf(s.x, wt, rho); phi = fmaf(s.y, wt, phi); a = fmaf(s.z, wt, a);
+                    if (VEL) {
+                        const float4 u = __ldg(T.vel + e[j]);
+                        ux = fmaf(u.x, wt, ux); uy = fmaf(u.y, wt, uy); uz = fmaf(u.z, wt, uz);
+                    }
                 }
             }
             res = Field7{rho, phi, gx, gy, gz, a, gt};
