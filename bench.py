@@ -706,7 +706,8 @@ def main():
                     help="amr = the benchmark configuration; cones16 = the catalogue over 16 cones of the uniform "
                          "64^3 field (with --mode catalogue); medium / small for profiling and debugging")
     ap.add_argument("--exact", action="store_true", help="reference float64 gather order")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the CPU baseline, the parity object and the accuracy statistic (profiling runs)")
     ap.add_argument("--zstop", type=float, default=2.0, help="stop redshift (profiling captures use a short path)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true",
@@ -884,7 +885,7 @@ def main():
         oracle_mod.build()
         line["cpu_baseline"], oracle_run = cpu_baseline(oracle_mod, rec, cos, length, launch, planes)
         line["parity"] = parity_entry(pkg, tree, cosmo, length, planes, oracle_run, exact=args.exact)
-    if rank == 0 and not args.exact:
+    if rank == 0 and not args.exact and not args.no_cpu_baseline:
         # the library's own statement of the call's error (mpf_propagate_accuracy): the same
         # kernel against the float64 kernel on 256 rays spread over the grid
         acc = pkg.propagate_accuracy(tree, cosmo, launch, length, sample=256, nsteps=8, order=2, stop="redshift",

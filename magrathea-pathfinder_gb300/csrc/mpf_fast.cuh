@@ -35,6 +35,11 @@ constexpr unsigned kFullMask = (1u << 27) - 1u;
 #ifndef MPF_FAST_MINB
 #define MPF_FAST_MINB 2
 #endif
+// Jacobian gathers unrolled per loop trip (1: one at a time)
+#ifndef MPF_JAC_UNROLL
+#define MPF_JAC_UNROLL 1
+#endif
+constexpr int kJacUnroll = MPF_JAC_UNROLL;
 constexpr int kFastThreads = MPF_FAST_THREADS;
 
 // Utility::interpolate with the uniform index table (same bracketing interval
@@ -599,7 +604,7 @@ __device__ __forceinline__ void jac_fast(const DevTree& T, const Loc& here, doub
     // dl = 2^-(level - 1 - log2 EXTENT) (lensing.h:430); h = dl / 2 = one cell of the point's level
     const double h = pow2(kLevelShift - here.level);
     float g[6][3];
-#pragma unroll 1
+#pragma unroll kJacUnroll
     for (int a = 0; a < 6; ++a) {
         const int ax = a >> 1;
         const int sgn = (a & 1) ? 1 : -1;
