@@ -40,6 +40,10 @@ constexpr unsigned kFullMask = (1u << 27) - 1u;
 #define MPF_JAC_UNROLL 1
 #endif
 constexpr int kJacUnroll = MPF_JAC_UNROLL;
+// TSC record gathers: 1 = a loop over the three x-slabs, 0 = fully unrolled
+#ifndef MPF_TSC_SLAB
+#define MPF_TSC_SLAB 0
+#endif
 constexpr int kFastThreads = MPF_FAST_THREADS;
 
 // Utility::interpolate with the uniform index table (same bracketing interval
@@ -382,6 +386,30 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
             tsc_w3(fd[2], wz);
             float gx = 0.f, gy = 0.f, gz = 0.f, gt = 0.f, rho = 0.f, phi = 0.f, a = 0.f;
             float ux = 0.f, uy = 0.f, uz = 0.f;
+#if MPF_TSC_SLAB
+            // one x-slab of 9 cells per loop trip: a third of the code of the
+            // fully unrolled loop (the kernel is instruction-fetch bound)
+            const int* re = reinterpret_cast<const int*>(rp);
+#pragma unroll 1
+            for (int ix = 0; ix < 3; ++ix) {
+                const float wxi = (ix == 0) ? wx[0] : ((ix == 1) ? wx[1] : wx[2]);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    const int e = __ldg(re + 9 * ix + k);
+                    const float wt = wxi * wy[k / 3] * wz[k % 3];
+                    const float4 g = __ldg(T.grad + e);
+                    gx = fmaf(g.x, wt, gx); gy = fmaf(g.y, wt, gy); gz = fmaf(g.z, wt, gz); gt = fmaf(g.w, wt, gt);
+                    if (need_all) {
+                        const float4 s = __ldg(T.scal + e);
+                        rho = fmaf(s.x, wt, rho); phi = fmaf(s.y, wt, phi); a = fmaf(s.z, wt, a);
+                        if (VEL) {
+                            const float4 u = __ldg(T.vel + e);
+                            ux = fmaf(u.x, wt, ux); uy = fmaf(u.y, wt, uy); uz = fmaf(u.z, wt, uz);
+                        }
+                    }
+                }
+            }
+#else
             int e[28];
 #pragma unroll
             for (int q = 0; q < 7; ++q) {
@@ -402,6 +430,7 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
                     }
                 }
             }
+#endif
             res = Field7{rho, phi, gx, gy, gz, a, gt};
             if (VEL) { vv[0] = ux; vv[1] = uy; vv[2] = uz; }
             return true;
