@@ -24,6 +24,33 @@ def test_pix2vec_matches_harness(gpu_lib, pkg, golden):
     assert abs(allv[:, 2].mean()) < 1e-12     # equal-area pixels: zero mean z
 
 
+def test_pix2vec_known_centres(gpu_lib, pkg):
+    """RING pixel centres that the HEALPix scheme fixes (Gorski et al. 2005,
+    ApJ 622, 759, the base tessellation of its Fig. 3): at nside 1 the north
+    cap ring at z = 2/3 with phi = pi/4 + k pi/2, the equator at z = 0 with
+    phi = k pi/2, the south ring at z = -2/3; at nside 2 the first ring at
+    z = 1 - 1/(3 nside^2) = 11/12 and the ring latitudes 2/3, 1/3, 0 after it,
+    the equatorial rings alternately shifted by half a pixel."""
+    v = pkg.pix2vec_ring(1, np.arange(12))
+    z = np.repeat([2.0 / 3.0, 0.0, -2.0 / 3.0], 4)
+    phi = np.concatenate([np.pi / 4 + np.arange(4) * np.pi / 2, np.arange(4) * np.pi / 2,
+                          np.pi / 4 + np.arange(4) * np.pi / 2])
+    np.testing.assert_allclose(v[:, 2], z, atol=1e-15)
+    np.testing.assert_allclose(np.mod(np.arctan2(v[:, 1], v[:, 0]), 2 * np.pi), phi, atol=1e-14)
+    v2 = pkg.pix2vec_ring(2, np.arange(48))
+    # rings: 4 (cap), 8 (cap edge), 8, 8 (equator), 8, 8, 4 pixels
+    ring_z = [11.0 / 12.0, 2.0 / 3.0, 1.0 / 3.0, 0.0, -1.0 / 3.0, -2.0 / 3.0, -11.0 / 12.0]
+    counts = [4, 8, 8, 8, 8, 8, 4]
+    np.testing.assert_allclose(v2[:, 2], np.repeat(ring_z, counts), atol=1e-15)
+    ph2 = np.mod(np.arctan2(v2[:, 1], v2[:, 0]), 2 * np.pi)
+    np.testing.assert_allclose(ph2[:4], np.pi / 4 + np.arange(4) * np.pi / 2, atol=1e-14)
+    np.testing.assert_allclose(ph2[4:12], np.pi / 8 + np.arange(8) * np.pi / 4, atol=1e-14)
+    # equatorial rings (z = 1/3, 0, -1/3): shifted by pi/8, not shifted, shifted
+    np.testing.assert_allclose(ph2[12:20], np.arange(8) * np.pi / 4, atol=1e-14)
+    np.testing.assert_allclose(ph2[20:28], np.pi / 8 + np.arange(8) * np.pi / 4, atol=1e-14)
+    np.testing.assert_allclose(ph2[28:36], np.arange(8) * np.pi / 4, atol=1e-14)
+
+
 @pytest.mark.parametrize("order", [0, 1, 2])
 @pytest.mark.parametrize("exact", [True, False])
 def test_hmaps_fill_matches_reference_fillmap(gpu_lib, pkg, golden, order, exact):
