@@ -61,3 +61,54 @@ def test_two_streams_share_the_handles(gpu_lib, pkg, golden):
     del keep
     tree.close()
     cos.close()
+
+
+def test_propagate_captured_in_a_cuda_graph(gpu_lib, pkg, golden):
+    """mpf_propagate_device on a stream is capturable in a CUDA graph once the
+    stream has seen one call (its work-queue counter and, for a batch of at
+    least 2^17 rays, the autotuned shape exist then): the graph's replays
+    (queue reset + the persistent launch) give the direct call's results,
+    also after the launch records change in place."""
+    torch = pytest.importorskip("torch")
+    from importlib import import_module
+    capi = import_module(pkg.__name__ + ".capi")
+    tree = pkg.Octree.from_records(golden["records"])
+    cos = pkg.Cosmology(golden["cosmo_t"], golden["cosmo_a"], golden["cosmo_dadt"], golden["cosmo_d2adt2"])
+    length = float(golden["cosmo_length"])
+    base = np.asarray(golden["launch"], dtype=np.float64)
+    zs = np.asarray(golden["zs"], dtype=np.float64)
+    batches = [np.tile(base, (600, 1)), np.tile(base * np.array([1, -1, 1, 1, -1, 1.0]), (600, 1))]
+    n = batches[0].shape[0]
+    assert n >= (1 << 17)
+    kw = dict(nsteps=int(golden["nsteps"]), order=2, stop="redshift", planes=zs, jacobian=True, exact=False)
+    ref = [pkg.propagate(tree, cos, b, length, **kw) for b in batches]
+    p, keep = capi.make_params(length, int(golden["nsteps"]), 2, "redshift", 0.0, zs, True, False, 0)
+    L = pkg.library()
+    dev = torch.device("cuda", 0)
+    s = torch.cuda.Stream(dev)
+    d_l = torch.from_numpy(batches[0]).to(dev)
+    d_s = torch.zeros(n, dtype=torch.int64, device=dev)
+    d_p = torch.zeros(n * zs.shape[0] * capi.MPF_PLANE_FIELDS, dtype=torch.float64, device=dev)
+    d_st = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def call():
+        capi.check(L.mpf_propagate_device(tree._h, cos._h, C.byref(p), n, C.c_void_p(d_l.data_ptr()),
+                                          C.c_void_p(d_s.data_ptr()), None, C.c_void_p(d_p.data_ptr()),
+                                          C.c_void_p(d_st.data_ptr()), C.c_void_p(s.cuda_stream)))
+
+    with torch.cuda.stream(s):
+        call()                      # first call on the stream: queue counter and tuned shape
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        call()
+    for j in (0, 1, 0):
+        d_l.copy_(torch.from_numpy(batches[j]))
+        d_s.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(d_s.cpu().numpy(), ref[j][0])
+        got = d_p.cpu().numpy().reshape(n, zs.shape[0], capi.MPF_PLANE_FIELDS)
+        np.testing.assert_array_equal(got.view(np.uint64), ref[j][2].view(np.uint64))
+    tree.close()
+    cos.close()
