@@ -150,3 +150,32 @@ def test_hmaps_fill_born_matches_reference(gpu_lib, pkg, golden, order, exact, k
         row += nrow
     tree.close()
     cos.close()
+
+
+def test_hmaps_fill_large_call_equals_small_calls(gpu_lib, pkg, golden):
+    """A call large enough to be traced as two halves on two streams (here
+    nside 4096: the ~78 000 pixels within 2 degrees of the cone's axis) writes
+    the same map bits as the same pixels in calls of 4096 pixels."""
+    ns = 4096
+    ncap = 2 * ns * (ns - 1)
+    # candidate pixels of the equatorial rings near z = 0 and phi = 0, then the exact cut
+    rings = np.arange(2 * ns - 300, 2 * ns + 301)
+    cols = np.concatenate([np.arange(0, 140), np.arange(4 * ns - 140, 4 * ns)])
+    cand = (ncap + (rings[:, None] - ns) * 4 * ns + cols[None, :]).reshape(-1).astype(np.int64)
+    v = pkg.pix2vec_ring(ns, cand)
+    phi = np.arctan2(v[:, 1], v[:, 0])
+    th = np.arccos(v[:, 2])
+    sel = (np.abs(phi) < np.radians(2.0)) & (np.abs(th - np.pi / 2) < np.radians(2.0))
+    pix = np.sort(cand[sel])
+    assert pix.shape[0] >= 65536, pix.shape
+    tree = pkg.Octree.from_records(golden["records"])
+    cos = pkg.Cosmology(golden["cosmo_t"], golden["cosmo_a"], golden["cosmo_dadt"], golden["cosmo_d2adt2"])
+    comps = str(golden["components"]).split(",")
+    kw = dict(nsteps=int(golden["nsteps"]), order=2, exact=False)
+    whole = pkg.hmaps_fill(tree, cos, ns, pix, golden["zs"], golden["homogeneous"], comps,
+                           float(golden["cosmo_length"]), **kw)
+    parts = [pkg.hmaps_fill(tree, cos, ns, pix[i:i + 4096], golden["zs"], golden["homogeneous"], comps,
+                            float(golden["cosmo_length"]), **kw) for i in range(0, pix.shape[0], 4096)]
+    np.testing.assert_array_equal(whole.view(np.uint32), np.concatenate(parts, axis=2).view(np.uint32))
+    tree.close()
+    cos.close()
