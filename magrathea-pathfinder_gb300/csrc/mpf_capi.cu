@@ -42,34 +42,27 @@ bool has_device()
     return cudaGetDeviceCount(&n) == cudaSuccess && n > 0;
 }
 
-// Two non-blocking streams per host thread and device for the host-buffer
-// calls: calls from different host threads never share a stream (nor the
-// stream's work-queue counter), and one call can run two halves at once.
-// Kept for the thread's lifetime.
-cudaError_t host_streams(cudaStream_t* out)
+// A non-blocking stream per host thread and device for the host-buffer
+// calls: calls from different host threads never share a stream, nor the
+// stream's work-queue counter (on the legacy default stream, one thread's
+// queue reset could land between another's reset and launch).  Kept for the
+// thread's lifetime.
+cudaError_t host_stream(cudaStream_t* out)
 {
-    thread_local std::map<int, std::pair<cudaStream_t, cudaStream_t>> mine;
+    thread_local std::map<int, cudaStream_t> mine;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     auto it = mine.find(dev);
     if (it == mine.end()) {
-        cudaStream_t a = nullptr, b = nullptr;
+        cudaStream_t a = nullptr;
         e = cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking);
-        if (e != cudaSuccess) {
-            if (a) cudaStreamDestroy(a);
-            return e;
-        }
-        it = mine.emplace(dev, std::make_pair(a, b)).first;
+        if (e != cudaSuccess) return e;
+        it = mine.emplace(dev, a).first;
     }
-    out[0] = it->second.first;
-    out[1] = it->second.second;
+    *out = it->second;
     return cudaSuccess;
 }
-
-// batches of at least this many rays are traced as two halves on two streams
-constexpr int64_t kSplitRays = 1 << 15;
 
 // RAII device buffer
 struct DBuf {
@@ -318,8 +311,8 @@ int mpf_propagate(const mpf_octree* o, const mpf_cosmology* c, const mpf_params*
     if (!o || !c || !fill_params(p, P) || n < 0 || (n > 0 && !launch))
         return set_err(MPF_BAD_INPUT, "mpf_propagate: bad argument");
     if (n == 0) return MPF_OK;
-    cudaStream_t st[2];
-    cudaError_t e = host_streams(st);
+    cudaStream_t st = nullptr;
+    cudaError_t e = host_stream(&st);
     if (e != cudaSuccess) return cuda_err(e, "mpf_propagate");
     const int np = p->nplanes;
     DBuf dl, ds, df, dp, dst;
@@ -327,46 +320,24 @@ int mpf_propagate(const mpf_octree* o, const mpf_cosmology* c, const mpf_params*
     if (e == cudaSuccess) e = ds.alloc((size_t)n * sizeof(int64_t));
     if (e == cudaSuccess && final_rec) e = df.alloc((size_t)n * MPF_PHOTON_FIELDS * sizeof(double));
     if (e == cudaSuccess && plane_rec && np > 0) e = dp.alloc((size_t)n * np * MPF_PLANE_FIELDS * sizeof(double));
-    if (e == cudaSuccess) e = dst.alloc(2 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = dst.alloc(sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(dst.p, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dl.p, launch, (size_t)n * 6 * sizeof(double), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_err(e, "mpf_propagate");
-    // A large batch goes as two halves on two streams: the second half's
-    // launch records are copied while the first half traces, the second
-    // half's blocks take the SMs the first half's last rays leave idle, and
-    // the first half's results are copied back while the second traces.
-    const int64_t h = (n >= kSplitRays) ? n / 2 : n;
-    const int64_t off[2] = {0, h}, cnt[2] = {h, n - h};
-    const int parts = (n - h > 0) ? 2 : 1;
-    auto* L = (double*)dl.p;
-    auto* S = (int64_t*)ds.p;
-    auto* F = (double*)df.p;
-    auto* Q = (double*)dp.p;
-    auto* W = (uint32_t*)dst.p;
-    for (int k = 0; k < parts; ++k) {
-        const int64_t o0 = off[k], m = cnt[k];
-        e = cudaMemsetAsync(W + k, 0, sizeof(uint32_t), st[k]);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(L + 6 * o0, launch + 6 * o0, (size_t)m * 6 * sizeof(double), cudaMemcpyHostToDevice, st[k]);
-        if (e != cudaSuccess) return cuda_err(e, "mpf_propagate");
-        const int rc = mpf_propagate_device(o, c, p, m, L + 6 * o0, S + o0, F ? F + (size_t)o0 * MPF_PHOTON_FIELDS : nullptr,
-                                            Q ? Q + (size_t)o0 * np * MPF_PLANE_FIELDS : nullptr, W + k, st[k]);
-        if (rc != MPF_OK) return rc;
-    }
-    uint32_t status[2] = {0, 0};
-    for (int k = 0; k < parts && e == cudaSuccess; ++k) {
-        const int64_t o0 = off[k], m = cnt[k];
-        e = cudaMemcpyAsync(status + k, W + k, sizeof(uint32_t), cudaMemcpyDeviceToHost, st[k]);
-        if (e == cudaSuccess && steps)
-            e = cudaMemcpyAsync(steps + o0, S + o0, (size_t)m * sizeof(int64_t), cudaMemcpyDeviceToHost, st[k]);
-        if (e == cudaSuccess && final_rec)
-            e = cudaMemcpyAsync(final_rec + (size_t)o0 * MPF_PHOTON_FIELDS, F + (size_t)o0 * MPF_PHOTON_FIELDS,
-                                (size_t)m * MPF_PHOTON_FIELDS * sizeof(double), cudaMemcpyDeviceToHost, st[k]);
-        if (e == cudaSuccess && plane_rec && np > 0)
-            e = cudaMemcpyAsync(plane_rec + (size_t)o0 * np * MPF_PLANE_FIELDS, Q + (size_t)o0 * np * MPF_PLANE_FIELDS,
-                                (size_t)m * np * MPF_PLANE_FIELDS * sizeof(double), cudaMemcpyDeviceToHost, st[k]);
-    }
-    for (int k = 0; k < parts && e == cudaSuccess; ++k) e = cudaStreamSynchronize(st[k]);
+    int rc = mpf_propagate_device(o, c, p, n, (const double*)dl.p, (int64_t*)ds.p, (double*)df.p, (double*)dp.p,
+                                  (uint32_t*)dst.p, st);
+    if (rc != MPF_OK) return rc;
+    uint32_t status = 0;
+    e = cudaMemcpyAsync(&status, dst.p, sizeof(status), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && steps)
+        e = cudaMemcpyAsync(steps, ds.p, (size_t)n * sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && final_rec)
+        e = cudaMemcpyAsync(final_rec, df.p, (size_t)n * MPF_PHOTON_FIELDS * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && plane_rec && np > 0)
+        e = cudaMemcpyAsync(plane_rec, dp.p, (size_t)n * np * MPF_PLANE_FIELDS * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_err(e, "mpf_propagate");
-    if ((status[0] | status[1]) & 1u) return set_err(MPF_WARN_MAX_STEPS, "mpf_propagate: a ray reached max_steps");
+    if (status & 1u) return set_err(MPF_WARN_MAX_STEPS, "mpf_propagate: a ray reached max_steps");
     return MPF_OK;
 }
 

@@ -254,9 +254,6 @@ namespace {
 unsigned blocks(long long n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
 }  // namespace
 
-// chunks of at least twice this many pixels are traced as two halves
-constexpr long long kMapSplitRays = 1 << 15;
-
 cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P, bool exact, long long nside,
                        long long npix, const long long* d_pixels, const MapSpec& M, float* d_maps, long long chunk,
                        unsigned* h_status, cudaStream_t stream)
@@ -297,55 +294,20 @@ cudaError_t hmaps_fill(const DevTree& T, const DevCosmo& C, const PropParams& P,
         if (!M.born) return cudaSuccess;
         return exact ? launch_propagate<true>(T, C, Pn, launch, m, On, stream) : launch_propagate<false>(T, C, Pn, launch, m, On, stream);
     };
-    // (lensing_born alone traces neither the central nor the bundle rays).
-    // Each chunk goes as two halves, the second on a stream of its own: the
-    // second half's blocks take the SMs that the first half's last rays
-    // leave idle.  The halves use disjoint parts of the chunk's buffers.
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev_start = nullptr, ev_done = nullptr;
-    const bool split = (!M.bundle || M.only_born) && cap >= 2 * kMapSplitRays;
-    if (e == cudaSuccess && split) {
-        e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventRecord(ev_start, stream);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev_start, 0);
-    }
-    auto trace_part = [&](long long c0, long long h0, long long m, cudaStream_t s) -> cudaError_t {
-        // pixels [c0 + h0, c0 + h0 + m) into the buffers' rows [h0, h0 + m)
-        double* lp = launch + 6 * h0;
-        k_pix_launch<<<blocks(m, 128), 128, 0, s>>>(m, nside, d_pixels + c0 + h0, lp);
-        cudaError_t r = cudaGetLastError();
-        if (r != cudaSuccess) return r;
-        const PropOut Op{steps + h0, nullptr, rec + h0 * nz * kPlaneFields, status, nullptr};
-        if (!M.only_born) {
-            r = exact ? launch_propagate<true>(T, C, P, lp, m, Op, s) : launch_propagate<false>(T, C, P, lp, m, Op, s);
-            if (r != cudaSuccess) return r;
-        }
-        if (M.born) {
-            const PropOut Ob{brn_steps + h0, nullptr, brn + h0 * nz * kWideFields, status, nullptr};
-            r = exact ? launch_propagate<true>(T, C, Pn, lp, m, Ob, s) : launch_propagate<false>(T, C, Pn, lp, m, Ob, s);
-            if (r != cudaSuccess) return r;
-        }
-        k_fill_maps<<<blocks(m * nz, 128), 128, 0, s>>>(m, nz, M, lp, rec + h0 * nz * kPlaneFields, kPlaneFields, nullptr,
-                                                         M.born ? brn + h0 * nz * kWideFields : nullptr, d_maps, npix,
-                                                         c0 + h0);
-        return cudaGetLastError();
-    };
+    // (lensing_born alone traces neither the central nor the bundle rays)
     for (long long c0 = 0; (!M.bundle || M.only_born) && e == cudaSuccess && c0 < npix; c0 += cap) {
         const long long m = (npix - c0 < cap) ? npix - c0 : cap;
-        const long long h = (split && m >= 2 * kMapSplitRays) ? m / 2 : m;
-        e = trace_part(c0, 0, h, stream);
-        if (e == cudaSuccess && m > h) e = trace_part(c0, h, m - h, side);
+        k_pix_launch<<<blocks(m, 128), 128, 0, stream>>>(m, nside, d_pixels + c0, launch);
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        if (!M.only_born) {
+            e = exact ? launch_propagate<true>(T, C, P, launch, m, O, stream) : launch_propagate<false>(T, C, P, launch, m, O, stream);
+            if (e != cudaSuccess) break;
+        }
+        if ((e = born_pass(m)) != cudaSuccess) break;
+        k_fill_maps<<<blocks(m * nz, 128), 128, 0, stream>>>(m, nz, M, launch, rec, kPlaneFields, nullptr, brn, d_maps,
+                                                               npix, c0);
+        e = cudaGetLastError();
     }
-    if (side) {
-        if (e == cudaSuccess) e = cudaEventRecord(ev_done, side);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, ev_done, 0);
-        cudaStreamSynchronize(side);
-        cudaStreamDestroy(side);
-    }
-    if (ev_start) cudaEventDestroy(ev_start);
-    if (ev_done) cudaEventDestroy(ev_done);
     if (M.bundle && !M.only_born && e == cudaSuccess) {
         // central rays with wide records, then four bundle rays per pixel to
         // their own stop_bundle surfaces, then the Jacobians and the rows

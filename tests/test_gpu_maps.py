@@ -153,9 +153,10 @@ def test_hmaps_fill_born_matches_reference(gpu_lib, pkg, golden, order, exact, k
 
 
 def test_hmaps_fill_large_call_equals_small_calls(gpu_lib, pkg, golden):
-    """A call large enough to be traced as two halves on two streams (here
-    nside 4096: the ~78 000 pixels within 2 degrees of the cone's axis) writes
-    the same map bits as the same pixels in calls of 4096 pixels."""
+    """A call of many pixels (nside 4096: the ~78 000 pixels within 2 degrees
+    of the cone's axis, one persistent launch with the autotuned shape) writes
+    the same map bits as the same pixels in calls of 4096 pixels (one-warp
+    blocks): a pixel's rows do not depend on the batch it is traced in."""
     ns = 4096
     ncap = 2 * ns * (ns - 1)
     # candidate pixels of the equatorial rings near z = 0 and phi = 0, then the exact cut
