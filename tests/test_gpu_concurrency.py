@@ -112,3 +112,37 @@ def test_propagate_captured_in_a_cuda_graph(gpu_lib, pkg, golden):
         np.testing.assert_array_equal(got.view(np.uint64), ref[j][2].view(np.uint64))
     tree.close()
     cos.close()
+
+
+def test_host_buffer_calls_from_two_threads(gpu_lib, pkg, golden):
+    """mpf_propagate from two host threads at once (each thread gets its own
+    stream inside the library): each thread's results equal the same batch
+    traced alone."""
+    tree = pkg.Octree.from_records(golden["records"])
+    cos = pkg.Cosmology(golden["cosmo_t"], golden["cosmo_a"], golden["cosmo_dadt"], golden["cosmo_d2adt2"])
+    length = float(golden["cosmo_length"])
+    base = np.asarray(golden["launch"], dtype=np.float64)
+    batches = [np.tile(base, (64, 1)), np.tile(base * np.array([1, -1, 1, 1, -1, 1.0]), (64, 1))]
+    kw = dict(nsteps=int(golden["nsteps"]), order=2, stop="redshift", stop_value=float(golden["zs"][-1]),
+              exact=False, jacobian=True)
+    ref = [pkg.propagate(tree, cos, b, length, **kw) for b in batches]
+    out, errors = [None, None], []
+
+    def lane(j):
+        try:
+            for _ in range(3):
+                out[j] = pkg.propagate(tree, cos, batches[j], length, **kw)
+        except Exception as exc:   # reported below
+            errors.append(exc)
+
+    th = [threading.Thread(target=lane, args=(j,)) for j in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors, errors
+    for j in range(2):
+        np.testing.assert_array_equal(out[j][0], ref[j][0])
+        np.testing.assert_array_equal(out[j][1].view(np.uint64), ref[j][1].view(np.uint64))
+    tree.close()
+    cos.close()
