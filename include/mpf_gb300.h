@@ -425,7 +425,7 @@ int mpf_rays_propagate(const mpf_octree* o, const mpf_cosmology* c, const mpf_pa
 /* A per-cone neural field that stands in for the octree gather
  * (SimpleHyperOctree::tsc / cic, src/magrathea/simplehyperoctree.h:1410-1644)
  * inside the RK4 stages of Integrator::integrate (src/integrator.h:648-824).
- * It has no counterpart in the reference; the octree path stays its judge and
+ * It has no counterpart in the reference; the octree path stays its check and
  * fallback.  Network: (x, y, z, a) normalised to [-1, 1]^4 -> 64 Fourier
  * frequencies (sin, cos: 128 features) -> 4 hidden layers of 128 with SiLU ->
  * 5 outputs (phi, dphidx, dphidy, dphidz, dphidt), BF16 weights and FP32

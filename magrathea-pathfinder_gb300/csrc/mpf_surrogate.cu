@@ -2,7 +2,7 @@
 // network in mpf_surrogate.cuh).  It has no counterpart in the reference: it
 // stands in for SimpleHyperOctree::tsc / cic (simplehyperoctree.h:1410-1644)
 // inside the RK4 stages of Integrator::integrate (integrator.h:648-824), and
-// the octree stays its judge and fallback.
+// the octree stays its check and fallback.
 //
 //  * Training samples: points uniform in the cone volume labelled by the
 //    octree's TSC gather (the fast-mode record path).

@@ -1,6 +1,6 @@
 """Learned field surrogate (host side): a per-cone Fourier-feature MLP trained
 on the octree's TSC field and used in place of the octree gather inside the
-RK4 stages, with the octree as judge and fallback.  Compute in
+RK4 stages, with the octree as check and fallback.  Compute in
 libmpf_gb300.so (mpf_surrogate_* in include/mpf_gb300.h).
 
     s = Surrogate(cone_tan=(ty, tz), r_max=..., a_min=...)
