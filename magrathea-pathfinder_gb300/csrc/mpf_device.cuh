@@ -173,6 +173,44 @@ __device__ __forceinline__ Found locate(const DevTree& T, double x, double y, do
     return find_cell(T, kMaxLevel, axis_coord(kMaxLevel, x), axis_coord(kMaxLevel, y), axis_coord(kMaxLevel, z));
 }
 
+// find_cell(T, L, k) for the integer coordinates k of a level-L key, read
+// from the stencil record of the level-L cell `centre` (coordinates cc) when
+// k is one of its 27 neighbours (the record holds find_cell's result for each
+// of them), else found by the walk.  centre < 0: no record to read.
+#ifndef MPF_EXACT_STENCIL
+#define MPF_EXACT_STENCIL 1
+#endif
+__device__ __forceinline__ Found find_near(const DevTree& T, int centre, int L, const uint64_t* cc, const uint64_t* k)
+{
+    if (MPF_EXACT_STENCIL && centre >= 0 && L >= 2) {
+        const uint64_t mask = (L >= 64) ? ~0ull : ((1ull << L) - 1ull);
+        int o[3];
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const uint64_t dm = (k[d] - cc[d]) & mask;
+            o[d] = (dm == 0) ? 0 : (dm == 1) ? 1 : (dm == mask) ? -1 : 2;
+            ok = ok && o[d] != 2;
+        }
+        if (ok) {
+            const int e = __ldg(reinterpret_cast<const int*>(T.stencil + 8 * (size_t)centre) + (o[0] + 1) * 9 +
+                                (o[1] + 1) * 3 + (o[2] + 1));
+            if (e < 0) return Found{-1, 0};
+            return Found{e, __float_as_int(__ldg(&T.scal[e].w))};
+        }
+    }
+    return find_cell(T, L, k[0], k[1], k[2]);
+}
+
+// the level-`to` ancestor of the level-`from` cell `cell` through the records'
+// parent links, or -1
+__device__ __forceinline__ int ancestor_cell(const DevTree& T, int cell, int from, int to)
+{
+    for (int l = from; l > to && cell >= 0; --l)
+        cell = __ldg(reinterpret_cast<const int*>(T.stencil + 8 * (size_t)cell) + 30);
+    return cell;
+}
+
 // Cloud-in-cell (simplehyperoctree.h:1410-1469): trilinear over the 8 cells
 // of the located cell's level; restarts one level up when a neighbour is
 // coarser; empty when a neighbour is missing.  res.need_all = also accumulate
@@ -185,8 +223,10 @@ __device__ void cic_walk(const DevTree& T, double x, double y, double z, GatherA
     const Found f0 = find_cell(T, kMaxLevel, c32x, c32y, c32z);
     if (f0.cell < 0) return;
     int ilvl = f0.level, lvl = ilvl;
-    // coordinates of the current centre cell at level ilvl
+    // coordinates of the current centre cell at level ilvl (and, exact mode, its
+    // record: the vertex lookups read it)
     uint64_t ccx = c32x >> (kMaxLevel - ilvl), ccy = c32y >> (kMaxLevel - ilvl), ccz = c32z >> (kMaxLevel - ilvl);
+    int centre = f0.cell;
     // the child site holding the point: next bit below the centre's level
     int site = 0;
     if (ilvl < kMaxLevel) {
@@ -220,7 +260,8 @@ __device__ void cic_walk(const DevTree& T, double x, double y, double z, GatherA
                     (void)vert;
                 }
             }
-            const Found fi = find_cell(T, ilvl, kc[0], kc[1], kc[2]);
+            const uint64_t cc[3] = {ccx, ccy, ccz};
+            const Found fi = EXACT ? find_near(T, centre, ilvl, cc, kc) : find_cell(T, ilvl, kc[0], kc[1], kc[2]);
             if (fi.cell >= 0) {
                 lvl = min(lvl, fi.level);
                 res.template add<EXACT>(T, fi.cell, w);
@@ -235,6 +276,7 @@ __device__ void cic_walk(const DevTree& T, double x, double y, double z, GatherA
             const uint64_t px = c32x >> b, py = c32y >> b, pz = c32z >> b;   // coords at lvl+1
             site = (int)(px & 1ull) | ((int)(py & 1ull) << 1) | ((int)(pz & 1ull) << 2);
             ccx = px >> 1; ccy = py >> 1; ccz = pz >> 1;
+            if (EXACT) centre = ancestor_cell(T, centre, ilvl, lvl);
             res.reset();
             half = half_cell(lvl);
         }
@@ -279,9 +321,11 @@ __device__ void tsc_walk(const DevTree& T, double x, double y, double z, GatherA
     const Found f0 = find_cell(T, kMaxLevel, c32x, c32y, c32z);
     if (f0.cell < 0) return;
     int ilvl = f0.level, lvl = ilvl;
+    int centre = f0.cell;   // the record of the centre cell at level ilvl (exact mode)
     double half = half_cell(ilvl);
     const double pt[3] = {x, y, z};
     do {
+        if (EXACT && lvl < ilvl) centre = ancestor_cell(T, centre, ilvl, lvl);
         ilvl = lvl;
         const double tw = __dmul_rn(2.0, half);
         const uint64_t ccx = c32x >> (kMaxLevel - ilvl), ccy = c32y >> (kMaxLevel - ilvl), ccz = c32z >> (kMaxLevel - ilvl);
@@ -319,7 +363,8 @@ __device__ void tsc_walk(const DevTree& T, double x, double y, double z, GatherA
                                          tsc_w1f(abs(iz), fabsf(fd[2] - (float)iz));
                         w = (double)wf;
                     }
-                    const Found fi = find_cell(T, ilvl, kx, ky, kz);
+                    const uint64_t kk[3] = {kx, ky, kz}, cc[3] = {ccx, ccy, ccz};
+                    const Found fi = EXACT ? find_near(T, centre, ilvl, cc, kk) : find_cell(T, ilvl, kx, ky, kz);
                     if (fi.cell >= 0) {
                         lvl = min(lvl, fi.level);
                         if (lvl < ilvl) { res.reset(); stop = true; }
