@@ -168,10 +168,12 @@ struct PosAt {
 // rare path (a full walk, a restart at a coarser cell) needs them; the common
 // path works on the FP32 offset from the step's start cell.
 struct PosStage {
-    double bx, by, bz, c, kx, ky, kz;
-    __device__ __forceinline__ double px() const { return fma(c, kx, bx); }
-    __device__ __forceinline__ double py() const { return fma(c, ky, by); }
-    __device__ __forceinline__ double pz() const { return fma(c, kz, bz); }
+    double bx, by, bz, dlL;
+    float cfr, kx, ky, kz;   // converted to float64 on the rare paths only
+    __device__ __forceinline__ double c() const { return (double)cfr * dlL; }
+    __device__ __forceinline__ double px() const { return fma(c(), (double)kx, bx); }
+    __device__ __forceinline__ double py() const { return fma(c(), (double)ky, by); }
+    __device__ __forceinline__ double pz() const { return fma(c(), (double)kz, bz); }
 };
 
 // A located point: its deepest cell, that cell's level, integer coordinates
@@ -875,7 +877,7 @@ __device__ void propagate_fast(const DevTree& T, const DevCosmo& C, const PropPa
                 g = hom;
                 if (!born) {
                     const float cc = cfr * dlLf * cpu;
-                    const PosStage ps{b.x, b.y, b.z, (double)cfr * dlL, (double)pk1, (double)pk2, (double)pk3};
+                    const PosStage ps{b.x, b.y, b.z, dlL, cfr, pk1, pk2, pk3};
                     const Loc d = locate_rel(T, here, fmaf(cc, pk1, here.fd[0]), fmaf(cc, pk2, here.fd[1]),
                                              fmaf(cc, pk3, here.fd[2]), ps);
                     g = gather_at<ORDER>(T, d, ps, false, st, ST_RK_REC, false);

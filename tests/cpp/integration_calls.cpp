@@ -6,7 +6,12 @@
 // from a golden fixture; outputs are raw files it compares with the
 // reference's rows.
 //
-//   integration_calls <dir>     reads <dir>/*.in, writes <dir>/maps.out and <dir>/catalogue.out
+//   integration_calls <dir>            reads <dir>/*.in, writes <dir>/maps.out and <dir>/catalogue.out
+//   integration_calls <dir> velocity   the velocity-field map driver (hmaps.cpp:360-455): the
+//                                      particles of two shell files deposited (TSC), the maps traced
+//                                      with the observer velocity; writes velocity.out, rho.out,
+//                                      maps.out, and accuracy.out (mpf_propagate_accuracy on the
+//                                      pixels' rays)
 #include <array>
 #include <cstdint>
 #include <cstdio>
@@ -41,13 +46,99 @@ static void check(int rc, const char* what)
     if (rc < 0) throw std::runtime_error(std::string(what) + ": " + mpf_last_error());
 }
 
+// The velocity-field build's map driver, with the files of the velocity fixture.
+static void velocity_driver(const std::string& dir)
+{
+    struct Record48 {
+        unsigned char bytes[48];
+    };
+    const std::vector<Record48> octree = slurp<Record48>(dir + "/records.in");
+    const std::vector<double> table = slurp<double>(dir + "/cosmology.in");
+    const size_t nt = table.size() / 4;
+    // length, nsteps, nside, v0x, v0y, v0z, first-file particles
+    const std::vector<double> s = slurp<double>(dir + "/scalars.in");
+    std::vector<double> interpRefvec = slurp<double>(dir + "/surfaces.in");
+    std::vector<double> homogeneous = slurp<double>(dir + "/homogeneous.in");
+    std::vector<int64_t> pixel = slurp<int64_t>(dir + "/pixels.in");
+    const std::vector<float> pos_all = slurp<float>(dir + "/pos.in"), vel_all = slurp<float>(dir + "/vel.in");
+    const size_t split = (size_t)s[6];
+    // two shell files, as fill_particles_vectors hands them over
+    const std::vector<std::vector<float>> pos_part = {std::vector<float>(pos_all.begin(), pos_all.begin() + 3 * split),
+                                                      std::vector<float>(pos_all.begin() + 3 * split, pos_all.end())};
+    const std::vector<std::vector<float>> vel_part = {std::vector<float>(vel_all.begin(), vel_all.begin() + 3 * split),
+                                                      std::vector<float>(vel_all.begin() + 3 * split, vel_all.end())};
+
+    mpf_octree* dtree = nullptr;
+    check(mpf_octree_upload(octree.data(), (int64_t)octree.size(), &dtree), "mpf_octree_upload");
+    mpf_cosmology* dcosmo = nullptr;
+    check(mpf_cosmology_upload(table.data(), table.data() + nt, table.data() + 2 * nt, table.data() + 3 * nt,
+                               (int64_t)nt, &dcosmo),
+          "mpf_cosmology_upload");
+    const int scheme = 2;   // parameters.velocity_field == "tsc"
+    bool first = true;
+    for (size_t ifile = 0; ifile < pos_part.size(); ++ifile) {
+        check(mpf_velocity_deposit(dtree, scheme, (int64_t)(pos_part[ifile].size() / 3), pos_part[ifile].data(),
+                                   vel_part[ifile].data(), first ? MPF_VELOCITY_BEGIN : 0),
+              "mpf_velocity_deposit");
+        first = false;
+    }
+    check(mpf_velocity_deposit(dtree, scheme, 0, nullptr, nullptr, MPF_VELOCITY_FINISH), "mpf_velocity_deposit");
+    std::vector<float> v3(3 * octree.size()), rho(octree.size());
+    check(mpf_octree_get_velocity(dtree, v3.data(), rho.data()), "mpf_octree_get_velocity");
+    spill(dir + "/velocity.out", v3.data(), v3.size());
+    spill(dir + "/rho.out", rho.data(), rho.size());
+
+    mpf_params p = {};
+    p.length = s[0];
+    p.nsteps = (unsigned)s[1];
+    p.order = 2;
+    p.stop = MPF_STOP_REDSHIFT;
+    p.planes = interpRefvec.data();
+    p.nplanes = (int)interpRefvec.size();
+    p.jacobian = 1;
+    p.exact = 1;
+    p.vobs[0] = s[3];
+    p.vobs[1] = s[4];
+    p.vobs[2] = s[5];
+    const std::vector<int> comps = {MPF_MAP_LENSING, MPF_MAP_DZ, MPF_MAP_ISW, MPF_MAP_DENS, MPF_MAP_STEPS};
+    const int nmaps = 4 + 4;
+    const int64_t npix = (int64_t)pixel.size();
+    std::vector<float> rows((size_t)nmaps * interpRefvec.size() * npix);
+    check(mpf_hmaps_fill(dtree, dcosmo, &p, (int64_t)s[2], npix, pixel.data(), (int)comps.size(), comps.data(),
+                         homogeneous.data(), rows.data()),
+          "mpf_hmaps_fill");
+    spill(dir + "/maps.out", rows.data(), rows.size());
+
+    // the error the FP32-gather call carries against the float64 run, on the pixels' rays
+    std::vector<double> vec(3 * pixel.size()), launch(6 * pixel.size(), 0.0);
+    check(mpf_pix2vec_ring((int64_t)s[2], npix, pixel.data(), vec.data()), "mpf_pix2vec_ring");
+    for (int64_t i = 0; i < npix; ++i)
+        for (int d = 0; d < 3; ++d) launch[6 * i + 3 + d] = vec[3 * i + d];
+    mpf_accuracy acc;
+    check(mpf_propagate_accuracy(dtree, dcosmo, &p, npix, launch.data(), 64, &acc), "mpf_propagate_accuracy");
+    const double a[] = {(double)acc.rays, (double)acc.step_count_differs, acc.deflection_rel_max, acc.redshift_rel_max,
+                        acc.lensing_abs_max[0], acc.lensing_scale[0]};
+    spill(dir + "/accuracy.out", a, 6);
+    mpf_octree_destroy(dtree);
+    mpf_cosmology_destroy(dcosmo);
+}
+
 int main(int argc, char** argv)
 {
-    if (argc != 2) {
-        std::fprintf(stderr, "usage: %s <dir>\n", argv[0]);
+    if (argc != 2 && !(argc == 3 && std::string(argv[2]) == "velocity")) {
+        std::fprintf(stderr, "usage: %s <dir> [velocity]\n", argv[0]);
         return 2;
     }
     const std::string dir = argv[1];
+    if (argc == 3) {
+        try {
+            velocity_driver(dir);
+        } catch (const std::exception& e) {
+            std::fprintf(stderr, "integration_calls: %s\n", e.what());
+            return 1;
+        }
+        return 0;
+    }
     try {
         // the cone's records as Input::load read them (48-byte key + Gravity<float,3>)
         struct Record48 {
