@@ -420,7 +420,8 @@ __device__ __forceinline__ bool tsc_rec(const DevTree& T, const Loc& d, const P&
             }
 #pragma unroll
             for (int j = 0; j < 27; ++j) {
-                const float wt = wx[j / 9] * wy[(j / 3) % 3] * wz[j % 3];
+                // wy * wz is shared by the three x-slabs: 9 products, then one per cell
+                const float wt = wx[j / 9] * (wy[(j / 3) % 3] * wz[j % 3]);
                 const float4 g = __ldg(T.grad + e[j]);
                 gx = fmaf(g.x, wt, gx); gy = fmaf(g.y, wt, gy); gz = fmaf(g.z, wt, gz); gt = fmaf(g.w, wt, gt);
                 if (need_all) {
