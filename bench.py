@@ -606,6 +606,7 @@ def run_maps(args, synth, world, rank, local, dist):
                             np.arctan(np.sqrt(2.0) * np.tan(np.radians(MAPS_HALF_DEG))) * 1.02, (0.0, 0.0, 0.0),
                             4.0 / 512.0, spec.cosmo.h, spec.cosmo.omega_m, spec.lbox, synth.MPC, order=2)
     build_s = time.perf_counter() - t0
+    completion = pkg.cells_completion_info()
     built = np.frombuffer(built.tobytes(), dtype=synth.RECORD)
     t0 = time.perf_counter()
     tree = pkg.Octree.from_records(built)
@@ -656,7 +657,7 @@ def run_maps(args, synth, world, rank, local, dist):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": chunk * 8,
                     "d2h_bytes_per_step": chunk * 5 * 4},
             "build": {"synthetic_field_s": gen_s, "cells_build_s": build_s, "octree_upload_s": upload_s,
-                      "ascii_rows": int(rows.shape[0]), "cells": int(info["cells"])},
+                      "ascii_rows": int(rows.shape[0]), "cells": int(info["cells"]), "completion": completion},
             "map_error_vs_float64_kernel": map_err,
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -381,6 +381,14 @@ typedef struct {
  * sorted by key (what Input::save writes); count: the cells produced. */
 int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_params* cp, const mpf_cosmology* c, void* records,
                     int64_t capacity, int64_t* count);
+/* The completion of incomplete octs in the calling thread's last
+ * mpf_cells_build (Input::correct's sequential appends, src/input.h:1451-1482,
+ * run as waves of independent gathers): info[0] incomplete cells, info[1]
+ * children filled in waves, info[2] waves run, info[3] children filled in
+ * order on one thread after them (MPF_COMPLETION_WAVES in the environment
+ * caps the waves, default 32; 0 fills every child in order).  No counterpart
+ * in the reference. */
+int mpf_cells_completion_info(int64_t* info);
 /* The reference's ASCII cell reads (stream >> unsigned >> 9 floats): text of
  * length bytes -> rows[count x 10] (capacity rows at most). */
 int mpf_cells_parse(const char* text, int64_t length, float* rows, int64_t capacity, int64_t* count);

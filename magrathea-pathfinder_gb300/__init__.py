@@ -317,6 +317,16 @@ def cells_build(rows, cosmology: Cosmology, cone_vertex, cone_base, cone_angle, 
     return (rec, float(amin[0])) if acorrection else rec
 
 
+def cells_completion_info() -> dict:
+    """How the calling thread's last cells_build completed its incomplete
+    octs: the incomplete cells, the children filled in waves of independent
+    gathers, the waves run and the children filled in order after them."""
+    L = capi.load()
+    info = np.zeros(4, dtype=np.int64)
+    capi.check(L.mpf_cells_completion_info(capi.ptr(info)))
+    return {"incomplete": int(info[0]), "in_waves": int(info[1]), "waves": int(info[2]), "sequential": int(info[3])}
+
+
 def catalogue(octree: Octree, cosmology: Cosmology, sources, length: float, h: float, mpc: float = 3.08568e22,
               cat_accuracy: float = 1e-8, nsteps: int = 10, order: int = 2, vobs=(0.0, 0.0, 0.0), rotm1=None,
               exact: bool = False, max_iterations: int = 10, jacobian: str = "infinitesimal", plane: str = "normal",

@@ -32,7 +32,8 @@ EXPORTS = ("mpf_version", "mpf_last_error", "mpf_device_count", "mpf_octree_uplo
            "mpf_surrogate_get_params", "mpf_surrogate_set_params", "mpf_surrogate_loss_grad", "mpf_surrogate_eval",
            "mpf_surrogate_propagate", "mpf_rays_propagate", "mpf_cells_build", "mpf_cells_parse", "mpf_autotune_info",
            "mpf_octree_set_velocity", "mpf_octree_get_velocity", "mpf_velocity_deposit",
-           "mpf_velocity_deposit_device", "mpf_velocity_deposit_pairs", "mpf_propagate_accuracy")
+           "mpf_velocity_deposit_device", "mpf_velocity_deposit_pairs", "mpf_propagate_accuracy",
+           "mpf_cells_completion_info")
 
 MPF_VELOCITY_BEGIN = 1
 MPF_VELOCITY_FINISH = 2
@@ -171,6 +172,7 @@ def load(path: str = LIB_PATH):
     L.mpf_autotune_info.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), vp]
     L.mpf_cells_build.argtypes = [vp, i64, C.POINTER(CellsParams), vp, vp, i64, C.POINTER(i64)]
     L.mpf_cells_parse.argtypes = [C.c_char_p, i64, vp, i64, C.POINTER(i64)]
+    L.mpf_cells_completion_info.argtypes = [vp]
     L.mpf_rays_propagate.argtypes = [vp, vp, C.POINTER(Params), C.POINTER(BundleParams), i64, vp, vp, vp, vp]
     L.mpf_surrogate_create.argtypes = [C.POINTER(SurrogateDomain), C.POINTER(vp)]
     L.mpf_surrogate_destroy.argtypes = [vp]

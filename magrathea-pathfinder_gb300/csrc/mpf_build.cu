@@ -14,7 +14,8 @@
 //   Input::correct (input.h:1381-1516)      coarse densities from their
 //       neighbours, refined dphidt / rho from the parent level by level,
 //       incomplete octs completed from the gather at the children's centres
-//       (k_complete_serial: one thread, the reference's sequential appends)
+//       (k_complete_wave: children filled in waves, each reading only
+//       records final before it, so the sequential appends' values result)
 //       or, with correction = 0, the coarsening of the parents of refined
 //       cells with a non-normal density and of the incomplete octs;
 //       acorrection: the scale factors snapped to the next lower one of
@@ -25,8 +26,10 @@
 // Real = float in importascii); the unit is compiled with -fmad=false and
 // its host code without FMA contraction.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -433,6 +436,23 @@ __device__ __forceinline__ long long afind(const Rec48* r, long long n, u128 K)
     }
     return (first > 0 && containing128(k128(r[first - 1]), K)) ? first - 1 : -1;
 }
+// Which records a gather may read.  The completion fills the appended
+// children in waves: child j's fields are final once done[j] (the wave that
+// filled it) is below the current wave.  A gather that reaches a child not yet
+// final is blocked and retried in the next wave; the search paths themselves
+// read keys only, which are all written before the first wave.  Without a
+// table (done == nullptr) every record is final.
+struct Ready {
+    const int* done;
+    long long m;
+    int wave;
+    bool blocked;
+    __device__ __forceinline__ bool ok(long long i)
+    {
+        if (done && i >= m && done[i - m] >= wave) blocked = true;
+        return !blocked;
+    }
+};
 __device__ __forceinline__ void afields(const Rec48& r, float* f)
 {
     f[0] = r.rho; f[1] = r.phi; f[2] = r.dx; f[3] = r.dy; f[4] = r.dz; f[5] = r.a; f[6] = r.dt;
@@ -447,14 +467,15 @@ __device__ __forceinline__ void azero(float* a)
 }
 // SimpleHyperOctree::ngp (simplehyperoctree.h:1396-1401) over the array: the
 // record the containing search finds at the position's level-32 key
-__device__ void angp(const Rec48* r, long long n, double x, double y, double z, float* res)
+__device__ void angp(const Rec48* r, long long n, double x, double y, double z, float* res, Ready& rd)
 {
     const long long f0 = afind(r, n, compute128(32, x, y, z));
+    if (f0 >= 0 && !rd.ok(f0)) return;
     if (f0 >= 0) afields(r[f0], res);
     else azero(res);
 }
 // SimpleHyperOctree::cic (simplehyperoctree.h:1410-1469) over the array
-__device__ void acic(const Rec48* r, long long n, double x, double y, double z, float* res)
+__device__ void acic(const Rec48* r, long long n, double x, double y, double z, float* res, Ready& rd)
 {
     const double pt[3] = {x, y, z};
     u128 ekey = compute128(32, x, y, z);
@@ -482,6 +503,7 @@ __device__ void acic(const Rec48* r, long long n, double x, double y, double z, 
                 ekey = compute128(ilvl, vert[0], vert[1], vert[2]);
                 const long long fi = afind(r, n, ekey);
                 if (fi >= 0) {
+                    if (!rd.ok(fi)) return;
                     const unsigned fl = level128(k128(r[fi]));
                     if (fl < lvl) lvl = fl;
                     float f[7];
@@ -508,7 +530,7 @@ __device__ __forceinline__ double tsc_weight(int a, double d)
     return (double)a * 0.5 * (1.5 - d) * (1.5 - d) + (double)(1 - a) * (0.75 - d * d);
 }
 // SimpleHyperOctree::tsc (simplehyperoctree.h:1479-1541) over the array
-__device__ void atsc(const Rec48* r, long long n, double x, double y, double z, float* res)
+__device__ void atsc(const Rec48* r, long long n, double x, double y, double z, float* res, Ready& rd)
 {
     const double pt[3] = {x, y, z};
     u128 ekey = compute128(32, x, y, z);
@@ -518,7 +540,7 @@ __device__ void atsc(const Rec48* r, long long n, double x, double y, double z, 
     double half = 4.0 / 1.0 * (1.0 / (1.0 * (double)(((u128)1) << level128(idx)))) / 2.0;
     azero(res);
     if (x == 0.0 && y == 0.0 && z == 0.0) {
-        acic(r, n, 0., 0., 0., res);
+        acic(r, n, 0., 0., 0., res, rd);
         return;
     }
     for (int guard = 0; guard <= 33; ++guard) {
@@ -532,6 +554,7 @@ __device__ void atsc(const Rec48* r, long long n, double x, double y, double z, 
                         ekey = compute128(ilvl, pt[0] + ix * tw, pt[1] + iy * tw, pt[2] + iz * tw);
                         const long long fi = afind(r, n, ekey);
                         if (fi >= 0) {
+                            if (!rd.ok(fi)) return;
                             float f[7];
                             afields(r[fi], f);
                             double dist[3];
@@ -558,37 +581,72 @@ __device__ void atsc(const Rec48* r, long long n, double x, double y, double z, 
     }
 }
 
-// Input::correct's completion loop (input.h:1451-1482), in the reference's
-// order: for each incomplete cell (key order), its 8 children are gathered at
-// their centres on the array as it stands (the appended cells included) and
-// appended.  One thread: the appends make every gather depend on the previous
-// ones; the loop is short (the incomplete octs of the cone's boundary).
-__global__ void k_complete_serial(Rec48* r, long long m, const int* __restrict__ list, long long ninc, int order)
+// Input::correct's completion loop (input.h:1451-1482): for each incomplete
+// cell (key order) its 8 children are gathered at their centres on the array
+// as it stands -- the children appended before included -- and appended.
+// Child c (parent c / 8, site c % 8) is therefore gathered over the first
+// m + c records.  Which records a search visits depends on keys alone, and
+// every appended key is known before any gather, so the children are filled
+// in waves: in each wave every child whose gather reads only prefix records
+// or children of earlier waves is final; the others retry.  The lowest
+// unfilled child always completes (its reads are all earlier children), and
+// what a bounded number of waves leaves is filled in order on one thread.
+// Every child reads the same records with the same values as in the
+// sequential loop, so the result is the same bit for bit.
+
+// the appended children: key, level and the parent's fields (kept when the
+// gather is empty), all unfilled
+__global__ void k_complete_init(Rec48* r, long long m, const int* __restrict__ list, long long nch, int* done)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nch) return;
+    Rec48 o = r[list[c >> 3]];
+    const u128 ck = child128(k128(o), (unsigned)(c & 7));
+    o.hi = (unsigned long long)(ck >> 64);
+    o.lo = (unsigned long long)ck;
+    o.pad += 1;
+    r[m + c] = o;
+    done[c] = INT_MAX;
+}
+
+// child c's gather at its centre over the first m + c records; its fields
+// (not its key, which other gathers read meanwhile) written when non-empty
+__device__ bool complete_child(Rec48* r, long long m, long long c, int order, Ready& rd)
+{
+    const u128 ck = k128(r[m + c]);
+    // the child's centre as the reference computes it, in float
+    const float cx = (float)center128(ck, 0), cy = (float)center128(ck, 1), cz = (float)center128(ck, 2);
+    float f[7];
+    if (order == 0) angp(r, m + c, cx, cy, cz, f, rd);
+    else if (order == 1) acic(r, m + c, cx, cy, cz, f, rd);
+    else atsc(r, m + c, cx, cy, cz, f, rd);
+    if (rd.blocked) return false;
+    bool empty = true;
+    for (int k = 0; k < 7; ++k) empty = empty && (f[k] == 0.f);
+    if (!empty) {
+        Rec48& o = r[m + c];
+        o.rho = f[0]; o.phi = f[1]; o.dx = f[2]; o.dy = f[3]; o.dz = f[4]; o.a = f[5]; o.dt = f[6];
+    }
+    return true;
+}
+
+__global__ void k_complete_wave(Rec48* r, long long m, long long nch, int order, int* done, int wave, int* pending)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nch || done[c] != INT_MAX) return;
+    Ready rd{done, m, wave, false};
+    if (complete_child(r, m, c, order, rd)) done[c] = wave;
+    else atomicAdd(pending, 1);
+}
+
+// what the waves left, in the sequential order
+__global__ void k_complete_rest(Rec48* r, long long m, long long nch, int order, const int* __restrict__ done)
 {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    long long size = m;
-    for (long long q = 0; q < ninc; ++q) {
-        const Rec48 p = r[list[q]];
-        const u128 idx = k128(p);
-        for (unsigned site = 0; site < 8; ++site) {
-            const u128 ck = child128(idx, site);
-            // the child's centre as the reference computes it, in float
-            const float cx = (float)center128(ck, 0), cy = (float)center128(ck, 1), cz = (float)center128(ck, 2);
-            float f[7];
-            if (order == 0) angp(r, size, cx, cy, cz, f);
-            else if (order == 1) acic(r, size, cx, cy, cz, f);
-            else atsc(r, size, cx, cy, cz, f);
-            Rec48 o = p;
-            o.hi = (unsigned long long)(ck >> 64);
-            o.lo = (unsigned long long)ck;
-            o.pad = p.pad + 1;
-            bool empty = true;
-            for (int k = 0; k < 7; ++k) empty = empty && (f[k] == 0.f);
-            if (!empty) {
-                o.rho = f[0]; o.phi = f[1]; o.dx = f[2]; o.dy = f[3]; o.dz = f[4]; o.a = f[5]; o.dt = f[6];
-            }
-            r[size++] = o;
-        }
+    for (long long c = 0; c < nch; ++c) {
+        if (done[c] != INT_MAX) continue;
+        Ready rd{nullptr, m, 0, false};
+        complete_child(r, m, c, order, rd);
     }
 }
 
@@ -806,9 +864,42 @@ long long update(Arena& A, Rec48* r, long long n, Rec48* tmp, int* flag, cudaStr
 }
 }  // namespace
 
+// the completion of the calling thread's last mpf_cells_build: incomplete
+// cells, children filled in waves, waves run, children filled in order after
+// them
+namespace {
+struct Completion {
+    long long incomplete, in_waves;
+    int waves;
+    long long sequential;
+};
+thread_local Completion g_completion = {0, 0, 0, 0};
+
+// MPF_COMPLETION_WAVES: the most waves before the sequential fill (default
+// 32; 0 fills every child in order on one thread)
+int completion_waves()
+{
+    const char* v = std::getenv("MPF_COMPLETION_WAVES");
+    if (!v || !*v) return 32;
+    return std::min(std::max(std::atoi(v), 0), 4096);
+}
+}  // namespace
+
+extern "C" int mpf_cells_completion_info(int64_t* info)
+{
+    if (!info) return fail(MPF_BAD_INPUT, "mpf_cells_completion_info: bad argument");
+    info[0] = g_completion.incomplete;
+    info[1] = g_completion.in_waves;
+    info[2] = g_completion.waves;
+    info[3] = g_completion.sequential;
+    return MPF_OK;
+}
+
 extern "C" int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_params* cp, const mpf_cosmology* c, void* records,
                                int64_t capacity, int64_t* count)
 {
+    g_completion = {0, 0, 0, 0};
+    const int max_waves = completion_waves();
     if ((n > 0 && !rows) || n < 0 || !cp || !c || !count || (capacity > 0 && !records))
         return fail(MPF_BAD_INPUT, "mpf_cells_build: bad argument");
     if (cp->order < 0 || cp->order > 2) return fail(MPF_BAD_INPUT, "mpf_cells_build: order must be 0, 1 or 2");
@@ -909,9 +1000,27 @@ extern "C" int mpf_cells_build(const float* rows, int64_t n, const mpf_cells_par
             if (hflag[i + 1] > hflag[i]) hl.push_back((int)i);
         cudaMemcpy(list, hl.data(), hl.size() * sizeof(int), cudaMemcpyHostToDevice);
         cudaMemcpy(grown, r1, (size_t)m * sizeof(Rec48), cudaMemcpyDeviceToDevice);
-        k_complete_serial<<<1, 1, 0, s>>>(grown, m, list, ninc, cp->order);
+        const long long nch = 8 * ninc;
+        int* done = A.get<int>(nch);
+        int* pending = A.get<int>(std::max(max_waves, 1));
+        if (A.err != cudaSuccess) return fail(MPF_OUT_OF_MEMORY, "mpf_cells_build: device memory");
+        cudaMemsetAsync(pending, 0, (size_t)std::max(max_waves, 1) * sizeof(int), s);
+        k_complete_init<<<blk(nch, 128), 128, 0, s>>>(grown, m, list, nch, done);
+        long long left = nch;
+        int wave = 0;
+        while (left > 0 && wave < max_waves) {
+            ++wave;
+            k_complete_wave<<<blk(nch, 128), 128, 0, s>>>(grown, m, nch, cp->order, done, wave, pending + wave - 1);
+            int h_left = 0;
+            e = cudaMemcpyAsync(&h_left, pending + wave - 1, sizeof(int), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
+            left = h_left;
+        }
+        if (left > 0) k_complete_rest<<<1, 1, 0, s>>>(grown, m, nch, cp->order, done);
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));
+        g_completion = {ninc, nch - left, wave, left};
         // acorrection runs on the container with its appended children, before the final update
         if (cp->acorrection && (e = acorrect(A, grown, m + 8 * ninc, cp->amin, s)) != cudaSuccess)
             return fail(MPF_CUDA_ERROR, std::string("mpf_cells_build: ") + cudaGetErrorString(e));

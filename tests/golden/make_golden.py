@@ -337,6 +337,47 @@ def make_cells():
     print("cells -> %s (%d KB)" % (path, os.path.getsize(path) // 1024))
 
 
+# many incomplete octs: a quarter of the refined cells dropped at random and a
+# cone narrower than the field, so that the completion's appended children
+# read one another (Input::correct's sequential appends, input.h:1451-1482)
+CELLS_SPARSE_SPEC = dict(base_level=6, box_cells=16, lbox=2048.0, half_y=2.5, half_z=2.5, chi_max=1000.0, halos=12,
+                         max_level=9, mass_min=3e14, mass_max=2e15, refine_cells=2.5, seed=13)
+
+
+def make_cells_sparse():
+    spec = S.OctreeSpec(**CELLS_SPARSE_SPEC)
+    rec = S.make_octree(spec)
+    rows = S.cells_ramses(rec, spec)
+    rng = np.random.default_rng(37)
+    lev = rows[:, 0].astype(int)
+    fine = np.flatnonzero(lev > lev.min())
+    keep = np.ones(rows.shape[0], dtype=bool)
+    keep[rng.choice(fine, fine.shape[0] // 4, replace=False)] = False
+    rows = rows[keep]
+    rows = rows[rng.permutation(rows.shape[0])]
+    tmp = tempfile.mkdtemp(prefix="mpf_golden_")
+    cellfile = os.path.join(tmp, "cells_00000.dat")
+    S.write_cells(cellfile, rows)
+    celldir, pf, ef = S.write_param_files(tmp, spec.cosmo, spec.lbox)
+    cone7 = np.array([0.0, 0.0, 0.0, spec.chi_max / spec.lbox, 0.0, 0.0, np.radians(1.5)])
+    sphere4 = np.array([0.0, 0.0, 0.0, 1.0 / 32.0])
+    out = dict(cells_text=np.array(open(cellfile).read()), cone7=cone7, sphere4=sphere4, lboxmpch=spec.lbox,
+               h=spec.cosmo.h, omegam=spec.cosmo.omega_m, mpc=S.MPC)
+    for order in (1, 2):
+        R = Reference(order)
+        cos = R.cosmology(celldir, pf, ef)
+        if order == 2:
+            for k in ("t", "a", "dadt", "d2adt2", "length"):
+                out["cosmo_" + k] = cos[k]
+        recs, _ = R.build_cone(cellfile, cone7, sphere4, mpc=S.MPC, h=spec.cosmo.h, omegam=spec.cosmo.omega_m,
+                               lboxmpch=spec.lbox, correction=1, coarsecorrection=1)
+        out["ref_records_o%d" % order] = recs
+        print("cells_sparse o%d: %d rows in, %d cells out" % (order, rows.shape[0], recs.shape[0] // 48))
+    path = os.path.join(HERE, "cells_sparse.npz")
+    np.savez_compressed(path, **out)
+    print("cells_sparse -> %s (%d KB)" % (path, os.path.getsize(path) // 1024))
+
+
 def records_sha(rec) -> str:
     import hashlib
     return hashlib.sha256(np.ascontiguousarray(rec).tobytes()).hexdigest()
@@ -425,7 +466,7 @@ def make_velocity():
 
 
 if __name__ == "__main__":
-    names = sys.argv[1:] or list(CASES) + ["rays", "cells", "whole_rays", "velocity"]
+    names = sys.argv[1:] or list(CASES) + ["rays", "cells", "cells_sparse", "whole_rays", "velocity"]
     for name in names:
         if name == "velocity":
             make_velocity()
@@ -433,14 +474,14 @@ if __name__ == "__main__":
             make_whole_rays()
         elif name == "rays":
             make_rays()
-        elif name == "cells":
-            if names == ["cells"]:
-                make_cells()
+        elif name in ("cells", "cells_sparse"):
+            if names == [name]:
+                make_cells() if name == "cells" else make_cells_sparse()
             else:
                 # in a process of its own: the reference's SimpleHyperOctree::update reads one element past
                 # its container for the last cell (simplehyperoctree.h:1299), so that record, and through its
                 # scale factor acorrection's table, depends on the heap the process has used before
                 import subprocess
-                subprocess.run([sys.executable, os.path.abspath(__file__), "cells"], check=True)
+                subprocess.run([sys.executable, os.path.abspath(__file__), name], check=True)
         else:
             make(name, CASES[name])

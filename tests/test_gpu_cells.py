@@ -95,3 +95,39 @@ def test_empty_and_filtered_inputs(gpu_lib, pkg):
     with pytest.raises(RuntimeError):
         pkg.cells_build(rows, cos, *args, order=3)
     cos.close()
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("waves", ["default", "1", "0"])
+def test_completion_in_waves_bit_exact(gpu_lib, pkg, monkeypatch, order, waves):
+    """Many incomplete octs (tests/golden/cells_sparse.npz: a quarter of the
+    refined cells dropped, a cone narrower than the field), where the appended
+    children's gathers read children appended before them: filled in waves of
+    independent gathers (the default), after one wave with the rest in order,
+    or all in order on one thread (MPF_COMPLETION_WAVES=0), every record equals
+    the reference's build but the last one in key order (as above)."""
+    if waves != "default":
+        monkeypatch.setenv("MPF_COMPLETION_WAVES", waves)
+    g = load_golden("cells_sparse")
+    cos = pkg.Cosmology(g["cosmo_t"], g["cosmo_a"], g["cosmo_dadt"], g["cosmo_d2adt2"])
+    rows = pkg.cells_parse(str(g["cells_text"]))
+    c7, s4 = g["cone7"], g["sphere4"]
+    rec = pkg.cells_build(rows, cos, c7[:3], c7[3:6], c7[6], s4[:3], s4[3], float(g["h"]), float(g["omegam"]),
+                          float(g["lboxmpch"]), float(g["mpc"]), order=order)
+    info = pkg.cells_completion_info()
+    cos.close()
+    assert info["incomplete"] >= 100, info
+    assert info["in_waves"] + info["sequential"] == 8 * info["incomplete"], info
+    if waves == "0":
+        assert info["waves"] == 0 and info["in_waves"] == 0, info
+    elif waves == "1":
+        assert info["waves"] == 1, info
+    else:
+        assert info["sequential"] == 0 and info["waves"] >= 1, info
+    got, ref = _fields(rec), _fields(g["ref_records_o%d" % order])
+    assert got.shape == ref.shape
+    np.testing.assert_array_equal(got["hi"], ref["hi"])
+    np.testing.assert_array_equal(got["lo"], ref["lo"])
+    for name in ("dphidt", "a", "dphidx", "dphidy", "dphidz", "phi", "rho"):
+        np.testing.assert_array_equal(got[name][:-1].view(np.uint32), ref[name][:-1].view(np.uint32), err_msg=name)
+    print("completion", order, waves, info)
