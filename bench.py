@@ -711,6 +711,8 @@ def main():
                     help="skip the CPU baseline, the parity object and the accuracy statistic (profiling runs)")
     ap.add_argument("--zstop", type=float, default=2.0, help="stop redshift (profiling captures use a short path)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-catalogue", action="store_true",
+                    help="leave the catalogue root-finder's sub-object out of the default line")
     ap.add_argument("--no-surrogate", action="store_true",
                     help="skip the surrogate-vs-plain comparison of the default line")
     ap.add_argument("--mode", default="propagate", choices=["propagate", "catalogue", "surrogate", "maps", "velocity"],
@@ -893,6 +895,8 @@ def main():
                                      planes=planes, jacobian=True)
         acc["against"] = "the float64 kernel (the reference's operation order), mpf_propagate_accuracy"
         line["accuracy_of_call"] = acc
+    if rank == 0 and not args.no_catalogue:
+        line["catalogue"] = catalogue_entry(pkg, capi, lib, synth, tree, cosmo, length, spec.cosmo.h, dev)
     if rank == 0 and not args.no_surrogate:
         tree.close()      # the benchmark octree's 5 GB are not needed any more
         line["surrogate"] = surrogate_entry(pkg, synth, capi, lib)
@@ -900,6 +904,52 @@ def main():
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def catalogue_entry(pkg, capi, lib, synth, tree, cosmo, length, h, dev, nsrc=262144, calls=2):
+    """The catalogue root-finder (Catalogues::relCat's Newton iterations) on
+    the benchmark octree, in the default line: nsrc sources uniform in
+    comoving volume to z = 2 inside 9 x 9 deg, cat_accuracy 1e-8, TSC,
+    8 steps per cell; one warm-up call, then `calls` calls of
+    mpf_catalogue_newton_device on one stream (sources resident on the
+    device), timed with CUDA events.  `--mode catalogue` measures the same
+    workload with two host threads alternating their calls."""
+    import torch
+    kw = dict(cat_accuracy=1e-8, nsteps=8, order=2, vobs=(0.0, 0.0, 0.0), max_iterations=10)
+    pool = catalogue_sources(synth, nsrc * (calls + 1), 17)
+    d_src = torch.from_numpy(pool).to(dev)
+    d_rows = torch.zeros((nsrc, capi.MPF_CATALOGUE_FIELDS), dtype=torch.float64, device=dev)
+    p, keep = pkg.catalogue_params(length, h, **kw)
+    stream = torch.cuda.current_stream(dev)
+    stats = []
+
+    def call(k):
+        st = capi.CatalogueStats()
+        capi.check(lib.mpf_catalogue_newton_device(tree._h, cosmo._h, C.byref(p), nsrc,
+                                                   C.c_void_p(d_src.data_ptr() + k * nsrc * 8 * 8), 8,
+                                                   C.c_void_p(d_rows.data_ptr()), C.byref(st),
+                                                   C.c_void_p(stream.cuda_stream)))
+        return pkg.catalogue_stats(st)
+
+    call(0)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for k in range(1, calls + 1):
+        stats.append(call(k))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    sec = ev0.elapsed_time(ev1) / 1000.0
+    rows = d_rows.cpu().numpy()
+    del keep
+    return {"metric": CAT_METRIC, "value": nsrc * calls / sec, "unit": CAT_UNIT, "sources_per_call": nsrc,
+            "calls": calls, "ms_per_call": 1000.0 * sec / calls,
+            "photon_steps_per_s": sum(s["photon_steps"] for s in stats) / sec,
+            "rays_per_source": sum(s["rays"] for s in stats) / (nsrc * calls),
+            "converged_fraction": float(np.mean((rows[:, 2] != 42) & (rows[:, 5] != 42))),
+            "gpu_launches": sum(s["kernel_launches"] for s in stats),
+            "workload": "%d sources per call uniform in comoving volume to z=2 inside 9x9 deg on the benchmark "
+                        "octree, cat_accuracy 1e-8, TSC, 8 steps/cell; one stream, sources on the device" % nsrc}
 
 
 # 16 narrow cones over the 64^3 uniform field (octree level 8) to z = 2, the
