@@ -106,3 +106,43 @@ def test_cpp_call_sites_compile_against_the_header(pkg):
         subprocess.run([cxx, "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
                         os.path.join(ROOT, "tests", "cpp", "integration_calls.cpp"), "-o", os.path.join(d, "ic"),
                         "-L", libdir, "-lmpf_gb300"], check=True)
+
+
+def test_cpp_call_sites_compile_and_link(pkg, tmp_path):
+    """The reference-side C++ call sites (tests/cpp/integration_calls.cpp:
+    octree and cosmology upload, FillMap's map rows, relCat's catalogue rows,
+    the velocity-field deposit and maps) compile as C++17 against
+    include/mpf_gb300.h with every warning an error, and link against the
+    library; the GPU tests run the program."""
+    import importlib
+    import shutil
+    import subprocess
+    importlib.import_module(PKG + ".build").build()
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    libdir = os.path.join(ROOT, PKG)
+    exe = str(tmp_path / "integration_calls")
+    r = subprocess.run([cxx, "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "integration_calls.cpp"), "-o", exe, "-L", libdir,
+                        "-lmpf_gb300", "-Wl,-rpath," + libdir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert os.path.exists(exe)
+
+
+def test_header_compiles_as_c(tmp_path):
+    """The header is plain C: a C11 translation unit that includes it and
+    takes the address of every declared entry point compiles warning-free."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    names = declared_symbols()
+    src = tmp_path / "uses.c"
+    src.write_text('#include "mpf_gb300.h"\nvoid* table[] = {\n%s\n};\nint main(void) { return table[0] == 0; }\n'
+                   % ",\n".join("    (void*)&%s" % n for n in names))
+    r = subprocess.run([cc, "-std=c11", "-Wall", "-Wextra", "-Werror", "-pedantic", "-Wno-error=pedantic", "-c",
+                        "-I", os.path.join(ROOT, "include"), str(src), "-o", str(tmp_path / "uses.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
