@@ -50,6 +50,9 @@ def test_bad_input_is_a_status_not_a_crash(pkg):
     assert L.mpf_hmaps_fill(None, None, ctypes.byref(p), 4, 1, capi.ptr(pix), 1, capi.ptr(comps), capi.ptr(rows),
                             capi.ptr(maps)) == -1
     assert L.mpf_pix2vec_ring(0, 1, capi.ptr(pix), capi.ptr(rows)) == -1
+    assert L.mpf_cells_completion_info(None) == -1
+    info = np.full(4, 7, dtype=np.int64)
+    assert L.mpf_cells_completion_info(capi.ptr(info)) == 0 and not info.any()   # no build on this thread yet
     pix[0] = 12 * 4 * 4      # out of range for nside 4
     assert L.mpf_pix2vec_ring(4, 1, capi.ptr(pix), capi.ptr(rows)) == -1
     del keep
