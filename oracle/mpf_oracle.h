@@ -6,7 +6,9 @@
  * against (tests/, __graft_entry__.smoke) and the timed CPU baseline of
  * bench.py; the product never links or calls it.  It is itself pinned
  * bit-for-bit to the reference's own code (oracle/ref_harness.cpp) by
- * tests/test_oracle_vs_reference.py and the committed golden fixtures.
+ * the committed golden fixtures (tests/test_keys_and_oracle.py,
+ * tests/test_oracle_whole_rays.py, tests/test_oracle_velocity.py,
+ * tests/test_oracle_cells.py).
  *
  * Every floating-point expression keeps the reference's operation order and
  * must be compiled without FMA contraction (-ffp-contract=off), as the
@@ -133,6 +135,31 @@ int mpfo_bundle(const mpfo_tree* T, const mpfo_cosmo* C, int order, double lengt
  * not normal take the parent's v (hmaps.cpp:424-441). */
 int mpfo_velocity_deposit(const mpfo_tree* T, float* fields, float* v, int scheme, int64_t npart, const float* pos,
                           const float* pv, int flags);
+
+/* Create_octree::PreparationASCII's per-cone body (create_octree.h:544-580):
+ * Input::importascii of the cell rows (n x 10 floats: level x y z rho phi
+ * fx fy fz a) with the cone / microsphere filter, then correctOctree
+ * (sistemize, update, Input::correct, dphidt * da/dt).  records: capacity x
+ * 48-byte cone records sorted by key; returns the cell count (records beyond
+ * capacity are not written), -1 for bad arguments, -2 without memory.
+ * completion_waves: 0 fills the completed octs' children one after the
+ * other, as the reference's loop does; k > 0 fills them as the device does,
+ * in at most k waves of gathers that read only children of earlier waves,
+ * then the rest in order.  info (may be NULL): incomplete cells, children
+ * filled in waves, waves, children filled in order after them. */
+typedef struct {
+    double cone_vertex[3], cone_base[3], cone_angle;
+    double sphere_center[3], sphere_radius;
+    const double* rotm1;       /* 3x3 row-major, or NULL (full sky) */
+    double h, lboxmpch, mpc;
+    int coarseonly, ncoarse, correction, coarsecorrection, acorrection, order;
+    int completion_waves;
+} mpfo_cells_params;
+int64_t mpfo_cells_build(const float* rows, int64_t n, const mpfo_cells_params* P, const mpfo_cosmo* C, void* records,
+                         int64_t capacity, double* amin, int64_t* info);
+/* The reference's ASCII cell reads (stream >> unsigned >> 9 floats): rows
+ * (capacity x 10 at most); returns the row count, -1 on a malformed row. */
+int64_t mpfo_cells_parse(const char* text, int64_t length, float* rows, int64_t capacity);
 
 void mpfo_batch_locate(const mpfo_tree* T, int64_t n, const double* xyz, int64_t* out, int nthreads);
 void mpfo_batch_cic(const mpfo_tree* T, int64_t n, const double* xyz, float* out, int nthreads);

@@ -27,13 +27,20 @@ _i64 = C.c_int64
 _d = C.c_double
 
 
+SOURCES = ("mpf_oracle.c", "mpf_oracle_cells.c")
+HEADERS = ("mpf_oracle.h", "mpf_oracle_keys.h")
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle into oracle/_build/ (no FMA contraction)."""
-    src = os.path.join(HERE, "mpf_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in SOURCES]
+    newest = max(os.path.getmtime(os.path.join(HERE, f)) for f in SOURCES + HEADERS)
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < newest:
         os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+        tmp = LIB_PATH + ".%d.tmp" % os.getpid()
         subprocess.check_call(["gcc", "-O3", "-std=gnu11", "-ffp-contract=off", "-fPIC", "-shared",
-                               "-o", LIB_PATH, src, "-lm", "-lpthread"])
+                               "-o", tmp] + srcs + ["-lm", "-lpthread"])
+        os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
 
@@ -83,8 +90,69 @@ def lib():
         L.mpfo_velocity_deposit.argtypes = [_p, _p, _p, C.c_int, _i64, _p, _p, C.c_int]
         for f in ("mpfo_batch_locate", "mpfo_batch_cic", "mpfo_batch_tsc", "mpfo_batch_ngp"):
             getattr(L, f).argtypes = [_p, _i64, _p, _p, C.c_int]
+        L.mpfo_cells_parse.restype = _i64
+        L.mpfo_cells_parse.argtypes = [C.c_char_p, _i64, _p, _i64]
+        L.mpfo_cells_build.restype = _i64
+        L.mpfo_cells_build.argtypes = [_p, _i64, _p, _p, _p, _i64, _p, _p]
         _lib = L
     return _lib
+
+
+class _CellsParams(C.Structure):
+    _fields_ = [("cone_vertex", _d * 3), ("cone_base", _d * 3), ("cone_angle", _d), ("sphere_center", _d * 3),
+                ("sphere_radius", _d), ("rotm1", _p), ("h", _d), ("lboxmpch", _d), ("mpc", _d),
+                ("coarseonly", C.c_int), ("ncoarse", C.c_int), ("correction", C.c_int),
+                ("coarsecorrection", C.c_int), ("acorrection", C.c_int), ("order", C.c_int),
+                ("completion_waves", C.c_int)]
+
+
+def cells_parse(text: str) -> np.ndarray:
+    """The reference's ASCII cell reads: rows of 10 floats."""
+    L = lib()
+    raw = text.encode()
+    n = L.mpfo_cells_parse(raw, len(raw), None, 0)
+    if n < 0:
+        raise ValueError("malformed cell rows")
+    rows = np.zeros((n, 10), dtype=np.float32)
+    L.mpfo_cells_parse(raw, len(raw), _ptr(rows), n)
+    return rows
+
+
+def cells_build(rows, cosmo: dict, cone7, sphere4, h: float, lboxmpch: float, mpc: float, order: int = 2,
+                correction: bool = True, coarsecorrection: bool = True, acorrection: bool = False, rotm1=None,
+                coarseonly: bool = False, ncoarse: int = 0, completion_waves: int = 0):
+    """Create_octree's per-cone build (importascii + correctOctree) on the CPU:
+    (48-byte records as uint8, amin or None, completion info dict)."""
+    L = lib()
+    rows = np.ascontiguousarray(rows, dtype=np.float32).reshape(-1, 10)
+    p = _CellsParams()
+    for d in range(3):
+        p.cone_vertex[d], p.cone_base[d], p.sphere_center[d] = cone7[d], cone7[3 + d], sphere4[d]
+    p.cone_angle, p.sphere_radius = float(cone7[6]), float(sphere4[3])
+    rot = None if rotm1 is None else np.ascontiguousarray(rotm1, dtype=np.float64).reshape(9)
+    p.rotm1 = rot.ctypes.data if rot is not None else None
+    p.h, p.lboxmpch, p.mpc = float(h), float(lboxmpch), float(mpc)
+    p.coarseonly, p.ncoarse = int(bool(coarseonly)), int(ncoarse)
+    p.correction, p.coarsecorrection, p.acorrection = int(bool(correction)), int(bool(coarsecorrection)), int(bool(acorrection))
+    p.order, p.completion_waves = int(order), int(completion_waves)
+    a = np.ascontiguousarray(cosmo["a"], dtype=np.float64)
+    dadt = np.ascontiguousarray(cosmo["dadt"], dtype=np.float64)
+    t = np.ascontiguousarray(cosmo.get("t", cosmo["a"]), dtype=np.float64)
+    cs = _Cosmo(a.shape[0], t.ctypes.data, a.ctypes.data, dadt.ctypes.data)
+    amin = np.full(1, np.nan)
+    info = np.zeros(4, dtype=np.int64)
+    cap = 2 * rows.shape[0] + 64
+    out = np.zeros(cap * 48, dtype=np.uint8)
+    n = L.mpfo_cells_build(_ptr(rows), rows.shape[0], C.byref(p), C.byref(cs), _ptr(out), cap, _ptr(amin), _ptr(info))
+    if n > cap:
+        cap = n
+        out = np.zeros(cap * 48, dtype=np.uint8)
+        n = L.mpfo_cells_build(_ptr(rows), rows.shape[0], C.byref(p), C.byref(cs), _ptr(out), cap, _ptr(amin),
+                               _ptr(info))
+    if n < 0:
+        raise RuntimeError("mpfo_cells_build failed (%d)" % n)
+    return (out[:48 * n].copy(), None if np.isnan(amin[0]) else float(amin[0]),
+            {"incomplete": int(info[0]), "in_waves": int(info[1]), "waves": int(info[2]), "sequential": int(info[3])})
 
 
 def _ptr(a):

@@ -131,3 +131,35 @@ def test_completion_in_waves_bit_exact(gpu_lib, pkg, monkeypatch, order, waves):
     for name in ("dphidt", "a", "dphidx", "dphidy", "dphidz", "phi", "rho"):
         np.testing.assert_array_equal(got[name][:-1].view(np.uint32), ref[name][:-1].view(np.uint32), err_msg=name)
     print("completion", order, waves, info)
+
+
+def test_build_matches_oracle_on_a_larger_cone(gpu_lib, pkg, oracle_mod, synth):
+    """A larger input than the fixtures: 58k rows of a synthetic AMR field
+    (64^3 base refined to octree level 11 in 60 haloes), a tenth of its
+    refined cells dropped (about 2600 incomplete octs, their children filled
+    in waves), cut by a 4-degree cone.  The device build equals the C
+    oracle's (tests/test_oracle_cells.py pins the oracle to the reference's
+    own builds) record for record, the last one included: both keep the last
+    cell's own values."""
+    g = load_golden("cells")
+    spec = synth.OctreeSpec(base_level=8, box_cells=64, lbox=2048.0, half_y=5.0, half_z=5.0, chi_max=1800.0, halos=60,
+                            max_level=11, mass_min=3e14, mass_max=2e15, refine_cells=2.0, seed=21)
+    rows = synth.cells_ramses(synth.make_octree(spec), spec).astype(np.float32)
+    lev = rows[:, 0].astype(int)
+    fine = np.flatnonzero(lev > lev.min())
+    keep = np.ones(rows.shape[0], dtype=bool)
+    keep[np.random.default_rng(5).choice(fine, fine.shape[0] // 10, replace=False)] = False
+    rows = rows[keep]
+    cone7 = np.array([0.0, 0.0, 0.0, spec.chi_max / spec.lbox, 0.0, 0.0, np.radians(4.0)])
+    sphere4 = np.array([0.0, 0.0, 0.0, 1.0 / 32.0])
+    ref, _, ref_info = oracle_mod.cells_build(rows, {"t": g["cosmo_t"], "a": g["cosmo_a"], "dadt": g["cosmo_dadt"]},
+                                              cone7, sphere4, spec.cosmo.h, spec.lbox, float(g["mpc"]),
+                                              completion_waves=32)
+    cos = pkg.Cosmology(g["cosmo_t"], g["cosmo_a"], g["cosmo_dadt"], g["cosmo_d2adt2"])
+    rec = pkg.cells_build(rows, cos, cone7[:3], cone7[3:6], cone7[6], sphere4[:3], sphere4[3], spec.cosmo.h,
+                          spec.cosmo.omega_m, spec.lbox, float(g["mpc"]))
+    info = pkg.cells_completion_info()
+    cos.close()
+    assert ref_info["incomplete"] > 1000
+    assert info == ref_info
+    np.testing.assert_array_equal(rec, ref)
