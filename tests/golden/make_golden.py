@@ -373,6 +373,14 @@ def make_cells_sparse():
                                lboxmpch=spec.lbox, correction=1, coarsecorrection=1)
         out["ref_records_o%d" % order] = recs
         print("cells_sparse o%d: %d rows in, %d cells out" % (order, rows.shape[0], recs.shape[0] // 48))
+        if order == 2:
+            # a narrow cone's rotation of the cells (importascii's rotm1, input.h:1034-1039)
+            rot = rotation(0.004, -0.006, 0.009)
+            recs, _ = R.build_cone(cellfile, cone7, sphere4, rotm1=rot, mpc=S.MPC, h=spec.cosmo.h,
+                                   omegam=spec.cosmo.omega_m, lboxmpch=spec.lbox, correction=1, coarsecorrection=1)
+            out["rotm1"] = rot
+            out["ref_records_rot"] = recs
+            print("cells_sparse rotated: %d cells out" % (recs.shape[0] // 48))
     path = os.path.join(HERE, "cells_sparse.npz")
     np.savez_compressed(path, **out)
     print("cells_sparse -> %s (%d KB)" % (path, os.path.getsize(path) // 1024))

@@ -163,3 +163,22 @@ def test_build_matches_oracle_on_a_larger_cone(gpu_lib, pkg, oracle_mod, synth):
     assert ref_info["incomplete"] > 1000
     assert info == ref_info
     np.testing.assert_array_equal(rec, ref)
+
+
+def test_rotated_build_equals_reference(gpu_lib, pkg):
+    """A narrow cone's rotation of the cells (importascii's rotm1,
+    input.h:1034-1039): the device build equals the reference's rotated build
+    of tests/golden/cells_sparse.npz, the last record in key order aside."""
+    g = load_golden("cells_sparse")
+    cos = pkg.Cosmology(g["cosmo_t"], g["cosmo_a"], g["cosmo_dadt"], g["cosmo_d2adt2"])
+    rows = pkg.cells_parse(str(g["cells_text"]))
+    c7, s4 = g["cone7"], g["sphere4"]
+    rec = pkg.cells_build(rows, cos, c7[:3], c7[3:6], c7[6], s4[:3], s4[3], float(g["h"]), float(g["omegam"]),
+                          float(g["lboxmpch"]), float(g["mpc"]), rotm1=g["rotm1"])
+    cos.close()
+    got, ref = _fields(rec), _fields(g["ref_records_rot"])
+    assert got.shape == ref.shape
+    np.testing.assert_array_equal(got["hi"], ref["hi"])
+    np.testing.assert_array_equal(got["lo"], ref["lo"])
+    for name in ("dphidt", "a", "dphidx", "dphidy", "dphidz", "phi", "rho"):
+        np.testing.assert_array_equal(got[name][:-1].view(np.uint32), ref[name][:-1].view(np.uint32), err_msg=name)

@@ -112,3 +112,12 @@ def test_rotation_and_coarse_only(oracle_mod, cells):
     coarse = int(rows[:, 0].min())
     c, _, _ = _build(oracle_mod, cells, rows, coarseonly=True, ncoarse=coarse, coarsecorrection=False)
     assert 0 < c.shape[0] // 48 < a.shape[0] // 48
+
+
+def test_rotated_build_equals_reference(oracle_mod, sparse):
+    """A narrow cone's rotation of the cells' positions and forces
+    (importascii's rotm1, input.h:1034-1039) against the reference's rotated
+    build of the same file."""
+    rows = oracle_mod.cells_parse(str(sparse["cells_text"]))
+    rec, _, _ = _build(oracle_mod, sparse, rows, rotm1=sparse["rotm1"], completion_waves=32)
+    _assert_same(rec, sparse["ref_records_rot"])
