@@ -13,8 +13,10 @@ counts and final photon records (Integrator::integrate), FillMap maps, and
 catalogue rows (Catalogues::iterateNewtonMethod through relCat's per-source
 setup) for seeded sources at three accuracies, with and without a rotation,
 and FillMap maps with the bundle Jacobian (Lensing::dbetadtheta) for two
-screen / stop_bundle choices; and the reference's velocity-field build
-(-DVELOCITYFIELD): particle deposits and rays traced with the Doppler term.
+screen / stop_bundle choices; the reference's velocity-field build
+(-DVELOCITYFIELD): particle deposits and rays traced with the Doppler term;
+and its cone octree build from ASCII cells (create_octree): every correction
+option, a file with many incomplete octs, a rotated narrow cone.
 """
 from __future__ import annotations
 
